@@ -1,0 +1,309 @@
+"""Benchmark: wall-RPY M.F throughput (Gpairs/s) on one GB300.
+
+Workload (one "step"): one wall-corrected RPY product u = M_UF F in FP64 over
+the 256-shell suspension (256 bodies x 42 blobs = 10,752 blobs, a = 0.2436,
+x,y ~ U[0,60R], z ~ U[1.2R,5R], forces N(0,1), seed 1), with the inputs
+resident in HBM.  One step evaluates N^2 = 1.156e8 ordered pairs.  Inputs are
+far smaller than L2, so a 512 MB buffer is written between timed steps to
+flush L2.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's own CPU algorithm for the same product
+(the oracle's restatement of mobility/mobility.cpp:256-430: symmetric pair
+loop, OpenMP over all host cores, -O3 -ffast-math) on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOPS_PER_PAIR = {"uf": 200.0, "ut": 115.0, "wf": 115.0, "wt": 125.0}  # counted from the reference source
+METRIC = "wall-RPY M.F Gpairs/s"
+WORKLOAD = "wall-RPY M_UF.F, 256 shells x 42 blobs = 10,752 blobs (FP64)"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=8.0)
+    return p.parse_args()
+
+
+def workload():
+    from rigidmultiblobswall_gb300 import suspensions as S
+    s = S.shells_42_256()
+    r = s.r_vectors()
+    f = np.random.default_rng(1).standard_normal(r.shape)
+    return s, r, f
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    return ws, rank
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.lines = []
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(r, f, eta, a, seconds):
+    """The oracle's restatement of the reference C++ product on all host cores."""
+    from oracle import wall
+    threads = os.cpu_count() or 1
+    wall.uf_symmetric_fast(r[:512], f[:512], eta, a, threads=threads)  # warm-up (thread pool, pages)
+    n = len(r)
+    times = []
+    t_end = time.perf_counter() + seconds
+    while len(times) < 3 or time.perf_counter() < t_end:
+        t0 = time.perf_counter()
+        wall.uf_symmetric_fast(r, f, eta, a, threads=threads)
+        times.append(time.perf_counter() - t0)
+        if len(times) >= 200:
+            break
+    med = float(np.median(times))
+    return {"value": n * n / med / 1e9, "unit": "Gpairs/s", "cores": threads, "kind": "port",
+            "sample": "%d full M_UF.F products at N=%d (median %.3f s each); oracle/wall_oracle.c "
+                      "oracle_wall_uf_symmetric, restating mobility/mobility.cpp:256-430 with -O3 -ffast-math "
+                      "-fopenmp" % (len(times), n, med)}
+
+
+def run_reference(args):
+    ws, rank = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    s, r, f = workload()
+    from oracle import wall
+    threads = os.cpu_count() or 1
+    n = len(r)
+    for _ in range(max(args.warmup, 1)):
+        wall.uf_symmetric_fast(r, f, s.eta, s.a, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        wall.uf_symmetric_fast(r, f, s.eta, s.a, threads=threads)
+    dt = time.perf_counter() - t0
+    val = args.steps * n * n / dt / 1e9
+    line = {"metric": METRIC, "value": val, "unit": "Gpairs/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "n_blobs": n, "pairs_per_step": n * n, "l2": "CPU run"},
+            "cpu_baseline": {"value": val, "unit": "Gpairs/s", "cores": threads, "kind": "port",
+                             "sample": "%d full M_UF.F products at N=%d per timed run; oracle restatement of "
+                                       "mobility/mobility.cpp:256-430 (the reference C++ needs Eigen, absent)"
+                                       % (args.steps, n)},
+            "e2e": {"value": val, "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def time_product(kind, mode, rt, ft, out_fn, eta, a, steps, flush, stream):
+    import torch
+    from rigidmultiblobswall_gb300 import mobility as mb
+    from rigidmultiblobswall_gb300 import _native
+    n = rt.shape[0]
+    for _ in range(2):
+        mb.wall_product(kind, rt, ft, eta, a, mode=mode)
+    _native.trace_enable(True)
+    _native.trace_read(0, reset=True)
+    evs = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        mb.wall_product(kind, rt, ft, eta, a, mode=mode)
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / steps
+    pair_ms, launches = _native.trace_read(0, reset=True)
+    _native.trace_enable(False)
+    return {"ms": ms, "gpairs": n * n / (ms * 1e-3) / 1e9, "pair_kernel_ms": pair_ms / max(launches, 1)}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import torch.distributed as dist
+    from rigidmultiblobswall_gb300 import build as B
+    B.build()
+    from rigidmultiblobswall_gb300 import _native
+    from rigidmultiblobswall_gb300 import mobility as mb
+    ws, rank = dist_setup()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+
+    s, r, f = workload()
+    n = len(r)
+    eta, a = s.eta, s.a
+    rt = torch.tensor(r, device=dev)
+    ft = torch.tensor(f, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    peak64 = _native.fma_peak(True)
+    peak32 = _native.fma_peak(False)
+
+    # ---- warm-up
+    for _ in range(args.warmup):
+        mb.wall_product("uf", rt, ft, eta, a)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+
+    # ---- timed region: K steps of FP64 M.F with an L2 flush between steps
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    _native.trace_enable(True)
+    _native.trace_read(0, reset=True)
+    evs = []
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = mb.wall_product("uf", rt, ft, eta, a)
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    t_wall = time.perf_counter() - t_wall0
+    step_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
+    pair_ms_total, pair_launches = _native.trace_read(0, reset=True)
+    _native.trace_enable(False)
+    clk = clocks.stop()
+    t = torch.tensor([step_ms], dtype=torch.float64, device=dev)
+    if ws > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    step_ms = float(t.item())
+    ms_per_step = step_ms / args.steps
+    value = ws * args.steps * n * n / (step_ms * 1e-3) / 1e9
+
+    # ---- roofline of the dominant kernel (the pair kernel; bound by the FP64 pipe)
+    pair_ms = pair_ms_total / max(pair_launches, 1)
+    achieved = n * n * FLOPS_PER_PAIR["uf"] / (pair_ms * 1e-3) / 1e12
+    roofline = {"bound": "fp64-pipe", "achieved": achieved, "peak": peak64 / 1e12, "unit": "TFLOP/s",
+                "frac": achieved / (peak64 / 1e12), "traffic": None,
+                "peak_source": "measured by rmw_fma_peak (FP64 FMA chains on all SMs) in this run",
+                "pair_kernel_ms": pair_ms, "flops_per_pair": FLOPS_PER_PAIR["uf"]}
+
+    # ---- e2e through the public host-buffer API (copies inside the timed region)
+    rp = torch.empty(r.shape, dtype=torch.float64).pin_memory().numpy()
+    fp = torch.empty(f.shape, dtype=torch.float64).pin_memory().numpy()
+    rp[:] = r
+    fp[:] = f
+    mb.single_wall_mobility_trans_times_force_pycuda(rp, fp, eta, a)
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        u = mb.single_wall_mobility_trans_times_force_pycuda(rp, fp, eta, a)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e = {"value": n * n / float(np.mean(e2e_t)) / 1e9, "unit": "Gpairs/s",
+           "h2d_bytes_per_step": int(rp.nbytes + fp.nbytes), "d2h_bytes_per_step": int(u.nbytes)}
+
+    # ---- secondary: every product in both precisions (same workload)
+    products = {}
+    for kind in ("uf", "ut", "wf", "wt"):
+        for mode in ("fp64", "mixed"):
+            res = time_product(kind, mode, rt, ft, None, eta, a, max(3, args.steps // 4), flush, stream)
+            peak = peak64 if mode == "fp64" else peak32
+            res["pipe_frac"] = n * n * FLOPS_PER_PAIR[kind] / (res["pair_kernel_ms"] * 1e-3) / peak
+            products["%s_%s" % (kind, mode)] = {k: round(v, 6) for k, v in res.items()}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(r, f, eta, a, args.cpu_seconds)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD, "n_blobs": n, "pairs_per_step": n * n, "eta": eta, "a": a,
+                           "l2": "512 MB buffer written between timed steps (inputs 0.5 MB < L2)",
+                           "parallelism": "replicas" if ws > 1 else "single GPU"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+                "gpu_launches": 3 * args.steps, "wall_s_timed_region": t_wall,
+                "fp32_fma_peak_tflops": peak32 / 1e12, "fp64_fma_peak_tflops": peak64 / 1e12,
+                "products": products}
+        print(json.dumps(line))
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,101 @@
+"""Oracle (test infrastructure only): ctypes binding of the C restatement of the
+wall-RPY products (``oracle/wall_oracle.c``) and the reference's wall
+regularisation helpers.
+
+Only tests, ``__graft_entry__.smoke()`` and the CPU legs of ``bench.py`` use it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(_HERE, "_build")
+KINDS = {"uf": 0, "ut": 1, "wf": 2, "wt": 3}
+_libs = {}
+
+
+def build(quiet=True):
+    """Compile the oracle shared libraries (gcc, OpenMP)."""
+    cmd = ["make", "-C", _HERE, "-s"]
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL if quiet else None)
+
+
+def _lib(fast=False):
+    key = "fast" if fast else "parity"
+    if key in _libs:
+        return _libs[key]
+    path = os.path.join(_BUILD, "liboracle_fast.so" if fast else "liboracle.so")
+    if not os.path.exists(path):
+        build()
+    lib = ctypes.CDLL(path)
+    dp = ctypes.POINTER(ctypes.c_double)
+    lp = ctypes.POINTER(ctypes.c_long)
+    lib.oracle_wall_product_rows.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_long, lp, ctypes.c_long,
+                                             ctypes.c_double, ctypes.c_double, dp]
+    lib.oracle_wall_raw_rows.argtypes = lib.oracle_wall_product_rows.argtypes
+    lib.oracle_wall_uf_symmetric.argtypes = [dp, dp, dp, ctypes.c_long, ctypes.c_double, ctypes.c_double,
+                                             ctypes.c_int]
+    lib.oracle_max_threads.restype = ctypes.c_int
+    _libs[key] = lib
+    return lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def wall_product(kind, r_vectors, vector, eta, a, periodic_length=None, rows=None, regularize=True):
+    """B M(z_eff) B v for kind in {'uf','ut','wf','wt'} (flat (3N,) or (3*len(rows),))."""
+    lib = _lib()
+    r = np.ascontiguousarray(np.asarray(r_vectors, dtype=np.float64).reshape(-1, 3))
+    v = np.ascontiguousarray(np.asarray(vector, dtype=np.float64).reshape(-1))
+    n = r.shape[0]
+    assert v.size == 3 * n
+    L = np.zeros(3) if periodic_length is None else np.ascontiguousarray(periodic_length, dtype=np.float64)
+    if rows is not None:
+        rows = np.ascontiguousarray(rows, dtype=np.int64)
+        out = np.empty(3 * rows.size)
+        rp = rows.ctypes.data_as(ctypes.POINTER(ctypes.c_long))
+        nr = rows.size
+    else:
+        out = np.empty(3 * n)
+        rp = ctypes.POINTER(ctypes.c_long)()
+        nr = 0
+    fn = lib.oracle_wall_product_rows if regularize else lib.oracle_wall_raw_rows
+    fn(KINDS[kind], _dp(r), _dp(v), _dp(out), n, rp, nr, float(eta), float(a), _dp(L))
+    return out
+
+
+def shift_heights(r_vectors, blob_radius):
+    """mobility/mobility.py:52-64: z_eff = blob_radius where z <= blob_radius."""
+    r = np.array(r_vectors, dtype=np.float64, copy=True).reshape(-1, 3)
+    r[r[:, 2] <= blob_radius, 2] = blob_radius
+    return r
+
+
+def damping_vector(r_vectors, blob_radius):
+    """Diagonal of mobility/mobility.py:67-84's B (B_ii = z/a where z < a, else 1)."""
+    r = np.asarray(r_vectors, dtype=np.float64).reshape(-1, 3)
+    b = np.where(r[:, 2] < blob_radius, r[:, 2] / blob_radius, 1.0)
+    return np.repeat(b, 3), bool(np.any(r[:, 2] < blob_radius))
+
+
+def uf_symmetric_fast(r_vectors, force, eta, a, threads=0):
+    """Reference-C++-structured symmetric M_UF f (fast-math build), regularised
+    like mobility/mobility.py:187-219.  Used as the timed CPU baseline."""
+    lib = _lib(fast=True)
+    r = np.asarray(r_vectors, dtype=np.float64).reshape(-1, 3)
+    reff = np.ascontiguousarray(shift_heights(r, a))
+    b, overlap = damping_vector(r, a)
+    f = np.ascontiguousarray(np.asarray(force, dtype=np.float64).reshape(-1) * (b if overlap else 1.0))
+    out = np.empty(f.size)
+    lib.oracle_wall_uf_symmetric(_dp(reff), _dp(f), _dp(out), r.shape[0], float(eta), float(a), int(threads))
+    if overlap:
+        out *= b
+    return out
+
+
+def max_threads():
+    return _lib(fast=True).oracle_max_threads()

@@ -1,0 +1,107 @@
+"""ctypes binding of librmw_gb300.so (the C ABI declared in include/rmw_gb300.h).
+
+The library is required: importing a compute entry point without it raises.
+There is no CPU fallback anywhere in this package.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+RMW_OK = 0
+RMW_ERR_ARG = 1
+RMW_ERR_CUDA = 2
+RMW_ERR_NOT_CONVERGED = 3
+RMW_ERR_BREAKDOWN = 4
+RMW_ERR_NONFINITE = 5
+RMW_ERR_ALLOC = 6
+
+MODE_FP64 = 0
+MODE_MIXED = 1
+KINDS = {"uf": 0, "ut": 1, "wf": 2, "wt": 3}
+
+_lib = None
+
+
+class RMWError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("rmw_gb300 error %d: %s" % (code, msg))
+        self.code = code
+
+
+c_double_p = ctypes.POINTER(ctypes.c_double)
+_vp = ctypes.c_void_p
+_i64 = ctypes.c_int64
+_d = ctypes.c_double
+_i = ctypes.c_int
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "rmw_last_error": (ctypes.c_char_p, []),
+    "rmw_version": (_i, []),
+    "rmw_wall_product": (_i, [_i, _vp, _vp, _vp, _i64, _d, _d, _vp, _i, _vp]),
+    "rmw_wall_uf": (_i, [_vp, _vp, _vp, _i64, _d, _d, _vp, _i, _vp]),
+    "rmw_wall_ut": (_i, [_vp, _vp, _vp, _i64, _d, _d, _vp, _i, _vp]),
+    "rmw_wall_wf": (_i, [_vp, _vp, _vp, _i64, _d, _d, _vp, _i, _vp]),
+    "rmw_wall_wt": (_i, [_vp, _vp, _vp, _i64, _d, _d, _vp, _i, _vp]),
+    "rmw_wall_product_host": (_i, [_i, _vp, _vp, _vp, _i64, _d, _d, _vp, _i]),
+    "rmw_fma_peak": (_i, [_i, ctypes.POINTER(ctypes.c_double), _vp]),
+    "rmw_trace_enable": (_i, [_i]),
+    "rmw_trace_read": (_i, [_i, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64), _i]),
+}
+
+
+def fma_peak(fp64, stream=None):
+    """Measured FP64/FP32 FMA-pipe FLOP/s of the current device."""
+    out = ctypes.c_double(0.0)
+    call("rmw_fma_peak", 1 if fp64 else 0, ctypes.byref(out), stream)
+    return out.value
+
+
+def trace_enable(on=True):
+    call("rmw_trace_enable", 1 if on else 0)
+
+
+def trace_read(kind=0, reset=True):
+    """(total milliseconds, launches) of traced kernels of one class."""
+    ms = ctypes.c_double(0.0)
+    cnt = ctypes.c_int64(0)
+    call("rmw_trace_read", kind, ctypes.byref(ms), ctypes.byref(cnt), 1 if reset else 0)
+    return ms.value, cnt.value
+
+
+def lib_path():
+    return _build.lib_path()
+
+
+def load(build_if_missing=False):
+    """Load the shared library (raises if it is missing and not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = lib_path()
+    if not os.path.exists(p):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise RuntimeError("librmw_gb300.so is not built (%s); run rigidmultiblobswall_gb300.build.build()" % p)
+    lib = ctypes.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc):
+    if rc != RMW_OK:
+        msg = load().rmw_last_error()
+        raise RMWError(rc, msg.decode() if msg else "")
+    return rc
+
+
+def call(name, *args):
+    return check(getattr(load(), name)(*args))

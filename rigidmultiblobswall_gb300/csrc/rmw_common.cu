@@ -1,0 +1,139 @@
+// Error reporting and per-device scratch of the rmw_gb300 library.
+#include <cstdio>
+#include <mutex>
+#include <string>
+#include <vector>
+#include <map>
+#include <tuple>
+
+#include "rmw_common.cuh"
+
+namespace rmw {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+int fail(int code, const std::string &msg)
+{
+    set_error(msg);
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *where)
+{
+    std::string m = std::string(where) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    set_error(m);
+    return (e == cudaErrorMemoryAllocation) ? RMW_ERR_ALLOC : RMW_ERR_CUDA;
+}
+
+namespace {
+struct ScratchBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+std::mutex g_scratch_mu;
+// keyed by (device, stream, slot): calls on different streams never share scratch
+std::map<std::tuple<int, void *, int>, ScratchBuf> g_scratch;
+}  // namespace
+
+int scratch(ScratchSlot slot, size_t bytes, void **ptr, cudaStream_t st)
+{
+    int dev = 0;
+    RMW_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    ScratchBuf &b = g_scratch[std::make_tuple(dev, (void *)st, (int)slot)];
+    if (b.bytes < bytes) {
+        if (b.ptr) {
+            // cudaFree waits for all work on the device, so no kernel still uses the old buffer.
+            RMW_CUDA(cudaFree(b.ptr));
+            b.ptr = nullptr;
+            b.bytes = 0;
+        }
+        size_t want = bytes + bytes / 4 + 4096;  // headroom so that slowly growing sizes reallocate rarely
+        RMW_CUDA(cudaMalloc(&b.ptr, want));
+        b.bytes = want;
+    }
+    *ptr = b.ptr;
+    return RMW_OK;
+}
+
+// ---- tracing ---------------------------------------------------------------
+namespace {
+struct TraceRec {
+    int kind;
+    cudaEvent_t e0, e1;
+};
+std::mutex g_trace_mu;
+bool g_trace = false;
+std::vector<TraceRec> g_trace_recs;
+}  // namespace
+
+bool trace_on() { return g_trace; }
+
+int trace_begin(TraceKernel k, cudaStream_t st, void **token)
+{
+    *token = nullptr;
+    if (!g_trace) return RMW_OK;
+    TraceRec *r = new TraceRec{(int)k, nullptr, nullptr};
+    RMW_CUDA(cudaEventCreate(&r->e0));
+    RMW_CUDA(cudaEventCreate(&r->e1));
+    RMW_CUDA(cudaEventRecord(r->e0, st));
+    *token = r;
+    return RMW_OK;
+}
+
+int trace_end(void *token, cudaStream_t st)
+{
+    if (!token) return RMW_OK;
+    TraceRec *r = (TraceRec *)token;
+    RMW_CUDA(cudaEventRecord(r->e1, st));
+    std::lock_guard<std::mutex> lock(g_trace_mu);
+    g_trace_recs.push_back(*r);
+    delete r;
+    return RMW_OK;
+}
+
+}  // namespace rmw
+
+extern "C" {
+
+int rmw_trace_enable(int on)
+{
+    std::lock_guard<std::mutex> lock(rmw::g_trace_mu);
+    rmw::g_trace = (on != 0);
+    return RMW_OK;
+}
+
+int rmw_trace_read(int kind, double *total_ms_host, int64_t *launches_host, int reset)
+{
+    if (!total_ms_host || !launches_host) return rmw::fail(RMW_ERR_ARG, "null output pointer");
+    std::lock_guard<std::mutex> lock(rmw::g_trace_mu);
+    double tot = 0.0;
+    int64_t cnt = 0;
+    for (auto &r : rmw::g_trace_recs) {
+        if (r.kind != kind) continue;
+        RMW_CUDA(cudaEventSynchronize(r.e1));
+        float ms = 0.f;
+        RMW_CUDA(cudaEventElapsedTime(&ms, r.e0, r.e1));
+        tot += ms;
+        ++cnt;
+    }
+    *total_ms_host = tot;
+    *launches_host = cnt;
+    if (reset) {
+        for (auto &r : rmw::g_trace_recs) {
+            cudaEventDestroy(r.e0);
+            cudaEventDestroy(r.e1);
+        }
+        rmw::g_trace_recs.clear();
+    }
+    return RMW_OK;
+}
+
+
+const char *rmw_last_error(void) { return rmw::g_last_error.c_str(); }
+
+int rmw_version(void) { return 1; }
+
+}  // extern "C"

@@ -1,0 +1,66 @@
+// Shared host/device helpers of the rmw_gb300 library (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "../../include/rmw_gb300.h"
+
+namespace rmw {
+
+// ---- error reporting (thread-local message, status codes of rmw_gb300.h) --
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *where);
+
+#define RMW_CUDA(call)                                        \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return ::rmw::cuda_fail(e_, #call); \
+    } while (0)
+
+#define RMW_CHECK_LAUNCH(where)                               \
+    do {                                                      \
+        cudaError_t e_ = cudaGetLastError();                  \
+        if (e_ != cudaSuccess) return ::rmw::cuda_fail(e_, where); \
+    } while (0)
+
+// ---- per-device scratch --------------------------------------------------
+// A grow-only device buffer per (device, stream, slot).  Calls on the same
+// device, stream and slot share it (they are ordered by the stream); a call that
+// needs more frees the old buffer (cudaFree synchronises the device, so no
+// kernel still reads it) and allocates anew.
+enum ScratchSlot { SCRATCH_PAIR = 0, SCRATCH_SOLVER = 1, SCRATCH_SLOTS = 2 };
+int scratch(ScratchSlot slot, size_t bytes, void **ptr, cudaStream_t st);
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// ---- kernel tracing -------------------------------------------------------
+// When enabled (rmw_trace_enable), launchers bracket their dominant kernel with
+// CUDA events on the launching stream; rmw_trace_read sums the durations.
+enum TraceKernel { TRACE_PAIR = 0, TRACE_KRYLOV = 1, TRACE_PC = 2, TRACE_KINDS = 3 };
+bool trace_on();
+int trace_begin(TraceKernel k, cudaStream_t st, void **token);
+int trace_end(void *token, cudaStream_t st);
+
+constexpr double kPi = 3.14159265358979323846;
+
+// ---- compensated FP32 accumulation ----------------------------------------
+// TwoSum (Knuth): s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// (hi, lo) += x, keeping lo as the running compensation.
+__device__ __forceinline__ void comp_add(float &hi, float &lo, float x)
+{
+    float s, e;
+    two_sum(hi, x, s, e);
+    hi = s;
+    lo += e;
+}
+
+}  // namespace rmw

@@ -1,0 +1,507 @@
+// Single-wall Rotne-Prager-Yamakawa blob mobility products on GB300.
+//
+// u_i = b_i * nf * sum_j M_ij(z_eff) (b_j v_j)
+//
+// for the four blocks UF, UT, WF, WT of the wall mobility (Swan & Brady wall
+// correction on top of the RPY tensor), with the wall regularisation
+// z_eff = max(z, a), b = min(z/a, 1) of the reference (mobility/mobility.py:52-84).
+// The pair formulas are those of mobility/mobility_numba.py:124-287 (UF),
+// 548-686 (UT), 938-1073 (WF), 1189-1328 (WT), rewritten without divisions:
+//   h_hat * e_z      = h_j / R        (h_hat = h_j / (h_i + h_j), e_z = (h_i + h_j) / R)
+//   (1 - h_hat) e_z  = h_i / R
+// so each pair costs two reciprocal square roots and no division.
+//
+// Kernel structure (all-pairs, O(N^2)):
+//   1. pack     : one thread per blob; applies z_eff and b, writes a packed
+//                 source record (FP64: x,y,z,bv; mixed: pre-scaled double-float
+//                 positions hi/lo + FP32 bv) to scratch.
+//   2. pair     : grid (target tiles) x (source chunks).  Each CTA stages source
+//                 tiles of kTile records in shared memory; each thread owns one
+//                 target and loops over the tile (broadcast shared loads).
+//                 Mixed mode evaluates pairs in FP32 from double-float position
+//                 differences and folds each tile's FP32 partial sum into a
+//                 TwoSum-compensated accumulator.  Each CTA writes its FP64
+//                 partial sums to scratch partial[chunk][3n].
+//   3. finalize : one thread per blob; sums the chunks in fixed order (the
+//                 result is deterministic), adds the FP64 self term, applies
+//                 b_i and the 1/(8 pi eta a^p) factor.
+#include <algorithm>
+#include <cstdio>
+#include <mutex>
+#include <vector>
+
+#include "rmw_common.cuh"
+
+namespace rmw {
+
+constexpr int kThreads = 128;  // targets per CTA
+constexpr int kTile = 128;     // sources per shared-memory tile
+
+struct __align__(16) SrcD {
+    double x, y, z, pad0;
+    double vx, vy, vz, pad1;
+};
+struct __align__(16) SrcF {
+    float4 hi;  // x/a, y/a, z_eff/a (rounded to float), unused
+    float4 lo;  // residuals x/a - hi.x, ...
+    float4 v;   // b*v
+};
+
+struct Periodic {
+    double Lx, Ly, Lz;  // already divided by a for the mixed path
+};
+
+// ---------------------------------------------------------------------------
+// pack
+__global__ void pack_fp64_kernel(const double *__restrict__ r, const double *__restrict__ v, SrcD *__restrict__ src,
+                                 int n, double a)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double x = r[3 * i], y = r[3 * i + 1], z = r[3 * i + 2];
+    double b = (z < a) ? z / a : 1.0;
+    double ze = (z <= a) ? a : z;
+    SrcD s;
+    s.x = x; s.y = y; s.z = ze; s.pad0 = 0.0;
+    s.vx = b * v[3 * i]; s.vy = b * v[3 * i + 1]; s.vz = b * v[3 * i + 2]; s.pad1 = 0.0;
+    src[i] = s;
+}
+
+__global__ void pack_mixed_kernel(const double *__restrict__ r, const double *__restrict__ v, SrcF *__restrict__ src,
+                                  int n, double a)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double inva = 1.0 / a;
+    double x = r[3 * i], y = r[3 * i + 1], z = r[3 * i + 2];
+    double b = (z < a) ? z / a : 1.0;
+    double ze = (z <= a) ? a : z;
+    double xs = x * inva, ys = y * inva, zs = ze * inva;
+    float xh = (float)xs, yh = (float)ys, zh = (float)zs;
+    SrcF s;
+    s.hi = make_float4(xh, yh, zh, 0.f);
+    s.lo = make_float4((float)(xs - (double)xh), (float)(ys - (double)yh), (float)(zs - (double)zh), 0.f);
+    s.v = make_float4((float)(b * v[3 * i]), (float)(b * v[3 * i + 1]), (float)(b * v[3 * i + 2]), 0.f);
+    src[i] = s;
+}
+
+// ---------------------------------------------------------------------------
+// pair math.  (dx,dy,dz) = (r_i - r_j)/a; Rz = (z_i + z_j)/a; hi = z_i/a; hj = z_j/a.
+template <typename T> __device__ __forceinline__ T rsq(T x);
+template <> __device__ __forceinline__ double rsq<double>(double x) { return rsqrt(x); }
+template <> __device__ __forceinline__ float rsq<float>(float x) { return rsqrtf(x); }
+
+template <int KIND, typename T>
+__device__ __forceinline__ void pair_contrib(T dx, T dy, T dz, T Rz, T hi, T hj, T vx, T vy, T vz, T &ux, T &uy,
+                                             T &uz)
+{
+    const T r2 = dx * dx + dy * dy + dz * dz;
+    const T invr = rsq<T>(r2);
+    const T r = r2 * invr;
+    const T R2 = dx * dx + dy * dy + Rz * Rz;
+    const T invR = rsq<T>(R2);
+    const T invR2 = invR * invR;
+    const T ex = dx * invR, ey = dy * invR, ez = Rz * invR;
+    const T ez2 = ez * ez;
+    if (KIND == RMW_UF) {
+        const T invr2 = invr * invr;
+        T A, Bc;
+        if (r > T(2)) {
+            A = (T(1) + T(2.0 / 3.0) * invr2) * invr;
+            Bc = (T(1) - T(2) * invr2) * invr2 * invr;
+        } else {
+            A = T(4.0 / 3.0) * (T(1) - T(0.28125) * r);
+            Bc = T(0.125) * invr;
+        }
+        const T dv = dx * vx + dy * vy + dz * vz;
+        const T invR3 = invR2 * invR;
+        const T invR5 = invR3 * invR2;
+        const T hh = hi * hj * invR2;
+        const T f1 = -(T(3) * (T(1) + T(2) * hh) * invR + T(2) * (T(1) - T(3) * ez2) * invR3 -
+                       T(2) * (T(1) - T(5) * ez2) * invR5) * T(1.0 / 3.0);
+        const T f2 = -(T(3) * (T(1) - T(6) * hh) * invR - T(6) * (T(1) - T(5) * ez2) * invR3 +
+                       T(10) * (T(1) - T(7) * ez2) * invR5) * T(1.0 / 3.0);
+        const T f3 = T(2.0 / 3.0) * (T(3) * hj * invR2 - T(18) * hh * ez * invR +
+                                     ez * (T(10) * (T(2) - T(7) * ez2) * invR5 - T(6) * (T(1) - T(5) * ez2) * invR3));
+        const T f4 = T(2.0 / 3.0) * (T(3) * hj * invR2 - T(10) * ez * invR5);
+        const T f5 = T(-4.0 / 3.0) * (T(3) * (hj * hj + ez2) * invR3 + (T(2) - T(15) * ez2) * invR5);
+        const T ev = ex * vx + ey * vy + ez * vz;
+        const T ce = f2 * ev + f3 * vz;
+        const T Af = A + f1;
+        ux += Af * vx + Bc * dv * dx + ce * ex;
+        uy += Af * vy + Bc * dv * dy + ce * ey;
+        uz += Af * vz + Bc * dv * dz + ce * ez + f4 * ev + f5 * vz;
+    } else if (KIND == RMW_UT || KIND == RMW_WF) {
+        const T c = (r >= T(2)) ? invr * invr * invr : T(0.5) * (T(1) - T(0.375) * r);
+        // RPY part: c (v x d)
+        T ax = c * (vy * dz - vz * dy);
+        T ay = c * (vz * dx - vx * dz);
+        T az = c * (vx * dy - vy * dx);
+        const T invR3 = invR2 * invR;
+        const T invR4 = invR2 * invR2;
+        const T h = (KIND == RMW_UT) ? hi : hj;  // UT evaluates the wall term with i and j swapped
+        const T f1 = invR2;
+        const T f2 = T(2) * (T(6) * h * invR3 * ez + (T(1) - T(10) * ez2) * invR4);
+        const T f3 = T(-2) * (T(3) * h * invR3 - T(5) * ez * invR4);
+        const T f4 = T(-2) * (h * invR3 - ez * invR4);
+        const T g = f1 + f2 + f3 * ez;
+        const T p = f1 * ez + f4;
+        if (KIND == RMW_UT) {
+            const T q = ey * vx - ex * vy;
+            ax += f3 * ex * q + p * vy + f1 * ey * vz;
+            ay += f3 * ey * q - p * vx - f1 * ex * vz;
+            az -= g * q;
+        } else {
+            const T s2 = ex * vx + ey * vy;
+            ax += f3 * ey * s2 - p * vy + g * ey * vz;
+            ay += -f3 * ex * s2 + p * vx - g * ex * vz;
+            az += f1 * (ex * vy - ey * vx);
+        }
+        ux += ax;
+        uy += ay;
+        uz += az;
+    } else {  // RMW_WT
+        const T invr2 = invr * invr;
+        const T invr3 = invr2 * invr;
+        T A, Bc;
+        if (r >= T(2)) {
+            A = T(-0.5) * invr3;
+            Bc = T(1.5) * invr2 * invr3;
+        } else {
+            A = T(1) - T(0.84375) * r + T(0.078125) * r * r2;
+            Bc = T(0.28125) * invr - T(0.046875) * r;
+        }
+        const T dv = dx * vx + dy * vy + dz * vz;
+        const T invR3 = invR2 * invR;
+        const T f1 = T(0.5) * (T(1) - T(6) * ez2) * invR3;
+        const T f2 = T(-1.5) * invR3;
+        const T f3 = T(3) * invR3 * ez;
+        const T f4 = T(3) * invR3;
+        const T ev = ex * vx + ey * vy + ez * vz;
+        const T tv = f4 * (ex * vy - ey * vx);
+        const T Af = A + f1;
+        const T fe = f2 * ev;
+        ux += Af * vx + Bc * dv * dx + fe * ex - tv * ey;
+        uy += Af * vy + Bc * dv * dy + fe * ey + tv * ex;
+        uz += Af * vz + Bc * dv * dz + fe * ez + f3 * ev;
+    }
+}
+
+// Minimum-image projection of mobility/mobility_numba.py (int() truncates toward zero).
+template <typename T> __device__ __forceinline__ T project(T d, T L)
+{
+    T s = (T)((d > T(0)) - (d < T(0)));
+    return d - (T)(long long)(d / L + T(0.5) * s) * L;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 pair kernel
+template <int KIND, bool PER>
+__global__ void __launch_bounds__(kThreads) wall_pair_fp64_kernel(const SrcD *__restrict__ src, int n, int chunk,
+                                                                   double inva, Periodic P,
+                                                                   double *__restrict__ partial)
+{
+    __shared__ SrcD tile[kTile];
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    const int j0 = blockIdx.y * chunk;
+    const int j1 = min(n, j0 + chunk);
+    SrcD me;
+    if (i < n) me = src[i];
+    else { me.x = 0.0; me.y = 0.0; me.z = 1.0; }
+    const double hi = me.z * inva;
+    double ux = 0.0, uy = 0.0, uz = 0.0;
+    for (int t0 = j0; t0 < j1; t0 += kTile) {
+        const int cnt = min(kTile, j1 - t0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt; k += kThreads) tile[k] = src[t0 + k];
+        __syncthreads();
+#pragma unroll 2
+        for (int k = 0; k < cnt; ++k) {
+            const SrcD s = tile[k];
+            const int j = t0 + k;
+            const double hj = s.z * inva;
+            const double Rz = (me.z + s.z) * inva;
+            if (!PER) {
+                double cx = 0.0, cy = 0.0, cz = 0.0;
+                pair_contrib<KIND, double>((me.x - s.x) * inva, (me.y - s.y) * inva, (me.z - s.z) * inva, Rz, hi, hj,
+                                           s.vx, s.vy, s.vz, cx, cy, cz);
+                if (j != i) { ux += cx; uy += cy; uz += cz; }
+            } else {
+                double rx = me.x - s.x, ry = me.y - s.y, rz = me.z - s.z;
+                if (P.Lx > 0) rx = project(rx, P.Lx);
+                if (P.Ly > 0) ry = project(ry, P.Ly);
+                if (P.Lz > 0) rz = project(rz, P.Lz);
+                const int px = P.Lx > 0, py = P.Ly > 0, pz = P.Lz > 0;
+                for (int bx = -px; bx <= px; ++bx)
+                    for (int by = -py; by <= py; ++by)
+                        for (int bz = -pz; bz <= pz; ++bz) {
+                            double cx = 0.0, cy = 0.0, cz = 0.0;
+                            pair_contrib<KIND, double>((rx + bx * P.Lx) * inva, (ry + by * P.Ly) * inva,
+                                                       (rz + bz * P.Lz) * inva, Rz, hi, hj, s.vx, s.vy, s.vz, cx, cy,
+                                                       cz);
+                            const bool self = (j == i) && bx == 0 && by == 0 && bz == 0;
+                            if (!self) { ux += cx; uy += cy; uz += cz; }
+                        }
+            }
+        }
+    }
+    if (i < n) {
+        double *o = partial + (size_t)blockIdx.y * 3 * n + 3 * (size_t)i;
+        o[0] = ux; o[1] = uy; o[2] = uz;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed pair kernel: FP32 pair evaluation, double-float position differences,
+// per-tile FP32 sums folded into TwoSum-compensated accumulators.
+template <int KIND, bool PER>
+__global__ void __launch_bounds__(kThreads) wall_pair_mixed_kernel(const SrcF *__restrict__ src, int n, int chunk,
+                                                                    Periodic P, double *__restrict__ partial)
+{
+    __shared__ SrcF tile[kTile];
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    const int j0 = blockIdx.y * chunk;
+    const int j1 = min(n, j0 + chunk);
+    float4 mh = make_float4(0.f, 0.f, 1.f, 0.f), ml = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (i < n) { mh = src[i].hi; ml = src[i].lo; }
+    const float hi = mh.z + ml.z;
+    float sx = 0.f, sy = 0.f, sz = 0.f;   // compensated running sums (hi parts)
+    float ex_ = 0.f, ey_ = 0.f, ez_ = 0.f;  // compensation terms
+    const float Lx = (float)P.Lx, Ly = (float)P.Ly, Lz = (float)P.Lz;
+    for (int t0 = j0; t0 < j1; t0 += kTile) {
+        const int cnt = min(kTile, j1 - t0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt; k += kThreads) tile[k] = src[t0 + k];
+        __syncthreads();
+        float ux = 0.f, uy = 0.f, uz = 0.f;
+#pragma unroll 4
+        for (int k = 0; k < cnt; ++k) {
+            const float4 sh = tile[k].hi;
+            const float4 sl = tile[k].lo;
+            const float4 sv = tile[k].v;
+            const int j = t0 + k;
+            const float dx = (mh.x - sh.x) + (ml.x - sl.x);
+            const float dy = (mh.y - sh.y) + (ml.y - sl.y);
+            const float dz = (mh.z - sh.z) + (ml.z - sl.z);
+            const float hj = sh.z + sl.z;
+            const float Rz = hi + hj;
+            if (!PER) {
+                float cx = 0.f, cy = 0.f, cz = 0.f;
+                pair_contrib<KIND, float>(dx, dy, dz, Rz, hi, hj, sv.x, sv.y, sv.z, cx, cy, cz);
+                if (j != i) { ux += cx; uy += cy; uz += cz; }
+            } else {
+                float rx = dx, ry = dy, rz = dz;
+                if (Lx > 0.f) rx = project(rx, Lx);
+                if (Ly > 0.f) ry = project(ry, Ly);
+                if (Lz > 0.f) rz = project(rz, Lz);
+                const int px = Lx > 0.f, py = Ly > 0.f, pz = Lz > 0.f;
+                for (int bx = -px; bx <= px; ++bx)
+                    for (int by = -py; by <= py; ++by)
+                        for (int bz = -pz; bz <= pz; ++bz) {
+                            float cx = 0.f, cy = 0.f, cz = 0.f;
+                            pair_contrib<KIND, float>(rx + bx * Lx, ry + by * Ly, rz + bz * Lz, Rz, hi, hj, sv.x,
+                                                      sv.y, sv.z, cx, cy, cz);
+                            const bool self = (j == i) && bx == 0 && by == 0 && bz == 0;
+                            if (!self) { ux += cx; uy += cy; uz += cz; }
+                        }
+            }
+        }
+        comp_add(sx, ex_, ux);
+        comp_add(sy, ey_, uy);
+        comp_add(sz, ez_, uz);
+    }
+    if (i < n) {
+        double *o = partial + (size_t)blockIdx.y * 3 * n + 3 * (size_t)i;
+        o[0] = (double)sx + (double)ex_;
+        o[1] = (double)sy + (double)ey_;
+        o[2] = (double)sz + (double)ez_;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// finalize: fixed-order chunk sum + FP64 self term + b_i * norm factor.
+template <int KIND>
+__global__ void wall_finalize_kernel(const double *__restrict__ r, const double *__restrict__ v,
+                                     const double *__restrict__ partial, int nchunks, double *__restrict__ out,
+                                     int n, double a, double nf)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double ux = 0.0, uy = 0.0, uz = 0.0;
+    for (int s = 0; s < nchunks; ++s) {
+        const double *p = partial + (size_t)s * 3 * n + 3 * (size_t)i;
+        ux += p[0]; uy += p[1]; uz += p[2];
+    }
+    const double z = r[3 * i + 2];
+    const double b = (z < a) ? z / a : 1.0;
+    const double ze = (z <= a) ? a : z;
+    const double vx = b * v[3 * i], vy = b * v[3 * i + 1], vz = b * v[3 * i + 2];
+    const double iz = a / ze;  // 1/h
+    if (KIND == RMW_UF) {
+        const double iz3 = iz * iz * iz, iz5 = iz3 * iz * iz;
+        const double mxx = 4.0 / 3.0 - (9.0 * iz - 2.0 * iz3 + iz5) / 12.0;
+        const double mzz = 4.0 / 3.0 - (9.0 * iz - 4.0 * iz3 + iz5) / 6.0;
+        ux += mxx * vx; uy += mxx * vy; uz += mzz * vz;
+    } else if (KIND == RMW_UT) {
+        const double s = 0.125 * iz * iz * iz * iz;
+        ux += s * vy; uy -= s * vx;
+    } else if (KIND == RMW_WF) {
+        const double s = 0.125 * iz * iz * iz * iz;
+        ux -= s * vy; uy += s * vx;
+    } else {
+        const double iz3 = iz * iz * iz;
+        ux += (1.0 - 0.3125 * iz3) * vx; uy += (1.0 - 0.3125 * iz3) * vy; uz += (1.0 - 0.125 * iz3) * vz;
+    }
+    const double sc = b * nf;
+    out[3 * i] = ux * sc;
+    out[3 * i + 1] = uy * sc;
+    out[3 * i + 2] = uz * sc;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+static int choose_chunks(int n)
+{
+    const int tiles = (n + kThreads - 1) / kThreads;
+    const int want = 152 * 8;  // CTAs to fill the 152 SMs several times over
+    int s = (want + tiles - 1) / tiles;
+    s = std::min(s, std::max(1, n / 256));  // keep each chunk >= 256 sources
+    return std::max(1, std::min(s, 64));
+}
+
+size_t wall_scratch_bytes(int n, int mode, int nchunks)
+{
+    size_t rec = (mode == RMW_MODE_FP64) ? sizeof(SrcD) : sizeof(SrcF);
+    size_t packed = ((rec * (size_t)n + 255) / 256) * 256;
+    return packed + sizeof(double) * 3 * (size_t)n * (size_t)nchunks;
+}
+
+template <int KIND>
+static int launch_kind(const double *r, const double *v, double *out, int n, double eta, double a, const double *L,
+                       int mode, cudaStream_t st, void *scratch_ptr, int nchunks)
+{
+    const double inva = 1.0 / a;
+    const double nf = (KIND == RMW_UF)   ? 1.0 / (8.0 * kPi * eta * a)
+                      : (KIND == RMW_WT) ? 1.0 / (8.0 * kPi * eta * a * a * a)
+                                         : 1.0 / (8.0 * kPi * eta * a * a);
+    const bool per = L && (L[0] > 0 || L[1] > 0 || L[2] > 0);
+    Periodic P{L ? L[0] : 0.0, L ? L[1] : 0.0, L ? L[2] : 0.0};
+    size_t rec = (mode == RMW_MODE_FP64) ? sizeof(SrcD) : sizeof(SrcF);
+    size_t packed = ((rec * (size_t)n + 255) / 256) * 256;
+    char *base = (char *)scratch_ptr;
+    double *partial = (double *)(base + packed);
+    const int chunk = (n + nchunks - 1) / nchunks;
+    dim3 grid((n + kThreads - 1) / kThreads, nchunks);
+    const int pb = 256, pg = (n + pb - 1) / pb;
+    void *tok = nullptr;
+    if (mode == RMW_MODE_FP64) {
+        SrcD *src = (SrcD *)base;
+        pack_fp64_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
+        if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
+        if (per) wall_pair_fp64_kernel<KIND, true><<<grid, kThreads, 0, st>>>(src, n, chunk, inva, P, partial);
+        else wall_pair_fp64_kernel<KIND, false><<<grid, kThreads, 0, st>>>(src, n, chunk, inva, P, partial);
+    } else {
+        SrcF *src = (SrcF *)base;
+        pack_mixed_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
+        Periodic Ps{P.Lx * inva, P.Ly * inva, P.Lz * inva};
+        if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
+        if (per) wall_pair_mixed_kernel<KIND, true><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial);
+        else wall_pair_mixed_kernel<KIND, false><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial);
+    }
+    if (int rc = trace_end(tok, st)) return rc;
+    wall_finalize_kernel<KIND><<<pg, pb, 0, st>>>(r, v, partial, nchunks, out, n, a, nf);
+    RMW_CHECK_LAUNCH("wall product kernels");
+    return RMW_OK;
+}
+
+int validate_product_args(int kind, const void *r, const void *v, const void *out, int64_t n, double eta, double a,
+                          int mode)
+{
+    if (kind < RMW_UF || kind > RMW_WT) return fail(RMW_ERR_ARG, "unknown product kind");
+    if (mode != RMW_MODE_FP64 && mode != RMW_MODE_MIXED) return fail(RMW_ERR_ARG, "unknown precision mode");
+    if (n < 0 || n > (int64_t(1) << 28)) return fail(RMW_ERR_ARG, "number of blobs out of range [0, 2^28]");
+    if (n > 0 && (!r || !v || !out)) return fail(RMW_ERR_ARG, "null array pointer");
+    if (!(a > 0) || !(eta > 0)) return fail(RMW_ERR_ARG, "blob radius and viscosity must be positive");
+    return RMW_OK;
+}
+
+int wall_product_with_scratch(int kind, const double *r, const double *v, double *out, int n, double eta, double a,
+                              const double *L, int mode, cudaStream_t st, void *scratch_ptr, int nchunks)
+{
+    switch (kind) {
+    case RMW_UF: return launch_kind<RMW_UF>(r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks);
+    case RMW_UT: return launch_kind<RMW_UT>(r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks);
+    case RMW_WF: return launch_kind<RMW_WF>(r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks);
+    default: return launch_kind<RMW_WT>(r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks);
+    }
+}
+
+int wall_product(int kind, const double *r, const double *v, double *out, int64_t n, double eta, double a,
+                 const double *L, int mode, cudaStream_t st)
+{
+    int rc = validate_product_args(kind, r, v, out, n, eta, a, mode);
+    if (rc) return rc;
+    if (n == 0) return RMW_OK;
+    const int nchunks = choose_chunks((int)n);
+    void *ws = nullptr;
+    rc = scratch(SCRATCH_PAIR, wall_scratch_bytes((int)n, mode, nchunks), &ws, st);
+    if (rc) return rc;
+    return wall_product_with_scratch(kind, r, v, out, (int)n, eta, a, L, mode, st, ws, nchunks);
+}
+
+}  // namespace rmw
+
+// ---------------------------------------------------------------------------
+// C ABI
+extern "C" {
+
+int rmw_wall_product(int kind, const double *r, const double *v, double *out, int64_t n, double eta, double a,
+                     const double *L_host, int mode, void *stream)
+{
+    return rmw::wall_product(kind, r, v, out, n, eta, a, L_host, mode, rmw::as_stream(stream));
+}
+
+int rmw_wall_uf(const double *r, const double *v, double *out, int64_t n, double eta, double a, const double *L_host,
+                int mode, void *stream)
+{
+    return rmw_wall_product(RMW_UF, r, v, out, n, eta, a, L_host, mode, stream);
+}
+int rmw_wall_ut(const double *r, const double *v, double *out, int64_t n, double eta, double a, const double *L_host,
+                int mode, void *stream)
+{
+    return rmw_wall_product(RMW_UT, r, v, out, n, eta, a, L_host, mode, stream);
+}
+int rmw_wall_wf(const double *r, const double *v, double *out, int64_t n, double eta, double a, const double *L_host,
+                int mode, void *stream)
+{
+    return rmw_wall_product(RMW_WF, r, v, out, n, eta, a, L_host, mode, stream);
+}
+int rmw_wall_wt(const double *r, const double *v, double *out, int64_t n, double eta, double a, const double *L_host,
+                int mode, void *stream)
+{
+    return rmw_wall_product(RMW_WT, r, v, out, n, eta, a, L_host, mode, stream);
+}
+
+int rmw_wall_product_host(int kind, const double *r_host, const double *v_host, double *out_host, int64_t n,
+                          double eta, double a, const double *L_host, int mode)
+{
+    int rc = rmw::validate_product_args(kind, r_host, v_host, out_host, n, eta, a, mode);
+    if (rc) return rc;
+    if (n == 0) return RMW_OK;
+    // Device staging for r, v and out lives in the solver scratch slot.
+    const size_t bytes = sizeof(double) * 3 * (size_t)n;
+    void *stage = nullptr;
+    rc = rmw::scratch(rmw::SCRATCH_SOLVER, 3 * bytes, &stage, 0);
+    if (rc) return rc;
+    double *dr = (double *)stage, *dv = dr + 3 * n, *dout = dv + 3 * n;
+    cudaStream_t st = 0;
+    RMW_CUDA(cudaMemcpyAsync(dr, r_host, bytes, cudaMemcpyHostToDevice, st));
+    RMW_CUDA(cudaMemcpyAsync(dv, v_host, bytes, cudaMemcpyHostToDevice, st));
+    rc = rmw::wall_product(kind, dr, dv, dout, n, eta, a, L_host, mode, st);
+    if (rc) return rc;
+    RMW_CUDA(cudaMemcpyAsync(out_host, dout, bytes, cudaMemcpyDeviceToHost, st));
+    RMW_CUDA(cudaStreamSynchronize(st));
+    return RMW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,138 @@
+"""Drop-in for the wall-RPY part of the reference's ``mobility/mobility.py``.
+
+Same names, argument meaning and return convention as the reference:
+``f(r_vectors, vector, eta, a, *args, **kwargs)`` with ``r_vectors`` an (N,3)
+array, ``vector`` (N,3) or (3N,), the keyword ``periodic_length`` (3 lengths,
+> 0 means pseudo-periodic) and a NEW flat (3N,) float64 result.  Inputs are
+never modified.
+
+All products run on the GPU through librmw_gb300.so:
+
+* numpy inputs take the host path (copy in, launch, copy out; synchronous), the
+  contract of the reference's pycuda wrappers (mobility/mobility_pycuda.py:2235-2267);
+* CUDA torch tensors stay on the device; the call is asynchronous on the current
+  torch stream and returns a CUDA tensor.
+
+The extra keyword ``mode`` selects 'fp64' (default, every pair in FP64) or
+'mixed' (FP32 pair evaluation with double-float position differences and
+compensated accumulation; error <= 1e-6 relative to FP64).
+
+The ``_pycuda``, ``_numba`` and ``_cpp`` suffixes of the reference are all
+aliases of the GPU implementation, so ``set_mobility_vector_prod`` callers can
+swap the backend without changing their implementation string.
+"""
+import ctypes
+
+import numpy as np
+import scipy.sparse
+
+from . import _native
+
+_MODES = {"fp64": _native.MODE_FP64, "mixed": _native.MODE_MIXED}
+
+
+def _mode(kwargs):
+    m = kwargs.get("mode", "fp64")
+    if m not in _MODES:
+        raise ValueError("mode must be 'fp64' or 'mixed'")
+    return _MODES[m]
+
+
+def _periodic(kwargs):
+    L = kwargs.get("periodic_length", None)
+    if L is None:
+        return np.zeros(3)
+    L = np.ascontiguousarray(np.asarray(L, dtype=np.float64).reshape(-1))
+    if L.size != 3:
+        raise ValueError("periodic_length must have 3 entries")
+    return L
+
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+def wall_product(kind, r_vectors, vector, eta, a, **kwargs):
+    """B M(z_eff) B v for kind in {'uf','ut','wf','wt'} (see module docstring)."""
+    L = _periodic(kwargs)
+    mode = _mode(kwargs)
+    k = _native.KINDS[kind]
+    Lp = L.ctypes.data_as(ctypes.c_void_p)
+    if _is_torch(r_vectors) or _is_torch(vector):
+        import torch
+        r = torch.as_tensor(r_vectors, dtype=torch.float64)
+        v = torch.as_tensor(vector, dtype=torch.float64)
+        if not (r.is_cuda and v.is_cuda):
+            raise ValueError("torch inputs must both be CUDA tensors")
+        r = r.reshape(-1, 3).contiguous()
+        n = r.shape[0]
+        v = v.reshape(-1).contiguous()
+        if v.numel() != 3 * n:
+            raise ValueError("vector must have 3N entries")
+        out = torch.empty(3 * n, dtype=torch.float64, device=r.device)
+        stream = torch.cuda.current_stream(r.device).cuda_stream
+        with torch.cuda.device(r.device):
+            _native.call("rmw_wall_product", k, r.data_ptr(), v.data_ptr(), out.data_ptr(), n, float(eta),
+                         float(a), Lp, mode, stream)
+        return out
+    r = np.ascontiguousarray(np.asarray(r_vectors, dtype=np.float64).reshape(-1, 3))
+    n = r.shape[0]
+    v = np.ascontiguousarray(np.asarray(vector, dtype=np.float64).reshape(-1))
+    if v.size != 3 * n:
+        raise ValueError("vector must have 3N entries")
+    out = np.empty(3 * n)
+    _native.call("rmw_wall_product_host", k, r.ctypes.data_as(ctypes.c_void_p), v.ctypes.data_as(ctypes.c_void_p),
+                 out.ctypes.data_as(ctypes.c_void_p), n, float(eta), float(a), Lp, mode)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# wall regularisation helpers (mobility/mobility.py:52-84)
+def shift_heights(r_vectors, blob_radius, *args, **kwargs):
+    """z_effective = blob_radius wherever z <= blob_radius (copy; input untouched)."""
+    r_effective = np.copy(r_vectors)
+    r_effective[r_vectors[:, 2] <= blob_radius, 2] = blob_radius
+    return r_effective
+
+
+def damping_matrix_B(r_vectors, blob_radius, *args, **kwargs):
+    """(sparse diag B, overlap): B_ii = z_i/blob_radius where z_i < blob_radius, else 1."""
+    r = np.asarray(r_vectors).reshape(-1, 3)
+    b = np.where(r[:, 2] < blob_radius, r[:, 2] / blob_radius, 1.0)
+    B = np.repeat(b, 3)
+    overlap = bool(np.any(r[:, 2] < blob_radius))
+    return (scipy.sparse.dia_matrix((B, 0), shape=(B.size, B.size)), overlap)
+
+
+# ---------------------------------------------------------------------------
+# the four wall products under the reference's names
+def single_wall_mobility_trans_times_force_gb300(r_vectors, force, eta, a, *args, **kwargs):
+    """u = M_UF F  (reference: mobility/mobility.py:222-252, kernel mobility_pycuda.py:150-254)."""
+    return wall_product("uf", r_vectors, force, eta, a, **kwargs)
+
+
+def single_wall_mobility_trans_times_torque_gb300(r_vectors, torque, eta, a, *args, **kwargs):
+    """u = M_UT T  (reference: mobility/mobility.py:427-452, kernel mobility_pycuda.py:1516-1622)."""
+    return wall_product("ut", r_vectors, torque, eta, a, **kwargs)
+
+
+def single_wall_mobility_rot_times_force_gb300(r_vectors, force, eta, a, *args, **kwargs):
+    """w = M_WF F  (reference: mobility/mobility.py:300-325, kernel mobility_pycuda.py:926-1031)."""
+    return wall_product("wf", r_vectors, force, eta, a, **kwargs)
+
+
+def single_wall_mobility_rot_times_torque_gb300(r_vectors, torque, eta, a, *args, **kwargs):
+    """w = M_WT T  (reference: mobility/mobility.py:342-367, kernel mobility_pycuda.py:593-697)."""
+    return wall_product("wt", r_vectors, torque, eta, a, **kwargs)
+
+
+# Reference backend names: all served by the GPU implementation.
+single_wall_mobility_trans_times_force_pycuda = single_wall_mobility_trans_times_force_gb300
+single_wall_mobility_trans_times_force_numba = single_wall_mobility_trans_times_force_gb300
+single_wall_mobility_trans_times_force_cpp = single_wall_mobility_trans_times_force_gb300
+single_wall_mobility_trans_times_torque_pycuda = single_wall_mobility_trans_times_torque_gb300
+single_wall_mobility_trans_times_torque_numba = single_wall_mobility_trans_times_torque_gb300
+single_wall_mobility_rot_times_force_pycuda = single_wall_mobility_rot_times_force_gb300
+single_wall_mobility_rot_times_force_numba = single_wall_mobility_rot_times_force_gb300
+single_wall_mobility_rot_times_torque_pycuda = single_wall_mobility_rot_times_torque_gb300
+single_wall_mobility_rot_times_torque_numba = single_wall_mobility_rot_times_torque_gb300

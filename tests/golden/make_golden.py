@@ -1,0 +1,222 @@
+"""Generate the golden fixtures in this folder from the reference's own FP64 code.
+
+Runs only where a RigidMultiblobsWall checkout is available (default
+/root/reference, override with RMW_REFERENCE_ROOT); it imports the reference's
+Python read-only through ``oracle/ref_shims.py`` (numba source run as plain
+Python, no fastmath).  The fixtures it writes are small ``.npz`` files that the
+tests load on any machine:
+
+  products.npz   the four wall products (mobility/mobility.py *_numba wrappers)
+                 on seeded blobs: far from the wall, overlapping the wall
+                 (damping active), with blobs at exactly r = 2a, and periodic;
+                 plus the dense wall mobility (mobility/mobility.py:1018-1116)
+  rigid.npz      rigid-body pieces and a full mobility solve through
+                 multi_bodies.linear_operator_rigid, build_block_diagonal_preconditioner
+                 and general_application_utils.gmres (restart 60, tol 1e-8)
+  lanczos.npz    stochastic_forcing_lanczos on a dense wall mobility and on the
+                 block-preconditioned operator of build_block_diagonal_preconditioners_det_stoch
+  shells.npz     the reference's 12- and 42-blob shell vertex files (geometry inputs)
+  quaternion.npz Quaternion.from_rotation, products and rotation matrices
+
+Usage:  python tests/golden/make_golden.py
+"""
+import os
+import sys
+from functools import partial
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "..", "oracle"))
+import ref_shims  # noqa: E402
+
+REF = ref_shims.REFERENCE_ROOT
+
+
+def blobs(rng, n, a, zlo, zhi, box):
+    r = np.empty((n, 3))
+    r[:, 0:2] = rng.uniform(0, box, (n, 2))
+    r[:, 2] = rng.uniform(zlo, zhi, n)
+    return r
+
+
+def make_products():
+    mb = ref_shims.load("mobility.mobility")
+    fns = {
+        "uf": mb.single_wall_mobility_trans_times_force_numba,
+        "ut": mb.single_wall_mobility_trans_times_torque_numba,
+        "wf": mb.single_wall_mobility_rot_times_force_numba,
+        "wt": mb.single_wall_mobility_rot_times_torque_numba,
+    }
+    out = {}
+    cases = [
+        # name, seed, n, a, eta, zlo, zhi, box, L
+        ("far", 10, 80, 0.5, 1.0, 0.75, 5.0, 32.0, None),
+        ("damped", 11, 64, 0.4, 0.7, 0.05, 2.0, 6.0, None),
+        ("touching", 12, 48, 0.3, 1.3, 0.35, 1.5, 3.0, None),
+        ("periodic", 13, 40, 0.5, 1.0, 0.3, 3.0, 8.0, np.array([8.0, 9.0, 0.0])),
+        ("single", 14, 1, 0.5, 1.0, 0.3, 0.4, 1.0, None),
+    ]
+    for name, seed, n, a, eta, zlo, zhi, box, L in cases:
+        rng = np.random.default_rng(seed)
+        r = blobs(rng, n, a, zlo, zhi, box)
+        if name == "touching" and n >= 4:
+            # exact contact pairs at r = 2a (the RPY branch point)
+            r[1] = r[0] + np.array([2 * a, 0.0, 0.0])
+            r[3] = r[2] + np.array([0.0, 0.0, 2 * a])
+        v = rng.standard_normal((n, 3))
+        kw = {} if L is None else {"periodic_length": L}
+        out[name + "_r"] = r
+        out[name + "_v"] = v
+        out[name + "_params"] = np.array([a, eta])
+        out[name + "_L"] = np.zeros(3) if L is None else L
+        for k, fn in fns.items():
+            out[name + "_" + k] = fn(r, v, eta, a, **kw)
+        if L is None and n <= 64:
+            out[name + "_dense"] = mb.single_wall_fluid_mobility(r, eta, a)
+    np.savez_compressed(os.path.join(HERE, "products.npz"), **out)
+
+
+def read_vertex(rel):
+    rv = ref_shims.load("read_input.read_vertex_file")
+    return rv.read_vertex_file(os.path.join(REF, rel))
+
+
+def make_shells():
+    s42 = read_vertex("multi_bodies/Structures/shell_N_42_Rg_0_8913_Rh_1.vertex")
+    s12 = read_vertex("multi_bodies/Structures/shell_N_12_Rg_1.vertex")
+    np.savez_compressed(os.path.join(HERE, "shells.npz"), shell42=s42, shell12=s12)
+    return s42, s12
+
+
+def random_quaternions(rng, n):
+    q = rng.standard_normal((n, 4))
+    return q / np.linalg.norm(q, axis=1)[:, None]
+
+
+def make_quaternion():
+    Q = ref_shims.load("quaternion_integrator.quaternion").Quaternion
+    rng = np.random.default_rng(20)
+    q = random_quaternions(rng, 8)
+    phi = rng.standard_normal((8, 3)) * 0.3
+    phi[0] = 0.0
+    rot = np.array([Q(x).rotation_matrix() for x in q])
+    fr = np.array([Q.from_rotation(p).entries for p in phi])
+    prod = np.array([(Q.from_rotation(p) * Q(x)).entries for p, x in zip(phi, q)])
+    np.savez_compressed(os.path.join(HERE, "quaternion.npz"), q=q, phi=phi, rot=rot,
+                        from_rotation=fr, product=prod)
+
+
+def place_bodies(rng, nb, R, a, box, zlo, zhi):
+    locs = []
+    for _ in range(100000):
+        if len(locs) == nb:
+            break
+        c = np.array([rng.uniform(0, box), rng.uniform(0, box), rng.uniform(zlo, zhi)])
+        if all(np.linalg.norm(c - o) > 2 * R + 2 * a for o in locs):
+            locs.append(c)
+    assert len(locs) == nb, "body placement failed"
+    return np.array(locs)
+
+
+def make_rigid(s42, s12):
+    Q = ref_shims.load("quaternion_integrator.quaternion").Quaternion
+    body_mod = ref_shims.load("body.body")
+    mb = ref_shims.load("mobility.mobility")
+    utils = ref_shims.load("general_application_utils")
+    mbs = ref_shims.load_script("multi_bodies/multi_bodies.py", "ref_multi_bodies")
+    from scipy.spatial.distance import pdist
+    out = {}
+    for name, ref_cfg, nb, seed, zlo_f, box_f in (("s42", s42, 6, 30, 1.2, 8.0), ("s12", s12, 8, 31, 1.05, 16.0)):
+        R = np.linalg.norm(ref_cfg[0])
+        a = 0.5 * pdist(ref_cfg).min()
+        eta = 1.0
+        rng = np.random.default_rng(seed)
+        locs = place_bodies(rng, nb, R, a, box_f * R, zlo_f * R, 3 * R)
+        quats = random_quaternions(rng, nb)
+        bodies = []
+        for k in range(nb):
+            b = body_mod.Body(locs[k], Q(quats[k]), ref_cfg, a)
+            b.mobility_blobs = mb.single_wall_fluid_mobility
+            bodies.append(b)
+        Nblobs = sum(b.Nblobs for b in bodies)
+        r = mbs.get_blobs_r_vectors(bodies, Nblobs)
+        mbs.mobility_vector_prod = mb.single_wall_fluid_mobility_product
+        K_bodies = mbs.calc_K_matrix_bodies(bodies, Nblobs)
+        size = 3 * Nblobs + 6 * nb
+        x = rng.standard_normal(size)
+        Ax = mbs.linear_operator_rigid(x, bodies, [], r, eta, a, K_bodies=K_bodies, periodic_length=np.zeros(3))
+        mbs.build_block_diagonal_preconditioner.mobility_bodies = []
+        mbs.build_block_diagonal_preconditioner.initialized = []
+        PC = mbs.build_block_diagonal_preconditioner(bodies, [], r, Nblobs, eta, a, periodic_length=np.zeros(3),
+                                                     update_PC=1, step=0)
+        Px = PC(x)
+        # Mobility problem: force (0,0,-1) per body, zero torque, zero slip (cfg-2 style)
+        FT = np.zeros((nb, 6))
+        FT[:, 2] = -1.0
+        FT[:, 3:6] = rng.standard_normal((nb, 3)) * 0.1
+        RHS = np.concatenate([np.zeros(3 * Nblobs), -FT.flatten()])
+        RHS_norm = np.linalg.norm(RHS)
+        import scipy.sparse.linalg as spla
+        A = spla.LinearOperator((size, size), matvec=partial(mbs.linear_operator_rigid, bodies=bodies, constraints=[],
+                                                             r_vectors=r, eta=eta, a=a, K_bodies=K_bodies,
+                                                             periodic_length=np.zeros(3)), dtype="float64")
+        P = spla.LinearOperator((size, size), matvec=PC, dtype="float64")
+        it = [0]
+
+        def cb(rk):
+            it[0] += 1
+        sol, info = utils.gmres(A, RHS / RHS_norm, tol=1e-8, M=P, maxiter=1000, restart=60, callback=cb)
+        sol = sol * RHS_norm
+        true_res = np.linalg.norm(RHS - A.matvec(sol)) / RHS_norm
+        # stochastic det/stoch preconditioners and a Lanczos draw through them
+        sf = ref_shims.load("stochastic_forcing.stochastic_forcing")
+        mbs.build_block_diagonal_preconditioners_det_stoch.mobility_bodies = []
+        mbs.build_block_diagonal_preconditioners_det_stoch.initialized = []
+        PC2, mob_pc, P_inv = mbs.build_block_diagonal_preconditioners_det_stoch(
+            bodies, r, Nblobs, eta, a, periodic_length=np.zeros(3), update_PC=1, step=0)
+        w = rng.standard_normal(3 * Nblobs)
+        mob_pc_w = mob_pc(w.copy())
+        P_inv_w = P_inv(w.copy())
+        z = rng.standard_normal(3 * Nblobs)
+        noise, lit = sf.stochastic_forcing_lanczos(factor=np.sqrt(2.0 * 1.0 / 1e-3), tolerance=1e-3,
+                                                   dim=3 * Nblobs, mobility_mult=mob_pc, L_mult=P_inv, z=z)
+        p = name + "_"
+        out.update({p + "ref_cfg": ref_cfg, p + "locs": locs, p + "quats": quats, p + "params": np.array([a, eta]),
+                    p + "r": r, p + "K": np.array(K_bodies), p + "x": x, p + "Ax": Ax, p + "Px": Px,
+                    p + "FT": FT, p + "sol": sol, p + "info": np.array([info, it[0]]), p + "true_res": np.array([true_res]),
+                    p + "w": w, p + "mob_pc_w": mob_pc_w, p + "P_inv_w": P_inv_w, p + "z": z,
+                    p + "noise": noise, p + "lanczos_iters": np.array([lit])})
+        print(name, "bodies", nb, "blobs", Nblobs, "gmres info", info, "iters", it[0], "true res", true_res,
+              "lanczos iters", lit)
+    np.savez_compressed(os.path.join(HERE, "rigid.npz"), **out)
+
+
+def make_lanczos():
+    mb = ref_shims.load("mobility.mobility")
+    sf = ref_shims.load("stochastic_forcing.stochastic_forcing")
+    rng = np.random.default_rng(40)
+    out = {}
+    for name, n, tol in (("small", 24, 1e-6), ("tight", 40, 1e-10), ("loose", 40, 1e-3)):
+        a = 0.5
+        r = blobs(rng, n, a, 0.6, 4.0, 8.0)
+        M = mb.single_wall_fluid_mobility(r, 1.0, a)
+        z = rng.standard_normal(3 * n)
+        noise, it = sf.stochastic_forcing_lanczos(factor=1.7, tolerance=tol, mobility=M, z=z)
+        out[name + "_r"] = r
+        out[name + "_z"] = z
+        out[name + "_M"] = M
+        out[name + "_tol"] = np.array([tol, 1.7])
+        out[name + "_noise"] = noise
+        out[name + "_iters"] = np.array([it])
+        out[name + "_exact"] = 1.7 * np.real(__import__("scipy").linalg.sqrtm(M)) @ z
+    np.savez_compressed(os.path.join(HERE, "lanczos.npz"), **out)
+
+
+if __name__ == "__main__":
+    make_products()
+    s42, s12 = make_shells()
+    make_quaternion()
+    make_rigid(s42, s12)
+    make_lanczos()
+    print("golden fixtures written to", HERE)

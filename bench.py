@@ -38,6 +38,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true", help="skip the per-product secondary timings")
     p.add_argument("--cpu-seconds", type=float, default=8.0)
     return p.parse_args()
 
@@ -278,7 +279,7 @@ def main():
 
     # ---- secondary: every product in both precisions (same workload)
     products = {}
-    for kind in ("uf", "ut", "wf", "wt"):
+    for kind in (() if args.no_extras else ("uf", "ut", "wf", "wt")):
         for mode in ("fp64", "mixed"):
             res = time_product(kind, mode, rt, ft, None, eta, a, max(3, args.steps // 4), flush, stream)
             peak = peak64 if mode == "fp64" else peak32

@@ -81,6 +81,26 @@ int rmw_wall_product(int kind, const double *r, const double *v, double *out, in
 int rmw_wall_product_host(int kind, const double *r_host, const double *v_host, double *out_host,
                           int64_t n, double eta, double a, const double *L_host, int mode);
 
+/* Allocation-free variant of rmw_wall_product.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc - a host
+ * application whose device memory belongs to another allocator (a framework
+ * that reserves the whole GPU up front), code that must keep its device-memory
+ * footprint fixed after start-up, or a latency-sensitive loop that cannot take
+ * the implicit device-wide synchronisation of cudaMalloc/cudaFree.  Arguments
+ * and result are those of rmw_wall_product (device pointers; the caller still
+ * provides inputs and outputs).  The scratch is a file-scope device array of
+ * 16 MiB that every GPU loading the library holds until process exit, so n is
+ * limited to RMW_NOALLOC_MAX_BLOBS (larger n returns RMW_ERR_ARG).  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress,
+ * with that device current) and caches it; make that first call before any
+ * stream capture.  All calls share the one array: calls whose work overlaps on
+ * the GPU (different streams, or several host threads) race on it and must be
+ * serialised by the caller.  The function calls no cudaMalloc, cudaFree or
+ * other allocating routine. */
+#define RMW_NOALLOC_MAX_BLOBS 180000
+int rmw_wall_product_noalloc(int kind, const double *r, const double *v, double *out, int64_t n, double eta,
+                             double a, const double *L_host, int mode, void *stream);
+
 /* Measured FMA-pipe throughput of the current device (FLOP/s, FMA = 2 flops)
  * for FP64 (fp64 != 0) or FP32: the denominator of the pair kernels' roofline
  * fraction.  Synchronous.  Library-only (no reference counterpart). */

@@ -45,6 +45,7 @@ SIGNATURES = {
     "rmw_wall_wf": (_i, [_vp, _vp, _vp, _i64, _d, _d, _vp, _i, _vp]),
     "rmw_wall_wt": (_i, [_vp, _vp, _vp, _i64, _d, _d, _vp, _i, _vp]),
     "rmw_wall_product_host": (_i, [_i, _vp, _vp, _vp, _i64, _d, _d, _vp, _i]),
+    "rmw_wall_product_noalloc": (_i, [_i, _vp, _vp, _vp, _i64, _d, _d, _vp, _i, _vp]),
     "rmw_fma_peak": (_i, [_i, ctypes.POINTER(ctypes.c_double), _vp]),
     "rmw_trace_enable": (_i, [_i]),
     "rmw_trace_read": (_i, [_i, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64), _i]),

@@ -369,6 +369,8 @@ static int choose_chunks(int n)
     return std::max(1, std::min(s, 64));
 }
 
+int wall_default_chunks(int n) { return choose_chunks(n); }
+
 size_t wall_scratch_bytes(int n, int mode, int nchunks)
 {
     size_t rec = (mode == RMW_MODE_FP64) ? sizeof(SrcD) : sizeof(SrcF);

@@ -81,6 +81,103 @@ int rmw_wall_product(int kind, const double *r, const double *v, double *out, in
 int rmw_wall_product_host(int kind, const double *r_host, const double *v_host, double *out_host,
                           int64_t n, double eta, double a, const double *L_host, int mode);
 
+/* ---- rigid multiblob bodies ------------------------------------------
+ * A handle (opaque, void*) holds one suspension of rigid bodies: body b owns
+ * blobs [blob_offsets[b], blob_offsets[b+1]) (the reference's bodies list in
+ * order, multi_bodies/multi_bodies.py:194-204).  Vectors of the saddle-point
+ * system are [lambda (3N); U (6 Nb)] with U_b = (velocity, angular velocity),
+ * the layout of linear_operator_rigid (multi_bodies.py:424-471).  The handle
+ * is bound to the stream it was created with; all device arrays are owned by
+ * the caller except the handle's own copies. */
+
+/* Create a handle (blob_offsets_host: n_bodies + 1 entries, starting at 0). */
+int rmw_rigid_create(void **handle, int64_t n_bodies, const int64_t *blob_offsets_host, double eta, double a,
+                     const double *L_host, void *stream);
+int rmw_rigid_destroy(void *handle);
+int rmw_rigid_sizes(void *handle, int64_t *n_blobs_host, int64_t *n_bodies_host);
+/* Copy blob positions r (N,3) and body locations x (Nb,3) (device pointers)
+ * into the handle; invalidates the preconditioner
+ * (body/body.py:64-78 get_r_vectors gives r from location + orientation). */
+int rmw_rigid_set_configuration(void *handle, const double *r_blobs, const double *x_bodies);
+/* Block-diagonal preconditioner: per body the dense wall mobility, its
+ * Cholesky factor, inverse and N = (K^T M^-1 K)^-1.  Replaces
+ * build_block_diagonal_preconditioner (multi_bodies.py:752-903); with
+ * stochastic != 0 also keeps L and L^-1, replacing
+ * build_block_diagonal_preconditioners_det_stoch (multi_bodies.py:480-618).
+ * Synchronous; RMW_ERR_NONFINITE if a body matrix is not positive definite. */
+int rmw_rigid_build_pc(void *handle, int stochastic);
+/* y = [[M, -K], [-K^T, 0]] x  (linear_operator_rigid, multi_bodies.py:424-471). */
+int rmw_rigid_apply(void *handle, const double *x, double *y, int mode);
+/* y = P^-1 x  (block_diagonal_preconditioner apply, multi_bodies.py:825-861). */
+int rmw_rigid_apply_pc(void *handle, const double *x, double *y);
+/* y = L^-1 M L^-T w on the 3N blob space (det_stoch mobility_pc, multi_bodies.py:591-606). */
+int rmw_rigid_mobility_pc(void *handle, const double *w, double *y, int mode);
+/* y = L w  (det_stoch P_inv_mult, multi_bodies.py:609-615). */
+int rmw_rigid_P_inv_mult(void *handle, const double *w, double *y);
+/* out (3N) = K u (u: 6 Nb)  (K_matrix_vector_prod, multi_bodies.py:328-347). */
+int rmw_rigid_K_mult(void *handle, const double *u, double *out);
+/* out (6 Nb) = K^T lambda  (K_matrix_T_vector_prod, multi_bodies.py:350-371). */
+int rmw_rigid_KT_mult(void *handle, const double *lambda, double *out);
+/* Dense per-body wall mobility blocks, bodies concatenated (each 3n_b x 3n_b,
+ * row-major): Body.calc_mobility_blobs with single_wall_fluid_mobility
+ * (body/body.py:186-191, mobility/mobility.py:1018-1116). */
+int rmw_rigid_body_mobility(void *handle, double *out);
+/* r_out (N,3) = R(q_b) r_ref + x_b for every blob: r_ref (N,3) body-frame
+ * blob coordinates, q (Nb,4) quaternions (s, p), x (Nb,3) locations
+ * (Body.get_r_vectors, body/body.py:64-78; Quaternion.rotation_matrix,
+ * quaternion_integrator/quaternion.py:42-51). */
+int rmw_rigid_blob_positions(void *handle, const double *x_bodies, const double *q_bodies, const double *r_ref,
+                             double *r_out);
+/* Euler-Maruyama body update x_new = x + U dt, q_new = from_rotation(w dt) q
+ * with velocities (Nb,6) = (U, w) per body
+ * (quaternion_integrator_multi_bodies.py:308-312, quaternion.py:16-39). */
+int rmw_rigid_euler_update(void *handle, const double *x_bodies, const double *q_bodies, const double *velocities,
+                           double dt, double *x_new, double *q_new);
+/* Number of blobs with z < zmin (the wall check of Body.check_function,
+ * body/body.py:118-140).  Synchronous. */
+int rmw_count_below(const double *r, int64_t n, double zmin, int *count_host, void *stream);
+/* Right-preconditioned restarted GMRES on the saddle-point system with the
+ * block-diagonal preconditioner (zero initial guess), stopping when the true
+ * residual |b - A x| <= tol |b|: utils.gmres as called by
+ * solve_mobility_problem (general_application_utils.py:514-635,
+ * quaternion_integrator_multi_bodies.py:1441-1547).  mode RMW_MODE_MIXED runs
+ * the inner GMRES on the FP32-pair operator inside FP64 iterative refinement.
+ * Synchronous.  Returns RMW_ERR_NOT_CONVERGED after maxiter iterations (the
+ * best iterate is still written to sol). */
+int rmw_rigid_solve(void *handle, const double *rhs, double *sol, double tol, int restart, int maxiter, int mode,
+                    int *iters_host, double *relres_host);
+/* noise = factor * L (L^-1 M L^-T)^(1/2) z by Lanczos: stochastic_forcing_lanczos
+ * with mobility_mult = mobility_pc and L_mult = P_inv_mult
+ * (stochastic_forcing/stochastic_forcing.py:112-264), z and noise 3N device
+ * vectors.  Synchronous. */
+int rmw_rigid_lanczos(void *handle, const double *z, double *noise, double factor, double tol, int max_iter,
+                      int mode, int *iters_host);
+/* noise = factor * M^(1/2) z for the wall mobility of n free blobs (Lanczos
+ * without preconditioner).  Synchronous. */
+int rmw_wall_lanczos(const double *r, const double *z, double *noise, int64_t n, double eta, double a,
+                     const double *L_host, double factor, double tol, int max_iter, int mode, void *stream,
+                     int *iters_host);
+
+/* ---- generic Krylov solvers with caller-supplied operators ------------
+ * op(ctx, x, y) must write y = A x for device vectors of length n, enqueue its
+ * work on the solver's stream (or finish it before returning) and return 0 on
+ * success.  These serve the reference's generic entry points, whose operators
+ * are arbitrary callables. */
+typedef int (*rmw_operator_fn)(void *ctx, const double *x, double *y);
+/* Right-preconditioned restarted GMRES (pc may be NULL: no preconditioner),
+ * zero initial guess, stop on the true residual |b - A x| <= tol |b|:
+ * general_application_utils.gmres (general_application_utils.py:514-635).
+ * history_host (optional, history_cap entries) receives the relative residual
+ * estimate of every iteration.  Synchronous. */
+int rmw_gmres(int64_t n, rmw_operator_fn op, void *op_ctx, rmw_operator_fn pc, void *pc_ctx, const double *b,
+              double *x, double tol, int restart, int maxiter, void *stream, int *iters_host, double *relres_host,
+              double *history_host, int history_cap);
+/* noise = factor * A^(1/2) z by Lanczos with one full reorthogonalisation
+ * pass per step: stochastic_forcing_lanczos (stochastic_forcing.py:112-264)
+ * without L_mult.  Synchronous. */
+int rmw_lanczos(int64_t n, rmw_operator_fn op, void *op_ctx, const double *z, double *noise, double factor,
+                double tol, int max_iter, void *stream, int *iters_host);
+
 /* Allocation-free variant of rmw_wall_product.  No counterpart in the
  * reference: it exists for callers that cannot call cudaMalloc - a host
  * application whose device memory belongs to another allocator (a framework

@@ -38,6 +38,7 @@ def _lib(fast=False):
     lib.oracle_wall_uf_symmetric.argtypes = [dp, dp, dp, ctypes.c_long, ctypes.c_double, ctypes.c_double,
                                              ctypes.c_int]
     lib.oracle_max_threads.restype = ctypes.c_int
+    lib.oracle_wall_dense.argtypes = [dp, ctypes.c_long, ctypes.c_double, ctypes.c_double, dp]
     _libs[key] = lib
     return lib
 
@@ -66,6 +67,15 @@ def wall_product(kind, r_vectors, vector, eta, a, periodic_length=None, rows=Non
     fn = lib.oracle_wall_product_rows if regularize else lib.oracle_wall_raw_rows
     fn(KINDS[kind], _dp(r), _dp(v), _dp(out), n, rp, nr, float(eta), float(a), _dp(L))
     return out
+
+
+def dense_mobility(r_vectors, eta, a):
+    """Dense regularised wall mobility (3N, 3N) (mobility/mobility.py:1018-1116)."""
+    r = np.ascontiguousarray(np.asarray(r_vectors, dtype=np.float64).reshape(-1, 3))
+    n = r.shape[0]
+    M = np.empty((3 * n, 3 * n))
+    _lib().oracle_wall_dense(_dp(r), n, float(eta), float(a), _dp(M))
+    return M
 
 
 def shift_heights(r_vectors, blob_radius):

@@ -346,6 +346,34 @@ void oracle_wall_product(int kind, const double *r, const double *v, double *out
     oracle_wall_product_rows(kind, r, v, out, n, NULL, 0, eta, a, L);
 }
 
+/* Dense wall mobility (3n x 3n, row-major) of n blobs, regularised like
+ * single_wall_fluid_mobility (mobility/mobility.py:1018-1116): entries of
+ * B M(z_eff) B with the per-pair formulas of the UF product. */
+void oracle_wall_dense(const double *r, long n, double eta, double a, double *M)
+{
+    double inva = 1.0 / a;
+    double nf = norm_factor(0, eta, a);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long i = 0; i < n; ++i) {
+        double zi = r[3 * i + 2];
+        double bi = (zi < a) ? zi / a : 1.0;
+        double zie = (zi <= a) ? a : zi;
+        for (long j = 0; j < n; ++j) {
+            double zj = r[3 * j + 2];
+            double bj = (zj < a) ? zj / a : 1.0;
+            double zje = (zj <= a) ? a : zj;
+            for (int c = 0; c < 3; ++c) {
+                double e[3] = {0.0, 0.0, 0.0};
+                double col[3] = {0.0, 0.0, 0.0};
+                e[c] = 1.0;
+                pair_block(0, r[3 * i] - r[3 * j], r[3 * i + 1] - r[3 * j + 1], zie - zje, zie, zje, i == j, inva,
+                           e, col);
+                for (int u = 0; u < 3; ++u) M[(3 * i + u) * 3 * n + 3 * j + c] = col[u] * nf * bi * bj;
+            }
+        }
+    }
+}
+
 /* Symmetric-pair M_UF f in the loop structure of mobility/mobility.cpp:256-430
  * (non-periodic).  r must already hold z_eff and f must already be damped. */
 void oracle_wall_uf_symmetric(const double *r, const double *f, double *u,

@@ -45,6 +45,29 @@ SIGNATURES = {
     "rmw_wall_wf": (_i, [_vp, _vp, _vp, _i64, _d, _d, _vp, _i, _vp]),
     "rmw_wall_wt": (_i, [_vp, _vp, _vp, _i64, _d, _d, _vp, _i, _vp]),
     "rmw_wall_product_host": (_i, [_i, _vp, _vp, _vp, _i64, _d, _d, _vp, _i]),
+    "rmw_rigid_create": (_i, [ctypes.POINTER(ctypes.c_void_p), _i64, _vp, _d, _d, _vp, _vp]),
+    "rmw_rigid_destroy": (_i, [_vp]),
+    "rmw_rigid_sizes": (_i, [_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
+    "rmw_rigid_set_configuration": (_i, [_vp, _vp, _vp]),
+    "rmw_rigid_build_pc": (_i, [_vp, _i]),
+    "rmw_rigid_apply": (_i, [_vp, _vp, _vp, _i]),
+    "rmw_rigid_apply_pc": (_i, [_vp, _vp, _vp]),
+    "rmw_rigid_mobility_pc": (_i, [_vp, _vp, _vp, _i]),
+    "rmw_rigid_P_inv_mult": (_i, [_vp, _vp, _vp]),
+    "rmw_rigid_K_mult": (_i, [_vp, _vp, _vp]),
+    "rmw_rigid_KT_mult": (_i, [_vp, _vp, _vp]),
+    "rmw_rigid_body_mobility": (_i, [_vp, _vp]),
+    "rmw_rigid_blob_positions": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "rmw_rigid_euler_update": (_i, [_vp, _vp, _vp, _vp, _d, _vp, _vp]),
+    "rmw_count_below": (_i, [_vp, _i64, _d, ctypes.POINTER(ctypes.c_int), _vp]),
+    "rmw_rigid_solve": (_i, [_vp, _vp, _vp, _d, _i, _i, _i, ctypes.POINTER(ctypes.c_int),
+                             ctypes.POINTER(ctypes.c_double)]),
+    "rmw_rigid_lanczos": (_i, [_vp, _vp, _vp, _d, _d, _i, _i, ctypes.POINTER(ctypes.c_int)]),
+    "rmw_wall_lanczos": (_i, [_vp, _vp, _vp, _i64, _d, _d, _vp, _d, _d, _i, _i, _vp,
+                              ctypes.POINTER(ctypes.c_int)]),
+    "rmw_gmres": (_i, [_i64, _vp, _vp, _vp, _vp, _vp, _vp, _d, _i, _i, _vp, ctypes.POINTER(ctypes.c_int),
+                       ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _i]),
+    "rmw_lanczos": (_i, [_i64, _vp, _vp, _vp, _vp, _d, _d, _i, _vp, ctypes.POINTER(ctypes.c_int)]),
     "rmw_wall_product_noalloc": (_i, [_i, _vp, _vp, _vp, _i64, _d, _d, _vp, _i, _vp]),
     "rmw_fma_peak": (_i, [_i, ctypes.POINTER(ctypes.c_double), _vp]),
     "rmw_trace_enable": (_i, [_i]),
@@ -69,6 +92,9 @@ def trace_read(kind=0, reset=True):
     cnt = ctypes.c_int64(0)
     call("rmw_trace_read", kind, ctypes.byref(ms), ctypes.byref(cnt), 1 if reset else 0)
     return ms.value, cnt.value
+
+
+OPERATOR_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p)
 
 
 def lib_path():

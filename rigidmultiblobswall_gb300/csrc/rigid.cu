@@ -1,0 +1,734 @@
+// Rigid multiblob bodies: geometric matrix K, the block-diagonal
+// preconditioners of multi_bodies/multi_bodies.py and the saddle-point
+// operator of linear_operator_rigid, all on the GPU.
+//
+//   K [U; w]_i  = U_b + w_b x (r_i - x_b)               (body/body.py:81-115)
+//   K^T l       = [sum_i l_i ; sum_i (r_i - x_b) x l_i]  (multi_bodies.py:350-371)
+//   A [l; U]    = [M l - K U ; -K^T l]                   (multi_bodies.py:424-471)
+//
+// Block-diagonal preconditioner (multi_bodies.py:752-903 / 480-618), per body b
+// with m = 3 n_b blob unknowns:
+//   M_b      dense wall mobility of the body's blobs (mobility/mobility.py:1018-1116)
+//   M_b = L L^T (Cholesky), L^-1, M_b^-1 = L^-T L^-1, N_b = (K^T M_b^-1 K)^-1
+//   apply:  l~ = M_b^-1 s ; U = N_b (-F - K^T l~) ; l = l~ + (M_b^-1 K) U
+// (M_b^-1 K is precomputed, so one apply reads M_b^-1 once instead of twice.)
+//
+// One CTA per body.  The factorisation runs in shared memory when m^2 doubles
+// fit (m <= 160, i.e. up to 53 blobs per body), else in global memory.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "pair_math.cuh"
+#include "rigid.cuh"
+#include "wall_pair.cuh"
+
+namespace rmw {
+
+constexpr int kRigidThreads = 256;
+constexpr int kSmemMaxM = 160;
+
+// ---------------------------------------------------------------------------
+// K and K^T
+__global__ void k_times_u_kernel(const double *__restrict__ r, const double *__restrict__ xb,
+                                 const int *__restrict__ blob_body, const double *__restrict__ u,
+                                 double *__restrict__ out, int n, double alpha, double beta)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int b = blob_body[i];
+    const double dx = r[3 * i] - xb[3 * b], dy = r[3 * i + 1] - xb[3 * b + 1], dz = r[3 * i + 2] - xb[3 * b + 2];
+    const double *U = u + 6 * b;
+    const double kx = U[0] + (U[4] * dz - U[5] * dy);
+    const double ky = U[1] + (U[5] * dx - U[3] * dz);
+    const double kz = U[2] + (U[3] * dy - U[4] * dx);
+    if (beta == 0.0) {
+        out[3 * i] = alpha * kx;
+        out[3 * i + 1] = alpha * ky;
+        out[3 * i + 2] = alpha * kz;
+    } else {
+        out[3 * i] = beta * out[3 * i] + alpha * kx;
+        out[3 * i + 1] = beta * out[3 * i + 1] + alpha * ky;
+        out[3 * i + 2] = beta * out[3 * i + 2] + alpha * kz;
+    }
+}
+
+// one warp per body; out_b = alpha * K_b^T l
+__global__ void kt_times_lambda_kernel(const double *__restrict__ r, const double *__restrict__ xb,
+                                       const int *__restrict__ boff, const double *__restrict__ lam,
+                                       double *__restrict__ out, int nb, double alpha)
+{
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= nb) return;
+    const int b = warp;
+    const double cx = xb[3 * b], cy = xb[3 * b + 1], cz = xb[3 * b + 2];
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = boff[b] + lane; i < boff[b + 1]; i += 32) {
+        const double lx = lam[3 * i], ly = lam[3 * i + 1], lz = lam[3 * i + 2];
+        const double dx = r[3 * i] - cx, dy = r[3 * i + 1] - cy, dz = r[3 * i + 2] - cz;
+        s[0] += lx; s[1] += ly; s[2] += lz;
+        s[3] += dy * lz - dz * ly;
+        s[4] += dz * lx - dx * lz;
+        s[5] += dx * ly - dy * lx;
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c)
+        for (int o = 16; o > 0; o >>= 1) s[c] += __shfl_xor_sync(0xffffffffu, s[c], o);
+    if (lane < 6) out[6 * b + lane] = alpha * s[lane];
+}
+
+// ---------------------------------------------------------------------------
+// dense per-body wall mobility M_b = nf * B M~(z_eff) B (row-major m x m)
+__global__ void body_mobility_kernel(const double *__restrict__ r, const int *__restrict__ boff,
+                                     const long long *__restrict__ moff, double *__restrict__ M, double eta,
+                                     double a)
+{
+    const int b = blockIdx.x;
+    const int o = boff[b], nbl = boff[b + 1] - o, m = 3 * nbl;
+    double *Mb = M + moff[b];
+    const double inva = 1.0 / a;
+    const double nf = 1.0 / (8.0 * kPi * eta * a);
+    for (int pq = threadIdx.x; pq < nbl * nbl; pq += blockDim.x) {
+        const int p = pq / nbl, q = pq % nbl;
+        const int i = o + p, j = o + q;
+        const double zi = r[3 * i + 2], zj = r[3 * j + 2];
+        const double bi = (zi < a) ? zi / a : 1.0, bj = (zj < a) ? zj / a : 1.0;
+        const double zie = (zi <= a) ? a : zi, zje = (zj <= a) ? a : zj;
+        double blk[3][3];
+        if (p == q) {
+            const double iz = a / zie, iz3 = iz * iz * iz, iz5 = iz3 * iz * iz;
+            const double mxx = 4.0 / 3.0 - (9.0 * iz - 2.0 * iz3 + iz5) / 12.0;
+            const double mzz = 4.0 / 3.0 - (9.0 * iz - 4.0 * iz3 + iz5) / 6.0;
+            for (int u = 0; u < 3; ++u)
+                for (int w = 0; w < 3; ++w) blk[u][w] = 0.0;
+            blk[0][0] = mxx; blk[1][1] = mxx; blk[2][2] = mzz;
+        } else {
+            const double dx = (r[3 * i] - r[3 * j]) * inva, dy = (r[3 * i + 1] - r[3 * j + 1]) * inva;
+            const double dz = (zie - zje) * inva;
+            const double hi = zie * inva, hj = zje * inva, Rz = (zie + zje) * inva;
+            for (int w = 0; w < 3; ++w) {
+                double c[3] = {0.0, 0.0, 0.0};
+                pair_contrib<RMW_UF, double>(dx, dy, dz, Rz, hi, hj, w == 0 ? 1.0 : 0.0, w == 1 ? 1.0 : 0.0,
+                                             w == 2 ? 1.0 : 0.0, c[0], c[1], c[2]);
+                blk[0][w] = c[0]; blk[1][w] = c[1]; blk[2][w] = c[2];
+            }
+        }
+        const double sc = nf * bi * bj;
+        for (int u = 0; u < 3; ++u)
+            for (int w = 0; w < 3; ++w) Mb[(long long)(3 * p + u) * m + 3 * q + w] = sc * blk[u][w];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Cholesky + inverse of every M_b.  A (m x m, row-major) is the working copy
+// (shared memory or global); on exit minv holds M_b^-1, and lfac / linv (if
+// non-null) hold L and L^-1 (lower triangles, upper zero).
+__device__ void factor_and_invert(double *A, int m, double *tmp, double *minv, double *lfac, double *linv,
+                                  int *status)
+{
+    const int tid = threadIdx.x, nt = blockDim.x;
+    // right-looking Cholesky, lower triangle
+    for (int k = 0; k < m; ++k) {
+        if (tid == 0) {
+            const double d = A[k * m + k];
+            if (!(d > 0.0)) atomicExch(status, 1);  // not positive definite
+            A[k * m + k] = sqrt(fmax(d, 1e-300));
+        }
+        __syncthreads();
+        const double dk = A[k * m + k];
+        for (int i = k + 1 + tid; i < m; i += nt) A[i * m + k] /= dk;
+        __syncthreads();
+        const int t = m - k - 1;
+        for (int idx = tid; idx < t * t; idx += nt) {
+            const int i = k + 1 + idx / t, j = k + 1 + idx % t;
+            if (j <= i) A[i * m + j] -= A[i * m + k] * A[j * m + k];
+        }
+        __syncthreads();
+    }
+    for (int idx = tid; idx < m * m; idx += nt) {
+        const int i = idx / m, j = idx % m;
+        if (j > i) A[idx] = 0.0;
+        if (lfac) lfac[idx] = (j > i) ? 0.0 : A[idx];
+    }
+    __syncthreads();
+    // in-place inverse of the lower-triangular L, column by column from the right
+    for (int j = m - 1; j >= 0; --j) {
+        const double ajj = 1.0 / A[j * m + j];
+        for (int k = j + 1 + tid; k < m; k += nt) tmp[k] = A[k * m + j];
+        __syncthreads();
+        for (int i = j + 1 + tid; i < m; i += nt) {
+            double s = 0.0;
+            for (int k = j + 1; k <= i; ++k) s += A[i * m + k] * tmp[k];
+            A[i * m + j] = -ajj * s;
+        }
+        if (tid == 0) A[j * m + j] = ajj;
+        __syncthreads();
+    }
+    if (linv)
+        for (int idx = tid; idx < m * m; idx += nt) linv[idx] = A[idx];
+    // M^-1 = L^-T L^-1 : minv[i][j] = sum_{k >= max(i,j)} X[k][i] X[k][j]
+    for (int idx = tid; idx < m * m; idx += nt) {
+        const int i = idx / m, j = idx % m;
+        if (j < i) continue;
+        double s = 0.0;
+        for (int k = j; k < m; ++k) s += A[k * m + i] * A[k * m + j];
+        minv[(long long)i * m + j] = s;
+        minv[(long long)j * m + i] = s;
+    }
+}
+
+__global__ void pc_factor_smem_kernel(const double *__restrict__ M, const long long *__restrict__ moff,
+                                      const int *__restrict__ boff, double *__restrict__ minv, double *lfac,
+                                      double *linv, int *status)
+{
+    extern __shared__ double sm[];
+    const int b = blockIdx.x;
+    const int m = 3 * (boff[b + 1] - boff[b]);
+    double *A = sm, *tmp = sm + m * m;
+    const double *Mb = M + moff[b];
+    for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) A[idx] = Mb[idx];
+    __syncthreads();
+    factor_and_invert(A, m, tmp, minv + moff[b], lfac ? lfac + moff[b] : nullptr, linv ? linv + moff[b] : nullptr,
+                      status);
+}
+
+// global-memory variant: M is overwritten (it is the working copy), tmp is m doubles per body
+__global__ void pc_factor_global_kernel(double *__restrict__ M, const long long *__restrict__ moff,
+                                        const int *__restrict__ boff, double *__restrict__ minv, double *lfac,
+                                        double *linv, double *tmpg, int *status)
+{
+    const int b = blockIdx.x;
+    const int m = 3 * (boff[b + 1] - boff[b]);
+    factor_and_invert(M + moff[b], m, tmpg + 3 * boff[b], minv + moff[b], lfac ? lfac + moff[b] : nullptr,
+                      linv ? linv + moff[b] : nullptr, status);
+}
+
+// M^-1 K (m x 6) and N = (K^T M^-1 K)^-1 (6 x 6) per body
+__global__ void pc_body_kernel(const double *__restrict__ r, const double *__restrict__ xb,
+                               const int *__restrict__ boff, const long long *__restrict__ moff,
+                               const double *__restrict__ minv, double *__restrict__ minvK,
+                               double *__restrict__ nmat, int *status)
+{
+    __shared__ double G[36];
+    __shared__ double aug[6][12];
+    const int b = blockIdx.x;
+    const int o = boff[b], m = 3 * (boff[b + 1] - o);
+    const double *Mi = minv + moff[b];
+    double *MK = minvK + 6LL * 3 * o;
+    const double cx = xb[3 * b], cy = xb[3 * b + 1], cz = xb[3 * b + 2];
+    if (threadIdx.x < 36) G[threadIdx.x] = 0.0;
+    __syncthreads();
+    // MK[t][c] = sum_k Minv[t][k] K[k][c]; K row k = 3p+u: J part e_u, rot part R_p row u
+    for (int t = threadIdx.x; t < m; t += blockDim.x) {
+        double acc[6] = {0, 0, 0, 0, 0, 0};
+        for (int p = 0; p < m / 3; ++p) {
+            const int i = o + p;
+            const double dx = r[3 * i] - cx, dy = r[3 * i + 1] - cy, dz = r[3 * i + 2] - cz;
+            const double m0 = Mi[(long long)t * m + 3 * p], m1 = Mi[(long long)t * m + 3 * p + 1],
+                         m2 = Mi[(long long)t * m + 3 * p + 2];
+            acc[0] += m0; acc[1] += m1; acc[2] += m2;
+            // R_p = [[0, dz, -dy], [-dz, 0, dx], [dy, -dx, 0]] (R w = w x d)
+            acc[3] += -dz * m1 + dy * m2;
+            acc[4] += dz * m0 - dx * m2;
+            acc[5] += -dy * m0 + dx * m1;
+        }
+        for (int c = 0; c < 6; ++c) MK[6LL * t + c] = acc[c];
+    }
+    __syncthreads();
+    // G = K^T (M^-1 K)
+    if (threadIdx.x < 36) {
+        const int rr = threadIdx.x / 6, c = threadIdx.x % 6;
+        double s = 0.0;
+        for (int p = 0; p < m / 3; ++p) {
+            const int i = o + p;
+            const double dx = r[3 * i] - cx, dy = r[3 * i + 1] - cy, dz = r[3 * i + 2] - cz;
+            const double k0 = MK[6LL * (3 * p) + c], k1 = MK[6LL * (3 * p + 1) + c], k2 = MK[6LL * (3 * p + 2) + c];
+            double kr;
+            if (rr < 3) kr = (rr == 0) ? k0 : (rr == 1 ? k1 : k2);
+            else if (rr == 3) kr = -dz * k1 + dy * k2;
+            else if (rr == 4) kr = dz * k0 - dx * k2;
+            else kr = -dy * k0 + dx * k1;
+            s += kr;
+        }
+        G[threadIdx.x] = s;
+    }
+    __syncthreads();
+    // invert the symmetric positive definite 6x6 by Gauss-Jordan with partial pivoting
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 12; ++j) aug[i][j] = (j < 6) ? G[6 * i + j] : (j - 6 == i ? 1.0 : 0.0);
+        for (int c = 0; c < 6; ++c) {
+            int piv = c;
+            for (int i = c + 1; i < 6; ++i)
+                if (fabs(aug[i][c]) > fabs(aug[piv][c])) piv = i;
+            if (piv != c)
+                for (int j = 0; j < 12; ++j) {
+                    double t = aug[c][j]; aug[c][j] = aug[piv][j]; aug[piv][j] = t;
+                }
+            const double d = aug[c][c];
+            if (d == 0.0) { atomicExch(status, 2); continue; }
+            for (int j = 0; j < 12; ++j) aug[c][j] /= d;
+            for (int i = 0; i < 6; ++i) {
+                if (i == c) continue;
+                const double f = aug[i][c];
+                for (int j = 0; j < 12; ++j) aug[i][j] -= f * aug[c][j];
+            }
+        }
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) nmat[36 * b + 6 * i + j] = aug[i][6 + j];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// preconditioner apply, one CTA per body
+__global__ void pc_apply_kernel(const double *__restrict__ x, double *__restrict__ y,
+                                const double *__restrict__ r, const double *__restrict__ xb,
+                                const int *__restrict__ boff, const long long *__restrict__ moff,
+                                const double *__restrict__ minv, const double *__restrict__ minvK,
+                                const double *__restrict__ nmat, int n)
+{
+    extern __shared__ double sh[];
+    const int b = blockIdx.x;
+    const int o = boff[b], m = 3 * (boff[b + 1] - o);
+    double *s = sh;            // m
+    double *lt = sh + m;       // m
+    double *red = sh + 2 * m;  // 6 * (blockDim/32)
+    __shared__ double Y[6];
+    const double *Mi = minv + moff[b];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int t = tid; t < m; t += nt) s[t] = x[3LL * o + t];
+    __syncthreads();
+    for (int t = tid; t < m; t += nt) {
+        double acc = 0.0;
+        for (int k = 0; k < m; ++k) acc += Mi[(long long)k * m + t] * s[k];  // M^-1 symmetric: coalesced
+        lt[t] = acc;
+    }
+    __syncthreads();
+    // K^T l~
+    const double cx = xb[3 * b], cy = xb[3 * b + 1], cz = xb[3 * b + 2];
+    double p6[6] = {0, 0, 0, 0, 0, 0};
+    for (int p = tid; p < m / 3; p += nt) {
+        const int i = o + p;
+        const double dx = r[3 * i] - cx, dy = r[3 * i + 1] - cy, dz = r[3 * i + 2] - cz;
+        const double lx = lt[3 * p], ly = lt[3 * p + 1], lz = lt[3 * p + 2];
+        p6[0] += lx; p6[1] += ly; p6[2] += lz;
+        p6[3] += dy * lz - dz * ly;
+        p6[4] += dz * lx - dx * lz;
+        p6[5] += dx * ly - dy * lx;
+    }
+    const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        for (int off = 16; off > 0; off >>= 1) p6[c] += __shfl_xor_sync(0xffffffffu, p6[c], off);
+        if (lane == 0) red[6 * wid + c] = p6[c];
+    }
+    __syncthreads();
+    if (tid < 6) {
+        double ktl = 0.0;
+        for (int w = 0; w < nt / 32; ++w) ktl += red[6 * w + tid];
+        red[6 * (nt / 32) + tid] = -x[3LL * n + 6 * b + tid] - ktl;  // -F - K^T l~
+    }
+    __syncthreads();
+    if (tid < 6) {
+        const double *Nb = nmat + 36 * b;
+        const double *rhs = red + 6 * (nt / 32);
+        double u = 0.0;
+        for (int c = 0; c < 6; ++c) u += Nb[6 * tid + c] * rhs[c];
+        Y[tid] = u;
+        y[3LL * n + 6 * b + tid] = u;
+    }
+    __syncthreads();
+    const double *MK = minvK + 6LL * 3 * o;
+    for (int t = tid; t < m; t += nt) {
+        double acc = lt[t];
+        for (int c = 0; c < 6; ++c) acc += MK[6LL * t + c] * Y[c];
+        y[3LL * o + t] = acc;
+    }
+}
+
+// y_b = T_b x_b (T lower triangular, row-major) or T_b^T x_b, per body
+__global__ void block_tri_mult_kernel(const double *__restrict__ T, const long long *__restrict__ moff,
+                                      const int *__restrict__ boff, const double *__restrict__ x,
+                                      double *__restrict__ y, int transpose)
+{
+    extern __shared__ double xs[];
+    const int b = blockIdx.x;
+    const int o = boff[b], m = 3 * (boff[b + 1] - o);
+    const double *Tb = T + moff[b];
+    for (int t = threadIdx.x; t < m; t += blockDim.x) xs[t] = x[3LL * o + t];
+    __syncthreads();
+    for (int t = threadIdx.x; t < m; t += blockDim.x) {
+        double acc = 0.0;
+        if (!transpose)
+            for (int k = 0; k <= t; ++k) acc += Tb[(long long)t * m + k] * xs[k];
+        else
+            for (int k = t; k < m; ++k) acc += Tb[(long long)k * m + t] * xs[k];
+        y[3LL * o + t] = acc;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// body kinematics (FP64)
+// r_i = R(q_b) r_ref_i + x_b  (body/body.py:64-78, quaternion.py:42-51)
+__global__ void blob_positions_kernel(const double *__restrict__ xb, const double *__restrict__ q,
+                                      const double *__restrict__ rref, const int *__restrict__ blob_body,
+                                      double *__restrict__ r, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int b = blob_body[i];
+    const double s = q[4 * b], p0 = q[4 * b + 1], p1 = q[4 * b + 2], p2 = q[4 * b + 3];
+    const double dg = s * s - 0.5;
+    const double R00 = 2 * (p0 * p0 + dg), R01 = 2 * (p0 * p1 - s * p2), R02 = 2 * (p0 * p2 + s * p1);
+    const double R10 = 2 * (p1 * p0 + s * p2), R11 = 2 * (p1 * p1 + dg), R12 = 2 * (p1 * p2 - s * p0);
+    const double R20 = 2 * (p2 * p0 - s * p1), R21 = 2 * (p2 * p1 + s * p0), R22 = 2 * (p2 * p2 + dg);
+    const double a = rref[3 * i], bb = rref[3 * i + 1], c = rref[3 * i + 2];
+    r[3 * i] = R00 * a + R01 * bb + R02 * c + xb[3 * b];
+    r[3 * i + 1] = R10 * a + R11 * bb + R12 * c + xb[3 * b + 1];
+    r[3 * i + 2] = R20 * a + R21 * bb + R22 * c + xb[3 * b + 2];
+}
+
+// x_new = x + U dt ; q_new = from_rotation(w dt) * q   (quaternion_integrator_multi_bodies.py:308-312)
+__global__ void euler_update_kernel(const double *__restrict__ x, const double *__restrict__ q,
+                                    const double *__restrict__ vel, double dt, double *__restrict__ xn,
+                                    double *__restrict__ qn, int nb)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const double *U = vel + 6 * b;
+    xn[3 * b] = x[3 * b] + U[0] * dt;
+    xn[3 * b + 1] = x[3 * b + 1] + U[1] * dt;
+    xn[3 * b + 2] = x[3 * b + 2] + U[2] * dt;
+    const double f0 = U[3] * dt, f1 = U[4] * dt, f2 = U[5] * dt;
+    const double ph = sqrt(f0 * f0 + f1 * f1 + f2 * f2);
+    const double s1 = cos(ph / 2.0);
+    double p0 = 0.0, p1 = 0.0, p2 = 0.0;
+    if (ph != 0.0) {
+        const double sf = sin(ph / 2.0) / ph;
+        p0 = sf * f0; p1 = sf * f1; p2 = sf * f2;
+    }
+    const double s2 = q[4 * b], r0 = q[4 * b + 1], r1 = q[4 * b + 2], r2 = q[4 * b + 3];
+    // (s1, p) * (s2, r) = (s1 s2 - p.r, s1 r + s2 p + p x r)
+    qn[4 * b] = s1 * s2 - (p0 * r0 + p1 * r1 + p2 * r2);
+    qn[4 * b + 1] = s1 * r0 + s2 * p0 + (p1 * r2 - p2 * r1);
+    qn[4 * b + 2] = s1 * r1 + s2 * p1 + (p2 * r0 - p0 * r2);
+    qn[4 * b + 3] = s1 * r2 + s2 * p2 + (p0 * r1 - p1 * r0);
+}
+
+// count of blobs with z < zmin (Body.check_function, body/body.py:118-140)
+__global__ void count_below_kernel(const double *__restrict__ r, int n, double zmin, int *__restrict__ count)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool below = (i < n) && (r[3 * i + 2] < zmin);
+    const unsigned m = __ballot_sync(0xffffffffu, below);
+    if ((threadIdx.x & 31) == 0 && m) atomicAdd(count, __popc(m));
+}
+
+// ---------------------------------------------------------------------------
+// host side
+static int build_pc(RigidSystem &S, bool stochastic)
+{
+    cudaStream_t st = S.st;
+    const long long tot = S.moff_h[S.nb];
+    // working copy of the dense body mobilities (stream-ordered, freed below)
+    void *ws = nullptr;
+    const size_t ws_bytes = sizeof(double) * ((size_t)tot + 3 * (size_t)S.n);
+    RMW_CUDA(cudaMallocAsync(&ws, ws_bytes, st));
+    double *M = (double *)ws;
+    double *tmpg = M + tot;
+    if (!S.minv) {
+        RMW_CUDA(cudaMalloc(&S.minv, sizeof(double) * tot));
+        RMW_CUDA(cudaMalloc(&S.minvK, sizeof(double) * 6 * 3 * (size_t)S.n));
+        RMW_CUDA(cudaMalloc(&S.nmat, sizeof(double) * 36 * (size_t)S.nb));
+    }
+    if (stochastic && !S.lfac) {
+        RMW_CUDA(cudaMalloc(&S.lfac, sizeof(double) * tot));
+        RMW_CUDA(cudaMalloc(&S.linv, sizeof(double) * tot));
+    }
+    RMW_CUDA(cudaMemsetAsync(S.dstatus, 0, sizeof(int), st));
+    body_mobility_kernel<<<S.nb, kRigidThreads, 0, st>>>(S.r, S.boff, S.moff, M, S.eta, S.a);
+    double *lf = stochastic ? S.lfac : nullptr, *li = stochastic ? S.linv : nullptr;
+    if (S.max_m <= kSmemMaxM) {
+        const size_t sm = sizeof(double) * ((size_t)S.max_m * S.max_m + S.max_m);
+        RMW_CUDA(cudaFuncSetAttribute(pc_factor_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        pc_factor_smem_kernel<<<S.nb, kRigidThreads, sm, st>>>(M, S.moff, S.boff, S.minv, lf, li, S.dstatus);
+    } else {
+        pc_factor_global_kernel<<<S.nb, kRigidThreads, 0, st>>>(M, S.moff, S.boff, S.minv, lf, li, tmpg, S.dstatus);
+    }
+    pc_body_kernel<<<S.nb, 128, 0, st>>>(S.r, S.xb, S.boff, S.moff, S.minv, S.minvK, S.nmat, S.dstatus);
+    RMW_CHECK_LAUNCH("preconditioner build");
+    int hstat = 0;
+    RMW_CUDA(cudaMemcpyAsync(&hstat, S.dstatus, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RMW_CUDA(cudaFreeAsync(ws, st));
+    RMW_CUDA(cudaStreamSynchronize(st));
+    if (hstat == 1) return fail(RMW_ERR_NONFINITE, "body mobility matrix is not positive definite (Cholesky failed)");
+    if (hstat == 2) return fail(RMW_ERR_NONFINITE, "singular 6x6 body resistance K^T M^-1 K");
+    S.pc_ready = true;
+    S.stoch_ready = stochastic;
+    return RMW_OK;
+}
+
+int rigid_apply(RigidSystem &S, const double *x, double *y, int mode)
+{
+    cudaStream_t st = S.st;
+    // y_blob = M l
+    if (int rc = wall_product(RMW_UF, S.r, x, y, S.n, S.eta, S.a, S.L, mode, st)) return rc;
+    const int tb = 256;
+    // y_blob -= K U
+    k_times_u_kernel<<<(S.n + tb - 1) / tb, tb, 0, st>>>(S.r, S.xb, S.blob_body, x + 3LL * S.n, y, S.n, -1.0, 1.0);
+    // y_body = -K^T l
+    kt_times_lambda_kernel<<<(S.nb * 32 + tb - 1) / tb, tb, 0, st>>>(S.r, S.xb, S.boff, x, y + 3LL * S.n, S.nb,
+                                                                       -1.0);
+    RMW_CHECK_LAUNCH("rigid operator");
+    return RMW_OK;
+}
+
+int rigid_apply_pc(RigidSystem &S, const double *x, double *y)
+{
+    if (!S.pc_ready) return fail(RMW_ERR_ARG, "preconditioner not built (call rmw_rigid_build_pc)");
+    const int nt = 128;
+    const size_t sm = sizeof(double) * (2 * (size_t)S.max_m + 6 * (nt / 32 + 1));
+    if (sm > 48 * 1024)
+        RMW_CUDA(cudaFuncSetAttribute(pc_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    void *tok = nullptr;
+    if (int rc = trace_begin(TRACE_PC, S.st, &tok)) return rc;
+    pc_apply_kernel<<<S.nb, nt, sm, S.st>>>(x, y, S.r, S.xb, S.boff, S.moff, S.minv, S.minvK, S.nmat, S.n);
+    if (int rc = trace_end(tok, S.st)) return rc;
+    RMW_CHECK_LAUNCH("preconditioner apply");
+    return RMW_OK;
+}
+
+static int tri_mult(RigidSystem &S, const double *T, const double *x, double *y, int transpose)
+{
+    const size_t sm = sizeof(double) * (size_t)S.max_m;
+    block_tri_mult_kernel<<<S.nb, 128, sm, S.st>>>(T, S.moff, S.boff, x, y, transpose);
+    RMW_CHECK_LAUNCH("block triangular multiply");
+    return RMW_OK;
+}
+
+int rigid_mobility_pc(RigidSystem &S, const double *w, double *y, int mode)
+{
+    if (!S.stoch_ready) return fail(RMW_ERR_ARG, "stochastic preconditioner not built");
+    // y = L^-1 M L^-T w   (P = L^-T, reference: P^T M P with P = U^-1, U = L^T)
+    if (int rc = tri_mult(S, S.linv, w, S.tmp3n, 1)) return rc;
+    if (int rc = wall_product(RMW_UF, S.r, S.tmp3n, y, S.n, S.eta, S.a, S.L, mode, S.st)) return rc;
+    // in place is safe per body: each CTA stages its own slice in shared memory first
+    return tri_mult(S, S.linv, y, y, 0);
+}
+
+int rigid_P_inv_mult(RigidSystem &S, const double *w, double *y)
+{
+    if (!S.stoch_ready) return fail(RMW_ERR_ARG, "stochastic preconditioner not built");
+    return tri_mult(S, S.lfac, w, y, 0);
+}
+
+static void free_system(RigidSystem *S)
+{
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(S->device);
+    void *ptrs[] = {S->boff, S->blob_body, S->moff, S->r, S->xb, S->minv, S->minvK, S->nmat, S->lfac, S->linv,
+                    S->dstatus, S->tmp3n};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    cudaSetDevice(cur);
+    delete S;
+}
+
+}  // namespace rmw
+
+// ---------------------------------------------------------------------------
+// C ABI
+using rmw::RigidSystem;
+
+extern "C" {
+
+int rmw_rigid_create(void **out, int64_t n_bodies, const int64_t *blob_offsets_host, double eta, double a,
+                     const double *L_host, void *stream)
+{
+    if (!out) return rmw::fail(RMW_ERR_ARG, "null output handle");
+    *out = nullptr;
+    if (n_bodies <= 0 || n_bodies > (1 << 24)) return rmw::fail(RMW_ERR_ARG, "n_bodies out of range");
+    if (!blob_offsets_host) return rmw::fail(RMW_ERR_ARG, "null blob offsets");
+    if (!(a > 0) || !(eta > 0)) return rmw::fail(RMW_ERR_ARG, "blob radius and viscosity must be positive");
+    if (blob_offsets_host[0] != 0) return rmw::fail(RMW_ERR_ARG, "blob offsets must start at 0");
+    RigidSystem *S = new RigidSystem();
+    S->nb = (int)n_bodies;
+    S->eta = eta;
+    S->a = a;
+    if (L_host)
+        for (int k = 0; k < 3; ++k) S->L[k] = L_host[k];
+    S->st = rmw::as_stream(stream);
+    cudaGetDevice(&S->device);
+    S->boff_h.resize(S->nb + 1);
+    S->moff_h.resize(S->nb + 1);
+    S->moff_h[0] = 0;
+    for (int b = 0; b <= S->nb; ++b) {
+        S->boff_h[b] = (int)blob_offsets_host[b];
+        if (b > 0) {
+            const long long nbl = blob_offsets_host[b] - blob_offsets_host[b - 1];
+            if (nbl <= 0 || blob_offsets_host[b] > (1LL << 28)) {
+                delete S;
+                return rmw::fail(RMW_ERR_ARG, "blob offsets must be strictly increasing (every body needs a blob)");
+            }
+            S->max_m = std::max(S->max_m, (int)(3 * nbl));
+            S->moff_h[b] = S->moff_h[b - 1] + 9 * nbl * nbl;
+        }
+    }
+    S->n = S->boff_h[S->nb];
+    std::vector<int> bb(S->n);
+    for (int b = 0; b < S->nb; ++b)
+        for (int i = S->boff_h[b]; i < S->boff_h[b + 1]; ++i) bb[i] = b;
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if (e == cudaSuccess) e = x;
+    };
+    chk(cudaMalloc(&S->boff, sizeof(int) * (S->nb + 1)));
+    chk(cudaMalloc(&S->blob_body, sizeof(int) * S->n));
+    chk(cudaMalloc(&S->moff, sizeof(long long) * (S->nb + 1)));
+    chk(cudaMalloc(&S->r, sizeof(double) * 3 * S->n));
+    chk(cudaMalloc(&S->xb, sizeof(double) * 3 * S->nb));
+    chk(cudaMalloc(&S->dstatus, sizeof(int)));
+    chk(cudaMalloc(&S->tmp3n, sizeof(double) * 3 * S->n));
+    if (e == cudaSuccess) {
+        chk(cudaMemcpy(S->boff, S->boff_h.data(), sizeof(int) * (S->nb + 1), cudaMemcpyHostToDevice));
+        chk(cudaMemcpy(S->blob_body, bb.data(), sizeof(int) * S->n, cudaMemcpyHostToDevice));
+        chk(cudaMemcpy(S->moff, S->moff_h.data(), sizeof(long long) * (S->nb + 1), cudaMemcpyHostToDevice));
+    }
+    if (e != cudaSuccess) {
+        rmw::free_system(S);
+        return rmw::cuda_fail(e, "rmw_rigid_create");
+    }
+    *out = S;
+    return RMW_OK;
+}
+
+int rmw_rigid_destroy(void *sys)
+{
+    if (sys) rmw::free_system((RigidSystem *)sys);
+    return RMW_OK;
+}
+
+int rmw_rigid_sizes(void *sys, int64_t *n_blobs_host, int64_t *n_bodies_host)
+{
+    if (!sys || !n_blobs_host || !n_bodies_host) return rmw::fail(RMW_ERR_ARG, "null argument");
+    RigidSystem *S = (RigidSystem *)sys;
+    *n_blobs_host = S->n;
+    *n_bodies_host = S->nb;
+    return RMW_OK;
+}
+
+int rmw_rigid_set_configuration(void *sys, const double *r_blobs, const double *x_bodies)
+{
+    if (!sys || !r_blobs || !x_bodies) return rmw::fail(RMW_ERR_ARG, "null argument");
+    RigidSystem *S = (RigidSystem *)sys;
+    RMW_CUDA(cudaMemcpyAsync(S->r, r_blobs, sizeof(double) * 3 * S->n, cudaMemcpyDeviceToDevice, S->st));
+    RMW_CUDA(cudaMemcpyAsync(S->xb, x_bodies, sizeof(double) * 3 * S->nb, cudaMemcpyDeviceToDevice, S->st));
+    S->pc_ready = S->stoch_ready = false;
+    return RMW_OK;
+}
+
+int rmw_rigid_build_pc(void *sys, int stochastic)
+{
+    if (!sys) return rmw::fail(RMW_ERR_ARG, "null handle");
+    return rmw::build_pc(*(RigidSystem *)sys, stochastic != 0);
+}
+
+int rmw_rigid_apply(void *sys, const double *x, double *y, int mode)
+{
+    if (!sys || !x || !y) return rmw::fail(RMW_ERR_ARG, "null argument");
+    if (x == y) return rmw::fail(RMW_ERR_ARG, "rmw_rigid_apply cannot run in place");
+    return rmw::rigid_apply(*(RigidSystem *)sys, x, y, mode);
+}
+
+int rmw_rigid_apply_pc(void *sys, const double *x, double *y)
+{
+    if (!sys || !x || !y) return rmw::fail(RMW_ERR_ARG, "null argument");
+    if (x == y) return rmw::fail(RMW_ERR_ARG, "rmw_rigid_apply_pc cannot run in place");
+    return rmw::rigid_apply_pc(*(RigidSystem *)sys, x, y);
+}
+
+int rmw_rigid_mobility_pc(void *sys, const double *w, double *y, int mode)
+{
+    if (!sys || !w || !y) return rmw::fail(RMW_ERR_ARG, "null argument");
+    return rmw::rigid_mobility_pc(*(RigidSystem *)sys, w, y, mode);
+}
+
+int rmw_rigid_P_inv_mult(void *sys, const double *w, double *y)
+{
+    if (!sys || !w || !y) return rmw::fail(RMW_ERR_ARG, "null argument");
+    return rmw::rigid_P_inv_mult(*(RigidSystem *)sys, w, y);
+}
+
+int rmw_rigid_K_mult(void *sys, const double *u, double *out)
+{
+    if (!sys || !u || !out) return rmw::fail(RMW_ERR_ARG, "null argument");
+    RigidSystem *S = (RigidSystem *)sys;
+    rmw::k_times_u_kernel<<<(S->n + 255) / 256, 256, 0, S->st>>>(S->r, S->xb, S->blob_body, u, out, S->n, 1.0, 0.0);
+    RMW_CHECK_LAUNCH("K multiply");
+    return RMW_OK;
+}
+
+int rmw_rigid_KT_mult(void *sys, const double *lam, double *out)
+{
+    if (!sys || !lam || !out) return rmw::fail(RMW_ERR_ARG, "null argument");
+    RigidSystem *S = (RigidSystem *)sys;
+    rmw::kt_times_lambda_kernel<<<(S->nb * 32 + 255) / 256, 256, 0, S->st>>>(S->r, S->xb, S->boff, lam, out, S->nb,
+                                                                              1.0);
+    RMW_CHECK_LAUNCH("K^T multiply");
+    return RMW_OK;
+}
+
+int rmw_rigid_blob_positions(void *sys, const double *x_bodies, const double *q_bodies, const double *r_ref,
+                             double *r_out)
+{
+    if (!sys || !x_bodies || !q_bodies || !r_ref || !r_out) return rmw::fail(RMW_ERR_ARG, "null argument");
+    RigidSystem *S = (RigidSystem *)sys;
+    rmw::blob_positions_kernel<<<(S->n + 255) / 256, 256, 0, S->st>>>(x_bodies, q_bodies, r_ref, S->blob_body,
+                                                                       r_out, S->n);
+    RMW_CHECK_LAUNCH("blob positions");
+    return RMW_OK;
+}
+
+int rmw_rigid_euler_update(void *sys, const double *x_bodies, const double *q_bodies, const double *velocities,
+                           double dt, double *x_new, double *q_new)
+{
+    if (!sys || !x_bodies || !q_bodies || !velocities || !x_new || !q_new)
+        return rmw::fail(RMW_ERR_ARG, "null argument");
+    RigidSystem *S = (RigidSystem *)sys;
+    rmw::euler_update_kernel<<<(S->nb + 127) / 128, 128, 0, S->st>>>(x_bodies, q_bodies, velocities, dt, x_new,
+                                                                      q_new, S->nb);
+    RMW_CHECK_LAUNCH("euler update");
+    return RMW_OK;
+}
+
+int rmw_count_below(const double *r, int64_t n, double zmin, int *count_host, void *stream)
+{
+    if (!r || !count_host || n < 0) return rmw::fail(RMW_ERR_ARG, "bad argument");
+    cudaStream_t st = rmw::as_stream(stream);
+    *count_host = 0;
+    if (n == 0) return RMW_OK;
+    int *d = nullptr;
+    RMW_CUDA(cudaMallocAsync(&d, sizeof(int), st));
+    RMW_CUDA(cudaMemsetAsync(d, 0, sizeof(int), st));
+    rmw::count_below_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(r, (int)n, zmin, d);
+    RMW_CHECK_LAUNCH("count below");
+    RMW_CUDA(cudaMemcpyAsync(count_host, d, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RMW_CUDA(cudaFreeAsync(d, st));
+    RMW_CUDA(cudaStreamSynchronize(st));
+    return RMW_OK;
+}
+
+// Dense per-body wall mobility blocks (each body's 3n_b x 3n_b matrix, bodies
+// concatenated) - the matrices the preconditioner factorises.
+int rmw_rigid_body_mobility(void *sys, double *out)
+{
+    if (!sys || !out) return rmw::fail(RMW_ERR_ARG, "null argument");
+    RigidSystem *S = (RigidSystem *)sys;
+    rmw::body_mobility_kernel<<<S->nb, rmw::kRigidThreads, 0, S->st>>>(S->r, S->boff, S->moff, out, S->eta, S->a);
+    RMW_CHECK_LAUNCH("body mobility");
+    return RMW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,48 @@
+// Rigid multiblob bodies on the GPU: state of one suspension and its
+// operators (geometric matrix K, block-diagonal preconditioner, saddle-point
+// operator).  Used by the C ABI in rigid.cu and the Krylov solvers in krylov.cu.
+#pragma once
+#include <vector>
+
+#include "rmw_common.cuh"
+
+namespace rmw {
+
+struct RigidSystem {
+    int nb = 0;       // bodies
+    int n = 0;        // blobs
+    int max_m = 0;    // largest 3 * blobs-per-body
+    double eta = 1.0, a = 1.0;
+    double L[3] = {0, 0, 0};
+    cudaStream_t st = 0;
+    int device = 0;
+    std::vector<int> boff_h;       // nb+1 blob offsets (host copy)
+    std::vector<long long> moff_h; // nb+1 offsets of the per-body m x m matrices
+    // device arrays (owned)
+    int *boff = nullptr;           // nb+1
+    int *blob_body = nullptr;      // n
+    long long *moff = nullptr;     // nb+1
+    double *r = nullptr;           // 3n blob positions
+    double *xb = nullptr;          // 3nb body locations
+    double *minv = nullptr;        // sum m^2 : inverse blob mobility per body
+    double *minvK = nullptr;       // sum 6m  : M^-1 K per body (row-major m x 6)
+    double *nmat = nullptr;        // 36 nb   : N = (K^T M^-1 K)^-1
+    double *lfac = nullptr;        // sum m^2 : Cholesky factor L (lower), stochastic PC only
+    double *linv = nullptr;        // sum m^2 : L^-1 (lower), stochastic PC only
+    int *dstatus = nullptr;        // device status word
+    double *tmp3n = nullptr;       // 3n scratch vector
+    bool pc_ready = false, stoch_ready = false;
+
+    long long sys_size() const { return 3LL * n + 6LL * nb; }
+};
+
+// y = A x with A = [[M, -K], [-K^T, 0]] (multi_bodies.py:424-471); mode = RMW_MODE_*.
+int rigid_apply(RigidSystem &S, const double *x, double *y, int mode);
+// y = P^-1 x (block-diagonal preconditioner, multi_bodies.py:825-861).
+int rigid_apply_pc(RigidSystem &S, const double *x, double *y);
+// y = L^-1 M L^-T w on the blob space (det_stoch mobility_pc, multi_bodies.py:591-606).
+int rigid_mobility_pc(RigidSystem &S, const double *w, double *y, int mode);
+// y = L w (det_stoch P_inv_mult, multi_bodies.py:609-615).
+int rigid_P_inv_mult(RigidSystem &S, const double *w, double *y);
+
+}  // namespace rmw

@@ -181,7 +181,24 @@ def make_rigid(s42, s12):
         z = rng.standard_normal(3 * Nblobs)
         noise, lit = sf.stochastic_forcing_lanczos(factor=np.sqrt(2.0 * 1.0 / 1e-3), tolerance=1e-3,
                                                    dim=3 * Nblobs, mobility_mult=mob_pc, L_mult=P_inv, z=z)
+        # One Euler-Maruyama step with that noise, as stochastic_EM does
+        # (quaternion_integrator_multi_bodies.py:262-322): RHS = [-noise; -FT]
+        # scaled to norm 1, GMRES with the deterministic PC, then x += U dt and
+        # q <- from_rotation(w dt) * q.
+        dt = 1e-3
+        RHS2 = np.concatenate([-noise, -FT.flatten()])
+        n2 = np.linalg.norm(RHS2)
+        sol2, info2 = utils.gmres(A, RHS2 / n2, tol=1e-8, M=spla.LinearOperator((size, size), matvec=PC2,
+                                                                                dtype="float64"),
+                                  maxiter=1000, restart=60)
+        sol2 = sol2 * n2
+        vel = sol2[3 * Nblobs:]
+        new_locs = np.array([locs[k] + vel[6 * k:6 * k + 3] * dt for k in range(nb)])
+        new_quats = np.array([(Q.from_rotation(vel[6 * k + 3:6 * k + 6] * dt) * Q(quats[k])).entries
+                              for k in range(nb)])
         p = name + "_"
+        out.update({p + "bd_dt": np.array([dt]), p + "bd_sol": sol2, p + "bd_locs": new_locs,
+                    p + "bd_quats": new_quats, p + "bd_info": np.array([info2])})
         out.update({p + "ref_cfg": ref_cfg, p + "locs": locs, p + "quats": quats, p + "params": np.array([a, eta]),
                     p + "r": r, p + "K": np.array(K_bodies), p + "x": x, p + "Ax": Ax, p + "Px": Px,
                     p + "FT": FT, p + "sol": sol, p + "info": np.array([info, it[0]]), p + "true_res": np.array([true_res]),

@@ -1,11 +1,16 @@
 """Benchmark: wall-RPY M.F throughput (Gpairs/s) on one GB300.
 
-Workload (one "step"): one wall-corrected RPY product u = M_UF F in FP64 over
-the 256-shell suspension (256 bodies x 42 blobs = 10,752 blobs, a = 0.2436,
+Workload (one "step"): one wall-corrected RPY product u = M_UF F, FP64-accurate,
+over the 256-shell suspension (256 bodies x 42 blobs = 10,752 blobs, a = 0.2436,
 x,y ~ U[0,60R], z ~ U[1.2R,5R], forces N(0,1), seed 1), with the inputs
 resident in HBM.  One step evaluates N^2 = 1.156e8 ordered pairs.  Inputs are
 far smaller than L2, so a 512 MB buffer is written between timed steps to
 flush L2.
+
+The headline runs the df64 mode: double-float pair arithmetic on the FP32 pipe
+with FP64 accumulation, tested to <= 1e-12 relative error against the FP64
+oracle (the FP64-mode bar).  GB300's FP64 pipe runs at 1/74 of its FP32 pipe,
+so the native-FP64 kernel (reported under "products" as uf_fp64) is 6x slower.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -28,7 +33,13 @@ sys.path.insert(0, ROOT)
 
 FLOPS_PER_PAIR = {"uf": 200.0, "ut": 115.0, "wf": 115.0, "wt": 125.0}  # counted from the reference source
 METRIC = "wall-RPY M.F Gpairs/s"
-WORKLOAD = "wall-RPY M_UF.F, 256 shells x 42 blobs = 10,752 blobs (FP64)"
+HEAD_MODE = "df64"
+WORKLOAD = "wall-RPY M_UF.F, 256 shells x 42 blobs = 10,752 blobs (FP64-accurate: df64, <= 1e-12 vs FP64)"
+# FP32-pipe (FMA-pipe) thread instructions per pair of the df64 pair kernels,
+# from the ncu capture summarised in profiles/wall_pair_df64_uf_shells42x256.md
+# (sm__inst_executed_pipe_fma.sum * 32 / pairs); None until measured.
+DF64_FMA_PIPE_INST_PER_PAIR = {"uf": None}
+DF64_TRAFFIC_BYTES_PER_LAUNCH = None  # dram__bytes_read.sum + dram__bytes_write.sum, same capture
 
 
 def parse():
@@ -188,6 +199,66 @@ def time_product(kind, mode, rt, ft, out_fn, eta, a, steps, flush, stream):
     return {"ms": ms, "gpairs": n * n / (ms * 1e-3) / 1e9, "pair_kernel_ms": pair_ms / max(launches, 1)}
 
 
+def solver_metrics(dev, reps=2):
+    """Secondary: the 256-shell mobility solve (GMRES + block-diagonal PC to a
+    1e-8 relative residual) in FP64 and mixed precision, and one Brownian
+    Euler-Maruyama step of 1024 12-blob shells (Lanczos 1e-3 + GMRES 1e-8)."""
+    import torch
+    from rigidmultiblobswall_gb300 import integrator
+    from rigidmultiblobswall_gb300 import suspensions as S
+    from rigidmultiblobswall_gb300.rigid import RigidSystem
+    out = {}
+    s2 = S.shells_42_256()
+    sys2 = RigidSystem([42] * s2.n_bodies, s2.eta, s2.a, device=dev)
+    sys2.set_configuration(s2.r_vectors(), s2.locations)
+    FT = np.zeros((s2.n_bodies, 6))
+    FT[:, 2] = -1.0
+    sols = {}
+    for mode in ("fp64", "mixed"):
+        best = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sys2.build_pc()
+            sol, info, its, rr = integrator.solve_mobility_problem(sys2, FT, tol=1e-8, mode=mode)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        sols[mode] = sol[3 * sys2.n_blobs:].cpu().numpy()
+        out["solve_shells42x256_%s" % mode] = {"ms": best * 1e3, "iterations": its, "relres_fp64": rr, "info": info}
+    u64, u32 = sols["fp64"], sols["mixed"]
+    out["solve_shells42x256_mixed"]["velocity_rel_err_vs_fp64"] = float(np.linalg.norm(u32 - u64) /
+                                                                        np.linalg.norm(u64))
+    out["solve_shells42x256_speedup_mixed"] = out["solve_shells42x256_fp64"]["ms"] / \
+        out["solve_shells42x256_mixed"]["ms"]
+    # Brownian step, 1024 shells x 12 blobs
+    s3 = S.shells_12_1024()
+    sys3 = RigidSystem([12] * s3.n_bodies, s3.eta, s3.a, device=dev)
+    FT3 = np.zeros((s3.n_bodies, 6))
+    FT3[:, 2] = -1.0
+    z = torch.randn(3 * s3.n_blobs, generator=torch.Generator(device=dev).manual_seed(3), dtype=torch.float64,
+                    device=dev)
+    vel = {}
+    for mode in ("fp64", "mixed"):
+        best = None
+        for _ in range(reps):
+            st = integrator.BrownianStepper(sys3, s3.locations, s3.quaternions,
+                                            np.tile(s3.shell, (s3.n_bodies, 1)), kT=1.0, mode=mode)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = st.step(1e-3, FT3, z=z)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        vel[mode] = res["velocities"].cpu().numpy()
+        out["bd_step_shells12x1024_%s" % mode] = {"ms": best * 1e3, "lanczos_iterations": res["lanczos_iterations"],
+                                                  "gmres_iterations": res["gmres_iterations"],
+                                                  "relres_fp64": res["relres"]}
+    out["bd_step_shells12x1024_mixed"]["velocity_rel_err_vs_fp64"] = float(
+        np.linalg.norm(vel["mixed"] - vel["fp64"]) / np.linalg.norm(vel["fp64"]))
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -215,7 +286,7 @@ def main():
 
     # ---- warm-up
     for _ in range(args.warmup):
-        mb.wall_product("uf", rt, ft, eta, a)
+        mb.wall_product("uf", rt, ft, eta, a, mode=HEAD_MODE)
     torch.cuda.synchronize()
     if ws > 1:
         dist.barrier()
@@ -235,7 +306,7 @@ def main():
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        out = mb.wall_product("uf", rt, ft, eta, a)
+        out = mb.wall_product("uf", rt, ft, eta, a, mode=HEAD_MODE)
         e1.record(stream)
         evs.append((e0, e1))
     torch.cuda.synchronize()
@@ -253,26 +324,32 @@ def main():
     ms_per_step = step_ms / args.steps
     value = ws * args.steps * n * n / (step_ms * 1e-3) / 1e9
 
-    # ---- roofline of the dominant kernel (the pair kernel; bound by the FP64 pipe)
+    # ---- roofline of the dominant kernel (the df64 pair kernel; bound by the FP32/FMA pipe)
     pair_ms = pair_ms_total / max(pair_launches, 1)
-    achieved = n * n * FLOPS_PER_PAIR["uf"] / (pair_ms * 1e-3) / 1e12
-    roofline = {"bound": "fp64-pipe", "achieved": achieved, "peak": peak64 / 1e12, "unit": "TFLOP/s",
-                "frac": achieved / (peak64 / 1e12), "traffic": None,
-                "peak_source": "measured by rmw_fma_peak (FP64 FMA chains on all SMs) in this run",
-                "pair_kernel_ms": pair_ms, "flops_per_pair": FLOPS_PER_PAIR["uf"]}
+    alg_tflops = n * n * FLOPS_PER_PAIR["uf"] / (pair_ms * 1e-3) / 1e12
+    ipp = DF64_FMA_PIPE_INST_PER_PAIR["uf"]
+    peak_inst = peak32 / 2.0  # FMA-pipe thread instructions per second (one FFMA = 2 flops)
+    roofline = {"bound": "fp32-pipe", "unit": "Tinst/s", "peak": peak_inst / 1e12,
+                "achieved": (n * n * ipp / (pair_ms * 1e-3) / 1e12) if ipp else None,
+                "frac": (n * n * ipp / (pair_ms * 1e-3) / peak_inst) if ipp else None,
+                "traffic": DF64_TRAFFIC_BYTES_PER_LAUNCH,
+                "peak_source": "measured by rmw_fma_peak (FP32 FMA chains on all SMs) in this run, / 2 per FFMA",
+                "pair_kernel_ms": pair_ms, "fma_pipe_inst_per_pair": ipp,
+                "algorithmic_tflops_fp64_equivalent": alg_tflops, "flops_per_pair": FLOPS_PER_PAIR["uf"],
+                "algorithmic_vs_measured_fp64_peak": alg_tflops / (peak64 / 1e12)}
 
     # ---- e2e through the public host-buffer API (copies inside the timed region)
     rp = torch.empty(r.shape, dtype=torch.float64).pin_memory().numpy()
     fp = torch.empty(f.shape, dtype=torch.float64).pin_memory().numpy()
     rp[:] = r
     fp[:] = f
-    mb.single_wall_mobility_trans_times_force_pycuda(rp, fp, eta, a)
+    mb.single_wall_mobility_trans_times_force_pycuda(rp, fp, eta, a, mode=HEAD_MODE)
     e2e_t = []
     for _ in range(args.steps):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        u = mb.single_wall_mobility_trans_times_force_pycuda(rp, fp, eta, a)
+        u = mb.single_wall_mobility_trans_times_force_pycuda(rp, fp, eta, a, mode=HEAD_MODE)
         e2e_t.append(time.perf_counter() - t0)
     e2e = {"value": n * n / float(np.mean(e2e_t)) / 1e9, "unit": "Gpairs/s",
            "h2d_bytes_per_step": int(rp.nbytes + fp.nbytes), "d2h_bytes_per_step": int(u.nbytes)}
@@ -280,11 +357,17 @@ def main():
     # ---- secondary: every product in both precisions (same workload)
     products = {}
     for kind in (() if args.no_extras else ("uf", "ut", "wf", "wt")):
-        for mode in ("fp64", "mixed"):
+        for mode in ("fp64", "df64", "mixed"):
             res = time_product(kind, mode, rt, ft, None, eta, a, max(3, args.steps // 4), flush, stream)
-            peak = peak64 if mode == "fp64" else peak32
-            res["pipe_frac"] = n * n * FLOPS_PER_PAIR[kind] / (res["pair_kernel_ms"] * 1e-3) / peak
+            peak = peak64 if mode in ("fp64", "df64") else peak32
+            # algorithmic (reference) flops per second over the pipe peak of the mode's arithmetic
+            # class; for df64 this is FP64-equivalent work over the FP64 peak (> 1 = faster than the
+            # FP64 pipe could do it)
+            res["alg_tflops"] = n * n * FLOPS_PER_PAIR[kind] / (res["pair_kernel_ms"] * 1e-3) / 1e12
+            res["alg_frac_of_mode_peak"] = res["alg_tflops"] * 1e12 / peak
             products["%s_%s" % (kind, mode)] = {k: round(v, 6) for k, v in res.items()}
+
+    solver = {} if args.no_extras else solver_metrics(dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -293,14 +376,14 @@ def main():
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-                "config": {"workload": WORKLOAD, "n_blobs": n, "pairs_per_step": n * n, "eta": eta, "a": a,
+                "scaling": "weak", "vs_baseline": None, "dtype": "df64 (f64-accurate)", "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD, "mode": HEAD_MODE, "n_blobs": n, "pairs_per_step": n * n, "eta": eta, "a": a,
                            "l2": "512 MB buffer written between timed steps (inputs 0.5 MB < L2)",
                            "parallelism": "replicas" if ws > 1 else "single GPU"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
                 "gpu_launches": 3 * args.steps, "wall_s_timed_region": t_wall,
                 "fp32_fma_peak_tflops": peak32 / 1e12, "fp64_fma_peak_tflops": peak64 / 1e12,
-                "products": products}
+                "products": products, "solver": solver}
         print(json.dumps(line))
     if ws > 1:
         dist.destroy_process_group()

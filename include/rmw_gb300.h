@@ -35,7 +35,11 @@ extern "C" {
 /* ---- precision modes ------------------------------------------------- */
 #define RMW_MODE_FP64 0  /* every pair in FP64 */
 #define RMW_MODE_MIXED 1 /* FP32 pair evaluation (double-float positions),
-                            compensated per-target accumulation, FP64 output */
+                            compensated per-target accumulation, FP64 output;
+                            relative error <= 1e-6 against FP64 */
+#define RMW_MODE_DF64 2  /* double-float (hi+lo FP32 pairs, ~48-bit) pair
+                            evaluation on the FP32 pipe with FP64 accumulation;
+                            relative error <= 1e-12 against FP64 */
 
 /* ---- product kinds ---------------------------------------------------- */
 #define RMW_UF 0 /* u = M_UF f  (1/(8 pi eta a))   */
@@ -140,8 +144,10 @@ int rmw_count_below(const double *r, int64_t n, double zmin, int *count_host, vo
  * block-diagonal preconditioner (zero initial guess), stopping when the true
  * residual |b - A x| <= tol |b|: utils.gmres as called by
  * solve_mobility_problem (general_application_utils.py:514-635,
- * quaternion_integrator_multi_bodies.py:1441-1547).  mode RMW_MODE_MIXED runs
- * the inner GMRES on the FP32-pair operator inside FP64 iterative refinement.
+ * quaternion_integrator_multi_bodies.py:1441-1547).  mode RMW_MODE_FP64 or
+ * RMW_MODE_DF64 selects the operator's pair arithmetic; RMW_MODE_MIXED runs the
+ * inner GMRES on the FP32-pair operator inside iterative refinement whose
+ * residual uses the FP64-accurate double-float operator.
  * Synchronous.  Returns RMW_ERR_NOT_CONVERGED after maxiter iterations (the
  * best iterate is still written to sol). */
 int rmw_rigid_solve(void *handle, const double *rhs, double *sol, double tol, int restart, int maxiter, int mode,

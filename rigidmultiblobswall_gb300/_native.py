@@ -18,6 +18,7 @@ RMW_ERR_ALLOC = 6
 
 MODE_FP64 = 0
 MODE_MIXED = 1
+MODE_DF64 = 2
 KINDS = {"uf": 0, "ut": 1, "wf": 2, "wt": 3}
 
 _lib = None

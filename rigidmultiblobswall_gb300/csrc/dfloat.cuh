@@ -1,0 +1,106 @@
+// Double-float ("df64") arithmetic on the FP32 pipe: a value is hi + lo with
+// |lo| <= ulp(hi)/2, about 48 significant bits.  Built from the error-free
+// transformations TwoSum (Knuth), FastTwoSum (Dekker) and the FMA-based exact
+// product; additions use the cheap ("sloppy") variant, whose error is bounded
+// by ~2^-47 (|a| + |b|) - the same form as an FP64 addition, 30x looser.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace rmw {
+
+struct df {
+    float hi, lo;
+};
+
+__device__ __forceinline__ df df_from(float h) { return {h, 0.0f}; }
+
+__device__ __forceinline__ df fast_two_sum(float a, float b)
+{
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+
+__device__ __forceinline__ df two_sum_df(float a, float b)
+{
+    const float s = a + b;
+    const float bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+
+__device__ __forceinline__ df operator+(df a, df b)
+{
+    const df s = two_sum_df(a.hi, b.hi);
+    return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+}
+__device__ __forceinline__ df operator+(df a, float b)
+{
+    const df s = two_sum_df(a.hi, b);
+    return fast_two_sum(s.hi, s.lo + a.lo);
+}
+__device__ __forceinline__ df operator+(float a, df b) { return b + a; }
+__device__ __forceinline__ df operator-(df a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ df operator-(df a, df b) { return a + (-b); }
+__device__ __forceinline__ df operator-(df a, float b) { return a + (-b); }
+__device__ __forceinline__ df operator-(float a, df b) { return (-b) + a; }
+
+__device__ __forceinline__ df operator*(df a, df b)
+{
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ df operator*(df a, float b)
+{
+    const float p = a.hi * b;
+    float e = fmaf(a.hi, b, -p);
+    e = fmaf(a.lo, b, e);
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ df operator*(float a, df b) { return b * a; }
+
+// exact scaling by a power of two
+__device__ __forceinline__ df scale2(df a, float p2) { return {a.hi * p2, a.lo * p2}; }
+
+__device__ __forceinline__ df sqr(df a)
+{
+    const float p = a.hi * a.hi;
+    float e = fmaf(a.hi, a.hi, -p);
+    e = fmaf(2.0f * a.hi, a.lo, e);
+    return fast_two_sum(p, e);
+}
+
+// exact product of two floats
+__device__ __forceinline__ df two_prod(float a, float b)
+{
+    const float p = a * b;
+    return {p, fmaf(a, b, -p)};
+}
+
+// 1/sqrt(x): hardware estimate, one FP32 Newton step (to ~1 ulp of float),
+// then one Newton step in double-float: y1 = y + y (1 - x y^2) / 2, where the
+// residual 1 - x y^2 is formed in double-float and the (tiny) correction in
+// FP32.  Relative error ~ 1.5 * (2^-24)^2 + 2^-47.
+__device__ __forceinline__ df rsqrt_df(df x)
+{
+    float y = rsqrtf(x.hi);
+    y = y * fmaf(-0.5f * x.hi, y * y, 1.5f);
+    const df t = x * two_prod(y, y);
+    const float e = (1.0f - t.hi) - t.lo;
+    return fast_two_sum(y, 0.5f * y * e);
+}
+
+__device__ __forceinline__ bool operator>(df a, float b) { return a.hi > b || (a.hi == b && a.lo > 0.0f); }
+__device__ __forceinline__ bool operator>=(df a, float b) { return a.hi > b || (a.hi == b && a.lo >= 0.0f); }
+
+__device__ __forceinline__ double to_double(df a) { return (double)a.hi + (double)a.lo; }
+
+// double -> double-float (round hi, exact remainder in lo)
+__device__ __forceinline__ df df_of_double(double d)
+{
+    const float h = (float)d;
+    return {h, (float)(d - (double)h)};
+}
+
+}  // namespace rmw

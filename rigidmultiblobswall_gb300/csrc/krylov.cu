@@ -568,18 +568,20 @@ int rmw_rigid_solve(void *sys, const double *rhs, double *sol, double tol, int r
 {
     if (!sys || !rhs || !sol) return rmw::fail(RMW_ERR_ARG, "null argument");
     if (!(tol > 0)) return rmw::fail(RMW_ERR_ARG, "tolerance must be positive");
-    if (mode != RMW_MODE_FP64 && mode != RMW_MODE_MIXED) return rmw::fail(RMW_ERR_ARG, "unknown precision mode");
+    if (mode != RMW_MODE_FP64 && mode != RMW_MODE_MIXED && mode != RMW_MODE_DF64)
+        return rmw::fail(RMW_ERR_ARG, "unknown precision mode");
     RigidSystem &S = *(RigidSystem *)sys;
     if (!S.pc_ready) {
         if (int rc = rmw_rigid_build_pc(sys, 0)) return rc;
     }
     const long long n = S.sys_size();
     auto pc = [&](const double *x, double *y) { return rmw::rigid_apply_pc(S, x, y); };
-    if (mode == RMW_MODE_FP64) {
-        auto op = [&](const double *x, double *y) { return rmw::rigid_apply(S, x, y, RMW_MODE_FP64); };
+    if (mode == RMW_MODE_FP64 || mode == RMW_MODE_DF64) {
+        auto op = [&](const double *x, double *y) { return rmw::rigid_apply(S, x, y, mode); };
         return rmw::gmres_right(op, pc, rhs, sol, n, tol, restart, maxiter, S.st, iters_host, relres_host, nullptr);
     }
-    // mixed: inner GMRES on the FP32-pair operator, FP64 residual refinement
+    // mixed: inner GMRES on the FP32-pair operator; the refinement residual
+    // b - A x uses the FP64-accurate double-float operator (<= 1e-12 against FP64)
     auto op32 = [&](const double *x, double *y) { return rmw::rigid_apply(S, x, y, RMW_MODE_MIXED); };
     double *buf = nullptr;  // x, r, d
     RMW_CUDA(cudaMallocAsync(&buf, sizeof(double) * 3 * n, S.st));
@@ -627,8 +629,8 @@ int rmw_rigid_solve(void *sys, const double *rhs, double *sol, double tol, int r
         total += it;
         if (rc != RMW_OK && rc != RMW_ERR_NOT_CONVERGED) return rc;
         rmw::axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S.st>>>(d, x, n, 1.0, 1.0);
-        // r = b - A64 x
-        if (int rc2 = rmw::rigid_apply(S, x, r, RMW_MODE_FP64)) return rc2;
+        // r = b - A x with the FP64-accurate operator
+        if (int rc2 = rmw::rigid_apply(S, x, r, RMW_MODE_DF64)) return rc2;
         rmw::axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S.st>>>(rhs, r, n, 1.0, -1.0);
         if (total >= maxiter) {
             if (int rc3 = norm(r, &rnorm)) return rc3;

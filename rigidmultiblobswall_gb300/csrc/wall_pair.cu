@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "pair_math.cuh"
+#include "pair_math_df.cuh"
 #include "rmw_common.cuh"
 #include "wall_pair.cuh"
 
@@ -47,6 +48,13 @@ struct __align__(16) SrcF {
     float4 hi;  // x/a, y/a, z_eff/a (rounded to float), unused
     float4 lo;  // residuals x/a - hi.x, ...
     float4 v;   // b*v
+};
+
+struct __align__(16) SrcDF {
+    float4 hi;   // x/a, y/a, z_eff/a : high floats
+    float4 lo;   //                     low floats
+    float4 vhi;  // b*v : high floats
+    float4 vlo;  //       low floats
 };
 
 struct Periodic {
@@ -85,6 +93,100 @@ __global__ void pack_mixed_kernel(const double *__restrict__ r, const double *__
     s.lo = make_float4((float)(xs - (double)xh), (float)(ys - (double)yh), (float)(zs - (double)zh), 0.f);
     s.v = make_float4((float)(b * v[3 * i]), (float)(b * v[3 * i + 1]), (float)(b * v[3 * i + 2]), 0.f);
     src[i] = s;
+}
+
+__global__ void pack_df_kernel(const double *__restrict__ r, const double *__restrict__ v, SrcDF *__restrict__ src,
+                               int n, double a)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double inva = 1.0 / a;
+    const double z = r[3 * i + 2];
+    const double b = (z < a) ? z / a : 1.0;
+    const double ze = (z <= a) ? a : z;
+    const df x = df_of_double(r[3 * i] * inva), y = df_of_double(r[3 * i + 1] * inva), zz = df_of_double(ze * inva);
+    const df vx = df_of_double(b * v[3 * i]), vy = df_of_double(b * v[3 * i + 1]), vz = df_of_double(b * v[3 * i + 2]);
+    SrcDF s;
+    s.hi = make_float4(x.hi, y.hi, zz.hi, 0.f);
+    s.lo = make_float4(x.lo, y.lo, zz.lo, 0.f);
+    s.vhi = make_float4(vx.hi, vy.hi, vz.hi, 0.f);
+    s.vlo = make_float4(vx.lo, vy.lo, vz.lo, 0.f);
+    src[i] = s;
+}
+
+// ---------------------------------------------------------------------------
+// df64 pair kernel: double-float pair evaluation on the FP32 pipe; the
+// double-float sum over each group of kDfGroup sources is folded into FP64
+// accumulators (FP64 pipe, a few adds per group).
+constexpr int kDfGroup = 32;
+
+template <int KIND, bool PER>
+__global__ void __launch_bounds__(kThreads) wall_pair_df_kernel(const SrcDF *__restrict__ src, int n, int chunk,
+                                                                 Periodic P, double *__restrict__ partial)
+{
+    __shared__ SrcDF tile[kTile];
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    const int j0 = blockIdx.y * chunk;
+    const int j1 = min(n, j0 + chunk);
+    float4 mh = make_float4(0.f, 0.f, 1.f, 0.f), ml = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (i < n) { mh = src[i].hi; ml = src[i].lo; }
+    const df xi = {mh.x, ml.x}, yi = {mh.y, ml.y}, zi = {mh.z, ml.z};
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int t0 = j0; t0 < j1; t0 += kTile) {
+        const int cnt = min(kTile, j1 - t0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt; k += kThreads) tile[k] = src[t0 + k];
+        __syncthreads();
+        for (int g0 = 0; g0 < cnt; g0 += kDfGroup) {
+            const int g1 = min(cnt, g0 + kDfGroup);
+            df ux = df_from(0.f), uy = df_from(0.f), uz = df_from(0.f);
+            for (int k = g0; k < g1; ++k) {
+                const float4 sh = tile[k].hi, sl = tile[k].lo, svh = tile[k].vhi, svl = tile[k].vlo;
+                const int j = t0 + k;
+                const df xj = {sh.x, sl.x}, yj = {sh.y, sl.y}, zj = {sh.z, sl.z};
+                const df vx = {svh.x, svl.x}, vy = {svh.y, svl.y}, vz = {svh.z, svl.z};
+                const df dz = zi - zj;
+                const df Rz = zi + zj;
+                if (!PER) {
+                    df cx = df_from(0.f), cy = df_from(0.f), cz = df_from(0.f);
+                    pair_contrib_df<KIND>(xi - xj, yi - yj, dz, Rz, zi, zj, vx, vy, vz, cx, cy, cz);
+                    if (j != i) {
+                        ux = ux + cx;
+                        uy = uy + cy;
+                        uz = uz + cz;
+                    }
+                } else {
+                    // minimum image in FP64 (rare path), then back to double-float
+                    double rx = to_double(xi - xj), ry = to_double(yi - yj), rz = to_double(dz);
+                    if (P.Lx > 0) rx = project(rx, P.Lx);
+                    if (P.Ly > 0) ry = project(ry, P.Ly);
+                    if (P.Lz > 0) rz = project(rz, P.Lz);
+                    const int px = P.Lx > 0, py = P.Ly > 0, pz = P.Lz > 0;
+                    for (int bx = -px; bx <= px; ++bx)
+                        for (int by = -py; by <= py; ++by)
+                            for (int bz = -pz; bz <= pz; ++bz) {
+                                df cx = df_from(0.f), cy = df_from(0.f), cz = df_from(0.f);
+                                pair_contrib_df<KIND>(df_of_double(rx + bx * P.Lx), df_of_double(ry + by * P.Ly),
+                                                      df_of_double(rz + bz * P.Lz), Rz, zi, zj, vx, vy, vz, cx,
+                                                      cy, cz);
+                                const bool self = (j == i) && bx == 0 && by == 0 && bz == 0;
+                                if (!self) {
+                                    ux = ux + cx;
+                                    uy = uy + cy;
+                                    uz = uz + cz;
+                                }
+                            }
+                }
+            }
+            ax += to_double(ux);
+            ay += to_double(uy);
+            az += to_double(uz);
+        }
+    }
+    if (i < n) {
+        double *o = partial + (size_t)blockIdx.y * 3 * n + 3 * (size_t)i;
+        o[0] = ax; o[1] = ay; o[2] = az;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -266,7 +368,7 @@ int wall_default_chunks(int n) { return choose_chunks(n); }
 
 size_t wall_scratch_bytes(int n, int mode, int nchunks)
 {
-    size_t rec = (mode == RMW_MODE_FP64) ? sizeof(SrcD) : sizeof(SrcF);
+    size_t rec = (mode == RMW_MODE_FP64) ? sizeof(SrcD) : (mode == RMW_MODE_DF64 ? sizeof(SrcDF) : sizeof(SrcF));
     size_t packed = ((rec * (size_t)n + 255) / 256) * 256;
     return packed + sizeof(double) * 3 * (size_t)n * (size_t)nchunks;
 }
@@ -281,7 +383,7 @@ static int launch_kind(const double *r, const double *v, double *out, int n, dou
                                          : 1.0 / (8.0 * kPi * eta * a * a);
     const bool per = L && (L[0] > 0 || L[1] > 0 || L[2] > 0);
     Periodic P{L ? L[0] : 0.0, L ? L[1] : 0.0, L ? L[2] : 0.0};
-    size_t rec = (mode == RMW_MODE_FP64) ? sizeof(SrcD) : sizeof(SrcF);
+    size_t rec = (mode == RMW_MODE_FP64) ? sizeof(SrcD) : (mode == RMW_MODE_DF64 ? sizeof(SrcDF) : sizeof(SrcF));
     size_t packed = ((rec * (size_t)n + 255) / 256) * 256;
     char *base = (char *)scratch_ptr;
     double *partial = (double *)(base + packed);
@@ -295,6 +397,13 @@ static int launch_kind(const double *r, const double *v, double *out, int n, dou
         if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
         if (per) wall_pair_fp64_kernel<KIND, true><<<grid, kThreads, 0, st>>>(src, n, chunk, inva, P, partial);
         else wall_pair_fp64_kernel<KIND, false><<<grid, kThreads, 0, st>>>(src, n, chunk, inva, P, partial);
+    } else if (mode == RMW_MODE_DF64) {
+        SrcDF *src = (SrcDF *)base;
+        pack_df_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
+        Periodic Ps{P.Lx * inva, P.Ly * inva, P.Lz * inva};
+        if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
+        if (per) wall_pair_df_kernel<KIND, true><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial);
+        else wall_pair_df_kernel<KIND, false><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial);
     } else {
         SrcF *src = (SrcF *)base;
         pack_mixed_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
@@ -313,7 +422,8 @@ int validate_product_args(int kind, const void *r, const void *v, const void *ou
                           int mode)
 {
     if (kind < RMW_UF || kind > RMW_WT) return fail(RMW_ERR_ARG, "unknown product kind");
-    if (mode != RMW_MODE_FP64 && mode != RMW_MODE_MIXED) return fail(RMW_ERR_ARG, "unknown precision mode");
+    if (mode != RMW_MODE_FP64 && mode != RMW_MODE_MIXED && mode != RMW_MODE_DF64)
+        return fail(RMW_ERR_ARG, "unknown precision mode");
     if (n < 0 || n > (int64_t(1) << 28)) return fail(RMW_ERR_ARG, "number of blobs out of range [0, 2^28]");
     if (n > 0 && (!r || !v || !out)) return fail(RMW_ERR_ARG, "null array pointer");
     if (!(a > 0) || !(eta > 0)) return fail(RMW_ERR_ARG, "blob radius and viscosity must be positive");

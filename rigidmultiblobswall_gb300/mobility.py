@@ -13,9 +13,12 @@ All products run on the GPU through librmw_gb300.so:
 * CUDA torch tensors stay on the device; the call is asynchronous on the current
   torch stream and returns a CUDA tensor.
 
-The extra keyword ``mode`` selects 'fp64' (default, every pair in FP64) or
-'mixed' (FP32 pair evaluation with double-float position differences and
-compensated accumulation; error <= 1e-6 relative to FP64).
+The extra keyword ``mode`` selects 'fp64' (default, every pair in FP64),
+'df64' (double-float pair arithmetic on the FP32 pipe with FP64 accumulation;
+error <= 1e-12 relative to FP64, several times faster on GB300, whose FP64
+rate is 1/64 of FP32) or 'mixed' (FP32 pair evaluation with double-float
+position differences and compensated accumulation; error <= 1e-6 relative to
+FP64).
 
 The ``_pycuda``, ``_numba`` and ``_cpp`` suffixes of the reference are all
 aliases of the GPU implementation, so ``set_mobility_vector_prod`` callers can
@@ -28,13 +31,13 @@ import scipy.sparse
 
 from . import _native
 
-_MODES = {"fp64": _native.MODE_FP64, "mixed": _native.MODE_MIXED}
+_MODES = {"fp64": _native.MODE_FP64, "mixed": _native.MODE_MIXED, "df64": _native.MODE_DF64}
 
 
 def _mode(kwargs):
     m = kwargs.get("mode", "fp64")
     if m not in _MODES:
-        raise ValueError("mode must be 'fp64' or 'mixed'")
+        raise ValueError("mode must be 'fp64', 'df64' or 'mixed'")
     return _MODES[m]
 
 

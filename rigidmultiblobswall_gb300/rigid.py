@@ -10,12 +10,12 @@ import numpy as np
 
 from . import _native
 
-MODES = {"fp64": _native.MODE_FP64, "mixed": _native.MODE_MIXED}
+MODES = {"fp64": _native.MODE_FP64, "mixed": _native.MODE_MIXED, "df64": _native.MODE_DF64}
 
 
 def _mode(mode):
     if mode not in MODES:
-        raise ValueError("mode must be 'fp64' or 'mixed'")
+        raise ValueError("mode must be 'fp64', 'df64' or 'mixed'")
     return MODES[mode]
 
 

@@ -17,7 +17,7 @@ from rigidmultiblobswall_gb300 import suspensions as S
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": 1e-12, "mixed": 1e-6}
+TOL = {"fp64": 1e-12, "df64": 1e-12, "mixed": 1e-6}
 CASES = ["far", "damped", "touching", "periodic", "single"]
 KINDS = ["uf", "ut", "wf", "wt"]
 FN = {
@@ -28,7 +28,7 @@ FN = {
 }
 
 
-@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+@pytest.mark.parametrize("mode", ["fp64", "df64", "mixed"])
 @pytest.mark.parametrize("case", CASES)
 @pytest.mark.parametrize("kind", KINDS)
 def test_products_match_reference_golden(cuda_device, kind, case, mode):
@@ -39,7 +39,7 @@ def test_products_match_reference_golden(cuda_device, kind, case, mode):
     assert rel_err(out, g[case + "_" + kind]) <= TOL[mode]
 
 
-@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+@pytest.mark.parametrize("mode", ["fp64", "df64", "mixed"])
 @pytest.mark.parametrize("kind", KINDS)
 def test_plain_matvec_workload_matches_oracle(cuda_device, kind, mode):
     r, f, eta, a = S.blobs_wall_matvec(2048, seed=0)
@@ -47,7 +47,7 @@ def test_plain_matvec_workload_matches_oracle(cuda_device, kind, mode):
     assert rel_err(FN[kind](r, f, eta, a, mode=mode), ref) <= TOL[mode]
 
 
-@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+@pytest.mark.parametrize("mode", ["fp64", "df64", "mixed"])
 @pytest.mark.parametrize("kind", KINDS)
 def test_shell_suspension_rows_match_oracle(cuda_device, kind, mode):
     """256 shells x 42 blobs (blobs below z=a present): 400 sampled target rows."""
@@ -96,7 +96,8 @@ def test_tile_tail_sizes(cuda_device):
     for n in (127, 128, 129, 255, 257, 1025):
         r, f, eta, a = S.blobs_wall_matvec(n, seed=n)
         for kind in ("uf", "wt"):
-            assert rel_err(FN[kind](r, f, eta, a), wall.wall_product(kind, r, f, eta, a)) <= 1e-12
+            for mode in ("fp64", "df64"):
+                assert rel_err(FN[kind](r, f, eta, a, mode=mode), wall.wall_product(kind, r, f, eta, a)) <= 1e-12
 
 
 def test_errors_raise(cuda_device):
@@ -106,6 +107,21 @@ def test_errors_raise(cuda_device):
         mb.single_wall_mobility_trans_times_force_pycuda(r, f, eta, -1.0)
     with pytest.raises(ValueError):
         mb.single_wall_mobility_trans_times_force_pycuda(r, f, eta, a, mode="fp16")
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_df64_large_suspension_rows(cuda_device, kind):
+    """df64 at 4096 shells x 42 blobs (172,032 blobs): 96 sampled rows against
+    the FP64 oracle at the FP64-mode bar (1e-12)."""
+    import torch
+    s = S.shells_42_4096()
+    r = s.r_vectors()
+    v = np.random.default_rng(13).standard_normal(r.shape)
+    out = mb.wall_product(kind, torch.tensor(r, device=cuda_device), torch.tensor(v, device=cuda_device), s.eta,
+                          s.a, mode="df64").cpu().numpy()
+    rows = np.random.default_rng(14).choice(s.n_blobs, 96, replace=False)
+    ref = wall.wall_product(kind, r, v, s.eta, s.a, rows=rows)
+    assert rel_err(out.reshape(-1, 3)[rows], ref) <= 1e-12
 
 
 def test_large_suspension_linearity_and_sampled_rows(cuda_device):

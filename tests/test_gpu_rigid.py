@@ -69,7 +69,7 @@ def test_body_mobility_blocks_match_oracle(cuda_device, c):
         assert rel_err(blocks[b].cpu().numpy(), ref) <= 1e-13
 
 
-@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+@pytest.mark.parametrize("mode", ["fp64", "df64", "mixed"])
 @pytest.mark.parametrize("c", CASES)
 def test_solve_matches_reference(cuda_device, c, mode):
     g = golden("rigid.npz")
@@ -152,13 +152,13 @@ def test_larger_suspension_matches_oracle(cuda_device):
     rhs = np.concatenate([np.zeros(3 * s.n_blobs), -FT.flatten()])
     xo, ito, relo = orc.gmres_right(o.apply, o.apply_pc, rhs / np.linalg.norm(rhs), tol=1e-8)
     xo *= np.linalg.norm(rhs)
-    for mode in ("fp64", "mixed"):
+    for mode in ("fp64", "df64", "mixed"):
         sol, info, its, rr = integrator.solve_mobility_problem(s, FT, tol=1e-8, mode=mode)
         sol = sol.cpu().numpy()
         assert info == 0
         assert np.linalg.norm(rhs - o.apply(sol)) <= 1.05e-8 * np.linalg.norm(rhs)
         assert rel_err(sol[3 * s.n_blobs:], xo[3 * s.n_blobs:]) <= 1e-6
-        if mode == "fp64":
+        if mode != "mixed":
             assert abs(its - ito) <= 2
 
 

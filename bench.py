@@ -35,11 +35,14 @@ FLOPS_PER_PAIR = {"uf": 200.0, "ut": 115.0, "wf": 115.0, "wt": 125.0}  # counted
 METRIC = "wall-RPY M.F Gpairs/s"
 HEAD_MODE = "df64"
 WORKLOAD = "wall-RPY M_UF.F, 256 shells x 42 blobs = 10,752 blobs (FP64-accurate: df64, <= 1e-12 vs FP64)"
-# FP32-pipe (FMA-pipe) thread instructions per pair of the df64 pair kernels,
-# from the ncu capture summarised in profiles/wall_pair_df64_uf_shells42x256.md
-# (sm__inst_executed_pipe_fma.sum * 32 / pairs); None until measured.
-DF64_FMA_PIPE_INST_PER_PAIR = {"uf": None}
-DF64_TRAFFIC_BYTES_PER_LAUNCH = None  # dram__bytes_read.sum + dram__bytes_write.sum, same capture
+# Issued thread instructions per pair of the df64 UF pair kernel (all pipes;
+# 85 % of them on the FMA pipe), from the ncu capture summarised in
+# profiles/wall_pair_df64_uf_shells42x256.md: smsp__inst_executed.sum * 32 / N^2
+# = 3,879,824,880 * 32 / 10752^2.  The FP32 pipe issues at most one thread
+# instruction per lane per clock, the rate the FMA-chain probe measures
+# (FLOP/s / 2), so achieved / peak is the fraction of issue capacity used.
+DF64_FMA_PIPE_INST_PER_PAIR = {"uf": 3879824880.0 * 32 / 10752 ** 2}
+DF64_TRAFFIC_BYTES_PER_LAUNCH = 710912  # dram__bytes_read.sum + dram__bytes_write.sum, same capture
 
 
 def parse():
@@ -329,7 +332,7 @@ def main():
     alg_tflops = n * n * FLOPS_PER_PAIR["uf"] / (pair_ms * 1e-3) / 1e12
     ipp = DF64_FMA_PIPE_INST_PER_PAIR["uf"]
     peak_inst = peak32 / 2.0  # FMA-pipe thread instructions per second (one FFMA = 2 flops)
-    roofline = {"bound": "fp32-pipe", "unit": "Tinst/s", "peak": peak_inst / 1e12,
+    roofline = {"bound": "fp32-pipe (issue)", "unit": "Tinst/s", "peak": peak_inst / 1e12,
                 "achieved": (n * n * ipp / (pair_ms * 1e-3) / 1e12) if ipp else None,
                 "frac": (n * n * ipp / (pair_ms * 1e-3) / peak_inst) if ipp else None,
                 "traffic": DF64_TRAFFIC_BYTES_PER_LAUNCH,

@@ -67,6 +67,22 @@ struct TraceRec {
 std::mutex g_trace_mu;
 bool g_trace = false;
 std::vector<TraceRec> g_trace_recs;
+std::vector<cudaEvent_t> g_event_pool;  // reused events: no event creation on the launch path
+
+cudaError_t pooled_event(cudaEvent_t *e)
+{
+    if (g_event_pool.empty()) {
+        for (int k = 0; k < 64; ++k) {
+            cudaEvent_t x;
+            cudaError_t rc = cudaEventCreate(&x);
+            if (rc != cudaSuccess) return rc;
+            g_event_pool.push_back(x);
+        }
+    }
+    *e = g_event_pool.back();
+    g_event_pool.pop_back();
+    return cudaSuccess;
+}
 }  // namespace
 
 bool trace_on() { return g_trace; }
@@ -76,8 +92,11 @@ int trace_begin(TraceKernel k, cudaStream_t st, void **token)
     *token = nullptr;
     if (!g_trace) return RMW_OK;
     TraceRec *r = new TraceRec{(int)k, nullptr, nullptr};
-    RMW_CUDA(cudaEventCreate(&r->e0));
-    RMW_CUDA(cudaEventCreate(&r->e1));
+    {
+        std::lock_guard<std::mutex> lock(g_trace_mu);
+        RMW_CUDA(pooled_event(&r->e0));
+        RMW_CUDA(pooled_event(&r->e1));
+    }
     RMW_CUDA(cudaEventRecord(r->e0, st));
     *token = r;
     return RMW_OK;
@@ -123,8 +142,8 @@ int rmw_trace_read(int kind, double *total_ms_host, int64_t *launches_host, int 
     *launches_host = cnt;
     if (reset) {
         for (auto &r : rmw::g_trace_recs) {
-            cudaEventDestroy(r.e0);
-            cudaEventDestroy(r.e1);
+            rmw::g_event_pool.push_back(r.e0);
+            rmw::g_event_pool.push_back(r.e1);
         }
         rmw::g_trace_recs.clear();
     }

@@ -54,6 +54,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true", help="skip the per-product secondary timings")
     p.add_argument("--cpu-seconds", type=float, default=8.0)
+    p.add_argument("--large", action="store_true",
+                   help="only run the 4096-shell (172,032-blob) solve comparison and print its JSON line")
+    p.add_argument("--large-modes", default="mixed,df64,fp64")
     return p.parse_args()
 
 
@@ -262,8 +265,56 @@ def solver_metrics(dev, reps=2):
     return out
 
 
+def large_solve(args):
+    """4096 42-blob shells at area fraction 0.3, force (0,0,-1) per body: block-diagonal preconditioned GMRES
+    to a 1e-8 relative residual in each precision mode, on one GPU.  The plain FP64 solve is the baseline
+    the mixed-precision solve is compared against."""
+    import torch
+    from rigidmultiblobswall_gb300 import build as B
+    from rigidmultiblobswall_gb300 import integrator
+    from rigidmultiblobswall_gb300 import suspensions as S
+    from rigidmultiblobswall_gb300.rigid import RigidSystem
+    B.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    s5 = S.shells_42_4096()
+    sys5 = RigidSystem([42] * s5.n_bodies, s5.eta, s5.a, device=dev)
+    sys5.set_configuration(s5.r_vectors(), s5.locations)
+    FT = np.zeros((s5.n_bodies, 6))
+    FT[:, 2] = -1.0
+    out = {"workload": "4096 shells x 42 blobs = 172,032 blobs, area fraction 0.3, z in [1.1R, 3R], F=(0,0,-1)",
+           "tol": 1e-8, "restart": 60}
+    clocks = ClockSampler(0)
+    clocks.start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sys5.build_pc()
+    torch.cuda.synchronize()
+    out["pc_build_ms"] = (time.perf_counter() - t0) * 1e3
+    sols = {}
+    for mode in args.large_modes.split(","):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sol, info, its, rr = integrator.solve_mobility_problem(sys5, FT, tol=1e-8, mode=mode)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        sols[mode] = sol[3 * sys5.n_blobs:].cpu().numpy()
+        out["solve_" + mode] = {"ms": dt * 1e3, "iterations": its, "relres": rr, "info": info}
+    out["clocks"] = clocks.stop()
+    ref = sols.get("fp64", sols.get("df64"))
+    for mode, u in sols.items():
+        out["solve_" + mode]["velocity_rel_err_vs_fp64"] = float(np.linalg.norm(u - ref) / np.linalg.norm(ref))
+    for base in ("fp64", "df64"):
+        if base in sols and "mixed" in sols:
+            out["speedup_mixed_vs_" + base] = out["solve_" + base]["ms"] / out["solve_mixed"]["ms"]
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
+    if args.large:
+        large_solve(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return

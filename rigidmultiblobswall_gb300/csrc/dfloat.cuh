@@ -60,6 +60,46 @@ __device__ __forceinline__ df operator*(df a, float b)
 }
 __device__ __forceinline__ df operator*(float a, df b) { return b * a; }
 
+// a*b + c with a single renormalisation
+__device__ __forceinline__ df mad(df a, df b, df c)
+{
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    const df t = two_sum_df(p, c.hi);
+    return fast_two_sum(t.hi, t.lo + (e + c.lo));
+}
+__device__ __forceinline__ df mad(df a, float b, df c)
+{
+    const float p = a.hi * b;
+    float e = fmaf(a.hi, b, -p);
+    e = fmaf(a.lo, b, e);
+    const df t = two_sum_df(p, c.hi);
+    return fast_two_sum(t.hi, t.lo + (e + c.lo));
+}
+// a*b + c*d with a single renormalisation
+__device__ __forceinline__ df mad2(df a, df b, df c, df d)
+{
+    const float p1 = a.hi * b.hi, p2 = c.hi * d.hi;
+    float e1 = fmaf(a.hi, b.hi, -p1);
+    e1 = fmaf(a.hi, b.lo, e1);
+    e1 = fmaf(a.lo, b.hi, e1);
+    float e2 = fmaf(c.hi, d.hi, -p2);
+    e2 = fmaf(c.hi, d.lo, e2);
+    e2 = fmaf(c.lo, d.hi, e2);
+    const df t = two_sum_df(p1, p2);
+    return fast_two_sum(t.hi, t.lo + (e1 + e2));
+}
+// acc += x without renormalising acc (the running low part absorbs the
+// rounding errors; fold before converting)
+__device__ __forceinline__ void acc_add(df &acc, df x)
+{
+    const df t = two_sum_df(acc.hi, x.hi);
+    acc.hi = t.hi;
+    acc.lo += t.lo + x.lo;
+}
+
 // exact scaling by a power of two
 __device__ __forceinline__ df scale2(df a, float p2) { return {a.hi * p2, a.lo * p2}; }
 

@@ -11,18 +11,26 @@ template <typename T> __device__ __forceinline__ T rsq(T x);
 template <> __device__ __forceinline__ double rsq<double>(double x) { return rsqrt(x); }
 template <> __device__ __forceinline__ float rsq<float>(float x) { return rsqrtf(x); }
 
+// The reference builds each 3x3 block from unit vectors e = (dx, dy, Rz)/R and
+// then multiplies by v.  Here the products are regrouped so that e never
+// appears: with s = 1/R, W = dx vx + dy vy + Rz vz and Q = dy vx - dx vy,
+//   (f2 (e.v) + f3 vz) e  = (f2 W s^2 + f3 vz s) (dx, dy, Rz)
+// and the RPY term Bc (d.v) d shares dx vx + dy vy with W.  h_hat never
+// appears either (h_hat e_z = h_j s, (1 - h_hat) e_z = h_i s).
 template <int KIND, typename T>
 __device__ __forceinline__ void pair_contrib(T dx, T dy, T dz, T Rz, T hi, T hj, T vx, T vy, T vz, T &ux, T &uy,
                                              T &uz)
 {
-    const T r2 = dx * dx + dy * dy + dz * dz;
+    const T rho2 = dx * dx + dy * dy;
+    const T r2 = rho2 + dz * dz;
     const T invr = rsq<T>(r2);
     const T r = r2 * invr;
-    const T R2 = dx * dx + dy * dy + Rz * Rz;
-    const T invR = rsq<T>(R2);
-    const T invR2 = invR * invR;
-    const T ex = dx * invR, ey = dy * invR, ez = Rz * invR;
-    const T ez2 = ez * ez;
+    const T Rz2 = Rz * Rz;
+    const T s = rsq<T>(rho2 + Rz2);
+    const T s2 = s * s;
+    const T s3 = s2 * s;
+    const T E = Rz2 * s2;  // e_z^2
+    const T Pxy = dx * vx + dy * vy;
     if (KIND == RMW_UF) {
         const T invr2 = invr * invr;
         T A, Bc;
@@ -33,49 +41,54 @@ __device__ __forceinline__ void pair_contrib(T dx, T dy, T dz, T Rz, T hi, T hj,
             A = T(4.0 / 3.0) * (T(1) - T(0.28125) * r);
             Bc = T(0.125) * invr;
         }
-        const T dv = dx * vx + dy * vy + dz * vz;
-        const T invR3 = invR2 * invR;
-        const T invR5 = invR3 * invR2;
-        const T hh = hi * hj * invR2;
-        const T f1 = -(T(3) * (T(1) + T(2) * hh) * invR + T(2) * (T(1) - T(3) * ez2) * invR3 -
-                       T(2) * (T(1) - T(5) * ez2) * invR5) * T(1.0 / 3.0);
-        const T f2 = -(T(3) * (T(1) - T(6) * hh) * invR - T(6) * (T(1) - T(5) * ez2) * invR3 +
-                       T(10) * (T(1) - T(7) * ez2) * invR5) * T(1.0 / 3.0);
-        const T f3 = T(2.0 / 3.0) * (T(3) * hj * invR2 - T(18) * hh * ez * invR +
-                                     ez * (T(10) * (T(2) - T(7) * ez2) * invR5 - T(6) * (T(1) - T(5) * ez2) * invR3));
-        const T f4 = T(2.0 / 3.0) * (T(3) * hj * invR2 - T(10) * ez * invR5);
-        const T f5 = T(-4.0 / 3.0) * (T(3) * (hj * hj + ez2) * invR3 + (T(2) - T(15) * ez2) * invR5);
-        const T ev = ex * vx + ey * vy + ez * vz;
-        const T ce = f2 * ev + f3 * vz;
+        const T dv = Pxy + dz * vz;
+        const T W = Pxy + Rz * vz;
+        const T s5 = s3 * s2;
+        const T hh = hi * hj * s2;
+        const T ez = Rz * s;
+        const T q5 = (T(1) - T(5) * E) * s3;
+        const T f1 = -((T(1) + T(2) * hh) * s + T(2.0 / 3.0) * ((T(1) - T(3) * E) * s3 - q5 * s2));
+        const T f2 = -((T(1) - T(6) * hh) * s - T(2) * q5 + T(10.0 / 3.0) * (T(1) - T(7) * E) * s5);
+        const T f3 = T(2.0 / 3.0) * (T(3) * hj * s2 - T(18) * hh * ez * s +
+                                     ez * (T(10) * (T(2) - T(7) * E) * s5 - T(6) * q5));
+        const T f4 = T(2.0 / 3.0) * (T(3) * hj * s2 - T(10) * ez * s5);
+        const T f5 = T(-4.0 / 3.0) * (T(3) * (hj * hj + E) * s3 + (T(2) - T(15) * E) * s5);
         const T Af = A + f1;
-        ux += Af * vx + Bc * dv * dx + ce * ex;
-        uy += Af * vy + Bc * dv * dy + ce * ey;
-        uz += Af * vz + Bc * dv * dz + ce * ez + f4 * ev + f5 * vz;
+        const T Gr = Bc * dv;
+        const T Gw = (f2 * W * s + f3 * vz) * s;
+        const T G = Gr + Gw;
+        ux += Af * vx + G * dx;
+        uy += Af * vy + G * dy;
+        uz += Af * vz + Gr * dz + Gw * Rz + f4 * W * s + f5 * vz;
     } else if (KIND == RMW_UT || KIND == RMW_WF) {
         const T c = (r >= T(2)) ? invr * invr * invr : T(0.5) * (T(1) - T(0.375) * r);
+        const T Q = dy * vx - dx * vy;  // (v x d)_z
         // RPY part: c (v x d)
         T ax = c * (vy * dz - vz * dy);
         T ay = c * (vz * dx - vx * dz);
-        T az = c * (vx * dy - vy * dx);
-        const T invR3 = invR2 * invR;
-        const T invR4 = invR2 * invR2;
+        T az = c * Q;
+        const T s4 = s2 * s2;
+        const T ez = Rz * s;
         const T h = (KIND == RMW_UT) ? hi : hj;  // UT evaluates the wall term with i and j swapped
-        const T f1 = invR2;
-        const T f2 = T(2) * (T(6) * h * invR3 * ez + (T(1) - T(10) * ez2) * invR4);
-        const T f3 = T(-2) * (T(3) * h * invR3 - T(5) * ez * invR4);
-        const T f4 = T(-2) * (h * invR3 - ez * invR4);
-        const T g = f1 + f2 + f3 * ez;
-        const T p = f1 * ez + f4;
+        const T hs3 = h * s3;
+        const T ezs4 = ez * s4;
+        const T f2 = T(2) * (T(6) * hs3 * ez + (T(1) - T(10) * E) * s4);
+        const T f3 = T(-2) * (T(3) * hs3 - T(5) * ezs4);
+        const T f4 = T(-2) * (hs3 - ezs4);
+        const T p = s2 * ez + f4;  // f1 = s^2
         if (KIND == RMW_UT) {
-            const T q = ey * vx - ex * vy;
-            ax += f3 * ex * q + p * vy + f1 * ey * vz;
-            ay += f3 * ey * q - p * vx - f1 * ex * vz;
-            az -= g * q;
+            const T F3 = f3 * s2 * Q;
+            const T F1 = s3 * vz;
+            const T g = s2 + f2 + f3 * ez;
+            ax += F3 * dx + p * vy + F1 * dy;
+            ay += F3 * dy - p * vx - F1 * dx;
+            az -= g * s * Q;
         } else {
-            const T s2 = ex * vx + ey * vy;
-            ax += f3 * ey * s2 - p * vy + g * ey * vz;
-            ay += -f3 * ex * s2 + p * vx - g * ex * vz;
-            az += f1 * (ex * vy - ey * vx);
+            const T g = s2 + f2 + f3 * ez;
+            const T H = f3 * s2 * Pxy + g * s * vz;
+            ax += H * dy - p * vy;
+            ay += p * vx - H * dx;
+            az -= s3 * Q;
         }
         ux += ax;
         uy += ay;
@@ -91,19 +104,17 @@ __device__ __forceinline__ void pair_contrib(T dx, T dy, T dz, T Rz, T hi, T hj,
             A = T(1) - T(0.84375) * r + T(0.078125) * r * r2;
             Bc = T(0.28125) * invr - T(0.046875) * r;
         }
-        const T dv = dx * vx + dy * vy + dz * vz;
-        const T invR3 = invR2 * invR;
-        const T f1 = T(0.5) * (T(1) - T(6) * ez2) * invR3;
-        const T f2 = T(-1.5) * invR3;
-        const T f3 = T(3) * invR3 * ez;
-        const T f4 = T(3) * invR3;
-        const T ev = ex * vx + ey * vy + ez * vz;
-        const T tv = f4 * (ex * vy - ey * vx);
-        const T Af = A + f1;
-        const T fe = f2 * ev;
-        ux += Af * vx + Bc * dv * dx + fe * ex - tv * ey;
-        uy += Af * vy + Bc * dv * dy + fe * ey + tv * ex;
-        uz += Af * vz + Bc * dv * dz + fe * ez + f3 * ev;
+        const T dv = Pxy + dz * vz;
+        const T W = Pxy + Rz * vz;
+        const T Q = dy * vx - dx * vy;
+        const T s5 = s3 * s2;
+        const T Af = A + T(0.5) * (T(1) - T(6) * E) * s3;
+        const T Gw = T(-1.5) * s5 * W;
+        const T Tq = T(3) * s5 * Q;
+        const T Gr = Bc * dv;
+        ux += Af * vx + (Gr + Gw) * dx + Tq * dy;
+        uy += Af * vy + (Gr + Gw) * dy - Tq * dx;
+        uz += Af * vz + Gr * dz - Gw * Rz;
     }
 }
 

@@ -151,9 +151,9 @@ __global__ void __launch_bounds__(kThreads) wall_pair_df_kernel(const SrcDF *__r
                     df cx = df_from(0.f), cy = df_from(0.f), cz = df_from(0.f);
                     pair_contrib_df<KIND>(xi - xj, yi - yj, dz, Rz, zi, zj, vx, vy, vz, cx, cy, cz);
                     if (j != i) {
-                        ux = ux + cx;
-                        uy = uy + cy;
-                        uz = uz + cz;
+                        acc_add(ux, cx);
+                        acc_add(uy, cy);
+                        acc_add(uz, cz);
                     }
                 } else {
                     // minimum image in FP64 (rare path), then back to double-float
@@ -171,9 +171,9 @@ __global__ void __launch_bounds__(kThreads) wall_pair_df_kernel(const SrcDF *__r
                                                       cy, cz);
                                 const bool self = (j == i) && bx == 0 && by == 0 && bz == 0;
                                 if (!self) {
-                                    ux = ux + cx;
-                                    uy = uy + cy;
-                                    uz = uz + cz;
+                                    acc_add(ux, cx);
+                                    acc_add(uy, cy);
+                                    acc_add(uz, cz);
                                 }
                             }
                 }

@@ -33,13 +33,16 @@ __device__ __forceinline__ void pair_contrib(T dx, T dy, T dz, T Rz, T hi, T hj,
     const T Pxy = dx * vx + dy * vy;
     if (KIND == RMW_UF) {
         const T invr2 = invr * invr;
-        T A, Bc;
-        if (r > T(2)) {
-            A = (T(1) + T(2.0 / 3.0) * invr2) * invr;
-            Bc = (T(1) - T(2) * invr2) * invr2 * invr;
-        } else {
-            A = T(4.0 / 3.0) * (T(1) - T(0.28125) * r);
-            Bc = T(0.125) * invr;
+        // far branch always; the near (r <= 2) branch only when some lane of the
+        // warp needs it (rare: touching blobs), so warps stay convergent
+        T A = (T(1) + T(2.0 / 3.0) * invr2) * invr;
+        T Bc = (T(1) - T(2) * invr2) * invr2 * invr;
+        const bool near = !(r > T(2));
+        if (__any_sync(__activemask(), near)) {
+            if (near) {
+                A = T(4.0 / 3.0) * (T(1) - T(0.28125) * r);
+                Bc = T(0.125) * invr;
+            }
         }
         const T dv = Pxy + dz * vz;
         const T W = Pxy + Rz * vz;
@@ -61,7 +64,11 @@ __device__ __forceinline__ void pair_contrib(T dx, T dy, T dz, T Rz, T hi, T hj,
         uy += Af * vy + G * dy;
         uz += Af * vz + Gr * dz + Gw * Rz + f4 * W * s + f5 * vz;
     } else if (KIND == RMW_UT || KIND == RMW_WF) {
-        const T c = (r >= T(2)) ? invr * invr * invr : T(0.5) * (T(1) - T(0.375) * r);
+        T c = invr * invr * invr;
+        const bool near = !(r >= T(2));
+        if (__any_sync(__activemask(), near)) {
+            if (near) c = T(0.5) * (T(1) - T(0.375) * r);
+        }
         const T Q = dy * vx - dx * vy;  // (v x d)_z
         // RPY part: c (v x d)
         T ax = c * (vy * dz - vz * dy);
@@ -96,13 +103,14 @@ __device__ __forceinline__ void pair_contrib(T dx, T dy, T dz, T Rz, T hi, T hj,
     } else {  // RMW_WT
         const T invr2 = invr * invr;
         const T invr3 = invr2 * invr;
-        T A, Bc;
-        if (r >= T(2)) {
-            A = T(-0.5) * invr3;
-            Bc = T(1.5) * invr2 * invr3;
-        } else {
-            A = T(1) - T(0.84375) * r + T(0.078125) * r * r2;
-            Bc = T(0.28125) * invr - T(0.046875) * r;
+        T A = T(-0.5) * invr3;
+        T Bc = T(1.5) * invr2 * invr3;
+        const bool near = !(r >= T(2));
+        if (__any_sync(__activemask(), near)) {
+            if (near) {
+                A = T(1) - T(0.84375) * r + T(0.078125) * r * r2;
+                Bc = T(0.28125) * invr - T(0.046875) * r;
+            }
         }
         const T dv = Pxy + dz * vz;
         const T W = Pxy + Rz * vz;

@@ -33,13 +33,14 @@ __device__ __forceinline__ void pair_contrib_df(df dx, df dy, df dz, df Rz, df h
     const df Pxy = mad2(dx, vx, dy, vy);
     if (KIND == RMW_UF) {
         const df invr2 = sqr(invr);
-        df A, Bc;
-        if (r > 2.0f) {
-            A = mad(TWO_THIRDS, invr2, df_from(1.0f)) * invr;
-            Bc = (1.0f - scale2(invr2, 2.0f)) * invr2 * invr;
-        } else {
-            A = FOUR_THIRDS * (1.0f - r * 0.28125f);
-            Bc = scale2(invr, 0.125f);
+        df A = mad(TWO_THIRDS, invr2, df_from(1.0f)) * invr;
+        df Bc = (1.0f - scale2(invr2, 2.0f)) * invr2 * invr;
+        const bool near = !(r > 2.0f);
+        if (__any_sync(__activemask(), near)) {
+            if (near) {
+                A = FOUR_THIRDS * (1.0f - r * 0.28125f);
+                Bc = scale2(invr, 0.125f);
+            }
         }
         const df dv = mad(dz, vz, Pxy);
         const df W = mad(Rz, vz, Pxy);
@@ -61,7 +62,11 @@ __device__ __forceinline__ void pair_contrib_df(df dx, df dy, df dz, df Rz, df h
         uy = mad2(Af, vy, G, dy);
         uz = mad2(Af, vz, Gr, dz) + mad2(Gw, Rz, f4 * W, s) + f5 * vz;
     } else if (KIND == RMW_UT || KIND == RMW_WF) {
-        const df c = (r >= 2.0f) ? sqr(invr) * invr : scale2(1.0f - r * 0.375f, 0.5f);
+        df c = sqr(invr) * invr;
+        const bool near = !(r >= 2.0f);
+        if (__any_sync(__activemask(), near)) {
+            if (near) c = scale2(1.0f - r * 0.375f, 0.5f);
+        }
         const df Q = mad2(dy, vx, -dx, vy);  // (v x d)_z
         df ax = c * mad2(vy, dz, -vz, dy);
         df ay = c * mad2(vz, dx, -vx, dz);
@@ -94,13 +99,14 @@ __device__ __forceinline__ void pair_contrib_df(df dx, df dy, df dz, df Rz, df h
     } else {  // RMW_WT
         const df invr2 = sqr(invr);
         const df invr3 = invr2 * invr;
-        df A, Bc;
-        if (r >= 2.0f) {
-            A = invr3 * -0.5f;
-            Bc = (invr2 * invr3) * 1.5f;
-        } else {
-            A = (1.0f - r * 0.84375f) + (r * r2) * 0.078125f;
-            Bc = invr * 0.28125f - r * 0.046875f;
+        df A = invr3 * -0.5f;
+        df Bc = (invr2 * invr3) * 1.5f;
+        const bool near = !(r >= 2.0f);
+        if (__any_sync(__activemask(), near)) {
+            if (near) {
+                A = (1.0f - r * 0.84375f) + (r * r2) * 0.078125f;
+                Bc = invr * 0.28125f - r * 0.046875f;
+            }
         }
         const df dv = mad(dz, vz, Pxy);
         const df W = mad(Rz, vz, Pxy);

@@ -137,9 +137,27 @@ __global__ void __launch_bounds__(kThreads) wall_pair_df_kernel(const SrcDF *__r
         __syncthreads();
         for (int k = threadIdx.x; k < cnt; k += kThreads) tile[k] = src[t0 + k];
         __syncthreads();
+        const bool self_possible = (t0 < (int)(blockIdx.x + 1) * kThreads) && (t0 + cnt > (int)blockIdx.x * kThreads);
         for (int g0 = 0; g0 < cnt; g0 += kDfGroup) {
             const int g1 = min(cnt, g0 + kDfGroup);
             df ux = df_from(0.f), uy = df_from(0.f), uz = df_from(0.f);
+            if (!PER && !self_possible) {
+                // tiles that cannot hold this CTA's targets: no self-pair test
+                for (int k = g0; k < g1; ++k) {
+                    const float4 sh = tile[k].hi, sl = tile[k].lo, svh = tile[k].vhi, svl = tile[k].vlo;
+                    const df xj = {sh.x, sl.x}, yj = {sh.y, sl.y}, zj = {sh.z, sl.z};
+                    const df vx = {svh.x, svl.x}, vy = {svh.y, svl.y}, vz = {svh.z, svl.z};
+                    df cx, cy, cz;
+                    pair_contrib_df<KIND>(xi - xj, yi - yj, zi - zj, zi + zj, zi, zj, vx, vy, vz, cx, cy, cz);
+                    acc_add(ux, cx);
+                    acc_add(uy, cy);
+                    acc_add(uz, cz);
+                }
+                ax += to_double(ux);
+                ay += to_double(uy);
+                az += to_double(uz);
+                continue;
+            }
             for (int k = g0; k < g1; ++k) {
                 const float4 sh = tile[k].hi, sl = tile[k].lo, svh = tile[k].vhi, svl = tile[k].vlo;
                 const int j = t0 + k;
@@ -269,6 +287,21 @@ __global__ void __launch_bounds__(kThreads) wall_pair_mixed_kernel(const SrcF *_
         for (int k = threadIdx.x; k < cnt; k += kThreads) tile[k] = src[t0 + k];
         __syncthreads();
         float ux = 0.f, uy = 0.f, uz = 0.f;
+        // only tiles that overlap this CTA's own targets can hold the self pair
+        const bool self_possible = (t0 < (int)(blockIdx.x + 1) * kThreads) && (t0 + cnt > (int)blockIdx.x * kThreads);
+        if (!PER && !self_possible) {
+#pragma unroll 4
+            for (int k = 0; k < cnt; ++k) {
+                const float4 sh = tile[k].hi;
+                const float4 sl = tile[k].lo;
+                const float4 sv = tile[k].v;
+                const float dx = (mh.x - sh.x) + (ml.x - sl.x);
+                const float dy = (mh.y - sh.y) + (ml.y - sl.y);
+                const float dz = (mh.z - sh.z) + (ml.z - sl.z);
+                const float hj = sh.z + sl.z;
+                pair_contrib<KIND, float>(dx, dy, dz, hi + hj, hi, hj, sv.x, sv.y, sv.z, ux, uy, uz);
+            }
+        } else
 #pragma unroll 4
         for (int k = 0; k < cnt; ++k) {
             const float4 sh = tile[k].hi;

@@ -78,6 +78,16 @@ int rmw_wall_wt(const double *r, const double *v, double *out, int64_t n, double
 int rmw_wall_product(int kind, const double *r, const double *v, double *out, int64_t n, double eta,
                      double a, const double *L_host, int mode, void *stream);
 
+/* Segmented products of many independent suspensions in one launch:
+ * suspension k owns blobs [blob_offsets[k], blob_offsets[k+1]) of one (N,3)
+ * array and interacts only with itself (block-diagonal mobility).  The batch
+ * handle holds the CTA job table; no reference counterpart (the reference
+ * loops over systems one call at a time). */
+int rmw_wall_batch_create(void **handle, int64_t n_suspensions, const int64_t *blob_offsets_host);
+int rmw_wall_batch_destroy(void *handle);
+int rmw_wall_product_batched(void *handle, int kind, const double *r, const double *v, double *out, double eta,
+                             double a, int mode, void *stream);
+
 /* Host-buffer form: the drop-in for the reference's pycuda wrappers, which
  * copy host arrays to the device, launch, and copy the result back on every
  * call (mobility/mobility_pycuda.py:2235-2267).  Synchronous.  Pinned or
@@ -163,6 +173,21 @@ int rmw_rigid_lanczos(void *handle, const double *z, double *noise, double facto
 int rmw_wall_lanczos(const double *r, const double *z, double *noise, int64_t n, double eta, double a,
                      const double *L_host, double factor, double tol, int max_iter, int mode, void *stream,
                      int *iters_host);
+
+/* Declare that the handle's bodies form independent suspensions: suspension
+ * k owns bodies [body_offsets[k], body_offsets[k+1]) and its blobs interact
+ * only with each other (segmented pair products).  Enables the batched
+ * solver.  No reference counterpart: the reference solves one suspension per
+ * process. */
+int rmw_rigid_set_suspensions(void *handle, int64_t n_suspensions, const int64_t *body_offsets_host);
+/* Solve every suspension of the handle with its own right-preconditioned
+ * restarted GMRES (own Krylov space, tolerance, iteration count) in lockstep:
+ * one operator and preconditioner application per step for all suspensions.
+ * rhs/sol use the [lambda; U] layout; iters/relres/status_host receive one
+ * entry per suspension.  mode as rmw_rigid_solve (MIXED refines per
+ * suspension).  Synchronous; returns RMW_OK when every suspension converged. */
+int rmw_rigid_solve_batched(void *handle, const double *rhs, double *sol, double tol, int restart, int maxiter,
+                            int mode, int *iters_host, double *relres_host, int *status_host);
 
 /* ---- generic Krylov solvers with caller-supplied operators ------------
  * op(ctx, x, y) must write y = A x for device vectors of length n, enqueue its

@@ -3,6 +3,12 @@
 // transformations TwoSum (Knuth), FastTwoSum (Dekker) and the FMA-based exact
 // product; additions use the cheap ("sloppy") variant, whose error is bounded
 // by ~2^-47 (|a| + |b|) - the same form as an FP64 addition, 30x looser.
+//
+// Every rounding step of these transformations uses the _rn intrinsics:
+// the compiler never contracts them into an FMA.  A contracted
+// `p = x*y; s = p + c` becomes s = fma(x, y, c), no longer the rounded sum of
+// the p that the error term is computed from, and the transformation stops
+// being error-free (a ~2^-24 relative error leaks into the result).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -16,26 +22,26 @@ __device__ __forceinline__ df df_from(float h) { return {h, 0.0f}; }
 
 __device__ __forceinline__ df fast_two_sum(float a, float b)
 {
-    const float s = a + b;
-    return {s, b - (s - a)};
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
 
 __device__ __forceinline__ df two_sum_df(float a, float b)
 {
-    const float s = a + b;
-    const float bb = s - a;
-    return {s, (a - (s - bb)) + (b - bb)};
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
 }
 
 __device__ __forceinline__ df operator+(df a, df b)
 {
     const df s = two_sum_df(a.hi, b.hi);
-    return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
 __device__ __forceinline__ df operator+(df a, float b)
 {
     const df s = two_sum_df(a.hi, b);
-    return fast_two_sum(s.hi, s.lo + a.lo);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
 }
 __device__ __forceinline__ df operator+(float a, df b) { return b + a; }
 __device__ __forceinline__ df operator-(df a) { return {-a.hi, -a.lo}; }
@@ -45,7 +51,7 @@ __device__ __forceinline__ df operator-(float a, df b) { return (-b) + a; }
 
 __device__ __forceinline__ df operator*(df a, df b)
 {
-    const float p = a.hi * b.hi;
+    const float p = __fmul_rn(a.hi, b.hi);
     float e = fmaf(a.hi, b.hi, -p);
     e = fmaf(a.hi, b.lo, e);
     e = fmaf(a.lo, b.hi, e);
@@ -53,7 +59,7 @@ __device__ __forceinline__ df operator*(df a, df b)
 }
 __device__ __forceinline__ df operator*(df a, float b)
 {
-    const float p = a.hi * b;
+    const float p = __fmul_rn(a.hi, b);
     float e = fmaf(a.hi, b, -p);
     e = fmaf(a.lo, b, e);
     return fast_two_sum(p, e);
@@ -63,25 +69,25 @@ __device__ __forceinline__ df operator*(float a, df b) { return b * a; }
 // a*b + c with a single renormalisation
 __device__ __forceinline__ df mad(df a, df b, df c)
 {
-    const float p = a.hi * b.hi;
+    const float p = __fmul_rn(a.hi, b.hi);
     float e = fmaf(a.hi, b.hi, -p);
     e = fmaf(a.hi, b.lo, e);
     e = fmaf(a.lo, b.hi, e);
     const df t = two_sum_df(p, c.hi);
-    return fast_two_sum(t.hi, t.lo + (e + c.lo));
+    return fast_two_sum(t.hi, __fadd_rn(t.lo, __fadd_rn(e, c.lo)));
 }
 __device__ __forceinline__ df mad(df a, float b, df c)
 {
-    const float p = a.hi * b;
+    const float p = __fmul_rn(a.hi, b);
     float e = fmaf(a.hi, b, -p);
     e = fmaf(a.lo, b, e);
     const df t = two_sum_df(p, c.hi);
-    return fast_two_sum(t.hi, t.lo + (e + c.lo));
+    return fast_two_sum(t.hi, __fadd_rn(t.lo, __fadd_rn(e, c.lo)));
 }
 // a*b + c*d with a single renormalisation
 __device__ __forceinline__ df mad2(df a, df b, df c, df d)
 {
-    const float p1 = a.hi * b.hi, p2 = c.hi * d.hi;
+    const float p1 = __fmul_rn(a.hi, b.hi), p2 = __fmul_rn(c.hi, d.hi);
     float e1 = fmaf(a.hi, b.hi, -p1);
     e1 = fmaf(a.hi, b.lo, e1);
     e1 = fmaf(a.lo, b.hi, e1);
@@ -89,7 +95,7 @@ __device__ __forceinline__ df mad2(df a, df b, df c, df d)
     e2 = fmaf(c.hi, d.lo, e2);
     e2 = fmaf(c.lo, d.hi, e2);
     const df t = two_sum_df(p1, p2);
-    return fast_two_sum(t.hi, t.lo + (e1 + e2));
+    return fast_two_sum(t.hi, __fadd_rn(t.lo, __fadd_rn(e1, e2)));
 }
 // acc += x without renormalising acc (the running low part absorbs the
 // rounding errors; fold before converting)
@@ -97,15 +103,15 @@ __device__ __forceinline__ void acc_add(df &acc, df x)
 {
     const df t = two_sum_df(acc.hi, x.hi);
     acc.hi = t.hi;
-    acc.lo += t.lo + x.lo;
+    acc.lo = __fadd_rn(acc.lo, __fadd_rn(t.lo, x.lo));
 }
 
 // exact scaling by a power of two
-__device__ __forceinline__ df scale2(df a, float p2) { return {a.hi * p2, a.lo * p2}; }
+__device__ __forceinline__ df scale2(df a, float p2) { return {__fmul_rn(a.hi, p2), __fmul_rn(a.lo, p2)}; }
 
 __device__ __forceinline__ df sqr(df a)
 {
-    const float p = a.hi * a.hi;
+    const float p = __fmul_rn(a.hi, a.hi);
     float e = fmaf(a.hi, a.hi, -p);
     e = fmaf(2.0f * a.hi, a.lo, e);
     return fast_two_sum(p, e);
@@ -114,7 +120,7 @@ __device__ __forceinline__ df sqr(df a)
 // exact product of two floats
 __device__ __forceinline__ df two_prod(float a, float b)
 {
-    const float p = a * b;
+    const float p = __fmul_rn(a, b);
     return {p, fmaf(a, b, -p)};
 }
 
@@ -127,8 +133,8 @@ __device__ __forceinline__ df rsqrt_df(df x)
     float y = rsqrtf(x.hi);
     y = y * fmaf(-0.5f * x.hi, y * y, 1.5f);
     const df t = x * two_prod(y, y);
-    const float e = (1.0f - t.hi) - t.lo;
-    return fast_two_sum(y, 0.5f * y * e);
+    const float e = __fsub_rn(__fsub_rn(1.0f, t.hi), t.lo);
+    return fast_two_sum(y, __fmul_rn(__fmul_rn(0.5f, y), e));
 }
 
 __device__ __forceinline__ bool operator>(df a, float b) { return a.hi > b || (a.hi == b && a.lo > 0.0f); }

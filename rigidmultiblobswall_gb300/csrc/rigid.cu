@@ -469,11 +469,17 @@ static int build_pc(RigidSystem &S, bool stochastic)
     return RMW_OK;
 }
 
+int rigid_mobility(RigidSystem &S, const double *v, double *y, int mode)
+{
+    if (S.batch) return wall_product_batched(*S.batch, RMW_UF, S.r, v, y, S.eta, S.a, mode, S.st);
+    return wall_product(RMW_UF, S.r, v, y, S.n, S.eta, S.a, S.L, mode, S.st);
+}
+
 int rigid_apply(RigidSystem &S, const double *x, double *y, int mode)
 {
     cudaStream_t st = S.st;
     // y_blob = M l
-    if (int rc = wall_product(RMW_UF, S.r, x, y, S.n, S.eta, S.a, S.L, mode, st)) return rc;
+    if (int rc = rigid_mobility(S, x, y, mode)) return rc;
     const int tb = 256;
     // y_blob -= K U
     k_times_u_kernel<<<(S.n + tb - 1) / tb, tb, 0, st>>>(S.r, S.xb, S.blob_body, x + 3LL * S.n, y, S.n, -1.0, 1.0);
@@ -512,7 +518,7 @@ int rigid_mobility_pc(RigidSystem &S, const double *w, double *y, int mode)
     if (!S.stoch_ready) return fail(RMW_ERR_ARG, "stochastic preconditioner not built");
     // y = L^-1 M L^-T w   (P = L^-T, reference: P^T M P with P = U^-1, U = L^T)
     if (int rc = tri_mult(S, S.linv, w, S.tmp3n, 1)) return rc;
-    if (int rc = wall_product(RMW_UF, S.r, S.tmp3n, y, S.n, S.eta, S.a, S.L, mode, S.st)) return rc;
+    if (int rc = rigid_mobility(S, S.tmp3n, y, mode)) return rc;
     // in place is safe per body: each CTA stages its own slice in shared memory first
     return tri_mult(S, S.linv, y, y, 0);
 }
@@ -529,9 +535,13 @@ static void free_system(RigidSystem *S)
     cudaGetDevice(&cur);
     cudaSetDevice(S->device);
     void *ptrs[] = {S->boff, S->blob_body, S->moff, S->r, S->xb, S->minv, S->minvK, S->nmat, S->lfac, S->linv,
-                    S->dstatus, S->tmp3n};
+                    S->dstatus, S->tmp3n, S->perm};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    if (S->batch) {
+        wall_batch_free(*S->batch);
+        delete S->batch;
+    }
     cudaSetDevice(cur);
     delete S;
 }

@@ -8,6 +8,8 @@
 
 namespace rmw {
 
+struct WallBatch;
+
 struct RigidSystem {
     int nb = 0;       // bodies
     int n = 0;        // blobs
@@ -32,6 +34,12 @@ struct RigidSystem {
     int *dstatus = nullptr;        // device status word
     double *tmp3n = nullptr;       // 3n scratch vector
     bool pc_ready = false, stoch_ready = false;
+    // independent suspensions inside the handle (rmw_rigid_set_suspensions):
+    // segmented pair products and the instance-major permutation
+    WallBatch *batch = nullptr;
+    std::vector<long long> susp_body_off;  // bodies of suspension k: [off[k], off[k+1])
+    std::vector<long long> susp_off;       // instance-major offsets of the system vector
+    long long *perm = nullptr;             // device: instance-major index -> [lambda; U] index
 
     long long sys_size() const { return 3LL * n + 6LL * nb; }
 };
@@ -44,5 +52,7 @@ int rigid_apply_pc(RigidSystem &S, const double *x, double *y);
 int rigid_mobility_pc(RigidSystem &S, const double *w, double *y, int mode);
 // y = L w (det_stoch P_inv_mult, multi_bodies.py:609-615).
 int rigid_P_inv_mult(RigidSystem &S, const double *w, double *y);
+// M v on the handle's blobs (segmented by suspension when suspensions are set).
+int rigid_mobility(RigidSystem &S, const double *v, double *y, int mode);
 
 }  // namespace rmw

@@ -49,9 +49,10 @@ constexpr double kPi = 3.14159265358979323846;
 // TwoSum (Knuth): s + e == a + b exactly.
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
 {
-    s = a + b;
-    float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
+    // _rn intrinsics: never contracted into an FMA, so the transformation stays exact
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
 // (hi, lo) += x, keeping lo as the running compensation.
@@ -60,7 +61,7 @@ __device__ __forceinline__ void comp_add(float &hi, float &lo, float x)
     float s, e;
     two_sum(hi, x, s, e);
     hi = s;
-    lo += e;
+    lo = __fadd_rn(lo, e);
 }
 
 }  // namespace rmw

@@ -61,6 +61,26 @@ struct Periodic {
     double Lx, Ly, Lz;  // already divided by a for the mixed path
 };
 
+// Work of one CTA: targets [tbeg, tend) against sources [j0, j1), partial sums
+// into chunk slot `slot`.  Without a job table (SEG = false) it follows from
+// the 2-D grid: target tile blockIdx.x, source chunk blockIdx.y.  With one
+// (segmented products of many independent suspensions) each CTA reads its job.
+struct PairRange {
+    int tbeg, tend, j0, j1, slot;
+};
+
+template <bool SEG>
+__device__ __forceinline__ PairRange pair_range(const TileJob *jobs, int n, int chunk)
+{
+    if (SEG) {
+        const TileJob jb = jobs[blockIdx.x];
+        return {jb.t0, jb.t1, jb.s0, jb.s1, jb.slot};
+    }
+    const int tb = blockIdx.x * kThreads;
+    const int j0 = blockIdx.y * chunk;
+    return {tb, min(n, tb + kThreads), j0, min(n, j0 + chunk), (int)blockIdx.y};
+}
+
 // ---------------------------------------------------------------------------
 // pack
 __global__ void pack_fp64_kernel(const double *__restrict__ r, const double *__restrict__ v, SrcD *__restrict__ src,
@@ -120,16 +140,18 @@ __global__ void pack_df_kernel(const double *__restrict__ r, const double *__res
 // accumulators (FP64 pipe, a few adds per group).
 constexpr int kDfGroup = 32;
 
-template <int KIND, bool PER>
+template <int KIND, bool PER, bool SEG>
 __global__ void __launch_bounds__(kThreads) wall_pair_df_kernel(const SrcDF *__restrict__ src, int n, int chunk,
-                                                                 Periodic P, double *__restrict__ partial)
+                                                                 Periodic P, double *__restrict__ partial,
+                                                                 const TileJob *__restrict__ jobs)
 {
     __shared__ SrcDF tile[kTile];
-    const int i = blockIdx.x * kThreads + threadIdx.x;
-    const int j0 = blockIdx.y * chunk;
-    const int j1 = min(n, j0 + chunk);
+    const PairRange pr = pair_range<SEG>(jobs, n, chunk);
+    const int i = pr.tbeg + threadIdx.x;
+    const bool valid = i < pr.tend;
+    const int j0 = pr.j0, j1 = pr.j1;
     float4 mh = make_float4(0.f, 0.f, 1.f, 0.f), ml = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (i < n) { mh = src[i].hi; ml = src[i].lo; }
+    if (valid) { mh = src[i].hi; ml = src[i].lo; }
     const df xi = {mh.x, ml.x}, yi = {mh.y, ml.y}, zi = {mh.z, ml.z};
     double ax = 0.0, ay = 0.0, az = 0.0;
     for (int t0 = j0; t0 < j1; t0 += kTile) {
@@ -137,7 +159,7 @@ __global__ void __launch_bounds__(kThreads) wall_pair_df_kernel(const SrcDF *__r
         __syncthreads();
         for (int k = threadIdx.x; k < cnt; k += kThreads) tile[k] = src[t0 + k];
         __syncthreads();
-        const bool self_possible = (t0 < (int)(blockIdx.x + 1) * kThreads) && (t0 + cnt > (int)blockIdx.x * kThreads);
+        const bool self_possible = (t0 < pr.tend) && (t0 + cnt > pr.tbeg);
         for (int g0 = 0; g0 < cnt; g0 += kDfGroup) {
             const int g1 = min(cnt, g0 + kDfGroup);
             df ux = df_from(0.f), uy = df_from(0.f), uz = df_from(0.f);
@@ -201,25 +223,27 @@ __global__ void __launch_bounds__(kThreads) wall_pair_df_kernel(const SrcDF *__r
             az += to_double(uz);
         }
     }
-    if (i < n) {
-        double *o = partial + (size_t)blockIdx.y * 3 * n + 3 * (size_t)i;
+    if (valid) {
+        double *o = partial + (size_t)pr.slot * 3 * n + 3 * (size_t)i;
         o[0] = ax; o[1] = ay; o[2] = az;
     }
 }
 
 // ---------------------------------------------------------------------------
 // FP64 pair kernel
-template <int KIND, bool PER>
+template <int KIND, bool PER, bool SEG>
 __global__ void __launch_bounds__(kThreads) wall_pair_fp64_kernel(const SrcD *__restrict__ src, int n, int chunk,
                                                                    double inva, Periodic P,
-                                                                   double *__restrict__ partial)
+                                                                   double *__restrict__ partial,
+                                                                   const TileJob *__restrict__ jobs)
 {
     __shared__ SrcD tile[kTile];
-    const int i = blockIdx.x * kThreads + threadIdx.x;
-    const int j0 = blockIdx.y * chunk;
-    const int j1 = min(n, j0 + chunk);
+    const PairRange pr = pair_range<SEG>(jobs, n, chunk);
+    const int i = pr.tbeg + threadIdx.x;
+    const bool valid = i < pr.tend;
+    const int j0 = pr.j0, j1 = pr.j1;
     SrcD me;
-    if (i < n) me = src[i];
+    if (valid) me = src[i];
     else { me.x = 0.0; me.y = 0.0; me.z = 1.0; }
     const double hi = me.z * inva;
     double ux = 0.0, uy = 0.0, uz = 0.0;
@@ -258,8 +282,8 @@ __global__ void __launch_bounds__(kThreads) wall_pair_fp64_kernel(const SrcD *__
             }
         }
     }
-    if (i < n) {
-        double *o = partial + (size_t)blockIdx.y * 3 * n + 3 * (size_t)i;
+    if (valid) {
+        double *o = partial + (size_t)pr.slot * 3 * n + 3 * (size_t)i;
         o[0] = ux; o[1] = uy; o[2] = uz;
     }
 }
@@ -267,16 +291,18 @@ __global__ void __launch_bounds__(kThreads) wall_pair_fp64_kernel(const SrcD *__
 // ---------------------------------------------------------------------------
 // Mixed pair kernel: FP32 pair evaluation, double-float position differences,
 // per-tile FP32 sums folded into TwoSum-compensated accumulators.
-template <int KIND, bool PER>
+template <int KIND, bool PER, bool SEG>
 __global__ void __launch_bounds__(kThreads) wall_pair_mixed_kernel(const SrcF *__restrict__ src, int n, int chunk,
-                                                                    Periodic P, double *__restrict__ partial)
+                                                                    Periodic P, double *__restrict__ partial,
+                                                                    const TileJob *__restrict__ jobs)
 {
     __shared__ SrcF tile[kTile];
-    const int i = blockIdx.x * kThreads + threadIdx.x;
-    const int j0 = blockIdx.y * chunk;
-    const int j1 = min(n, j0 + chunk);
+    const PairRange pr = pair_range<SEG>(jobs, n, chunk);
+    const int i = pr.tbeg + threadIdx.x;
+    const bool valid = i < pr.tend;
+    const int j0 = pr.j0, j1 = pr.j1;
     float4 mh = make_float4(0.f, 0.f, 1.f, 0.f), ml = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (i < n) { mh = src[i].hi; ml = src[i].lo; }
+    if (valid) { mh = src[i].hi; ml = src[i].lo; }
     const float hi = mh.z + ml.z;
     float sx = 0.f, sy = 0.f, sz = 0.f;   // compensated running sums (hi parts)
     float ex_ = 0.f, ey_ = 0.f, ez_ = 0.f;  // compensation terms
@@ -288,7 +314,7 @@ __global__ void __launch_bounds__(kThreads) wall_pair_mixed_kernel(const SrcF *_
         __syncthreads();
         float ux = 0.f, uy = 0.f, uz = 0.f;
         // only tiles that overlap this CTA's own targets can hold the self pair
-        const bool self_possible = (t0 < (int)(blockIdx.x + 1) * kThreads) && (t0 + cnt > (int)blockIdx.x * kThreads);
+        const bool self_possible = (t0 < pr.tend) && (t0 + cnt > pr.tbeg);
         if (!PER && !self_possible) {
 #pragma unroll 4
             for (int k = 0; k < cnt; ++k) {
@@ -338,8 +364,8 @@ __global__ void __launch_bounds__(kThreads) wall_pair_mixed_kernel(const SrcF *_
         comp_add(sy, ey_, uy);
         comp_add(sz, ez_, uz);
     }
-    if (i < n) {
-        double *o = partial + (size_t)blockIdx.y * 3 * n + 3 * (size_t)i;
+    if (valid) {
+        double *o = partial + (size_t)pr.slot * 3 * n + 3 * (size_t)i;
         o[0] = (double)sx + (double)ex_;
         o[1] = (double)sy + (double)ey_;
         o[2] = (double)sz + (double)ez_;
@@ -351,12 +377,13 @@ __global__ void __launch_bounds__(kThreads) wall_pair_mixed_kernel(const SrcF *_
 template <int KIND>
 __global__ void wall_finalize_kernel(const double *__restrict__ r, const double *__restrict__ v,
                                      const double *__restrict__ partial, int nchunks, double *__restrict__ out,
-                                     int n, double a, double nf)
+                                     int n, double a, double nf, const int *__restrict__ blob_nchunks)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double ux = 0.0, uy = 0.0, uz = 0.0;
-    for (int s = 0; s < nchunks; ++s) {
+    const int nc = blob_nchunks ? blob_nchunks[i] : nchunks;
+    for (int s = 0; s < nc; ++s) {
         const double *p = partial + (size_t)s * 3 * n + 3 * (size_t)i;
         ux += p[0]; uy += p[1]; uz += p[2];
     }
@@ -408,45 +435,49 @@ size_t wall_scratch_bytes(int n, int mode, int nchunks)
 
 template <int KIND>
 static int launch_kind(const double *r, const double *v, double *out, int n, double eta, double a, const double *L,
-                       int mode, cudaStream_t st, void *scratch_ptr, int nchunks)
+                       int mode, cudaStream_t st, void *scratch_ptr, int nchunks, const WallBatch *B)
 {
     const double inva = 1.0 / a;
     const double nf = (KIND == RMW_UF)   ? 1.0 / (8.0 * kPi * eta * a)
                       : (KIND == RMW_WT) ? 1.0 / (8.0 * kPi * eta * a * a * a)
                                          : 1.0 / (8.0 * kPi * eta * a * a);
-    const bool per = L && (L[0] > 0 || L[1] > 0 || L[2] > 0);
+    const bool per = !B && L && (L[0] > 0 || L[1] > 0 || L[2] > 0);
     Periodic P{L ? L[0] : 0.0, L ? L[1] : 0.0, L ? L[2] : 0.0};
     size_t rec = (mode == RMW_MODE_FP64) ? sizeof(SrcD) : (mode == RMW_MODE_DF64 ? sizeof(SrcDF) : sizeof(SrcF));
     size_t packed = ((rec * (size_t)n + 255) / 256) * 256;
     char *base = (char *)scratch_ptr;
     double *partial = (double *)(base + packed);
     const int chunk = (n + nchunks - 1) / nchunks;
-    dim3 grid((n + kThreads - 1) / kThreads, nchunks);
+    const dim3 grid = B ? dim3(B->njobs) : dim3((n + kThreads - 1) / kThreads, nchunks);
+    const TileJob *jobs = B ? B->jobs : nullptr;
     const int pb = 256, pg = (n + pb - 1) / pb;
     void *tok = nullptr;
     if (mode == RMW_MODE_FP64) {
         SrcD *src = (SrcD *)base;
         pack_fp64_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
         if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
-        if (per) wall_pair_fp64_kernel<KIND, true><<<grid, kThreads, 0, st>>>(src, n, chunk, inva, P, partial);
-        else wall_pair_fp64_kernel<KIND, false><<<grid, kThreads, 0, st>>>(src, n, chunk, inva, P, partial);
+        if (B) wall_pair_fp64_kernel<KIND, false, true><<<grid, kThreads, 0, st>>>(src, n, chunk, inva, P, partial, jobs);
+        else if (per) wall_pair_fp64_kernel<KIND, true, false><<<grid, kThreads, 0, st>>>(src, n, chunk, inva, P, partial, jobs);
+        else wall_pair_fp64_kernel<KIND, false, false><<<grid, kThreads, 0, st>>>(src, n, chunk, inva, P, partial, jobs);
     } else if (mode == RMW_MODE_DF64) {
         SrcDF *src = (SrcDF *)base;
         pack_df_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
         Periodic Ps{P.Lx * inva, P.Ly * inva, P.Lz * inva};
         if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
-        if (per) wall_pair_df_kernel<KIND, true><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial);
-        else wall_pair_df_kernel<KIND, false><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial);
+        if (B) wall_pair_df_kernel<KIND, false, true><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial, jobs);
+        else if (per) wall_pair_df_kernel<KIND, true, false><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial, jobs);
+        else wall_pair_df_kernel<KIND, false, false><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial, jobs);
     } else {
         SrcF *src = (SrcF *)base;
         pack_mixed_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
         Periodic Ps{P.Lx * inva, P.Ly * inva, P.Lz * inva};
         if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
-        if (per) wall_pair_mixed_kernel<KIND, true><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial);
-        else wall_pair_mixed_kernel<KIND, false><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial);
+        if (B) wall_pair_mixed_kernel<KIND, false, true><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial, jobs);
+        else if (per) wall_pair_mixed_kernel<KIND, true, false><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial, jobs);
+        else wall_pair_mixed_kernel<KIND, false, false><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial, jobs);
     }
     if (int rc = trace_end(tok, st)) return rc;
-    wall_finalize_kernel<KIND><<<pg, pb, 0, st>>>(r, v, partial, nchunks, out, n, a, nf);
+    wall_finalize_kernel<KIND><<<pg, pb, 0, st>>>(r, v, partial, nchunks, out, n, a, nf, B ? B->blob_nch : nullptr);
     RMW_CHECK_LAUNCH("wall product kernels");
     return RMW_OK;
 }
@@ -463,15 +494,22 @@ int validate_product_args(int kind, const void *r, const void *v, const void *ou
     return RMW_OK;
 }
 
+static int launch_dispatch(int kind, const double *r, const double *v, double *out, int n, double eta, double a,
+                           const double *L, int mode, cudaStream_t st, void *scratch_ptr, int nchunks,
+                           const WallBatch *B)
+{
+    switch (kind) {
+    case RMW_UF: return launch_kind<RMW_UF>(r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks, B);
+    case RMW_UT: return launch_kind<RMW_UT>(r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks, B);
+    case RMW_WF: return launch_kind<RMW_WF>(r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks, B);
+    default: return launch_kind<RMW_WT>(r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks, B);
+    }
+}
+
 int wall_product_with_scratch(int kind, const double *r, const double *v, double *out, int n, double eta, double a,
                               const double *L, int mode, cudaStream_t st, void *scratch_ptr, int nchunks)
 {
-    switch (kind) {
-    case RMW_UF: return launch_kind<RMW_UF>(r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks);
-    case RMW_UT: return launch_kind<RMW_UT>(r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks);
-    case RMW_WF: return launch_kind<RMW_WF>(r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks);
-    default: return launch_kind<RMW_WT>(r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks);
-    }
+    return launch_dispatch(kind, r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks, nullptr);
 }
 
 int wall_product(int kind, const double *r, const double *v, double *out, int64_t n, double eta, double a,
@@ -485,6 +523,74 @@ int wall_product(int kind, const double *r, const double *v, double *out, int64_
     rc = scratch(SCRATCH_PAIR, wall_scratch_bytes((int)n, mode, nchunks), &ws, st);
     if (rc) return rc;
     return wall_product_with_scratch(kind, r, v, out, (int)n, eta, a, L, mode, st, ws, nchunks);
+}
+
+// ---------------------------------------------------------------------------
+// segmented products of many suspensions
+int wall_batch_build(WallBatch &B, const long long *off, int ninst)
+{
+    if (ninst <= 0) return fail(RMW_ERR_ARG, "need at least one suspension");
+    if (off[0] != 0) return fail(RMW_ERR_ARG, "suspension offsets must start at 0");
+    for (int k = 0; k < ninst; ++k)
+        if (off[k + 1] < off[k]) return fail(RMW_ERR_ARG, "suspension offsets must not decrease");
+    if (off[ninst] > (1LL << 28)) return fail(RMW_ERR_ARG, "too many blobs");
+    B.n = (int)off[ninst];
+    B.ninst = ninst;
+    B.off.assign(off, off + ninst + 1);
+    RMW_CUDA(cudaGetDevice(&B.device));
+    // one chunk factor for all suspensions, sized so the whole batch fills the GPU,
+    // never splitting a suspension's sources below 256 per chunk
+    long long tiles = 0;
+    for (int k = 0; k < ninst; ++k) tiles += (off[k + 1] - off[k] + kThreads - 1) / kThreads;
+    const long long want = 152 * 8;
+    const int factor = (int)std::max<long long>(1, std::min<long long>(64, (want + tiles - 1) / std::max(1LL, tiles)));
+    std::vector<TileJob> jobs;
+    std::vector<int> nch(B.n);
+    int max_slots = 1;
+    for (int k = 0; k < ninst; ++k) {
+        const int b0 = (int)off[k], m = (int)(off[k + 1] - off[k]);
+        if (m == 0) continue;
+        const int c = std::max(1, std::min(factor, m / 256));
+        const int chunk = (m + c - 1) / c;
+        max_slots = std::max(max_slots, c);
+        for (int i = b0; i < b0 + m; ++i) nch[i] = c;
+        for (int t = 0; t < m; t += kThreads)
+            for (int q = 0; q < c; ++q) {
+                const int s0 = b0 + q * chunk, s1 = std::min(b0 + m, s0 + chunk);
+                jobs.push_back({b0 + t, std::min(b0 + m, b0 + t + kThreads), s0, std::max(s0, s1), q});
+            }
+    }
+    B.njobs = (int)jobs.size();
+    B.max_slots = max_slots;
+    RMW_CUDA(cudaMalloc(&B.jobs, sizeof(TileJob) * std::max<size_t>(1, jobs.size())));
+    RMW_CUDA(cudaMalloc(&B.blob_nch, sizeof(int) * std::max(1, B.n)));
+    RMW_CUDA(cudaMemcpy(B.jobs, jobs.data(), sizeof(TileJob) * jobs.size(), cudaMemcpyHostToDevice));
+    if (B.n) RMW_CUDA(cudaMemcpy(B.blob_nch, nch.data(), sizeof(int) * B.n, cudaMemcpyHostToDevice));
+    return RMW_OK;
+}
+
+void wall_batch_free(WallBatch &B)
+{
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(B.device);
+    if (B.jobs) cudaFree(B.jobs);
+    if (B.blob_nch) cudaFree(B.blob_nch);
+    cudaSetDevice(cur);
+    B.jobs = nullptr;
+    B.blob_nch = nullptr;
+}
+
+int wall_product_batched(const WallBatch &B, int kind, const double *r, const double *v, double *out, double eta,
+                         double a, int mode, cudaStream_t st)
+{
+    int rc = validate_product_args(kind, r, v, out, B.n, eta, a, mode);
+    if (rc) return rc;
+    if (B.n == 0 || B.njobs == 0) return RMW_OK;
+    void *ws = nullptr;
+    rc = scratch(SCRATCH_PAIR, wall_scratch_bytes(B.n, mode, B.max_slots), &ws, st);
+    if (rc) return rc;
+    return launch_dispatch(kind, r, v, out, B.n, eta, a, nullptr, mode, st, ws, B.max_slots, &B);
 }
 
 }  // namespace rmw
@@ -518,6 +624,40 @@ int rmw_wall_wt(const double *r, const double *v, double *out, int64_t n, double
                 int mode, void *stream)
 {
     return rmw_wall_product(RMW_WT, r, v, out, n, eta, a, L_host, mode, stream);
+}
+
+int rmw_wall_batch_create(void **handle, int64_t n_suspensions, const int64_t *blob_offsets_host)
+{
+    if (!handle || !blob_offsets_host) return rmw::fail(RMW_ERR_ARG, "null argument");
+    *handle = nullptr;
+    if (n_suspensions <= 0 || n_suspensions > (1 << 20)) return rmw::fail(RMW_ERR_ARG, "bad suspension count");
+    std::vector<long long> off(blob_offsets_host, blob_offsets_host + n_suspensions + 1);
+    rmw::WallBatch *B = new rmw::WallBatch();
+    int rc = rmw::wall_batch_build(*B, off.data(), (int)n_suspensions);
+    if (rc) {
+        rmw::wall_batch_free(*B);
+        delete B;
+        return rc;
+    }
+    *handle = B;
+    return RMW_OK;
+}
+
+int rmw_wall_batch_destroy(void *handle)
+{
+    if (handle) {
+        rmw::WallBatch *B = (rmw::WallBatch *)handle;
+        rmw::wall_batch_free(*B);
+        delete B;
+    }
+    return RMW_OK;
+}
+
+int rmw_wall_product_batched(void *handle, int kind, const double *r, const double *v, double *out, double eta,
+                             double a, int mode, void *stream)
+{
+    if (!handle) return rmw::fail(RMW_ERR_ARG, "null batch handle");
+    return rmw::wall_product_batched(*(rmw::WallBatch *)handle, kind, r, v, out, eta, a, mode, rmw::as_stream(stream));
 }
 
 int rmw_wall_product_host(int kind, const double *r_host, const double *v_host, double *out_host, int64_t n,

@@ -2,7 +2,33 @@
 #pragma once
 #include "rmw_common.cuh"
 
+#include <vector>
+
 namespace rmw {
+
+// One CTA of a segmented (batched) product: targets [t0, t1) against sources
+// [s0, s1) of the same suspension, partial sums into chunk slot `slot`.
+struct TileJob {
+    int t0, t1, s0, s1, slot;
+};
+
+// Segmented product layout for many independent suspensions of one blob
+// array: suspension k owns blobs [off[k], off[k+1]) and only interacts with
+// itself.  Built once (rmw_wall_batch_create) and reused by every product.
+struct WallBatch {
+    int n = 0;          // total blobs
+    int ninst = 0;      // suspensions
+    int njobs = 0;      // CTAs per product
+    int max_slots = 1;  // chunk slots of the partial-sum buffer
+    TileJob *jobs = nullptr;  // device
+    int *blob_nch = nullptr;  // device: chunk count of each blob's suspension
+    std::vector<long long> off;
+    int device = 0;
+};
+int wall_batch_build(WallBatch &B, const long long *off_host, int ninst);
+void wall_batch_free(WallBatch &B);
+int wall_product_batched(const WallBatch &B, int kind, const double *r, const double *v, double *out, double eta,
+                         double a, int mode, cudaStream_t st);
 
 // Source-chunk count the standard entry points use for n blobs.
 int wall_default_chunks(int n);

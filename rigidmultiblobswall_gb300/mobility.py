@@ -89,6 +89,41 @@ def wall_product(kind, r_vectors, vector, eta, a, **kwargs):
     return out
 
 
+class SuspensionBatch:
+    """Segmented products of many independent suspensions stored in one (N,3)
+    array: suspension k owns blobs [blob_offsets[k], blob_offsets[k+1]) and
+    interacts only with itself.  One launch serves all suspensions."""
+
+    def __init__(self, blob_offsets):
+        off = np.ascontiguousarray(blob_offsets, dtype=np.int64).reshape(-1)
+        h = ctypes.c_void_p()
+        _native.call("rmw_wall_batch_create", ctypes.byref(h), off.size - 1, off.ctypes.data_as(ctypes.c_void_p))
+        self._h = h
+        self.offsets = off
+        self.n = int(off[-1])
+
+    def __del__(self):
+        try:
+            if self._h is not None and self._h.value:
+                _native.load().rmw_wall_batch_destroy(self._h)
+        except Exception:
+            pass
+
+    def product(self, kind, r_vectors, vector, eta, a, mode="fp64"):
+        """Block-diagonal B M B v (CUDA torch tensors in and out)."""
+        import torch
+        r = torch.as_tensor(r_vectors, dtype=torch.float64).reshape(-1, 3).contiguous()
+        v = torch.as_tensor(vector, dtype=torch.float64).reshape(-1).contiguous()
+        if not (r.is_cuda and v.is_cuda) or r.shape[0] != self.n or v.numel() != 3 * self.n:
+            raise ValueError("expected CUDA tensors of the batch's size")
+        out = torch.empty(3 * self.n, dtype=torch.float64, device=r.device)
+        with torch.cuda.device(r.device):
+            _native.call("rmw_wall_product_batched", self._h, _native.KINDS[kind], r.data_ptr(), v.data_ptr(),
+                         out.data_ptr(), float(eta), float(a), _MODES[mode],
+                         torch.cuda.current_stream(r.device).cuda_stream)
+        return out
+
+
 # ---------------------------------------------------------------------------
 # wall regularisation helpers (mobility/mobility.py:52-84)
 def shift_heights(r_vectors, blob_radius, *args, **kwargs):

@@ -168,6 +168,39 @@ class RigidSystem:
                      self.stream.cuda_stream)
         return c.value
 
+    # -- independent suspensions -----------------------------------------------
+    def set_suspensions(self, bodies_per_suspension):
+        """Declare consecutive groups of bodies as independent suspensions
+        (block-diagonal mobility); enables solve_batched."""
+        counts = np.asarray(bodies_per_suspension, dtype=np.int64).reshape(-1)
+        if counts.sum() != self.n_bodies or (counts < 0).any():
+            raise ValueError("suspension body counts must add up to the number of bodies")
+        off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+        _native.call("rmw_rigid_set_suspensions", self._h, counts.size, off.ctypes.data_as(ctypes.c_void_p))
+        self.suspension_body_offsets = off
+        blob_off = self.offsets[off]
+        self.suspension_blob_offsets = blob_off
+        self.n_suspensions = int(counts.size)
+
+    def solve_batched(self, rhs, tol=1e-8, restart=60, maxiter=1000, mode="fp64"):
+        """Every suspension solved by its own GMRES (lockstep).  Returns
+        (solution, iterations[k], relative residual[k], status[k]); status 0 = converged."""
+        import torch
+        b = _dev(rhs, self.device).reshape(-1)
+        x = self._out(self.size)
+        k = self.n_suspensions
+        it = np.zeros(k, dtype=np.int32)
+        rr = np.zeros(k)
+        stt = np.zeros(k, dtype=np.int32)
+        with torch.cuda.device(self.device):
+            rc = _native.load().rmw_rigid_solve_batched(
+                self._h, b.data_ptr(), x.data_ptr(), float(tol), int(restart), int(maxiter), _mode(mode),
+                it.ctypes.data_as(ctypes.c_void_p), rr.ctypes.data_as(ctypes.c_void_p),
+                stt.ctypes.data_as(ctypes.c_void_p))
+        if rc not in (_native.RMW_OK, _native.RMW_ERR_NOT_CONVERGED):
+            _native.check(rc)
+        return x, it, rr, stt
+
     # -- solvers -----------------------------------------------------------------
     def solve(self, rhs, tol=1e-8, restart=60, maxiter=1000, mode="fp64", raise_on_fail=False):
         """GMRES with the block-diagonal preconditioner.  Returns (solution, info, iterations, rel_residual);

@@ -39,10 +39,16 @@ def test_products_match_reference_golden(cuda_device, kind, case, mode):
     assert rel_err(out, g[case + "_" + kind]) <= TOL[mode]
 
 
+@pytest.mark.parametrize("damped", [False, True])
 @pytest.mark.parametrize("mode", ["fp64", "df64", "mixed"])
 @pytest.mark.parametrize("kind", KINDS)
-def test_plain_matvec_workload_matches_oracle(cuda_device, kind, mode):
+def test_plain_matvec_workload_matches_oracle(cuda_device, kind, mode, damped):
+    """2048 free blobs; with damped=True every 17th blob sits at z = 0.3a
+    (wall regularisation on), where the far-field wall image nearly cancels
+    the free-space term and exposes any precision leak in the pair algebra."""
     r, f, eta, a = S.blobs_wall_matvec(2048, seed=0)
+    if damped:
+        r[::17, 2] = 0.3 * a
     ref = wall.wall_product(kind, r, f, eta, a)
     assert rel_err(FN[kind](r, f, eta, a, mode=mode), ref) <= TOL[mode]
 

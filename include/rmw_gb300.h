@@ -88,6 +88,14 @@ int rmw_wall_batch_destroy(void *handle);
 int rmw_wall_product_batched(void *handle, int kind, const double *r, const double *v, double *out, double eta,
                              double a, int mode, void *stream);
 
+/* M_UF applied to nrhs vectors at once (V and Y: nrhs rows of 3n doubles),
+ * mixed precision (<= 1e-6): each pair block is formed once and applied to
+ * every vector.  batch may be NULL or a rmw_wall_batch_create handle
+ * (segmented).  Serves multi-right-hand-side Lanczos; no reference
+ * counterpart. */
+int rmw_wall_uf_multi(const double *r, const double *V, double *Y, int64_t n, int nrhs, double eta, double a,
+                      void *batch, void *stream);
+
 /* Host-buffer form: the drop-in for the reference's pycuda wrappers, which
  * copy host arrays to the device, launch, and copy the result back on every
  * call (mobility/mobility_pycuda.py:2235-2267).  Synchronous.  Pinned or
@@ -188,6 +196,16 @@ int rmw_rigid_set_suspensions(void *handle, int64_t n_suspensions, const int64_t
  * suspension).  Synchronous; returns RMW_OK when every suspension converged. */
 int rmw_rigid_solve_batched(void *handle, const double *rhs, double *sol, double tol, int restart, int maxiter,
                             int mode, int *iters_host, double *relres_host, int *status_host);
+
+/* Lanczos Brownian noise for nrhs right-hand sides of every suspension:
+ * noise_q = factor * L (L^-1 M L^-T)^(1/2) z_q per suspension (the det_stoch
+ * preconditioned stochastic_forcing_lanczos, stochastic_forcing.py:112-264),
+ * all (suspension, right-hand side) recurrences in lockstep with one
+ * multi-right-hand-side operator application per step.  Z, noise: nrhs rows
+ * of 3N doubles.  iters_host: nrhs * n_suspensions entries.  The basis is
+ * capped at 96 vectors.  Synchronous. */
+int rmw_rigid_lanczos_batched(void *handle, const double *Z, double *noise, int nrhs, double factor, double tol,
+                              int max_iter, int mode, int *iters_host);
 
 /* ---- generic Krylov solvers with caller-supplied operators ------------
  * op(ctx, x, y) must write y = A x for device vectors of length n, enqueue its

@@ -48,6 +48,7 @@ SIGNATURES = {
     "rmw_wall_batch_create": (_i, [ctypes.POINTER(ctypes.c_void_p), _i64, _vp]),
     "rmw_wall_batch_destroy": (_i, [_vp]),
     "rmw_wall_product_batched": (_i, [_vp, _i, _vp, _vp, _vp, _d, _d, _i, _vp]),
+    "rmw_wall_uf_multi": (_i, [_vp, _vp, _vp, _i64, _i, _d, _d, _vp, _vp]),
     "rmw_wall_product_host": (_i, [_i, _vp, _vp, _vp, _i64, _d, _d, _vp, _i]),
     "rmw_rigid_create": (_i, [ctypes.POINTER(ctypes.c_void_p), _i64, _vp, _d, _d, _vp, _vp]),
     "rmw_rigid_destroy": (_i, [_vp]),
@@ -71,6 +72,7 @@ SIGNATURES = {
                               ctypes.POINTER(ctypes.c_int)]),
     "rmw_rigid_set_suspensions": (_i, [_vp, _i64, _vp]),
     "rmw_rigid_solve_batched": (_i, [_vp, _vp, _vp, _d, _i, _i, _i, _vp, _vp, _vp]),
+    "rmw_rigid_lanczos_batched": (_i, [_vp, _vp, _vp, _i, _d, _d, _i, _i, _vp]),
     "rmw_gmres": (_i, [_i64, _vp, _vp, _vp, _vp, _vp, _vp, _d, _i, _i, _vp, ctypes.POINTER(ctypes.c_int),
                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _i]),
     "rmw_lanczos": (_i, [_i64, _vp, _vp, _vp, _vp, _d, _d, _i, _vp, ctypes.POINTER(ctypes.c_int)]),

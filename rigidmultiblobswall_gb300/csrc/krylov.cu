@@ -448,6 +448,11 @@ static bool tridiag_eigen(std::vector<double> &d, std::vector<double> e, std::ve
     return true;
 }
 
+bool tridiag_eigen_host(std::vector<double> &d, std::vector<double> e, std::vector<double> &z)
+{
+    return tridiag_eigen(d, std::move(e), z);
+}
+
 // Lanczos noise = factor * M^(1/2) z (op: y = M x).  z and noise are device vectors.
 template <typename Op>
 static int lanczos(Op op, const double *z, double *noise, long long n, double factor, double tol, int max_iter,

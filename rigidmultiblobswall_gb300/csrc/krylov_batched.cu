@@ -431,6 +431,129 @@ static int gmres_batched(Op op, Pc pc, const double *b, double *x_out, const std
     return RMW_OK;
 }
 
+// implicit-QL eigen-decomposition of a symmetric tridiagonal matrix (krylov.cu)
+bool tridiag_eigen_host(std::vector<double> &d, std::vector<double> e, std::vector<double> &z);
+
+// Lockstep Lanczos over independent segments (one per suspension and right-
+// hand side): each segment has its own recurrence, tridiagonal matrix,
+// eigen-decomposition and convergence test (stochastic_forcing.py:112-264),
+// the operator is applied to all of them at once.  Converged segments are
+// frozen by zeroing their part of the next basis vector.
+template <typename Op>
+static int lanczos_batched(Op op, const double *z, double *noise, const std::vector<long long> &off, double factor,
+                           double tol, int max_iter, cudaStream_t st, std::vector<int> &iters)
+{
+    const int nseg = (int)off.size() - 1;
+    const long long n = off.back();
+    const long long ldv = ((n + 31) / 32) * 32;
+    const int kcap = std::max(2, std::min(max_iter + 1, 96));
+    const int HD = 0, HS = 1, ZN = 2, CF = 8;  // per-segment scalars; CF: coefficients (kcap)
+    const int stride = CF + 2 * kcap + 8;
+    SegOps O;
+    if (int rc = O.init(off, stride, st)) return rc;
+    int vcap = std::min(kcap + 1, 16);
+    double *V = nullptr, *w = nullptr;
+    RMW_CUDA(cudaMallocAsync(&w, sizeof(double) * ldv, st));
+    RMW_CUDA(cudaMallocAsync(&V, sizeof(double) * ldv * vcap, st));
+    struct Free {
+        double **a, **b;
+        cudaStream_t s;
+        ~Free() { if (*a) cudaFreeAsync(*a, s); if (*b) cudaFreeAsync(*b, s); }
+    } fr{&V, &w, st};
+    if (int rc = O.norm2(z, ZN)) return rc;
+    if (int rc = O.fetch()) return rc;
+    std::vector<double> zn(nseg);
+    std::vector<char> active(nseg, 0);
+    iters.assign(nseg, max_iter);
+    for (int k = 0; k < nseg; ++k) {
+        zn[k] = std::sqrt(O.h(k, ZN));
+        if (!std::isfinite(zn[k])) return fail(RMW_ERR_NONFINITE, "batched Lanczos: z not finite");
+        active[k] = zn[k] > 0.0 && factor != 0.0;
+        if (!active[k]) iters[k] = 0;
+        O.h(k, HD) = active[k] ? 1.0 / zn[k] : 0.0;
+        for (int q = 0; q < kcap; ++q) O.h(k, CF + q) = 0.0;
+    }
+    if (int rc = O.put()) return rc;
+    if (int rc = O.scale(z, V, HD, false)) return rc;
+    std::vector<std::vector<double>> hd(nseg), hs(nseg), cold(nseg), cfin(nseg);
+    int kmax_used = 1;
+    for (int i = 0; i <= max_iter && i < kcap; ++i) {
+        int n_active = 0;
+        for (int k = 0; k < nseg; ++k) n_active += active[k];
+        if (!n_active) break;
+        double *Vi = V + (long long)i * ldv;
+        if (int rc = op(Vi, w)) return rc;
+        if (i > 0) {  // w -= hs[i-1] V_{i-1}
+            if (int rc = O.fetch()) return rc;
+            for (int k = 0; k < nseg; ++k) O.h(k, HS) = active[k] ? hs[k][i - 1] : 0.0;
+            if (int rc = O.put()) return rc;
+            if (int rc = O.update(V + (long long)(i - 1) * ldv, ldv, 1, HS, w, -1)) return rc;
+        }
+        if (int rc = O.dots(Vi, ldv, 1, w, HD)) return rc;        // hd = <w, V_i>
+        if (int rc = O.update(Vi, ldv, 1, HD, w, ZN)) return rc;  // w -= hd V_i ; |w|^2
+        if (int rc = O.scale(w, w, ZN, true)) return rc;          // w /= |w|
+        if (int rc = O.fetch()) return rc;
+        for (int k = 0; k < nseg; ++k) {
+            if (!active[k]) continue;
+            hd[k].push_back(O.h(k, HD));
+            const double wn = std::sqrt(O.h(k, ZN));
+            hs[k].push_back(wn);
+            if (!std::isfinite(wn) || !std::isfinite(hd[k].back()))
+                return fail(RMW_ERR_BREAKDOWN, "batched Lanczos: non-finite value");
+            std::vector<double> dd(hd[k]), ee(hs[k].begin(), hs[k].begin() + i), zq;
+            if (!tridiag_eigen_host(dd, ee, zq)) return fail(RMW_ERR_BREAKDOWN, "batched Lanczos: eigensolver");
+            const int kk = i + 1;
+            std::vector<double> c(kk, 0.0);
+            for (int j = 0; j < kk; ++j) {
+                const double lam = dd[j] > 0 ? std::sqrt(dd[j]) : 0.0;
+                const double w1 = zq[(size_t)kk * j] * lam * zn[k] * factor;
+                for (int q = 0; q < kk; ++q) c[q] += zq[q + (size_t)kk * j] * w1;
+            }
+            bool conv = false;
+            if (i > 0) {
+                double dn = 0.0, on = 0.0;
+                for (int q = 0; q < kk; ++q) {
+                    const double co = q < (int)cold[k].size() ? cold[k][q] : 0.0;
+                    dn += (c[q] - co) * (c[q] - co);
+                    on += co * co;
+                }
+                conv = std::sqrt(dn) / std::max(std::sqrt(on), 2.220446049250313e-16) < tol;
+            }
+            cold[k] = c;
+            cfin[k] = c;
+            if (conv || wn == 0.0) {
+                iters[k] = i;
+                active[k] = 0;
+            }
+        }
+        kmax_used = i + 1;
+        // reorthogonalise w against V_0..V_i (one pass) -> V_{i+1}; frozen segments get zeros
+        if (int rc = O.dots(V, ldv, i + 1, w, CF + kcap)) return rc;
+        if (int rc = O.update(V, ldv, i + 1, CF + kcap, w, -1)) return rc;
+        if (i + 2 > vcap) {
+            const int ncap = std::min(kcap + 1, 2 * vcap);
+            double *nv = nullptr;
+            RMW_CUDA(cudaMallocAsync(&nv, sizeof(double) * ldv * ncap, st));
+            RMW_CUDA(cudaMemcpyAsync(nv, V, sizeof(double) * ldv * vcap, cudaMemcpyDeviceToDevice, st));
+            RMW_CUDA(cudaFreeAsync(V, st));
+            V = nv;
+            vcap = ncap;
+        }
+        if (int rc = O.fetch()) return rc;
+        for (int k = 0; k < nseg; ++k) O.h(k, HD) = active[k] ? 1.0 : 0.0;
+        if (int rc = O.put()) return rc;
+        if (int rc = O.scale(w, V + (long long)(i + 1) * ldv, HD, false)) return rc;
+    }
+    // noise = V c per segment
+    if (int rc = O.fetch()) return rc;
+    for (int k = 0; k < nseg; ++k)
+        for (int q = 0; q < kcap; ++q) O.h(k, CF + q) = q < (int)cfin[k].size() ? cfin[k][q] : 0.0;
+    if (int rc = O.put()) return rc;
+    if (int rc = O.combine(V, ldv, kmax_used, CF, noise)) return rc;
+    RMW_CUDA(cudaStreamSynchronize(st));
+    return RMW_OK;
+}
+
 }  // namespace rmw
 
 // ---------------------------------------------------------------------------
@@ -582,6 +705,43 @@ done:
     }
     if (worst != RMW_OK) rmw::set_error("some suspensions did not reach the tolerance");
     return worst;
+}
+
+// Lanczos noise for nrhs right-hand sides of every suspension of the handle:
+// noise_q = factor * L (L^-1 M L^-T)^(1/2) z_q restricted to each suspension,
+// i.e. stochastic_forcing_lanczos with the det_stoch preconditioner, run for
+// every (suspension, right-hand side) pair in lockstep.  Z and noise hold nrhs
+// rows of 3N doubles; iters_host receives nrhs * n_suspensions counts
+// (row-major by right-hand side).
+int rmw_rigid_lanczos_batched(void *sys, const double *Z, double *noise, int nrhs, double factor, double tol,
+                              int max_iter, int mode, int *iters_host)
+{
+    if (!sys || !Z || !noise) return rmw::fail(RMW_ERR_ARG, "null argument");
+    if (nrhs < 1 || max_iter < 1) return rmw::fail(RMW_ERR_ARG, "nrhs and max_iter must be positive");
+    RigidSystem &S = *(RigidSystem *)sys;
+    if (!S.batch) return rmw::fail(RMW_ERR_ARG, "call rmw_rigid_set_suspensions first");
+    if (!S.stoch_ready) {
+        if (int rc = rmw_rigid_build_pc(sys, 1)) return rc;
+    }
+    const int nsusp = (int)S.susp_body_off.size() - 1;
+    const long long N3 = 3LL * S.n;
+    std::vector<long long> off((size_t)nrhs * nsusp + 1);
+    for (int q = 0; q < nrhs; ++q)
+        for (int k = 0; k < nsusp; ++k) off[(size_t)q * nsusp + k] = q * N3 + 3LL * S.batch->off[k];
+    off[(size_t)nrhs * nsusp] = (long long)nrhs * N3;
+    double *buf = nullptr;
+    RMW_CUDA(cudaMallocAsync(&buf, sizeof(double) * 2 * nrhs * N3, S.st));
+    double *tmp = buf, *raw = buf + nrhs * N3;
+    auto op = [&](const double *x, double *y) { return rmw::rigid_mobility_pc_multi(S, x, y, nrhs, mode, tmp); };
+    std::vector<int> it;
+    int rc = rmw::lanczos_batched(op, Z, raw, off, factor, tol, max_iter, S.st, it);
+    if (rc == RMW_OK) rc = rmw::rigid_P_inv_mult_multi(S, raw, noise, nrhs);
+    cudaFreeAsync(buf, S.st);
+    cudaStreamSynchronize(S.st);
+    if (rc) return rc;
+    if (iters_host)
+        for (size_t k = 0; k < it.size(); ++k) iters_host[k] = it[k];
+    return RMW_OK;
 }
 
 }  // extern "C"

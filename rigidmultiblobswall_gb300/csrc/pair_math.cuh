@@ -126,6 +126,61 @@ __device__ __forceinline__ void pair_contrib(T dx, T dy, T dz, T Rz, T hi, T hj,
     }
 }
 
+// Vector-independent part of one M_UF block, for products with several
+// right-hand sides:  M v = Af v + (Bc (d.v) + c2 W + c3 vz) (dx, dy, .) ...
+// with W = dx vx + dy vy + Rz vz (see uf_apply).
+template <typename T> struct UFCoeffs {
+    T Af, Bc, c2, c3, c4, f5;
+};
+
+template <typename T>
+__device__ __forceinline__ UFCoeffs<T> uf_coeffs(T dx, T dy, T dz, T Rz, T hi, T hj)
+{
+    const T rho2 = dx * dx + dy * dy;
+    const T r2 = rho2 + dz * dz;
+    const T invr = rsq<T>(r2);
+    const T r = r2 * invr;
+    const T Rz2 = Rz * Rz;
+    const T s = rsq<T>(rho2 + Rz2);
+    const T s2 = s * s;
+    const T s3 = s2 * s;
+    const T E = Rz2 * s2;
+    const T invr2 = invr * invr;
+    T A = (T(1) + T(2.0 / 3.0) * invr2) * invr;
+    T Bc = (T(1) - T(2) * invr2) * invr2 * invr;
+    const bool near = !(r > T(2));
+    if (__any_sync(__activemask(), near)) {
+        if (near) {
+            A = T(4.0 / 3.0) * (T(1) - T(0.28125) * r);
+            Bc = T(0.125) * invr;
+        }
+    }
+    const T s5 = s3 * s2;
+    const T hh = hi * hj * s2;
+    const T ez = Rz * s;
+    const T q5 = (T(1) - T(5) * E) * s3;
+    const T f1 = -((T(1) + T(2) * hh) * s + T(2.0 / 3.0) * ((T(1) - T(3) * E) * s3 - q5 * s2));
+    const T f2 = -((T(1) - T(6) * hh) * s - T(2) * q5 + T(10.0 / 3.0) * (T(1) - T(7) * E) * s5);
+    const T f3 = T(2.0 / 3.0) * (T(3) * hj * s2 - T(18) * hh * ez * s + ez * (T(10) * (T(2) - T(7) * E) * s5 - T(6) * q5));
+    const T f4 = T(2.0 / 3.0) * (T(3) * hj * s2 - T(10) * ez * s5);
+    const T f5 = T(-4.0 / 3.0) * (T(3) * (hj * hj + E) * s3 + (T(2) - T(15) * E) * s5);
+    return {A + f1, Bc, f2 * s2, f3 * s, f4 * s, f5};
+}
+
+template <typename T>
+__device__ __forceinline__ void uf_apply(const UFCoeffs<T> &c, T dx, T dy, T dz, T Rz, T vx, T vy, T vz, T &ux,
+                                         T &uy, T &uz)
+{
+    const T Pxy = dx * vx + dy * vy;
+    const T Gr = c.Bc * (Pxy + dz * vz);
+    const T W = Pxy + Rz * vz;
+    const T Gw = c.c2 * W + c.c3 * vz;
+    const T G = Gr + Gw;
+    ux += c.Af * vx + G * dx;
+    uy += c.Af * vy + G * dy;
+    uz += c.Af * vz + Gr * dz + Gw * Rz + c.c4 * W + c.f5 * vz;
+}
+
 // Minimum-image projection of mobility/mobility_numba.py (int() truncates toward zero).
 template <typename T> __device__ __forceinline__ T project(T d, T L)
 {

@@ -347,13 +347,16 @@ __global__ void pc_apply_kernel(const double *__restrict__ x, double *__restrict
     }
 }
 
-// y_b = T_b x_b (T lower triangular, row-major) or T_b^T x_b, per body
+// y_b = T_b x_b (T lower triangular, row-major) or T_b^T x_b, per body;
+// blockIdx.y selects one of several vectors (stride ld)
 __global__ void block_tri_mult_kernel(const double *__restrict__ T, const long long *__restrict__ moff,
                                       const int *__restrict__ boff, const double *__restrict__ x,
-                                      double *__restrict__ y, int transpose)
+                                      double *__restrict__ y, int transpose, long long ld)
 {
     extern __shared__ double xs[];
     const int b = blockIdx.x;
+    x += (long long)blockIdx.y * ld;
+    y += (long long)blockIdx.y * ld;
     const int o = boff[b], m = 3 * (boff[b + 1] - o);
     const double *Tb = T + moff[b];
     for (int t = threadIdx.x; t < m; t += blockDim.x) xs[t] = x[3LL * o + t];
@@ -505,10 +508,10 @@ int rigid_apply_pc(RigidSystem &S, const double *x, double *y)
     return RMW_OK;
 }
 
-static int tri_mult(RigidSystem &S, const double *T, const double *x, double *y, int transpose)
+static int tri_mult(RigidSystem &S, const double *T, const double *x, double *y, int transpose, int nvec = 1)
 {
     const size_t sm = sizeof(double) * (size_t)S.max_m;
-    block_tri_mult_kernel<<<S.nb, 128, sm, S.st>>>(T, S.moff, S.boff, x, y, transpose);
+    block_tri_mult_kernel<<<dim3(S.nb, nvec), 128, sm, S.st>>>(T, S.moff, S.boff, x, y, transpose, 3LL * S.n);
     RMW_CHECK_LAUNCH("block triangular multiply");
     return RMW_OK;
 }
@@ -521,6 +524,26 @@ int rigid_mobility_pc(RigidSystem &S, const double *w, double *y, int mode)
     if (int rc = rigid_mobility(S, S.tmp3n, y, mode)) return rc;
     // in place is safe per body: each CTA stages its own slice in shared memory first
     return tri_mult(S, S.linv, y, y, 0);
+}
+
+int rigid_mobility_pc_multi(RigidSystem &S, const double *W, double *Y, int nvec, int mode, double *tmp)
+{
+    if (!S.stoch_ready) return fail(RMW_ERR_ARG, "stochastic preconditioner not built");
+    const long long ld = 3LL * S.n;
+    if (int rc = tri_mult(S, S.linv, W, tmp, 1, nvec)) return rc;
+    if (mode == RMW_MODE_MIXED) {
+        if (int rc = wall_uf_multi(S.r, tmp, ld, Y, ld, nvec, S.n, S.eta, S.a, S.batch, S.st)) return rc;
+    } else {
+        for (int q = 0; q < nvec; ++q)
+            if (int rc = rigid_mobility(S, tmp + q * ld, Y + q * ld, mode)) return rc;
+    }
+    return tri_mult(S, S.linv, Y, Y, 0, nvec);
+}
+
+int rigid_P_inv_mult_multi(RigidSystem &S, const double *W, double *Y, int nvec)
+{
+    if (!S.stoch_ready) return fail(RMW_ERR_ARG, "stochastic preconditioner not built");
+    return tri_mult(S, S.lfac, W, Y, 0, nvec);
 }
 
 int rigid_P_inv_mult(RigidSystem &S, const double *w, double *y)

@@ -52,6 +52,10 @@ int rigid_apply_pc(RigidSystem &S, const double *x, double *y);
 int rigid_mobility_pc(RigidSystem &S, const double *w, double *y, int mode);
 // y = L w (det_stoch P_inv_mult, multi_bodies.py:609-615).
 int rigid_P_inv_mult(RigidSystem &S, const double *w, double *y);
+// nvec vectors (stride 3N) at once; tmp holds nvec * 3N doubles.  Mixed mode
+// uses the multi-right-hand-side pair kernel.
+int rigid_mobility_pc_multi(RigidSystem &S, const double *W, double *Y, int nvec, int mode, double *tmp);
+int rigid_P_inv_mult_multi(RigidSystem &S, const double *W, double *Y, int nvec);
 // M v on the handle's blobs (segmented by suspension when suspensions are set).
 int rigid_mobility(RigidSystem &S, const double *v, double *y, int mode);
 

@@ -373,6 +373,136 @@ __global__ void __launch_bounds__(kThreads) wall_pair_mixed_kernel(const SrcF *_
 }
 
 // ---------------------------------------------------------------------------
+// Multi-right-hand-side M_UF product (mixed precision): the vector-independent
+// part of each pair block is computed once and applied to kMultiRhs vectors.
+// vec[j * kMultiRhs + q] holds b_j v_q,j (float4, w unused).
+constexpr int kMultiRhs = 8;
+
+__global__ void pack_multi_kernel(const double *__restrict__ r, const double *__restrict__ V, long long ldv, int nrhs,
+                                  SrcF *__restrict__ src, float4 *__restrict__ vec, int n, double a)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double inva = 1.0 / a;
+    const double z = r[3 * i + 2];
+    const double b = (z < a) ? z / a : 1.0;
+    const double ze = (z <= a) ? a : z;
+    const double xs = r[3 * i] * inva, ys = r[3 * i + 1] * inva, zs = ze * inva;
+    const float xh = (float)xs, yh = (float)ys, zh = (float)zs;
+    SrcF s;
+    s.hi = make_float4(xh, yh, zh, 0.f);
+    s.lo = make_float4((float)(xs - (double)xh), (float)(ys - (double)yh), (float)(zs - (double)zh), 0.f);
+    s.v = make_float4(0.f, 0.f, 0.f, 0.f);
+    src[i] = s;
+    for (int q = 0; q < kMultiRhs; ++q) {
+        float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (q < nrhs) {
+            const double *v = V + (long long)q * ldv + 3LL * i;
+            w = make_float4((float)(b * v[0]), (float)(b * v[1]), (float)(b * v[2]), 0.f);
+        }
+        vec[(long long)i * kMultiRhs + q] = w;
+    }
+}
+
+template <bool SEG>
+__global__ void __launch_bounds__(kThreads) wall_pair_multi_kernel(const SrcF *__restrict__ src,
+                                                                    const float4 *__restrict__ vec, int n, int chunk,
+                                                                    double *__restrict__ partial,
+                                                                    const TileJob *__restrict__ jobs)
+{
+    __shared__ float4 tpos[2 * kTile / 2];      // hi, lo of kTile/2 sources
+    __shared__ float4 tvec[kTile / 2 * kMultiRhs];
+    const PairRange pr = pair_range<SEG>(jobs, n, chunk);
+    const int i = pr.tbeg + threadIdx.x;
+    const bool valid = i < pr.tend;
+    float4 mh = make_float4(0.f, 0.f, 1.f, 0.f), ml = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (valid) { mh = src[i].hi; ml = src[i].lo; }
+    const float hi = mh.z + ml.z;
+    float sh_[kMultiRhs][3], sl_[kMultiRhs][3];
+#pragma unroll
+    for (int q = 0; q < kMultiRhs; ++q)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) sh_[q][c] = sl_[q][c] = 0.f;
+    constexpr int kT = kTile / 2;
+    for (int t0 = pr.j0; t0 < pr.j1; t0 += kT) {
+        const int cnt = min(kT, pr.j1 - t0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt; k += kThreads) {
+            tpos[2 * k] = src[t0 + k].hi;
+            tpos[2 * k + 1] = src[t0 + k].lo;
+        }
+        for (int k = threadIdx.x; k < cnt * kMultiRhs; k += kThreads) tvec[k] = vec[(long long)t0 * kMultiRhs + k];
+        __syncthreads();
+        float acc[kMultiRhs][3];
+#pragma unroll
+        for (int q = 0; q < kMultiRhs; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.f;
+        for (int k = 0; k < cnt; ++k) {
+            const float4 shp = tpos[2 * k], slp = tpos[2 * k + 1];
+            const int j = t0 + k;
+            const float dx = (mh.x - shp.x) + (ml.x - slp.x);
+            const float dy = (mh.y - shp.y) + (ml.y - slp.y);
+            const float dz = (mh.z - shp.z) + (ml.z - slp.z);
+            const float hj = shp.z + slp.z;
+            const float Rz = hi + hj;
+            const UFCoeffs<float> c = uf_coeffs<float>(dx, dy, dz, Rz, hi, hj);
+            const bool use = (j != i);
+#pragma unroll
+            for (int q = 0; q < kMultiRhs; ++q) {
+                const float4 v = tvec[k * kMultiRhs + q];
+                float cx = 0.f, cy = 0.f, cz = 0.f;
+                uf_apply<float>(c, dx, dy, dz, Rz, v.x, v.y, v.z, cx, cy, cz);
+                if (use) { acc[q][0] += cx; acc[q][1] += cy; acc[q][2] += cz; }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kMultiRhs; ++q)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) comp_add(sh_[q][c], sl_[q][c], acc[q][c]);
+    }
+    if (valid) {
+#pragma unroll
+        for (int q = 0; q < kMultiRhs; ++q) {
+            double *o = partial + ((size_t)pr.slot * kMultiRhs + q) * 3 * n + 3 * (size_t)i;
+            o[0] = (double)sh_[q][0] + (double)sl_[q][0];
+            o[1] = (double)sh_[q][1] + (double)sl_[q][1];
+            o[2] = (double)sh_[q][2] + (double)sl_[q][2];
+        }
+    }
+}
+
+// out[q][3i..] = b_i nf (sum_slots partial + self block (b_i v_q,i)) for q < nrhs
+__global__ void wall_finalize_multi_kernel(const double *__restrict__ r, const double *__restrict__ V, long long ldv,
+                                           int nrhs, const double *__restrict__ partial, int nchunks,
+                                           double *__restrict__ out, long long ldo, int n, double a, double nf,
+                                           const int *__restrict__ blob_nchunks)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    if (i >= n || q >= nrhs) return;
+    const int nc = blob_nchunks ? blob_nchunks[i] : nchunks;
+    double ux = 0.0, uy = 0.0, uz = 0.0;
+    for (int s = 0; s < nc; ++s) {
+        const double *p = partial + ((size_t)s * kMultiRhs + q) * 3 * n + 3 * (size_t)i;
+        ux += p[0]; uy += p[1]; uz += p[2];
+    }
+    const double z = r[3 * i + 2];
+    const double b = (z < a) ? z / a : 1.0;
+    const double ze = (z <= a) ? a : z;
+    const double *v = V + (long long)q * ldv + 3LL * i;
+    const double iz = a / ze, iz3 = iz * iz * iz, iz5 = iz3 * iz * iz;
+    const double mxx = 4.0 / 3.0 - (9.0 * iz - 2.0 * iz3 + iz5) / 12.0;
+    const double mzz = 4.0 / 3.0 - (9.0 * iz - 4.0 * iz3 + iz5) / 6.0;
+    ux += mxx * b * v[0];
+    uy += mxx * b * v[1];
+    uz += mzz * b * v[2];
+    double *o = out + (long long)q * ldo + 3LL * i;
+    const double sc = b * nf;
+    o[0] = ux * sc;
+    o[1] = uy * sc;
+    o[2] = uz * sc;
+}
+
+// ---------------------------------------------------------------------------
 // finalize: fixed-order chunk sum + FP64 self term + b_i * norm factor.
 template <int KIND>
 __global__ void wall_finalize_kernel(const double *__restrict__ r, const double *__restrict__ v,
@@ -593,6 +723,40 @@ int wall_product_batched(const WallBatch &B, int kind, const double *r, const do
     return launch_dispatch(kind, r, v, out, B.n, eta, a, nullptr, mode, st, ws, B.max_slots, &B);
 }
 
+// M_UF applied to nrhs vectors (rows of V with stride ldv; outputs rows of Y
+// with stride ldy), mixed precision, kMultiRhs vectors per pass.
+int wall_uf_multi(const double *r, const double *V, long long ldv, double *Y, long long ldy, int nrhs, int n,
+                  double eta, double a, const WallBatch *B, cudaStream_t st)
+{
+    if (nrhs <= 0 || n <= 0) return RMW_OK;
+    const int nchunks = B ? B->max_slots : choose_chunks(n);
+    const size_t pos = ((sizeof(SrcF) * (size_t)n + 255) / 256) * 256;
+    const size_t vecb = ((sizeof(float4) * (size_t)n * kMultiRhs + 255) / 256) * 256;
+    const size_t bytes = pos + vecb + sizeof(double) * 3 * (size_t)n * kMultiRhs * nchunks;
+    void *ws = nullptr;
+    if (int rc = scratch(SCRATCH_PAIR, bytes, &ws, st)) return rc;
+    SrcF *src = (SrcF *)ws;
+    float4 *vec = (float4 *)((char *)ws + pos);
+    double *partial = (double *)((char *)ws + pos + vecb);
+    const double nf = 1.0 / (8.0 * kPi * eta * a);
+    const int chunk = (n + nchunks - 1) / nchunks;
+    const dim3 grid = B ? dim3(B->njobs) : dim3((n + kThreads - 1) / kThreads, nchunks);
+    for (int q0 = 0; q0 < nrhs; q0 += kMultiRhs) {
+        const int nr = std::min(kMultiRhs, nrhs - q0);
+        pack_multi_kernel<<<(n + 255) / 256, 256, 0, st>>>(r, V + (long long)q0 * ldv, ldv, nr, src, vec, n, a);
+        void *tok = nullptr;
+        if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
+        if (B) wall_pair_multi_kernel<true><<<grid, kThreads, 0, st>>>(src, vec, n, chunk, partial, B->jobs);
+        else wall_pair_multi_kernel<false><<<grid, kThreads, 0, st>>>(src, vec, n, chunk, partial, nullptr);
+        if (int rc = trace_end(tok, st)) return rc;
+        wall_finalize_multi_kernel<<<dim3((n + 255) / 256, nr), 256, 0, st>>>(
+            r, V + (long long)q0 * ldv, ldv, nr, partial, nchunks, Y + (long long)q0 * ldy, ldy, n, a, nf,
+            B ? B->blob_nch : nullptr);
+    }
+    RMW_CHECK_LAUNCH("multi-rhs product");
+    return RMW_OK;
+}
+
 }  // namespace rmw
 
 // ---------------------------------------------------------------------------
@@ -658,6 +822,17 @@ int rmw_wall_product_batched(void *handle, int kind, const double *r, const doub
 {
     if (!handle) return rmw::fail(RMW_ERR_ARG, "null batch handle");
     return rmw::wall_product_batched(*(rmw::WallBatch *)handle, kind, r, v, out, eta, a, mode, rmw::as_stream(stream));
+}
+
+int rmw_wall_uf_multi(const double *r, const double *V, double *Y, int64_t n, int nrhs, double eta, double a,
+                      void *batch, void *stream)
+{
+    int rc = rmw::validate_product_args(RMW_UF, r, V, Y, n, eta, a, RMW_MODE_MIXED);
+    if (rc) return rc;
+    if (nrhs < 0) return rmw::fail(RMW_ERR_ARG, "nrhs must be >= 0");
+    rmw::WallBatch *B = (rmw::WallBatch *)batch;
+    if (B && B->n != n) return rmw::fail(RMW_ERR_ARG, "batch handle does not match n");
+    return rmw::wall_uf_multi(r, V, 3 * n, Y, 3 * n, nrhs, (int)n, eta, a, B, rmw::as_stream(stream));
 }
 
 int rmw_wall_product_host(int kind, const double *r_host, const double *v_host, double *out_host, int64_t n,

@@ -27,6 +27,9 @@ struct WallBatch {
 };
 int wall_batch_build(WallBatch &B, const long long *off_host, int ninst);
 void wall_batch_free(WallBatch &B);
+// M_UF applied to nrhs vectors in mixed precision (rows of V, stride ldv).
+int wall_uf_multi(const double *r, const double *V, long long ldv, double *Y, long long ldy, int nrhs, int n,
+                  double eta, double a, const WallBatch *B, cudaStream_t st);
 int wall_product_batched(const WallBatch &B, int kind, const double *r, const double *v, double *out, double eta,
                          double a, int mode, cudaStream_t st);
 

@@ -124,6 +124,20 @@ class SuspensionBatch:
         return out
 
 
+def uf_multi(r_vectors, V, eta, a, batch=None):
+    """M_UF applied to the rows of V (nrhs, 3N) at once, mixed precision
+    (each pair block formed once for all right-hand sides).  CUDA tensors."""
+    import torch
+    r = torch.as_tensor(r_vectors, dtype=torch.float64).reshape(-1, 3).contiguous()
+    n = r.shape[0]
+    Vt = torch.as_tensor(V, dtype=torch.float64).reshape(-1, 3 * n).contiguous()
+    Y = torch.empty_like(Vt)
+    with torch.cuda.device(r.device):
+        _native.call("rmw_wall_uf_multi", r.data_ptr(), Vt.data_ptr(), Y.data_ptr(), n, Vt.shape[0], float(eta),
+                     float(a), batch._h if batch is not None else None, torch.cuda.current_stream(r.device).cuda_stream)
+    return Y
+
+
 # ---------------------------------------------------------------------------
 # wall regularisation helpers (mobility/mobility.py:52-84)
 def shift_heights(r_vectors, blob_radius, *args, **kwargs):

@@ -201,6 +201,19 @@ class RigidSystem:
             _native.check(rc)
         return x, it, rr, stt
 
+    def lanczos_batched(self, Z, factor=1.0, tol=1e-3, max_iter=95, mode="fp64"):
+        """Brownian noise for several right-hand sides of every suspension:
+        Z (nrhs, 3N) -> (noise (nrhs, 3N), iterations (nrhs, n_suspensions))."""
+        import torch
+        Zt = _dev(Z, self.device).reshape(-1, 3 * self.n_blobs).contiguous()
+        nrhs = Zt.shape[0]
+        out = torch.empty_like(Zt)
+        it = np.zeros(nrhs * self.n_suspensions, dtype=np.int32)
+        with torch.cuda.device(self.device):
+            _native.call("rmw_rigid_lanczos_batched", self._h, Zt.data_ptr(), out.data_ptr(), nrhs, float(factor),
+                         float(tol), int(max_iter), _mode(mode), it.ctypes.data_as(ctypes.c_void_p))
+        return out, it.reshape(nrhs, self.n_suspensions)
+
     # -- solvers -----------------------------------------------------------------
     def solve(self, rhs, tol=1e-8, restart=60, maxiter=1000, mode="fp64", raise_on_fail=False):
         """GMRES with the block-diagonal preconditioner.  Returns (solution, info, iterations, rel_residual);

@@ -86,3 +86,59 @@ def test_batched_product_rejects_bad_offsets(cuda_device):
         mb.SuspensionBatch([0, 5, 3])
     with pytest.raises(RMWError):
         mb.SuspensionBatch([1, 5])
+
+
+@pytest.mark.parametrize("nrhs", [1, 3, 8, 11])
+def test_multi_rhs_product_matches_single_products(cuda_device, nrhs):
+    import torch
+    r, _, eta, a = S.blobs_wall_matvec(900, seed=31)
+    r[::13, 2] = 0.3 * a
+    rng = np.random.default_rng(nrhs)
+    V = rng.standard_normal((nrhs, r.size))
+    rt = torch.tensor(r, device=cuda_device)
+    Y = mb.uf_multi(rt, torch.tensor(V, device=cuda_device), eta, a).cpu().numpy()
+    for q in range(nrhs):
+        assert rel_err(Y[q], wall.wall_product("uf", r, V[q], eta, a)) <= 1e-6
+    # segmented: two suspensions in one array
+    off = np.array([0, 400, 900])
+    Yb = mb.uf_multi(rt, torch.tensor(V, device=cuda_device), eta, a, batch=mb.SuspensionBatch(off)).cpu().numpy()
+    for q in range(nrhs):
+        for k in range(2):
+            sl = slice(3 * off[k], 3 * off[k + 1])
+            ref = wall.wall_product("uf", r[off[k]:off[k + 1]], V[q][sl], eta, a)
+            assert rel_err(Yb[q][sl], ref) <= 1e-6
+
+
+def _batched_system(counts, seed0):
+    susps = [S.shells_42_256(seed=seed0 + k, n_bodies=c) for k, c in enumerate(counts)]
+    r = np.concatenate([s.r_vectors() for s in susps])
+    locs = np.concatenate([s.locations for s in susps])
+    eta, a = susps[0].eta, susps[0].a
+    sys_ = RigidSystem([42] * sum(counts), eta, a)
+    sys_.set_configuration(r, locs)
+    sys_.set_suspensions(counts)
+    return sys_, r, locs, eta, a
+
+
+def test_batched_lanczos_matches_per_suspension_oracle(cuda_device):
+    counts = [2, 5, 1, 3]
+    sys_, r, locs, eta, a = _batched_system(counts, 300)
+    sys_.build_pc(stochastic=True)
+    nrhs = 3
+    Z = np.random.default_rng(9).standard_normal((nrhs, 3 * sys_.n_blobs))
+    factor = np.sqrt(2.0 / 1e-3)
+    noise, it = sys_.lanczos_batched(Z, factor=factor, tol=1e-3, mode="fp64")
+    noise = noise.cpu().numpy()
+    boff = sys_.suspension_body_offsets
+    for k, c in enumerate(counts):
+        bl0, bl1 = sys_.offsets[boff[k]], sys_.offsets[boff[k + 1]]
+        o = orc.Rigid(r[bl0:bl1], locs[boff[k]:boff[k + 1]], np.arange(c + 1) * 42, eta, a)
+        for q in range(nrhs):
+            nz, itk = orc.lanczos(o.mobility_pc, Z[q][3 * bl0:3 * bl1], factor=factor, tol=1e-3)
+            nz = o.P_inv_mult(nz)
+            assert it[q, k] == itk
+            assert rel_err(noise[q][3 * bl0:3 * bl1], nz) <= 1e-8
+    # mixed precision (multi-right-hand-side kernel) against the FP64 result
+    noise32, it32 = sys_.lanczos_batched(Z, factor=factor, tol=1e-3, mode="mixed")
+    assert np.abs(it32 - it).max() <= 1
+    assert rel_err(noise32.cpu().numpy(), noise) <= 1e-4

@@ -310,6 +310,53 @@ def large_solve(args):
     print(json.dumps(out))
 
 
+def batched_metrics(dev, nrhs=16):
+    """64 independent suspensions of 42-blob shells (16..512 bodies each, seeded):
+    stochastic block-diagonal preconditioner, 16 Lanczos right-hand sides per
+    suspension (tolerance 1e-3, mixed precision, lockstep over all
+    (suspension, RHS) pairs) and every suspension's mobility solve to 1e-8
+    (lockstep batched GMRES, mixed precision with df64 refinement)."""
+    import torch
+    from rigidmultiblobswall_gb300 import suspensions as S
+    from rigidmultiblobswall_gb300.rigid import RigidSystem
+    susps = S.shells_42_batch()
+    counts = [s.n_bodies for s in susps]
+    r = np.concatenate([s.r_vectors() for s in susps])
+    locs = np.concatenate([s.locations for s in susps])
+    sysb = RigidSystem([42] * sum(counts), susps[0].eta, susps[0].a, device=dev)
+    sysb.set_configuration(r, locs)
+    sysb.set_suspensions(counts)
+    pairs = int(sum((42 * c) ** 2 for c in counts))
+    out = {"workload": "64 suspensions, 16..512 42-blob shells each (%d bodies, %d blobs, %.3g pairs/product)"
+           % (sum(counts), sysb.n_blobs, pairs)}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sysb.build_pc(stochastic=True)
+    torch.cuda.synchronize()
+    out["pc_build_ms"] = (time.perf_counter() - t0) * 1e3
+    Z = torch.randn(nrhs, 3 * sysb.n_blobs, generator=torch.Generator(device=dev).manual_seed(4),
+                    dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    noise, itl = sysb.lanczos_batched(Z, factor=np.sqrt(2.0 / 1e-3), tol=1e-3, mode="mixed")
+    torch.cuda.synchronize()
+    out["lanczos_16rhs_ms"] = (time.perf_counter() - t0) * 1e3
+    out["lanczos_iterations_min_max"] = [int(itl.min()), int(itl.max())]
+    FT = np.zeros((sum(counts), 6))
+    FT[:, 2] = -1.0
+    rhs = torch.cat([torch.zeros(3 * sysb.n_blobs, dtype=torch.float64, device=dev),
+                     -torch.tensor(FT.reshape(-1), device=dev)])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x, its, rr, stt = sysb.solve_batched(rhs, tol=1e-8, mode="mixed")
+    torch.cuda.synchronize()
+    out["solve_ms"] = (time.perf_counter() - t0) * 1e3
+    out["solve_iterations_min_max"] = [int(its.min()), int(its.max())]
+    out["solve_relres_max"] = float(rr.max())
+    out["all_converged"] = bool((stt == 0).all())
+    return out
+
+
 def main():
     args = parse()
     if args.large:
@@ -422,6 +469,8 @@ def main():
             products["%s_%s" % (kind, mode)] = {k: round(v, 6) for k, v in res.items()}
 
     solver = {} if args.no_extras else solver_metrics(dev)
+    if not args.no_extras:
+        solver["batched_64_suspensions"] = batched_metrics(dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

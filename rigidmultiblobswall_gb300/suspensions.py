@@ -16,6 +16,8 @@ Workloads (numpy.random.default_rng(seed) with seed = workload index):
                      1024 centres 2R+2a apart in that slab, so the side is doubled,
                      which keeps the 256-shell workload's bodies per unit area
   shells_42_4096     4096 shells x 42 blobs (172,032 blobs), area fraction 0.3, z ~ U[1.1R,3R]
+  shells_42_batch    64 independent suspensions of 42-blob shells, body counts ~ U{16..512};
+                     each placed like shells_42_256 in a box of side 60R sqrt(max(n,256)/256)
 """
 import numpy as np
 
@@ -189,3 +191,16 @@ def shells_42_4096(seed=4, n_bodies=4096, area_fraction=0.3):
     R = R42
     side = np.sqrt(n_bodies * np.pi * R * R / area_fraction)
     return shells(n_bodies, icosphere_42(R), seed, side, 1.1 * R, 3 * R, name="shells_42_%d" % n_bodies)
+
+
+def shells_42_batch(seed=3, n_suspensions=64, lo=16, hi=512):
+    """Independent suspensions of uneven size (list of Suspension)."""
+    rng = np.random.default_rng(seed)
+    counts = rng.integers(lo, hi + 1, size=n_suspensions)
+    out = []
+    R = R42
+    for k, c in enumerate(counts):
+        side = 60 * R * np.sqrt(max(int(c), 256) / 256.0)
+        out.append(shells(int(c), icosphere_42(R), seed * 1000 + k, side, 1.2 * R, 5 * R,
+                          name="batch_%d_%d" % (k, c)))
+    return out

@@ -207,6 +207,39 @@ int rmw_rigid_solve_batched(void *handle, const double *rhs, double *sol, double
 int rmw_rigid_lanczos_batched(void *handle, const double *Z, double *noise, int nrhs, double factor, double tol,
                               int max_iter, int mode, int *iters_host);
 
+/* ---- near-field augmented preconditioner (no reference counterpart) ----
+ * The block-diagonal preconditioner (rmw_rigid_build_pc) drops every
+ * inter-body blob block of M.  The augmented form adds the first Neumann term
+ * of the near blocks: y = P0 x, v_i = sum_{j near i} M_ij lambda_j(y),
+ * y <- y - P0 [v; 0].  Pairs closer than an exact cutoff use the blob-level
+ * blocks; from there to the network's cutoff a small network (3 -> 64 -> 64
+ * -> 64 -> 121, SiLU, BF16 weights, FP32 accumulation on the tensor cores)
+ * predicts the 11x11 coupling of the bodies' low-order modes (3 translations,
+ * 3 rotations, 5 strains) from the horizontal distance and both heights. */
+/* 11x11 mode couplings G_01, G_10 (lab frame, row-major; 242 doubles per
+ * sample) of every pair of handle bodies (2s, 2s+1); call after
+ * rmw_rigid_build_pc.  Training data. */
+int rmw_rigid_pair_coupling(void *handle, double *out);
+int rmw_nearfield_create(void **net, double body_radius, double cutoff, unsigned long long seed);
+int rmw_nearfield_destroy(void *net);
+int rmw_nearfield_sizes(int *n_weights, int *n_biases, int *n_in, int *width, int *n_out, int *n_target);
+int rmw_nearfield_get(void *net, float *w_host, float *b_host, float *norm_host);
+int rmw_nearfield_set(void *net, const float *w_host, const float *b_host, const float *norm_host);
+/* forward / gradient on host batches of normalised inputs (tests, checks) */
+int rmw_nearfield_forward(void *net, const float *X_host, int P, float *Y_host);
+int rmw_nearfield_grad(void *net, const float *X_host, const float *T_host, int P, float *gW_host, float *gb_host,
+                       float *loss_host);
+/* Adam on device data: feat (S x 3: horizontal distance, z_i, z_j over the
+ * body radius), targ (S x 121: pair-frame mode coupling).  Synchronous. */
+int rmw_nearfield_train(void *net, const float *feat, const float *targ, int S, int steps, int batch, float lr,
+                        unsigned long long seed, float *loss_host, void *stream);
+/* Switch a handle's preconditioner (after rmw_rigid_build_pc) to the
+ * augmented form: exact couplings below exact_cutoff, learned ones from there
+ * to the network's cutoff (net may be NULL).  net == NULL with exact_cutoff <= 0
+ * restores the block-diagonal form.  n_pairs_host (optional): 2 entries,
+ * ordered exact and learned pair counts.  Synchronous. */
+int rmw_rigid_set_nearfield(void *handle, void *net, double exact_cutoff, int64_t *n_pairs_host);
+
 /* ---- generic Krylov solvers with caller-supplied operators ------------
  * op(ctx, x, y) must write y = A x for device vectors of length n, enqueue its
  * work on the solver's stream (or finish it before returning) and return 0 on

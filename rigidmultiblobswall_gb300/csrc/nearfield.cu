@@ -1,0 +1,1178 @@
+// Near-field augmented block-diagonal preconditioner, and the learned
+// coupling network that feeds it.
+//
+// The block-diagonal preconditioner P0 is the exact inverse of the saddle-point
+// operator with every inter-body blob block of M dropped:
+//   A0 = [[Mbd, -K], [-K^T, 0]],   A P0 = I + [[M - Mbd, 0], [0, 0]] A0^-1 .
+// The error lives in the blob rows only: the velocities that other bodies'
+// blob forces induce on a body.  The augmented preconditioner takes the first
+// Neumann term of (A0 + E)^-1 with E the near part of M - Mbd:
+//   y = P0 x;   v_i = sum_{j near i} M_ij lambda_j(y);   y <- y - P0 [v; 0] .
+// It stays an exact-inverse-like operator (the force rows of the correction
+// are consistent), which is why it helps where changing only the body
+// velocities - even with the exact many-body mobility - costs iterations.
+//
+// Two kinds of near pairs:
+//  * exact pairs (centre distance below the exact cutoff): M_ij lambda_j
+//    evaluated blob by blob in FP64 (same pair formulas and periodic images
+//    as the all-pairs product);
+//  * learned pairs (from the exact cutoff to the network's cutoff): M_ij is
+//    replaced by its projection on the 11 low-order modes of each body -
+//    3 translations, 3 rotations, 5 strains E_k d (d = blob - centre):
+//      v_i ~ X_i G_ij X_j^T lambda_j,  X_b the mode velocities of body b,
+//    with G_ij = (X_i^T M_i^-1 X_i)^-1 X_i^T M_i^-1  M_ij  M_j^-1 X_j (X_j^T M_j^-1 X_j)^-1,
+//    the response of body i's modes to body j's force, torque and stresslet
+//    above the wall.  A small network predicts G_ij from the horizontal
+//    distance and both heights (units of the body radius) in the frame
+//    rotated about the wall normal so that the separation lies along +x;
+//    the kernels rotate it back (translations and rotations as vectors,
+//    strains by the 5x5 representation of the rotation).
+// GMRES with right preconditioning accepts any nonsingular P^-1, so a poor
+// prediction only costs iterations; the caller compares against the plain
+// solve and falls back.
+//
+// Training data come from two-body configurations through the plain method's
+// own machinery on the GPU: a handle whose bodies are the samples' single
+// shells builds each body's M^-1 (rmw_rigid_build_pc) and pair_fts_kernel
+// forms both G_ij and G_ji of every sample.
+//
+// Network: 3 -> 64 -> 64 -> 64 -> 121 (inputs padded to 16, outputs to 128),
+// SiLU activations, BF16 weights and activations, FP32 accumulation on the
+// tensor cores (mma.sync m16n8k16 BF16); backward pass and Adam in FP32 on
+// the CUDA cores with the same BF16-rounded weights (straight-through for the
+// activation rounding).
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "pair_math.cuh"
+#include "rigid.cuh"
+
+namespace rmw {
+
+constexpr int kModes = 11;
+constexpr double kS2 = 0.70710678118654752440;  // 1/sqrt(2)
+constexpr double kS6 = 0.40824829046386301637;  // 1/sqrt(6)
+
+// velocity of mode c at displacement d from the body centre: 0-2 translations,
+// 3-5 rotations (e_c x d), 6-10 strains E_k d with the orthonormal symmetric
+// traceless basis (xx-yy)/sqrt2, (2zz-xx-yy)/sqrt6, (xy+yx)/sqrt2,
+// (xz+zx)/sqrt2, (yz+zy)/sqrt2
+__host__ __device__ __forceinline__ void mode_velocity(int c, double dx, double dy, double dz, double &vx,
+                                                       double &vy, double &vz)
+{
+    switch (c) {
+    case 0: vx = 1.0; vy = 0.0; vz = 0.0; break;
+    case 1: vx = 0.0; vy = 1.0; vz = 0.0; break;
+    case 2: vx = 0.0; vy = 0.0; vz = 1.0; break;
+    case 3: vx = 0.0; vy = -dz; vz = dy; break;
+    case 4: vx = dz; vy = 0.0; vz = -dx; break;
+    case 5: vx = -dy; vy = dx; vz = 0.0; break;
+    case 6: vx = kS2 * dx; vy = -kS2 * dy; vz = 0.0; break;
+    case 7: vx = -kS6 * dx; vy = -kS6 * dy; vz = 2.0 * kS6 * dz; break;
+    case 8: vx = kS2 * dy; vy = kS2 * dx; vz = 0.0; break;
+    case 9: vx = kS2 * dz; vy = 0.0; vz = kS2 * dx; break;
+    default: vx = 0.0; vy = kS2 * dz; vz = kS2 * dy; break;
+    }
+}
+
+__host__ __device__ __forceinline__ void strain_basis(int k, double E[3][3])
+{
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) E[a][b] = 0.0;
+    switch (k) {
+    case 0: E[0][0] = kS2; E[1][1] = -kS2; break;
+    case 1: E[0][0] = -kS6; E[1][1] = -kS6; E[2][2] = 2.0 * kS6; break;
+    case 2: E[0][1] = E[1][0] = kS2; break;
+    case 3: E[0][2] = E[2][0] = kS2; break;
+    default: E[1][2] = E[2][1] = kS2; break;
+    }
+}
+
+// Q = diag(Rz, Rz, R5) for the rotation about z with cos c, sin s
+__host__ __device__ inline void mode_rotation(double c, double s, double Q[kModes][kModes])
+{
+    for (int a = 0; a < kModes; ++a)
+        for (int b = 0; b < kModes; ++b) Q[a][b] = 0.0;
+    for (int blk = 0; blk < 2; ++blk) {
+        const int o = 3 * blk;
+        Q[o][o] = c; Q[o][o + 1] = -s;
+        Q[o + 1][o] = s; Q[o + 1][o + 1] = c;
+        Q[o + 2][o + 2] = 1.0;
+    }
+    const double Rz[3][3] = {{c, -s, 0.0}, {s, c, 0.0}, {0.0, 0.0, 1.0}};
+    for (int l = 0; l < 5; ++l) {
+        double El[3][3], T[3][3];
+        strain_basis(l, El);
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                double acc = 0.0;
+                for (int p = 0; p < 3; ++p)
+                    for (int q = 0; q < 3; ++q) acc += Rz[a][p] * El[p][q] * Rz[b][q];
+                T[a][b] = acc;
+            }
+        for (int k = 0; k < 5; ++k) {
+            double Ek[3][3];
+            strain_basis(k, Ek);
+            double acc = 0.0;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) acc += Ek[a][b] * T[a][b];
+            Q[6 + k][6 + l] = acc;
+        }
+    }
+}
+
+struct Images {
+    double Lx, Ly, Lz;
+};
+
+// Unscaled single-wall RPY velocity at blob (xi, yi, zie) from blob (xj, yj, zje)
+// carrying v (heights already clamped at a, v already damped), summed over the
+// periodic images the all-pairs product uses; the caller multiplies by
+// b_i / (8 pi eta a).
+__device__ __forceinline__ void wall_uf_pair(double xi, double yi, double zie, double xj, double yj, double zje,
+                                             double inva, const Images &P, double vx, double vy, double vz,
+                                             double &ux, double &uy, double &uz)
+{
+    const double hi = zie * inva, hj = zje * inva, Rz = (zie + zje) * inva;
+    double rx = xi - xj, ry = yi - yj, rz = zie - zje;
+    if (!(P.Lx > 0 || P.Ly > 0 || P.Lz > 0)) {
+        double cx = 0.0, cy = 0.0, cz = 0.0;
+        pair_contrib<RMW_UF, double>(rx * inva, ry * inva, rz * inva, Rz, hi, hj, vx, vy, vz, cx, cy, cz);
+        ux += cx; uy += cy; uz += cz;
+        return;
+    }
+    if (P.Lx > 0) rx = project(rx, P.Lx);
+    if (P.Ly > 0) ry = project(ry, P.Ly);
+    if (P.Lz > 0) rz = project(rz, P.Lz);
+    const int px = P.Lx > 0, py = P.Ly > 0, pz = P.Lz > 0;
+    for (int bx = -px; bx <= px; ++bx)
+        for (int by = -py; by <= py; ++by)
+            for (int bz = -pz; bz <= pz; ++bz) {
+                double cx = 0.0, cy = 0.0, cz = 0.0;
+                pair_contrib<RMW_UF, double>((rx + bx * P.Lx) * inva, (ry + by * P.Ly) * inva,
+                                             (rz + bz * P.Lz) * inva, Rz, hi, hj, vx, vy, vz, cx, cy, cz);
+                ux += cx; uy += cy; uz += cz;
+            }
+}
+
+__device__ __forceinline__ double wall_damp(double z, double a) { return (z < a) ? z / a : 1.0; }
+__device__ __forceinline__ double wall_clamp(double z, double a) { return (z <= a) ? a : z; }
+
+// ---------------------------------------------------------------------------
+// two-body mode couplings (training targets)
+
+// A = M_b^-1 X_b (m x 11, row-major)
+__device__ void body_minv_modes(const double *__restrict__ Mi, const double *__restrict__ r, int o, int nbl,
+                                const double *c, double *A)
+{
+    const int m = 3 * nbl;
+    for (int t = threadIdx.x; t < m; t += blockDim.x) {
+        double acc[kModes];
+        for (int k = 0; k < kModes; ++k) acc[k] = 0.0;
+        for (int q = 0; q < nbl; ++q) {
+            const int i = o + q;
+            const double dx = r[3 * i] - c[0], dy = r[3 * i + 1] - c[1], dz = r[3 * i + 2] - c[2];
+            // M^-1 symmetric: column t of rows 3q..3q+2, coalesced across threads
+            const double m0 = Mi[(long long)(3 * q) * m + t], m1 = Mi[(long long)(3 * q + 1) * m + t],
+                         m2 = Mi[(long long)(3 * q + 2) * m + t];
+#pragma unroll
+            for (int k = 0; k < kModes; ++k) {
+                double vx, vy, vz;
+                mode_velocity(k, dx, dy, dz, vx, vy, vz);
+                acc[k] += m0 * vx + m1 * vy + m2 * vz;
+            }
+        }
+        for (int k = 0; k < kModes; ++k) A[t * kModes + k] = acc[k];
+    }
+}
+
+// Ginv = (X_b^T A)^-1 (11 x 11), Gauss-Jordan with partial pivoting by one thread
+__device__ void mode_gram_inverse(const double *A, const double *__restrict__ r, int o, int nbl, const double *c,
+                                  double *aug, double *Ginv, int *status)
+{
+    for (int e = threadIdx.x; e < kModes * kModes; e += blockDim.x) {
+        const int k = e / kModes, l = e % kModes;
+        double g = 0.0;
+        for (int q = 0; q < nbl; ++q) {
+            const int i = o + q;
+            double vx, vy, vz;
+            mode_velocity(k, r[3 * i] - c[0], r[3 * i + 1] - c[1], r[3 * i + 2] - c[2], vx, vy, vz);
+            g += vx * A[(3 * q) * kModes + l] + vy * A[(3 * q + 1) * kModes + l] + vz * A[(3 * q + 2) * kModes + l];
+        }
+        aug[k * 2 * kModes + l] = g;
+        aug[k * 2 * kModes + kModes + l] = (k == l) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int w = 2 * kModes;
+        for (int cc = 0; cc < kModes; ++cc) {
+            int piv = cc;
+            for (int i = cc + 1; i < kModes; ++i)
+                if (fabs(aug[i * w + cc]) > fabs(aug[piv * w + cc])) piv = i;
+            if (piv != cc)
+                for (int j = 0; j < w; ++j) {
+                    const double t = aug[cc * w + j];
+                    aug[cc * w + j] = aug[piv * w + j];
+                    aug[piv * w + j] = t;
+                }
+            const double dg = aug[cc * w + cc];
+            if (!(fabs(dg) > 0.0)) {
+                atomicExch(status, 3);
+                continue;
+            }
+            for (int j = 0; j < w; ++j) aug[cc * w + j] /= dg;
+            for (int i = 0; i < kModes; ++i) {
+                if (i == cc) continue;
+                const double f = aug[i * w + cc];
+                for (int j = 0; j < w; ++j) aug[i * w + j] -= f * aug[cc * w + j];
+            }
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kModes * kModes; e += blockDim.x)
+        Ginv[e] = aug[(e / kModes) * 2 * kModes + kModes + e % kModes];
+    __syncthreads();
+}
+
+// out = Gi^-1 A_i^T M_ij A_j Gj^-1 (11 x 11, row-major): response of body i's
+// modes to body j's mode moments.  Lam, V: scratch (m x 11).
+__device__ void mode_coupling(const double *__restrict__ r, int oi, int ni, const double *Ai, const double *Giinv,
+                              int oj, int nj, const double *Aj, const double *Gjinv, double a, double nf,
+                              const Images &P, double *Lam, double *V, double *W, double *out)
+{
+    const int mj = 3 * nj, mi = 3 * ni;
+    const double inva = 1.0 / a;
+    for (int e = threadIdx.x; e < mj * kModes; e += blockDim.x) {
+        const int t = e / kModes, l = e % kModes;
+        double acc = 0.0;
+        for (int k = 0; k < kModes; ++k) acc += Aj[t * kModes + k] * Gjinv[k * kModes + l];
+        Lam[e] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < ni * kModes; e += blockDim.x) {
+        const int p = e / kModes, l = e % kModes;
+        const int i = oi + p;
+        const double zi = r[3 * i + 2];
+        const double zie = wall_clamp(zi, a);
+        double ux = 0.0, uy = 0.0, uz = 0.0;
+        for (int q = 0; q < nj; ++q) {
+            const int j = oj + q;
+            const double zj = r[3 * j + 2];
+            const double bj = wall_damp(zj, a);
+            wall_uf_pair(r[3 * i], r[3 * i + 1], zie, r[3 * j], r[3 * j + 1], wall_clamp(zj, a), inva, P,
+                         bj * Lam[(3 * q) * kModes + l], bj * Lam[(3 * q + 1) * kModes + l],
+                         bj * Lam[(3 * q + 2) * kModes + l], ux, uy, uz);
+        }
+        const double sc = nf * wall_damp(zi, a);
+        V[(3 * p) * kModes + l] = sc * ux;
+        V[(3 * p + 1) * kModes + l] = sc * uy;
+        V[(3 * p + 2) * kModes + l] = sc * uz;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kModes * kModes; e += blockDim.x) {
+        const int k = e / kModes, l = e % kModes;
+        double acc = 0.0;
+        for (int t = 0; t < mi; ++t) acc += Ai[t * kModes + k] * V[t * kModes + l];
+        W[e] = acc;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kModes * kModes; e += blockDim.x) {
+        const int k = e / kModes, l = e % kModes;
+        double acc = 0.0;
+        for (int p = 0; p < kModes; ++p) acc += Giinv[k * kModes + p] * W[p * kModes + l];
+        out[e] = acc;
+    }
+    __syncthreads();
+}
+
+// One CTA per sample s = bodies (2s, 2s+1): out[242 s ..] = G_01, G_10 (lab frame).
+__global__ void pair_fts_kernel(const double *__restrict__ r, const double *__restrict__ xb,
+                                const int *__restrict__ boff, const long long *__restrict__ moff,
+                                const double *__restrict__ minv, double a, double nf, Images P, int max_m,
+                                double *__restrict__ out, int *status)
+{
+    extern __shared__ double sh[];
+    const int s = blockIdx.x;
+    const int b0 = 2 * s, b1 = 2 * s + 1;
+    const int o0 = boff[b0], n0 = boff[b0 + 1] - o0, o1 = boff[b1], n1 = boff[b1 + 1] - o1;
+    double *A0 = sh, *A1 = A0 + max_m * kModes, *Lam = A1 + max_m * kModes, *V = Lam + max_m * kModes;
+    double *G0 = V + max_m * kModes, *G1 = G0 + kModes * kModes, *W = G1 + kModes * kModes;
+    double *aug = W + kModes * kModes;
+    __shared__ double c0[3], c1[3];
+    if (threadIdx.x < 3) {
+        c0[threadIdx.x] = xb[3 * b0 + threadIdx.x];
+        c1[threadIdx.x] = xb[3 * b1 + threadIdx.x];
+    }
+    __syncthreads();
+    body_minv_modes(minv + moff[b0], r, o0, n0, c0, A0);
+    body_minv_modes(minv + moff[b1], r, o1, n1, c1, A1);
+    __syncthreads();
+    mode_gram_inverse(A0, r, o0, n0, c0, aug, G0, status);
+    mode_gram_inverse(A1, r, o1, n1, c1, aug, G1, status);
+    mode_coupling(r, o0, n0, A0, G0, o1, n1, A1, G1, a, nf, P, Lam, V, W, out + 242LL * s);
+    mode_coupling(r, o1, n1, A1, G1, o0, n0, A0, G0, a, nf, P, Lam, V, W, out + 242LL * s + 121);
+}
+
+// ---------------------------------------------------------------------------
+// MLP on the tensor cores
+constexpr int kIn = 16, kWidth = 64, kOut = 128, kLayers = 4;
+constexpr int kFeat = 3, kTarget = kModes * kModes;
+constexpr int kWide = kOut > kWidth ? kOut : kWidth;  // widest layer
+__host__ __device__ constexpr int layer_in(int l) { return l == 0 ? kIn : kWidth; }
+__host__ __device__ constexpr int layer_out(int l) { return l == kLayers - 1 ? kOut : kWidth; }
+__host__ __device__ constexpr int wofs(int l)
+{
+    return l == 0 ? 0 : (l == 1 ? kIn * kWidth : (l == 2 ? kIn * kWidth + kWidth * kWidth : kIn * kWidth + 2 * kWidth * kWidth));
+}
+constexpr int kNW = kIn * kWidth + 2 * kWidth * kWidth + kWidth * kOut;  // weights (Wt layout: [out][in])
+constexpr int kNB = 3 * kWidth + kOut;                                   // biases
+__host__ __device__ constexpr int bofs(int l) { return l * kWidth; }
+
+__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float silu_grad(float z)
+{
+    const float s = 1.0f / (1.0f + __expf(-z));
+    return s * (1.0f + z * (1.0f - s));
+}
+
+__device__ __forceinline__ unsigned pack_bf16x2(const __nv_bfloat16 *p) { return *(const unsigned *)p; }
+
+// Y = act(X W + b) for rows [0, P) (P a multiple of 16); X: P x nin (bf16,
+// row-major), Wt: nout x nin (bf16, row-major), one warp per 16-row tile.
+// Z (optional) keeps the FP32 pre-activations for the backward pass.
+__global__ void mlp_layer_fwd_kernel(const __nv_bfloat16 *__restrict__ X, int nin,
+                                     const __nv_bfloat16 *__restrict__ Wt, const float *__restrict__ bias, int nout,
+                                     float *__restrict__ Z, __nv_bfloat16 *__restrict__ Y, float *__restrict__ Yf,
+                                     int P, int act)
+{
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int row0 = warp * 16;
+    if (row0 >= P) return;
+    const int g = lane >> 2, tq = lane & 3;
+    for (int n0 = 0; n0 < nout; n0 += 8) {
+        float c[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int k0 = 0; k0 < nin; k0 += 16) {
+            const int kc = k0 + tq * 2;
+            unsigned a0 = pack_bf16x2(X + (long long)(row0 + g) * nin + kc);
+            unsigned a1 = pack_bf16x2(X + (long long)(row0 + g + 8) * nin + kc);
+            unsigned a2 = pack_bf16x2(X + (long long)(row0 + g) * nin + kc + 8);
+            unsigned a3 = pack_bf16x2(X + (long long)(row0 + g + 8) * nin + kc + 8);
+            unsigned b0 = pack_bf16x2(Wt + (long long)(n0 + g) * nin + kc);
+            unsigned b1 = pack_bf16x2(Wt + (long long)(n0 + g) * nin + kc + 8);
+            asm volatile(
+                "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                "{%0,%1,%2,%3};\n"
+                : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+        }
+        const int col = n0 + tq * 2;
+        for (int e = 0; e < 4; ++e) {
+            const int rr = row0 + g + (e >= 2 ? 8 : 0), cc = col + (e & 1);
+            const float z = c[e] + bias[cc];
+            const float y = act ? silu(z) : z;
+            if (Z) Z[(long long)rr * nout + cc] = z;
+            if (Y) Y[(long long)rr * nout + cc] = __float2bfloat16_rn(y);
+            if (Yf) Yf[(long long)rr * nout + cc] = y;
+        }
+    }
+}
+
+// dY (P x kOut) = 2 (Yf - T) / (P_valid * kTarget) on the first kTarget outputs;
+// the loss is reduced per block (256 threads) and added once per block
+__global__ void mse_grad_kernel(const float *__restrict__ Yf, const float *__restrict__ T, float *__restrict__ dY,
+                                int P, int Pvalid, float *__restrict__ loss)
+{
+    __shared__ float part[8];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float g = 0.f, l = 0.f;
+    if (i < P * kOut) {
+        const int p = i / kOut, o = i % kOut;
+        if (p < Pvalid && o < kTarget) {
+            const float d = Yf[i] - T[(long long)p * kTarget + o];
+            g = 2.0f * d / (float)(Pvalid * kTarget);
+            l = d * d / (float)(Pvalid * kTarget);
+        }
+        dY[i] = g;
+    }
+    for (int off = 16; off > 0; off >>= 1) l += __shfl_xor_sync(0xffffffffu, l, off);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = l;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float s = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += part[w];
+        atomicAdd(loss, s);
+    }
+}
+
+// dZ = dY * act'(Z)
+__global__ void act_grad_kernel(const float *__restrict__ dY, const float *__restrict__ Z, float *__restrict__ dZ,
+                                int count, int act)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) dZ[i] = act ? dY[i] * silu_grad(Z[i]) : dY[i];
+}
+
+// gW[o][i] = sum_p dZ[p][o] X[p][i];  gb[o] = sum_p dZ[p][o]   (one thread per weight)
+__global__ void weight_grad_kernel(const float *__restrict__ dZ, const __nv_bfloat16 *__restrict__ X, int nin,
+                                   int nout, int P, float *__restrict__ gW, float *__restrict__ gb)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nout * (nin + 1)) return;
+    const int o = t / (nin + 1), i = t % (nin + 1);
+    float s = 0.f;
+    if (i < nin)
+        for (int p = 0; p < P; ++p) s += dZ[(long long)p * nout + o] * __bfloat162float(X[(long long)p * nin + i]);
+    else
+        for (int p = 0; p < P; ++p) s += dZ[(long long)p * nout + o];
+    if (i < nin) gW[o * nin + i] = s;
+    else gb[o] = s;
+}
+
+// dX[p][i] = sum_o dZ[p][o] Wt[o][i]
+__global__ void input_grad_kernel(const float *__restrict__ dZ, const __nv_bfloat16 *__restrict__ Wt, int nin,
+                                  int nout, int P, float *__restrict__ dX)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P * nin) return;
+    const int p = t / nin, i = t % nin;
+    float s = 0.f;
+    for (int o = 0; o < nout; ++o) s += dZ[(long long)p * nout + o] * __bfloat162float(Wt[o * nin + i]);
+    dX[t] = s;
+}
+
+__global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m,
+                            float *__restrict__ v, __nv_bfloat16 *__restrict__ wb, int count, float lr, float b1,
+                            float b2, float c1, float c2, float eps)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    if (wb) wb[i] = __float2bfloat16_rn(wi);
+}
+
+// batch gather: X (P x kIn bf16, normalised features, zero padding) and T (P x kTarget)
+__global__ void gather_batch_kernel(const float *__restrict__ feat, const float *__restrict__ targ, int S,
+                                    const float *__restrict__ fmean, const float *__restrict__ fscale,
+                                    const float *__restrict__ tscale, int P, int Pvalid, unsigned long long seed,
+                                    int step, __nv_bfloat16 *__restrict__ X, float *__restrict__ T)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    int s = 0;
+    if (p < Pvalid) {
+        unsigned long long x = seed ^ ((unsigned long long)step * 0x9E3779B97F4A7C15ULL) ^ ((unsigned long long)p * 0xD1B54A32D192ED03ULL);
+        x ^= x >> 33; x *= 0xff51afd7ed558ccdULL; x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ULL; x ^= x >> 33;
+        s = (int)(x % (unsigned long long)S);
+    }
+    for (int i = 0; i < kIn; ++i) {
+        const float f = (p < Pvalid && i < kFeat) ? (feat[(long long)s * kFeat + i] - fmean[i]) / fscale[i] : 0.f;
+        X[(long long)p * kIn + i] = __float2bfloat16_rn(f);
+    }
+    if (p < Pvalid)
+        for (int o = 0; o < kTarget; ++o) T[(long long)p * kTarget + o] = targ[(long long)s * kTarget + o] / tscale[o];
+}
+
+// ---------------------------------------------------------------------------
+// the model
+struct NearfieldNet {
+    float *w = nullptr, *b = nullptr;           // FP32 master weights (Wt layout) and biases
+    __nv_bfloat16 *wb = nullptr;                // BF16 copy used by the forward pass
+    float *adam = nullptr;                      // m, v for weights and biases
+    float fmean[kFeat], fscale[kFeat], tscale[kTarget];
+    float *dnorm = nullptr;                     // device copy: fmean, fscale, tscale
+    double cutoff = 0.0, radius = 1.0;
+    int device = 0;
+};
+
+static int net_forward(NearfieldNet &net, const __nv_bfloat16 *X, int P, float *Z[kLayers],
+                       __nv_bfloat16 *A[kLayers], float *Yf, cudaStream_t st)
+{
+    const __nv_bfloat16 *in = X;
+    for (int l = 0; l < kLayers; ++l) {
+        const int warps = P / 16, threads = 128;
+        const bool last = l == kLayers - 1;
+        mlp_layer_fwd_kernel<<<(warps * 32 + threads - 1) / threads, threads, 0, st>>>(
+            in, layer_in(l), net.wb + wofs(l), net.b + bofs(l), layer_out(l), Z ? Z[l] : nullptr, last ? nullptr : A[l],
+            last ? Yf : nullptr, P, last ? 0 : 1);
+        in = A[l];
+    }
+    RMW_CHECK_LAUNCH("mlp forward");
+    return RMW_OK;
+}
+
+// one forward + backward pass on a prepared batch (X bf16 P x kIn, T P x kTarget,
+// both normalised); gradients to gW (kNW), gb (kNB); loss added to *loss
+struct NetWork {
+    float *Z[kLayers];
+    __nv_bfloat16 *A[kLayers];
+    float *Yf, *dY, *dZ, *dX;
+    void *base = nullptr;
+    cudaStream_t st = 0;
+    int P = 0;
+    int alloc(int P_, cudaStream_t s)
+    {
+        P = P_;
+        st = s;
+        size_t fl = 0;
+        for (int l = 0; l < kLayers; ++l) fl += (size_t)P * layer_out(l);
+        const size_t bytes = sizeof(float) * (fl + 4 * (size_t)P * kWide) + sizeof(__nv_bfloat16) * (fl + 64) + 1024;
+        RMW_CUDA(cudaMallocAsync(&base, bytes, st));
+        char *q = (char *)base;
+        for (int l = 0; l < kLayers; ++l) {
+            Z[l] = (float *)q;
+            q += sizeof(float) * (size_t)P * layer_out(l);
+        }
+        Yf = (float *)q; q += sizeof(float) * (size_t)P * kWide;
+        dY = (float *)q; q += sizeof(float) * (size_t)P * kWide;
+        dZ = (float *)q; q += sizeof(float) * (size_t)P * kWide;
+        dX = (float *)q; q += sizeof(float) * (size_t)P * kWide;
+        for (int l = 0; l < kLayers; ++l) {
+            A[l] = (__nv_bfloat16 *)q;
+            q += sizeof(__nv_bfloat16) * (size_t)P * layer_out(l);
+        }
+        return RMW_OK;
+    }
+    ~NetWork()
+    {
+        if (base) cudaFreeAsync(base, st);
+    }
+};
+
+static int net_backward(NearfieldNet &net, const __nv_bfloat16 *X, const float *T, int Pvalid, NetWork &W,
+                        float *gW, float *gb, float *loss)
+{
+    const int P = W.P;
+    cudaStream_t st = W.st;
+    if (int rc = net_forward(net, X, P, W.Z, W.A, W.Yf, st)) return rc;
+    mse_grad_kernel<<<(P * kOut + 255) / 256, 256, 0, st>>>(W.Yf, T, W.dY, P, Pvalid, loss);
+    for (int l = kLayers - 1; l >= 0; --l) {
+        const int ni = layer_in(l), no = layer_out(l);
+        const bool last = l == kLayers - 1;
+        act_grad_kernel<<<(P * no + 255) / 256, 256, 0, st>>>(W.dY, W.Z[l], W.dZ, P * no, last ? 0 : 1);
+        const __nv_bfloat16 *in = l == 0 ? X : W.A[l - 1];
+        weight_grad_kernel<<<(no * (ni + 1) + 127) / 128, 128, 0, st>>>(W.dZ, in, ni, no, P, gW + wofs(l),
+                                                                         gb + bofs(l));
+        if (l > 0) {
+            input_grad_kernel<<<(P * ni + 255) / 256, 256, 0, st>>>(W.dZ, net.wb + wofs(l), ni, no, P, W.dX);
+            std::swap(W.dY, W.dX);
+        }
+    }
+    RMW_CHECK_LAUNCH("mlp backward");
+    return RMW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// neighbour lists: ordered pairs (i, j != i) of one suspension with centre
+// distance (minimum image) in [lo, hi)
+__device__ __forceinline__ double centre_dist2(const double *__restrict__ xb, int i, int j, const Images &P)
+{
+    double dx = xb[3 * j] - xb[3 * i], dy = xb[3 * j + 1] - xb[3 * i + 1], dz = xb[3 * j + 2] - xb[3 * i + 2];
+    if (P.Lx > 0) dx = project(dx, P.Lx);
+    if (P.Ly > 0) dy = project(dy, P.Ly);
+    if (P.Lz > 0) dz = project(dz, P.Lz);
+    return dx * dx + dy * dy + dz * dz;
+}
+
+__global__ void nbr_band_kernel(const double *__restrict__ xb, int nb, double lo2, double hi2, Images P,
+                                const long long *__restrict__ susp, const int *__restrict__ off,
+                                int *__restrict__ out)
+{
+    // off == NULL: out[i] = count; else out = neighbour indices at off[i]
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    int c = off ? off[i] : 0;
+    for (int j = 0; j < nb; ++j) {
+        if (j == i) continue;
+        if (susp && susp[j] != susp[i]) continue;
+        const double d2 = centre_dist2(xb, i, j, P);
+        if (d2 >= lo2 && d2 < hi2) {
+            if (off) out[c] = j;
+            ++c;
+        }
+    }
+    if (!off) out[i] = c;
+}
+
+__device__ __forceinline__ int owner_of(const int *__restrict__ off, int nb, int q)
+{
+    int lo = 0, hi = nb;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) / 2;
+        if (off[mid] <= q) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// horizontal separation of entry q's pair (owner -> neighbour), minimum image
+__device__ __forceinline__ void pair_horizontal(const double *__restrict__ xb, int i, int j, const Images &P,
+                                                double &dx, double &dy)
+{
+    dx = xb[3 * j] - xb[3 * i];
+    dy = xb[3 * j + 1] - xb[3 * i + 1];
+    if (P.Lx > 0) dx = project(dx, P.Lx);
+    if (P.Ly > 0) dy = project(dy, P.Ly);
+}
+
+// normalised features (horizontal distance, z_i, z_j) / R of every learned entry, bf16, zero-padded rows
+__global__ void pair_features_kernel(const double *__restrict__ xb, const int *__restrict__ off,
+                                     const int *__restrict__ idx, int nb, int npairs, double inv_radius, Images P,
+                                     const float *__restrict__ norm, __nv_bfloat16 *__restrict__ X, int Prows)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= Prows) return;
+    float f[kFeat] = {0.f, 0.f, 0.f};
+    if (q < npairs) {
+        const int i = owner_of(off, nb, q), j = idx[q];
+        double dx, dy;
+        pair_horizontal(xb, i, j, P, dx, dy);
+        f[0] = (float)(sqrt(dx * dx + dy * dy) * inv_radius);
+        f[1] = (float)(xb[3 * i + 2] * inv_radius);
+        f[2] = (float)(xb[3 * j + 2] * inv_radius);
+    }
+    for (int k = 0; k < kIn; ++k) {
+        const float v = (q < npairs && k < kFeat) ? (f[k] - norm[k]) / norm[kFeat + k] : 0.f;
+        X[(long long)q * kIn + k] = __float2bfloat16_rn(v);
+    }
+}
+
+// G_lab = Q G' Q^T, G' = network output * target scale (pair frame)
+__global__ void pair_blocks_kernel(const float *__restrict__ Yf, const double *__restrict__ xb,
+                                   const int *__restrict__ off, const int *__restrict__ idx, int nb, int npairs,
+                                   Images P, const float *__restrict__ tscale, double *__restrict__ G)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= npairs) return;
+    const int i = owner_of(off, nb, q), j = idx[q];
+    double dx, dy;
+    pair_horizontal(xb, i, j, P, dx, dy);
+    const double rho = sqrt(dx * dx + dy * dy);
+    const double c = rho > 0 ? dx / rho : 1.0, s = rho > 0 ? dy / rho : 0.0;
+    double Q[kModes][kModes];
+    mode_rotation(c, s, Q);
+    const float *y = Yf + (long long)q * kOut;
+    for (int a = 0; a < kModes; ++a) {
+        double row[kModes];  // (Q G')[a][:]
+        for (int l = 0; l < kModes; ++l) {
+            double acc = 0.0;
+            for (int k = 0; k < kModes; ++k)
+                acc += Q[a][k] * (double)y[kModes * k + l] * (double)tscale[kModes * k + l];
+            row[l] = acc;
+        }
+        for (int b = 0; b < kModes; ++b) {
+            double acc = 0.0;
+            for (int l = 0; l < kModes; ++l) acc += row[l] * Q[b][l];
+            G[121LL * q + kModes * a + b] = acc;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// augmented preconditioner apply
+
+// mode moments X_b^T lambda_b of every body (one warp per body)
+__global__ void body_moments_kernel(const double *__restrict__ r, const double *__restrict__ xb,
+                                    const int *__restrict__ boff, int nb, const double *__restrict__ lam,
+                                    double *__restrict__ mom)
+{
+    const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (b >= nb) return;
+    const int o = boff[b], nbl = boff[b + 1] - o;
+    double acc[kModes];
+#pragma unroll
+    for (int k = 0; k < kModes; ++k) acc[k] = 0.0;
+    for (int p = lane; p < nbl; p += 32) {
+        const int i = o + p;
+        const double dx = r[3 * i] - xb[3 * b], dy = r[3 * i + 1] - xb[3 * b + 1], dz = r[3 * i + 2] - xb[3 * b + 2];
+        const double lx = lam[3 * i], ly = lam[3 * i + 1], lz = lam[3 * i + 2];
+#pragma unroll
+        for (int k = 0; k < kModes; ++k) {
+            double vx, vy, vz;
+            mode_velocity(k, dx, dy, dz, vx, vy, vz);
+            acc[k] += vx * lx + vy * ly + vz * lz;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kModes; ++k) {
+        for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], off);
+        if (lane == 0) mom[kModes * b + k] = acc[k];
+    }
+}
+
+// v_i = sum_{exact j} M_ij lambda_j + X_i sum_{learned j} G_ij mom_j on body i's
+// blob rows (one CTA per body; exact neighbours' blobs staged in shared memory)
+__global__ void nf_near_kernel(const double *__restrict__ r, const double *__restrict__ xb,
+                               const int *__restrict__ boff, const int *__restrict__ ex_off,
+                               const int *__restrict__ ex_idx, const int *__restrict__ ln_off,
+                               const int *__restrict__ ln_idx, const double *__restrict__ G,
+                               const double *__restrict__ mom, const double *__restrict__ lam, double a, double nf,
+                               Images P, double *__restrict__ v)
+{
+    extern __shared__ double src[];  // 6 per source blob: x, y, clamped z, damped lambda
+    __shared__ double cm[kModes];
+    const int i = blockIdx.x;
+    const int o = boff[i], nbl = boff[i + 1] - o;
+    const double inva = 1.0 / a;
+    if (threadIdx.x < kModes) {
+        double acc = 0.0;
+        if (ln_off)
+            for (int q = ln_off[i]; q < ln_off[i + 1]; ++q) {
+                const double *Gq = G + 121LL * q + kModes * threadIdx.x;
+                const double *mj = mom + kModes * ln_idx[q];
+                for (int l = 0; l < kModes; ++l) acc += Gq[l] * mj[l];
+            }
+        cm[threadIdx.x] = acc;
+    }
+    __syncthreads();
+    const int e0 = ex_off ? ex_off[i] : 0, e1 = ex_off ? ex_off[i + 1] : 0;
+    for (int t0 = 0; t0 < nbl; t0 += blockDim.x) {
+        const int p = t0 + threadIdx.x;
+        const bool valid = p < nbl;
+        const int ti = o + (valid ? p : 0);
+        const double xi = r[3 * ti], yi = r[3 * ti + 1], zi = r[3 * ti + 2];
+        const double zie = wall_clamp(zi, a);
+        double ux = 0.0, uy = 0.0, uz = 0.0;
+        for (int q = e0; q < e1; ++q) {
+            const int j = ex_idx[q];
+            const int oj = boff[j], nj = boff[j + 1] - oj;
+            __syncthreads();
+            for (int s = threadIdx.x; s < nj; s += blockDim.x) {
+                const int sj = oj + s;
+                const double zj = r[3 * sj + 2], bj = wall_damp(zj, a);
+                src[6 * s] = r[3 * sj];
+                src[6 * s + 1] = r[3 * sj + 1];
+                src[6 * s + 2] = wall_clamp(zj, a);
+                src[6 * s + 3] = bj * lam[3 * sj];
+                src[6 * s + 4] = bj * lam[3 * sj + 1];
+                src[6 * s + 5] = bj * lam[3 * sj + 2];
+            }
+            __syncthreads();
+            if (valid)
+                for (int s = 0; s < nj; ++s)
+                    wall_uf_pair(xi, yi, zie, src[6 * s], src[6 * s + 1], src[6 * s + 2], inva, P, src[6 * s + 3],
+                                 src[6 * s + 4], src[6 * s + 5], ux, uy, uz);
+        }
+        if (valid) {
+            const double sc = nf * wall_damp(zi, a);
+            double wx = sc * ux, wy = sc * uy, wz = sc * uz;
+            const double dx = xi - xb[3 * i], dy = yi - xb[3 * i + 1], dz = zi - xb[3 * i + 2];
+#pragma unroll
+            for (int k = 0; k < kModes; ++k) {
+                double mx, my, mz;
+                mode_velocity(k, dx, dy, dz, mx, my, mz);
+                wx += mx * cm[k];
+                wy += my * cm[k];
+                wz += mz * cm[k];
+            }
+            v[3LL * ti] = wx;
+            v[3LL * ti + 1] = wy;
+            v[3LL * ti + 2] = wz;
+        }
+    }
+}
+
+__global__ void nf_subtract_kernel(double *__restrict__ y, const double *__restrict__ z, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] -= z[i];
+}
+
+static Images images_of(const RigidSystem &S) { return Images{S.L[0], S.L[1], S.L[2]}; }
+
+int nearfield_apply_pc(RigidSystem &S, const double *x, double *y)
+{
+    if (int rc = rigid_apply_pc_plain(S, x, y)) return rc;
+    const double nf = 1.0 / (8.0 * kPi * S.eta * S.a);
+    if (S.nf_ln_pairs > 0)
+        body_moments_kernel<<<(S.nb * 32 + 127) / 128, 128, 0, S.st>>>(S.r, S.xb, S.boff, S.nb, y, S.nf_mom);
+    const int nt = 64;
+    const size_t sm = sizeof(double) * 2 * (size_t)S.max_m;
+    if (sm > 48 * 1024)
+        RMW_CUDA(cudaFuncSetAttribute(nf_near_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    nf_near_kernel<<<S.nb, nt, sm, S.st>>>(S.r, S.xb, S.boff, S.nf_ex_pairs ? S.nf_ex_off : nullptr, S.nf_ex_idx,
+                                            S.nf_ln_pairs ? S.nf_ln_off : nullptr, S.nf_ln_idx, S.nf_G, S.nf_mom, y,
+                                            S.a, nf, images_of(S), S.nf_v);
+    RMW_CHECK_LAUNCH("near-field velocities");
+    if (int rc = rigid_apply_pc_plain(S, S.nf_v, S.nf_z)) return rc;
+    const long long n = S.sys_size();
+    nf_subtract_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S.st>>>(y, S.nf_z, n);
+    RMW_CHECK_LAUNCH("near-field preconditioner apply");
+    return RMW_OK;
+}
+
+// neighbour list of one distance band into (off, idx) (device, reallocated)
+static int build_band(RigidSystem &S, double lo, double hi, const long long *susp, int **off_p, int **idx_p,
+                      int *count)
+{
+    cudaStream_t st = S.st;
+    if (*off_p) { cudaFree(*off_p); *off_p = nullptr; }
+    if (*idx_p) { cudaFree(*idx_p); *idx_p = nullptr; }
+    *count = 0;
+    RMW_CUDA(cudaMalloc(off_p, sizeof(int) * (S.nb + 1)));
+    const Images P = images_of(S);
+    nbr_band_kernel<<<(S.nb + 127) / 128, 128, 0, st>>>(S.xb, S.nb, lo * lo, hi * hi, P, susp, nullptr, *off_p);
+    RMW_CHECK_LAUNCH("neighbour count");
+    std::vector<int> cnt(S.nb), off(S.nb + 1, 0);
+    RMW_CUDA(cudaMemcpyAsync(cnt.data(), *off_p, sizeof(int) * S.nb, cudaMemcpyDeviceToHost, st));
+    RMW_CUDA(cudaStreamSynchronize(st));
+    for (int b = 0; b < S.nb; ++b) off[b + 1] = off[b] + cnt[b];
+    RMW_CUDA(cudaMemcpyAsync(*off_p, off.data(), sizeof(int) * (S.nb + 1), cudaMemcpyHostToDevice, st));
+    RMW_CUDA(cudaMalloc(idx_p, sizeof(int) * std::max(1, off[S.nb])));
+    nbr_band_kernel<<<(S.nb + 127) / 128, 128, 0, st>>>(S.xb, S.nb, lo * lo, hi * hi, P, susp, *off_p, *idx_p);
+    RMW_CHECK_LAUNCH("neighbour fill");
+    RMW_CUDA(cudaStreamSynchronize(st));
+    *count = off[S.nb];
+    return RMW_OK;
+}
+
+}  // namespace rmw
+
+// ---------------------------------------------------------------------------
+// C ABI
+using rmw::NearfieldNet;
+using rmw::RigidSystem;
+
+extern "C" {
+
+int rmw_rigid_pair_coupling(void *sys, double *out)
+{
+    if (!sys || !out) return rmw::fail(RMW_ERR_ARG, "null argument");
+    RigidSystem &S = *(RigidSystem *)sys;
+    if (!S.pc_ready) return rmw::fail(RMW_ERR_ARG, "build the preconditioner first (it forms each body's M^-1)");
+    if (S.nb % 2) return rmw::fail(RMW_ERR_ARG, "two-body samples need an even body count");
+    const int nt = 128;
+    const size_t sm = sizeof(double) * (4 * (size_t)S.max_m * rmw::kModes + 3 * rmw::kModes * rmw::kModes +
+                                        2 * rmw::kModes * rmw::kModes);
+    if (sm > 227 * 1024) return rmw::fail(RMW_ERR_ARG, "bodies too large for the two-body coupling kernel");
+    if (sm > 48 * 1024)
+        RMW_CUDA(cudaFuncSetAttribute(rmw::pair_fts_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    RMW_CUDA(cudaMemsetAsync(S.dstatus, 0, sizeof(int), S.st));
+    const double nf = 1.0 / (8.0 * rmw::kPi * S.eta * S.a);
+    rmw::pair_fts_kernel<<<S.nb / 2, nt, sm, S.st>>>(S.r, S.xb, S.boff, S.moff, S.minv, S.a, nf,
+                                                      rmw::Images{S.L[0], S.L[1], S.L[2]}, S.max_m, out, S.dstatus);
+    RMW_CHECK_LAUNCH("two-body mode coupling");
+    int h = 0;
+    RMW_CUDA(cudaMemcpyAsync(&h, S.dstatus, sizeof(int), cudaMemcpyDeviceToHost, S.st));
+    RMW_CUDA(cudaStreamSynchronize(S.st));
+    if (h) return rmw::fail(RMW_ERR_NONFINITE, "singular mode Gram matrix");
+    return RMW_OK;
+}
+
+int rmw_nearfield_create(void **net_out, double body_radius, double cutoff, unsigned long long seed)
+{
+    if (!net_out) return rmw::fail(RMW_ERR_ARG, "null argument");
+    NearfieldNet *N = new NearfieldNet();
+    N->radius = body_radius;
+    N->cutoff = cutoff;
+    cudaGetDevice(&N->device);
+    // He-style initialisation from a fixed-seed generator (host, deterministic)
+    std::vector<float> w(rmw::kNW), b(rmw::kNB, 0.0f);
+    unsigned long long x = seed ? seed : 1;
+    auto uni = [&]() {
+        x ^= x << 13; x ^= x >> 7; x ^= x << 17;
+        return (double)(x >> 11) / 9007199254740992.0;
+    };
+    for (int l = 0; l < rmw::kLayers; ++l) {
+        const int ni = rmw::layer_in(l), no = rmw::layer_out(l);
+        const double sc = std::sqrt(6.0 / (l == 0 ? rmw::kFeat : ni)) * (l == rmw::kLayers - 1 ? 0.25 : 1.0);
+        for (int o = 0; o < no; ++o)
+            for (int i = 0; i < ni; ++i) {
+                const bool live = (l > 0 || i < rmw::kFeat) && (l < rmw::kLayers - 1 || o < rmw::kTarget);
+                w[rmw::wofs(l) + o * ni + i] = live ? (float)((2.0 * uni() - 1.0) * sc) : 0.0f;
+            }
+    }
+    for (int i = 0; i < rmw::kFeat; ++i) { N->fmean[i] = 0.f; N->fscale[i] = 1.f; }
+    for (int o = 0; o < rmw::kTarget; ++o) N->tscale[o] = 1.f;
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t c) { if (e == cudaSuccess) e = c; };
+    chk(cudaMalloc(&N->w, sizeof(float) * rmw::kNW));
+    chk(cudaMalloc(&N->b, sizeof(float) * rmw::kNB));
+    chk(cudaMalloc(&N->wb, sizeof(__nv_bfloat16) * rmw::kNW));
+    chk(cudaMalloc(&N->adam, sizeof(float) * 2 * (rmw::kNW + rmw::kNB)));
+    chk(cudaMalloc(&N->dnorm, sizeof(float) * (2 * rmw::kFeat + rmw::kTarget)));
+    if (e == cudaSuccess) {
+        std::vector<__nv_bfloat16> wb(rmw::kNW);
+        for (int i = 0; i < rmw::kNW; ++i) wb[i] = __float2bfloat16_rn(w[i]);
+        chk(cudaMemcpy(N->w, w.data(), sizeof(float) * rmw::kNW, cudaMemcpyHostToDevice));
+        chk(cudaMemcpy(N->b, b.data(), sizeof(float) * rmw::kNB, cudaMemcpyHostToDevice));
+        chk(cudaMemcpy(N->wb, wb.data(), sizeof(__nv_bfloat16) * rmw::kNW, cudaMemcpyHostToDevice));
+        chk(cudaMemset(N->adam, 0, sizeof(float) * 2 * (rmw::kNW + rmw::kNB)));
+        std::vector<float> norm(2 * rmw::kFeat + rmw::kTarget, 1.0f);
+        for (int i = 0; i < rmw::kFeat; ++i) norm[i] = 0.0f;
+        chk(cudaMemcpy(N->dnorm, norm.data(), sizeof(float) * norm.size(), cudaMemcpyHostToDevice));
+    }
+    if (e != cudaSuccess) {
+        cudaFree(N->w); cudaFree(N->b); cudaFree(N->wb); cudaFree(N->adam); cudaFree(N->dnorm);
+        delete N;
+        return rmw::cuda_fail(e, "rmw_nearfield_create");
+    }
+    *net_out = N;
+    return RMW_OK;
+}
+
+int rmw_nearfield_destroy(void *net)
+{
+    if (!net) return RMW_OK;
+    NearfieldNet *N = (NearfieldNet *)net;
+    cudaFree(N->w); cudaFree(N->b); cudaFree(N->wb); cudaFree(N->adam); cudaFree(N->dnorm);
+    delete N;
+    return RMW_OK;
+}
+
+// Parameters in and out (FP32 master weights, biases, normalisation): for
+// checkpoints and for the gradient check.  Sizes: rmw_nearfield_sizes.
+int rmw_nearfield_sizes(int *n_weights, int *n_biases, int *n_in, int *width, int *n_out, int *n_target)
+{
+    if (n_weights) *n_weights = rmw::kNW;
+    if (n_biases) *n_biases = rmw::kNB;
+    if (n_in) *n_in = rmw::kIn;
+    if (width) *width = rmw::kWidth;
+    if (n_out) *n_out = rmw::kOut;
+    if (n_target) *n_target = rmw::kTarget;
+    return RMW_OK;
+}
+
+int rmw_nearfield_get(void *net, float *w_host, float *b_host, float *norm_host)
+{
+    if (!net) return rmw::fail(RMW_ERR_ARG, "null network");
+    NearfieldNet *N = (NearfieldNet *)net;
+    if (w_host) RMW_CUDA(cudaMemcpy(w_host, N->w, sizeof(float) * rmw::kNW, cudaMemcpyDeviceToHost));
+    if (b_host) RMW_CUDA(cudaMemcpy(b_host, N->b, sizeof(float) * rmw::kNB, cudaMemcpyDeviceToHost));
+    if (norm_host) {
+        std::memcpy(norm_host, N->fmean, sizeof(float) * rmw::kFeat);
+        std::memcpy(norm_host + rmw::kFeat, N->fscale, sizeof(float) * rmw::kFeat);
+        std::memcpy(norm_host + 2 * rmw::kFeat, N->tscale, sizeof(float) * rmw::kTarget);
+    }
+    return RMW_OK;
+}
+
+int rmw_nearfield_set(void *net, const float *w_host, const float *b_host, const float *norm_host)
+{
+    if (!net) return rmw::fail(RMW_ERR_ARG, "null network");
+    NearfieldNet *N = (NearfieldNet *)net;
+    if (w_host) {
+        std::vector<__nv_bfloat16> wb(rmw::kNW);
+        for (int i = 0; i < rmw::kNW; ++i) wb[i] = __float2bfloat16_rn(w_host[i]);
+        RMW_CUDA(cudaMemcpy(N->w, w_host, sizeof(float) * rmw::kNW, cudaMemcpyHostToDevice));
+        RMW_CUDA(cudaMemcpy(N->wb, wb.data(), sizeof(__nv_bfloat16) * rmw::kNW, cudaMemcpyHostToDevice));
+    }
+    if (b_host) RMW_CUDA(cudaMemcpy(N->b, b_host, sizeof(float) * rmw::kNB, cudaMemcpyHostToDevice));
+    if (norm_host) {
+        std::memcpy(N->fmean, norm_host, sizeof(float) * rmw::kFeat);
+        std::memcpy(N->fscale, norm_host + rmw::kFeat, sizeof(float) * rmw::kFeat);
+        std::memcpy(N->tscale, norm_host + 2 * rmw::kFeat, sizeof(float) * rmw::kTarget);
+        RMW_CUDA(cudaMemcpy(N->dnorm, norm_host, sizeof(float) * (2 * rmw::kFeat + rmw::kTarget), cudaMemcpyHostToDevice));
+    }
+    return RMW_OK;
+}
+
+// One forward + backward pass on a host batch of already normalised inputs
+// (P x 16, zero-padded) and targets (P x 121): gradients of the mean squared
+// error with respect to every weight and bias (for the gradient check).
+int rmw_nearfield_grad(void *net, const float *X_host, const float *T_host, int P, float *gW_host, float *gb_host,
+                       float *loss_host)
+{
+    if (!net || !X_host || !T_host || P <= 0) return rmw::fail(RMW_ERR_ARG, "bad argument");
+    NearfieldNet *N = (NearfieldNet *)net;
+    cudaStream_t st = 0;
+    const int Pp = ((P + 63) / 64) * 64;
+    rmw::NetWork W;
+    if (int rc = W.alloc(Pp, st)) return rc;
+    std::vector<__nv_bfloat16> xb((size_t)Pp * rmw::kIn, __float2bfloat16_rn(0.f));
+    for (int p = 0; p < P; ++p)
+        for (int i = 0; i < rmw::kIn; ++i) xb[(size_t)p * rmw::kIn + i] = __float2bfloat16_rn(X_host[(size_t)p * rmw::kIn + i]);
+    void *buf = nullptr;
+    const size_t bytes = sizeof(__nv_bfloat16) * xb.size() + sizeof(float) * ((size_t)P * rmw::kTarget + rmw::kNW + rmw::kNB + 1);
+    RMW_CUDA(cudaMalloc(&buf, bytes));
+    __nv_bfloat16 *dX = (__nv_bfloat16 *)buf;
+    float *dT = (float *)(dX + xb.size());
+    float *gW = dT + (size_t)P * rmw::kTarget, *gb = gW + rmw::kNW, *loss = gb + rmw::kNB;
+    RMW_CUDA(cudaMemcpy(dX, xb.data(), sizeof(__nv_bfloat16) * xb.size(), cudaMemcpyHostToDevice));
+    RMW_CUDA(cudaMemcpy(dT, T_host, sizeof(float) * (size_t)P * rmw::kTarget, cudaMemcpyHostToDevice));
+    RMW_CUDA(cudaMemset(loss, 0, sizeof(float)));
+    int rc = rmw::net_backward(*N, dX, dT, P, W, gW, gb, loss);
+    if (rc == RMW_OK) {
+        RMW_CUDA(cudaMemcpy(gW_host, gW, sizeof(float) * rmw::kNW, cudaMemcpyDeviceToHost));
+        RMW_CUDA(cudaMemcpy(gb_host, gb, sizeof(float) * rmw::kNB, cudaMemcpyDeviceToHost));
+        RMW_CUDA(cudaMemcpy(loss_host, loss, sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    cudaFree(buf);
+    return rc;
+}
+
+// Forward pass on a host batch of normalised inputs (P x 16): outputs P x 121.
+int rmw_nearfield_forward(void *net, const float *X_host, int P, float *Y_host)
+{
+    if (!net || !X_host || !Y_host || P <= 0) return rmw::fail(RMW_ERR_ARG, "bad argument");
+    NearfieldNet *N = (NearfieldNet *)net;
+    const int Pp = ((P + 63) / 64) * 64;
+    rmw::NetWork W;
+    if (int rc = W.alloc(Pp, 0)) return rc;
+    std::vector<__nv_bfloat16> xb((size_t)Pp * rmw::kIn, __float2bfloat16_rn(0.f));
+    for (int p = 0; p < P; ++p)
+        for (int i = 0; i < rmw::kIn; ++i) xb[(size_t)p * rmw::kIn + i] = __float2bfloat16_rn(X_host[(size_t)p * rmw::kIn + i]);
+    __nv_bfloat16 *dX = nullptr;
+    RMW_CUDA(cudaMalloc(&dX, sizeof(__nv_bfloat16) * xb.size()));
+    RMW_CUDA(cudaMemcpy(dX, xb.data(), sizeof(__nv_bfloat16) * xb.size(), cudaMemcpyHostToDevice));
+    int rc = rmw::net_forward(*N, dX, Pp, nullptr, W.A, W.Yf, 0);
+    if (rc == RMW_OK) {
+        std::vector<float> y((size_t)Pp * rmw::kOut);
+        RMW_CUDA(cudaMemcpy(y.data(), W.Yf, sizeof(float) * y.size(), cudaMemcpyDeviceToHost));
+        for (int p = 0; p < P; ++p)
+            for (int o = 0; o < rmw::kTarget; ++o) Y_host[(size_t)p * rmw::kTarget + o] = y[(size_t)p * rmw::kOut + o];
+    }
+    cudaFree(dX);
+    return rc;
+}
+
+// Train on device data feat (S x 3: horizontal distance, z_i, z_j over the
+// body radius) and targ (S x 121: the pair-frame 11x11 mode coupling), Adam,
+// mean squared error on normalised targets.  Sets the normalisation from the
+// data.
+// loss_host (optional, steps entries) receives the loss of every step.
+int rmw_nearfield_train(void *net, const float *feat, const float *targ, int S, int steps, int batch, float lr,
+                        unsigned long long seed, float *loss_host, void *stream)
+{
+    if (!net || !feat || !targ || S <= 0 || steps <= 0 || batch <= 0) return rmw::fail(RMW_ERR_ARG, "bad argument");
+    NearfieldNet *N = (NearfieldNet *)net;
+    cudaStream_t st = rmw::as_stream(stream);
+    // normalisation from the data (host copy of S x 39 floats)
+    std::vector<float> hf((size_t)S * rmw::kFeat), ht((size_t)S * rmw::kTarget);
+    RMW_CUDA(cudaMemcpyAsync(hf.data(), feat, sizeof(float) * hf.size(), cudaMemcpyDeviceToHost, st));
+    RMW_CUDA(cudaMemcpyAsync(ht.data(), targ, sizeof(float) * ht.size(), cudaMemcpyDeviceToHost, st));
+    RMW_CUDA(cudaStreamSynchronize(st));
+    std::vector<float> norm(2 * rmw::kFeat + rmw::kTarget);
+    for (int i = 0; i < rmw::kFeat; ++i) {
+        double m = 0, v = 0;
+        for (int s = 0; s < S; ++s) m += hf[(size_t)s * rmw::kFeat + i];
+        m /= S;
+        for (int s = 0; s < S; ++s) v += (hf[(size_t)s * rmw::kFeat + i] - m) * (hf[(size_t)s * rmw::kFeat + i] - m);
+        norm[i] = (float)m;
+        norm[rmw::kFeat + i] = (float)std::max(std::sqrt(v / S), 1e-6);
+    }
+    // per-output RMS, floored at 5% of the largest: outputs that vanish for a
+    // sphere by the pair's mirror symmetry carry only orientation noise, which
+    // must not be blown up to unit scale
+    double tmax = 0.0;
+    for (int o = 0; o < rmw::kTarget; ++o) {
+        double v = 0;
+        for (int s = 0; s < S; ++s) v += (double)ht[(size_t)s * rmw::kTarget + o] * ht[(size_t)s * rmw::kTarget + o];
+        norm[2 * rmw::kFeat + o] = (float)std::sqrt(v / S);
+        tmax = std::max(tmax, (double)norm[2 * rmw::kFeat + o]);
+    }
+    for (int o = 0; o < rmw::kTarget; ++o)
+        norm[2 * rmw::kFeat + o] = (float)std::max((double)norm[2 * rmw::kFeat + o], std::max(0.05 * tmax, 1e-30));
+    if (int rc = rmw_nearfield_set(net, nullptr, nullptr, norm.data())) return rc;
+    const int Pp = ((batch + 63) / 64) * 64;
+    rmw::NetWork W;
+    if (int rc = W.alloc(Pp, st)) return rc;
+    void *buf = nullptr;
+    const size_t bytes = sizeof(__nv_bfloat16) * (size_t)Pp * rmw::kIn +
+                         sizeof(float) * ((size_t)Pp * rmw::kTarget + rmw::kNW + rmw::kNB + steps);
+    RMW_CUDA(cudaMallocAsync(&buf, bytes, st));
+    __nv_bfloat16 *X = (__nv_bfloat16 *)buf;
+    float *T = (float *)(X + (size_t)Pp * rmw::kIn);
+    float *gW = T + (size_t)Pp * rmw::kTarget, *gb = gW + rmw::kNW, *loss = gb + rmw::kNB;
+    RMW_CUDA(cudaMemsetAsync(loss, 0, sizeof(float) * steps, st));
+    const float b1 = 0.9f, b2 = 0.999f;
+    float *mW = N->adam, *vW = N->adam + rmw::kNW, *mB = N->adam + 2 * rmw::kNW, *vB = mB + rmw::kNB;
+    int rc = RMW_OK;
+    for (int t = 0; t < steps && rc == RMW_OK; ++t) {
+        rmw::gather_batch_kernel<<<(Pp + 127) / 128, 128, 0, st>>>(feat, targ, S, N->dnorm, N->dnorm + rmw::kFeat,
+                                                                  N->dnorm + 2 * rmw::kFeat, Pp, batch, seed, t, X, T);
+        rc = rmw::net_backward(*N, X, T, batch, W, gW, gb, loss + t);
+        if (rc) break;
+        const float c1 = 1.f - std::pow(b1, (float)(t + 1)), c2 = 1.f - std::pow(b2, (float)(t + 1));
+        rmw::adam_kernel<<<(rmw::kNW + 255) / 256, 256, 0, st>>>(N->w, gW, mW, vW, N->wb, rmw::kNW, lr, b1, b2, c1,
+                                                                c2, 1e-8f);
+        rmw::adam_kernel<<<(rmw::kNB + 255) / 256, 256, 0, st>>>(N->b, gb, mB, vB, nullptr, rmw::kNB, lr, b1, b2, c1,
+                                                                c2, 1e-8f);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (rc == RMW_OK && e != cudaSuccess) rc = rmw::cuda_fail(e, "near-field training");
+    if (rc == RMW_OK && loss_host)
+        RMW_CUDA(cudaMemcpyAsync(loss_host, loss, sizeof(float) * steps, cudaMemcpyDeviceToHost, st));
+    cudaFreeAsync(buf, st);
+    RMW_CUDA(cudaStreamSynchronize(st));
+    return rc;
+}
+
+// Switch a handle's preconditioner (after rmw_rigid_build_pc) to the
+// near-field augmented form: exact blob-level couplings for body pairs closer
+// than exact_cutoff, network-predicted mode couplings for pairs from there to
+// the network's cutoff (net may be NULL: exact pairs only).  Pairs are found
+// within one suspension.  net == NULL and exact_cutoff <= 0 switch back to the
+// block-diagonal form.  n_pairs_host (optional, 2 entries) receives the
+// numbers of ordered exact and learned pairs.
+int rmw_rigid_set_nearfield(void *sys, void *net, double exact_cutoff, int64_t *n_pairs_host)
+{
+    if (!sys) return rmw::fail(RMW_ERR_ARG, "null handle");
+    RigidSystem &S = *(RigidSystem *)sys;
+    if (n_pairs_host) n_pairs_host[0] = n_pairs_host[1] = 0;
+    const double lo = exact_cutoff > 0 ? exact_cutoff : 0.0;
+    if (!net && !(lo > 0)) {
+        S.nf_on = false;
+        return RMW_OK;
+    }
+    if (!S.pc_ready) return rmw::fail(RMW_ERR_ARG, "build the preconditioner first");
+    NearfieldNet *N = (NearfieldNet *)net;
+    const double hi = N ? std::max(N->cutoff, lo) : lo;
+    cudaStream_t st = S.st;
+    S.nf_on = false;
+    long long *susp = nullptr;
+    if (!S.susp_body_off.empty()) {
+        std::vector<long long> sb(S.nb);
+        for (size_t k = 0; k + 1 < S.susp_body_off.size(); ++k)
+            for (long long b = S.susp_body_off[k]; b < S.susp_body_off[k + 1]; ++b) sb[b] = (long long)k;
+        RMW_CUDA(cudaMalloc(&susp, sizeof(long long) * S.nb));
+        RMW_CUDA(cudaMemcpy(susp, sb.data(), sizeof(long long) * S.nb, cudaMemcpyHostToDevice));
+    }
+    int rc = RMW_OK;
+    S.nf_ex_pairs = S.nf_ln_pairs = 0;
+    if (lo > 0) rc = rmw::build_band(S, 0.0, lo, susp, &S.nf_ex_off, &S.nf_ex_idx, &S.nf_ex_pairs);
+    if (rc == RMW_OK && N && hi > lo) rc = rmw::build_band(S, lo, hi, susp, &S.nf_ln_off, &S.nf_ln_idx, &S.nf_ln_pairs);
+    if (susp) cudaFree(susp);
+    if (rc) return rc;
+    if (!S.nf_mom) RMW_CUDA(cudaMalloc(&S.nf_mom, sizeof(double) * rmw::kModes * S.nb));
+    if (!S.nf_v) {
+        RMW_CUDA(cudaMalloc(&S.nf_v, sizeof(double) * S.sys_size()));
+        RMW_CUDA(cudaMemset(S.nf_v, 0, sizeof(double) * S.sys_size()));  // force rows stay zero
+    }
+    if (!S.nf_z) RMW_CUDA(cudaMalloc(&S.nf_z, sizeof(double) * S.sys_size()));
+    const int np = S.nf_ln_pairs;
+    if (S.nf_G) { cudaFree(S.nf_G); S.nf_G = nullptr; }
+    if (np > 0) {
+        RMW_CUDA(cudaMalloc(&S.nf_G, sizeof(double) * 121 * (size_t)np));
+        const int Pp = ((np + 63) / 64) * 64;
+        const rmw::Images P{S.L[0], S.L[1], S.L[2]};
+        rmw::NetWork W;
+        if (int rc2 = W.alloc(Pp, st)) return rc2;
+        __nv_bfloat16 *X = nullptr;
+        RMW_CUDA(cudaMallocAsync(&X, sizeof(__nv_bfloat16) * (size_t)Pp * rmw::kIn, st));
+        rmw::pair_features_kernel<<<(Pp + 127) / 128, 128, 0, st>>>(S.xb, S.nf_ln_off, S.nf_ln_idx, S.nb, np,
+                                                                   1.0 / N->radius, P, N->dnorm, X, Pp);
+        if (int rc2 = rmw::net_forward(*N, X, Pp, nullptr, W.A, W.Yf, st)) return rc2;
+        rmw::pair_blocks_kernel<<<(np + 127) / 128, 128, 0, st>>>(W.Yf, S.xb, S.nf_ln_off, S.nf_ln_idx, S.nb, np, P,
+                                                                 N->dnorm + 2 * rmw::kFeat, S.nf_G);
+        RMW_CUDA(cudaFreeAsync(X, st));
+    }
+    RMW_CHECK_LAUNCH("near-field attach");
+    RMW_CUDA(cudaStreamSynchronize(st));
+    S.nf_on = true;
+    if (n_pairs_host) {
+        n_pairs_host[0] = S.nf_ex_pairs;
+        n_pairs_host[1] = S.nf_ln_pairs;
+    }
+    return RMW_OK;
+}
+
+}  // extern "C"

@@ -496,6 +496,12 @@ int rigid_apply(RigidSystem &S, const double *x, double *y, int mode)
 int rigid_apply_pc(RigidSystem &S, const double *x, double *y)
 {
     if (!S.pc_ready) return fail(RMW_ERR_ARG, "preconditioner not built (call rmw_rigid_build_pc)");
+    if (S.nf_on) return nearfield_apply_pc(S, x, y);
+    return rigid_apply_pc_plain(S, x, y);
+}
+
+int rigid_apply_pc_plain(RigidSystem &S, const double *x, double *y)
+{
     const int nt = 128;
     const size_t sm = sizeof(double) * (2 * (size_t)S.max_m + 6 * (nt / 32 + 1));
     if (sm > 48 * 1024)
@@ -558,7 +564,8 @@ static void free_system(RigidSystem *S)
     cudaGetDevice(&cur);
     cudaSetDevice(S->device);
     void *ptrs[] = {S->boff, S->blob_body, S->moff, S->r, S->xb, S->minv, S->minvK, S->nmat, S->lfac, S->linv,
-                    S->dstatus, S->tmp3n, S->perm};
+                    S->dstatus, S->tmp3n, S->perm, S->nf_ex_off, S->nf_ex_idx, S->nf_ln_off, S->nf_ln_idx,
+                    S->nf_G, S->nf_mom, S->nf_v, S->nf_z};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (S->batch) {
@@ -659,6 +666,7 @@ int rmw_rigid_set_configuration(void *sys, const double *r_blobs, const double *
     RMW_CUDA(cudaMemcpyAsync(S->r, r_blobs, sizeof(double) * 3 * S->n, cudaMemcpyDeviceToDevice, S->st));
     RMW_CUDA(cudaMemcpyAsync(S->xb, x_bodies, sizeof(double) * 3 * S->nb, cudaMemcpyDeviceToDevice, S->st));
     S->pc_ready = S->stoch_ready = false;
+    S->nf_on = false;  // neighbour pairs and coupling blocks belong to the old configuration
     return RMW_OK;
 }
 

@@ -40,14 +40,28 @@ struct RigidSystem {
     std::vector<long long> susp_body_off;  // bodies of suspension k: [off[k], off[k+1])
     std::vector<long long> susp_off;       // instance-major offsets of the system vector
     long long *perm = nullptr;             // device: instance-major index -> [lambda; U] index
+    // near-field augmented preconditioner (rmw_rigid_set_nearfield): CSR
+    // neighbour lists by owner body of the exact blob-level pairs and of the
+    // pairs whose 11x11 mode coupling the network predicts
+    bool nf_on = false;
+    int nf_ex_pairs = 0, nf_ln_pairs = 0;
+    int *nf_ex_off = nullptr, *nf_ex_idx = nullptr;
+    int *nf_ln_off = nullptr, *nf_ln_idx = nullptr;
+    double *nf_G = nullptr;    // 121 per learned entry (lab frame)
+    double *nf_mom = nullptr;  // 11 mode moments per body
+    double *nf_v = nullptr;    // sys_size: near-field blob velocities, force rows zero
+    double *nf_z = nullptr;    // sys_size: second block-diagonal solve
 
     long long sys_size() const { return 3LL * n + 6LL * nb; }
 };
 
 // y = A x with A = [[M, -K], [-K^T, 0]] (multi_bodies.py:424-471); mode = RMW_MODE_*.
 int rigid_apply(RigidSystem &S, const double *x, double *y, int mode);
-// y = P^-1 x (block-diagonal preconditioner, multi_bodies.py:825-861).
+// y = P^-1 x (block-diagonal preconditioner, multi_bodies.py:825-861, or its
+// near-field augmented form when one is attached).
 int rigid_apply_pc(RigidSystem &S, const double *x, double *y);
+// the block-diagonal form alone
+int rigid_apply_pc_plain(RigidSystem &S, const double *x, double *y);
 // y = L^-1 M L^-T w on the blob space (det_stoch mobility_pc, multi_bodies.py:591-606).
 int rigid_mobility_pc(RigidSystem &S, const double *w, double *y, int mode);
 // y = L w (det_stoch P_inv_mult, multi_bodies.py:609-615).
@@ -56,6 +70,8 @@ int rigid_P_inv_mult(RigidSystem &S, const double *w, double *y);
 // uses the multi-right-hand-side pair kernel.
 int rigid_mobility_pc_multi(RigidSystem &S, const double *W, double *Y, int nvec, int mode, double *tmp);
 int rigid_P_inv_mult_multi(RigidSystem &S, const double *W, double *Y, int nvec);
+// near-field augmented preconditioner apply, nearfield.cu
+int nearfield_apply_pc(RigidSystem &S, const double *x, double *y);
 // M v on the handle's blobs (segmented by suspension when suspensions are set).
 int rigid_mobility(RigidSystem &S, const double *v, double *y, int mode);
 

@@ -1,0 +1,178 @@
+"""GPU: the near-field augmented preconditioner - two-body mode couplings
+(training targets) and the augmented apply against the oracle, the BF16
+tensor-core forward and the training gradients against the CPU oracle,
+training progress, and what the exact and the learned couplings gain over the
+plain block-diagonal preconditioner (with the fallback rule)."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle import nearfield as onf
+from oracle import rigid as orig
+from rigidmultiblobswall_gb300 import nearfield as nf
+from rigidmultiblobswall_gb300 import suspensions as S
+from rigidmultiblobswall_gb300.rigid import RigidSystem
+
+pytestmark = pytest.mark.gpu
+
+
+def _pairs_within(locs, lo, hi):
+    d = np.linalg.norm(locs[:, None] - locs[None], axis=-1)
+    n = locs.shape[0]
+    return [(i, j) for i in range(n) for j in range(n) if i != j and lo <= d[i, j] < hi]
+
+
+def test_pair_coupling_matches_oracle(cuda_device):
+    import torch
+    from rigidmultiblobswall_gb300 import _native
+    rng = np.random.default_rng(3)
+    shell = S.icosahedron(1.0)
+    a = 0.4
+    ns = 3
+    cen = np.array([[0.0, 0.0, 1.3], [2.9, 0.4, 1.9], [5.0, 5.0, 1.2], [5.3, 7.6, 2.7], [9.0, 0.0, 3.0],
+                    [9.0, 4.5, 1.1]])
+    q = S.random_quaternions(rng, 2 * ns)
+    r = S.blob_positions(cen, q, shell)
+    sys_ = RigidSystem([12] * (2 * ns), 1.0, a)
+    sys_.set_configuration(r, cen)
+    sys_.build_pc()
+    out = torch.empty(ns * 242, dtype=torch.float64, device=sys_.device)
+    _native.call("rmw_rigid_pair_coupling", sys_._h, out.data_ptr())
+    got = out.cpu().numpy().reshape(ns, 2, 11, 11)
+    for s in range(ns):
+        ri, rj = r[24 * s:24 * s + 12], r[24 * s + 12:24 * s + 24]
+        g01 = onf.pair_coupling(ri, rj, cen[2 * s], cen[2 * s + 1], 1.0, a)
+        g10 = onf.pair_coupling(rj, ri, cen[2 * s + 1], cen[2 * s], 1.0, a)
+        assert rel_err(got[s, 0], g01) <= 1e-10
+        assert rel_err(got[s, 1], g10) <= 1e-10
+    sys_.close()
+
+
+def _dense_suspension(n_bodies, seed):
+    susp = S.shells_42_4096(seed=seed, n_bodies=n_bodies)
+    sys_ = RigidSystem([42] * susp.n_bodies, susp.eta, susp.a)
+    sys_.set_configuration(susp.r_vectors(), susp.locations)
+    sys_.build_pc()
+    R = np.linalg.norm(susp.shell[0])
+    return susp, sys_, R
+
+
+def test_exact_nearfield_apply_matches_oracle(cuda_device):
+    susp, sys_, R = _dense_suspension(12, 31)
+    n_ex, n_ln = nf.attach_exact(sys_, 3 * R)
+    pairs = _pairs_within(susp.locations, 0.0, 3 * R)
+    assert n_ex == len(pairs) > 0 and n_ln == 0
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal(sys_.size)
+    got = sys_.apply_pc(x).cpu().numpy()
+    rig = orig.Rigid(susp.r_vectors(), susp.locations, np.arange(13) * 42, susp.eta, susp.a)
+    ref = onf.augmented_pc(rig, x, pairs, {})
+    assert rel_err(got, ref) <= 1e-10
+    nf.detach(sys_)
+    assert rel_err(sys_.apply_pc(x).cpu().numpy(), rig.apply_pc(x)) <= 1e-11
+    sys_.close()
+
+
+def test_forward_and_gradients_match_oracle(cuda_device):
+    rng = np.random.default_rng(1)
+    m = nf.NearfieldModel(body_radius=1.0, cutoff=3.0, seed=5)
+    w, b, _ = m.get_params()
+    b = (rng.standard_normal(b.size) * 0.1).astype(np.float32)
+    m.set_params(w, b, None)
+    P = 100
+    X = np.zeros((P, 16), dtype=np.float32)
+    X[:, :3] = rng.standard_normal((P, 3))
+    T = rng.standard_normal((P, onf.N_TARGET)).astype(np.float32)
+    Y = m.forward(X)
+    Yref, _, _ = onf.forward(w, b, X)
+    assert rel_err(Y, Yref) <= 5e-3
+    gW, gb, loss = m.grad(X, T)
+    gWr, gbr, lossr = onf.grad(w, b, X, T)
+    assert abs(loss - lossr) <= 1e-3 * lossr
+    assert rel_err(gW, gWr) <= 2e-2
+    assert rel_err(gb, gbr) <= 2e-2
+
+
+@pytest.fixture(scope="module")
+def trained(cuda_device):
+    shell = S.icosphere_42()
+    a = S.blob_radius_of(shell)
+    R = np.linalg.norm(shell[0])
+    feat, targ = nf.pair_training_data(shell, a, 1.0, 2048, d_range=(2 * R + 2 * a, 6 * R),
+                                       z_range=(1.1 * R, 3 * R), seed=11)
+    m = nf.NearfieldModel(body_radius=R, cutoff=6 * R, seed=2)
+    hist = m.train(feat, targ, steps=2000, batch=512, lr=2e-3)
+    return m, hist, R
+
+
+def test_training_reduces_the_loss(trained):
+    m, hist, _ = trained
+    assert np.isfinite(hist).all()
+    assert hist[-50:].mean() < 0.1 * hist[:10].mean()
+
+
+def test_learned_apply_matches_oracle(trained):
+    """The attached blocks are the network's outputs rotated into the lab
+    frame: the apply matches the oracle fed with the network's own outputs."""
+    m, _, R = trained
+    susp, sys_, _ = _dense_suspension(12, 31)
+    n_ex, n_ln = m.attach(sys_, exact_cutoff=3 * R)
+    locs = susp.locations
+    ex = _pairs_within(locs, 0.0, 3 * R)
+    ln = _pairs_within(locs, 3 * R, 6 * R)
+    assert (n_ex, n_ln) == (len(ex), len(ln)) and n_ln > 0
+    _, _, norm = m.get_params()
+    fmean, fscale, tscale = norm[:3], norm[3:6], norm[6:]
+    X = np.zeros((len(ln), 16), dtype=np.float32)
+    for k, (i, j) in enumerate(ln):
+        d = locs[j] - locs[i]
+        f = np.array([np.hypot(d[0], d[1]), locs[i, 2], locs[j, 2]]) / R
+        X[k, :3] = (f.astype(np.float32) - fmean) / fscale
+    Y = m.forward(X).astype(np.float64) * tscale
+    learned = {}
+    for k, (i, j) in enumerate(ln):
+        d = locs[j] - locs[i]
+        rho = np.hypot(d[0], d[1])
+        Q = onf.mode_rotation(d[0] / rho, d[1] / rho)
+        learned[(i, j)] = Q @ Y[k].reshape(11, 11) @ Q.T
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal(sys_.size)
+    got = sys_.apply_pc(x).cpu().numpy()
+    rig = orig.Rigid(susp.r_vectors(), locs, np.arange(13) * 42, susp.eta, susp.a)
+    ref = onf.augmented_pc(rig, x, ex, learned)
+    assert rel_err(got, ref) <= 1e-4  # a feature may round to a neighbouring BF16 value
+    sys_.close()
+
+
+def test_augmented_preconditioner_gain_and_fallback(trained):
+    """A dense suspension (area fraction 0.3, heights in [1.1R, 3R]): the exact
+    near field (< 3R), the learned couplings (< 6R) and both together must
+    each need fewer GMRES iterations than the plain block-diagonal
+    preconditioner and reach the same 1e-8 residual; a reference that no
+    preconditioner can beat triggers the fallback."""
+    m, _, R = trained
+    susp, sys_, _ = _dense_suspension(96, 21)
+    FT = np.zeros((susp.n_bodies, 6))
+    FT[:, 2] = -1.0
+    rhs = np.concatenate([np.zeros(3 * sys_.n_blobs), -FT.reshape(-1)])
+    rhs /= np.linalg.norm(rhs)
+    exact = nf.solve_with_fallback(sys_, None, rhs, mode="fp64", exact_cutoff=3 * R)
+    plain = exact["plain"]
+    learned = nf.solve_with_fallback(sys_, m, rhs, mode="fp64", reference=(plain["iterations"], plain["relres"]))
+    both = nf.solve_with_fallback(sys_, m, rhs, mode="fp64", reference=(plain["iterations"], plain["relres"]),
+                                  exact_cutoff=3 * R)
+    print("iterations: plain", plain["iterations"], "exact<3R", exact["augmented"]["iterations"],
+          "learned<6R", learned["augmented"]["iterations"], "exact<3R+learned<6R", both["augmented"]["iterations"],
+          "pairs", exact["augmented"]["pairs"], learned["augmented"]["pairs"], both["augmented"]["pairs"])
+    assert plain["relres"] <= 1e-8
+    for res in (exact, learned, both):
+        assert res["augmented"]["relres"] <= 1e-8
+        assert res["augmented"]["iterations"] < plain["iterations"]
+        assert res["kept"] == "augmented"
+    # both solutions have relative residual <= 1e-8; their difference is that
+    # times the conditioning of the saddle-point system
+    x_plain = plain["x"].cpu().numpy()
+    assert rel_err(both["augmented"]["x"].cpu().numpy(), x_plain) <= 1e-6
+    res2 = nf.solve_with_fallback(sys_, m, rhs, mode="fp64", reference=(1, 1e-12))
+    assert res2["kept"] == "plain"
+    sys_.close()

@@ -56,7 +56,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=8.0)
     p.add_argument("--large", action="store_true",
                    help="only run the 4096-shell (172,032-blob) solve comparison and print its JSON line")
-    p.add_argument("--large-modes", default="mixed,df64,fp64")
+    p.add_argument("--large-modes", default="mixed+nf,mixed,df64,fp64")
     return p.parse_args()
 
 
@@ -205,6 +205,27 @@ def time_product(kind, mode, rt, ft, out_fn, eta, a, steps, flush, stream):
     return {"ms": ms, "gpairs": n * n / (ms * 1e-3) / 1e9, "pair_kernel_ms": pair_ms / max(launches, 1)}
 
 
+def train_nearfield(shell, a, z_range, dev, n_samples=2048, steps=2000, seed=11):
+    """Near-field coupling network for one shell type: two-body training data
+    from the plain method on the GPU (centre distances 2R+2a .. 6R, heights in
+    z_range) and Adam on the GPU.  Returns (model, info)."""
+    import torch
+    from rigidmultiblobswall_gb300 import nearfield as nf
+    R = float(np.linalg.norm(shell[0]))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    feat, targ = nf.pair_training_data(shell, a, 1.0, n_samples, d_range=(2 * R + 2 * a, 6 * R), z_range=z_range,
+                                       seed=seed, device=dev)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    model = nf.NearfieldModel(body_radius=R, cutoff=6 * R, seed=2)
+    hist = model.train(feat, targ, steps=steps, batch=512, lr=2e-3)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return model, {"samples": 2 * n_samples, "data_ms": (t1 - t0) * 1e3, "train_ms": (t2 - t1) * 1e3,
+                   "steps": steps, "loss_first": float(hist[:10].mean()), "loss_last": float(hist[-50:].mean())}
+
+
 def solver_metrics(dev, reps=2):
     """Secondary: the 256-shell mobility solve (GMRES + block-diagonal PC to a
     1e-8 relative residual) in FP64 and mixed precision, and one Brownian
@@ -232,11 +253,33 @@ def solver_metrics(dev, reps=2):
             best = dt if best is None else min(best, dt)
         sols[mode] = sol[3 * sys2.n_blobs:].cpu().numpy()
         out["solve_shells42x256_%s" % mode] = {"ms": best * 1e3, "iterations": its, "relres_fp64": rr, "info": info}
-    u64, u32 = sols["fp64"], sols["mixed"]
-    out["solve_shells42x256_mixed"]["velocity_rel_err_vs_fp64"] = float(np.linalg.norm(u32 - u64) /
-                                                                        np.linalg.norm(u64))
+    # near-field augmented preconditioner: exact pairs < 3R, learned 3R..6R
+    from rigidmultiblobswall_gb300 import nearfield as nf
+    R2 = float(np.linalg.norm(s2.shell[0]))
+    model42, out["nearfield_training_shells42"] = train_nearfield(s2.shell, s2.a, (1.1 * R2, 5 * R2), dev)
+    for mode in ("fp64", "mixed"):
+        best = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sys2.build_pc()
+            pairs = model42.attach(sys2, exact_cutoff=3 * R2)
+            sol, info, its, rr = integrator.solve_mobility_problem(sys2, FT, tol=1e-8, mode=mode)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        nf.detach(sys2)
+        sols[mode + "_nf"] = sol[3 * sys2.n_blobs:].cpu().numpy()
+        out["solve_shells42x256_%s_nearfield" % mode] = {"ms": best * 1e3, "iterations": its, "relres_fp64": rr,
+                                                          "info": info, "pairs_exact_learned": list(pairs)}
+    u64 = sols["fp64"]
+    for key, sk in (("mixed", "solve_shells42x256_mixed"), ("fp64_nf", "solve_shells42x256_fp64_nearfield"),
+                    ("mixed_nf", "solve_shells42x256_mixed_nearfield")):
+        out[sk]["velocity_rel_err_vs_fp64"] = float(np.linalg.norm(sols[key] - u64) / np.linalg.norm(u64))
     out["solve_shells42x256_speedup_mixed"] = out["solve_shells42x256_fp64"]["ms"] / \
         out["solve_shells42x256_mixed"]["ms"]
+    out["solve_shells42x256_speedup_mixed_nearfield"] = out["solve_shells42x256_fp64"]["ms"] / \
+        out["solve_shells42x256_mixed_nearfield"]["ms"]
     # Brownian step, 1024 shells x 12 blobs
     s3 = S.shells_12_1024()
     sys3 = RigidSystem([12] * s3.n_bodies, s3.eta, s3.a, device=dev)
@@ -245,11 +288,15 @@ def solver_metrics(dev, reps=2):
     z = torch.randn(3 * s3.n_blobs, generator=torch.Generator(device=dev).manual_seed(3), dtype=torch.float64,
                     device=dev)
     vel = {}
-    for mode in ("fp64", "mixed"):
+    R3 = float(np.linalg.norm(s3.shell[0]))
+    model12, out["nearfield_training_shells12"] = train_nearfield(s3.shell, s3.a, (1.1 * R3, 5 * R3), dev)
+    for mode in ("fp64", "mixed", "mixed_nearfield"):
         best = None
         for _ in range(reps):
             st = integrator.BrownianStepper(sys3, s3.locations, s3.quaternions,
-                                            np.tile(s3.shell, (s3.n_bodies, 1)), kT=1.0, mode=mode)
+                                            np.tile(s3.shell, (s3.n_bodies, 1)), kT=1.0,
+                                            mode=mode.split("_")[0],
+                                            nearfield=(model12, 3 * R3) if "nearfield" in mode else None)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             res = st.step(1e-3, FT3, z=z)
@@ -260,15 +307,21 @@ def solver_metrics(dev, reps=2):
         out["bd_step_shells12x1024_%s" % mode] = {"ms": best * 1e3, "lanczos_iterations": res["lanczos_iterations"],
                                                   "gmres_iterations": res["gmres_iterations"],
                                                   "relres_fp64": res["relres"]}
-    out["bd_step_shells12x1024_mixed"]["velocity_rel_err_vs_fp64"] = float(
-        np.linalg.norm(vel["mixed"] - vel["fp64"]) / np.linalg.norm(vel["fp64"]))
+    for mode in ("mixed", "mixed_nearfield"):
+        out["bd_step_shells12x1024_" + mode]["velocity_rel_err_vs_fp64"] = float(
+            np.linalg.norm(vel[mode] - vel["fp64"]) / np.linalg.norm(vel["fp64"]))
+    out["bd_step_ms_learned_vs_blockdiag"] = {
+        "block_diag_fp64": out["bd_step_shells12x1024_fp64"]["ms"],
+        "block_diag_mixed": out["bd_step_shells12x1024_mixed"]["ms"],
+        "learned_mixed": out["bd_step_shells12x1024_mixed_nearfield"]["ms"]}
     return out
 
 
 def large_solve(args):
     """4096 42-blob shells at area fraction 0.3, force (0,0,-1) per body: block-diagonal preconditioned GMRES
     to a 1e-8 relative residual in each precision mode, on one GPU.  The plain FP64 solve is the baseline
-    the mixed-precision solve is compared against."""
+    the mixed-precision solve is compared against.  A mode "<mode>+nf" uses the near-field augmented
+    preconditioner (exact pairs < 3R, learned couplings 3R..6R from a network trained here first)."""
     import torch
     from rigidmultiblobswall_gb300 import build as B
     from rigidmultiblobswall_gb300 import integrator
@@ -292,21 +345,34 @@ def large_solve(args):
     torch.cuda.synchronize()
     out["pc_build_ms"] = (time.perf_counter() - t0) * 1e3
     sols = {}
+    model = None
+    from rigidmultiblobswall_gb300 import nearfield as nf
+    R5 = float(np.linalg.norm(s5.shell[0]))
     for mode in args.large_modes.split(","):
+        aug = mode.endswith("+nf")
+        base = mode[:-3] if aug else mode
+        if aug and model is None:
+            model, out["nearfield_training"] = train_nearfield(s5.shell, s5.a, (1.1 * R5, 3 * R5), dev)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sol, info, its, rr = integrator.solve_mobility_problem(sys5, FT, tol=1e-8, mode=mode)
+        pairs = model.attach(sys5, exact_cutoff=3 * R5) if aug else None
+        sol, info, its, rr = integrator.solve_mobility_problem(sys5, FT, tol=1e-8, mode=base)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
+        if aug:
+            nf.detach(sys5)
         sols[mode] = sol[3 * sys5.n_blobs:].cpu().numpy()
         out["solve_" + mode] = {"ms": dt * 1e3, "iterations": its, "relres": rr, "info": info}
+        if aug:
+            out["solve_" + mode]["pairs_exact_learned"] = list(pairs)
     out["clocks"] = clocks.stop()
     ref = sols.get("fp64", sols.get("df64"))
     for mode, u in sols.items():
         out["solve_" + mode]["velocity_rel_err_vs_fp64"] = float(np.linalg.norm(u - ref) / np.linalg.norm(ref))
     for base in ("fp64", "df64"):
-        if base in sols and "mixed" in sols:
-            out["speedup_mixed_vs_" + base] = out["solve_" + base]["ms"] / out["solve_mixed"]["ms"]
+        for fast in ("mixed", "mixed+nf"):
+            if base in sols and fast in sols:
+                out["speedup_%s_vs_%s" % (fast, base)] = out["solve_" + base]["ms"] / out["solve_" + fast]["ms"]
     print(json.dumps(out))
 
 

@@ -14,8 +14,8 @@
 //
 // Two kinds of near pairs:
 //  * exact pairs (centre distance below the exact cutoff): M_ij lambda_j
-//    evaluated blob by blob in FP64 (same pair formulas and periodic images
-//    as the all-pairs product);
+//    evaluated blob by blob in double-float arithmetic (same pair formulas
+//    and periodic images as the all-pairs product, ~1e-14 relative);
 //  * learned pairs (from the exact cutoff to the network's cutoff): M_ij is
 //    replaced by its projection on the 11 low-order modes of each body -
 //    3 translations, 3 rotations, 5 strains E_k d (d = blob - centre):
@@ -49,6 +49,7 @@
 #include <vector>
 
 #include "pair_math.cuh"
+#include "pair_math_df.cuh"
 #include "rigid.cuh"
 
 namespace rmw {
@@ -156,6 +157,37 @@ __device__ __forceinline__ void wall_uf_pair(double xi, double yi, double zie, d
                 pair_contrib<RMW_UF, double>((rx + bx * P.Lx) * inva, (ry + by * P.Ly) * inva,
                                              (rz + bz * P.Lz) * inva, Rz, hi, hj, vx, vy, vz, cx, cy, cz);
                 ux += cx; uy += cy; uz += cz;
+            }
+}
+
+// The same velocity in double-float arithmetic on the FP32 pipe (relative
+// error ~1e-14, like the df64 product mode): differences formed in FP64, the
+// pair math in df64, the result accumulated in FP64.
+__device__ __forceinline__ void wall_uf_pair_df(double xi, double yi, double zie, double xj, double yj, double zje,
+                                                double inva, const Images &P, double vx, double vy, double vz,
+                                                double &ux, double &uy, double &uz)
+{
+    const df hi = df_of_double(zie * inva), hj = df_of_double(zje * inva), Rz = df_of_double((zie + zje) * inva);
+    const df fx = df_of_double(vx), fy = df_of_double(vy), fz = df_of_double(vz);
+    double rx = xi - xj, ry = yi - yj, rz = zie - zje;
+    if (!(P.Lx > 0 || P.Ly > 0 || P.Lz > 0)) {
+        df cx, cy, cz;
+        pair_contrib_df<RMW_UF>(df_of_double(rx * inva), df_of_double(ry * inva), df_of_double(rz * inva), Rz, hi, hj,
+                                fx, fy, fz, cx, cy, cz);
+        ux += to_double(cx); uy += to_double(cy); uz += to_double(cz);
+        return;
+    }
+    if (P.Lx > 0) rx = project(rx, P.Lx);
+    if (P.Ly > 0) ry = project(ry, P.Ly);
+    if (P.Lz > 0) rz = project(rz, P.Lz);
+    const int px = P.Lx > 0, py = P.Ly > 0, pz = P.Lz > 0;
+    for (int bx = -px; bx <= px; ++bx)
+        for (int by = -py; by <= py; ++by)
+            for (int bz = -pz; bz <= pz; ++bz) {
+                df cx, cy, cz;
+                pair_contrib_df<RMW_UF>(df_of_double((rx + bx * P.Lx) * inva), df_of_double((ry + by * P.Ly) * inva),
+                                        df_of_double((rz + bz * P.Lz) * inva), Rz, hi, hj, fx, fy, fz, cx, cy, cz);
+                ux += to_double(cx); uy += to_double(cy); uz += to_double(cz);
             }
 }
 
@@ -708,20 +740,55 @@ __global__ void body_moments_kernel(const double *__restrict__ r, const double *
     }
 }
 
-// v_i = sum_{exact j} M_ij lambda_j + X_i sum_{learned j} G_ij mom_j on body i's
-// blob rows (one CTA per body; exact neighbours' blobs staged in shared memory)
-__global__ void nf_near_kernel(const double *__restrict__ r, const double *__restrict__ xb,
-                               const int *__restrict__ boff, const int *__restrict__ ex_off,
-                               const int *__restrict__ ex_idx, const int *__restrict__ ln_off,
-                               const int *__restrict__ ln_idx, const double *__restrict__ G,
-                               const double *__restrict__ mom, const double *__restrict__ lam, double a, double nf,
-                               Images P, double *__restrict__ v)
+// Exact near pairs, one CTA per neighbour entry q = (owner i, neighbour j):
+// part[q] (3 x blobs of i, unscaled) = sum over j's blobs of the pair
+// velocities.  Threads split as (target blob, source subset); the subsets are
+// added in a fixed order.
+__global__ void nf_pairs_kernel(const double *__restrict__ r, const int *__restrict__ boff,
+                                const int *__restrict__ ex_off, const int *__restrict__ ex_idx, int nb,
+                                const double *__restrict__ lam, double a, Images P, int part_stride,
+                                double *__restrict__ part)
 {
-    extern __shared__ double src[];  // 6 per source blob: x, y, clamped z, damped lambda
+    extern __shared__ double acc[];  // nsplit x ni x 3
+    const int q = blockIdx.x;
+    const int i = owner_of(ex_off, nb, q), j = ex_idx[q];
+    const int oi = boff[i], ni = boff[i + 1] - oi, oj = boff[j], nj = boff[j + 1] - oj;
+    const int nsplit = max(1, (int)blockDim.x / ni);
+    const double inva = 1.0 / a;
+    for (int w = threadIdx.x; w < ni * nsplit; w += blockDim.x) {
+        const int t = w % ni, sp = w / ni;
+        const int ti = oi + t;
+        const double zie = wall_clamp(r[3 * ti + 2], a);
+        double ux = 0.0, uy = 0.0, uz = 0.0;
+        for (int s = sp; s < nj; s += nsplit) {
+            const int sj = oj + s;
+            const double zj = r[3 * sj + 2], bj = wall_damp(zj, a);
+            wall_uf_pair_df(r[3 * ti], r[3 * ti + 1], zie, r[3 * sj], r[3 * sj + 1], wall_clamp(zj, a), inva, P,
+                            bj * lam[3 * sj], bj * lam[3 * sj + 1], bj * lam[3 * sj + 2], ux, uy, uz);
+        }
+        acc[3 * w] = ux;
+        acc[3 * w + 1] = uy;
+        acc[3 * w + 2] = uz;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 3 * ni; e += blockDim.x) {
+        double sum = 0.0;
+        for (int sp = 0; sp < nsplit; ++sp) sum += acc[3 * ni * sp + e];
+        part[(long long)q * part_stride + e] = sum;
+    }
+}
+
+// v_i = nf b_t sum_{exact entries of i} part + X_i sum_{learned j} G_ij mom_j on
+// body i's blob rows (one CTA per body; entries in CSR order)
+__global__ void nf_gather_kernel(const double *__restrict__ r, const double *__restrict__ xb,
+                                 const int *__restrict__ boff, const int *__restrict__ ex_off,
+                                 const double *__restrict__ part, int part_stride, const int *__restrict__ ln_off,
+                                 const int *__restrict__ ln_idx, const double *__restrict__ G,
+                                 const double *__restrict__ mom, double a, double nf, double *__restrict__ v)
+{
     __shared__ double cm[kModes];
     const int i = blockIdx.x;
     const int o = boff[i], nbl = boff[i + 1] - o;
-    const double inva = 1.0 / a;
     if (threadIdx.x < kModes) {
         double acc = 0.0;
         if (ln_off)
@@ -734,49 +801,28 @@ __global__ void nf_near_kernel(const double *__restrict__ r, const double *__res
     }
     __syncthreads();
     const int e0 = ex_off ? ex_off[i] : 0, e1 = ex_off ? ex_off[i + 1] : 0;
-    for (int t0 = 0; t0 < nbl; t0 += blockDim.x) {
-        const int p = t0 + threadIdx.x;
-        const bool valid = p < nbl;
-        const int ti = o + (valid ? p : 0);
-        const double xi = r[3 * ti], yi = r[3 * ti + 1], zi = r[3 * ti + 2];
-        const double zie = wall_clamp(zi, a);
+    for (int p = threadIdx.x; p < nbl; p += blockDim.x) {
+        const int ti = o + p;
         double ux = 0.0, uy = 0.0, uz = 0.0;
         for (int q = e0; q < e1; ++q) {
-            const int j = ex_idx[q];
-            const int oj = boff[j], nj = boff[j + 1] - oj;
-            __syncthreads();
-            for (int s = threadIdx.x; s < nj; s += blockDim.x) {
-                const int sj = oj + s;
-                const double zj = r[3 * sj + 2], bj = wall_damp(zj, a);
-                src[6 * s] = r[3 * sj];
-                src[6 * s + 1] = r[3 * sj + 1];
-                src[6 * s + 2] = wall_clamp(zj, a);
-                src[6 * s + 3] = bj * lam[3 * sj];
-                src[6 * s + 4] = bj * lam[3 * sj + 1];
-                src[6 * s + 5] = bj * lam[3 * sj + 2];
-            }
-            __syncthreads();
-            if (valid)
-                for (int s = 0; s < nj; ++s)
-                    wall_uf_pair(xi, yi, zie, src[6 * s], src[6 * s + 1], src[6 * s + 2], inva, P, src[6 * s + 3],
-                                 src[6 * s + 4], src[6 * s + 5], ux, uy, uz);
+            const double *pq = part + (long long)q * part_stride + 3 * p;
+            ux += pq[0]; uy += pq[1]; uz += pq[2];
         }
-        if (valid) {
-            const double sc = nf * wall_damp(zi, a);
-            double wx = sc * ux, wy = sc * uy, wz = sc * uz;
-            const double dx = xi - xb[3 * i], dy = yi - xb[3 * i + 1], dz = zi - xb[3 * i + 2];
+        const double zi = r[3 * ti + 2];
+        const double sc = nf * wall_damp(zi, a);
+        double wx = sc * ux, wy = sc * uy, wz = sc * uz;
+        const double dx = r[3 * ti] - xb[3 * i], dy = r[3 * ti + 1] - xb[3 * i + 1], dz = zi - xb[3 * i + 2];
 #pragma unroll
-            for (int k = 0; k < kModes; ++k) {
-                double mx, my, mz;
-                mode_velocity(k, dx, dy, dz, mx, my, mz);
-                wx += mx * cm[k];
-                wy += my * cm[k];
-                wz += mz * cm[k];
-            }
-            v[3LL * ti] = wx;
-            v[3LL * ti + 1] = wy;
-            v[3LL * ti + 2] = wz;
+        for (int k = 0; k < kModes; ++k) {
+            double mx, my, mz;
+            mode_velocity(k, dx, dy, dz, mx, my, mz);
+            wx += mx * cm[k];
+            wy += my * cm[k];
+            wz += mz * cm[k];
         }
+        v[3LL * ti] = wx;
+        v[3LL * ti + 1] = wy;
+        v[3LL * ti + 2] = wz;
     }
 }
 
@@ -792,15 +838,20 @@ int nearfield_apply_pc(RigidSystem &S, const double *x, double *y)
 {
     if (int rc = rigid_apply_pc_plain(S, x, y)) return rc;
     const double nf = 1.0 / (8.0 * kPi * S.eta * S.a);
+    const int stride = S.max_m;  // 3 x largest blob count per body
     if (S.nf_ln_pairs > 0)
         body_moments_kernel<<<(S.nb * 32 + 127) / 128, 128, 0, S.st>>>(S.r, S.xb, S.boff, S.nb, y, S.nf_mom);
-    const int nt = 64;
-    const size_t sm = sizeof(double) * 2 * (size_t)S.max_m;
-    if (sm > 48 * 1024)
-        RMW_CUDA(cudaFuncSetAttribute(nf_near_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    nf_near_kernel<<<S.nb, nt, sm, S.st>>>(S.r, S.xb, S.boff, S.nf_ex_pairs ? S.nf_ex_off : nullptr, S.nf_ex_idx,
-                                            S.nf_ln_pairs ? S.nf_ln_off : nullptr, S.nf_ln_idx, S.nf_G, S.nf_mom, y,
-                                            S.a, nf, images_of(S), S.nf_v);
+    if (S.nf_ex_pairs > 0) {
+        const int nt = 512;  // 42-blob bodies: 12 source subsets of 3-4 blobs per target
+        const size_t sm = sizeof(double) * 3 * (size_t)std::max(nt, S.max_m / 3);
+        if (sm > 48 * 1024)
+            RMW_CUDA(cudaFuncSetAttribute(nf_pairs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        nf_pairs_kernel<<<S.nf_ex_pairs, nt, sm, S.st>>>(S.r, S.boff, S.nf_ex_off, S.nf_ex_idx, S.nb, y, S.a,
+                                                          images_of(S), stride, S.nf_part);
+    }
+    nf_gather_kernel<<<S.nb, 64, 0, S.st>>>(S.r, S.xb, S.boff, S.nf_ex_pairs ? S.nf_ex_off : nullptr, S.nf_part,
+                                             stride, S.nf_ln_pairs ? S.nf_ln_off : nullptr, S.nf_ln_idx, S.nf_G,
+                                             S.nf_mom, S.a, nf, S.nf_v);
     RMW_CHECK_LAUNCH("near-field velocities");
     if (int rc = rigid_apply_pc_plain(S, S.nf_v, S.nf_z)) return rc;
     const long long n = S.sys_size();
@@ -1148,6 +1199,8 @@ int rmw_rigid_set_nearfield(void *sys, void *net, double exact_cutoff, int64_t *
         RMW_CUDA(cudaMemset(S.nf_v, 0, sizeof(double) * S.sys_size()));  // force rows stay zero
     }
     if (!S.nf_z) RMW_CUDA(cudaMalloc(&S.nf_z, sizeof(double) * S.sys_size()));
+    if (S.nf_part) { cudaFree(S.nf_part); S.nf_part = nullptr; }
+    if (S.nf_ex_pairs > 0) RMW_CUDA(cudaMalloc(&S.nf_part, sizeof(double) * (size_t)S.max_m * S.nf_ex_pairs));
     const int np = S.nf_ln_pairs;
     if (S.nf_G) { cudaFree(S.nf_G); S.nf_G = nullptr; }
     if (np > 0) {

@@ -51,6 +51,7 @@ struct RigidSystem {
     double *nf_mom = nullptr;  // 11 mode moments per body
     double *nf_v = nullptr;    // sys_size: near-field blob velocities, force rows zero
     double *nf_z = nullptr;    // sys_size: second block-diagonal solve
+    double *nf_part = nullptr;  // max_m per exact entry: unscaled pair velocities
 
     long long sys_size() const { return 3LL * n + 6LL * nb; }
 };

@@ -44,10 +44,15 @@ class BrownianStepper:
     the mobility problem with that slip noise, updates locations and
     quaternions and rejects the step (redraws the noise) if a blob crossed the
     wall, like the reference's check_positions.
+
+    nearfield: None, or (model, exact_cutoff) to augment every step's
+    block-diagonal preconditioner (nearfield.NearfieldModel or None for exact
+    near-field couplings only).  A step whose augmented solve does not reach
+    the tolerance is solved again with the plain preconditioner.
     """
 
     def __init__(self, sys_: RigidSystem, x, q, r_ref, kT=1.0, lanczos_tol=1e-3, gmres_tol=1e-8, mode="fp64",
-                 seed=0):
+                 seed=0, nearfield=None):
         import torch
         self.sys = sys_
         dev = sys_.device
@@ -63,6 +68,8 @@ class BrownianStepper:
         self.invalid = 0
         self.lanczos_iterations = 0
         self.gmres_iterations = 0
+        self.nearfield = nearfield
+        self.fallbacks = 0
 
     def r_vectors(self):
         return self.sys.blob_positions(self.x, self.q, self.r_ref)
@@ -79,8 +86,22 @@ class BrownianStepper:
             noise, it_l = s.lanczos(zz, factor=math.sqrt(2.0 * self.kT / dt), tol=self.lanczos_tol,
                                     mode=self.mode)
             self.lanczos_iterations += it_l
+            if self.nearfield is not None:
+                from . import nearfield as nf
+                model, cut = self.nearfield
+                if model is None:
+                    nf.attach_exact(s, cut)
+                else:
+                    model.attach(s, cut)
             sol, info, its, rr = solve_mobility_problem(s, force_torque, noise=noise, tol=self.gmres_tol,
                                                         mode=self.mode)
+            if self.nearfield is not None and (info != 0 or not rr <= self.gmres_tol):
+                from . import nearfield as nf
+                nf.detach(s)
+                self.fallbacks += 1
+                self.gmres_iterations += its
+                sol, info, its, rr = solve_mobility_problem(s, force_torque, noise=noise, tol=self.gmres_tol,
+                                                            mode=self.mode)
             self.gmres_iterations += its
             vel = sol[3 * s.n_blobs:]
             xn, qn = s.euler_update(self.x, self.q, vel, dt)

@@ -253,6 +253,21 @@ def solver_metrics(dev, reps=2):
             best = dt if best is None else min(best, dt)
         sols[mode] = sol[3 * sys2.n_blobs:].cpu().numpy()
         out["solve_shells42x256_%s" % mode] = {"ms": best * 1e3, "iterations": its, "relres_fp64": rr, "info": info}
+    # the same mixed solve with the per-iteration operator launched kernel by kernel instead of as a
+    # captured CUDA graph
+    from rigidmultiblobswall_gb300 import _native
+    _native.use_graphs(False)
+    best = None
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sys2.build_pc()
+        _, _, its_ng, _ = integrator.solve_mobility_problem(sys2, FT, tol=1e-8, mode="mixed")
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    _native.use_graphs(True)
+    out["solve_shells42x256_mixed_without_graphs"] = {"ms": best * 1e3, "iterations": its_ng}
     # near-field augmented preconditioner: exact pairs < 3R, learned 3R..6R
     from rigidmultiblobswall_gb300 import nearfield as nf
     R2 = float(np.linalg.norm(s2.shell[0]))
@@ -451,6 +466,9 @@ def main():
     peak64 = _native.fma_peak(True)
     peak32 = _native.fma_peak(False)
 
+    # ---- launch shape: the library's autotuner picks the pair grid's source split for this size
+    tune = mb.autotune("uf", n, HEAD_MODE, reps=5)
+
     # ---- warm-up
     for _ in range(args.warmup):
         mb.wall_product("uf", rt, ft, eta, a, mode=HEAD_MODE)
@@ -525,6 +543,7 @@ def main():
     products = {}
     for kind in (() if args.no_extras else ("uf", "ut", "wf", "wt")):
         for mode in ("fp64", "df64", "mixed"):
+            mb.autotune(kind, n, mode, reps=3)
             res = time_product(kind, mode, rt, ft, None, eta, a, max(3, args.steps // 4), flush, stream)
             peak = peak64 if mode in ("fp64", "df64") else peak32
             # algorithmic (reference) flops per second over the pipe peak of the mode's arithmetic
@@ -548,6 +567,8 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "df64 (f64-accurate)", "data": "synthetic (seeded)",
                 "config": {"workload": WORKLOAD, "mode": HEAD_MODE, "n_blobs": n, "pairs_per_step": n * n, "eta": eta, "a": a,
                            "l2": "512 MB buffer written between timed steps (inputs 0.5 MB < L2)",
+                           "launch_shape": {"source_chunks": tune["nchunks"], "chosen_by": "rmw_wall_autotune",
+                                            "tuned_ms": tune["ms"], "builtin_rule_ms": tune["default_ms"]},
                            "parallelism": "replicas" if ws > 1 else "single GPU"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
                 "gpu_launches": 3 * args.steps, "wall_s_timed_region": t_wall,

@@ -103,6 +103,26 @@ int rmw_wall_uf_multi(const double *r, const double *V, double *Y, int64_t n, in
 int rmw_wall_product_host(int kind, const double *r_host, const double *v_host, double *out_host,
                           int64_t n, double eta, double a, const double *L_host, int mode);
 
+/* Launch-shape autotuner (no reference counterpart): times every admissible
+ * source split of the all-pairs grid on n synthetic blobs and caches the
+ * fastest for (device, kind, mode, n's quarter-octave size bucket); the
+ * product entry points above and the rigid-body operators then use it.
+ * Synchronous.  best_ms / default_ms: mean time of the chosen split and of
+ * the built-in rule's. */
+int rmw_wall_autotune(int kind, int mode, int64_t n, int reps, void *stream, int *best_nchunks, double *best_ms,
+                      double *default_ms);
+int rmw_wall_autotune_lookup(int kind, int mode, int64_t n, int *nchunks, int *tuned);
+int rmw_wall_autotune_clear(void);
+
+/* CUDA graphs (no reference counterpart): the solvers' per-iteration
+ * operators (A P^-1 of rmw_rigid_solve / rmw_rigid_solve_batched, the
+ * preconditioned mobility of the Lanczos entry points) are captured once per
+ * call and replayed as one graph launch per application.  on = 0 runs them
+ * as plain launches.  Stats: graphs captured and replayed since the last
+ * reset. */
+int rmw_use_graphs(int on);
+int rmw_graph_stats(int64_t *captures_host, int64_t *replays_host, int reset);
+
 /* ---- rigid multiblob bodies ------------------------------------------
  * A handle (opaque, void*) holds one suspension of rigid bodies: body b owns
  * blobs [blob_offsets[b], blob_offsets[b+1]) (the reference's bodies list in

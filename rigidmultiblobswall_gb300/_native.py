@@ -50,6 +50,11 @@ SIGNATURES = {
     "rmw_wall_product_batched": (_i, [_vp, _i, _vp, _vp, _vp, _d, _d, _i, _vp]),
     "rmw_wall_uf_multi": (_i, [_vp, _vp, _vp, _i64, _i, _d, _d, _vp, _vp]),
     "rmw_wall_product_host": (_i, [_i, _vp, _vp, _vp, _i64, _d, _d, _vp, _i]),
+    "rmw_wall_autotune": (_i, [_i, _i, _i64, _i, _vp, _vp, _vp, _vp]),
+    "rmw_wall_autotune_lookup": (_i, [_i, _i, _i64, _vp, _vp]),
+    "rmw_wall_autotune_clear": (_i, []),
+    "rmw_use_graphs": (_i, [_i]),
+    "rmw_graph_stats": (_i, [_vp, _vp, _i]),
     "rmw_rigid_create": (_i, [ctypes.POINTER(ctypes.c_void_p), _i64, _vp, _d, _d, _vp, _vp]),
     "rmw_rigid_destroy": (_i, [_vp]),
     "rmw_rigid_sizes": (_i, [_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
@@ -150,3 +155,16 @@ def check(rc):
 
 def call(name, *args):
     return check(getattr(load(), name)(*args))
+
+
+def use_graphs(on=True):
+    """Replay the solvers' per-iteration operators as CUDA graphs (default on)."""
+    call("rmw_use_graphs", 1 if on else 0)
+
+
+def graph_stats(reset=False):
+    """(graphs captured, graph replays) since the last reset."""
+    c = ctypes.c_int64(0)
+    r = ctypes.c_int64(0)
+    call("rmw_graph_stats", ctypes.byref(c), ctypes.byref(r), 1 if reset else 0)
+    return c.value, r.value

@@ -27,6 +27,7 @@
 #include <cstring>
 #include <vector>
 
+#include "graph_op.cuh"
 #include "rigid.cuh"
 #include "wall_pair.cuh"
 
@@ -283,9 +284,11 @@ static int make_work(long long n, int kmax, cudaStream_t st, KrylovWork &K, int 
 static inline long long ldv_of(long long n) { return ((n + 31) / 32) * 32; }
 
 // ---------------------------------------------------------------------------
-// GMRES (right preconditioned).  op(x, y): y = A x ; pc(x, y): y = P^-1 x.
-template <typename Op, typename Pc>
-static int gmres_right(Op op, Pc pc, const double *b, double *x_out, long long n, double tol, int restart,
+// GMRES (right preconditioned).  op(x, y): y = A x ; pc(x, y): y = P^-1 x ;
+// pcop(x, y): y = A P^-1 x, the Arnoldi step's operator (given separately so
+// that the caller can fuse it and replay it as a CUDA graph).
+template <typename Op, typename Pc, typename PcOp>
+static int gmres_right(Op op, Pc pc, PcOp pcop, const double *b, double *x_out, long long n, double tol, int restart,
                        int maxiter, cudaStream_t st, int *iters_out, double *relres_out, std::vector<double> *hist)
 {
     restart = std::max(1, std::min(restart, 120));
@@ -323,8 +326,7 @@ static int gmres_right(Op op, Pc pc, const double *b, double *x_out, long long n
         for (int j = 0; j < restart; ++j) {
             double *Vj = K.V + (long long)j * ldv;
             double *Vn = K.V + (long long)(j + 1) * ldv;
-            if (int rc = pc(Vj, K.t1)) return rc;
-            if (int rc = op(K.t1, K.w)) return rc;
+            if (int rc = pcop(Vj, K.w)) return rc;
             // CGS2 against V_0..V_j
             if (int rc = O.dots(K.V, ldv, j + 1, K.w, 0)) return rc;
             if (int rc = O.update(K.V, ldv, j + 1, 0, K.w, -1)) return rc;
@@ -581,9 +583,26 @@ int rmw_rigid_solve(void *sys, const double *rhs, double *sol, double tol, int r
     }
     const long long n = S.sys_size();
     auto pc = [&](const double *x, double *y) { return rmw::rigid_apply_pc(S, x, y); };
+    // A P^-1 fused through a private buffer and replayed as one CUDA graph
+    double *pbuf = nullptr;
+    RMW_CUDA(cudaMallocAsync(&pbuf, sizeof(double) * n, S.st));
+    struct FreeP {
+        double *p;
+        cudaStream_t s;
+        ~FreeP() { cudaFreeAsync(p, s); }
+    } free_p{pbuf, S.st};
+    auto fused = [&](int m) {
+        return [&, m](const double *x, double *y) -> int {
+            if (int rc = rmw::rigid_apply_pc(S, x, pbuf)) return rc;
+            return rmw::rigid_apply(S, pbuf, y, m);
+        };
+    };
+    auto gop = rmw::make_graph_op(fused(mode == RMW_MODE_MIXED ? RMW_MODE_MIXED : mode), &S.st, n, n);
+    auto pcop = [&](const double *x, double *y) -> int { return gop(x, y); };
     if (mode == RMW_MODE_FP64 || mode == RMW_MODE_DF64) {
         auto op = [&](const double *x, double *y) { return rmw::rigid_apply(S, x, y, mode); };
-        return rmw::gmres_right(op, pc, rhs, sol, n, tol, restart, maxiter, S.st, iters_host, relres_host, nullptr);
+        return rmw::gmres_right(op, pc, pcop, rhs, sol, n, tol, restart, maxiter, S.st, iters_host, relres_host,
+                                nullptr);
     }
     // mixed: inner GMRES on the FP32-pair operator; the refinement residual
     // b - A x uses the FP64-accurate double-float operator (<= 1e-12 against FP64)
@@ -629,8 +648,8 @@ int rmw_rigid_solve(void *sys, const double *rhs, double *sol, double tol, int r
         const double itol = std::max(inner_tol, 0.5 * tol * bnorm / rnorm);
         int it = 0;
         double rr = 0.0;
-        int rc = rmw::gmres_right(op32, pc, r, d, n, itol, restart, std::max(1, maxiter - total), S.st, &it, &rr,
-                                  nullptr);
+        int rc = rmw::gmres_right(op32, pc, pcop, r, d, n, itol, restart, std::max(1, maxiter - total), S.st, &it,
+                                  &rr, nullptr);
         total += it;
         if (rc != RMW_OK && rc != RMW_ERR_NOT_CONVERGED) return rc;
         rmw::axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S.st>>>(d, x, n, 1.0, 1.0);
@@ -663,8 +682,10 @@ int rmw_rigid_lanczos(void *sys, const double *z, double *noise, double factor, 
     if (!S.stoch_ready) {
         if (int rc = rmw_rigid_build_pc(sys, 1)) return rc;
     }
-    auto op = [&](const double *x, double *y) { return rmw::rigid_mobility_pc(S, x, y, mode); };
+    auto op_direct = [&](const double *x, double *y) { return rmw::rigid_mobility_pc(S, x, y, mode); };
     const long long n = 3LL * S.n;
+    auto gop = rmw::make_graph_op(op_direct, &S.st, n, n);  // one graph per application
+    auto op = [&](const double *x, double *y) -> int { return gop(x, y); };
     double *tmp = nullptr;
     RMW_CUDA(cudaMallocAsync(&tmp, sizeof(double) * n, S.st));
     int rc = rmw::lanczos(op, z, tmp, n, factor, tol, max_iter, S.st, iters_host);
@@ -695,8 +716,15 @@ int rmw_gmres(int64_t n, rmw_operator_fn op, void *op_ctx, rmw_operator_fn pc, v
         int rc = pc(pc_ctx, xx, yy);
         return rc ? rmw::fail(rc, "preconditioner callback failed") : RMW_OK;
     };
+    double *tmp = nullptr;
+    RMW_CUDA(cudaMallocAsync(&tmp, sizeof(double) * n, st));
+    auto AP = [&](const double *xx, double *yy) -> int {
+        if (int rc = P(xx, tmp)) return rc;
+        return A(tmp, yy);
+    };
     std::vector<double> hist;
-    int rc = rmw::gmres_right(A, P, b, x, n, tol, restart, maxiter, st, iters_host, relres_host, &hist);
+    int rc = rmw::gmres_right(A, P, AP, b, x, n, tol, restart, maxiter, st, iters_host, relres_host, &hist);
+    cudaFreeAsync(tmp, st);
     if (history_host)
         for (int i = 0; i < (int)hist.size() && i < history_cap; ++i) history_host[i] = hist[i];
     return rc;

@@ -17,6 +17,7 @@
 #include <cstring>
 #include <vector>
 
+#include "graph_op.cuh"
 #include "rigid.cuh"
 #include "wall_pair.cuh"
 
@@ -293,8 +294,10 @@ struct SegOps {
 // Batched right-preconditioned restarted GMRES (zero initial guess).
 // op/pc act on instance-major vectors.  tol_abs[k] is suspension k's absolute
 // residual target; a suspension whose b segment is zero is solved by x = 0.
-template <typename Op, typename Pc>
-static int gmres_batched(Op op, Pc pc, const double *b, double *x_out, const std::vector<long long> &off,
+// pcop(x, y) = op(pc(x)): the Arnoldi step's operator, given separately so that
+// the caller can fuse and graph-capture it
+template <typename Op, typename Pc, typename PcOp>
+static int gmres_batched(Op op, Pc pc, PcOp pcop, const double *b, double *x_out, const std::vector<long long> &off,
                          const std::vector<double> &tol_rel, int restart, int maxiter, cudaStream_t st,
                          std::vector<int> &iters, std::vector<double> &relres, std::vector<int> &status)
 {
@@ -351,8 +354,7 @@ static int gmres_batched(Op op, Pc pc, const double *b, double *x_out, const std
         int jmax = 0;
         for (int j = 0; j < R; ++j) {
             double *Vj = V + (long long)j * ldv, *Vn = V + (long long)(j + 1) * ldv;
-            if (int rc = pc(Vj, t1)) return rc;
-            if (int rc = op(t1, w)) return rc;
+            if (int rc = pcop(Vj, w)) return rc;
             if (int rc = O.dots(V, ldv, j + 1, w, H1)) return rc;
             if (int rc = O.update(V, ldv, j + 1, H1, w, -1)) return rc;
             if (int rc = O.dots(V, ldv, j + 1, w, H2)) return rc;
@@ -623,8 +625,9 @@ int rmw_rigid_solve_batched(void *sys, const double *rhs, double *sol, double to
     RMW_CUDA(cudaMallocAsync(&buf, sizeof(double) * n * 6, st));
     double *gx = buf, *gy = buf + n, *bim = buf + 2 * n, *xim = buf + 3 * n, *rim = buf + 4 * n, *dim = buf + 5 * n;
     const unsigned pg = (unsigned)((n + 255) / 256);
-    auto to_global = [&](const double *xi, double *xg) { rmw::permute_kernel<<<pg, 256, 0, st>>>(xi, xg, S.perm, n, 1); };
-    auto to_im = [&](const double *xg, double *xi) { rmw::permute_kernel<<<pg, 256, 0, st>>>(xg, xi, S.perm, n, 0); };
+    // S.st, not st: inside a graph capture the handle's stream is redirected
+    auto to_global = [&](const double *xi, double *xg) { rmw::permute_kernel<<<pg, 256, 0, S.st>>>(xi, xg, S.perm, n, 1); };
+    auto to_im = [&](const double *xg, double *xi) { rmw::permute_kernel<<<pg, 256, 0, S.st>>>(xg, xi, S.perm, n, 0); };
     auto op_mode = [&](int m) {
         return [&, m](const double *xi, double *yi) -> int {
             to_global(xi, gx);
@@ -639,13 +642,27 @@ int rmw_rigid_solve_batched(void *sys, const double *rhs, double *sol, double to
         to_im(gy, yi);
         return RMW_OK;
     };
+    // the Arnoldi operator A P^-1 over all suspensions, fused (no permutation
+    // between the two) and replayed as one CUDA graph per application
+    auto pcop_mode = [&](int m) {
+        return [&, m](const double *xi, double *yi) -> int {
+            to_global(xi, gx);
+            if (int rc = rmw::rigid_apply_pc(S, gx, gy)) return rc;
+            if (int rc = rmw::rigid_apply(S, gy, gx, m)) return rc;
+            to_im(gx, yi);
+            return RMW_OK;
+        };
+    };
+    auto gop = rmw::make_graph_op(pcop_mode(mode == RMW_MODE_MIXED ? RMW_MODE_MIXED : mode), &S.st, n, n);
+    auto pcop = [&](const double *xi, double *yi) -> int { return gop(xi, yi); };
     to_im(rhs, bim);
     std::vector<int> it, stt, tot(nseg, 0);
     std::vector<double> rr;
     int rc = RMW_OK;
     if (mode != RMW_MODE_MIXED) {
         std::vector<double> tolv(nseg, tol);
-        rc = rmw::gmres_batched(op_mode(mode), pc, bim, xim, S.susp_off, tolv, restart, maxiter, st, it, rr, stt);
+        rc = rmw::gmres_batched(op_mode(mode), pc, pcop, bim, xim, S.susp_off, tolv, restart, maxiter, st, it, rr,
+                                stt);
         tot = it;
     } else {
         // per-suspension iterative refinement: inner GMRES on the FP32-pair
@@ -681,7 +698,7 @@ int rmw_rigid_solve_batched(void *sys, const double *rhs, double *sol, double to
                 if ((rc = O.scale(rim, rim, 2, false))) goto done;
                 std::vector<double> rri;
                 std::vector<int> si;
-                rc = rmw::gmres_batched(op_mode(RMW_MODE_MIXED), pc, rim, dim, S.susp_off, itol, restart,
+                rc = rmw::gmres_batched(op_mode(RMW_MODE_MIXED), pc, pcop, rim, dim, S.susp_off, itol, restart,
                                         std::max(1, maxiter), st, it, rri, si);
                 if (rc) goto done;
                 for (int k = 0; k < nseg; ++k) tot[k] += it[k];
@@ -732,7 +749,11 @@ int rmw_rigid_lanczos_batched(void *sys, const double *Z, double *noise, int nrh
     double *buf = nullptr;
     RMW_CUDA(cudaMallocAsync(&buf, sizeof(double) * 2 * nrhs * N3, S.st));
     double *tmp = buf, *raw = buf + nrhs * N3;
-    auto op = [&](const double *x, double *y) { return rmw::rigid_mobility_pc_multi(S, x, y, nrhs, mode, tmp); };
+    auto op_direct = [&](const double *x, double *y) {
+        return rmw::rigid_mobility_pc_multi(S, x, y, nrhs, mode, tmp);
+    };
+    auto gop = rmw::make_graph_op(op_direct, &S.st, nrhs * N3, nrhs * N3);  // one graph per application
+    auto op = [&](const double *x, double *y) -> int { return gop(x, y); };
     std::vector<int> it;
     int rc = rmw::lanczos_batched(op, Z, raw, off, factor, tol, max_iter, S.st, it);
     if (rc == RMW_OK) rc = rmw::rigid_P_inv_mult_multi(S, raw, noise, nrhs);

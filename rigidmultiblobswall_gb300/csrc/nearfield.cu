@@ -80,47 +80,49 @@ __host__ __device__ __forceinline__ void mode_velocity(int c, double dx, double 
     }
 }
 
-__host__ __device__ __forceinline__ void strain_basis(int k, double E[3][3])
+template <typename T>
+__host__ __device__ __forceinline__ void strain_basis(int k, T E[3][3])
 {
     for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 3; ++b) E[a][b] = 0.0;
+        for (int b = 0; b < 3; ++b) E[a][b] = T(0);
     switch (k) {
-    case 0: E[0][0] = kS2; E[1][1] = -kS2; break;
-    case 1: E[0][0] = -kS6; E[1][1] = -kS6; E[2][2] = 2.0 * kS6; break;
-    case 2: E[0][1] = E[1][0] = kS2; break;
-    case 3: E[0][2] = E[2][0] = kS2; break;
-    default: E[1][2] = E[2][1] = kS2; break;
+    case 0: E[0][0] = T(kS2); E[1][1] = -T(kS2); break;
+    case 1: E[0][0] = -T(kS6); E[1][1] = -T(kS6); E[2][2] = T(2.0 * kS6); break;
+    case 2: E[0][1] = E[1][0] = T(kS2); break;
+    case 3: E[0][2] = E[2][0] = T(kS2); break;
+    default: E[1][2] = E[2][1] = T(kS2); break;
     }
 }
 
 // Q = diag(Rz, Rz, R5) for the rotation about z with cos c, sin s
-__host__ __device__ inline void mode_rotation(double c, double s, double Q[kModes][kModes])
+template <typename T>
+__host__ __device__ inline void mode_rotation(T c, T s, T Q[kModes][kModes])
 {
     for (int a = 0; a < kModes; ++a)
-        for (int b = 0; b < kModes; ++b) Q[a][b] = 0.0;
+        for (int b = 0; b < kModes; ++b) Q[a][b] = T(0);
     for (int blk = 0; blk < 2; ++blk) {
         const int o = 3 * blk;
         Q[o][o] = c; Q[o][o + 1] = -s;
         Q[o + 1][o] = s; Q[o + 1][o + 1] = c;
-        Q[o + 2][o + 2] = 1.0;
+        Q[o + 2][o + 2] = T(1);
     }
-    const double Rz[3][3] = {{c, -s, 0.0}, {s, c, 0.0}, {0.0, 0.0, 1.0}};
+    const T Rz[3][3] = {{c, -s, T(0)}, {s, c, T(0)}, {T(0), T(0), T(1)}};
     for (int l = 0; l < 5; ++l) {
-        double El[3][3], T[3][3];
+        T El[3][3], R[3][3];
         strain_basis(l, El);
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) {
-                double acc = 0.0;
+                T acc = T(0);
                 for (int p = 0; p < 3; ++p)
                     for (int q = 0; q < 3; ++q) acc += Rz[a][p] * El[p][q] * Rz[b][q];
-                T[a][b] = acc;
+                R[a][b] = acc;
             }
         for (int k = 0; k < 5; ++k) {
-            double Ek[3][3];
+            T Ek[3][3];
             strain_basis(k, Ek);
-            double acc = 0.0;
+            T acc = T(0);
             for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b) acc += Ek[a][b] * T[a][b];
+                for (int b = 0; b < 3; ++b) acc += Ek[a][b] * R[a][b];
             Q[6 + k][6 + l] = acc;
         }
     }
@@ -604,35 +606,74 @@ static int net_backward(NearfieldNet &net, const __nv_bfloat16 *X, const float *
 }
 
 // ---------------------------------------------------------------------------
-// neighbour lists: ordered pairs (i, j != i) of one suspension with centre
-// distance (minimum image) in [lo, hi)
-__device__ __forceinline__ double centre_dist2(const double *__restrict__ xb, int i, int j, const Images &P)
-{
-    double dx = xb[3 * j] - xb[3 * i], dy = xb[3 * j + 1] - xb[3 * i + 1], dz = xb[3 * j + 2] - xb[3 * i + 2];
-    if (P.Lx > 0) dx = project(dx, P.Lx);
-    if (P.Ly > 0) dy = project(dy, P.Ly);
-    if (P.Lz > 0) dz = project(dz, P.Lz);
-    return dx * dx + dy * dy + dz * dz;
-}
+// neighbour lists: ordered pairs (i, j != i) of one suspension by centre
+// distance (minimum image)
 
-__global__ void nbr_band_kernel(const double *__restrict__ xb, int nb, double lo2, double hi2, Images P,
-                                const long long *__restrict__ susp, const int *__restrict__ off,
-                                int *__restrict__ out)
+// Both neighbour bands of body i in one pass over the bodies of its
+// suspension: exact pairs (d < cut_ex) and learned pairs (cut_ex <= d < cut_ln).
+// off == NULL: cnt[i], cnt[nb + i] = the two counts; else fill the lists
+// (ascending neighbour index).  Body centres are staged through shared memory
+// in tiles of blockDim bodies, covering the union of the block's ranges.  The
+// distance test runs in FP32 (a neighbour test needs no more; both passes use
+// the same arithmetic, so counts and lists agree).
+__global__ void nbr_bands_kernel(const double *__restrict__ xb, int nb, float cut_ex2, float cut_ln2, Images P,
+                                 const int2 *__restrict__ range, int *__restrict__ cnt,
+                                 const int *__restrict__ ex_off, int *__restrict__ ex_idx,
+                                 const int *__restrict__ ln_off, int *__restrict__ ln_idx)
 {
-    // off == NULL: out[i] = count; else out = neighbour indices at off[i]
+    extern __shared__ float tile[];  // 3 x blockDim
+    __shared__ int blo, bhi;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nb) return;
-    int c = off ? off[i] : 0;
-    for (int j = 0; j < nb; ++j) {
-        if (j == i) continue;
-        if (susp && susp[j] != susp[i]) continue;
-        const double d2 = centre_dist2(xb, i, j, P);
-        if (d2 >= lo2 && d2 < hi2) {
-            if (off) out[c] = j;
-            ++c;
-        }
+    const bool valid = i < nb;
+    const int2 rg = valid ? (range ? range[i] : make_int2(0, nb)) : make_int2(0, 0);
+    if (threadIdx.x == 0) {
+        blo = nb;
+        bhi = 0;
     }
-    if (!off) out[i] = c;
+    __syncthreads();
+    if (valid) {
+        atomicMin(&blo, rg.x);
+        atomicMax(&bhi, rg.y);
+    }
+    __syncthreads();
+    const float xi = valid ? (float)xb[3 * i] : 0.f, yi = valid ? (float)xb[3 * i + 1] : 0.f,
+                zi = valid ? (float)xb[3 * i + 2] : 0.f;
+    const float Lx = (float)P.Lx, Ly = (float)P.Ly, Lz = (float)P.Lz;
+    int ce = (valid && ex_off) ? ex_off[i] : 0, cl = (valid && ln_off) ? ln_off[i] : 0;
+    int ne = 0, nl = 0;
+    const int lo = blo, hi = bhi, nt = blockDim.x;
+    for (int t0 = lo; t0 < hi; t0 += nt) {
+        const int j = t0 + threadIdx.x;
+        if (j < hi) {
+            tile[threadIdx.x] = (float)xb[3 * j];
+            tile[nt + threadIdx.x] = (float)xb[3 * j + 1];
+            tile[2 * nt + threadIdx.x] = (float)xb[3 * j + 2];
+        }
+        __syncthreads();
+        const int cntk = min(nt, hi - t0);
+        if (valid)
+            for (int k = 0; k < cntk; ++k) {
+                const int jj = t0 + k;
+                if (jj == i || jj < rg.x || jj >= rg.y) continue;
+                float dx = tile[k] - xi, dy = tile[nt + k] - yi, dz = tile[2 * nt + k] - zi;
+                if (Lx > 0.f) dx = project(dx, Lx);
+                if (Ly > 0.f) dy = project(dy, Ly);
+                if (Lz > 0.f) dz = project(dz, Lz);
+                const float d2 = dx * dx + dy * dy + dz * dz;
+                if (d2 < cut_ex2) {
+                    if (ex_off) ex_idx[ce++] = jj;
+                    ++ne;
+                } else if (d2 < cut_ln2) {
+                    if (ln_off) ln_idx[cl++] = jj;
+                    ++nl;
+                }
+            }
+        __syncthreads();
+    }
+    if (valid && !ex_off && !ln_off) {
+        cnt[i] = ne;
+        cnt[nb + i] = nl;
+    }
 }
 
 __device__ __forceinline__ int owner_of(const int *__restrict__ off, int nb, int q)
@@ -677,34 +718,34 @@ __global__ void pair_features_kernel(const double *__restrict__ xb, const int *_
     }
 }
 
-// G_lab = Q G' Q^T, G' = network output * target scale (pair frame)
+// G_lab = Q G' Q^T, G' = network output * target scale (pair frame).  FP32:
+// the network's outputs carry BF16-level accuracy.  One thread per (entry,
+// row of G_lab).
 __global__ void pair_blocks_kernel(const float *__restrict__ Yf, const double *__restrict__ xb,
                                    const int *__restrict__ off, const int *__restrict__ idx, int nb, int npairs,
                                    Images P, const float *__restrict__ tscale, double *__restrict__ G)
 {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= npairs) return;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)npairs * kModes) return;
+    const int q = (int)(t / kModes), a = (int)(t % kModes);
     const int i = owner_of(off, nb, q), j = idx[q];
     double dx, dy;
     pair_horizontal(xb, i, j, P, dx, dy);
     const double rho = sqrt(dx * dx + dy * dy);
-    const double c = rho > 0 ? dx / rho : 1.0, s = rho > 0 ? dy / rho : 0.0;
-    double Q[kModes][kModes];
+    const float c = rho > 0 ? (float)(dx / rho) : 1.f, s = rho > 0 ? (float)(dy / rho) : 0.f;
+    float Q[kModes][kModes];
     mode_rotation(c, s, Q);
     const float *y = Yf + (long long)q * kOut;
-    for (int a = 0; a < kModes; ++a) {
-        double row[kModes];  // (Q G')[a][:]
-        for (int l = 0; l < kModes; ++l) {
-            double acc = 0.0;
-            for (int k = 0; k < kModes; ++k)
-                acc += Q[a][k] * (double)y[kModes * k + l] * (double)tscale[kModes * k + l];
-            row[l] = acc;
-        }
-        for (int b = 0; b < kModes; ++b) {
-            double acc = 0.0;
-            for (int l = 0; l < kModes; ++l) acc += row[l] * Q[b][l];
-            G[121LL * q + kModes * a + b] = acc;
-        }
+    float row[kModes];  // (Q G')[a][:]
+    for (int l = 0; l < kModes; ++l) {
+        float acc = 0.f;
+        for (int k = 0; k < kModes; ++k) acc += Q[a][k] * y[kModes * k + l] * tscale[kModes * k + l];
+        row[l] = acc;
+    }
+    for (int b = 0; b < kModes; ++b) {
+        float acc = 0.f;
+        for (int l = 0; l < kModes; ++l) acc += row[l] * Q[b][l];
+        G[121LL * q + kModes * a + b] = (double)acc;
     }
 }
 
@@ -860,28 +901,77 @@ int nearfield_apply_pc(RigidSystem &S, const double *x, double *y)
     return RMW_OK;
 }
 
-// neighbour list of one distance band into (off, idx) (device, reallocated)
-static int build_band(RigidSystem &S, double lo, double hi, const long long *susp, int **off_p, int **idx_p,
-                      int *count)
+// grow-only per-entry arrays of the two lists: capacities in entries, shared
+// by the index array and the per-entry data (pair velocities, mode couplings)
+static int grow_lists(RigidSystem &S, size_t need_ex, size_t need_ln)
+{
+    if (!S.nf_ex_idx || need_ex > S.nf_cap_ex) {
+        if (S.nf_ex_idx) RMW_CUDA(cudaFree(S.nf_ex_idx));
+        if (S.nf_part) RMW_CUDA(cudaFree(S.nf_part));
+        S.nf_ex_idx = nullptr;
+        S.nf_part = nullptr;
+        S.nf_cap_ex = 0;
+        const size_t want = std::max<size_t>(need_ex + need_ex / 4, 64);
+        RMW_CUDA(cudaMalloc(&S.nf_ex_idx, sizeof(int) * want));
+        RMW_CUDA(cudaMalloc(&S.nf_part, sizeof(double) * (size_t)S.max_m * want));
+        S.nf_cap_ex = want;
+    }
+    if (!S.nf_ln_idx || need_ln > S.nf_cap_ln) {
+        if (S.nf_ln_idx) RMW_CUDA(cudaFree(S.nf_ln_idx));
+        if (S.nf_G) RMW_CUDA(cudaFree(S.nf_G));
+        S.nf_ln_idx = nullptr;
+        S.nf_G = nullptr;
+        S.nf_cap_ln = 0;
+        const size_t want = std::max<size_t>(need_ln + need_ln / 4, 64);
+        RMW_CUDA(cudaMalloc(&S.nf_ln_idx, sizeof(int) * want));
+        RMW_CUDA(cudaMalloc(&S.nf_G, sizeof(double) * 121 * want));
+        S.nf_cap_ln = want;
+    }
+    return RMW_OK;
+}
+
+// exact (d < cut_ex) and learned (cut_ex <= d < cut_ln) neighbour lists of the
+// handle's bodies: one counting pass, one host round trip, one filling pass
+static int build_bands(RigidSystem &S, double cut_ex, double cut_ln)
 {
     cudaStream_t st = S.st;
-    if (*off_p) { cudaFree(*off_p); *off_p = nullptr; }
-    if (*idx_p) { cudaFree(*idx_p); *idx_p = nullptr; }
-    *count = 0;
-    RMW_CUDA(cudaMalloc(off_p, sizeof(int) * (S.nb + 1)));
+    const int nb = S.nb;
+    if (!S.nf_off) {
+        RMW_CUDA(cudaMalloc(&S.nf_off, sizeof(int) * 2 * (nb + 1)));
+        RMW_CUDA(cudaMalloc(&S.nf_cnt, sizeof(int) * 2 * nb));
+    }
+    S.nf_ex_off = S.nf_off;
+    S.nf_ln_off = S.nf_off + nb + 1;
+    const int2 *range = nullptr;
+    if (!S.susp_body_off.empty()) {
+        std::vector<int2> rg(nb);
+        for (size_t k = 0; k + 1 < S.susp_body_off.size(); ++k)
+            for (long long b = S.susp_body_off[k]; b < S.susp_body_off[k + 1]; ++b)
+                rg[b] = make_int2((int)S.susp_body_off[k], (int)S.susp_body_off[k + 1]);
+        if (!S.nf_range) RMW_CUDA(cudaMalloc(&S.nf_range, sizeof(int2) * nb));
+        RMW_CUDA(cudaMemcpyAsync(S.nf_range, rg.data(), sizeof(int2) * nb, cudaMemcpyHostToDevice, st));
+        range = S.nf_range;
+    }
     const Images P = images_of(S);
-    nbr_band_kernel<<<(S.nb + 127) / 128, 128, 0, st>>>(S.xb, S.nb, lo * lo, hi * hi, P, susp, nullptr, *off_p);
+    const float e2 = (float)(cut_ex * cut_ex), l2 = (float)(cut_ln * cut_ln);
+    const unsigned g = (unsigned)((nb + 63) / 64);
+    const size_t tsm = sizeof(float) * 3 * 64;
+    nbr_bands_kernel<<<g, 64, tsm, st>>>(S.xb, nb, e2, l2, P, range, S.nf_cnt, nullptr, nullptr, nullptr, nullptr);
     RMW_CHECK_LAUNCH("neighbour count");
-    std::vector<int> cnt(S.nb), off(S.nb + 1, 0);
-    RMW_CUDA(cudaMemcpyAsync(cnt.data(), *off_p, sizeof(int) * S.nb, cudaMemcpyDeviceToHost, st));
+    std::vector<int> cnt(2 * (size_t)nb), off(2 * ((size_t)nb + 1), 0);
+    RMW_CUDA(cudaMemcpyAsync(cnt.data(), S.nf_cnt, sizeof(int) * 2 * nb, cudaMemcpyDeviceToHost, st));
     RMW_CUDA(cudaStreamSynchronize(st));
-    for (int b = 0; b < S.nb; ++b) off[b + 1] = off[b] + cnt[b];
-    RMW_CUDA(cudaMemcpyAsync(*off_p, off.data(), sizeof(int) * (S.nb + 1), cudaMemcpyHostToDevice, st));
-    RMW_CUDA(cudaMalloc(idx_p, sizeof(int) * std::max(1, off[S.nb])));
-    nbr_band_kernel<<<(S.nb + 127) / 128, 128, 0, st>>>(S.xb, S.nb, lo * lo, hi * hi, P, susp, *off_p, *idx_p);
+    for (int band = 0; band < 2; ++band) {
+        int *o = off.data() + (size_t)band * (nb + 1);
+        for (int b = 0; b < nb; ++b) o[b + 1] = o[b] + cnt[(size_t)band * nb + b];
+    }
+    S.nf_ex_pairs = off[nb];
+    S.nf_ln_pairs = off[2 * (size_t)nb + 1];
+    RMW_CUDA(cudaMemcpyAsync(S.nf_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, st));
+    if (int rc = grow_lists(S, (size_t)S.nf_ex_pairs, (size_t)S.nf_ln_pairs)) return rc;
+    nbr_bands_kernel<<<g, 64, tsm, st>>>(S.xb, nb, e2, l2, P, range, nullptr, S.nf_ex_off, S.nf_ex_idx, S.nf_ln_off,
+                                          S.nf_ln_idx);
     RMW_CHECK_LAUNCH("neighbour fill");
-    RMW_CUDA(cudaStreamSynchronize(st));
-    *count = off[S.nb];
     return RMW_OK;
 }
 
@@ -1179,32 +1269,15 @@ int rmw_rigid_set_nearfield(void *sys, void *net, double exact_cutoff, int64_t *
     const double hi = N ? std::max(N->cutoff, lo) : lo;
     cudaStream_t st = S.st;
     S.nf_on = false;
-    long long *susp = nullptr;
-    if (!S.susp_body_off.empty()) {
-        std::vector<long long> sb(S.nb);
-        for (size_t k = 0; k + 1 < S.susp_body_off.size(); ++k)
-            for (long long b = S.susp_body_off[k]; b < S.susp_body_off[k + 1]; ++b) sb[b] = (long long)k;
-        RMW_CUDA(cudaMalloc(&susp, sizeof(long long) * S.nb));
-        RMW_CUDA(cudaMemcpy(susp, sb.data(), sizeof(long long) * S.nb, cudaMemcpyHostToDevice));
-    }
-    int rc = RMW_OK;
-    S.nf_ex_pairs = S.nf_ln_pairs = 0;
-    if (lo > 0) rc = rmw::build_band(S, 0.0, lo, susp, &S.nf_ex_off, &S.nf_ex_idx, &S.nf_ex_pairs);
-    if (rc == RMW_OK && N && hi > lo) rc = rmw::build_band(S, lo, hi, susp, &S.nf_ln_off, &S.nf_ln_idx, &S.nf_ln_pairs);
-    if (susp) cudaFree(susp);
-    if (rc) return rc;
+    if (int rc = rmw::build_bands(S, lo, hi)) return rc;
     if (!S.nf_mom) RMW_CUDA(cudaMalloc(&S.nf_mom, sizeof(double) * rmw::kModes * S.nb));
     if (!S.nf_v) {
         RMW_CUDA(cudaMalloc(&S.nf_v, sizeof(double) * S.sys_size()));
         RMW_CUDA(cudaMemset(S.nf_v, 0, sizeof(double) * S.sys_size()));  // force rows stay zero
     }
     if (!S.nf_z) RMW_CUDA(cudaMalloc(&S.nf_z, sizeof(double) * S.sys_size()));
-    if (S.nf_part) { cudaFree(S.nf_part); S.nf_part = nullptr; }
-    if (S.nf_ex_pairs > 0) RMW_CUDA(cudaMalloc(&S.nf_part, sizeof(double) * (size_t)S.max_m * S.nf_ex_pairs));
     const int np = S.nf_ln_pairs;
-    if (S.nf_G) { cudaFree(S.nf_G); S.nf_G = nullptr; }
     if (np > 0) {
-        RMW_CUDA(cudaMalloc(&S.nf_G, sizeof(double) * 121 * (size_t)np));
         const int Pp = ((np + 63) / 64) * 64;
         const rmw::Images P{S.L[0], S.L[1], S.L[2]};
         rmw::NetWork W;
@@ -1214,8 +1287,8 @@ int rmw_rigid_set_nearfield(void *sys, void *net, double exact_cutoff, int64_t *
         rmw::pair_features_kernel<<<(Pp + 127) / 128, 128, 0, st>>>(S.xb, S.nf_ln_off, S.nf_ln_idx, S.nb, np,
                                                                    1.0 / N->radius, P, N->dnorm, X, Pp);
         if (int rc2 = rmw::net_forward(*N, X, Pp, nullptr, W.A, W.Yf, st)) return rc2;
-        rmw::pair_blocks_kernel<<<(np + 127) / 128, 128, 0, st>>>(W.Yf, S.xb, S.nf_ln_off, S.nf_ln_idx, S.nb, np, P,
-                                                                 N->dnorm + 2 * rmw::kFeat, S.nf_G);
+        rmw::pair_blocks_kernel<<<(unsigned)(((long long)np * rmw::kModes + 127) / 128), 128, 0, st>>>(
+            W.Yf, S.xb, S.nf_ln_off, S.nf_ln_idx, S.nb, np, P, N->dnorm + 2 * rmw::kFeat, S.nf_G);
         RMW_CUDA(cudaFreeAsync(X, st));
     }
     RMW_CHECK_LAUNCH("near-field attach");

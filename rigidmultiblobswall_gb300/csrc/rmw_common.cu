@@ -1,5 +1,6 @@
 // Error reporting and per-device scratch of the rmw_gb300 library.
 #include <cstdio>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -37,6 +38,28 @@ std::mutex g_scratch_mu;
 std::map<std::tuple<int, void *, int>, ScratchBuf> g_scratch;
 }  // namespace
 
+// Buffers replaced while a captured CUDA graph may still reference them are
+// freed only when the last graph is gone.
+static int g_live_graphs = 0;
+static std::vector<std::pair<int, void *>> g_deferred;
+
+void graph_live(int delta)
+{
+    std::vector<std::pair<int, void *>> release;
+    {
+        std::lock_guard<std::mutex> lock(g_scratch_mu);
+        g_live_graphs += delta;
+        if (g_live_graphs == 0) release.swap(g_deferred);
+    }
+    int cur = 0;
+    cudaGetDevice(&cur);
+    for (auto &d : release) {
+        cudaSetDevice(d.first);
+        cudaFree(d.second);  // waits for the device: no replay still uses it
+    }
+    if (!release.empty()) cudaSetDevice(cur);
+}
+
 int scratch(ScratchSlot slot, size_t bytes, void **ptr, cudaStream_t st)
 {
     int dev = 0;
@@ -45,8 +68,12 @@ int scratch(ScratchSlot slot, size_t bytes, void **ptr, cudaStream_t st)
     ScratchBuf &b = g_scratch[std::make_tuple(dev, (void *)st, (int)slot)];
     if (b.bytes < bytes) {
         if (b.ptr) {
-            // cudaFree waits for all work on the device, so no kernel still uses the old buffer.
-            RMW_CUDA(cudaFree(b.ptr));
+            if (g_live_graphs > 0) {
+                g_deferred.push_back({dev, b.ptr});
+            } else {
+                // cudaFree waits for all work on the device, so no kernel still uses the old buffer.
+                RMW_CUDA(cudaFree(b.ptr));
+            }
             b.ptr = nullptr;
             b.bytes = 0;
         }
@@ -91,6 +118,10 @@ int trace_begin(TraceKernel k, cudaStream_t st, void **token)
 {
     *token = nullptr;
     if (!g_trace) return RMW_OK;
+    // work captured into a CUDA graph is not traced (its events would be
+    // recorded once at capture, not at every replay)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone) return RMW_OK;
     TraceRec *r = new TraceRec{(int)k, nullptr, nullptr};
     {
         std::lock_guard<std::mutex> lock(g_trace_mu);
@@ -113,9 +144,52 @@ int trace_end(void *token, cudaStream_t st)
     return RMW_OK;
 }
 
+static std::atomic<bool> g_graphs{true};
+static std::atomic<long long> g_graph_captures{0}, g_graph_replays{0};
+
+bool graphs_enabled() { return g_graphs.load(); }
+
+// one private non-blocking stream per (device, home stream), kept for the
+// process lifetime so that its scratch buffers are reused across solves
+static std::mutex g_capture_mu;
+static std::map<std::pair<int, void *>, cudaStream_t> g_capture_streams;
+
+int capture_stream(cudaStream_t home, cudaStream_t *out)
+{
+    int dev = 0;
+    RMW_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_capture_mu);
+    cudaStream_t &s = g_capture_streams[{dev, (void *)home}];
+    if (!s) RMW_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    *out = s;
+    return RMW_OK;
+}
+void graph_count(bool captured)
+{
+    if (captured) ++g_graph_captures;
+    else ++g_graph_replays;
+}
+
 }  // namespace rmw
 
 extern "C" {
+
+int rmw_use_graphs(int on)
+{
+    rmw::g_graphs = (on != 0);
+    return RMW_OK;
+}
+
+int rmw_graph_stats(int64_t *captures_host, int64_t *replays_host, int reset)
+{
+    if (captures_host) *captures_host = rmw::g_graph_captures.load();
+    if (replays_host) *replays_host = rmw::g_graph_replays.load();
+    if (reset) {
+        rmw::g_graph_captures = 0;
+        rmw::g_graph_replays = 0;
+    }
+    return RMW_OK;
+}
 
 int rmw_trace_enable(int on)
 {

@@ -648,7 +648,7 @@ int wall_product(int kind, const double *r, const double *v, double *out, int64_
     int rc = validate_product_args(kind, r, v, out, n, eta, a, mode);
     if (rc) return rc;
     if (n == 0) return RMW_OK;
-    const int nchunks = choose_chunks((int)n);
+    const int nchunks = wall_chunks(kind, mode, (int)n);
     void *ws = nullptr;
     rc = scratch(SCRATCH_PAIR, wall_scratch_bytes((int)n, mode, nchunks), &ws, st);
     if (rc) return rc;

@@ -33,8 +33,12 @@ int wall_uf_multi(const double *r, const double *V, long long ldv, double *Y, lo
 int wall_product_batched(const WallBatch &B, int kind, const double *r, const double *v, double *out, double eta,
                          double a, int mode, cudaStream_t st);
 
-// Source-chunk count the standard entry points use for n blobs.
+// Source-chunk count of the built-in rule for n blobs.
 int wall_default_chunks(int n);
+// Source-chunk count the standard entry points use: the autotuned split of
+// (kind, mode, n's size bucket) on the current device if there is one
+// (autotune.cu), else the built-in rule.
+int wall_chunks(int kind, int mode, int n);
 // Scratch bytes needed for n blobs in `mode` split into `nchunks` source chunks:
 // packed sources (64 B/blob FP64, 48 B/blob mixed, rounded up to 256 B) plus
 // nchunks * 3n doubles of partial sums.

@@ -138,6 +138,36 @@ def uf_multi(r_vectors, V, eta, a, batch=None):
     return Y
 
 
+def autotune(kind="uf", n=10752, mode="df64", reps=3, device=None):
+    """Time every admissible source split of the `kind` product in `mode` on n
+    synthetic blobs and cache the fastest for n's size bucket on the device;
+    later products of that size use it.  Returns {"nchunks", "ms",
+    "default_ms"}."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+    best = ctypes.c_int(0)
+    ms = ctypes.c_double(0.0)
+    dms = ctypes.c_double(0.0)
+    with torch.cuda.device(dev):
+        _native.call("rmw_wall_autotune", _native.KINDS[kind], _MODES[mode], int(n), int(reps),
+                     torch.cuda.current_stream(dev).cuda_stream, ctypes.byref(best), ctypes.byref(ms),
+                     ctypes.byref(dms))
+    return {"nchunks": best.value, "ms": ms.value, "default_ms": dms.value}
+
+
+def autotune_lookup(kind="uf", n=10752, mode="df64"):
+    """(source split the products use for this size, whether it was tuned)."""
+    c = ctypes.c_int(0)
+    t = ctypes.c_int(0)
+    _native.call("rmw_wall_autotune_lookup", _native.KINDS[kind], _MODES[mode], int(n), ctypes.byref(c),
+                 ctypes.byref(t))
+    return c.value, bool(t.value)
+
+
+def autotune_clear():
+    _native.call("rmw_wall_autotune_clear")
+
+
 # ---------------------------------------------------------------------------
 # wall regularisation helpers (mobility/mobility.py:52-84)
 def shift_heights(r_vectors, blob_radius, *args, **kwargs):

@@ -38,10 +38,10 @@ WORKLOAD = "wall-RPY M_UF.F, 256 shells x 42 blobs = 10,752 blobs (FP64-accurate
 # Issued thread instructions per pair of the df64 UF pair kernel (all pipes;
 # 85 % of them on the FMA pipe), from the ncu capture summarised in
 # profiles/wall_pair_df64_uf_shells42x256.md: smsp__inst_executed.sum * 32 / N^2
-# = 3,295,640,078 * 32 / 10752^2 = 912.2.  The FP32 pipe issues at most one
+# = 3,310,220,558 * 32 / 10752^2 = 916.3.  The FP32 pipe issues at most one
 # thread instruction per lane per clock, the rate the FMA-chain probe measures
 # (FLOP/s / 2), so achieved / peak is the fraction of issue capacity used.
-DF64_FMA_PIPE_INST_PER_PAIR = {"uf": 3295640078.0 * 32 / 10752 ** 2}
+DF64_FMA_PIPE_INST_PER_PAIR = {"uf": 3310220558.0 * 32 / 10752 ** 2}
 DF64_TRAFFIC_BYTES_PER_LAUNCH = 723456  # dram__bytes_read.sum + dram__bytes_write.sum, same capture
 
 

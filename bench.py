@@ -48,7 +48,7 @@ DF64_TRAFFIC_BYTES_PER_LAUNCH = 723456  # dram__bytes_read.sum + dram__bytes_wri
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=300)  # ~1 s timed: several clock samples
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -77,6 +77,22 @@ def dist_setup():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
     return ws, rank
+
+
+def reduce_step_ms(step_ms, ws, device=None):
+    """Max over ranks of the timed-region milliseconds (every rank calls it)."""
+    if ws == 1:
+        return float(step_ms)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(step_ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_gpairs(step_ms_max, ws, steps, n):
+    """Whole-job pairs per second: every replica evaluates steps x N^2 pairs."""
+    return ws * steps * n * n / (step_ms_max * 1e-3) / 1e9
 
 
 class ClockSampler:
@@ -502,12 +518,9 @@ def main():
     pair_ms_total, pair_launches = _native.trace_read(0, reset=True)
     _native.trace_enable(False)
     clk = clocks.stop()
-    t = torch.tensor([step_ms], dtype=torch.float64, device=dev)
-    if ws > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    step_ms = float(t.item())
+    step_ms = reduce_step_ms(step_ms, ws, dev)
     ms_per_step = step_ms / args.steps
-    value = ws * args.steps * n * n / (step_ms * 1e-3) / 1e9
+    value = aggregate_gpairs(step_ms, ws, args.steps, n)
 
     # ---- roofline of the dominant kernel (the df64 pair kernel; bound by the FP32/FMA pipe)
     pair_ms = pair_ms_total / max(pair_launches, 1)
@@ -544,7 +557,7 @@ def main():
     for kind in (() if args.no_extras else ("uf", "ut", "wf", "wt")):
         for mode in ("fp64", "df64", "mixed"):
             mb.autotune(kind, n, mode, reps=3)
-            res = time_product(kind, mode, rt, ft, None, eta, a, max(3, args.steps // 4), flush, stream)
+            res = time_product(kind, mode, rt, ft, None, eta, a, max(3, min(40, args.steps // 4)), flush, stream)
             peak = peak64 if mode in ("fp64", "df64") else peak32
             # algorithmic (reference) flops per second over the pipe peak of the mode's arithmetic
             # class; for df64 this is FP64-equivalent work over the FP64 peak (> 1 = faster than the

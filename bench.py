@@ -79,6 +79,35 @@ def dist_setup():
     return ws, rank
 
 
+def hbm_peak_gbs():
+    """Measured HBM copy bandwidth of the GB300s (MEASURED_PEAKS.json), else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def arnoldi_traffic(fn):
+    """Run fn() with tracing on; return (fn's result, the Arnoldi orthogonalisation's time, algorithmic
+    bytes and bandwidth against the HBM peak)."""
+    from rigidmultiblobswall_gb300 import _native
+    _native.trace_enable(True)
+    _native.trace_read(1, reset=True)
+    _native.trace_bytes(1, reset=True)
+    res = fn()
+    ms, launches = _native.trace_read(1, reset=True)
+    nbytes = _native.trace_bytes(1, reset=True)
+    _native.trace_read(0, reset=True)
+    _native.trace_read(2, reset=True)
+    _native.trace_enable(False)
+    peak, src = hbm_peak_gbs()
+    gbs = nbytes / (ms * 1e-3) / 1e9 if ms > 0 else None
+    return res, {"steps": launches, "ms": ms, "gbytes": nbytes / 1e9, "gbs": gbs,
+                 "frac_of_hbm": (gbs / peak) if gbs else None, "hbm_peak_gbs": peak, "peak_source": src,
+                 "bytes_per_step": "(4j + 12) n doubles: CGS2 = 2 x (dots + update) + scale"}
+
+
 def reduce_step_ms(step_ms, ws, device=None):
     """Max over ranks of the timed-region milliseconds (every rank calls it)."""
     if ws == 1:
@@ -303,6 +332,10 @@ def solver_metrics(dev, reps=2):
         sols[mode + "_nf"] = sol[3 * sys2.n_blobs:].cpu().numpy()
         out["solve_shells42x256_%s_nearfield" % mode] = {"ms": best * 1e3, "iterations": its, "relres_fp64": rr,
                                                           "info": info, "pairs_exact_learned": list(pairs)}
+    # bandwidth of the Arnoldi vector work (33,792-long vectors: the basis stays in L2)
+    sys2.build_pc()
+    _, out["solve_shells42x256_mixed_arnoldi"] = arnoldi_traffic(
+        lambda: integrator.solve_mobility_problem(sys2, FT, tol=1e-8, mode="mixed"))
     u64 = sols["fp64"]
     for key, sk in (("mixed", "solve_shells42x256_mixed"), ("fp64_nf", "solve_shells42x256_fp64_nearfield"),
                     ("mixed_nf", "solve_shells42x256_mixed_nearfield")):
@@ -387,19 +420,21 @@ def large_solve(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         pairs = model.attach(sys5, exact_cutoff=3 * R5) if aug else None
-        sol, info, its, rr = integrator.solve_mobility_problem(sys5, FT, tol=1e-8, mode=base)
+        (sol, info, its, rr), arn = arnoldi_traffic(
+            lambda: integrator.solve_mobility_problem(sys5, FT, tol=1e-8, mode=base))
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         if aug:
             nf.detach(sys5)
         sols[mode] = sol[3 * sys5.n_blobs:].cpu().numpy()
-        out["solve_" + mode] = {"ms": dt * 1e3, "iterations": its, "relres": rr, "info": info}
+        out["solve_" + mode] = {"ms": dt * 1e3, "iterations": its, "relres": rr, "info": info, "arnoldi": arn}
         if aug:
             out["solve_" + mode]["pairs_exact_learned"] = list(pairs)
     out["clocks"] = clocks.stop()
     ref = sols.get("fp64", sols.get("df64"))
     for mode, u in sols.items():
-        out["solve_" + mode]["velocity_rel_err_vs_fp64"] = float(np.linalg.norm(u - ref) / np.linalg.norm(ref))
+        if ref is not None:
+            out["solve_" + mode]["velocity_rel_err_vs_fp64"] = float(np.linalg.norm(u - ref) / np.linalg.norm(ref))
     for base in ("fp64", "df64"):
         for fast in ("mixed", "mixed+nf"):
             if base in sols and fast in sols:
@@ -451,6 +486,8 @@ def batched_metrics(dev, nrhs=16):
     out["solve_iterations_min_max"] = [int(its.min()), int(its.max())]
     out["solve_relres_max"] = float(rr.max())
     out["all_converged"] = bool((stt == 0).all())
+    # the same solve again, traced: bandwidth of the segmented Arnoldi work (2.1 M-long vectors, basis > L2)
+    _, out["solve_arnoldi"] = arnoldi_traffic(lambda: sysb.solve_batched(rhs, tol=1e-8, mode="mixed"))
     return out
 
 

@@ -313,6 +313,9 @@ int rmw_fma_peak(int fp64, double *flops_per_s_host, void *stream);
  * optionally clears the records.  rmw_trace_read synchronises the events. */
 int rmw_trace_enable(int on);
 int rmw_trace_read(int kind, double *total_ms_host, int64_t *launches_host, int reset);
+/* Algorithmic bytes the traced work of one class moved while tracing was on
+ * (kind 1: the GMRES Arnoldi orthogonalisation, (4j + 12) n doubles at step j). */
+int rmw_trace_bytes(int kind, double *bytes_host, int reset);
 
 #ifdef __cplusplus
 }

@@ -109,3 +109,35 @@ def uf_symmetric_fast(r_vectors, force, eta, a, threads=0):
 
 def max_threads():
     return _lib(fast=True).oracle_max_threads()
+
+
+def blake_point_mobility(r_vectors, eta):
+    """Off-diagonal 3x3 blocks of the point-particle (Blake 1971) image system
+    above a no-slip wall at z = 0: S(r) - S(R) + 2h SD(R) - h^2 PD(R), with R
+    the separation from the image of the source at height h, S the Stokeslet
+    (I/|r| + r r^T/|r|^3)/(8 pi eta), SD the Stokes doublet and PD the
+    potential dipole with the sign flips of the image system's wall-parallel
+    forcing (helpers of mobility/mobility.py:152-171).  Diagonal blocks zero.
+    The finite-size wall mobility tends to it as a -> 0."""
+    r = np.asarray(r_vectors, dtype=np.float64).reshape(-1, 3)
+    n = r.shape[0]
+    e3 = np.array([0.0, 0.0, 1.0])
+    M = np.zeros((3 * n, 3 * n))
+    for j in range(n):
+        for k in range(n):
+            if j == k:
+                continue
+            d = r[j] - r[k]
+            rn = np.linalg.norm(d)
+            h = r[k, 2]
+            R = r[j] - (r[k] - 2.0 * h * e3)
+            Rn = np.linalg.norm(R)
+            S = (np.eye(3) / rn + np.outer(d, d) / rn ** 3 - (np.eye(3) / Rn + np.outer(R, R) / Rn ** 3)) / (8 * np.pi)
+            SD = np.outer(R, e3) + R[2] * np.eye(3) - np.outer(e3, R) - 3.0 * R[2] * np.outer(R, R) / Rn ** 2
+            SD[:, 0:2] *= -1.0
+            SD /= 8 * np.pi * Rn ** 3
+            PD = np.eye(3) - 3.0 * np.outer(R, R) / Rn ** 2
+            PD[:, 0:2] *= -1.0
+            PD /= 4 * np.pi * Rn ** 3
+            M[3 * j:3 * j + 3, 3 * k:3 * k + 3] = (S + 2.0 * h * SD - h * h * PD) / eta
+    return M

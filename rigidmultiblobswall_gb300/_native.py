@@ -54,6 +54,7 @@ SIGNATURES = {
     "rmw_wall_autotune_lookup": (_i, [_i, _i, _i64, _vp, _vp]),
     "rmw_wall_autotune_clear": (_i, []),
     "rmw_use_graphs": (_i, [_i]),
+    "rmw_trace_bytes": (_i, [_i, _vp, _i]),
     "rmw_graph_stats": (_i, [_vp, _vp, _i]),
     "rmw_rigid_create": (_i, [ctypes.POINTER(ctypes.c_void_p), _i64, _vp, _d, _d, _vp, _vp]),
     "rmw_rigid_destroy": (_i, [_vp]),
@@ -115,6 +116,13 @@ def trace_read(kind=0, reset=True):
     cnt = ctypes.c_int64(0)
     call("rmw_trace_read", kind, ctypes.byref(ms), ctypes.byref(cnt), 1 if reset else 0)
     return ms.value, cnt.value
+
+
+def trace_bytes(kind=1, reset=True):
+    """Algorithmic bytes moved by traced work of one class."""
+    b = ctypes.c_double(0.0)
+    call("rmw_trace_bytes", kind, ctypes.byref(b), 1 if reset else 0)
+    return b.value
 
 
 OPERATOR_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p)

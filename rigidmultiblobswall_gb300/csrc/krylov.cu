@@ -327,12 +327,16 @@ static int gmres_right(Op op, Pc pc, PcOp pcop, const double *b, double *x_out, 
             double *Vj = K.V + (long long)j * ldv;
             double *Vn = K.V + (long long)(j + 1) * ldv;
             if (int rc = pcop(Vj, K.w)) return rc;
-            // CGS2 against V_0..V_j
+            // CGS2 against V_0..V_j; algorithmic bytes: 2 x (dots (j+2) n + update (j+3) n) + scale 2 n
+            void *tok = nullptr;
+            if (int rc = trace_begin(TRACE_KRYLOV, st, &tok)) return rc;
             if (int rc = O.dots(K.V, ldv, j + 1, K.w, 0)) return rc;
             if (int rc = O.update(K.V, ldv, j + 1, 0, K.w, -1)) return rc;
             if (int rc = O.dots(K.V, ldv, j + 1, K.w, restart + 2)) return rc;
             if (int rc = O.update(K.V, ldv, j + 1, restart + 2, K.w, SC + 1)) return rc;
             if (int rc = O.scale(K.w, Vn, 1.0, O.dsc + SC + 1)) return rc;
+            if (int rc = trace_end(tok, st)) return rc;
+            if (tok) trace_bytes(TRACE_KRYLOV, 8.0 * (4.0 * j + 12.0) * (double)n);
             if (int rc = O.fetch(0, SC + 2)) return rc;
             double *h = &H[(size_t)j * (restart + 1)];
             for (int q = 0; q <= j; ++q) h[q] = O.hpin[q] + O.hpin[restart + 2 + q];

@@ -355,11 +355,16 @@ static int gmres_batched(Op op, Pc pc, PcOp pcop, const double *b, double *x_out
         for (int j = 0; j < R; ++j) {
             double *Vj = V + (long long)j * ldv, *Vn = V + (long long)(j + 1) * ldv;
             if (int rc = pcop(Vj, w)) return rc;
+            // CGS2 per segment; algorithmic bytes as in the single-system GMRES
+            void *tok = nullptr;
+            if (int rc = trace_begin(TRACE_KRYLOV, st, &tok)) return rc;
             if (int rc = O.dots(V, ldv, j + 1, w, H1)) return rc;
             if (int rc = O.update(V, ldv, j + 1, H1, w, -1)) return rc;
             if (int rc = O.dots(V, ldv, j + 1, w, H2)) return rc;
             if (int rc = O.update(V, ldv, j + 1, H2, w, NW)) return rc;
             if (int rc = O.scale(w, Vn, NW, true)) return rc;
+            if (int rc = trace_end(tok, st)) return rc;
+            if (tok) trace_bytes(TRACE_KRYLOV, 8.0 * (4.0 * j + 12.0) * (double)n);
             if (int rc = O.fetch()) return rc;
             jmax = j + 1;
             int still = 0;

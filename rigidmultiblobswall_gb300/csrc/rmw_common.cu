@@ -133,6 +133,14 @@ int trace_begin(TraceKernel k, cudaStream_t st, void **token)
     return RMW_OK;
 }
 
+static double g_trace_byte_count[TRACE_KINDS] = {0.0, 0.0, 0.0};
+
+void trace_bytes(TraceKernel k, double bytes)
+{
+    std::lock_guard<std::mutex> lock(g_trace_mu);
+    if (g_trace) g_trace_byte_count[k] += bytes;
+}
+
 int trace_end(void *token, cudaStream_t st)
 {
     if (!token) return RMW_OK;
@@ -224,6 +232,15 @@ int rmw_trace_read(int kind, double *total_ms_host, int64_t *launches_host, int 
     return RMW_OK;
 }
 
+
+int rmw_trace_bytes(int kind, double *bytes_host, int reset)
+{
+    if (kind < 0 || kind >= rmw::TRACE_KINDS || !bytes_host) return rmw::fail(RMW_ERR_ARG, "bad trace kind or pointer");
+    std::lock_guard<std::mutex> lock(rmw::g_trace_mu);
+    *bytes_host = rmw::g_trace_byte_count[kind];
+    if (reset) rmw::g_trace_byte_count[kind] = 0.0;
+    return RMW_OK;
+}
 
 const char *rmw_last_error(void) { return rmw::g_last_error.c_str(); }
 

@@ -42,6 +42,8 @@ enum TraceKernel { TRACE_PAIR = 0, TRACE_KRYLOV = 1, TRACE_PC = 2, TRACE_KINDS =
 bool trace_on();
 int trace_begin(TraceKernel k, cudaStream_t st, void **token);
 int trace_end(void *token, cudaStream_t st);
+// algorithmic bytes moved by traced work of one class (counted while tracing is on)
+void trace_bytes(TraceKernel k, double bytes);
 
 constexpr double kPi = 3.14159265358979323846;
 

@@ -80,3 +80,14 @@ def test_workloads_are_seeded_and_non_overlapping():
     R = np.linalg.norm(s1.shell[0])
     assert d.min() > 2 * R + 2 * s1.a
     assert s1.n_blobs == 10752
+
+
+def test_oracle_point_particle_limit_is_blake():
+    """Property test of mobility/mobility_test.py:70-82 (finite-size limit),
+    against the full Blake image system: off-diagonal blocks agree to O(a^2)."""
+    rng = np.random.default_rng(0)
+    r = rng.normal(5.0, 1.0, (4, 3))
+    M = wall.dense_mobility(r, 1.0, 1e-4)
+    B = wall.blake_point_mobility(r, 1.0)
+    off = ~np.kron(np.eye(4, dtype=bool), np.ones((3, 3), dtype=bool))
+    assert np.abs(M - B)[off].max() <= 1e-7 * np.abs(B[off]).max()

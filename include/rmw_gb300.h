@@ -104,7 +104,8 @@ int rmw_wall_product_host(int kind, const double *r_host, const double *v_host, 
                           int64_t n, double eta, double a, const double *L_host, int mode);
 
 /* Launch-shape autotuner (no reference counterpart): times every admissible
- * source split of the all-pairs grid on n synthetic blobs and caches the
+ * source split of the all-pairs grid (and, for the df64 UF product, the
+ * symmetric kernel, reported as nchunks = -1) on n synthetic blobs and caches the
  * fastest for (device, kind, mode, n's quarter-octave size bucket); the
  * product entry points above and the rigid-body operators then use it.
  * Synchronous.  best_ms / default_ms: mean time of the chosen split and of
@@ -112,6 +113,12 @@ int rmw_wall_product_host(int kind, const double *r_host, const double *v_host, 
 int rmw_wall_autotune(int kind, int mode, int64_t n, int reps, void *stream, int *best_nchunks, double *best_ms,
                       double *default_ms);
 int rmw_wall_autotune_lookup(int kind, int mode, int64_t n, int *nchunks, int *tuned);
+/* Pin a choice instead of measuring: nchunks in [1, 64], or -1 for the
+ * symmetric df64 UF kernel (each unordered pair evaluated once and applied
+ * both ways; non-periodic, n >= 256, up to about 185,000 blobs: its
+ * deterministic partial sums take ceil(n/128) x 3n doubles, 5.5 GB at
+ * 172,032 blobs). */
+int rmw_wall_autotune_set(int kind, int mode, int64_t n, int nchunks);
 int rmw_wall_autotune_clear(void);
 
 /* CUDA graphs (no reference counterpart): the solvers' per-iteration

@@ -2,7 +2,9 @@
 //
 // The tunable shape is the source split of the 2-D grid (target tiles x
 // source chunks): more chunks fill the 152 SMs for small N, fewer chunks cut
-// the partial-sum traffic of the finalize pass for large N.  rmw_wall_autotune
+// the partial-sum traffic of the finalize pass for large N.  For the df64
+// UF product the symmetric kernel (each unordered pair once) is a further
+// candidate.  rmw_wall_autotune
 // times every admissible split on synthetic blobs of the requested size with
 // CUDA events and caches the fastest per (device, kind, precision mode, size
 // bucket); the standard product entry points and the rigid-body operators use
@@ -76,7 +78,10 @@ int wall_chunks(int kind, int mode, int n)
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         auto it = g_tuned.find(key_of(kind, mode, n));
-        if (it != g_tuned.end()) return std::max(1, std::min(it->second, max_chunks(n)));
+        if (it != g_tuned.end()) {
+            if (it->second == kSymChunks) return kSymChunks;
+            return std::max(1, std::min(it->second, max_chunks(n)));
+        }
     }
     return wall_default_chunks(n);
 }
@@ -102,7 +107,9 @@ int rmw_wall_autotune(int kind, int mode, int64_t n, int reps, void *stream, int
         if (c <= rmw::max_chunks(N)) cand.push_back(c);
     const int def = rmw::wall_default_chunks(N);
     if (std::find(cand.begin(), cand.end(), def) == cand.end()) cand.push_back(def);
-    const int cmax = *std::max_element(cand.begin(), cand.end());
+    const bool try_sym = rmw::wall_sym_applicable(kind, mode, N, nullptr);
+    if (try_sym) cand.push_back(rmw::kSymChunks);
+    const int cmax = std::max(*std::max_element(cand.begin(), cand.end()), try_sym ? rmw::wall_sym_slots(N) : 1);
     const size_t vec = sizeof(double) * 3 * (size_t)N;
     const size_t ws_bytes = rmw::wall_scratch_bytes(N, mode, cmax);
     char *buf = nullptr;
@@ -115,12 +122,15 @@ int rmw_wall_autotune(int kind, int mode, int64_t n, int reps, void *stream, int
     RMW_CUDA(cudaEventCreate(&e1));
     int rc = RMW_OK, best = def;
     float tbest = 0.f, tdef = 0.f;
+    auto run = [&](int c) {
+        if (c == rmw::kSymChunks) return rmw::wall_product_sym_with_scratch(r, v, out, N, 1.0, 1.0, st, ws);
+        return rmw::wall_product_with_scratch(kind, r, v, out, N, 1.0, 1.0, nullptr, mode, st, ws, c);
+    };
     for (int c : cand) {
-        rc = rmw::wall_product_with_scratch(kind, r, v, out, N, 1.0, 1.0, nullptr, mode, st, ws, c);
+        rc = run(c);
         if (rc) break;
         cudaEventRecord(e0, st);
-        for (int k = 0; k < reps && rc == RMW_OK; ++k)
-            rc = rmw::wall_product_with_scratch(kind, r, v, out, N, 1.0, 1.0, nullptr, mode, st, ws, c);
+        for (int k = 0; k < reps && rc == RMW_OK; ++k) rc = run(c);
         cudaEventRecord(e1, st);
         if (rc) break;
         cudaError_t e = cudaEventSynchronize(e1);
@@ -153,7 +163,8 @@ int rmw_wall_autotune(int kind, int mode, int64_t n, int reps, void *stream, int
 }
 
 // Source split the product entry points use for (kind, mode, n) on the
-// current device; *tuned = 1 when it comes from rmw_wall_autotune.
+// current device (-1: the symmetric kernel); *tuned = 1 when it comes from
+// rmw_wall_autotune.
 int rmw_wall_autotune_lookup(int kind, int mode, int64_t n, int *nchunks, int *tuned)
 {
     if (n < 1 || n > (int64_t(1) << 28)) return rmw::fail(RMW_ERR_ARG, "number of blobs out of range");
@@ -165,6 +176,25 @@ int rmw_wall_autotune_lookup(int kind, int mode, int64_t n, int *nchunks, int *t
     }
     if (nchunks) *nchunks = c;
     if (tuned) *tuned = hit ? 1 : 0;
+    return RMW_OK;
+}
+
+// Pin the launch choice of (kind, mode, n's size bucket) on the current
+// device: a source split in [1, 64], or -1 for the symmetric kernel (only
+// where it applies).
+int rmw_wall_autotune_set(int kind, int mode, int64_t n, int nchunks)
+{
+    if (int rc = rmw::validate_product_args(kind, (void *)1, (void *)1, (void *)1, n, 1.0, 1.0, mode)) return rc;
+    if (n < 1) return rmw::fail(RMW_ERR_ARG, "number of blobs must be positive");
+    if (nchunks == rmw::kSymChunks) {
+        if (!rmw::wall_sym_applicable(kind, mode, (int)n, nullptr))
+            return rmw::fail(RMW_ERR_ARG, "the symmetric kernel covers the df64 UF product of 256 or more blobs "
+                                          "within its partial-sum budget");
+    } else if (nchunks < 1 || nchunks > 64) {
+        return rmw::fail(RMW_ERR_ARG, "source split must be in [1, 64] or -1");
+    }
+    std::lock_guard<std::mutex> lk(rmw::g_tune_mu);
+    rmw::g_tuned[rmw::key_of(kind, mode, (int)n)] = nchunks;
     return RMW_OK;
 }
 

@@ -123,4 +123,72 @@ __device__ __forceinline__ void pair_contrib_df(df dx, df dy, df dz, df Rz, df h
     }
 }
 
+// UF for both orders of one pair: (ux, uy, uz) = M_ij v_j for target i and
+// (wx, wy, wz) = M_ji v_i = M_ij^T v_i for target j (the wall mobility is
+// symmetric).  In block form
+//   M_ij = Af I + Bc d d^T + s^2 f2 e e^T + s f3 e z^T + s f4 z e^T + f5 z z^T
+// with e = (dx, dy, Rz) and z the wall normal, so the transpose only swaps
+// the roles of f3 and f4: the coefficients are formed once for both.
+__device__ __forceinline__ void pair_uf_sym_df(df dx, df dy, df dz, df Rz, df hi, df hj, df vx, df vy, df vz,
+                                               df qx, df qy, df qz, df &ux, df &uy, df &uz, df &wx, df &wy,
+                                               df &wz)
+{
+    constexpr df TWO_THIRDS = dfc::make(2.0 / 3.0);
+    constexpr df FOUR_THIRDS = dfc::make(4.0 / 3.0);
+    constexpr df TEN_THIRDS = dfc::make(10.0 / 3.0);
+    const df rho2 = mad(dx, dx, sqr(dy));
+    const df r2 = mad(dz, dz, rho2);
+    const df invr = rsqrt_df(r2);
+    const df r = r2 * invr;
+    const df Rz2 = sqr(Rz);
+    const df s = rsqrt_df(rho2 + Rz2);
+    const df s2 = sqr(s);
+    const df s3 = s2 * s;
+    const df E = Rz2 * s2;
+    const df invr2 = sqr(invr);
+    df A = mad(TWO_THIRDS, invr2, df_from(1.0f)) * invr;
+    df Bc = (1.0f - scale2(invr2, 2.0f)) * invr2 * invr;
+    const bool near = !(r > 2.0f);
+    if (__any_sync(__activemask(), near)) {
+        if (near) {
+            A = FOUR_THIRDS * (1.0f - r * 0.28125f);
+            Bc = scale2(invr, 0.125f);
+        }
+    }
+    const df s5 = s3 * s2;
+    const df hh = hi * hj * s2;
+    const df ez = Rz * s;
+    const df q5 = (1.0f - E * 5.0f) * s3;
+    const df f1 = -mad(scale2(hh, 2.0f) + 1.0f, s, TWO_THIRDS * ((1.0f - E * 3.0f) * s3 - q5 * s2));
+    const df f2 = -(mad((1.0f - hh * 6.0f), s, -scale2(q5, 2.0f)) + TEN_THIRDS * ((1.0f - E * 7.0f) * s5));
+    const df f3 = TWO_THIRDS * (hj * s2 * 3.0f - (hh * ez * s) * 18.0f +
+                                ez * (((2.0f - E * 7.0f) * s5) * 10.0f - q5 * 6.0f));
+    const df f4 = TWO_THIRDS * (hj * s2 * 3.0f - (ez * s5) * 10.0f);
+    const df f5 = -FOUR_THIRDS * mad((sqr(hj) + E) * 3.0f, s3, (2.0f - E * 15.0f) * s5);
+    const df Af = A + f1;
+    const df f2s = f2 * s;
+    {  // M_ij v_j
+        const df Pxy = mad2(dx, vx, dy, vy);
+        const df dv = mad(dz, vz, Pxy);
+        const df W = mad(Rz, vz, Pxy);
+        const df Gr = Bc * dv;
+        const df Gw = mad(f2s, W, f3 * vz) * s;
+        const df G = Gr + Gw;
+        ux = mad2(Af, vx, G, dx);
+        uy = mad2(Af, vy, G, dy);
+        uz = mad2(Af, vz, Gr, dz) + mad2(Gw, Rz, f4 * W, s) + f5 * vz;
+    }
+    {  // M_ij^T v_i
+        const df Pxy = mad2(dx, qx, dy, qy);
+        const df dv = mad(dz, qz, Pxy);
+        const df W = mad(Rz, qz, Pxy);
+        const df Gr = Bc * dv;
+        const df Gw = mad(f2s, W, f4 * qz) * s;
+        const df G = Gr + Gw;
+        wx = mad2(Af, qx, G, dx);
+        wy = mad2(Af, qy, G, dy);
+        wz = mad2(Af, qz, Gr, dz) + mad2(Gw, Rz, f3 * W, s) + f5 * qz;
+    }
+}
+
 }  // namespace rmw

@@ -230,6 +230,125 @@ __global__ void __launch_bounds__(kThreads) wall_pair_df_kernel(const SrcDF *__r
 }
 
 // ---------------------------------------------------------------------------
+// Symmetric df64 UF kernel: every unordered pair is evaluated once and applied
+// both ways (M_ji = M_ij^T), about half the issued instructions per ordered
+// pair of wall_pair_df_kernel.  One CTA per (target tile T, source tile S),
+// T <= S, over the upper triangle of tiles.  Within a CTA, lane l of a warp
+// meets source (l + k) mod 128 at step k, so the 32 lanes of a warp always
+// touch 32 different sources: the source-side sums are per-warp shared-memory
+// accumulators updated without atomics (a __syncwarp orders consecutive
+// steps).  On diagonal tiles the step offset (source - target) mod 128 is
+// warp-uniform, and only offsets 1..63 (and 64 for the lower half of the
+// targets) are evaluated: each unordered pair once.
+// Partial sums: blob b of tile X receives one write per tile Y - from CTA
+// (X, Y) as a target for Y >= X (the diagonal CTA adds both roles), from CTA
+// (Y, X) as a source for Y < X - into partial[Y][3n], so the finalize kernel
+// sums ntiles slots in fixed order and the result is deterministic.
+constexpr int kSymWarps = kThreads / 32;
+
+__device__ __forceinline__ void sym_tile_pair(long long b, int nt, int &T, int &S)
+{
+    // rows T = 0.. of the upper triangle hold nt - T entries; offset(T) = T nt - T (T - 1) / 2
+    const double c = 2.0 * nt + 1.0;
+    int t = (int)floor(0.5 * (c - sqrt(fmax(c * c - 8.0 * (double)b, 0.0))));
+    t = max(0, min(nt - 1, t));
+    auto off = [nt](long long tt) { return tt * nt - tt * (tt - 1) / 2; };
+    while (t > 0 && off(t) > b) --t;
+    while (t + 1 < nt && off(t + 1) <= b) ++t;
+    T = t;
+    S = t + (int)(b - off(t));
+}
+
+__global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *__restrict__ src, int n, int nt,
+                                                                   double *__restrict__ partial)
+{
+    // structure-of-arrays source tile: the rotated reads of a warp hit 32
+    // consecutive 16-byte entries (no bank conflicts)
+    __shared__ float4 thi[kTile], tlo[kTile], tvh[kTile], tvl[kTile];
+    __shared__ double sacc[kSymWarps][3][kTile];  // per-warp source-side sums
+    int T, S;
+    sym_tile_pair(blockIdx.x, nt, T, S);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool diag = (T == S);
+    const int i = T * kTile + tid;
+    const bool valid_i = i < n;
+    // a target or source past the end is a dummy far above the wall with a zero vector
+    const SrcDF dummy = {make_float4(1.0e6f, 1.0e6f, 1.0e6f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f),
+                         make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+    const SrcDF me = valid_i ? src[i] : dummy;
+    const df xi = {me.hi.x, me.lo.x}, yi = {me.hi.y, me.lo.y}, zi = {me.hi.z, me.lo.z};
+    const df qx = {me.vhi.x, me.vlo.x}, qy = {me.vhi.y, me.vlo.y}, qz = {me.vhi.z, me.vlo.z};
+    {
+        const int j = S * kTile + tid;
+        const SrcDF sj = (j < n) ? src[j] : dummy;
+        thi[tid] = sj.hi;
+        tlo[tid] = sj.lo;
+        tvh[tid] = sj.vhi;
+        tvl[tid] = sj.vlo;
+    }
+    for (int c = 0; c < 3; ++c)
+        for (int k = lane; k < kTile; k += 32) sacc[warp][c][k] = 0.0;
+    __syncthreads();
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    df ux = df_from(0.f), uy = df_from(0.f), uz = df_from(0.f);
+    for (int k = 0; k < kTile; ++k) {
+        __syncwarp();
+        if (k && !(k & 31)) {  // fold each group of 32 double-float sums into FP64
+            ax += to_double(ux);
+            ay += to_double(uy);
+            az += to_double(uz);
+            ux = df_from(0.f);
+            uy = df_from(0.f);
+            uz = df_from(0.f);
+        }
+        if (diag) {
+            const int off = (k - 32 * warp) & (kTile - 1);  // (source - target) mod 128, warp-uniform
+            if (off == 0 || off > kTile / 2 || (off == kTile / 2 && warp >= kSymWarps / 2)) continue;
+        }
+        const int jl = (lane + k) & (kTile - 1);
+        const float4 sh = thi[jl], sl = tlo[jl], svh = tvh[jl], svl = tvl[jl];
+        const df xj = {sh.x, sl.x}, yj = {sh.y, sl.y}, zj = {sh.z, sl.z};
+        const df vx = {svh.x, svl.x}, vy = {svh.y, svl.y}, vz = {svh.z, svl.z};
+        df cx, cy, cz, wx, wy, wz;
+        pair_uf_sym_df(xi - xj, yi - yj, zi - zj, zi + zj, zi, zj, vx, vy, vz, qx, qy, qz, cx, cy, cz, wx, wy, wz);
+        acc_add(ux, cx);
+        acc_add(uy, cy);
+        acc_add(uz, cz);
+        sacc[warp][0][jl] += to_double(wx);
+        sacc[warp][1][jl] += to_double(wy);
+        sacc[warp][2][jl] += to_double(wz);
+    }
+    ax += to_double(ux);
+    ay += to_double(uy);
+    az += to_double(uz);
+    __syncthreads();
+    // source role of blob S*128 + tid (dummy pairs contributed exact zeros)
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int w = 0; w < kSymWarps; ++w) {
+        sx += sacc[w][0][tid];
+        sy += sacc[w][1][tid];
+        sz += sacc[w][2][tid];
+    }
+    const size_t stride = 3 * (size_t)n;
+    if (diag) {
+        if (valid_i) {
+            double *o = partial + (size_t)T * stride + 3 * (size_t)i;
+            o[0] = ax + sx; o[1] = ay + sy; o[2] = az + sz;
+        }
+    } else {
+        if (valid_i) {
+            double *o = partial + (size_t)S * stride + 3 * (size_t)i;
+            o[0] = ax; o[1] = ay; o[2] = az;
+        }
+        const int j = S * kTile + tid;
+        if (j < n) {
+            double *o = partial + (size_t)T * stride + 3 * (size_t)j;
+            o[0] = sx; o[1] = sy; o[2] = sz;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // FP64 pair kernel
 template <int KIND, bool PER, bool SEG>
 __global__ void __launch_bounds__(kThreads) wall_pair_fp64_kernel(const SrcD *__restrict__ src, int n, int chunk,
@@ -642,16 +761,51 @@ int wall_product_with_scratch(int kind, const double *r, const double *v, double
     return launch_dispatch(kind, r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks, nullptr);
 }
 
+bool wall_sym_applicable(int kind, int mode, int n, const double *L)
+{
+    if (kind != RMW_UF || mode != RMW_MODE_DF64) return false;
+    if (L && (L[0] > 0 || L[1] > 0 || L[2] > 0)) return false;
+    if (n < 2 * kTile) return false;
+    const double nt = (double)((n + kTile - 1) / kTile);
+    return nt * 3.0 * (double)n * sizeof(double) <= (double)kSymMaxPartialBytes;
+}
+
+int wall_sym_slots(int n) { return (n + kTile - 1) / kTile; }
+
+int wall_product_sym_with_scratch(const double *r, const double *v, double *out, int n, double eta, double a,
+                                  cudaStream_t st, void *scratch_ptr)
+{
+    const int nt = wall_sym_slots(n);
+    const size_t packed = ((sizeof(SrcDF) * (size_t)n + 255) / 256) * 256;
+    char *base = (char *)scratch_ptr;
+    SrcDF *src = (SrcDF *)base;
+    double *partial = (double *)(base + packed);
+    const int pb = 256, pg = (n + pb - 1) / pb;
+    pack_df_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
+    void *tok = nullptr;
+    if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
+    const unsigned ncta = (unsigned)((long long)nt * (nt + 1) / 2);
+    wall_uf_df_sym_kernel<<<ncta, kThreads, 0, st>>>(src, n, nt, partial);
+    if (int rc = trace_end(tok, st)) return rc;
+    wall_finalize_kernel<RMW_UF><<<pg, pb, 0, st>>>(r, v, partial, nt, out, n, a, 1.0 / (8.0 * kPi * eta * a),
+                                                     nullptr);
+    RMW_CHECK_LAUNCH("symmetric wall product kernels");
+    return RMW_OK;
+}
+
 int wall_product(int kind, const double *r, const double *v, double *out, int64_t n, double eta, double a,
                  const double *L, int mode, cudaStream_t st)
 {
     int rc = validate_product_args(kind, r, v, out, n, eta, a, mode);
     if (rc) return rc;
     if (n == 0) return RMW_OK;
-    const int nchunks = wall_chunks(kind, mode, (int)n);
+    int nchunks = wall_chunks(kind, mode, (int)n);
+    const bool sym = nchunks == kSymChunks && wall_sym_applicable(kind, mode, (int)n, L);
+    if (nchunks == kSymChunks && !sym) nchunks = wall_default_chunks((int)n);
     void *ws = nullptr;
-    rc = scratch(SCRATCH_PAIR, wall_scratch_bytes((int)n, mode, nchunks), &ws, st);
+    rc = scratch(SCRATCH_PAIR, wall_scratch_bytes((int)n, mode, sym ? wall_sym_slots((int)n) : nchunks), &ws, st);
     if (rc) return rc;
+    if (sym) return wall_product_sym_with_scratch(r, v, out, (int)n, eta, a, st, ws);
     return wall_product_with_scratch(kind, r, v, out, (int)n, eta, a, L, mode, st, ws, nchunks);
 }
 

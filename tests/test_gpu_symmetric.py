@@ -1,0 +1,80 @@
+"""GPU: the symmetric df64 M_UF kernel (each unordered pair evaluated once and
+applied both ways) against the oracle and against the standard df64 kernel:
+tile tails, diagonal-tile pairing, wall-overlapping (damped) blobs, a shell
+suspension, determinism, and the fallback where it does not apply."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle import wall as owall
+from rigidmultiblobswall_gb300 import mobility as mob
+from rigidmultiblobswall_gb300 import suspensions as S
+
+pytestmark = pytest.mark.gpu
+
+
+def _blobs(n, seed, damped=False):
+    rng = np.random.default_rng(seed)
+    r = np.empty((n, 3))
+    side = 2.0 * np.cbrt(n)
+    r[:, :2] = rng.uniform(0, side, (n, 2))
+    r[:, 2] = rng.uniform(0.1 if damped else 0.8, 4.0, n)
+    return r, rng.standard_normal(3 * n)
+
+
+def _product(r, v, a, pin):
+    import torch
+    mob.autotune_clear()
+    if pin is not None:
+        mob.autotune_set("uf", len(r), "df64", pin)
+    out = mob.wall_product("uf", torch.tensor(r, device="cuda"), torch.tensor(v, device="cuda"), 1.0, a,
+                           mode="df64").cpu().numpy()
+    mob.autotune_clear()
+    return out
+
+
+@pytest.mark.parametrize("n", [256, 257, 300, 383, 1000, 2049])
+@pytest.mark.parametrize("damped", [False, True])
+def test_symmetric_matches_oracle_and_standard(cuda_device, n, damped):
+    r, v = _blobs(n, n, damped)
+    a = 0.35
+    sym = _product(r, v, a, -1)
+    std = _product(r, v, a, 8)
+    ref = owall.wall_product("uf", r, v, 1.0, a)
+    assert rel_err(sym, ref) <= 1e-12
+    assert rel_err(sym, std) <= 1e-13
+
+
+def test_symmetric_shell_suspension_and_determinism(cuda_device):
+    s = S.shells_42_256(n_bodies=64)
+    r = s.r_vectors()
+    v = np.random.default_rng(1).standard_normal(3 * len(r))
+    a = s.a
+    x1 = _product(r, v, a, -1)
+    x2 = _product(r, v, a, -1)
+    assert np.array_equal(x1, x2)
+    rows = np.arange(0, len(r), 7)
+    ref = owall.wall_product("uf", r, v, 1.0, a, rows=rows)
+    got = x1.reshape(-1, 3)[rows].reshape(-1)
+    assert rel_err(got, ref) <= 1e-12
+
+
+def test_symmetric_choice_rules(cuda_device):
+    import torch
+    from rigidmultiblobswall_gb300._native import RMWError
+    with pytest.raises(RMWError):
+        mob.autotune_set("uf", 100, "df64", -1)  # fewer than 256 blobs
+    with pytest.raises(RMWError):
+        mob.autotune_set("ut", 1000, "df64", -1)  # only M_UF is symmetric block-wise
+    with pytest.raises(RMWError):
+        mob.autotune_set("uf", 1000, "mixed", -1)
+    mob.autotune_set("uf", 1000, "df64", -1)
+    assert mob.autotune_lookup("uf", 1000, "df64") == (-1, True)
+    # periodic products fall back to the standard kernel and stay correct
+    r, v = _blobs(1000, 5)
+    L = np.array([30.0, 30.0, 0.0])
+    got = mob.wall_product("uf", torch.tensor(r, device="cuda"), torch.tensor(v, device="cuda"), 1.0, 0.35,
+                           mode="df64", periodic_length=L).cpu().numpy()
+    mob.autotune_clear()
+    ref = owall.wall_product("uf", r, v, 1.0, 0.35, periodic_length=L)
+    assert rel_err(got, ref) <= 1e-12

@@ -114,7 +114,7 @@ int rmw_wall_autotune(int kind, int mode, int64_t n, int reps, void *stream, int
                       double *default_ms);
 int rmw_wall_autotune_lookup(int kind, int mode, int64_t n, int *nchunks, int *tuned);
 /* Pin a choice instead of measuring: nchunks in [1, 64], or -1 for the
- * symmetric df64 UF kernel (each unordered pair evaluated once and applied
+ * symmetric df64 / mixed UF kernel (each unordered pair evaluated once and applied
  * both ways; non-periodic, n >= 256, up to about 185,000 blobs: its
  * deterministic partial sums take ceil(n/128) x 3n doubles, 5.5 GB at
  * 172,032 blobs). */

@@ -348,6 +348,91 @@ __global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *_
     }
 }
 
+// Symmetric mixed-precision UF kernel: the same grid, pairing and partial-sum
+// slots as wall_uf_df_sym_kernel, FP32 pair math from double-float position
+// differences (as wall_pair_mixed_kernel).  The target-side FP32 sum over the
+// tile is folded into a TwoSum-compensated accumulator; the source side sums
+// its 32 contributions per warp in FP32 shared memory and the four warp
+// copies in FP64.
+__global__ void __launch_bounds__(kThreads) wall_uf_mixed_sym_kernel(const SrcF *__restrict__ src, int n, int nt,
+                                                                      double *__restrict__ partial)
+{
+    __shared__ float4 thi[kTile], tlo[kTile], tv[kTile];
+    __shared__ float sacc[kSymWarps][3][kTile];
+    int T, S;
+    sym_tile_pair(blockIdx.x, nt, T, S);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool diag = (T == S);
+    const int i = T * kTile + tid;
+    const bool valid_i = i < n;
+    const SrcF dummy = {make_float4(1.0e6f, 1.0e6f, 1.0e6f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f),
+                        make_float4(0.f, 0.f, 0.f, 0.f)};
+    const SrcF me = valid_i ? src[i] : dummy;
+    const float hi = me.hi.z + me.lo.z;
+    {
+        const int j = S * kTile + tid;
+        const SrcF sj = (j < n) ? src[j] : dummy;
+        thi[tid] = sj.hi;
+        tlo[tid] = sj.lo;
+        tv[tid] = sj.v;
+    }
+    for (int c = 0; c < 3; ++c)
+        for (int k = lane; k < kTile; k += 32) sacc[warp][c][k] = 0.f;
+    __syncthreads();
+    float ux = 0.f, uy = 0.f, uz = 0.f;
+    for (int k = 0; k < kTile; ++k) {
+        __syncwarp();
+        if (diag) {
+            const int off = (k - 32 * warp) & (kTile - 1);
+            if (off == 0 || off > kTile / 2 || (off == kTile / 2 && warp >= kSymWarps / 2)) continue;
+        }
+        const int jl = (lane + k) & (kTile - 1);
+        const float4 sh = thi[jl], sl = tlo[jl], sv = tv[jl];
+        const float dx = (me.hi.x - sh.x) + (me.lo.x - sl.x);
+        const float dy = (me.hi.y - sh.y) + (me.lo.y - sl.y);
+        const float dz = (me.hi.z - sh.z) + (me.lo.z - sl.z);
+        const float hj = sh.z + sl.z;
+        const float Rz = hi + hj;
+        const UFCoeffs<float> c = uf_coeffs<float>(dx, dy, dz, Rz, hi, hj);
+        uf_apply<float>(c, dx, dy, dz, Rz, sv.x, sv.y, sv.z, ux, uy, uz);
+        const UFCoeffs<float> ct = {c.Af, c.Bc, c.c2, c.c4, c.c3, c.f5};  // M^T: f3 and f4 trade places
+        float wx = 0.f, wy = 0.f, wz = 0.f;
+        uf_apply<float>(ct, dx, dy, dz, Rz, me.v.x, me.v.y, me.v.z, wx, wy, wz);
+        sacc[warp][0][jl] += wx;
+        sacc[warp][1][jl] += wy;
+        sacc[warp][2][jl] += wz;
+    }
+    float sx = 0.f, sy = 0.f, sz = 0.f, ex_ = 0.f, ey_ = 0.f, ez_ = 0.f;
+    comp_add(sx, ex_, ux);
+    comp_add(sy, ey_, uy);
+    comp_add(sz, ez_, uz);
+    const double ax = (double)sx + (double)ex_, ay = (double)sy + (double)ey_, az = (double)sz + (double)ez_;
+    __syncthreads();
+    double qx = 0.0, qy = 0.0, qz = 0.0;
+    for (int w = 0; w < kSymWarps; ++w) {
+        qx += (double)sacc[w][0][tid];
+        qy += (double)sacc[w][1][tid];
+        qz += (double)sacc[w][2][tid];
+    }
+    const size_t stride = 3 * (size_t)n;
+    if (diag) {
+        if (valid_i) {
+            double *o = partial + (size_t)T * stride + 3 * (size_t)i;
+            o[0] = ax + qx; o[1] = ay + qy; o[2] = az + qz;
+        }
+    } else {
+        if (valid_i) {
+            double *o = partial + (size_t)S * stride + 3 * (size_t)i;
+            o[0] = ax; o[1] = ay; o[2] = az;
+        }
+        const int j = S * kTile + tid;
+        if (j < n) {
+            double *o = partial + (size_t)T * stride + 3 * (size_t)j;
+            o[0] = qx; o[1] = qy; o[2] = qz;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // FP64 pair kernel
 template <int KIND, bool PER, bool SEG>
@@ -763,7 +848,7 @@ int wall_product_with_scratch(int kind, const double *r, const double *v, double
 
 bool wall_sym_applicable(int kind, int mode, int n, const double *L)
 {
-    if (kind != RMW_UF || mode != RMW_MODE_DF64) return false;
+    if (kind != RMW_UF || (mode != RMW_MODE_DF64 && mode != RMW_MODE_MIXED)) return false;
     if (L && (L[0] > 0 || L[1] > 0 || L[2] > 0)) return false;
     if (n < 2 * kTile) return false;
     const double nt = (double)((n + kTile - 1) / kTile);
@@ -773,19 +858,27 @@ bool wall_sym_applicable(int kind, int mode, int n, const double *L)
 int wall_sym_slots(int n) { return (n + kTile - 1) / kTile; }
 
 int wall_product_sym_with_scratch(const double *r, const double *v, double *out, int n, double eta, double a,
-                                  cudaStream_t st, void *scratch_ptr)
+                                  int mode, cudaStream_t st, void *scratch_ptr)
 {
     const int nt = wall_sym_slots(n);
-    const size_t packed = ((sizeof(SrcDF) * (size_t)n + 255) / 256) * 256;
+    const size_t rec = (mode == RMW_MODE_DF64) ? sizeof(SrcDF) : sizeof(SrcF);
+    const size_t packed = ((rec * (size_t)n + 255) / 256) * 256;
     char *base = (char *)scratch_ptr;
-    SrcDF *src = (SrcDF *)base;
     double *partial = (double *)(base + packed);
     const int pb = 256, pg = (n + pb - 1) / pb;
-    pack_df_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
-    void *tok = nullptr;
-    if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
     const unsigned ncta = (unsigned)((long long)nt * (nt + 1) / 2);
-    wall_uf_df_sym_kernel<<<ncta, kThreads, 0, st>>>(src, n, nt, partial);
+    void *tok = nullptr;
+    if (mode == RMW_MODE_DF64) {
+        SrcDF *src = (SrcDF *)base;
+        pack_df_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
+        if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
+        wall_uf_df_sym_kernel<<<ncta, kThreads, 0, st>>>(src, n, nt, partial);
+    } else {
+        SrcF *src = (SrcF *)base;
+        pack_mixed_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
+        if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
+        wall_uf_mixed_sym_kernel<<<ncta, kThreads, 0, st>>>(src, n, nt, partial);
+    }
     if (int rc = trace_end(tok, st)) return rc;
     wall_finalize_kernel<RMW_UF><<<pg, pb, 0, st>>>(r, v, partial, nt, out, n, a, 1.0 / (8.0 * kPi * eta * a),
                                                      nullptr);
@@ -805,7 +898,7 @@ int wall_product(int kind, const double *r, const double *v, double *out, int64_
     void *ws = nullptr;
     rc = scratch(SCRATCH_PAIR, wall_scratch_bytes((int)n, mode, sym ? wall_sym_slots((int)n) : nchunks), &ws, st);
     if (rc) return rc;
-    if (sym) return wall_product_sym_with_scratch(r, v, out, (int)n, eta, a, st, ws);
+    if (sym) return wall_product_sym_with_scratch(r, v, out, (int)n, eta, a, mode, st, ws);
     return wall_product_with_scratch(kind, r, v, out, (int)n, eta, a, L, mode, st, ws, nchunks);
 }
 

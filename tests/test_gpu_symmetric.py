@@ -1,5 +1,6 @@
-"""GPU: the symmetric df64 M_UF kernel (each unordered pair evaluated once and
-applied both ways) against the oracle and against the standard df64 kernel:
+"""GPU: the symmetric M_UF kernels, df64 and mixed (each unordered pair
+evaluated once and applied both ways) against the oracle and against the
+standard kernels:
 tile tails, diagonal-tile pairing, wall-overlapping (damped) blobs, a shell
 suspension, determinism, and the fallback where it does not apply."""
 import numpy as np
@@ -22,13 +23,13 @@ def _blobs(n, seed, damped=False):
     return r, rng.standard_normal(3 * n)
 
 
-def _product(r, v, a, pin):
+def _product(r, v, a, pin, mode="df64"):
     import torch
     mob.autotune_clear()
     if pin is not None:
-        mob.autotune_set("uf", len(r), "df64", pin)
+        mob.autotune_set("uf", len(r), mode, pin)
     out = mob.wall_product("uf", torch.tensor(r, device="cuda"), torch.tensor(v, device="cuda"), 1.0, a,
-                           mode="df64").cpu().numpy()
+                           mode=mode).cpu().numpy()
     mob.autotune_clear()
     return out
 
@@ -43,6 +44,18 @@ def test_symmetric_matches_oracle_and_standard(cuda_device, n, damped):
     ref = owall.wall_product("uf", r, v, 1.0, a)
     assert rel_err(sym, ref) <= 1e-12
     assert rel_err(sym, std) <= 1e-13
+
+
+@pytest.mark.parametrize("n", [256, 300, 1000, 2049])
+@pytest.mark.parametrize("damped", [False, True])
+def test_mixed_symmetric_matches_oracle_and_standard(cuda_device, n, damped):
+    r, v = _blobs(n, n + 1, damped)
+    a = 0.35
+    sym = _product(r, v, a, -1, "mixed")
+    std = _product(r, v, a, 8, "mixed")
+    ref = owall.wall_product("uf", r, v, 1.0, a)
+    assert rel_err(sym, ref) <= 1e-6
+    assert rel_err(sym, std) <= 1e-6
 
 
 def test_symmetric_shell_suspension_and_determinism(cuda_device):
@@ -67,7 +80,7 @@ def test_symmetric_choice_rules(cuda_device):
     with pytest.raises(RMWError):
         mob.autotune_set("ut", 1000, "df64", -1)  # only M_UF is symmetric block-wise
     with pytest.raises(RMWError):
-        mob.autotune_set("uf", 1000, "mixed", -1)
+        mob.autotune_set("uf", 1000, "fp64", -1)
     mob.autotune_set("uf", 1000, "df64", -1)
     assert mob.autotune_lookup("uf", 1000, "df64") == (-1, True)
     # periodic products fall back to the standard kernel and stay correct

@@ -236,8 +236,8 @@ __global__ void __launch_bounds__(kThreads) wall_pair_df_kernel(const SrcDF *__r
 // T <= S, over the upper triangle of tiles.  Within a CTA, lane l of a warp
 // meets source (l + k) mod 128 at step k, so the 32 lanes of a warp always
 // touch 32 different sources: the source-side sums are per-warp shared-memory
-// accumulators updated without atomics (a __syncwarp orders consecutive
-// steps).  On diagonal tiles the step offset (source - target) mod 128 is
+// double-float accumulators updated without atomics (a __syncwarp orders
+// consecutive steps).  On diagonal tiles the step offset (source - target) mod 128 is
 // warp-uniform, and only offsets 1..63 (and 64 for the lower half of the
 // targets) are evaluated: each unordered pair once.
 // Partial sums: blob b of tile X receives one write per tile Y - from CTA
@@ -265,7 +265,7 @@ __global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *_
     // structure-of-arrays source tile: the rotated reads of a warp hit 32
     // consecutive 16-byte entries (no bank conflicts)
     __shared__ float4 thi[kTile], tlo[kTile], tvh[kTile], tvl[kTile];
-    __shared__ double sacc[kSymWarps][3][kTile];  // per-warp source-side sums
+    __shared__ float2 sacc[kSymWarps][3][kTile];  // per-warp source-side double-float sums (hi, lo)
     int T, S;
     sym_tile_pair(blockIdx.x, nt, T, S);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *_
         tvl[tid] = sj.vlo;
     }
     for (int c = 0; c < 3; ++c)
-        for (int k = lane; k < kTile; k += 32) sacc[warp][c][k] = 0.0;
+        for (int k = lane; k < kTile; k += 32) sacc[warp][c][k] = make_float2(0.f, 0.f);
     __syncthreads();
     double ax = 0.0, ay = 0.0, az = 0.0;
     df ux = df_from(0.f), uy = df_from(0.f), uz = df_from(0.f);
@@ -314,9 +314,15 @@ __global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *_
         acc_add(ux, cx);
         acc_add(uy, cy);
         acc_add(uz, cz);
-        sacc[warp][0][jl] += to_double(wx);
-        sacc[warp][1][jl] += to_double(wy);
-        sacc[warp][2][jl] += to_double(wz);
+        // double-float accumulation on the FP32 pipe (no FP64 conversions per pair)
+        const df wv[3] = {wx, wy, wz};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float2 a2 = sacc[warp][c][jl];
+            df acc = {a2.x, a2.y};
+            acc_add(acc, wv[c]);
+            sacc[warp][c][jl] = make_float2(acc.hi, acc.lo);
+        }
     }
     ax += to_double(ux);
     ay += to_double(uy);
@@ -325,9 +331,9 @@ __global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *_
     // source role of blob S*128 + tid (dummy pairs contributed exact zeros)
     double sx = 0.0, sy = 0.0, sz = 0.0;
     for (int w = 0; w < kSymWarps; ++w) {
-        sx += sacc[w][0][tid];
-        sy += sacc[w][1][tid];
-        sz += sacc[w][2][tid];
+        sx += (double)sacc[w][0][tid].x + (double)sacc[w][0][tid].y;
+        sy += (double)sacc[w][1][tid].x + (double)sacc[w][1][tid].y;
+        sz += (double)sacc[w][2][tid].x + (double)sacc[w][2][tid].y;
     }
     const size_t stride = 3 * (size_t)n;
     if (diag) {

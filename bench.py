@@ -35,14 +35,17 @@ FLOPS_PER_PAIR = {"uf": 200.0, "ut": 115.0, "wf": 115.0, "wt": 125.0}  # counted
 METRIC = "wall-RPY M.F Gpairs/s"
 HEAD_MODE = "df64"
 WORKLOAD = "wall-RPY M_UF.F, 256 shells x 42 blobs = 10,752 blobs (FP64-accurate: df64, <= 1e-12 vs FP64)"
-# Issued thread instructions per pair of the df64 UF pair kernel (all pipes;
-# 85 % of them on the FMA pipe), from the ncu capture summarised in
-# profiles/wall_pair_df64_uf_shells42x256.md: smsp__inst_executed.sum * 32 / N^2
-# = 3,310,220,558 * 32 / 10752^2 = 916.3.  The FP32 pipe issues at most one
+# Issued thread instructions per ordered pair of the df64 UF kernels (all
+# pipes, 80-85 % of them on the FMA pipe), from the ncu captures summarised in
+# profiles/wall_uf_df_sym_shells42x256.md (symmetric kernel, each unordered
+# pair once: smsp__inst_executed.sum * 32 / N^2 = 2,149,318,640 * 32 / 10752^2
+# = 594.9) and profiles/wall_pair_df64_uf_shells42x256.md (standard kernel:
+# 3,310,220,558 * 32 / 10752^2 = 916.3).  The FP32 pipe issues at most one
 # thread instruction per lane per clock, the rate the FMA-chain probe measures
 # (FLOP/s / 2), so achieved / peak is the fraction of issue capacity used.
-DF64_FMA_PIPE_INST_PER_PAIR = {"uf": 3310220558.0 * 32 / 10752 ** 2}
-DF64_TRAFFIC_BYTES_PER_LAUNCH = 723456  # dram__bytes_read.sum + dram__bytes_write.sum, same capture
+DF64_UF_INST_PER_PAIR = {"symmetric": 2149318640.0 * 32 / 10752 ** 2, "standard": 3310220558.0 * 32 / 10752 ** 2}
+# dram__bytes_read.sum + dram__bytes_write.sum per launch, same captures
+DF64_UF_TRAFFIC_BYTES = {"symmetric": 722176, "standard": 723456}
 
 
 def parse():
@@ -562,14 +565,16 @@ def main():
     # ---- roofline of the dominant kernel (the df64 pair kernel; bound by the FP32/FMA pipe)
     pair_ms = pair_ms_total / max(pair_launches, 1)
     alg_tflops = n * n * FLOPS_PER_PAIR["uf"] / (pair_ms * 1e-3) / 1e12
-    ipp = DF64_FMA_PIPE_INST_PER_PAIR["uf"]
+    kernel = "symmetric" if tune["nchunks"] == -1 else "standard"
+    ipp = DF64_UF_INST_PER_PAIR[kernel]
     peak_inst = peak32 / 2.0  # FMA-pipe thread instructions per second (one FFMA = 2 flops)
     roofline = {"bound": "fp32-pipe (issue)", "unit": "Tinst/s", "peak": peak_inst / 1e12,
                 "achieved": (n * n * ipp / (pair_ms * 1e-3) / 1e12) if ipp else None,
                 "frac": (n * n * ipp / (pair_ms * 1e-3) / peak_inst) if ipp else None,
-                "traffic": DF64_TRAFFIC_BYTES_PER_LAUNCH,
+                "traffic": DF64_UF_TRAFFIC_BYTES[kernel], "kernel": "wall_uf_df_sym_kernel" if kernel == "symmetric"
+                else "wall_pair_df_kernel<UF>",
                 "peak_source": "measured by rmw_fma_peak (FP32 FMA chains on all SMs) in this run, / 2 per FFMA",
-                "pair_kernel_ms": pair_ms, "fma_pipe_inst_per_pair": ipp,
+                "pair_kernel_ms": pair_ms, "issued_inst_per_ordered_pair": ipp,
                 "algorithmic_tflops_fp64_equivalent": alg_tflops, "flops_per_pair": FLOPS_PER_PAIR["uf"],
                 "algorithmic_vs_measured_fp64_peak": alg_tflops / (peak64 / 1e12)}
 
@@ -617,8 +622,10 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "df64 (f64-accurate)", "data": "synthetic (seeded)",
                 "config": {"workload": WORKLOAD, "mode": HEAD_MODE, "n_blobs": n, "pairs_per_step": n * n, "eta": eta, "a": a,
                            "l2": "512 MB buffer written between timed steps (inputs 0.5 MB < L2)",
-                           "launch_shape": {"source_chunks": tune["nchunks"], "chosen_by": "rmw_wall_autotune",
-                                            "tuned_ms": tune["ms"], "builtin_rule_ms": tune["default_ms"]},
+                           "launch_shape": {"kernel": kernel, "source_chunks": None if kernel == "symmetric"
+                                            else tune["nchunks"], "chosen_by": "rmw_wall_autotune",
+                                            "tuned_ms": tune["ms"],
+                                            "standard_kernel_builtin_split_ms": tune["default_ms"]},
                            "parallelism": "replicas" if ws > 1 else "single GPU"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
                 "gpu_launches": 3 * args.steps, "wall_s_timed_region": t_wall,

@@ -608,6 +608,33 @@ def main():
             res["alg_frac_of_mode_peak"] = res["alg_tflops"] * 1e12 / peak
             products["%s_%s" % (kind, mode)] = {k: round(v, 6) for k, v in res.items()}
 
+    # fused force-and-torque product [U; W] = M [F; T] against its four single products
+    if not args.no_extras:
+        tt = torch.tensor(np.random.default_rng(7).standard_normal(3 * n), device=dev)
+        for mode in ("fp64", "df64", "mixed"):
+            reps = 3 if mode == "fp64" else 10
+
+            def fused():
+                return mb.wall_force_torque(rt, ft, tt, eta, a, mode=mode)
+
+            def four():
+                return [mb.wall_product(k, rt, v, eta, a, mode=mode) for k, v in (("uf", ft), ("ut", tt), ("wf", ft),
+                                                                                 ("wt", tt))]
+            res = {}
+            for name, fn in (("fused_ms", fused), ("four_products_ms", four)):
+                fn()
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(reps):
+                    fn()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                res[name] = e0.elapsed_time(e1) / reps
+            res["gpairs_fused"] = n * n / (res["fused_ms"] * 1e-3) / 1e9
+            products["force_torque_6n_%s" % mode] = {k: round(v, 6) for k, v in res.items()}
+
     solver = {} if args.no_extras else solver_metrics(dev)
     if not args.no_extras:
         solver["batched_64_suspensions"] = batched_metrics(dev)

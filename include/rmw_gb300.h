@@ -103,6 +103,17 @@ int rmw_wall_uf_multi(const double *r, const double *V, double *Y, int64_t n, in
 int rmw_wall_product_host(int kind, const double *r_host, const double *v_host, double *out_host,
                           int64_t n, double eta, double a, const double *L_host, int mode);
 
+/* Fused force-and-torque product: U = M_UF F + M_UT T and, if W != NULL,
+ * W = M_WF F + M_WT T, in one pass over the pairs (the four blocks share
+ * each pair's geometry).  U alone replaces
+ * single_wall_mobility_trans_times_force_torque_pycuda (mobility/mobility.py:
+ * 384-411, kernel mobility/mobility_pycuda.py:1266-1392); [U; W] replaces the
+ * four products of Lub_Solver.Wall_Mobility_Mult (Lubrication/Lub_Solver.py:
+ * 277-305).  Device arrays of 3n doubles; same regularisation, periodic
+ * images, modes and errors as rmw_wall_product. */
+int rmw_wall_force_torque(const double *r, const double *F, const double *T, double *U, double *W, int64_t n,
+                          double eta, double a, const double *L_host, int mode, void *stream);
+
 /* Launch-shape autotuner (no reference counterpart): times every admissible
  * source split of the all-pairs grid (and, for the df64 UF product, the
  * symmetric kernel, reported as nchunks = -1) on n synthetic blobs and caches the

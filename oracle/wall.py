@@ -141,3 +141,15 @@ def blake_point_mobility(r_vectors, eta):
             PD /= 4 * np.pi * Rn ** 3
             M[3 * j:3 * j + 3, 3 * k:3 * k + 3] = (S + 2.0 * h * SD - h * h * PD) / eta
     return M
+
+
+def force_torque(r_vectors, force, torque, eta, a, periodic_length=None, rows=None):
+    """(U, W) = (M_UF F + M_UT T, M_WF F + M_WT T): the reference's
+    single_wall_mobility_trans_times_force_torque (mobility/mobility.py:384-411)
+    for U and the four products of Lub_Solver.Wall_Mobility_Mult
+    (Lubrication/Lub_Solver.py:277-305) for both, composed from the oracle
+    products."""
+    kw = {"periodic_length": periodic_length, "rows": rows}
+    U = wall_product("uf", r_vectors, force, eta, a, **kw) + wall_product("ut", r_vectors, torque, eta, a, **kw)
+    W = wall_product("wf", r_vectors, force, eta, a, **kw) + wall_product("wt", r_vectors, torque, eta, a, **kw)
+    return U, W

@@ -89,6 +89,61 @@ def wall_product(kind, r_vectors, vector, eta, a, **kwargs):
     return out
 
 
+def wall_force_torque(r_vectors, force, torque, eta, a, with_rotation=True, **kwargs):
+    """U = M_UF F + M_UT T and (with_rotation) W = M_WF F + M_WT T in one pass
+    over the pairs, with the wall regularisation of the single products.
+    Returns U, or (U, W); numpy in -> numpy out, CUDA tensors stay on the device."""
+    import torch
+    L = _periodic(kwargs)
+    mode = _mode(kwargs)
+    on_device = _is_torch(r_vectors) or _is_torch(force) or _is_torch(torque)
+    dev = None
+    for x in (r_vectors, force, torque):
+        if _is_torch(x) and x.is_cuda:
+            dev = x.device
+    if dev is None:
+        if on_device:
+            raise ValueError("torch inputs must be CUDA tensors")
+        dev = torch.device("cuda", torch.cuda.current_device())
+    r = torch.as_tensor(r_vectors, dtype=torch.float64, device=dev).reshape(-1, 3).contiguous()
+    n = r.shape[0]
+    f = torch.as_tensor(force, dtype=torch.float64, device=dev).reshape(-1).contiguous()
+    t = torch.as_tensor(torque, dtype=torch.float64, device=dev).reshape(-1).contiguous()
+    if f.numel() != 3 * n or t.numel() != 3 * n:
+        raise ValueError("force and torque must have 3N entries")
+    U = torch.empty(3 * n, dtype=torch.float64, device=dev)
+    W = torch.empty(3 * n, dtype=torch.float64, device=dev) if with_rotation else None
+    with torch.cuda.device(dev):
+        _native.call("rmw_wall_force_torque", r.data_ptr(), f.data_ptr(), t.data_ptr(), U.data_ptr(),
+                     W.data_ptr() if W is not None else None, n, float(eta), float(a),
+                     L.ctypes.data_as(ctypes.c_void_p), mode, torch.cuda.current_stream(dev).cuda_stream)
+    if not on_device:
+        U = U.cpu().numpy()
+        W = W.cpu().numpy() if W is not None else None
+    return (U, W) if with_rotation else U
+
+
+def single_wall_mobility_trans_times_force_torque_gb300(r_vectors, force, torque, eta, a, *args, **kwargs):
+    """U = M_UF F + M_UT T (mobility/mobility.py:384-411)."""
+    return wall_force_torque(r_vectors, force, torque, eta, a, with_rotation=False, **kwargs)
+
+
+def wall_mobility_mult(r_vectors, X, eta, a, **kwargs):
+    """[U_1 W_1 U_2 W_2 ...] = M [F_1 T_1 F_2 T_2 ...], the layout of
+    Lub_Solver.Wall_Mobility_Mult (Lubrication/Lub_Solver.py:277-305), in one
+    fused pass instead of four products."""
+    xp = X
+    if _is_torch(X):
+        FT = X.reshape(-1, 6)
+    else:
+        FT = np.asarray(xp, dtype=np.float64).reshape(-1, 6)
+    U, W = wall_force_torque(r_vectors, FT[:, 0:3].reshape(-1), FT[:, 3:6].reshape(-1), eta, a, **kwargs)
+    if _is_torch(U):
+        import torch
+        return torch.cat([U.reshape(-1, 3), W.reshape(-1, 3)], dim=1).reshape(-1)
+    return np.concatenate([U.reshape(-1, 3), W.reshape(-1, 3)], axis=1).reshape(-1)
+
+
 class SuspensionBatch:
     """Segmented products of many independent suspensions stored in one (N,3)
     array: suspension k owns blobs [blob_offsets[k], blob_offsets[k+1]) and
@@ -224,3 +279,4 @@ single_wall_mobility_rot_times_force_pycuda = single_wall_mobility_rot_times_for
 single_wall_mobility_rot_times_force_numba = single_wall_mobility_rot_times_force_gb300
 single_wall_mobility_rot_times_torque_pycuda = single_wall_mobility_rot_times_torque_gb300
 single_wall_mobility_rot_times_torque_numba = single_wall_mobility_rot_times_torque_gb300
+single_wall_mobility_trans_times_force_torque_pycuda = single_wall_mobility_trans_times_force_torque_gb300

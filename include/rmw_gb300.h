@@ -103,6 +103,15 @@ int rmw_wall_uf_multi(const double *r, const double *V, double *Y, int64_t n, in
 int rmw_wall_product_host(int kind, const double *r_host, const double *v_host, double *out_host,
                           int64_t n, double eta, double a, const double *L_host, int mode);
 
+/* Free-space (no-wall) RPY products out = M_kind v, kind = RMW_UF .. RMW_WT:
+ * the reference's no_wall_mobility_{trans_times_force, trans_times_torque,
+ * rot_times_force, rot_times_torque}_{pycuda,numba} (mobility/mobility.py:
+ * 288-482, kernels mobility/mobility_numba.py:13-1190).  Positions are used
+ * as given (no wall, no regularisation); periodic images, modes, device
+ * pointers and errors as rmw_wall_product. */
+int rmw_nowall_product(int kind, const double *r, const double *v, double *out, int64_t n, double eta, double a,
+                       const double *L_host, int mode, void *stream);
+
 /* Fused force-and-torque product: U = M_UF F + M_UT T and, if W != NULL,
  * W = M_WF F + M_WT T, in one pass over the pairs (the four blocks share
  * each pair's geometry).  U alone replaces

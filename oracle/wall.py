@@ -35,6 +35,7 @@ def _lib(fast=False):
     lib.oracle_wall_product_rows.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_long, lp, ctypes.c_long,
                                              ctypes.c_double, ctypes.c_double, dp]
     lib.oracle_wall_raw_rows.argtypes = lib.oracle_wall_product_rows.argtypes
+    lib.oracle_nowall_rows.argtypes = lib.oracle_wall_product_rows.argtypes
     lib.oracle_wall_uf_symmetric.argtypes = [dp, dp, dp, ctypes.c_long, ctypes.c_double, ctypes.c_double,
                                              ctypes.c_int]
     lib.oracle_max_threads.restype = ctypes.c_int
@@ -66,6 +67,28 @@ def wall_product(kind, r_vectors, vector, eta, a, periodic_length=None, rows=Non
         nr = 0
     fn = lib.oracle_wall_product_rows if regularize else lib.oracle_wall_raw_rows
     fn(KINDS[kind], _dp(r), _dp(v), _dp(out), n, rp, nr, float(eta), float(a), _dp(L))
+    return out
+
+
+def no_wall_product(kind, r_vectors, vector, eta, a, periodic_length=None, rows=None):
+    """Free-space RPY product M v (no wall, no regularisation) of the no-wall
+    numba functions (mobility/mobility_numba.py:13-1190)."""
+    lib = _lib()
+    r = np.ascontiguousarray(np.asarray(r_vectors, dtype=np.float64).reshape(-1, 3))
+    v = np.ascontiguousarray(np.asarray(vector, dtype=np.float64).reshape(-1))
+    n = r.shape[0]
+    assert v.size == 3 * n
+    L = np.zeros(3) if periodic_length is None else np.ascontiguousarray(periodic_length, dtype=np.float64)
+    if rows is not None:
+        rows = np.ascontiguousarray(rows, dtype=np.int64)
+        out = np.empty(3 * rows.size)
+        rp = rows.ctypes.data_as(ctypes.POINTER(ctypes.c_long))
+        nr = rows.size
+    else:
+        out = np.empty(3 * n)
+        rp = ctypes.POINTER(ctypes.c_long)()
+        nr = 0
+    lib.oracle_nowall_rows(KINDS[kind], _dp(r), _dp(v), _dp(out), n, rp, nr, float(eta), float(a), _dp(L))
     return out
 
 

@@ -302,6 +302,106 @@ void oracle_wall_raw_rows(int kind, const double *r, const double *v, double *ou
     }
 }
 
+/* Free-space RPY block (no wall) applied to v, unscaled: the no-wall numba
+ * products mobility/mobility_numba.py:13-130 (UF), 440-560 (UT), 832-950 (WF),
+ * 1077-1190 (WT), same operation order.  r* are unscaled differences. */
+static void rpy_block(int kind, double rx, double ry, double rz, int self, double inva, const double *v,
+                      double *out)
+{
+    double Mxx, Mxy, Mxz, Myy, Myz, Mzz, Myx, Mzx, Mzy;
+    if (self) {
+        double d = (kind == 0) ? 4.0 / 3.0 : (kind == 3 ? 1.0 : 0.0);
+        Mxx = d; Myy = d; Mzz = d;
+        Mxy = Mxz = Myz = 0.0;
+        Myx = Mzx = Mzy = 0.0;
+    } else {
+        rx *= inva;
+        ry *= inva;
+        rz *= inva;
+        double r2 = rx * rx + ry * ry + rz * rz;
+        double r = sqrt(r2);
+        if (kind == 0) {
+            double invr = 1.0 / r, invr2 = invr * invr, c1, c2;
+            if (r > 2) {
+                c1 = 1.0 + 2.0 / (3.0 * r2);
+                c2 = (1.0 - 2.0 * invr2) * invr2;
+                Mxx = (c1 + c2 * rx * rx) * invr; Mxy = (c2 * rx * ry) * invr; Mxz = (c2 * rx * rz) * invr;
+                Myy = (c1 + c2 * ry * ry) * invr; Myz = (c2 * ry * rz) * invr; Mzz = (c1 + c2 * rz * rz) * invr;
+            } else {
+                c1 = 4.0 / 3.0 * (1.0 - 0.28125 * r);
+                c2 = 4.0 / 3.0 * 0.09375 * invr;
+                Mxx = c1 + c2 * rx * rx; Mxy = c2 * rx * ry; Mxz = c2 * rx * rz;
+                Myy = c1 + c2 * ry * ry; Myz = c2 * ry * rz; Mzz = c1 + c2 * rz * rz;
+            }
+            Myx = Mxy; Mzx = Mxz; Mzy = Myz;
+        } else if (kind == 1 || kind == 2) {
+            double r3 = r2 * r, invr3 = 1.0 / r3;
+            Mxx = Myy = Mzz = 0.0;
+            if (r >= 2) {
+                Mxy = rz * invr3; Mxz = -ry * invr3; Myz = rx * invr3;
+            } else {
+                double c1 = 0.5 * (1.0 - 0.375 * r);
+                Mxy = c1 * rz; Mxz = -c1 * ry; Myz = c1 * rx;
+            }
+            Myx = -Mxy; Mzx = -Mxz; Mzy = -Myz;
+        } else {
+            double r3 = r2 * r, invr = 1.0 / r, invr2 = 1.0 / r2, invr3 = 1.0 / r3, c1, c2;
+            if (r >= 2) {
+                c1 = -0.5;
+                c2 = 1.5 * invr2;
+                Mxx = (c1 + c2 * rx * rx) * invr3; Mxy = (c2 * rx * ry) * invr3; Mxz = (c2 * rx * rz) * invr3;
+                Myy = (c1 + c2 * ry * ry) * invr3; Myz = (c2 * ry * rz) * invr3; Mzz = (c1 + c2 * rz * rz) * invr3;
+            } else {
+                c1 = (1.0 - 0.84375 * r + 0.078125 * r3);
+                c2 = 0.28125 * invr - 0.046875 * r;
+                Mxx = c1 + c2 * rx * rx; Mxy = c2 * rx * ry; Mxz = c2 * rx * rz;
+                Myy = c1 + c2 * ry * ry; Myz = c2 * ry * rz; Mzz = c1 + c2 * rz * rz;
+            }
+            Myx = Mxy; Mzx = Mxz; Mzy = Myz;
+        }
+    }
+    out[0] = Mxx * v[0] + Mxy * v[1] + Mxz * v[2];
+    out[1] = Myx * v[0] + Myy * v[1] + Myz * v[2];
+    out[2] = Mzx * v[0] + Mzy * v[1] + Mzz * v[2];
+}
+
+/* Free-space RPY product (no wall, no regularisation) for all targets or the
+ * listed rows; periodic images as in the wall products. */
+void oracle_nowall_rows(int kind, const double *r, const double *v, double *out, long n, const long *rows,
+                        long nrows, double eta, double a, const double *L)
+{
+    double Lx = L ? L[0] : 0.0, Ly = L ? L[1] : 0.0, Lz = L ? L[2] : 0.0;
+    int px = Lx > 0, py = Ly > 0, pz = Lz > 0;
+    double inva = 1.0 / a;
+    double nf = norm_factor(kind, eta, a);
+    long nt = rows ? nrows : n;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (long t = 0; t < nt; ++t) {
+        long i = rows ? rows[t] : t;
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int bx = -px; bx <= px; ++bx)
+            for (int by = -py; by <= py; ++by)
+                for (int bz = -pz; bz <= pz; ++bz)
+                    for (long j = 0; j < n; ++j) {
+                        double rx = r[3 * i] - r[3 * j];
+                        double ry = r[3 * i + 1] - r[3 * j + 1];
+                        double rz = r[3 * i + 2] - r[3 * j + 2];
+                        if (Lx > 0) rx = project(rx, Lx) + bx * Lx;
+                        if (Ly > 0) ry = project(ry, Ly) + by * Ly;
+                        if (Lz > 0) rz = project(rz, Lz) + bz * Lz;
+                        int self = (i == j) && bx == 0 && by == 0 && bz == 0;
+                        double blk[3];
+                        rpy_block(kind, rx, ry, rz, self, inva, v + 3 * j, blk);
+                        acc[0] += blk[0] * nf;
+                        acc[1] += blk[1] * nf;
+                        acc[2] += blk[2] * nf;
+                    }
+        out[3 * t] = acc[0];
+        out[3 * t + 1] = acc[1];
+        out[3 * t + 2] = acc[2];
+    }
+}
+
 void oracle_wall_raw(int kind, const double *r, const double *v, double *out,
                      long n, double eta, double a, const double *L)
 {

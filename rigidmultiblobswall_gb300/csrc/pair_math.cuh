@@ -181,6 +181,59 @@ __device__ __forceinline__ void uf_apply(const UFCoeffs<T> &c, T dx, T dy, T dz,
     uz += c.Af * vz + Gr * dz + Gw * Rz + c.c4 * W + c.f5 * vz;
 }
 
+// Free-space RPY blocks (no wall): the RPY parts of pair_contrib, for the
+// no-wall products (mobility/mobility_numba.py:13-1190).  (dx, dy, dz) =
+// (r_i - r_j)/a.  Accumulates M_ij v into (ux, uy, uz), unscaled.
+template <int KIND, typename T>
+__device__ __forceinline__ void pair_rpy(T dx, T dy, T dz, T vx, T vy, T vz, T &ux, T &uy, T &uz)
+{
+    const T r2 = dx * dx + dy * dy + dz * dz;
+    const T invr = rsq<T>(r2);
+    const T r = r2 * invr;
+    const T dv = dx * vx + dy * vy + dz * vz;
+    if (KIND == RMW_UF) {
+        const T invr2 = invr * invr;
+        T A = (T(1) + T(2.0 / 3.0) * invr2) * invr;
+        T Bc = (T(1) - T(2) * invr2) * invr2 * invr;
+        const bool near = !(r > T(2));
+        if (__any_sync(__activemask(), near)) {
+            if (near) {
+                A = T(4.0 / 3.0) * (T(1) - T(0.28125) * r);
+                Bc = T(0.125) * invr;
+            }
+        }
+        const T G = Bc * dv;
+        ux += A * vx + G * dx;
+        uy += A * vy + G * dy;
+        uz += A * vz + G * dz;
+    } else if (KIND == RMW_UT || KIND == RMW_WF) {
+        T c = invr * invr * invr;
+        const bool near = !(r >= T(2));
+        if (__any_sync(__activemask(), near)) {
+            if (near) c = T(0.5) * (T(1) - T(0.375) * r);
+        }
+        ux += c * (vy * dz - vz * dy);
+        uy += c * (vz * dx - vx * dz);
+        uz += c * (dy * vx - dx * vy);
+    } else {  // RMW_WT
+        const T invr2 = invr * invr;
+        const T invr3 = invr2 * invr;
+        T A = T(-0.5) * invr3;
+        T Bc = T(1.5) * invr2 * invr3;
+        const bool near = !(r >= T(2));
+        if (__any_sync(__activemask(), near)) {
+            if (near) {
+                A = T(1) - T(0.84375) * r + T(0.078125) * r * r2;
+                Bc = T(0.28125) * invr - T(0.046875) * r;
+            }
+        }
+        const T G = Bc * dv;
+        ux += A * vx + G * dx;
+        uy += A * vy + G * dy;
+        uz += A * vz + G * dz;
+    }
+}
+
 // Minimum-image projection of mobility/mobility_numba.py (int() truncates toward zero).
 template <typename T> __device__ __forceinline__ T project(T d, T L)
 {

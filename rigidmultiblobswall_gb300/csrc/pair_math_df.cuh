@@ -123,6 +123,60 @@ __device__ __forceinline__ void pair_contrib_df(df dx, df dy, df dz, df Rz, df h
     }
 }
 
+// Free-space RPY block (no wall) in double-float: writes M_ij v (unscaled) to
+// (ux, uy, uz); the double-float form of pair_rpy (pair_math.cuh).
+template <int KIND>
+__device__ __forceinline__ void pair_rpy_df(df dx, df dy, df dz, df vx, df vy, df vz, df &ux, df &uy, df &uz)
+{
+    constexpr df TWO_THIRDS = dfc::make(2.0 / 3.0);
+    constexpr df FOUR_THIRDS = dfc::make(4.0 / 3.0);
+    const df r2 = mad(dz, dz, mad(dx, dx, sqr(dy)));
+    const df invr = rsqrt_df(r2);
+    const df r = r2 * invr;
+    const df dv = mad(dz, vz, mad2(dx, vx, dy, vy));
+    if (KIND == RMW_UF) {
+        const df invr2 = sqr(invr);
+        df A = mad(TWO_THIRDS, invr2, df_from(1.0f)) * invr;
+        df Bc = (1.0f - scale2(invr2, 2.0f)) * invr2 * invr;
+        const bool near = !(r > 2.0f);
+        if (__any_sync(__activemask(), near)) {
+            if (near) {
+                A = FOUR_THIRDS * (1.0f - r * 0.28125f);
+                Bc = scale2(invr, 0.125f);
+            }
+        }
+        const df G = Bc * dv;
+        ux = mad2(A, vx, G, dx);
+        uy = mad2(A, vy, G, dy);
+        uz = mad2(A, vz, G, dz);
+    } else if (KIND == RMW_UT || KIND == RMW_WF) {
+        df c = sqr(invr) * invr;
+        const bool near = !(r >= 2.0f);
+        if (__any_sync(__activemask(), near)) {
+            if (near) c = scale2(1.0f - r * 0.375f, 0.5f);
+        }
+        ux = c * mad2(vy, dz, -vz, dy);
+        uy = c * mad2(vz, dx, -vx, dz);
+        uz = c * mad2(dy, vx, -dx, vy);
+    } else {
+        const df invr2 = sqr(invr);
+        const df invr3 = invr2 * invr;
+        df A = invr3 * -0.5f;
+        df Bc = (invr2 * invr3) * 1.5f;
+        const bool near = !(r >= 2.0f);
+        if (__any_sync(__activemask(), near)) {
+            if (near) {
+                A = (1.0f - r * 0.84375f) + (r * r2) * 0.078125f;
+                Bc = invr * 0.28125f - r * 0.046875f;
+            }
+        }
+        const df G = Bc * dv;
+        ux = mad2(A, vx, G, dx);
+        uy = mad2(A, vy, G, dy);
+        uz = mad2(A, vz, G, dz);
+    }
+}
+
 // UF for both orders of one pair: (ux, uy, uz) = M_ij v_j for target i and
 // (wx, wy, wz) = M_ji v_i = M_ij^T v_i for target j (the wall mobility is
 // symmetric).  In block form

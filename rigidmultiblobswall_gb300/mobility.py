@@ -123,6 +123,60 @@ def wall_force_torque(r_vectors, force, torque, eta, a, with_rotation=True, **kw
     return (U, W) if with_rotation else U
 
 
+def no_wall_product(kind, r_vectors, vector, eta, a, **kwargs):
+    """Free-space RPY product M_kind v (no wall, no regularisation), kind in
+    {'uf','ut','wf','wt'}; numpy in -> numpy out, CUDA tensors stay on the device."""
+    import torch
+    L = _periodic(kwargs)
+    mode = _mode(kwargs)
+    on_device = _is_torch(r_vectors) or _is_torch(vector)
+    dev = None
+    for x in (r_vectors, vector):
+        if _is_torch(x) and x.is_cuda:
+            dev = x.device
+    if dev is None:
+        if on_device:
+            raise ValueError("torch inputs must be CUDA tensors")
+        dev = torch.device("cuda", torch.cuda.current_device())
+    r = torch.as_tensor(r_vectors, dtype=torch.float64, device=dev).reshape(-1, 3).contiguous()
+    n = r.shape[0]
+    v = torch.as_tensor(vector, dtype=torch.float64, device=dev).reshape(-1).contiguous()
+    if v.numel() != 3 * n:
+        raise ValueError("vector must have 3N entries")
+    out = torch.empty(3 * n, dtype=torch.float64, device=dev)
+    with torch.cuda.device(dev):
+        _native.call("rmw_nowall_product", _native.KINDS[kind], r.data_ptr(), v.data_ptr(), out.data_ptr(), n,
+                     float(eta), float(a), L.ctypes.data_as(ctypes.c_void_p), mode,
+                     torch.cuda.current_stream(dev).cuda_stream)
+    return out if on_device else out.cpu().numpy()
+
+
+def no_wall_mobility_trans_times_force_gb300(r_vectors, force, eta, a, *args, **kwargs):
+    """Free-space RPY M_UF F (mobility/mobility.py:288-297)."""
+    return no_wall_product("uf", r_vectors, force, eta, a, **kwargs)
+
+
+def no_wall_mobility_trans_times_torque_gb300(r_vectors, torque, eta, a, *args, **kwargs):
+    """Free-space RPY M_UT T (mobility/mobility.py:482-491)."""
+    return no_wall_product("ut", r_vectors, torque, eta, a, **kwargs)
+
+
+def no_wall_mobility_rot_times_force_gb300(r_vectors, force, eta, a, *args, **kwargs):
+    """Free-space RPY M_WF F (mobility/mobility.py:328-337)."""
+    return no_wall_product("wf", r_vectors, force, eta, a, **kwargs)
+
+
+def no_wall_mobility_rot_times_torque_gb300(r_vectors, torque, eta, a, *args, **kwargs):
+    """Free-space RPY M_WT T (mobility/mobility.py:370-379)."""
+    return no_wall_product("wt", r_vectors, torque, eta, a, **kwargs)
+
+
+def no_wall_mobility_trans_times_force_torque_gb300(r_vectors, force, torque, eta, a, *args, **kwargs):
+    """Free-space U = M_UF F + M_UT T (mobility/mobility.py:413-423)."""
+    return (no_wall_product("uf", r_vectors, force, eta, a, **kwargs) +
+            no_wall_product("ut", r_vectors, torque, eta, a, **kwargs))
+
+
 def single_wall_mobility_trans_times_force_torque_gb300(r_vectors, force, torque, eta, a, *args, **kwargs):
     """U = M_UF F + M_UT T (mobility/mobility.py:384-411)."""
     return wall_force_torque(r_vectors, force, torque, eta, a, with_rotation=False, **kwargs)
@@ -280,3 +334,12 @@ single_wall_mobility_rot_times_force_numba = single_wall_mobility_rot_times_forc
 single_wall_mobility_rot_times_torque_pycuda = single_wall_mobility_rot_times_torque_gb300
 single_wall_mobility_rot_times_torque_numba = single_wall_mobility_rot_times_torque_gb300
 single_wall_mobility_trans_times_force_torque_pycuda = single_wall_mobility_trans_times_force_torque_gb300
+no_wall_mobility_trans_times_force_pycuda = no_wall_mobility_trans_times_force_gb300
+no_wall_mobility_trans_times_force_numba = no_wall_mobility_trans_times_force_gb300
+no_wall_mobility_trans_times_torque_pycuda = no_wall_mobility_trans_times_torque_gb300
+no_wall_mobility_trans_times_torque_numba = no_wall_mobility_trans_times_torque_gb300
+no_wall_mobility_rot_times_force_pycuda = no_wall_mobility_rot_times_force_gb300
+no_wall_mobility_rot_times_force_numba = no_wall_mobility_rot_times_force_gb300
+no_wall_mobility_rot_times_torque_pycuda = no_wall_mobility_rot_times_torque_gb300
+no_wall_mobility_rot_times_torque_numba = no_wall_mobility_rot_times_torque_gb300
+no_wall_mobility_trans_times_force_torque_pycuda = no_wall_mobility_trans_times_force_torque_gb300

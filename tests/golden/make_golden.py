@@ -7,6 +7,7 @@ Python, no fastmath).  The fixtures it writes are small ``.npz`` files that the
 tests load on any machine:
 
   products.npz   the four wall products (mobility/mobility.py *_numba wrappers)
+  nowall.npz     the four free-space products (mobility/mobility.py *_no_wall_*_numba)
                  on seeded blobs: far from the wall, overlapping the wall
                  (damping active), with blobs at exactly r = 2a, and periodic;
                  plus the dense wall mobility (mobility/mobility.py:1018-1116)
@@ -75,6 +76,41 @@ def make_products():
         if L is None and n <= 64:
             out[name + "_dense"] = mb.single_wall_fluid_mobility(r, eta, a)
     np.savez_compressed(os.path.join(HERE, "products.npz"), **out)
+
+
+def make_nowall():
+    """Free-space products of the reference's no-wall numba functions
+    (mobility/mobility.py *_no_wall_*_numba wrappers).  Blobs may sit at any
+    height, below z = 0 included: there is no wall and no regularisation."""
+    mb = ref_shims.load("mobility.mobility")
+    fns = {
+        "uf": mb.no_wall_mobility_trans_times_force_numba,
+        "ut": mb.no_wall_mobility_trans_times_torque_numba,
+        "wf": mb.no_wall_mobility_rot_times_force_numba,
+        "wt": mb.no_wall_mobility_rot_times_torque_numba,
+    }
+    out = {}
+    cases = [
+        ("far", 20, 80, 0.5, 1.0, -3.0, 5.0, 32.0, None),
+        ("touching", 21, 48, 0.3, 1.3, -0.5, 1.5, 3.0, None),
+        ("periodic", 22, 40, 0.5, 1.0, -2.0, 3.0, 8.0, np.array([8.0, 9.0, 7.0])),
+        ("single", 23, 1, 0.5, 1.0, 0.3, 0.4, 1.0, None),
+    ]
+    for name, seed, n, a, eta, zlo, zhi, box, L in cases:
+        rng = np.random.default_rng(seed)
+        r = blobs(rng, n, a, zlo, zhi, box)
+        if name == "touching" and n >= 4:
+            r[1] = r[0] + np.array([2 * a, 0.0, 0.0])
+            r[3] = r[2] + np.array([0.0, 0.0, 2 * a])
+        v = rng.standard_normal((n, 3))
+        kw = {"periodic_length": np.zeros(3) if L is None else L}
+        out[name + "_r"] = r
+        out[name + "_v"] = v
+        out[name + "_params"] = np.array([a, eta])
+        out[name + "_L"] = kw["periodic_length"]
+        for k, fn in fns.items():
+            out[name + "_" + k] = fn(r, v, eta, a, **kw)
+    np.savez_compressed(os.path.join(HERE, "nowall.npz"), **out)
 
 
 def read_vertex(rel):
@@ -231,9 +267,18 @@ def make_lanczos():
 
 
 if __name__ == "__main__":
-    make_products()
-    s42, s12 = make_shells()
-    make_quaternion()
-    make_rigid(s42, s12)
-    make_lanczos()
+    # optional arguments select fixture sets (e.g. "nowall"); default: all
+    want = set(sys.argv[1:])
+    if not want or "products" in want:
+        make_products()
+    if not want or "nowall" in want:
+        make_nowall()
+    if not want or want & {"shells", "rigid"}:
+        s42, s12 = make_shells()
+    if not want or "quaternion" in want:
+        make_quaternion()
+    if not want or "rigid" in want:
+        make_rigid(s42, s12)
+    if not want or "lanczos" in want:
+        make_lanczos()
     print("golden fixtures written to", HERE)

@@ -1,4 +1,6 @@
 """CPU: the oracle against the golden vectors made from the reference's own code."""
+import os
+
 import numpy as np
 import pytest
 
@@ -91,3 +93,14 @@ def test_oracle_point_particle_limit_is_blake():
     B = wall.blake_point_mobility(r, 1.0)
     off = ~np.kron(np.eye(4, dtype=bool), np.ones((3, 3), dtype=bool))
     assert np.abs(M - B)[off].max() <= 1e-7 * np.abs(B[off]).max()
+
+
+@pytest.mark.parametrize("case", ["far", "touching", "periodic", "single"])
+@pytest.mark.parametrize("kind", ["uf", "ut", "wf", "wt"])
+def test_oracle_no_wall_matches_reference_golden(case, kind):
+    """The C restatement of the free-space products against the reference's
+    own no-wall numba functions (tests/golden/nowall.npz)."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "nowall.npz"))
+    a, eta = g[case + "_params"]
+    got = wall.no_wall_product(kind, g[case + "_r"], g[case + "_v"], eta, a, periodic_length=g[case + "_L"])
+    assert rel_err(got, g[case + "_" + kind]) <= 1e-14

@@ -8,6 +8,7 @@ tests load on any machine:
 
   products.npz   the four wall products (mobility/mobility.py *_numba wrappers)
   nowall.npz     the four free-space products (mobility/mobility.py *_no_wall_*_numba)
+  forces.npz     blob-blob and external blob forces (multi_bodies/multi_bodies_functions.py)
                  on seeded blobs: far from the wall, overlapping the wall
                  (damping active), with blobs at exactly r = 2a, and periodic;
                  plus the dense wall mobility (mobility/mobility.py:1018-1116)
@@ -111,6 +112,36 @@ def make_nowall():
         for k, fn in fns.items():
             out[name + "_" + k] = fn(r, v, eta, a, **kw)
     np.savez_compressed(os.path.join(HERE, "nowall.npz"), **out)
+
+
+def make_forces():
+    """Blob forces of the reference's Python implementations
+    (multi_bodies/multi_bodies_functions.py): calc_blob_blob_forces_python
+    (soft repulsion, both branches, periodic minimum image) and
+    blob_external_forces (gravity and wall repulsion, blobs above and below a)."""
+    mbf = ref_shims.load_script("multi_bodies/multi_bodies_functions.py", "multi_bodies_functions")
+    out = {}
+    cases = [
+        # name, seed, n, box, zlo, zhi, eps, b, a, L
+        ("dense", 30, 60, 3.0, 0.0, 2.0, 1.3, 0.2, 0.3, None),
+        ("periodic", 31, 50, 4.0, 0.1, 3.0, 0.7, 0.5, 0.25, np.array([4.0, 4.0, 0.0])),
+        ("far", 32, 30, 40.0, 0.5, 9.0, 2.0, 0.1, 0.4, None),
+    ]
+    for name, seed, n, box, zlo, zhi, eps, b, a, L in cases:
+        rng = np.random.default_rng(seed)
+        r = blobs(rng, n, a, zlo, zhi, box)
+        kw = {"periodic_length": np.zeros(3) if L is None else L, "repulsion_strength": eps, "debye_length": b,
+              "blob_radius": a}
+        out[name + "_r"] = r
+        out[name + "_params"] = np.array([eps, b, a])
+        out[name + "_L"] = kw["periodic_length"]
+        out[name + "_bb"] = mbf.calc_blob_blob_forces_python(r.copy(), **kw)
+        ext = {"blob_mass": 1.7, "blob_radius": a, "g": 0.9, "repulsion_strength_wall": 0.6,
+               "debye_length_wall": 0.15}
+        out[name + "_ext_params"] = np.array([ext["blob_mass"], ext["blob_radius"], ext["g"],
+                                              ext["repulsion_strength_wall"], ext["debye_length_wall"]])
+        out[name + "_ext"] = mbf.blob_external_forces(r.copy(), **ext)
+    np.savez_compressed(os.path.join(HERE, "forces.npz"), **out)
 
 
 def read_vertex(rel):
@@ -273,6 +304,8 @@ if __name__ == "__main__":
         make_products()
     if not want or "nowall" in want:
         make_nowall()
+    if not want or "forces" in want:
+        make_forces()
     if not want or want & {"shells", "rigid"}:
         s42, s12 = make_shells()
     if not want or "quaternion" in want:

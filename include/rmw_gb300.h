@@ -115,14 +115,16 @@ int rmw_nowall_product(int kind, const double *r, const double *v, double *out, 
 /* Blob forces (the mobility problem's right-hand side), device arrays of 3n
  * doubles; accumulate != 0 adds to f instead of overwriting it.
  * rmw_blob_blob_forces: soft repulsion of multi_bodies/forces_pycuda.py:40-118
- * (Python form multi_bodies/multi_bodies_functions.py:297-345), all pairs,
- * minimum periodic image (L_host may be NULL).
+ * (Python form multi_bodies/multi_bodies_functions.py:297-345), all pairs
+ * (cutoff <= 0) or the pairs within `cutoff` (the neighbour-list variant of
+ * multi_bodies/forces_numba.py:228-270 uses 2a + 30 b), minimum periodic
+ * image (L_host may be NULL).
  * rmw_blob_external_forces: gravity and wall repulsion of
  * multi_bodies/multi_bodies_functions.py:153-189.  Body forces and torques
  * follow with rmw_rigid_KT_mult (the reduction of
  * force_torque_calculator_sort_by_bodies, multi_bodies_functions.py:411-445). */
 int rmw_blob_blob_forces(const double *r, double *f, int64_t n, double repulsion_strength, double debye_length,
-                         double blob_radius, const double *L_host, int accumulate, void *stream);
+                         double blob_radius, double cutoff, const double *L_host, int accumulate, void *stream);
 int rmw_blob_external_forces(const double *r, double *f, int64_t n, double blob_mass, double blob_radius, double g,
                              double repulsion_strength_wall, double debye_length_wall, int accumulate, void *stream);
 

@@ -11,7 +11,9 @@
 //   CTA's first target) skips them before any FP64 work.  It is used only
 //   where the CTA's spatial extent bounds the FP32 error below the test's
 //   margin, so no contributing pair is ever skipped; elsewhere the FP64
-//   distance decides.
+//   distance decides.  An optional cutoff restricts the sum to pairs within
+//   it (the reference's neighbour-list variant uses 2a + 30 b,
+//   multi_bodies/forces_numba.py:228-270).
 // * external blob forces (multi_bodies_functions.py:153-189): gravity
 //   -g m e_z and the wall repulsion (e/b) exp(-(h - a)/b) (e/b for h <= a).
 // The body reduction [F_b, T_b] = K^T f is rmw_rigid_KT_mult.
@@ -133,9 +135,10 @@ __global__ void external_force_kernel(const double *__restrict__ r, double *__re
 
 extern "C" {
 
-// f (+)= blob-blob repulsion forces of n blobs (device arrays, 3n doubles).
+// f (+)= blob-blob repulsion forces of n blobs (device arrays, 3n doubles);
+// cutoff <= 0: every pair (exact), else pairs within the cutoff only.
 int rmw_blob_blob_forces(const double *r, double *f, int64_t n, double repulsion_strength, double debye_length,
-                         double blob_radius, const double *L_host, int accumulate, void *stream)
+                         double blob_radius, double cutoff, const double *L_host, int accumulate, void *stream)
 {
     if (n < 0 || n > (int64_t(1) << 28)) return rmw::fail(RMW_ERR_ARG, "number of blobs out of range [0, 2^28]");
     if (n > 0 && (!r || !f)) return rmw::fail(RMW_ERR_ARG, "null array pointer");
@@ -143,9 +146,12 @@ int rmw_blob_blob_forces(const double *r, double *f, int64_t n, double repulsion
         return rmw::fail(RMW_ERR_ARG, "debye length must be positive and the blob radius non-negative");
     if (n == 0) return RMW_OK;
     const double Lx = L_host ? L_host[0] : 0.0, Ly = L_host ? L_host[1] : 0.0, Lz = L_host ? L_host[2] : 0.0;
-    // beyond rc = 2a + 746 b the FP64 exponential is exactly zero: such pairs
-    // contribute nothing; the FP32 screen tests against rc + margin
-    const double rc = 2.0 * blob_radius + 746.0 * debye_length;
+    // beyond 2a + 746 b the FP64 exponential is exactly zero: such pairs
+    // contribute nothing; a positive cutoff truncates earlier (pairs farther
+    // than it are left out, as the reference's neighbour-list variant does);
+    // the FP32 screen tests against rc + margin
+    const double rexact = 2.0 * blob_radius + 746.0 * debye_length;
+    const double rc = (cutoff > 0.0) ? fmin(cutoff, rexact) : rexact;
     const double margin = 1e-3 * rc + 1e-6;
     const int N = (int)n;
     cudaStream_t st = rmw::as_stream(stream);

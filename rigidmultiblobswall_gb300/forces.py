@@ -6,7 +6,8 @@ return shapes:
 
 * calc_blob_blob_forces_pycuda(r_vectors, periodic_length=, repulsion_strength=,
   debye_length=, blob_radius=) -> (N, 3) soft blob-blob repulsion
-  (also under the numba and python implementation names);
+  (also under the numba and python implementation names), and
+  calc_blob_blob_forces_tree_numba (pairs within 2a + 30 b);
 * blob_external_forces(r_vectors, blob_mass=, blob_radius=, g=,
   repulsion_strength_wall=, debye_length_wall=) -> (N, 3) gravity and wall repulsion;
 * force_torque_calculator_sort_by_bodies(system, r_vectors, ...) -> (2 Nb, 3)
@@ -31,12 +32,13 @@ def _device_of(*xs):
     return torch.device("cuda", torch.cuda.current_device()), False
 
 
-def _blob_blob(r, f, L, eps, b, a, accumulate, dev):
+def _blob_blob(r, f, L, eps, b, a, accumulate, dev, cutoff=0.0):
     import torch
     Lh = np.ascontiguousarray(np.zeros(3) if L is None else np.asarray(L, dtype=np.float64).reshape(3))
     with torch.cuda.device(dev):
         _native.call("rmw_blob_blob_forces", r.data_ptr(), f.data_ptr(), r.shape[0], float(eps), float(b), float(a),
-                     Lh.ctypes.data, 1 if accumulate else 0, torch.cuda.current_stream(dev).cuda_stream)
+                     float(cutoff), Lh.ctypes.data, 1 if accumulate else 0,
+                     torch.cuda.current_stream(dev).cuda_stream)
 
 
 def _external(r, f, m, a, g, e, b, accumulate, dev):
@@ -59,6 +61,21 @@ def calc_blob_blob_forces_pycuda(r_vectors, *args, **kwargs):
 
 calc_blob_blob_forces_numba = calc_blob_blob_forces_pycuda
 calc_blob_blob_forces_python = calc_blob_blob_forces_pycuda
+
+
+def calc_blob_blob_forces_tree_numba(r_vectors, *args, **kwargs):
+    """Blob-blob repulsion over the pairs within d_max = 2a + 30 b, the
+    truncation of the reference's neighbour-list version
+    (multi_bodies/forces_numba.py:228-270); no neighbour list is needed on the
+    GPU: the all-pairs kernel screens by distance."""
+    import torch
+    dev, on_device = _device_of(r_vectors)
+    r = torch.as_tensor(r_vectors, dtype=torch.float64, device=dev).reshape(-1, 3).contiguous()
+    f = torch.empty_like(r)
+    a, b = kwargs.get("blob_radius"), kwargs.get("debye_length")
+    _blob_blob(r, f, kwargs.get("periodic_length"), kwargs.get("repulsion_strength"), b, a, False, dev,
+               cutoff=2 * a + 30 * b)
+    return f if on_device else f.cpu().numpy()
 
 
 def blob_external_forces(r_vectors, *args, **kwargs):

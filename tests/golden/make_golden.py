@@ -117,7 +117,8 @@ def make_nowall():
 def make_forces():
     """Blob forces of the reference's Python implementations
     (multi_bodies/multi_bodies_functions.py): calc_blob_blob_forces_python
-    (soft repulsion, both branches, periodic minimum image) and
+    (soft repulsion, both branches, periodic minimum image), its neighbour-list
+    variant calc_blob_blob_forces_tree_numba (multi_bodies/forces_numba.py) and
     blob_external_forces (gravity and wall repulsion, blobs above and below a)."""
     mbf = ref_shims.load_script("multi_bodies/multi_bodies_functions.py", "multi_bodies_functions")
     out = {}
@@ -136,6 +137,9 @@ def make_forces():
         out[name + "_params"] = np.array([eps, b, a])
         out[name + "_L"] = kw["periodic_length"]
         out[name + "_bb"] = mbf.calc_blob_blob_forces_python(r.copy(), **kw)
+        # neighbour-list variant, truncated at 2a + 30 b (multi_bodies/forces_numba.py:228-270)
+        import forces_numba
+        out[name + "_tree"] = forces_numba.calc_blob_blob_forces_tree_numba(r.copy(), **kw)
         ext = {"blob_mass": 1.7, "blob_radius": a, "g": 0.9, "repulsion_strength_wall": 0.6,
                "debye_length_wall": 0.15}
         out[name + "_ext_params"] = np.array([ext["blob_mass"], ext["blob_radius"], ext["g"],

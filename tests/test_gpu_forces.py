@@ -33,6 +33,16 @@ def test_forces_match_reference_golden(cuda_device, case):
     assert rel_err(ext, g[case + "_ext"]) <= 1e-14
 
 
+@pytest.mark.parametrize("case", ["dense", "periodic", "far"])
+def test_cutoff_variant_matches_reference_tree_golden(cuda_device, case):
+    """calc_blob_blob_forces_tree_numba: pairs within 2a + 30 b only."""
+    g = np.load(G)
+    eps, b, a = g[case + "_params"]
+    got = F.calc_blob_blob_forces_tree_numba(g[case + "_r"], periodic_length=g[case + "_L"], repulsion_strength=eps,
+                                             debye_length=b, blob_radius=a)
+    assert rel_err(got, g[case + "_tree"]) <= 1e-12
+
+
 @pytest.mark.parametrize("spread", [False, True])
 @pytest.mark.parametrize("periodic", [False, True])
 def test_blob_blob_matches_oracle_both_screen_paths(cuda_device, spread, periodic):
@@ -59,14 +69,14 @@ def test_accumulate_and_device_path(cuda_device):
     f = torch.ones_like(r)
     st = torch.cuda.current_stream().cuda_stream
     _native.call("rmw_blob_external_forces", r.data_ptr(), f.data_ptr(), 400, 1.0, 0.3, 2.0, 0.5, 0.2, 1, st)
-    _native.call("rmw_blob_blob_forces", r.data_ptr(), f.data_ptr(), 400, 1.0, 0.1, 0.3, None, 1, st)
+    _native.call("rmw_blob_blob_forces", r.data_ptr(), f.data_ptr(), 400, 1.0, 0.1, 0.3, 0.0, None, 1, st)
     rn = r.cpu().numpy()
     ref = 1.0 + of.external_forces(rn, 1.0, 0.3, 2.0, 0.5, 0.2) + of.blob_blob_forces(rn, 1.0, 0.1, 0.3)
     assert rel_err(f.cpu().numpy(), ref) <= 1e-12
     ft = F.calc_blob_blob_forces_pycuda(r, repulsion_strength=1.0, debye_length=0.1, blob_radius=0.3)
     assert ft.is_cuda
     with pytest.raises(_native.RMWError):
-        _native.call("rmw_blob_blob_forces", r.data_ptr(), f.data_ptr(), 400, 1.0, 0.0, 0.3, None, 0, st)
+        _native.call("rmw_blob_blob_forces", r.data_ptr(), f.data_ptr(), 400, 1.0, 0.0, 0.3, 0.0, None, 0, st)
 
 
 def test_body_force_torque_reduction(cuda_device):

@@ -245,6 +245,16 @@ int rmw_wall_lanczos(const double *r, const double *z, double *noise, int64_t n,
                      const double *L_host, double factor, double tol, int max_iter, int mode, void *stream,
                      int *iters_host);
 
+/* Wall (1, default) or free space (0) for every mobility of the handle: blob
+ * products, the preconditioners' dense per-body blocks, solves and Lanczos.
+ * Free space is the reference's *_no_wall implementations (mobility/mobility.py:
+ * 288-482; dense rotne_prager_tensor, :967-1015), as selected by
+ * mobility_blobs_implementation = 'python_no_wall' and
+ * mobility_vector_prod_implementation = 'pycuda_no_wall'
+ * (multi_bodies/multi_bodies.py:207-287).  Invalidates the preconditioners;
+ * batched suspensions and the near-field preconditioner are wall-only. */
+int rmw_rigid_set_wall(void *handle, int wall);
+
 /* Declare that the handle's bodies form independent suspensions: suspension
  * k owns bodies [body_offsets[k], body_offsets[k+1]) and its blobs interact
  * only with each other (segmented pair products).  Enables the batched

@@ -56,7 +56,7 @@ def KT_mult(Ks, offsets, lam):
 class Rigid:
     """One suspension: blob positions r (N,3), body locations (Nb,3), blob offsets."""
 
-    def __init__(self, r, locs, offsets, eta, a):
+    def __init__(self, r, locs, offsets, eta, a, wall_present=True):
         self.r = np.ascontiguousarray(r, dtype=np.float64).reshape(-1, 3)
         self.locs = np.asarray(locs, dtype=np.float64).reshape(-1, 3)
         self.offsets = np.asarray(offsets, dtype=np.int64)
@@ -66,8 +66,11 @@ class Rigid:
         self.size = 3 * self.N + 6 * self.Nb
         self.Ks = K_bodies(self.r, self.locs, self.offsets)
         self._pc = None
+        self.wall_present = wall_present  # False: free space (the *_no_wall implementations)
 
     def mobility(self, v):
+        if not self.wall_present:
+            return wall.no_wall_product("uf", self.r, v, self.eta, self.a)
         return wall.wall_product("uf", self.r, v, self.eta, self.a)
 
     def apply(self, x):
@@ -81,7 +84,8 @@ class Rigid:
         minv, nmat, lfac, linv = [], [], [], []
         for b in range(self.Nb):
             rb = self.r[self.offsets[b]:self.offsets[b + 1]]
-            M = wall.dense_mobility(rb, self.eta, self.a)
+            M = (wall.dense_mobility(rb, self.eta, self.a) if self.wall_present
+                 else wall.no_wall_dense(rb, self.eta, self.a))
             U, lower = scipy.linalg.cho_factor(M)
             U = np.triu(U)
             Uinv = scipy.linalg.solve_triangular(U, np.eye(M.shape[0]))

@@ -92,6 +92,21 @@ def no_wall_product(kind, r_vectors, vector, eta, a, periodic_length=None, rows=
     return out
 
 
+def no_wall_dense(r_vectors, eta, a):
+    """Dense free-space RPY blob mobility (3N, 3N), the reference's
+    rotne_prager_tensor (mobility/mobility.py:967-1015), column by column from
+    the free-space product."""
+    r = np.ascontiguousarray(np.asarray(r_vectors, dtype=np.float64).reshape(-1, 3))
+    n = r.shape[0]
+    M = np.empty((3 * n, 3 * n))
+    e = np.zeros(3 * n)
+    for c in range(3 * n):
+        e[c] = 1.0
+        M[:, c] = no_wall_product("uf", r, e, eta, a)
+        e[c] = 0.0
+    return M
+
+
 def dense_mobility(r_vectors, eta, a):
     """Dense regularised wall mobility (3N, 3N) (mobility/mobility.py:1018-1116)."""
     r = np.ascontiguousarray(np.asarray(r_vectors, dtype=np.float64).reshape(-1, 3))

@@ -573,6 +573,7 @@ int rmw_rigid_set_suspensions(void *sys, int64_t n_suspensions, const int64_t *b
 {
     if (!sys || !body_offsets_host) return rmw::fail(RMW_ERR_ARG, "null argument");
     RigidSystem &S = *(RigidSystem *)sys;
+    if (!S.wall) return rmw::fail(RMW_ERR_ARG, "batched suspensions are available with the wall only");
     if (n_suspensions <= 0 || body_offsets_host[0] != 0 || body_offsets_host[n_suspensions] != S.nb)
         return rmw::fail(RMW_ERR_ARG, "body offsets must run from 0 to the number of bodies");
     std::vector<long long> boff(n_suspensions + 1), blob_off(n_suspensions + 1), sys_off(n_suspensions + 1);

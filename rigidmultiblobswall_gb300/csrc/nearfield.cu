@@ -1265,6 +1265,7 @@ int rmw_rigid_set_nearfield(void *sys, void *net, double exact_cutoff, int64_t *
         return RMW_OK;
     }
     if (!S.pc_ready) return rmw::fail(RMW_ERR_ARG, "build the preconditioner first");
+    if (!S.wall) return rmw::fail(RMW_ERR_ARG, "the near-field preconditioner models bodies above the wall");
     NearfieldNet *N = (NearfieldNet *)net;
     const double hi = N ? std::max(N->cutoff, lo) : lo;
     cudaStream_t st = S.st;

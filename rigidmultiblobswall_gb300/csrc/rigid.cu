@@ -120,6 +120,39 @@ __global__ void body_mobility_kernel(const double *__restrict__ r, const int *__
     }
 }
 
+// Free-space variant (no wall, no regularisation): the blocks of
+// rotne_prager_tensor (mobility/mobility.py:967-1015), self block 4/3 I.
+__global__ void body_mobility_free_kernel(const double *__restrict__ r, const int *__restrict__ boff,
+                                          const long long *__restrict__ moff, double *__restrict__ M, double eta,
+                                          double a)
+{
+    const int b = blockIdx.x;
+    const int o = boff[b], nbl = boff[b + 1] - o, m = 3 * nbl;
+    double *Mb = M + moff[b];
+    const double inva = 1.0 / a;
+    const double nf = 1.0 / (8.0 * kPi * eta * a);
+    for (int pq = threadIdx.x; pq < nbl * nbl; pq += blockDim.x) {
+        const int p = pq / nbl, q = pq % nbl;
+        const int i = o + p, j = o + q;
+        double blk[3][3];
+        if (p == q) {
+            for (int u = 0; u < 3; ++u)
+                for (int w = 0; w < 3; ++w) blk[u][w] = (u == w) ? 4.0 / 3.0 : 0.0;
+        } else {
+            const double dx = (r[3 * i] - r[3 * j]) * inva, dy = (r[3 * i + 1] - r[3 * j + 1]) * inva,
+                         dz = (r[3 * i + 2] - r[3 * j + 2]) * inva;
+            for (int w = 0; w < 3; ++w) {
+                double c[3] = {0.0, 0.0, 0.0};
+                pair_rpy<RMW_UF, double>(dx, dy, dz, w == 0 ? 1.0 : 0.0, w == 1 ? 1.0 : 0.0, w == 2 ? 1.0 : 0.0,
+                                         c[0], c[1], c[2]);
+                blk[0][w] = c[0]; blk[1][w] = c[1]; blk[2][w] = c[2];
+            }
+        }
+        for (int u = 0; u < 3; ++u)
+            for (int w = 0; w < 3; ++w) Mb[(long long)(3 * p + u) * m + 3 * q + w] = nf * blk[u][w];
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Cholesky + inverse of every M_b.  A (m x m, row-major) is the working copy
 // (shared memory or global); on exit minv holds M_b^-1, and lfac / linv (if
@@ -450,7 +483,8 @@ static int build_pc(RigidSystem &S, bool stochastic)
         RMW_CUDA(cudaMalloc(&S.linv, sizeof(double) * tot));
     }
     RMW_CUDA(cudaMemsetAsync(S.dstatus, 0, sizeof(int), st));
-    body_mobility_kernel<<<S.nb, kRigidThreads, 0, st>>>(S.r, S.boff, S.moff, M, S.eta, S.a);
+    if (S.wall) body_mobility_kernel<<<S.nb, kRigidThreads, 0, st>>>(S.r, S.boff, S.moff, M, S.eta, S.a);
+    else body_mobility_free_kernel<<<S.nb, kRigidThreads, 0, st>>>(S.r, S.boff, S.moff, M, S.eta, S.a);
     double *lf = stochastic ? S.lfac : nullptr, *li = stochastic ? S.linv : nullptr;
     if (S.max_m <= kSmemMaxM) {
         const size_t sm = sizeof(double) * ((size_t)S.max_m * S.max_m + S.max_m);
@@ -474,6 +508,7 @@ static int build_pc(RigidSystem &S, bool stochastic)
 
 int rigid_mobility(RigidSystem &S, const double *v, double *y, int mode)
 {
+    if (!S.wall) return nowall_product(RMW_UF, S.r, v, y, S.n, S.eta, S.a, S.L, mode, S.st);
     if (S.batch) return wall_product_batched(*S.batch, RMW_UF, S.r, v, y, S.eta, S.a, mode, S.st);
     return wall_product(RMW_UF, S.r, v, y, S.n, S.eta, S.a, S.L, mode, S.st);
 }
@@ -537,7 +572,7 @@ int rigid_mobility_pc_multi(RigidSystem &S, const double *W, double *Y, int nvec
     if (!S.stoch_ready) return fail(RMW_ERR_ARG, "stochastic preconditioner not built");
     const long long ld = 3LL * S.n;
     if (int rc = tri_mult(S, S.linv, W, tmp, 1, nvec)) return rc;
-    if (mode == RMW_MODE_MIXED) {
+    if (mode == RMW_MODE_MIXED && S.wall) {
         if (int rc = wall_uf_multi(S.r, tmp, ld, Y, ld, nvec, S.n, S.eta, S.a, S.batch, S.st)) return rc;
     } else {
         for (int q = 0; q < nvec; ++q)
@@ -659,6 +694,26 @@ int rmw_rigid_sizes(void *sys, int64_t *n_blobs_host, int64_t *n_bodies_host)
     return RMW_OK;
 }
 
+// Wall (1, the default) or free space (0) for every mobility of the handle:
+// blob products, dense per-body blocks of the preconditioners, solves and
+// Lanczos.  Free space is the reference's *_no_wall implementations
+// (mobility/mobility.py:288-482, rotne_prager_tensor :967-1015).  Invalidates
+// the preconditioners.  Batched suspensions and the near-field augmented
+// preconditioner are wall-only.
+int rmw_rigid_set_wall(void *sys, int wall)
+{
+    if (!sys) return rmw::fail(RMW_ERR_ARG, "null handle");
+    RigidSystem *S = (RigidSystem *)sys;
+    if (!wall && S->batch) return rmw::fail(RMW_ERR_ARG, "batched suspensions are available with the wall only");
+    if (S->wall != (wall != 0)) {
+        S->wall = wall != 0;
+        S->pc_ready = false;
+        S->stoch_ready = false;
+        S->nf_on = false;
+    }
+    return RMW_OK;
+}
+
 int rmw_rigid_set_configuration(void *sys, const double *r_blobs, const double *x_bodies)
 {
     if (!sys || !r_blobs || !x_bodies) return rmw::fail(RMW_ERR_ARG, "null argument");
@@ -767,7 +822,11 @@ int rmw_rigid_body_mobility(void *sys, double *out)
 {
     if (!sys || !out) return rmw::fail(RMW_ERR_ARG, "null argument");
     RigidSystem *S = (RigidSystem *)sys;
-    rmw::body_mobility_kernel<<<S->nb, rmw::kRigidThreads, 0, S->st>>>(S->r, S->boff, S->moff, out, S->eta, S->a);
+    if (S->wall)
+        rmw::body_mobility_kernel<<<S->nb, rmw::kRigidThreads, 0, S->st>>>(S->r, S->boff, S->moff, out, S->eta, S->a);
+    else
+        rmw::body_mobility_free_kernel<<<S->nb, rmw::kRigidThreads, 0, S->st>>>(S->r, S->boff, S->moff, out, S->eta,
+                                                                               S->a);
     RMW_CHECK_LAUNCH("body mobility");
     return RMW_OK;
 }

@@ -56,6 +56,9 @@ int wall_chunks(int kind, int mode, int n);
 size_t wall_scratch_bytes(int n, int mode, int nchunks);
 int validate_product_args(int kind, const void *r, const void *v, const void *out, int64_t n, double eta, double a,
                           int mode);
+// Free-space (no-wall) RPY product (nowall.cu, rmw_nowall_product).
+int nowall_product(int kind, const double *r, const double *v, double *out, int64_t n, double eta, double a,
+                   const double *L, int mode, cudaStream_t st);
 // Full product with the library's per-stream scratch (rmw_wall_product).
 int wall_product(int kind, const double *r, const double *v, double *out, int64_t n, double eta, double a,
                  const double *L, int mode, cudaStream_t st);

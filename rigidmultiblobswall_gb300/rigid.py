@@ -29,9 +29,10 @@ class RigidSystem:
     """One suspension of rigid multiblob bodies on one GPU.
 
     blobs_per_body: sequence of blob counts (body b owns the next n_b blobs).
+    wall: False for free-space (no-wall) mobilities.
     """
 
-    def __init__(self, blobs_per_body, eta, a, periodic_length=None, device="cuda"):
+    def __init__(self, blobs_per_body, eta, a, periodic_length=None, device="cuda", wall=True):
         import torch
         self.device = torch.device(device)
         if self.device.index is None:
@@ -54,6 +55,15 @@ class RigidSystem:
                          self.L.ctypes.data_as(ctypes.c_void_p), self.stream.cuda_stream)
         self._h = h
         self.size = 3 * self.n_blobs + 6 * self.n_bodies
+        self.wall = True
+        if not wall:
+            self.set_wall(False)
+
+    def set_wall(self, wall):
+        """Mobility above the wall (True) or in free space (False, the reference's
+        *_no_wall implementations).  Invalidates the preconditioners."""
+        _native.call("rmw_rigid_set_wall", self._h, 1 if wall else 0)
+        self.wall = bool(wall)
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:

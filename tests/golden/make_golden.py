@@ -111,6 +111,9 @@ def make_nowall():
         out[name + "_L"] = kw["periodic_length"]
         for k, fn in fns.items():
             out[name + "_" + k] = fn(r, v, eta, a, **kw)
+        if L is None:
+            # dense free-space blob mobility of the preconditioner (python_no_wall)
+            out[name + "_dense"] = mb.rotne_prager_tensor(r, eta, a)
     np.savez_compressed(os.path.join(HERE, "nowall.npz"), **out)
 
 

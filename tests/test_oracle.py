@@ -104,3 +104,11 @@ def test_oracle_no_wall_matches_reference_golden(case, kind):
     a, eta = g[case + "_params"]
     got = wall.no_wall_product(kind, g[case + "_r"], g[case + "_v"], eta, a, periodic_length=g[case + "_L"])
     assert rel_err(got, g[case + "_" + kind]) <= 1e-14
+
+
+@pytest.mark.parametrize("case", ["far", "touching"])
+def test_oracle_free_space_dense_matches_rotne_prager_tensor(case):
+    """Dense free-space blob mobility against the reference's rotne_prager_tensor."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "nowall.npz"))
+    a, eta = g[case + "_params"]
+    assert rel_err(wall.no_wall_dense(g[case + "_r"], eta, a), g[case + "_dense"]) <= 1e-14

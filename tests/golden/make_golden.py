@@ -19,6 +19,8 @@ tests load on any machine:
                  block-preconditioned operator of build_block_diagonal_preconditioners_det_stoch
   shells.npz     the reference's 12- and 42-blob shell vertex files (geometry inputs)
   quaternion.npz Quaternion.from_rotation, products and rotation matrices
+  schemes.npz    two time steps of each GMRES-based time integrator of
+                 quaternion_integrator_multi_bodies.py with the normal draws it made
 
 Usage:  python tests/golden/make_golden.py
 """
@@ -304,6 +306,115 @@ def make_lanczos():
     np.savez_compressed(os.path.join(HERE, "lanczos.npz"), **out)
 
 
+SCHEMES = ("deterministic_forward_euler", "deterministic_adams_bashforth", "deterministic_midpoint",
+           "stochastic_EM", "stochastic_first_order_RFD", "stochastic_adams_bashforth", "stochastic_traction_EM",
+           "stochastic_traction_AB", "stochastic_Slip_Trapz", "stochastic_Slip_Mid")
+
+
+def make_schemes(s12):
+    """Two time steps of every GMRES-based scheme of the reference's
+    QuaternionIntegrator (quaternion_integrator/quaternion_integrator_multi_bodies.py)
+    on three 12-blob shells above the wall, wired as multi_bodies/multi_bodies.py:1318-1386
+    does (numba wall product, dense wall blocks for the preconditioners, external
+    and blob-blob forces of multi_bodies_functions.py), tolerance 1e-12 for GMRES
+    and Lanczos.  Every normal draw the schemes make (np.random.normal and the
+    np.random.randn of stochastic_forcing_lanczos) is recorded in order, so the
+    same draws can be fed to the other implementations."""
+    Q = ref_shims.load("quaternion_integrator.quaternion").Quaternion
+    qi = ref_shims.load("quaternion_integrator.quaternion_integrator_multi_bodies")
+    body_mod = ref_shims.load("body.body")
+    mb = ref_shims.load("mobility.mobility")
+    mbs = ref_shims.load_script("multi_bodies/multi_bodies.py", "ref_multi_bodies")
+    mbf = ref_shims.load_script("multi_bodies/multi_bodies_functions.py", "multi_bodies_functions")
+    from scipy.spatial.distance import pdist
+    mbf.calc_blob_blob_forces = mbf.calc_blob_blob_forces_python
+    mbf.calc_body_body_forces_torques = mbf.set_body_body_forces_torques("None")
+    mbs.mobility_vector_prod = mb.single_wall_mobility_trans_times_force_numba
+    R = np.linalg.norm(s12[0])
+    a = 0.5 * pdist(s12).min()
+    eta, kT, dt, nb = 1.0, 0.7, 0.02, 3
+    L = np.zeros(3)
+    fkw = {"g": 1.0, "repulsion_strength_wall": 0.5, "debye_length_wall": 0.1 * a, "repulsion_strength": 0.5,
+           "debye_length": 0.1 * a, "periodic_length": L}
+    rng = np.random.default_rng(50)
+    locs = place_bodies(rng, nb, R, a, 5 * R, 1.6 * R, 2.6 * R)
+    quats = random_quaternions(rng, nb)
+    out = {"ref_cfg": s12, "locs": locs, "quats": quats,
+           "params": np.array([eta, a, kT, dt, 1e-3, 1e-12]),
+           "force_params": np.array([1.0, fkw["g"], fkw["repulsion_strength_wall"], fkw["debye_length_wall"],
+                                     fkw["repulsion_strength"], fkw["debye_length"]])}
+    orig_normal, orig_randn = np.random.normal, np.random.randn
+    try:
+        for si, scheme in enumerate(SCHEMES):
+            bodies = []
+            for k in range(nb):
+                b = body_mod.Body(locs[k].copy(), Q(quats[k].copy()), s12, a)
+                b.mobility_blobs = mb.single_wall_fluid_mobility
+                if k == 0:
+                    b.calc_body_length()
+                else:
+                    b.body_length = bodies[0].body_length
+                bodies.append(b)
+            Nblobs = sum(b.Nblobs for b in bodies)
+            integ = qi.QuaternionIntegrator(bodies, Nblobs, scheme, tolerance=1e-12, domain="single_wall")
+            integ.build_block_diagonal_preconditioner = mbs.build_block_diagonal_preconditioner
+            integ.first_guess = np.zeros(3 * Nblobs + 6 * nb)
+            integ.calc_slip = None
+            integ.get_blobs_r_vectors = mbs.get_blobs_r_vectors
+            integ.mobility_blobs = mb.single_wall_fluid_mobility
+            integ.mobility_vector_prod = mb.single_wall_mobility_trans_times_force_numba
+            integ.force_torque_calculator = partial(mbf.force_torque_calculator_sort_by_bodies, **fkw)
+            integ.calc_K_matrix_bodies = mbs.calc_K_matrix_bodies
+            integ.calc_K_matrix = mbs.calc_K_matrix
+            integ.linear_operator = mbs.linear_operator_rigid
+            integ.build_block_diagonal_preconditioners_det_stoch = mbs.build_block_diagonal_preconditioners_det_stoch
+            integ.eta, integ.a, integ.kT = eta, a, kT
+            integ.K_matrix_T_vector_prod = mbs.K_matrix_T_vector_prod
+            integ.K_matrix_vector_prod = mbs.K_matrix_vector_prod
+            integ.preprocess = mbf.preprocess
+            integ.postprocess = mbf.postprocess
+            integ.periodic_length = L
+            integ.update_PC = 1
+            integ.print_residual = False
+            integ.rf_delta = 1e-3
+            integ.constraints = []
+            integ.articulated = []
+            for f in (mbs.build_block_diagonal_preconditioner, mbs.build_block_diagonal_preconditioners_det_stoch):
+                f.mobility_bodies = []
+                f.initialized = []
+            rs = np.random.RandomState(60 + si)
+            draws = []
+
+            def normal(loc=0.0, scale=1.0, size=None):
+                assert loc == 0.0 and scale == 1.0
+                x = rs.normal(loc, scale, size)
+                draws.append(np.array(x, dtype=np.float64).ravel().copy())
+                return x
+
+            def randn(*shape):
+                x = rs.randn(*shape)
+                draws.append(np.array(x, dtype=np.float64).ravel().copy())
+                return x
+
+            np.random.normal, np.random.randn = normal, randn
+            p = scheme + "_"
+            for step in range(2):
+                integ.advance_time_step(dt, step=step)
+                out[p + "locs%d" % step] = np.array([b.location for b in bodies])
+                out[p + "quats%d" % step] = np.array([b.orientation.entries for b in bodies])
+            np.random.normal, np.random.randn = orig_normal, orig_randn
+            out[p + "draws"] = np.concatenate(draws) if draws else np.zeros(0)
+            out[p + "draw_sizes"] = np.array([d.size for d in draws])
+            out[p + "counts"] = np.array([integ.invalid_configuration_count, integ.det_iterations_count,
+                                          integ.stoch_iterations_count])
+            out["body_length"] = np.array([bodies[0].body_length])
+            print(scheme, "draws", [d.size for d in draws], "counts", out[p + "counts"],
+                  "displacement", np.linalg.norm(out[p + "locs1"] - locs, axis=1).max())
+    finally:
+        np.random.normal, np.random.randn = orig_normal, orig_randn
+    np.savez_compressed(os.path.join(HERE, "schemes.npz"), **out)
+
+
 if __name__ == "__main__":
     # optional arguments select fixture sets (e.g. "nowall"); default: all
     want = set(sys.argv[1:])
@@ -313,7 +424,7 @@ if __name__ == "__main__":
         make_nowall()
     if not want or "forces" in want:
         make_forces()
-    if not want or want & {"shells", "rigid"}:
+    if not want or want & {"shells", "rigid", "schemes"}:
         s42, s12 = make_shells()
     if not want or "quaternion" in want:
         make_quaternion()
@@ -321,4 +432,6 @@ if __name__ == "__main__":
         make_rigid(s42, s12)
     if not want or "lanczos" in want:
         make_lanczos()
+    if not want or "schemes" in want:
+        make_schemes(s12)
     print("golden fixtures written to", HERE)

@@ -381,6 +381,25 @@ def solver_metrics(dev, reps=2):
         "block_diag_fp64": out["bd_step_shells12x1024_fp64"]["ms"],
         "block_diag_mixed": out["bd_step_shells12x1024_mixed"]["ms"],
         "learned_mixed": out["bd_step_shells12x1024_mixed_nearfield"]["ms"]}
+    # every time integrator, one step of 1024 shells x 12 blobs (mixed precision,
+    # GMRES and Lanczos tolerance 1e-8, force (0,0,-1) per body, kT = 1, dt = 1e-3)
+    FT3t = torch.as_tensor(FT3, device=dev).reshape(-1, 3)
+    sch = {}
+    for scheme in integrator.QuaternionIntegrator.SCHEMES:
+        qi = integrator.QuaternionIntegrator(sys3, scheme, s3.locations, s3.quaternions,
+                                             np.tile(s3.shell, (s3.n_bodies, 1)), tolerance=1e-8, kT=1.0,
+                                             mode="mixed", seed=5)
+        qi.force_torque_calculator = lambda s, r: FT3t
+        qi.advance_time_step(1e-3, step=0)  # warm-up (and the second step of the two-step schemes)
+        d0, s0 = qi.det_iterations_count, qi.stoch_iterations_count
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        qi.advance_time_step(1e-3, step=1)
+        torch.cuda.synchronize()
+        sch[scheme] = {"ms": (time.perf_counter() - t0) * 1e3, "gmres_iterations": qi.det_iterations_count - d0,
+                       "lanczos_iterations": qi.stoch_iterations_count - s0}
+        qi.close()
+    out["schemes_shells12x1024_mixed_step"] = sch
     return out
 
 

@@ -21,6 +21,8 @@ tests load on any machine:
   quaternion.npz Quaternion.from_rotation, products and rotation matrices
   schemes.npz    two time steps of each GMRES-based time integrator of
                  quaternion_integrator_multi_bodies.py with the normal draws it made
+  clones.npz     read_clones_file / read_vertex_file outputs and the trajectory
+                 text of multi_bodies/multi_bodies.py:1428-1457
 
 Usage:  python tests/golden/make_golden.py
 """
@@ -415,6 +417,60 @@ def make_schemes(s12):
     np.savez_compressed(os.path.join(HERE, "schemes.npz"), **out)
 
 
+def make_clones():
+    """Structure-file reading and trajectory text of the reference:
+    read_clones_file / read_vertex_file (read_input/) on two of the reference's
+    structure files and on a synthetic clones text (comments, blank lines,
+    unnormalised quaternions, lines past the last body), and the body lines
+    that multi_bodies/multi_bodies.py:1428-1457 writes ('%s' of numpy float64
+    locations and Quaternion.entries)."""
+    import tempfile
+    Q = ref_shims.load("quaternion_integrator.quaternion").Quaternion
+    rc = ref_shims.load("read_input.read_clones_file")
+    rv = ref_shims.load("read_input.read_vertex_file")
+    out = {}
+    for key, rel in (("shell12", "multi_bodies/Structures/shell_N_12_Rg_1"),
+                     ("boomerang15", "multi_bodies/Structures/boomerang_N_15")):
+        with open(os.path.join(REF, rel + ".clones")) as f:
+            out[key + "_clones_text"] = np.array(f.read())
+        n, loc, ori = rc.read_clones_file(os.path.join(REF, rel + ".clones"))
+        out[key + "_n"] = np.array([n])
+        out[key + "_locations"] = np.asarray(loc, dtype=np.float64).reshape(-1, 3)
+        out[key + "_orientations"] = np.array([q.entries for q in ori]).reshape(-1, 4)
+        with open(os.path.join(REF, rel + ".vertex")) as f:
+            out[key + "_vertex_text"] = np.array(f.read())
+        out[key + "_vertex"] = rv.read_vertex_file(os.path.join(REF, rel + ".vertex"))
+    synthetic = ("# header comment\n\n   3   # three bodies\n"
+                 "0.5 1.5 2.5 2.0 0.0 0.0 0.0\n"
+                 "\n# a comment line between bodies\n"
+                 "-1e-3 7 1.25e2   0.3 -0.4 0.5 0.6  # trailing comment\n"
+                 "4 5 6 1 1 1 1 extra tokens\n"
+                 "9 9 9 1 0 0 0\n")
+    out["synthetic_clones_text"] = np.array(synthetic)
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "s.clones")
+        with open(p, "w") as f:
+            f.write(synthetic)
+        n, loc, ori = rc.read_clones_file(p)
+    out["synthetic_n"] = np.array([n])
+    out["synthetic_locations"] = np.asarray(loc, dtype=np.float64)
+    out["synthetic_orientations"] = np.array([q.entries for q in ori])
+    rng = np.random.default_rng(70)
+    locs = rng.standard_normal((5, 3)) * np.array([1.0, 1e-7, 3e5])
+    locs[0] = [0.1, -0.0, 1e17]
+    quats = random_quaternions(rng, 5)
+    text = str(locs.shape[0]) + "\n"
+    for k in range(locs.shape[0]):
+        location = locs[k]
+        orientation = Q(quats[k]).entries
+        text += "%s %s %s %s %s %s %s\n" % (location[0], location[1], location[2], orientation[0], orientation[1],
+                                            orientation[2], orientation[3])
+    out["write_locations"] = locs
+    out["write_orientations"] = quats
+    out["write_text"] = np.array(text)
+    np.savez_compressed(os.path.join(HERE, "clones.npz"), **out)
+
+
 if __name__ == "__main__":
     # optional arguments select fixture sets (e.g. "nowall"); default: all
     want = set(sys.argv[1:])
@@ -434,4 +490,6 @@ if __name__ == "__main__":
         make_lanczos()
     if not want or "schemes" in want:
         make_schemes(s12)
+    if not want or "clones" in want:
+        make_clones()
     print("golden fixtures written to", HERE)

@@ -124,3 +124,37 @@ def test_zero_temperature_traction_is_forward_euler(cuda_device):
     b.advance_time_step(dt)
     np.testing.assert_allclose(a.x.cpu().numpy(), b.x.cpu().numpy(), rtol=0, atol=1e-12)
     np.testing.assert_allclose(a.q.cpu().numpy(), b.q.cpu().numpy(), rtol=0, atol=1e-12)
+
+
+def test_run_saves_and_resumes_on_device(cuda_device, tmp_path):
+    """clones.run with the device integrator: 4 steps of stochastic_traction_EM
+    saved every 2 steps to a .config trajectory, against 2 steps, a resume from
+    the saved frame at initial_step 2 and 2 more steps with the same draws."""
+    import os
+    from rigidmultiblobswall_gb300 import clones
+    g = golden("schemes.npz")
+    scheme = "stochastic_traction_EM"
+    nb = g["locs"].shape[0]
+    n3 = 3 * g["ref_cfg"].shape[0] * nb
+    sizes = [6 * nb, n3] * 4
+    vals = np.random.default_rng(11).standard_normal(sum(sizes))
+    it, dt = gpu_integrator(g, scheme, DeviceDraws(vals, sizes))
+    full = os.path.join(str(tmp_path), "full")
+    clones.run(it, dt, 4, n_save=2, output_name=full, save_clones="one_file")
+    frames = clones.read_config_file(full + ".body.config")
+    assert len(frames) == 3
+    np.testing.assert_array_equal(frames[0][0], g["locs"])
+    np.testing.assert_array_equal(frames[2][0], it.x.cpu().numpy())
+    np.testing.assert_array_equal(frames[2][1], it.q.cpu().numpy())
+    half = sum(sizes[:4])
+    a, _ = gpu_integrator(g, scheme, DeviceDraws(vals[:half], sizes[:4]))
+    clones.run(a, dt, 2, n_save=2, output_name=os.path.join(str(tmp_path), "p1"), save_clones="one_file")
+    loc, ori = clones.resume_state(os.path.join(str(tmp_path), "p1.body.config"))
+    b, _ = gpu_integrator(g, scheme, DeviceDraws(vals[half:], sizes[4:]))
+    b.x.copy_(__import__("torch").as_tensor(loc))
+    b.q.copy_(__import__("torch").as_tensor(ori))
+    clones.run(b, dt, 4, n_save=2, output_name=os.path.join(str(tmp_path), "p2"), initial_step=2,
+               save_clones="one_file")
+    np.testing.assert_allclose(b.x.cpu().numpy(), it.x.cpu().numpy(), rtol=0, atol=1e-12)
+    np.testing.assert_allclose(b.q.cpu().numpy(), it.q.cpu().numpy(), rtol=0, atol=1e-12)
+    assert "invalid_configuration_count    = 0" in open(full + ".info").read()

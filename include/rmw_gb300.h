@@ -112,6 +112,37 @@ int rmw_wall_product_host(int kind, const double *r_host, const double *v_host, 
 int rmw_nowall_product(int kind, const double *r, const double *v, double *out, int64_t n, double eta, double a,
                        const double *L_host, int mode, void *stream);
 
+/* Source-target translational products with per-blob radii: velocities
+ * out (3 n_target) of target blobs of radii radius_target from forces
+ * (3 n_source) on source blobs of radii radius_source, with the
+ * unequal-sphere RPY pair block.  geometry:
+ *   RMW_GEOM_NO_WALL       no_wall_mobility_trans_times_force_source_target_numba
+ *                          (mobility/mobility.py:593-616, kernel
+ *                          mobility/mobility_numba.py:1480-1572)
+ *   RMW_GEOM_WALL          single_wall_mobility_trans_times_force_source_target_{numba,pycuda}
+ *                          (mobility.py:494-590: heights shifted to max(z, radius),
+ *                          forces and velocities damped by z / radius, image
+ *                          system of mobility_numba.py:1573-1653)
+ *   RMW_GEOM_FREE_SURFACE  free_surface_mobility_trans_times_force_source_target_numba
+ *                          (mobility.py:1409-1429, mobility_numba.py:1941-2093)
+ * Every radius must be positive.  Periodic images (L_host, may be NULL) and
+ * precision modes as rmw_wall_product; device arrays; asynchronous. */
+#define RMW_GEOM_NO_WALL 0
+#define RMW_GEOM_WALL 1
+#define RMW_GEOM_FREE_SURFACE 2
+int rmw_source_target_product(int geometry, const double *source, const double *target, const double *force,
+                              const double *radius_source, const double *radius_target, int64_t n_source,
+                              int64_t n_target, double eta, const double *L_host, int mode, double *out,
+                              void *stream);
+
+/* Free-surface product out = M f of n blobs of radius a (the mirror image
+ * with diag(1, 1, -1) instead of the wall's image system):
+ * free_surface_mobility_trans_times_force_{numba,pycuda} (mobility/mobility.py:
+ * 533-548, 1390-1406, kernel mobility/mobility_numba.py:1770-1938).  Periodic
+ * images and modes as rmw_wall_product; device arrays; asynchronous. */
+int rmw_free_surface_product(const double *r, const double *force, double *out, int64_t n, double eta, double a,
+                             const double *L_host, int mode, void *stream);
+
 /* Blob forces (the mobility problem's right-hand side), device arrays of 3n
  * doubles; accumulate != 0 adds to f instead of overwriting it.
  * rmw_blob_blob_forces: soft repulsion of multi_bodies/forces_pycuda.py:40-118

@@ -343,3 +343,129 @@ no_wall_mobility_rot_times_force_numba = no_wall_mobility_rot_times_force_gb300
 no_wall_mobility_rot_times_torque_pycuda = no_wall_mobility_rot_times_torque_gb300
 no_wall_mobility_rot_times_torque_numba = no_wall_mobility_rot_times_torque_gb300
 no_wall_mobility_trans_times_force_torque_pycuda = no_wall_mobility_trans_times_force_torque_gb300
+
+
+# -- per-blob radii, sources -> targets; free surface --------------------------
+_GEOMETRIES = {"no_wall": 0, "wall": 1, "free_surface": 2}
+
+
+def _device_for(*xs):
+    import torch
+    on_device = any(_is_torch(x) for x in xs)
+    for x in xs:
+        if _is_torch(x) and x.is_cuda:
+            return x.device, True
+    if on_device:
+        raise ValueError("torch inputs must be CUDA tensors")
+    return torch.device("cuda", torch.cuda.current_device()), False
+
+
+def source_target_product(geometry, source, target, force, radius_source, radius_target, eta, **kwargs):
+    """Velocities (3 Nt,) of targets of radii radius_target from forces on
+    sources of radii radius_source; geometry 'no_wall', 'wall' (shifted heights
+    and damping on both sides) or 'free_surface'.  Keywords periodic_length and
+    mode as the other products; numpy in -> numpy out, CUDA tensors stay on the
+    device."""
+    import torch
+    L = _periodic(kwargs)
+    mode = _mode(kwargs)
+    dev, on_device = _device_for(source, target, force, radius_source, radius_target)
+    t = lambda x: torch.as_tensor(x, dtype=torch.float64, device=dev)  # noqa: E731
+    src = t(source).reshape(-1, 3).contiguous()
+    trg = t(target).reshape(-1, 3).contiguous()
+    ns, nt = src.shape[0], trg.shape[0]
+    f = t(force).reshape(-1).contiguous()
+
+    def radii(x, n):  # one radius per blob, or one for all
+        v = t(x).reshape(-1)
+        return (v.expand(n) if v.numel() == 1 else v).contiguous()
+
+    rs, rt = radii(radius_source, ns), radii(radius_target, nt)
+    if f.numel() != 3 * ns or rs.numel() != ns or rt.numel() != nt:
+        raise ValueError("force must have 3 Ns entries and one radius per blob")
+    out = torch.empty(3 * nt, dtype=torch.float64, device=dev)
+    with torch.cuda.device(dev):
+        _native.call("rmw_source_target_product", _GEOMETRIES[geometry], src.data_ptr(), trg.data_ptr(),
+                     f.data_ptr(), rs.data_ptr(), rt.data_ptr(), ns, nt, float(eta),
+                     L.ctypes.data_as(ctypes.c_void_p), mode, out.data_ptr(),
+                     torch.cuda.current_stream(dev).cuda_stream)
+    return out if on_device else out.cpu().numpy()
+
+
+def single_wall_mobility_trans_times_force_source_target_gb300(source, target, force, radius_source, radius_target,
+                                                               eta, *args, **kwargs):
+    """Wall source-target product (mobility/mobility.py:494-530, 551-590)."""
+    return source_target_product("wall", source, target, force, radius_source, radius_target, eta, **kwargs)
+
+
+def no_wall_mobility_trans_times_force_source_target_gb300(source, target, force, radius_source, radius_target,
+                                                           eta, *args, **kwargs):
+    """Free-space source-target product (mobility/mobility.py:593-616)."""
+    return source_target_product("no_wall", source, target, force, radius_source, radius_target, eta, **kwargs)
+
+
+def free_surface_mobility_trans_times_force_source_target_gb300(source, target, force, radius_source,
+                                                                radius_target, eta, *args, **kwargs):
+    """Free-surface source-target product (mobility/mobility.py:1409-1429)."""
+    return source_target_product("free_surface", source, target, force, radius_source, radius_target, eta,
+                                 **kwargs)
+
+
+def mobility_vector_product_source_target_one_wall(source, target, force, radius_source, radius_target, eta,
+                                                   *args, **kwargs):
+    """The Python form of the wall source-target product (mobility/mobility.py:830-902);
+    returns (Nt, 3)."""
+    out = single_wall_mobility_trans_times_force_source_target_gb300(source, target, force, radius_source,
+                                                                     radius_target, eta, **kwargs)
+    return out.reshape(-1, 3)
+
+
+def mobility_vector_product_source_target_unbounded(source, target, force, radius_source, radius_target, eta,
+                                                    *args, **kwargs):
+    """The Python form of the free-space source-target product (mobility/mobility.py:905-946);
+    returns (Nt, 3)."""
+    out = no_wall_mobility_trans_times_force_source_target_gb300(source, target, force, radius_source,
+                                                                 radius_target, eta, **kwargs)
+    return out.reshape(-1, 3)
+
+
+def free_surface_mobility_trans_times_force_gb300(r_vectors, force, eta, a, *args, **kwargs):
+    """Free-surface product of blobs of radius a (mobility/mobility.py:533-548, 1390-1406)."""
+    import torch
+    L = _periodic(kwargs)
+    mode = _mode(kwargs)
+    dev, on_device = _device_for(r_vectors, force)
+    r = torch.as_tensor(r_vectors, dtype=torch.float64, device=dev).reshape(-1, 3).contiguous()
+    n = r.shape[0]
+    f = torch.as_tensor(force, dtype=torch.float64, device=dev).reshape(-1).contiguous()
+    if f.numel() != 3 * n:
+        raise ValueError("force must have 3N entries")
+    out = torch.empty(3 * n, dtype=torch.float64, device=dev)
+    with torch.cuda.device(dev):
+        _native.call("rmw_free_surface_product", r.data_ptr(), f.data_ptr(), out.data_ptr(), n, float(eta),
+                     float(a), L.ctypes.data_as(ctypes.c_void_p), mode, torch.cuda.current_stream(dev).cuda_stream)
+    return out if on_device else out.cpu().numpy()
+
+
+def shift_heights_different_radius(r_vectors, blob_radius, *args, **kwargs):
+    """Heights raised to each blob's radius (mobility/mobility.py:87-99)."""
+    r = np.array(r_vectors, dtype=np.float64).reshape(-1, 3)
+    rad = np.asarray(blob_radius, dtype=np.float64).reshape(-1)
+    r[:, 2] = np.where(r[:, 2] > rad, r[:, 2], rad)
+    return r
+
+
+def damping_matrix_B_different_radius(r_vectors, blob_radius, *args, **kwargs):
+    """(diagonal B with z/radius below the radius, any overlap) (mobility/mobility.py:102-119)."""
+    r = np.asarray(r_vectors, dtype=np.float64).reshape(-1, 3)
+    rad = np.asarray(blob_radius, dtype=np.float64).reshape(-1)
+    d = np.where(r[:, 2] < rad, r[:, 2] / rad, 1.0)
+    return scipy.sparse.dia_matrix((np.repeat(d, 3), 0), shape=(3 * d.size, 3 * d.size)), bool((d != 1.0).any())
+
+
+single_wall_mobility_trans_times_force_source_target_pycuda = single_wall_mobility_trans_times_force_source_target_gb300
+single_wall_mobility_trans_times_force_source_target_numba = single_wall_mobility_trans_times_force_source_target_gb300
+no_wall_mobility_trans_times_force_source_target_numba = no_wall_mobility_trans_times_force_source_target_gb300
+free_surface_mobility_trans_times_force_source_target_numba = free_surface_mobility_trans_times_force_source_target_gb300
+free_surface_mobility_trans_times_force_pycuda = free_surface_mobility_trans_times_force_gb300
+free_surface_mobility_trans_times_force_numba = free_surface_mobility_trans_times_force_gb300

@@ -21,6 +21,8 @@ tests load on any machine:
   quaternion.npz Quaternion.from_rotation, products and rotation matrices
   schemes.npz    two time steps of each GMRES-based time integrator of
                  quaternion_integrator_multi_bodies.py with the normal draws it made
+  source_target.npz  products with per-blob radii from sources to targets (wall, free
+                 space, free surface) and the single-radius free-surface product
   clones.npz     read_clones_file / read_vertex_file outputs and the trajectory
                  text of multi_bodies/multi_bodies.py:1428-1457
 
@@ -417,6 +419,63 @@ def make_schemes(s12):
     np.savez_compressed(os.path.join(HERE, "schemes.npz"), **out)
 
 
+def make_source_target():
+    """Source-target products with per-blob radii (mobility/mobility.py:551-616, 1409-1429 over
+    mobility/mobility_numba.py:1480-1660, 1941-2093): wall (shifted heights and damping of
+    both sides), free space and free surface; and the single-radius free-surface product
+    (mobility.py:1390-1406, mobility_numba.py:1770-1938).  Cases: far pairs; close pairs
+    (r < a + b, one blob inside another, a target on a source, blobs below their radius);
+    pseudo-periodic in x and y."""
+    mb = ref_shims.load("mobility.mobility")
+    out = {}
+    cases = [
+        # name, seed, ns, nt, box, zlo, zhi, rlo, rhi, L
+        ("far", 80, 40, 30, 10.0, 0.7, 4.0, 0.2, 0.6, None),
+        ("close", 81, 36, 28, 1.6, 0.05, 1.5, 0.1, 0.7, None),
+        ("periodic", 82, 30, 24, 5.0, 0.3, 2.5, 0.2, 0.5, np.array([5.0, 6.0, 0.0])),
+    ]
+    for name, seed, ns, nt, box, zlo, zhi, rlo, rhi, L in cases:
+        rng = np.random.default_rng(seed)
+        src = blobs(rng, ns, 0.0, zlo, zhi, box)
+        trg = blobs(rng, nt, 0.0, zlo, zhi, box)
+        rs = rng.uniform(rlo, rhi, ns)
+        rt = rng.uniform(rlo, rhi, nt)
+        if name == "close":
+            trg[0] = src[0]                       # a target on a source (r = 0)
+            trg[1] = src[1] + np.array([0.05, 0.0, 0.0])
+            rt[1], rs[1] = 0.6, 0.2               # r < |b - a|: one blob inside the other
+            trg[2] = src[2] + np.array([0.0, 0.0, rs[2] + rt[2]])   # r = a + b exactly
+        f = rng.standard_normal((ns, 3))
+        kw = {"periodic_length": np.zeros(3) if L is None else L}
+        eta = 0.9
+        out[name + "_source"], out[name + "_target"] = src, trg
+        out[name + "_rs"], out[name + "_rt"], out[name + "_f"] = rs, rt, f
+        out[name + "_L"], out[name + "_eta"] = kw["periodic_length"], np.array([eta])
+        out[name + "_wall"] = mb.single_wall_mobility_trans_times_force_source_target_numba(
+            src, trg, f, rs, rt, eta, **kw)
+        out[name + "_nowall"] = mb.no_wall_mobility_trans_times_force_source_target_numba(
+            src, trg, f, rs, rt, eta, **kw)
+        out[name + "_free_surface"] = mb.free_surface_mobility_trans_times_force_source_target_numba(
+            src, trg, f, rs, rt, eta, **kw)
+        if L is None:
+            # the Python forms (no periodic images), mobility/mobility.py:830-946
+            out[name + "_one_wall_py"] = np.asarray(mb.mobility_vector_product_source_target_one_wall(
+                src, trg, f, rs, rt, eta)).reshape(-1)
+            out[name + "_unbounded_py"] = np.asarray(mb.mobility_vector_product_source_target_unbounded(
+                src, trg, f, rs, rt, eta)).reshape(-1)
+    for name, seed, n, a, box, zlo, zhi, L in (("fs", 83, 50, 0.4, 4.0, 0.1, 3.0, None),
+                                             ("fs_periodic", 84, 40, 0.5, 4.0, 0.3, 3.0,
+                                              np.array([4.0, 5.0, 0.0]))):
+        rng = np.random.default_rng(seed)
+        r = blobs(rng, n, a, zlo, zhi, box)
+        f = rng.standard_normal((n, 3))
+        kw = {"periodic_length": np.zeros(3) if L is None else L}
+        out[name + "_r"], out[name + "_f"], out[name + "_params"] = r, f, np.array([a, 1.1])
+        out[name + "_L"] = kw["periodic_length"]
+        out[name + "_u"] = mb.free_surface_mobility_trans_times_force_numba(r, f, 1.1, a, **kw)
+    np.savez_compressed(os.path.join(HERE, "source_target.npz"), **out)
+
+
 def make_clones():
     """Structure-file reading and trajectory text of the reference:
     read_clones_file / read_vertex_file (read_input/) on two of the reference's
@@ -492,4 +551,6 @@ if __name__ == "__main__":
         make_schemes(s12)
     if not want or "clones" in want:
         make_clones()
+    if not want or "source_target" in want:
+        make_source_target()
     print("golden fixtures written to", HERE)

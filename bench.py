@@ -654,6 +654,37 @@ def main():
             res["gpairs_fused"] = n * n / (res["fused_ms"] * 1e-3) / 1e9
             products["force_torque_6n_%s" % mode] = {k: round(v, 6) for k, v in res.items()}
 
+    # source-target products with per-blob radii (the same blobs as sources and
+    # targets, radii a (1 +- 20%)), and the single-radius free-surface product
+    if not args.no_extras:
+        rr = torch.tensor(a * np.random.default_rng(8).uniform(0.8, 1.2, n), device=dev)
+        for geom in ("wall", "no_wall", "free_surface"):
+            for mode in ("fp64", "df64", "mixed"):
+                reps = 3 if mode == "fp64" else 10
+                fn = lambda: mb.source_target_product(geom, rt, rt, ft, rr, rr, eta, mode=mode)  # noqa: E731
+                fn()
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(reps):
+                    fn()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                products["source_target_%s_%s" % (geom, mode)] = {"ms": round(ms, 6),
+                                                                   "gpairs": round(n * n / (ms * 1e-3) / 1e9, 3)}
+        for mode in ("fp64", "df64", "mixed"):
+            fn = lambda: mb.free_surface_mobility_trans_times_force_gb300(rt, ft, eta, a, mode=mode)  # noqa: E731
+            fn()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(5):
+                fn()
+            torch.cuda.synchronize()
+            ms = (time.perf_counter() - t0) * 1e3 / 5
+            products["free_surface_%s" % mode] = {"ms": round(ms, 6), "gpairs": round(n * n / (ms * 1e-3) / 1e9, 3)}
+
     solver = {} if args.no_extras else solver_metrics(dev)
     if not args.no_extras:
         solver["batched_64_suspensions"] = batched_metrics(dev)

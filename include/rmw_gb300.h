@@ -143,6 +143,19 @@ int rmw_source_target_product(int geometry, const double *source, const double *
 int rmw_free_surface_product(const double *r, const double *force, double *out, int64_t n, double eta, double a,
                              const double *L_host, int mode, void *stream);
 
+/* Rollers driven at a prescribed angular velocity: the torques solve
+ * M_WT torque = omega - M_WF force (unpreconditioned restarted GMRES from
+ * zero to the relative tolerance tol), then velocity = M_UF force +
+ * M_UT torque - QuaternionIntegratorRollers.compute_deterministic_velocity_and_torque
+ * (quaternion_integrator/quaternion_integrator_rollers.py:905-983).  wall = 1
+ * single-wall products, 0 free space; mode applies to every product.  Device
+ * arrays of 3n doubles; synchronous; RMW_ERR_NOT_CONVERGED (results still
+ * written) when maxiter is reached. */
+int rmw_rollers_velocity_and_torque(const double *r, const double *force, const double *omega, double *velocity,
+                                    double *torque, int64_t n, double eta, double a, const double *L_host, int wall,
+                                    double tol, int restart, int maxiter, int mode, void *stream, int *iters_host,
+                                    double *relres_host);
+
 /* Blob forces (the mobility problem's right-hand side), device arrays of 3n
  * doubles; accumulate != 0 adds to f instead of overwriting it.
  * rmw_blob_blob_forces: soft repulsion of multi_bodies/forces_pycuda.py:40-118

@@ -762,3 +762,69 @@ int rmw_wall_lanczos(const double *r, const double *z, double *noise, int64_t n,
 }
 
 }  // extern "C"
+
+namespace rmw {
+int wall_force_torque(const double *r, const double *F, const double *T, double *U, double *W, int64_t n,
+                      double eta, double a, const double *L, int mode, cudaStream_t st);
+}
+
+extern "C" {
+
+// Rollers with a prescribed angular velocity
+// (quaternion_integrator/quaternion_integrator_rollers.py:905-983): the torques
+// solve M_WT torque = omega - M_WF force by unpreconditioned GMRES from zero
+// (relative tolerance, restart), then velocity = M_UF force + M_UT torque.
+// wall = 1: single-wall products; 0: free space.  Device arrays of 3n doubles.
+int rmw_rollers_velocity_and_torque(const double *r, const double *force, const double *omega, double *velocity,
+                                    double *torque, int64_t n, double eta, double a, const double *L_host, int wall,
+                                    double tol, int restart, int maxiter, int mode, void *stream, int *iters_host,
+                                    double *relres_host)
+{
+    if (!r || !force || !omega || !velocity || !torque) return rmw::fail(RMW_ERR_ARG, "null argument");
+    if (n <= 0 || n > (int64_t(1) << 28)) return rmw::fail(RMW_ERR_ARG, "number of rollers out of range [1, 2^28]");
+    if (!(tol > 0) || maxiter < 1) return rmw::fail(RMW_ERR_ARG, "tolerance and maxiter must be positive");
+    if (!(eta > 0) || !(a > 0)) return rmw::fail(RMW_ERR_ARG, "viscosity and radius must be positive");
+    if (mode != RMW_MODE_FP64 && mode != RMW_MODE_MIXED && mode != RMW_MODE_DF64)
+        return rmw::fail(RMW_ERR_ARG, "unknown precision mode");
+    cudaStream_t st = rmw::as_stream(stream);
+    const long long m = 3 * (long long)n;
+    auto product = [&](int kind, const double *x, double *y) -> int {
+        return wall ? rmw::wall_product(kind, r, x, y, n, eta, a, L_host, mode, st)
+                    : rmw::nowall_product(kind, r, x, y, n, eta, a, L_host, mode, st);
+    };
+    double *rhs = nullptr;
+    RMW_CUDA(cudaMallocAsync(&rhs, sizeof(double) * 2 * m, st));
+    double *tmp = rhs + m;
+    struct Free {
+        double *p;
+        cudaStream_t s;
+        ~Free() { cudaFreeAsync(p, s); }
+    } free_rhs{rhs, st};
+    // rhs = omega - M_WF force
+    if (int rc = product(RMW_WF, force, rhs)) return rc;
+    rmw::axpby_kernel<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(omega, rhs, m, 1.0, -1.0);
+    RMW_CHECK_LAUNCH("rollers right-hand side");
+    auto op = [&](const double *x, double *y) -> int { return product(RMW_WT, x, y); };
+    auto pc = [&](const double *x, double *y) -> int {
+        RMW_CUDA(cudaMemcpyAsync(y, x, sizeof(double) * m, cudaMemcpyDeviceToDevice, st));
+        return RMW_OK;
+    };
+    const int status =
+        rmw::gmres_right(op, pc, op, rhs, torque, m, tol, restart, maxiter, st, iters_host, relres_host, nullptr);
+    if (status != RMW_OK && status != RMW_ERR_NOT_CONVERGED) return status;
+    // velocity = M_UF force + M_UT torque
+    if (wall) {
+        if (int rc = rmw::wall_force_torque(r, force, torque, velocity, nullptr, n, eta, a, L_host, mode, st))
+            return rc;
+    } else {
+        if (int rc = product(RMW_UF, force, velocity)) return rc;
+        if (int rc = product(RMW_UT, torque, tmp)) return rc;
+        rmw::axpby_kernel<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(tmp, velocity, m, 1.0, 1.0);
+        RMW_CHECK_LAUNCH("rollers velocity");
+    }
+    RMW_CUDA(cudaStreamSynchronize(st));
+    if (status != RMW_OK) rmw::set_error("rollers torque solve did not reach the tolerance");
+    return status;
+}
+
+}  // extern "C"

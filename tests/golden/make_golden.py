@@ -23,6 +23,8 @@ tests load on any machine:
                  quaternion_integrator_multi_bodies.py with the normal draws it made
   source_target.npz  products with per-blob radii from sources to targets (wall, free
                  space, free surface) and the single-radius free-surface product
+  rollers.npz    rollers at a prescribed angular velocity (velocity-and-torque solve,
+                 two forward Euler steps) through QuaternionIntegratorRollers
   clones.npz     read_clones_file / read_vertex_file outputs and the trajectory
                  text of multi_bodies/multi_bodies.py:1428-1457
 
@@ -476,6 +478,57 @@ def make_source_target():
     np.savez_compressed(os.path.join(HERE, "source_target.npz"), **out)
 
 
+def make_rollers():
+    """Rollers at a prescribed angular velocity through the reference's
+    QuaternionIntegratorRollers (quaternion_integrator/quaternion_integrator_rollers.py):
+    compute_deterministic_velocity_and_torque (:905-983) and two
+    deterministic_forward_euler steps (:119-152) with the numba wall products,
+    gravity, wall and blob-blob repulsion (multi_bodies_functions.py), GMRES
+    tolerance 1e-12; prescribed and free kinematics; and free space."""
+    qr = ref_shims.load("quaternion_integrator.quaternion_integrator_rollers")
+    mbf = ref_shims.load_script("multi_bodies/multi_bodies_functions.py", "multi_bodies_functions")
+    mbf.calc_blob_blob_forces = mbf.calc_blob_blob_forces_python
+    out = {}
+    for name, seed, n, a, domain, free, L in (("wall", 90, 40, 0.5, "single_wall", "False", np.zeros(3)),
+                                           ("wall_free", 91, 30, 0.5, "single_wall", "True", np.zeros(3)),
+                                           ("periodic", 92, 30, 0.4, "single_wall", "False",
+                                            np.array([6.0, 6.0, 0.0])),
+                                           ("no_wall", 93, 30, 0.5, "no_wall", "False", np.zeros(3))):
+        rng = np.random.default_rng(seed)
+        r = blobs(rng, n, a, 1.05 * a, 3.0, 6.0)
+        fkw = {"g": 0.8, "repulsion_strength_wall": 0.4, "debye_length_wall": 0.2 * a}
+        bkw = dict(fkw, repulsion_strength=0.6, debye_length=0.2 * a, periodic_length=L)
+
+        class Blob:
+            def __init__(self, x):
+                self.location = np.array(x)
+
+        bodies = [Blob(x) for x in r]
+        integ = qr.QuaternionIntegratorRollers(bodies, n, "deterministic_forward_euler_rollers", tolerance=1e-12,
+                                               domain=domain, mobility_vector_prod_implementation="numba")
+        integ.calc_one_blob_forces = partial(mbf.calc_one_blob_forces, **fkw)
+        integ.calc_blob_blob_forces = partial(mbf.calc_blob_blob_forces, **bkw)
+        integ.eta, integ.a = 0.9, a
+        integ.omega_one_roller = np.array([0.0, 2.0, 0.3])
+        integ.free_kinematics = free
+        integ.hydro_interactions = 1
+        integ.periodic_length = L
+        integ.print_residual = False
+        force = np.asarray(mbf.calc_one_blob_forces(r.copy(), blob_radius=a, blob_mass=1.0, **fkw)).reshape(-1) + \
+            np.asarray(mbf.calc_blob_blob_forces(r.copy(), blob_radius=a, **bkw)).reshape(-1)
+        u, t = integ.compute_deterministic_velocity_and_torque()
+        p = name + "_"
+        out.update({p + "r": r, p + "force": force, p + "params": np.array([0.9, a]), p + "omega": integ.omega_one_roller,
+                    p + "L": L, p + "velocity": np.asarray(u).reshape(-1), p + "torque": np.asarray(t).reshape(-1),
+                    p + "force_params": np.array([fkw["g"], fkw["repulsion_strength_wall"], fkw["debye_length_wall"],
+                                                  bkw["repulsion_strength"], bkw["debye_length"]])})
+        integ.deterministic_torque_previous_step = None
+        for step in range(2):
+            integ.advance_time_step(0.01)
+            out[p + "x%d" % step] = np.array([b.location for b in bodies])
+    np.savez_compressed(os.path.join(HERE, "rollers.npz"), **out)
+
+
 def make_clones():
     """Structure-file reading and trajectory text of the reference:
     read_clones_file / read_vertex_file (read_input/) on two of the reference's
@@ -553,4 +606,6 @@ if __name__ == "__main__":
         make_clones()
     if not want or "source_target" in want:
         make_source_target()
+    if not want or "rollers" in want:
+        make_rollers()
     print("golden fixtures written to", HERE)

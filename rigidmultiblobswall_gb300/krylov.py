@@ -88,9 +88,10 @@ def gmres(A, b, x0=None, tol=1e-05, restart=None, maxiter=None, xtype=None, M=No
     maxiter = maxiter if maxiter is not None else 10 * n
     Af, Mf = _as_fn(A), _as_fn(M)
     if PC_side in ("left", "left_res") and Mf is not None:
-        A0, M0 = Af, Mf
-        Af = lambda x: M0(A0(x))  # noqa: E731
-        bt = torch.as_tensor(M0(bt), dtype=torch.float64, device=device).reshape(-1).contiguous()
+        # M A x = M b; either operator may take tensors or only numpy arrays
+        A0, M0 = _Callback(Af, n, device), _Callback(Mf, n, device)
+        Af = lambda x: M0._apply(A0._apply(x))  # noqa: E731
+        bt = M0._apply(bt).contiguous()
         Mf = None
     cbA = _Callback(Af, n, device)
     cbM = _Callback(Mf, n, device) if Mf is not None else None

@@ -143,6 +143,12 @@ int rmw_source_target_product(int geometry, const double *source, const double *
 int rmw_free_surface_product(const double *r, const double *force, double *out, int64_t n, double eta, double a,
                              const double *L_host, int mode, void *stream);
 
+/* Dense translational blob mobility M (row-major 3n x 3n, FP64) of n <= 65535
+ * blobs: wall = 1 single_wall_fluid_mobility (mobility/mobility.py:1018-1116,
+ * shifted heights and damping), wall = 0 rotne_prager_tensor
+ * (mobility/mobility.py:967-1015).  Device arrays; asynchronous. */
+int rmw_dense_mobility(int wall, const double *r, double *M, int64_t n, double eta, double a, void *stream);
+
 /* Rollers driven at a prescribed angular velocity: the torques solve
  * M_WT torque = omega - M_WF force (unpreconditioned restarted GMRES from
  * zero to the relative tolerance tol), then velocity = M_UF force +

@@ -54,6 +54,7 @@ SIGNATURES = {
     "rmw_nowall_product": (_i, [_i, _vp, _vp, _vp, _i64, _d, _d, _vp, _i, _vp]),
     "rmw_source_target_product": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _i64, _i64, _d, _vp, _i, _vp, _vp]),
     "rmw_free_surface_product": (_i, [_vp, _vp, _vp, _i64, _d, _d, _vp, _i, _vp]),
+    "rmw_dense_mobility": (_i, [_i, _vp, _vp, _i64, _d, _d, _vp]),
     "rmw_rollers_velocity_and_torque": (_i, [_vp, _vp, _vp, _vp, _vp, _i64, _d, _d, _vp, _i, _d, _i, _i, _i, _vp,
                                             _vp, _vp]),
     "rmw_rigid_set_wall": (_i, [_vp, _i]),

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "pair_math.cuh"
+#include "mobility_block.cuh"
 #include "rigid.cuh"
 #include "wall_pair.cuh"
 
@@ -87,41 +88,19 @@ __global__ void body_mobility_kernel(const double *__restrict__ r, const int *__
     const int b = blockIdx.x;
     const int o = boff[b], nbl = boff[b + 1] - o, m = 3 * nbl;
     double *Mb = M + moff[b];
-    const double inva = 1.0 / a;
     const double nf = 1.0 / (8.0 * kPi * eta * a);
     for (int pq = threadIdx.x; pq < nbl * nbl; pq += blockDim.x) {
         const int p = pq / nbl, q = pq % nbl;
-        const int i = o + p, j = o + q;
-        const double zi = r[3 * i + 2], zj = r[3 * j + 2];
-        const double bi = (zi < a) ? zi / a : 1.0, bj = (zj < a) ? zj / a : 1.0;
-        const double zie = (zi <= a) ? a : zi, zje = (zj <= a) ? a : zj;
-        double blk[3][3];
-        if (p == q) {
-            const double iz = a / zie, iz3 = iz * iz * iz, iz5 = iz3 * iz * iz;
-            const double mxx = 4.0 / 3.0 - (9.0 * iz - 2.0 * iz3 + iz5) / 12.0;
-            const double mzz = 4.0 / 3.0 - (9.0 * iz - 4.0 * iz3 + iz5) / 6.0;
-            for (int u = 0; u < 3; ++u)
-                for (int w = 0; w < 3; ++w) blk[u][w] = 0.0;
-            blk[0][0] = mxx; blk[1][1] = mxx; blk[2][2] = mzz;
-        } else {
-            const double dx = (r[3 * i] - r[3 * j]) * inva, dy = (r[3 * i + 1] - r[3 * j + 1]) * inva;
-            const double dz = (zie - zje) * inva;
-            const double hi = zie * inva, hj = zje * inva, Rz = (zie + zje) * inva;
-            for (int w = 0; w < 3; ++w) {
-                double c[3] = {0.0, 0.0, 0.0};
-                pair_contrib<RMW_UF, double>(dx, dy, dz, Rz, hi, hj, w == 0 ? 1.0 : 0.0, w == 1 ? 1.0 : 0.0,
-                                             w == 2 ? 1.0 : 0.0, c[0], c[1], c[2]);
-                blk[0][w] = c[0]; blk[1][w] = c[1]; blk[2][w] = c[2];
-            }
-        }
-        const double sc = nf * bi * bj;
+        double blk[3][3], sc;
+        uf_block(r, o + p, o + q, a, true, blk, &sc);
+        sc *= nf;
         for (int u = 0; u < 3; ++u)
             for (int w = 0; w < 3; ++w) Mb[(long long)(3 * p + u) * m + 3 * q + w] = sc * blk[u][w];
     }
 }
 
 // Free-space variant (no wall, no regularisation): the blocks of
-// rotne_prager_tensor (mobility/mobility.py:967-1015), self block 4/3 I.
+// rotne_prager_tensor (mobility/mobility.py:967-1015).
 __global__ void body_mobility_free_kernel(const double *__restrict__ r, const int *__restrict__ boff,
                                           const long long *__restrict__ moff, double *__restrict__ M, double eta,
                                           double a)
@@ -129,25 +108,11 @@ __global__ void body_mobility_free_kernel(const double *__restrict__ r, const in
     const int b = blockIdx.x;
     const int o = boff[b], nbl = boff[b + 1] - o, m = 3 * nbl;
     double *Mb = M + moff[b];
-    const double inva = 1.0 / a;
     const double nf = 1.0 / (8.0 * kPi * eta * a);
     for (int pq = threadIdx.x; pq < nbl * nbl; pq += blockDim.x) {
         const int p = pq / nbl, q = pq % nbl;
-        const int i = o + p, j = o + q;
-        double blk[3][3];
-        if (p == q) {
-            for (int u = 0; u < 3; ++u)
-                for (int w = 0; w < 3; ++w) blk[u][w] = (u == w) ? 4.0 / 3.0 : 0.0;
-        } else {
-            const double dx = (r[3 * i] - r[3 * j]) * inva, dy = (r[3 * i + 1] - r[3 * j + 1]) * inva,
-                         dz = (r[3 * i + 2] - r[3 * j + 2]) * inva;
-            for (int w = 0; w < 3; ++w) {
-                double c[3] = {0.0, 0.0, 0.0};
-                pair_rpy<RMW_UF, double>(dx, dy, dz, w == 0 ? 1.0 : 0.0, w == 1 ? 1.0 : 0.0, w == 2 ? 1.0 : 0.0,
-                                         c[0], c[1], c[2]);
-                blk[0][w] = c[0]; blk[1][w] = c[1]; blk[2][w] = c[2];
-            }
-        }
+        double blk[3][3], sc;
+        uf_block(r, o + p, o + q, a, false, blk, &sc);
         for (int u = 0; u < 3; ++u)
             for (int w = 0; w < 3; ++w) Mb[(long long)(3 * p + u) * m + 3 * q + w] = nf * blk[u][w];
     }

@@ -469,3 +469,47 @@ no_wall_mobility_trans_times_force_source_target_numba = no_wall_mobility_trans_
 free_surface_mobility_trans_times_force_source_target_numba = free_surface_mobility_trans_times_force_source_target_gb300
 free_surface_mobility_trans_times_force_pycuda = free_surface_mobility_trans_times_force_gb300
 free_surface_mobility_trans_times_force_numba = free_surface_mobility_trans_times_force_gb300
+
+
+# -- dense matrices ---------------------------------------------------------------
+def _dense(wall, r_vectors, eta, a):
+    import torch
+    dev, on_device = _device_for(r_vectors)
+    r = torch.as_tensor(r_vectors, dtype=torch.float64, device=dev).reshape(-1, 3).contiguous()
+    n = r.shape[0]
+    M = torch.empty((3 * n, 3 * n), dtype=torch.float64, device=dev)
+    with torch.cuda.device(dev):
+        _native.call("rmw_dense_mobility", 1 if wall else 0, r.data_ptr(), M.data_ptr(), n, float(eta), float(a),
+                     torch.cuda.current_stream(dev).cuda_stream)
+    return M if on_device else M.cpu().numpy()
+
+
+def single_wall_fluid_mobility(r_vectors, eta, a, *args, **kwargs):
+    """Dense (3N, 3N) wall mobility with shifted heights and damping
+    (mobility/mobility.py:1018-1116); periodic images are not part of it, as
+    in the reference."""
+    return _dense(True, r_vectors, eta, a)
+
+
+def rotne_prager_tensor(r_vectors, eta, a, *args, **kwargs):
+    """Dense (3N, 3N) free-space RPY mobility (mobility/mobility.py:967-1015)."""
+    return _dense(False, r_vectors, eta, a)
+
+
+def single_wall_fluid_mobility_product(r_vectors, vector, eta, a, *args, **kwargs):
+    """M v with the wall mobility (mobility/mobility.py:711-724, the dense
+    product); evaluated pairwise without forming M."""
+    kwargs.pop("periodic_length", None)
+    return wall_product("uf", r_vectors, vector, eta, a, **kwargs)
+
+
+def no_wall_fluid_mobility_product(r_vectors, vector, eta, a, *args, **kwargs):
+    """M v with the free-space mobility (mobility/mobility.py:727-737)."""
+    kwargs.pop("periodic_length", None)
+    return no_wall_product("uf", r_vectors, vector, eta, a, **kwargs)
+
+
+single_wall_fluid_mobility_loops = single_wall_fluid_mobility
+single_wall_fluid_mobility_cpp = single_wall_fluid_mobility
+rotne_prager_tensor_loops = rotne_prager_tensor
+rotne_prager_tensor_cpp = rotne_prager_tensor

@@ -132,3 +132,85 @@ def build_block_diagonal_preconditioners_det_stoch(bodies, r_vectors, Nblobs, et
     mode = kwargs.get("mode", "fp64")
     return (_Applier(sys_.apply_pc), _Applier(lambda w: sys_.mobility_pc(w, mode=mode)),
             _Applier(sys_.P_inv_mult))
+
+
+# ---------------------------------------------------------------------------
+# the simulation driver (multi_bodies/multi_bodies.py:1112-1627)
+def _no_wall(read):
+    impl = (read.mobility_blobs_implementation + " " + read.mobility_vector_prod_implementation).lower()
+    return read.domain == "no_wall" or "no_wall" in impl
+
+
+def setup_simulation(read):
+    """Bodies, handle and integrator of an input file (read_input.ReadInput):
+    structures (vertex + clones files), blob radius, mobility with or without
+    the wall, the scheme, forces (gravity and wall repulsion on every blob,
+    blob-blob repulsion unless blob_blob_force_implementation is 'None'),
+    seed.  Returns (integrator, structures_ID, body_types)."""
+    import torch
+    from . import clones, forces, integrator
+    if read.articulated or len(read.structures) > read.num_free_bodies:
+        raise NotImplementedError("articulated bodies and obstacles are not supported")
+    if read.body_body_force_torque_implementation != "None":
+        raise NotImplementedError("body-body forces are not supported")
+    if read.scheme not in integrator.QuaternionIntegrator.SCHEMES:
+        raise NotImplementedError("scheme %r is not available on the device" % read.scheme)
+    a = read.blob_radius
+    r_ref, locs, quats, counts, body_types = [], [], [], [], []
+    for files in read.structures:
+        if len(files) > 2:
+            raise NotImplementedError("slip and Laplace files are not supported")
+        ref = clones.read_vertex_file(files[0])
+        n, loc, ori = clones.read_clones_file(files[1])
+        body_types.append(n)
+        for k in range(n):
+            r_ref.append(ref)
+            counts.append(ref.shape[0])
+        locs.append(loc)
+        quats.append(ori)
+    L = read.periodic_length if read.periodic_length.size == 3 else np.zeros(3)
+    system = RigidSystem(counts, read.eta, a, periodic_length=L, wall=not _no_wall(read))
+    seed = int(read.seed) if read.seed is not None else int(torch.randint(0, 2 ** 31 - 1, (1,)).item())
+    integ = integrator.QuaternionIntegrator(
+        system, read.scheme, np.concatenate(locs), np.concatenate(quats), np.concatenate(r_ref),
+        tolerance=read.solver_tolerance, domain="no_wall" if _no_wall(read) else "single_wall", kT=read.kT,
+        rf_delta=read.rf_delta, mode=read.gb300_precision, seed=seed)
+    kw = {"g": read.g, "repulsion_strength_wall": read.repulsion_strength_wall,
+          "debye_length_wall": read.debye_length_wall, "periodic_length": L}
+    if read.blob_blob_force_implementation != "None":
+        kw.update(repulsion_strength=read.repulsion_strength, debye_length=read.debye_length)
+    integ.force_torque_calculator = lambda s, r: forces.force_torque_calculator_sort_by_bodies(s, r, **kw)
+    return integ, list(read.structures_ID), body_types
+
+
+def main(argv=None):
+    """python -m rigidmultiblobswall_gb300.multi_bodies --input-file data.main"""
+    import argparse
+    import shutil
+    from . import clones
+    from .read_input import ReadInput
+    parser = argparse.ArgumentParser(description="Run a multi-body simulation and save trajectory.")
+    parser.add_argument("--input-file", dest="input_file", type=str, default="data.main")
+    parser.add_argument("--print-residual", action="store_true")
+    args = parser.parse_args(argv)
+    read = ReadInput(args.input_file)
+    import os
+    out_dir = os.path.dirname(read.output_name)
+    if out_dir:
+        os.makedirs(out_dir, exist_ok=True)
+    shutil.copyfile(args.input_file, read.output_name + ".inputfile")
+    integ, ids, body_types = setup_simulation(read)
+    with open(read.output_name + ".bodies_info", "w") as f:
+        f.write("num_of_body_types  " + str(len(ids)) + "\n")
+        f.write("body_names         " + str(ids) + "\n")
+        f.write("body_types         " + str(body_types) + "\n")
+        f.write("num_bodies         " + str(sum(body_types)) + "\n")
+        f.write("num_blobs          " + str(integ.system.n_blobs) + "\n")
+    clones.run(integ, read.dt, read.n_steps, n_save=read.n_save, output_name=read.output_name, structures_ID=ids,
+               body_types=body_types, save_clones=read.save_clones, initial_step=read.initial_step, verbose=True)
+    integ.close()
+    return integ
+
+
+if __name__ == "__main__":
+    main()

@@ -580,6 +580,35 @@ def make_clones():
     out["write_locations"] = locs
     out["write_orientations"] = quats
     out["write_text"] = np.array(text)
+    # input files through the reference's ReadInput (read_input/read_input.py)
+    ri = ref_shims.load("read_input.read_input")
+    inp = ("# comment line\nscheme   stochastic_Slip_Trapz  # trailing\n\ndt 0.005\nn_steps 20\nn_save 5\n"
+           "eta 0.8\ng 1.5\nblob_radius 0.25\nkT 0.3\nsolver_tolerance 1e-9\nrf_delta 2e-3\n"
+           "periodic_length 10 12 0\nmobility_vector_prod_implementation numba_no_wall\n"
+           "blob_blob_force_implementation python\nrepulsion_strength 2.5\ndebye_length 0.1\n"
+           "output_name out/run\nsave_clones one_file\nseed 7\n"
+           # given explicitly: the reference parses their 'None' defaults with np.fromstring,
+           # which numpy 2 rejects
+           "plot_velocity_field 0 1 2\nplot_concentration_field 0 1 2\nbackground_Laplace 0 0 0\n"
+           "structure Structures/shell_N_12_Rg_1.vertex Structures/shell_N_12_Rg_1.clones\n"
+           "structure Structures/boomerang_N_15.vertex Structures/boomerang_N_15.clones\n")
+    keys = ["n_steps", "initial_step", "n_save", "dt", "eta", "g", "blob_radius", "kT", "scheme", "output_name",
+            "repulsion_strength_wall", "debye_length_wall", "mobility_blobs_implementation",
+            "mobility_vector_prod_implementation", "repulsion_strength", "debye_length",
+            "blob_blob_force_implementation", "solver_tolerance", "rf_delta", "save_clones", "domain", "update_PC",
+            "hydro_interactions", "seed"]
+    with tempfile.TemporaryDirectory() as d:
+        for tag, extra in (("input", ""), ("restart", "initial_step 10\n")):
+            p = os.path.join(d, tag + ".dat")
+            with open(p, "w") as f:
+                f.write(inp + extra)
+            rd = ri.ReadInput(p)
+            out[tag + "_text"] = np.array(inp + extra)
+            out[tag + "_values"] = np.array([str(getattr(rd, k)) for k in keys])
+            out[tag + "_periodic_length"] = np.asarray(rd.periodic_length, dtype=np.float64)
+            out[tag + "_structures"] = np.array([" ".join(s) for s in rd.structures])
+            out[tag + "_structures_ID"] = np.array(rd.structures_ID)
+    out["input_keys"] = np.array(keys)
     np.savez_compressed(os.path.join(HERE, "clones.npz"), **out)
 
 

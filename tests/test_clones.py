@@ -112,3 +112,18 @@ def test_run_save_cadence_and_resume(tmp_path, save_clones):
                save_clones=save_clones)
     assert second.steps == [3, 4, 5]
     np.testing.assert_array_equal(second.x.numpy(), s6.x.numpy())
+
+
+@pytest.mark.parametrize("tag", ["input", "restart"])
+def test_read_input_matches_reference(tmp_path, tag):
+    """ReadInput against the reference's parse of the same file (values as the
+    reference's str() of each attribute; restart rewrites the clones paths)."""
+    from rigidmultiblobswall_gb300.read_input import ReadInput
+    g = golden("clones.npz")
+    rd = ReadInput(_write(tmp_path, tag + ".dat", g[tag + "_text"]))
+    for k, v in zip(g["input_keys"], g[tag + "_values"]):
+        assert str(getattr(rd, str(k))) == str(v), k
+    np.testing.assert_array_equal(rd.periodic_length, g[tag + "_periodic_length"])
+    assert [" ".join(s) for s in rd.structures] == [str(s) for s in g[tag + "_structures"]]
+    assert rd.structures_ID == [str(s) for s in g[tag + "_structures_ID"]]
+    assert rd.gb300_precision == "fp64"

@@ -416,6 +416,14 @@ def large_solve(args):
     B.build()
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
+    # warm-up on 4 shells in every mode: the first use of each torch elementwise kernel in a process
+    # costs seconds on this image (PyTorch's own kernels are compiled for the GPU at first launch)
+    sw = S.shells_42_256(n_bodies=4, seed=9)
+    sysw = RigidSystem([42] * 4, sw.eta, sw.a, device=dev)
+    sysw.set_configuration(sw.r_vectors(), sw.locations)
+    for m in ("fp64", "df64", "mixed"):
+        integrator.solve_mobility_problem(sysw, np.ones((4, 6)), tol=1e-8, mode=m)
+    sysw.close()
     s5 = S.shells_42_4096()
     sys5 = RigidSystem([42] * s5.n_bodies, s5.eta, s5.a, device=dev)
     sys5.set_configuration(s5.r_vectors(), s5.locations)

@@ -60,6 +60,9 @@ def parse():
     p.add_argument("--large", action="store_true",
                    help="only run the 4096-shell (172,032-blob) solve comparison and print its JSON line")
     p.add_argument("--large-modes", default="mixed+nf,mixed,df64,fp64")
+    p.add_argument("--product", default=None, metavar="KIND:MODE",
+                   help="only time one wall product (kind uf|ut|wf|wt, mode fp64|df64|mixed) on the headline "
+                        "workload for --steps steps after --warmup, and print its JSON line")
     return p.parse_args()
 
 
@@ -521,10 +524,36 @@ def batched_metrics(dev, nrhs=16):
     return out
 
 
+def single_product(args):
+    """One wall product on the 256-shell workload (the default split of the autotuner's cache, i.e. the
+    symmetric kernel for UF in df64 and mixed at this size): CUDA-event time per step, L2 flushed between
+    steps."""
+    import torch
+    from rigidmultiblobswall_gb300 import build as B
+    from rigidmultiblobswall_gb300 import mobility as mb
+    B.build()
+    kind, mode = args.product.split(":")
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    s, r, f = workload()
+    rt = torch.tensor(r, device=dev)
+    ft = torch.tensor(f, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for _ in range(max(args.warmup - 2, 0)):
+        mb.wall_product(kind, rt, ft, s.eta, s.a, mode=mode)
+    res = time_product(kind, mode, rt, ft, None, s.eta, s.a, args.steps, flush, torch.cuda.current_stream(dev))
+    print(json.dumps({"metric": "M_%s product Gpairs/s" % kind.upper(), "mode": mode,
+                      "workload": "256 shells x 42 blobs = 10,752 blobs, forces N(0,1), seed 1",
+                      "n_blobs": len(r), "steps": args.steps, **res}))
+
+
 def main():
     args = parse()
     if args.large:
         large_solve(args)
+        return
+    if args.product:
+        single_product(args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -291,20 +291,15 @@ __global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *_
     __syncthreads();
     double ax = 0.0, ay = 0.0, az = 0.0;
     df ux = df_from(0.f), uy = df_from(0.f), uz = df_from(0.f);
-    for (int k = 0; k < kTile; ++k) {
-        __syncwarp();
-        if (k && !(k & 31)) {  // fold each group of 32 double-float sums into FP64
-            ax += to_double(ux);
-            ay += to_double(uy);
-            az += to_double(uz);
-            ux = df_from(0.f);
-            uy = df_from(0.f);
-            uz = df_from(0.f);
-        }
-        if (diag) {
-            const int off = (k - 32 * warp) & (kTile - 1);  // (source - target) mod 128, warp-uniform
-            if (off == 0 || off > kTile / 2 || (off == kTile / 2 && warp >= kSymWarps / 2)) continue;
-        }
+    auto fold = [&]() {  // fold each group of 32 double-float sums into FP64
+        ax += to_double(ux);
+        ay += to_double(uy);
+        az += to_double(uz);
+        ux = df_from(0.f);
+        uy = df_from(0.f);
+        uz = df_from(0.f);
+    };
+    auto step = [&](int k) {
         const int jl = (lane + k) & (kTile - 1);
         const float4 sh = thi[jl], sl = tlo[jl], svh = tvh[jl], svl = tvl[jl];
         const df xj = {sh.x, sl.x}, yj = {sh.y, sl.y}, zj = {sh.z, sl.z};
@@ -322,6 +317,25 @@ __global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *_
             df acc = {a2.x, a2.y};
             acc_add(acc, wv[c]);
             sacc[warp][c][jl] = make_float2(acc.hi, acc.lo);
+        }
+    };
+    if (diag) {
+        for (int k = 0; k < kTile; ++k) {
+            __syncwarp();
+            if (k && !(k & 31)) fold();
+            const int off = (k - 32 * warp) & (kTile - 1);  // (source - target) mod 128, warp-uniform
+            if (off == 0 || off > kTile / 2 || (off == kTile / 2 && warp >= kSymWarps / 2)) continue;
+            step(k);
+        }
+    } else {
+        // off-diagonal tiles: no per-step skip test (unrolling measured slower here)
+        for (int g = 0; g < kTile; g += 32) {
+            if (g) fold();
+#pragma unroll 1
+            for (int k = g; k < g + 32; ++k) {
+                __syncwarp();
+                step(k);
+            }
         }
     }
     ax += to_double(ux);
@@ -386,12 +400,7 @@ __global__ void __launch_bounds__(kThreads) wall_uf_mixed_sym_kernel(const SrcF 
         for (int k = lane; k < kTile; k += 32) sacc[warp][c][k] = 0.f;
     __syncthreads();
     float ux = 0.f, uy = 0.f, uz = 0.f;
-    for (int k = 0; k < kTile; ++k) {
-        __syncwarp();
-        if (diag) {
-            const int off = (k - 32 * warp) & (kTile - 1);
-            if (off == 0 || off > kTile / 2 || (off == kTile / 2 && warp >= kSymWarps / 2)) continue;
-        }
+    auto step = [&](int k) {
         const int jl = (lane + k) & (kTile - 1);
         const float4 sh = thi[jl], sl = tlo[jl], sv = tv[jl];
         const float dx = (me.hi.x - sh.x) + (me.lo.x - sl.x);
@@ -407,6 +416,21 @@ __global__ void __launch_bounds__(kThreads) wall_uf_mixed_sym_kernel(const SrcF 
         sacc[warp][0][jl] += wx;
         sacc[warp][1][jl] += wy;
         sacc[warp][2][jl] += wz;
+    };
+    if (diag) {
+        for (int k = 0; k < kTile; ++k) {
+            __syncwarp();
+            const int off = (k - 32 * warp) & (kTile - 1);
+            if (off == 0 || off > kTile / 2 || (off == kTile / 2 && warp >= kSymWarps / 2)) continue;
+            step(k);
+        }
+    } else {
+        // off-diagonal tiles (all but nt of them): no per-step skip test; two steps per trip
+#pragma unroll 2
+        for (int k = 0; k < kTile; ++k) {
+            __syncwarp();
+            step(k);
+        }
     }
     float sx = 0.f, sy = 0.f, sz = 0.f, ex_ = 0.f, ey_ = 0.f, ez_ = 0.f;
     comp_add(sx, ex_, ux);

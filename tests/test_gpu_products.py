@@ -5,7 +5,6 @@ Tolerances (relative 2-norm error of the whole output vector):
   FP64 mode   <= 1e-12
   mixed mode  <= 1e-6
 """
-import ctypes
 
 import numpy as np
 import pytest

@@ -12,7 +12,6 @@ import numpy as np
 import pytest
 
 from conftest import golden
-from oracle import schemes as osch
 from rigidmultiblobswall_gb300 import forces, integrator
 from rigidmultiblobswall_gb300.rigid import RigidSystem
 from test_oracle_schemes import SCHEMES, Draws, make

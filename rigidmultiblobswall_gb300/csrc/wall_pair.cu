@@ -259,15 +259,36 @@ __device__ __forceinline__ void sym_tile_pair(long long b, int nt, int &T, int &
     S = t + (int)(b - off(t));
 }
 
+// The CTA's tile pair: from blockIdx.x over the upper triangle of nt tiles, or
+// (SEG) from its job, which also moves src and partial to its suspension.
+template <bool SEG, typename Rec>
+__device__ __forceinline__ void sym_cta(const SymJob *jobs, int &n, int &nt, int &T, int &S,
+                                        const Rec *__restrict__ &src, double *__restrict__ &partial)
+{
+    if (SEG) {
+        const SymJob jb = jobs[blockIdx.x];
+        src += jb.base;
+        partial += jb.pbase;
+        n = jb.n;
+        nt = (jb.n + kTile - 1) / kTile;
+        T = jb.T;
+        S = jb.S;
+    } else {
+        sym_tile_pair(blockIdx.x, nt, T, S);
+    }
+}
+
+template <bool SEG>
 __global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *__restrict__ src, int n, int nt,
-                                                                   double *__restrict__ partial)
+                                                                   double *__restrict__ partial,
+                                                                   const SymJob *__restrict__ jobs)
 {
     // structure-of-arrays source tile: the rotated reads of a warp hit 32
     // consecutive 16-byte entries (no bank conflicts)
     __shared__ float4 thi[kTile], tlo[kTile], tvh[kTile], tvl[kTile];
     __shared__ float2 sacc[kSymWarps][3][kTile];  // per-warp source-side double-float sums (hi, lo)
     int T, S;
-    sym_tile_pair(blockIdx.x, nt, T, S);
+    sym_cta<SEG>(jobs, n, nt, T, S, src, partial);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool diag = (T == S);
     const int i = T * kTile + tid;
@@ -374,13 +395,15 @@ __global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *_
 // tile is folded into a TwoSum-compensated accumulator; the source side sums
 // its 32 contributions per warp in FP32 shared memory and the four warp
 // copies in FP64.
+template <bool SEG>
 __global__ void __launch_bounds__(kThreads) wall_uf_mixed_sym_kernel(const SrcF *__restrict__ src, int n, int nt,
-                                                                      double *__restrict__ partial)
+                                                                      double *__restrict__ partial,
+                                                                      const SymJob *__restrict__ jobs)
 {
     __shared__ float4 thi[kTile], tlo[kTile], tv[kTile];
     __shared__ float sacc[kSymWarps][3][kTile];
     int T, S;
-    sym_tile_pair(blockIdx.x, nt, T, S);
+    sym_cta<SEG>(jobs, n, nt, T, S, src, partial);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool diag = (T == S);
     const int i = T * kTile + tid;
@@ -738,17 +761,23 @@ __global__ void wall_finalize_multi_kernel(const double *__restrict__ r, const d
 
 // ---------------------------------------------------------------------------
 // finalize: fixed-order chunk sum + FP64 self term + b_i * norm factor.
+// With pbase / pstride (segmented symmetric layout) blob i's slot s is at
+// partial + pbase[i] + s * pstride[i]; otherwise at partial + s * 3n + 3i.
 template <int KIND>
 __global__ void wall_finalize_kernel(const double *__restrict__ r, const double *__restrict__ v,
                                      const double *__restrict__ partial, int nchunks, double *__restrict__ out,
-                                     int n, double a, double nf, const int *__restrict__ blob_nchunks)
+                                     int n, double a, double nf, const int *__restrict__ blob_nchunks,
+                                     const long long *__restrict__ pbase = nullptr,
+                                     const int *__restrict__ pstride = nullptr)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double ux = 0.0, uy = 0.0, uz = 0.0;
     const int nc = blob_nchunks ? blob_nchunks[i] : nchunks;
+    const double *p0 = pbase ? partial + pbase[i] : partial + 3 * (size_t)i;
+    const size_t ps = pstride ? (size_t)pstride[i] : 3 * (size_t)n;
     for (int s = 0; s < nc; ++s) {
-        const double *p = partial + (size_t)s * 3 * n + 3 * (size_t)i;
+        const double *p = p0 + (size_t)s * ps;
         ux += p[0]; uy += p[1]; uz += p[2];
     }
     const double z = r[3 * i + 2];
@@ -902,12 +931,12 @@ int wall_product_sym_with_scratch(const double *r, const double *v, double *out,
         SrcDF *src = (SrcDF *)base;
         pack_df_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
         if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
-        wall_uf_df_sym_kernel<<<ncta, kThreads, 0, st>>>(src, n, nt, partial);
+        wall_uf_df_sym_kernel<false><<<ncta, kThreads, 0, st>>>(src, n, nt, partial, nullptr);
     } else {
         SrcF *src = (SrcF *)base;
         pack_mixed_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
         if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
-        wall_uf_mixed_sym_kernel<<<ncta, kThreads, 0, st>>>(src, n, nt, partial);
+        wall_uf_mixed_sym_kernel<false><<<ncta, kThreads, 0, st>>>(src, n, nt, partial, nullptr);
     }
     if (int rc = trace_end(tok, st)) return rc;
     wall_finalize_kernel<RMW_UF><<<pg, pb, 0, st>>>(r, v, partial, nt, out, n, a, 1.0 / (8.0 * kPi * eta * a),
@@ -973,6 +1002,37 @@ int wall_batch_build(WallBatch &B, const long long *off, int ninst)
     RMW_CUDA(cudaMalloc(&B.blob_nch, sizeof(int) * std::max(1, B.n)));
     RMW_CUDA(cudaMemcpy(B.jobs, jobs.data(), sizeof(TileJob) * jobs.size(), cudaMemcpyHostToDevice));
     if (B.n) RMW_CUDA(cudaMemcpy(B.blob_nch, nch.data(), sizeof(int) * B.n, cudaMemcpyHostToDevice));
+    // symmetric UF layout: every suspension's upper triangle of tile pairs,
+    // partial sums suspension after suspension
+    std::vector<SymJob> sj;
+    std::vector<long long> pb(B.n);
+    std::vector<int> pst(B.n), nsl(B.n);
+    long long pbase = 0;
+    for (int k = 0; k < ninst; ++k) {
+        const int b0 = (int)off[k], m = (int)(off[k + 1] - off[k]);
+        if (m == 0) continue;
+        const int nt = (m + kTile - 1) / kTile;
+        for (int T = 0; T < nt; ++T)
+            for (int S = T; S < nt; ++S) sj.push_back({pbase, b0, m, T, S});
+        for (int i = 0; i < m; ++i) {
+            pb[b0 + i] = pbase + 3LL * i;
+            pst[b0 + i] = 3 * m;
+            nsl[b0 + i] = nt;
+        }
+        pbase += (long long)nt * 3 * m;
+    }
+    B.nsym = (long long)sj.size();
+    B.sym_doubles = pbase;
+    RMW_CUDA(cudaMalloc(&B.sym_jobs, sizeof(SymJob) * std::max<size_t>(1, sj.size())));
+    RMW_CUDA(cudaMalloc(&B.blob_pbase, sizeof(long long) * std::max(1, B.n)));
+    RMW_CUDA(cudaMalloc(&B.blob_pstride, sizeof(int) * std::max(1, B.n)));
+    RMW_CUDA(cudaMalloc(&B.blob_nslots, sizeof(int) * std::max(1, B.n)));
+    if (!sj.empty()) RMW_CUDA(cudaMemcpy(B.sym_jobs, sj.data(), sizeof(SymJob) * sj.size(), cudaMemcpyHostToDevice));
+    if (B.n) {
+        RMW_CUDA(cudaMemcpy(B.blob_pbase, pb.data(), sizeof(long long) * B.n, cudaMemcpyHostToDevice));
+        RMW_CUDA(cudaMemcpy(B.blob_pstride, pst.data(), sizeof(int) * B.n, cudaMemcpyHostToDevice));
+        RMW_CUDA(cudaMemcpy(B.blob_nslots, nsl.data(), sizeof(int) * B.n, cudaMemcpyHostToDevice));
+    }
     return RMW_OK;
 }
 
@@ -983,9 +1043,15 @@ void wall_batch_free(WallBatch &B)
     cudaSetDevice(B.device);
     if (B.jobs) cudaFree(B.jobs);
     if (B.blob_nch) cudaFree(B.blob_nch);
+    for (void *p : {(void *)B.sym_jobs, (void *)B.blob_pbase, (void *)B.blob_pstride, (void *)B.blob_nslots})
+        if (p) cudaFree(p);
     cudaSetDevice(cur);
     B.jobs = nullptr;
     B.blob_nch = nullptr;
+    B.sym_jobs = nullptr;
+    B.blob_pbase = nullptr;
+    B.blob_pstride = nullptr;
+    B.blob_nslots = nullptr;
 }
 
 int wall_product_batched(const WallBatch &B, int kind, const double *r, const double *v, double *out, double eta,
@@ -995,6 +1061,33 @@ int wall_product_batched(const WallBatch &B, int kind, const double *r, const do
     if (rc) return rc;
     if (B.n == 0 || B.njobs == 0) return RMW_OK;
     void *ws = nullptr;
+    if (kind == RMW_UF && (mode == RMW_MODE_DF64 || mode == RMW_MODE_MIXED) && B.nsym > 0 &&
+        B.sym_doubles * (long long)sizeof(double) <= (long long)kSymMaxPartialBytes) {
+        // each suspension's unordered pairs once, applied both ways
+        const size_t rec = (mode == RMW_MODE_DF64) ? sizeof(SrcDF) : sizeof(SrcF);
+        const size_t packed = ((rec * (size_t)B.n + 255) / 256) * 256;
+        rc = scratch(SCRATCH_PAIR, packed + sizeof(double) * (size_t)B.sym_doubles, &ws, st);
+        if (rc) return rc;
+        double *partial = (double *)((char *)ws + packed);
+        const int pb = 256, pg = (B.n + pb - 1) / pb;
+        void *tok = nullptr;
+        if (mode == RMW_MODE_DF64) {
+            pack_df_kernel<<<pg, pb, 0, st>>>(r, v, (SrcDF *)ws, B.n, a);
+            if (int rc2 = trace_begin(TRACE_PAIR, st, &tok)) return rc2;
+            wall_uf_df_sym_kernel<true><<<(unsigned)B.nsym, kThreads, 0, st>>>((const SrcDF *)ws, 0, 0, partial,
+                                                                               B.sym_jobs);
+        } else {
+            pack_mixed_kernel<<<pg, pb, 0, st>>>(r, v, (SrcF *)ws, B.n, a);
+            if (int rc2 = trace_begin(TRACE_PAIR, st, &tok)) return rc2;
+            wall_uf_mixed_sym_kernel<true><<<(unsigned)B.nsym, kThreads, 0, st>>>((const SrcF *)ws, 0, 0, partial,
+                                                                                  B.sym_jobs);
+        }
+        if (int rc2 = trace_end(tok, st)) return rc2;
+        wall_finalize_kernel<RMW_UF><<<pg, pb, 0, st>>>(r, v, partial, 0, out, B.n, a, 1.0 / (8.0 * kPi * eta * a),
+                                                         B.blob_nslots, B.blob_pbase, B.blob_pstride);
+        RMW_CHECK_LAUNCH("segmented symmetric wall product");
+        return RMW_OK;
+    }
     rc = scratch(SCRATCH_PAIR, wall_scratch_bytes(B.n, mode, B.max_slots), &ws, st);
     if (rc) return rc;
     return launch_dispatch(kind, r, v, out, B.n, eta, a, nullptr, mode, st, ws, B.max_slots, &B);

@@ -12,6 +12,14 @@ struct TileJob {
     int t0, t1, s0, s1, slot;
 };
 
+// One CTA of a segmented symmetric UF product: tile pair T <= S of the
+// suspension whose blobs start at `base` (n of them), partial sums of that
+// suspension at `pbase` (its nt slots of 3n doubles).
+struct SymJob {
+    long long pbase;
+    int base, n, T, S;
+};
+
 // Segmented product layout for many independent suspensions of one blob
 // array: suspension k owns blobs [off[k], off[k+1]) and only interacts with
 // itself.  Built once (rmw_wall_batch_create) and reused by every product.
@@ -22,6 +30,13 @@ struct WallBatch {
     int max_slots = 1;  // chunk slots of the partial-sum buffer
     TileJob *jobs = nullptr;  // device
     int *blob_nch = nullptr;  // device: chunk count of each blob's suspension
+    // symmetric UF layout: per suspension nt = ceil(n / 128) tiles, nt (nt + 1) / 2 CTAs
+    long long nsym = 0;             // CTAs
+    long long sym_doubles = 0;      // partial-sum doubles (sum over suspensions of nt * 3n)
+    SymJob *sym_jobs = nullptr;     // device
+    long long *blob_pbase = nullptr;  // device: slot-0 entry of each blob's partial sums
+    int *blob_pstride = nullptr;    // device: 3n of each blob's suspension (slot stride)
+    int *blob_nslots = nullptr;     // device: nt of each blob's suspension
     std::vector<long long> off;
     int device = 0;
 };

@@ -701,14 +701,12 @@ __global__ void __launch_bounds__(kThreads) wall_pair_multi_kernel(const SrcF *_
             const float dz = (mh.z - shp.z) + (ml.z - slp.z);
             const float hj = shp.z + slp.z;
             const float Rz = hi + hj;
-            const UFCoeffs<float> c = uf_coeffs<float>(dx, dy, dz, Rz, hi, hj);
-            const bool use = (j != i);
+            UFCoeffs<float> c = uf_coeffs<float>(dx, dy, dz, Rz, hi, hj);
+            if (j == i) c = UFCoeffs<float>{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // self pair: zero block (finite inputs)
 #pragma unroll
             for (int q = 0; q < kMultiRhs; ++q) {
                 const float4 v = tvec[k * kMultiRhs + q];
-                float cx = 0.f, cy = 0.f, cz = 0.f;
-                uf_apply<float>(c, dx, dy, dz, Rz, v.x, v.y, v.z, cx, cy, cz);
-                if (use) { acc[q][0] += cx; acc[q][1] += cy; acc[q][2] += cz; }
+                uf_apply<float>(c, dx, dy, dz, Rz, v.x, v.y, v.z, acc[q][0], acc[q][1], acc[q][2]);
             }
         }
 #pragma unroll

@@ -446,9 +446,11 @@ bool tridiag_eigen_host(std::vector<double> &d, std::vector<double> e, std::vect
 // eigen-decomposition and convergence test (stochastic_forcing.py:112-264),
 // the operator is applied to all of them at once.  Converged segments are
 // frozen by zeroing their part of the next basis vector.
-template <typename Op>
+// before_op(active) runs before every operator application with the
+// segments' current active flags (converged segments are 0).
+template <typename Op, typename Pre>
 static int lanczos_batched(Op op, const double *z, double *noise, const std::vector<long long> &off, double factor,
-                           double tol, int max_iter, cudaStream_t st, std::vector<int> &iters)
+                           double tol, int max_iter, cudaStream_t st, std::vector<int> &iters, Pre before_op)
 {
     const int nseg = (int)off.size() - 1;
     const long long n = off.back();
@@ -489,6 +491,7 @@ static int lanczos_batched(Op op, const double *z, double *noise, const std::vec
         for (int k = 0; k < nseg; ++k) n_active += active[k];
         if (!n_active) break;
         double *Vi = V + (long long)i * ldv;
+        if (int rc = before_op(active)) return rc;
         if (int rc = op(Vi, w)) return rc;
         if (i > 0) {  // w -= hs[i-1] V_{i-1}
             if (int rc = O.fetch()) return rc;
@@ -755,13 +758,42 @@ int rmw_rigid_lanczos_batched(void *sys, const double *Z, double *noise, int nrh
     double *buf = nullptr;
     RMW_CUDA(cudaMallocAsync(&buf, sizeof(double) * 2 * nrhs * N3, S.st));
     double *tmp = buf, *raw = buf + nrhs * N3;
+    // mixed precision: the multi-vector product skips suspensions whose
+    // segments of a pass of 8 right-hand sides have all converged (their rows
+    // are zero anyway), through one byte per (pass, suspension)
+    const bool mask = (mode == RMW_MODE_MIXED) && S.wall;
+    const int npass = (nrhs + 7) / 8;
+    unsigned char *d_act = nullptr;
+    static thread_local unsigned char *h_act = nullptr;
+    static thread_local size_t h_cap = 0;
+    const size_t nact = (size_t)npass * nsusp;
+    if (mask) {
+        RMW_CUDA(cudaMallocAsync(&d_act, nact, S.st));
+        if (h_cap < nact) {
+            if (h_act) cudaFreeHost(h_act);
+            RMW_CUDA(cudaHostAlloc(&h_act, nact, cudaHostAllocDefault));
+            h_cap = nact;
+        }
+    }
     auto op_direct = [&](const double *x, double *y) {
-        return rmw::rigid_mobility_pc_multi(S, x, y, nrhs, mode, tmp);
+        return rmw::rigid_mobility_pc_multi(S, x, y, nrhs, mode, tmp, d_act);
     };
     auto gop = rmw::make_graph_op(op_direct, &S.st, nrhs * N3, nrhs * N3);  // one graph per application
     auto op = [&](const double *x, double *y) -> int { return gop(x, y); };
+    auto before_op = [&](const std::vector<char> &act) -> int {
+        if (!mask) return RMW_OK;
+        for (int p = 0; p < npass; ++p)
+            for (int k = 0; k < nsusp; ++k) {
+                unsigned char any = 0;
+                for (int q = 8 * p; q < std::min(nrhs, 8 * p + 8); ++q) any |= act[(size_t)q * nsusp + k] ? 1 : 0;
+                h_act[(size_t)p * nsusp + k] = any;
+            }
+        RMW_CUDA(cudaMemcpyAsync(d_act, h_act, nact, cudaMemcpyHostToDevice, S.st));
+        return RMW_OK;
+    };
     std::vector<int> it;
-    int rc = rmw::lanczos_batched(op, Z, raw, off, factor, tol, max_iter, S.st, it);
+    int rc = rmw::lanczos_batched(op, Z, raw, off, factor, tol, max_iter, S.st, it, before_op);
+    if (d_act) cudaFreeAsync(d_act, S.st);
     if (rc == RMW_OK) rc = rmw::rigid_P_inv_mult_multi(S, raw, noise, nrhs);
     cudaFreeAsync(buf, S.st);
     cudaStreamSynchronize(S.st);

@@ -532,13 +532,14 @@ int rigid_mobility_pc(RigidSystem &S, const double *w, double *y, int mode)
     return tri_mult(S, S.linv, y, y, 0);
 }
 
-int rigid_mobility_pc_multi(RigidSystem &S, const double *W, double *Y, int nvec, int mode, double *tmp)
+int rigid_mobility_pc_multi(RigidSystem &S, const double *W, double *Y, int nvec, int mode, double *tmp,
+                            const unsigned char *active)
 {
     if (!S.stoch_ready) return fail(RMW_ERR_ARG, "stochastic preconditioner not built");
     const long long ld = 3LL * S.n;
     if (int rc = tri_mult(S, S.linv, W, tmp, 1, nvec)) return rc;
     if (mode == RMW_MODE_MIXED && S.wall) {
-        if (int rc = wall_uf_multi(S.r, tmp, ld, Y, ld, nvec, S.n, S.eta, S.a, S.batch, S.st)) return rc;
+        if (int rc = wall_uf_multi(S.r, tmp, ld, Y, ld, nvec, S.n, S.eta, S.a, S.batch, S.st, active)) return rc;
     } else {
         for (int q = 0; q < nvec; ++q)
             if (int rc = rigid_mobility(S, tmp + q * ld, Y + q * ld, mode)) return rc;

@@ -74,7 +74,10 @@ int rigid_mobility_pc(RigidSystem &S, const double *w, double *y, int mode);
 int rigid_P_inv_mult(RigidSystem &S, const double *w, double *y);
 // nvec vectors (stride 3N) at once; tmp holds nvec * 3N doubles.  Mixed mode
 // uses the multi-right-hand-side pair kernel.
-int rigid_mobility_pc_multi(RigidSystem &S, const double *W, double *Y, int nvec, int mode, double *tmp);
+// active: optional per (pass of 8 vectors, suspension) bytes of the mixed
+// multi-vector product (wall_uf_multi); 0 skips that suspension's rows.
+int rigid_mobility_pc_multi(RigidSystem &S, const double *W, double *Y, int nvec, int mode, double *tmp,
+                            const unsigned char *active = nullptr);
 int rigid_P_inv_mult_multi(RigidSystem &S, const double *W, double *Y, int nvec);
 // near-field augmented preconditioner apply, nearfield.cu
 int nearfield_apply_pc(RigidSystem &S, const double *x, double *y);

@@ -665,10 +665,12 @@ template <bool SEG>
 __global__ void __launch_bounds__(kThreads) wall_pair_multi_kernel(const SrcF *__restrict__ src,
                                                                     const float4 *__restrict__ vec, int n, int chunk,
                                                                     double *__restrict__ partial,
-                                                                    const TileJob *__restrict__ jobs)
+                                                                    const TileJob *__restrict__ jobs,
+                                                                    const unsigned char *__restrict__ active)
 {
     __shared__ float4 tpos[2 * kTile / 2];      // hi, lo of kTile/2 sources
     __shared__ float4 tvec[kTile / 2 * kMultiRhs];
+    if (SEG && active && !active[jobs[blockIdx.x].susp]) return;  // converged suspension: nothing to do
     const PairRange pr = pair_range<SEG>(jobs, n, chunk);
     const int i = pr.tbeg + threadIdx.x;
     const bool valid = i < pr.tend;
@@ -729,11 +731,18 @@ __global__ void __launch_bounds__(kThreads) wall_pair_multi_kernel(const SrcF *_
 __global__ void wall_finalize_multi_kernel(const double *__restrict__ r, const double *__restrict__ V, long long ldv,
                                            int nrhs, const double *__restrict__ partial, int nchunks,
                                            double *__restrict__ out, long long ldo, int n, double a, double nf,
-                                           const int *__restrict__ blob_nchunks)
+                                           const int *__restrict__ blob_nchunks,
+                                           const unsigned char *__restrict__ active = nullptr,
+                                           const int *__restrict__ blob_susp = nullptr)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
     if (i >= n || q >= nrhs) return;
+    if (active && !active[blob_susp[i]]) {  // skipped suspension: zero rows
+        double *o = out + (long long)q * ldo + 3LL * i;
+        o[0] = o[1] = o[2] = 0.0;
+        return;
+    }
     const int nc = blob_nchunks ? blob_nchunks[i] : nchunks;
     double ux = 0.0, uy = 0.0, uz = 0.0;
     for (int s = 0; s < nc; ++s) {
@@ -979,7 +988,9 @@ int wall_batch_build(WallBatch &B, const long long *off, int ninst)
     const long long want = 152 * 8;
     const int factor = (int)std::max<long long>(1, std::min<long long>(64, (want + tiles - 1) / std::max(1LL, tiles)));
     std::vector<TileJob> jobs;
-    std::vector<int> nch(B.n);
+    std::vector<int> nch(B.n), bsusp(B.n);
+    for (int k = 0; k < ninst; ++k)
+        for (long long i = off[k]; i < off[k + 1]; ++i) bsusp[i] = k;
     int max_slots = 1;
     for (int k = 0; k < ninst; ++k) {
         const int b0 = (int)off[k], m = (int)(off[k + 1] - off[k]);
@@ -991,15 +1002,17 @@ int wall_batch_build(WallBatch &B, const long long *off, int ninst)
         for (int t = 0; t < m; t += kThreads)
             for (int q = 0; q < c; ++q) {
                 const int s0 = b0 + q * chunk, s1 = std::min(b0 + m, s0 + chunk);
-                jobs.push_back({b0 + t, std::min(b0 + m, b0 + t + kThreads), s0, std::max(s0, s1), q});
+                jobs.push_back({b0 + t, std::min(b0 + m, b0 + t + kThreads), s0, std::max(s0, s1), q, k});
             }
     }
     B.njobs = (int)jobs.size();
     B.max_slots = max_slots;
     RMW_CUDA(cudaMalloc(&B.jobs, sizeof(TileJob) * std::max<size_t>(1, jobs.size())));
     RMW_CUDA(cudaMalloc(&B.blob_nch, sizeof(int) * std::max(1, B.n)));
+    RMW_CUDA(cudaMalloc(&B.blob_susp, sizeof(int) * std::max(1, B.n)));
     RMW_CUDA(cudaMemcpy(B.jobs, jobs.data(), sizeof(TileJob) * jobs.size(), cudaMemcpyHostToDevice));
     if (B.n) RMW_CUDA(cudaMemcpy(B.blob_nch, nch.data(), sizeof(int) * B.n, cudaMemcpyHostToDevice));
+    if (B.n) RMW_CUDA(cudaMemcpy(B.blob_susp, bsusp.data(), sizeof(int) * B.n, cudaMemcpyHostToDevice));
     // symmetric UF layout: every suspension's upper triangle of tile pairs,
     // partial sums suspension after suspension
     std::vector<SymJob> sj;
@@ -1041,7 +1054,8 @@ void wall_batch_free(WallBatch &B)
     cudaSetDevice(B.device);
     if (B.jobs) cudaFree(B.jobs);
     if (B.blob_nch) cudaFree(B.blob_nch);
-    for (void *p : {(void *)B.sym_jobs, (void *)B.blob_pbase, (void *)B.blob_pstride, (void *)B.blob_nslots})
+    for (void *p : {(void *)B.sym_jobs, (void *)B.blob_pbase, (void *)B.blob_pstride, (void *)B.blob_nslots,
+                    (void *)B.blob_susp})
         if (p) cudaFree(p);
     cudaSetDevice(cur);
     B.jobs = nullptr;
@@ -1050,6 +1064,7 @@ void wall_batch_free(WallBatch &B)
     B.blob_pbase = nullptr;
     B.blob_pstride = nullptr;
     B.blob_nslots = nullptr;
+    B.blob_susp = nullptr;
 }
 
 int wall_product_batched(const WallBatch &B, int kind, const double *r, const double *v, double *out, double eta,
@@ -1094,8 +1109,9 @@ int wall_product_batched(const WallBatch &B, int kind, const double *r, const do
 // M_UF applied to nrhs vectors (rows of V with stride ldv; outputs rows of Y
 // with stride ldy), mixed precision, kMultiRhs vectors per pass.
 int wall_uf_multi(const double *r, const double *V, long long ldv, double *Y, long long ldy, int nrhs, int n,
-                  double eta, double a, const WallBatch *B, cudaStream_t st)
+                  double eta, double a, const WallBatch *B, cudaStream_t st, const unsigned char *active)
 {
+    if (!B) active = nullptr;
     if (nrhs <= 0 || n <= 0) return RMW_OK;
     const int nchunks = B ? B->max_slots : choose_chunks(n);
     const size_t pos = ((sizeof(SrcF) * (size_t)n + 255) / 256) * 256;
@@ -1114,12 +1130,13 @@ int wall_uf_multi(const double *r, const double *V, long long ldv, double *Y, lo
         pack_multi_kernel<<<(n + 255) / 256, 256, 0, st>>>(r, V + (long long)q0 * ldv, ldv, nr, src, vec, n, a);
         void *tok = nullptr;
         if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
-        if (B) wall_pair_multi_kernel<true><<<grid, kThreads, 0, st>>>(src, vec, n, chunk, partial, B->jobs);
-        else wall_pair_multi_kernel<false><<<grid, kThreads, 0, st>>>(src, vec, n, chunk, partial, nullptr);
+        const unsigned char *act = active ? active + (size_t)(q0 / kMultiRhs) * B->ninst : nullptr;
+        if (B) wall_pair_multi_kernel<true><<<grid, kThreads, 0, st>>>(src, vec, n, chunk, partial, B->jobs, act);
+        else wall_pair_multi_kernel<false><<<grid, kThreads, 0, st>>>(src, vec, n, chunk, partial, nullptr, nullptr);
         if (int rc = trace_end(tok, st)) return rc;
         wall_finalize_multi_kernel<<<dim3((n + 255) / 256, nr), 256, 0, st>>>(
             r, V + (long long)q0 * ldv, ldv, nr, partial, nchunks, Y + (long long)q0 * ldy, ldy, n, a, nf,
-            B ? B->blob_nch : nullptr);
+            B ? B->blob_nch : nullptr, act, B ? B->blob_susp : nullptr);
     }
     RMW_CHECK_LAUNCH("multi-rhs product");
     return RMW_OK;

@@ -9,7 +9,7 @@ namespace rmw {
 // One CTA of a segmented (batched) product: targets [t0, t1) against sources
 // [s0, s1) of the same suspension, partial sums into chunk slot `slot`.
 struct TileJob {
-    int t0, t1, s0, s1, slot;
+    int t0, t1, s0, s1, slot, susp;
 };
 
 // One CTA of a segmented symmetric UF product: tile pair T <= S of the
@@ -30,6 +30,7 @@ struct WallBatch {
     int max_slots = 1;  // chunk slots of the partial-sum buffer
     TileJob *jobs = nullptr;  // device
     int *blob_nch = nullptr;  // device: chunk count of each blob's suspension
+    int *blob_susp = nullptr; // device: suspension of each blob
     // symmetric UF layout: per suspension nt = ceil(n / 128) tiles, nt (nt + 1) / 2 CTAs
     long long nsym = 0;             // CTAs
     long long sym_doubles = 0;      // partial-sum doubles (sum over suspensions of nt * 3n)
@@ -43,8 +44,10 @@ struct WallBatch {
 int wall_batch_build(WallBatch &B, const long long *off_host, int ninst);
 void wall_batch_free(WallBatch &B);
 // M_UF applied to nrhs vectors in mixed precision (rows of V, stride ldv).
+// With a batch and `active` (one byte per suspension and pass of 8 vectors,
+// pass-major), suspensions whose byte is 0 are skipped and get zero rows.
 int wall_uf_multi(const double *r, const double *V, long long ldv, double *Y, long long ldy, int nrhs, int n,
-                  double eta, double a, const WallBatch *B, cudaStream_t st);
+                  double eta, double a, const WallBatch *B, cudaStream_t st, const unsigned char *active = nullptr);
 int wall_product_batched(const WallBatch &B, int kind, const double *r, const double *v, double *out, double eta,
                          double a, int mode, cudaStream_t st);
 

@@ -297,7 +297,7 @@ def solver_metrics(dev, reps=2):
         for _ in range(reps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            sys2.build_pc()
+            sys2.build_pc(mode=mode)
             sol, info, its, rr = integrator.solve_mobility_problem(sys2, FT, tol=1e-8, mode=mode)
             torch.cuda.synchronize()
             dt = time.perf_counter() - t0
@@ -312,7 +312,7 @@ def solver_metrics(dev, reps=2):
     for _ in range(reps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sys2.build_pc()
+        sys2.build_pc(mode="mixed")
         _, _, its_ng, _ = integrator.solve_mobility_problem(sys2, FT, tol=1e-8, mode="mixed")
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
@@ -328,7 +328,7 @@ def solver_metrics(dev, reps=2):
         for _ in range(reps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            sys2.build_pc()
+            sys2.build_pc(mode=mode)
             pairs = model42.attach(sys2, exact_cutoff=3 * R2)
             sol, info, its, rr = integrator.solve_mobility_problem(sys2, FT, tol=1e-8, mode=mode)
             torch.cuda.synchronize()
@@ -496,7 +496,7 @@ def batched_metrics(dev, nrhs=16):
            % (sum(counts), sysb.n_blobs, pairs)}
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    sysb.build_pc(stochastic=True)
+    sysb.build_pc(stochastic=True, mode="mixed")
     torch.cuda.synchronize()
     out["pc_build_ms"] = (time.perf_counter() - t0) * 1e3
     Z = torch.randn(nrhs, 3 * sysb.n_blobs, generator=torch.Generator(device=dev).manual_seed(4),

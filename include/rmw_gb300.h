@@ -241,6 +241,13 @@ int rmw_rigid_set_configuration(void *handle, const double *r_blobs, const doubl
  * build_block_diagonal_preconditioners_det_stoch (multi_bodies.py:480-618).
  * Synchronous; RMW_ERR_NONFINITE if a body matrix is not positive definite. */
 int rmw_rigid_build_pc(void *handle, int stochastic);
+/* The same for the solves of one precision mode: RMW_MODE_MIXED factorises the
+ * body blocks on the FP32 pipe (FP64 runs at 1/64 of its rate on GB300) - an
+ * equally valid block-diagonal preconditioner, convergence still judged by the
+ * FP64-accurate residual; a block that is not positive definite in FP32 makes
+ * it fall back to FP64.  RMW_MODE_FP64 / RMW_MODE_DF64: rmw_rigid_build_pc.
+ * Solves and Lanczos in FP64 or df64 rebuild an FP32-factorised one. */
+int rmw_rigid_build_pc_mode(void *handle, int stochastic, int mode);
 /* y = [[M, -K], [-K^T, 0]] x  (linear_operator_rigid, multi_bodies.py:424-471). */
 int rmw_rigid_apply(void *handle, const double *x, double *y, int mode);
 /* y = P^-1 x  (block_diagonal_preconditioner apply, multi_bodies.py:825-861). */

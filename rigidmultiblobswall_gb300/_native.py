@@ -72,6 +72,7 @@ SIGNATURES = {
     "rmw_rigid_sizes": (_i, [_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
     "rmw_rigid_set_configuration": (_i, [_vp, _vp, _vp]),
     "rmw_rigid_build_pc": (_i, [_vp, _i]),
+    "rmw_rigid_build_pc_mode": (_i, [_vp, _i, _i]),
     "rmw_rigid_apply": (_i, [_vp, _vp, _vp, _i]),
     "rmw_rigid_apply_pc": (_i, [_vp, _vp, _vp]),
     "rmw_rigid_mobility_pc": (_i, [_vp, _vp, _vp, _i]),

@@ -582,8 +582,9 @@ int rmw_rigid_solve(void *sys, const double *rhs, double *sol, double tol, int r
     if (mode != RMW_MODE_FP64 && mode != RMW_MODE_MIXED && mode != RMW_MODE_DF64)
         return rmw::fail(RMW_ERR_ARG, "unknown precision mode");
     RigidSystem &S = *(RigidSystem *)sys;
-    if (!S.pc_ready) {
-        if (int rc = rmw_rigid_build_pc(sys, 0)) return rc;
+    // an FP32-factorised preconditioner serves the mixed solves only
+    if (!S.pc_ready || (S.pc_fp32 && mode != RMW_MODE_MIXED)) {
+        if (int rc = rmw_rigid_build_pc_mode(sys, 0, mode)) return rc;
     }
     const long long n = S.sys_size();
     auto pc = [&](const double *x, double *y) { return rmw::rigid_apply_pc(S, x, y); };
@@ -683,8 +684,8 @@ int rmw_rigid_lanczos(void *sys, const double *z, double *noise, double factor, 
     if (!sys || !z || !noise) return rmw::fail(RMW_ERR_ARG, "null argument");
     if (max_iter < 1) return rmw::fail(RMW_ERR_ARG, "max_iter must be >= 1");
     RigidSystem &S = *(RigidSystem *)sys;
-    if (!S.stoch_ready) {
-        if (int rc = rmw_rigid_build_pc(sys, 1)) return rc;
+    if (!S.stoch_ready || (S.pc_fp32 && mode != RMW_MODE_MIXED)) {
+        if (int rc = rmw_rigid_build_pc_mode(sys, 1, mode)) return rc;
     }
     auto op_direct = [&](const double *x, double *y) { return rmw::rigid_mobility_pc(S, x, y, mode); };
     const long long n = 3LL * S.n;

@@ -624,8 +624,9 @@ int rmw_rigid_solve_batched(void *sys, const double *rhs, double *sol, double to
     if (!(tol > 0)) return rmw::fail(RMW_ERR_ARG, "tolerance must be positive");
     if (mode != RMW_MODE_FP64 && mode != RMW_MODE_MIXED && mode != RMW_MODE_DF64)
         return rmw::fail(RMW_ERR_ARG, "unknown precision mode");
-    if (!S.pc_ready) {
-        if (int rc = rmw_rigid_build_pc(sys, 0)) return rc;
+    // an FP32-factorised preconditioner serves the mixed solves only
+    if (!S.pc_ready || (S.pc_fp32 && mode != RMW_MODE_MIXED)) {
+        if (int rc = rmw_rigid_build_pc_mode(sys, 0, mode)) return rc;
     }
     const int nseg = (int)S.susp_off.size() - 1;
     const long long n = S.sys_size();
@@ -746,8 +747,8 @@ int rmw_rigid_lanczos_batched(void *sys, const double *Z, double *noise, int nrh
     if (nrhs < 1 || max_iter < 1) return rmw::fail(RMW_ERR_ARG, "nrhs and max_iter must be positive");
     RigidSystem &S = *(RigidSystem *)sys;
     if (!S.batch) return rmw::fail(RMW_ERR_ARG, "call rmw_rigid_set_suspensions first");
-    if (!S.stoch_ready) {
-        if (int rc = rmw_rigid_build_pc(sys, 1)) return rc;
+    if (!S.stoch_ready || (S.pc_fp32 && mode != RMW_MODE_MIXED)) {
+        if (int rc = rmw_rigid_build_pc_mode(sys, 1, mode)) return rc;
     }
     const int nsusp = (int)S.susp_body_off.size() - 1;
     const long long N3 = 3LL * S.n;

@@ -12,6 +12,9 @@
 
 namespace rmw {
 
+// T = float evaluates the pair block in FP32 (from FP64 position differences):
+// the preconditioner blocks of the mixed-precision solves.
+template <typename T = double>
 __device__ __forceinline__ void uf_block(const double *__restrict__ r, int i, int j, double a, bool wall,
                                          double blk[3][3], double *scale)
 {
@@ -31,13 +34,13 @@ __device__ __forceinline__ void uf_block(const double *__restrict__ r, int i, in
             blk[2][2] = 4.0 / 3.0 - (9.0 * iz - 4.0 * iz3 + iz5) / 6.0;
             return;
         }
-        const double dx = (r[3 * i] - r[3 * j]) * inva, dy = (r[3 * i + 1] - r[3 * j + 1]) * inva;
-        const double dz = (zie - zje) * inva;
-        const double hi = zie * inva, hj = zje * inva, Rz = (zie + zje) * inva;
+        const T dx = (T)((r[3 * i] - r[3 * j]) * inva), dy = (T)((r[3 * i + 1] - r[3 * j + 1]) * inva);
+        const T dz = (T)((zie - zje) * inva);
+        const T hi = (T)(zie * inva), hj = (T)(zje * inva), Rz = (T)((zie + zje) * inva);
         for (int w = 0; w < 3; ++w) {
-            double c[3] = {0.0, 0.0, 0.0};
-            pair_contrib<RMW_UF, double>(dx, dy, dz, Rz, hi, hj, w == 0 ? 1.0 : 0.0, w == 1 ? 1.0 : 0.0,
-                                         w == 2 ? 1.0 : 0.0, c[0], c[1], c[2]);
+            T c[3] = {T(0), T(0), T(0)};
+            pair_contrib<RMW_UF, T>(dx, dy, dz, Rz, hi, hj, w == 0 ? T(1) : T(0), w == 1 ? T(1) : T(0),
+                                    w == 2 ? T(1) : T(0), c[0], c[1], c[2]);
             blk[0][w] = c[0];
             blk[1][w] = c[1];
             blk[2][w] = c[2];
@@ -48,12 +51,12 @@ __device__ __forceinline__ void uf_block(const double *__restrict__ r, int i, in
         blk[0][0] = blk[1][1] = blk[2][2] = 4.0 / 3.0;
         return;
     }
-    const double dx = (r[3 * i] - r[3 * j]) * inva, dy = (r[3 * i + 1] - r[3 * j + 1]) * inva,
-                 dz = (r[3 * i + 2] - r[3 * j + 2]) * inva;
+    const T dx = (T)((r[3 * i] - r[3 * j]) * inva), dy = (T)((r[3 * i + 1] - r[3 * j + 1]) * inva),
+            dz = (T)((r[3 * i + 2] - r[3 * j + 2]) * inva);
     for (int w = 0; w < 3; ++w) {
-        double c[3] = {0.0, 0.0, 0.0};
-        pair_rpy<RMW_UF, double>(dx, dy, dz, w == 0 ? 1.0 : 0.0, w == 1 ? 1.0 : 0.0, w == 2 ? 1.0 : 0.0, c[0], c[1],
-                                 c[2]);
+        T c[3] = {T(0), T(0), T(0)};
+        pair_rpy<RMW_UF, T>(dx, dy, dz, w == 0 ? T(1) : T(0), w == 1 ? T(1) : T(0), w == 2 ? T(1) : T(0), c[0], c[1],
+                            c[2]);
         blk[0][w] = c[0];
         blk[1][w] = c[1];
         blk[2][w] = c[2];

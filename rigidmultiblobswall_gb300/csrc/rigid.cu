@@ -28,6 +28,7 @@ namespace rmw {
 
 constexpr int kRigidThreads = 256;
 constexpr int kSmemMaxM = 160;
+constexpr int kSmemMaxM32 = 224;  // FP32 factorisation in shared memory up to 224 x 224 (196 KB)
 
 // ---------------------------------------------------------------------------
 // K and K^T
@@ -81,6 +82,7 @@ __global__ void kt_times_lambda_kernel(const double *__restrict__ r, const doubl
 
 // ---------------------------------------------------------------------------
 // dense per-body wall mobility M_b = nf * B M~(z_eff) B (row-major m x m)
+template <typename T>
 __global__ void body_mobility_kernel(const double *__restrict__ r, const int *__restrict__ boff,
                                      const long long *__restrict__ moff, double *__restrict__ M, double eta,
                                      double a)
@@ -92,7 +94,7 @@ __global__ void body_mobility_kernel(const double *__restrict__ r, const int *__
     for (int pq = threadIdx.x; pq < nbl * nbl; pq += blockDim.x) {
         const int p = pq / nbl, q = pq % nbl;
         double blk[3][3], sc;
-        uf_block(r, o + p, o + q, a, true, blk, &sc);
+        uf_block<T>(r, o + p, o + q, a, true, blk, &sc);
         sc *= nf;
         for (int u = 0; u < 3; ++u)
             for (int w = 0; w < 3; ++w) Mb[(long long)(3 * p + u) * m + 3 * q + w] = sc * blk[u][w];
@@ -101,6 +103,7 @@ __global__ void body_mobility_kernel(const double *__restrict__ r, const int *__
 
 // Free-space variant (no wall, no regularisation): the blocks of
 // rotne_prager_tensor (mobility/mobility.py:967-1015).
+template <typename T>
 __global__ void body_mobility_free_kernel(const double *__restrict__ r, const int *__restrict__ boff,
                                           const long long *__restrict__ moff, double *__restrict__ M, double eta,
                                           double a)
@@ -112,7 +115,7 @@ __global__ void body_mobility_free_kernel(const double *__restrict__ r, const in
     for (int pq = threadIdx.x; pq < nbl * nbl; pq += blockDim.x) {
         const int p = pq / nbl, q = pq % nbl;
         double blk[3][3], sc;
-        uf_block(r, o + p, o + q, a, false, blk, &sc);
+        uf_block<T>(r, o + p, o + q, a, false, blk, &sc);
         for (int u = 0; u < 3; ++u)
             for (int w = 0; w < 3; ++w) Mb[(long long)(3 * p + u) * m + 3 * q + w] = nf * blk[u][w];
     }
@@ -122,19 +125,26 @@ __global__ void body_mobility_free_kernel(const double *__restrict__ r, const in
 // Cholesky + inverse of every M_b.  A (m x m, row-major) is the working copy
 // (shared memory or global); on exit minv holds M_b^-1, and lfac / linv (if
 // non-null) hold L and L^-1 (lower triangles, upper zero).
-__device__ void factor_and_invert(double *A, int m, double *tmp, double *minv, double *lfac, double *linv,
-                                  int *status)
+template <typename T> __device__ __forceinline__ T fsqrt(T x);
+template <> __device__ __forceinline__ double fsqrt<double>(double x) { return sqrt(fmax(x, 1e-300)); }
+template <> __device__ __forceinline__ float fsqrt<float>(float x) { return sqrtf(fmaxf(x, 1e-30f)); }
+
+// T = float: the preconditioner of the mixed-precision solves (a different but
+// equally valid block-diagonal P; the FP64-accurate refinement residual
+// decides convergence), factorised on the FP32 pipe; results stored as double.
+template <typename T>
+__device__ void factor_and_invert(T *A, int m, T *tmp, double *minv, double *lfac, double *linv, int *status)
 {
     const int tid = threadIdx.x, nt = blockDim.x;
     // right-looking Cholesky, lower triangle
     for (int k = 0; k < m; ++k) {
         if (tid == 0) {
-            const double d = A[k * m + k];
-            if (!(d > 0.0)) atomicExch(status, 1);  // not positive definite
-            A[k * m + k] = sqrt(fmax(d, 1e-300));
+            const T d = A[k * m + k];
+            if (!(d > T(0))) atomicExch(status, 1);  // not positive definite
+            A[k * m + k] = fsqrt<T>(d);
         }
         __syncthreads();
-        const double dk = A[k * m + k];
+        const T dk = A[k * m + k];
         for (int i = k + 1 + tid; i < m; i += nt) A[i * m + k] /= dk;
         __syncthreads();
         const int t = m - k - 1;
@@ -146,17 +156,17 @@ __device__ void factor_and_invert(double *A, int m, double *tmp, double *minv, d
     }
     for (int idx = tid; idx < m * m; idx += nt) {
         const int i = idx / m, j = idx % m;
-        if (j > i) A[idx] = 0.0;
-        if (lfac) lfac[idx] = (j > i) ? 0.0 : A[idx];
+        if (j > i) A[idx] = T(0);
+        if (lfac) lfac[idx] = (j > i) ? 0.0 : (double)A[idx];
     }
     __syncthreads();
     // in-place inverse of the lower-triangular L, column by column from the right
     for (int j = m - 1; j >= 0; --j) {
-        const double ajj = 1.0 / A[j * m + j];
+        const T ajj = T(1) / A[j * m + j];
         for (int k = j + 1 + tid; k < m; k += nt) tmp[k] = A[k * m + j];
         __syncthreads();
         for (int i = j + 1 + tid; i < m; i += nt) {
-            double s = 0.0;
+            T s = T(0);
             for (int k = j + 1; k <= i; ++k) s += A[i * m + k] * tmp[k];
             A[i * m + j] = -ajj * s;
         }
@@ -164,31 +174,33 @@ __device__ void factor_and_invert(double *A, int m, double *tmp, double *minv, d
         __syncthreads();
     }
     if (linv)
-        for (int idx = tid; idx < m * m; idx += nt) linv[idx] = A[idx];
+        for (int idx = tid; idx < m * m; idx += nt) linv[idx] = (double)A[idx];
     // M^-1 = L^-T L^-1 : minv[i][j] = sum_{k >= max(i,j)} X[k][i] X[k][j]
     for (int idx = tid; idx < m * m; idx += nt) {
         const int i = idx / m, j = idx % m;
         if (j < i) continue;
-        double s = 0.0;
+        T s = T(0);
         for (int k = j; k < m; ++k) s += A[k * m + i] * A[k * m + j];
-        minv[(long long)i * m + j] = s;
-        minv[(long long)j * m + i] = s;
+        minv[(long long)i * m + j] = (double)s;
+        minv[(long long)j * m + i] = (double)s;
     }
 }
 
+template <typename T>
 __global__ void pc_factor_smem_kernel(const double *__restrict__ M, const long long *__restrict__ moff,
                                       const int *__restrict__ boff, double *__restrict__ minv, double *lfac,
                                       double *linv, int *status)
 {
-    extern __shared__ double sm[];
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T *sm = (T *)smraw;
     const int b = blockIdx.x;
     const int m = 3 * (boff[b + 1] - boff[b]);
-    double *A = sm, *tmp = sm + m * m;
+    T *A = sm, *tmp = sm + m * m;
     const double *Mb = M + moff[b];
-    for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) A[idx] = Mb[idx];
+    for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) A[idx] = (T)Mb[idx];
     __syncthreads();
-    factor_and_invert(A, m, tmp, minv + moff[b], lfac ? lfac + moff[b] : nullptr, linv ? linv + moff[b] : nullptr,
-                      status);
+    factor_and_invert<T>(A, m, tmp, minv + moff[b], lfac ? lfac + moff[b] : nullptr, linv ? linv + moff[b] : nullptr,
+                         status);
 }
 
 // global-memory variant: M is overwritten (it is the working copy), tmp is m doubles per body
@@ -198,8 +210,8 @@ __global__ void pc_factor_global_kernel(double *__restrict__ M, const long long 
 {
     const int b = blockIdx.x;
     const int m = 3 * (boff[b + 1] - boff[b]);
-    factor_and_invert(M + moff[b], m, tmpg + 3 * boff[b], minv + moff[b], lfac ? lfac + moff[b] : nullptr,
-                      linv ? linv + moff[b] : nullptr, status);
+    factor_and_invert<double>(M + moff[b], m, tmpg + 3 * boff[b], minv + moff[b], lfac ? lfac + moff[b] : nullptr,
+                              linv ? linv + moff[b] : nullptr, status);
 }
 
 // M^-1 K (m x 6) and N = (K^T M^-1 K)^-1 (6 x 6) per body
@@ -428,7 +440,7 @@ __global__ void count_below_kernel(const double *__restrict__ r, int n, double z
 
 // ---------------------------------------------------------------------------
 // host side
-static int build_pc(RigidSystem &S, bool stochastic)
+static int build_pc(RigidSystem &S, bool stochastic, bool fp32 = false)
 {
     cudaStream_t st = S.st;
     const long long tot = S.moff_h[S.nb];
@@ -448,13 +460,25 @@ static int build_pc(RigidSystem &S, bool stochastic)
         RMW_CUDA(cudaMalloc(&S.linv, sizeof(double) * tot));
     }
     RMW_CUDA(cudaMemsetAsync(S.dstatus, 0, sizeof(int), st));
-    if (S.wall) body_mobility_kernel<<<S.nb, kRigidThreads, 0, st>>>(S.r, S.boff, S.moff, M, S.eta, S.a);
-    else body_mobility_free_kernel<<<S.nb, kRigidThreads, 0, st>>>(S.r, S.boff, S.moff, M, S.eta, S.a);
+    if (fp32 && S.max_m > kSmemMaxM32) fp32 = false;
+    if (fp32) {
+        if (S.wall) body_mobility_kernel<float><<<S.nb, kRigidThreads, 0, st>>>(S.r, S.boff, S.moff, M, S.eta, S.a);
+        else body_mobility_free_kernel<float><<<S.nb, kRigidThreads, 0, st>>>(S.r, S.boff, S.moff, M, S.eta, S.a);
+    } else {
+        if (S.wall) body_mobility_kernel<double><<<S.nb, kRigidThreads, 0, st>>>(S.r, S.boff, S.moff, M, S.eta, S.a);
+        else body_mobility_free_kernel<double><<<S.nb, kRigidThreads, 0, st>>>(S.r, S.boff, S.moff, M, S.eta, S.a);
+    }
     double *lf = stochastic ? S.lfac : nullptr, *li = stochastic ? S.linv : nullptr;
-    if (S.max_m <= kSmemMaxM) {
+    if (fp32) {
+        const size_t sm = sizeof(float) * ((size_t)S.max_m * S.max_m + S.max_m);
+        RMW_CUDA(cudaFuncSetAttribute(pc_factor_smem_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sm));
+        pc_factor_smem_kernel<float><<<S.nb, kRigidThreads, sm, st>>>(M, S.moff, S.boff, S.minv, lf, li, S.dstatus);
+    } else if (S.max_m <= kSmemMaxM) {
         const size_t sm = sizeof(double) * ((size_t)S.max_m * S.max_m + S.max_m);
-        RMW_CUDA(cudaFuncSetAttribute(pc_factor_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        pc_factor_smem_kernel<<<S.nb, kRigidThreads, sm, st>>>(M, S.moff, S.boff, S.minv, lf, li, S.dstatus);
+        RMW_CUDA(cudaFuncSetAttribute(pc_factor_smem_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sm));
+        pc_factor_smem_kernel<double><<<S.nb, kRigidThreads, sm, st>>>(M, S.moff, S.boff, S.minv, lf, li, S.dstatus);
     } else {
         pc_factor_global_kernel<<<S.nb, kRigidThreads, 0, st>>>(M, S.moff, S.boff, S.minv, lf, li, tmpg, S.dstatus);
     }
@@ -464,10 +488,12 @@ static int build_pc(RigidSystem &S, bool stochastic)
     RMW_CUDA(cudaMemcpyAsync(&hstat, S.dstatus, sizeof(int), cudaMemcpyDeviceToHost, st));
     RMW_CUDA(cudaFreeAsync(ws, st));
     RMW_CUDA(cudaStreamSynchronize(st));
+    if (hstat != 0 && fp32) return build_pc(S, stochastic, false);  // FP32 factorisation failed: FP64 instead
     if (hstat == 1) return fail(RMW_ERR_NONFINITE, "body mobility matrix is not positive definite (Cholesky failed)");
     if (hstat == 2) return fail(RMW_ERR_NONFINITE, "singular 6x6 body resistance K^T M^-1 K");
     S.pc_ready = true;
     S.stoch_ready = stochastic;
+    S.pc_fp32 = fp32;
     return RMW_OK;
 }
 
@@ -697,6 +723,18 @@ int rmw_rigid_build_pc(void *sys, int stochastic)
     return rmw::build_pc(*(RigidSystem *)sys, stochastic != 0);
 }
 
+// As rmw_rigid_build_pc for the solves of one precision mode: RMW_MODE_MIXED
+// factorises the body blocks on the FP32 pipe (the FP64 pipe runs at 1/64 of
+// it on GB300); a block that is not positive definite in FP32 makes it fall
+// back to FP64.  Convergence is still judged by the FP64-accurate residual.
+int rmw_rigid_build_pc_mode(void *sys, int stochastic, int mode)
+{
+    if (!sys) return rmw::fail(RMW_ERR_ARG, "null handle");
+    if (mode != RMW_MODE_FP64 && mode != RMW_MODE_MIXED && mode != RMW_MODE_DF64)
+        return rmw::fail(RMW_ERR_ARG, "unknown precision mode");
+    return rmw::build_pc(*(RigidSystem *)sys, stochastic != 0, mode == RMW_MODE_MIXED);
+}
+
 int rmw_rigid_apply(void *sys, const double *x, double *y, int mode)
 {
     if (!sys || !x || !y) return rmw::fail(RMW_ERR_ARG, "null argument");
@@ -789,9 +827,9 @@ int rmw_rigid_body_mobility(void *sys, double *out)
     if (!sys || !out) return rmw::fail(RMW_ERR_ARG, "null argument");
     RigidSystem *S = (RigidSystem *)sys;
     if (S->wall)
-        rmw::body_mobility_kernel<<<S->nb, rmw::kRigidThreads, 0, S->st>>>(S->r, S->boff, S->moff, out, S->eta, S->a);
+        rmw::body_mobility_kernel<double><<<S->nb, rmw::kRigidThreads, 0, S->st>>>(S->r, S->boff, S->moff, out, S->eta, S->a);
     else
-        rmw::body_mobility_free_kernel<<<S->nb, rmw::kRigidThreads, 0, S->st>>>(S->r, S->boff, S->moff, out, S->eta,
+        rmw::body_mobility_free_kernel<double><<<S->nb, rmw::kRigidThreads, 0, S->st>>>(S->r, S->boff, S->moff, out, S->eta,
                                                                                S->a);
     RMW_CHECK_LAUNCH("body mobility");
     return RMW_OK;

@@ -34,6 +34,7 @@ struct RigidSystem {
     int *dstatus = nullptr;        // device status word
     double *tmp3n = nullptr;       // 3n scratch vector
     bool pc_ready = false, stoch_ready = false;
+    bool pc_fp32 = false;  // body blocks factorised in FP32 (preconditioner of the mixed solves)
     bool wall = true;  // false: free-space (no-wall) mobility (rmw_rigid_set_wall)
     // independent suspensions inside the handle (rmw_rigid_set_suspensions):
     // segmented pair products and the instance-major permutation

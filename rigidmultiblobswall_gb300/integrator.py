@@ -80,7 +80,7 @@ class BrownianStepper:
         for _ in range(max_retries):
             r = self.r_vectors()
             s.set_configuration(r, self.x)
-            s.build_pc(stochastic=True)
+            s.build_pc(stochastic=True, mode=self.mode)
             zz = z if z is not None else torch.randn(3 * s.n_blobs, generator=self.gen, dtype=torch.float64,
                                                      device=s.device)
             noise, it_l = s.lanczos(zz, factor=math.sqrt(2.0 * self.kT / dt), tol=self.lanczos_tol,
@@ -233,7 +233,7 @@ class QuaternionIntegrator:
         factorisations the Lanczos noise needs."""
         S.set_configuration(S.blob_positions(x, q, self.r_ref), x)
         if stochastic:
-            S.build_pc(stochastic=True)
+            S.build_pc(stochastic=True, mode=self.mode)
         return S
 
     def _move(self, x, q, vel, scale, length_scaled=False):

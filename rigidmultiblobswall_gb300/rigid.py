@@ -88,10 +88,12 @@ class RigidSystem:
         with torch.cuda.device(self.device):
             _native.call("rmw_rigid_set_configuration", self._h, r.data_ptr(), x.data_ptr())
 
-    def build_pc(self, stochastic=False):
+    def build_pc(self, stochastic=False, mode="fp64"):
+        """Block-diagonal preconditioner(s) at the current configuration; mode
+        'mixed' factorises the body blocks in FP32 for the mixed solves."""
         import torch
         with torch.cuda.device(self.device):
-            _native.call("rmw_rigid_build_pc", self._h, 1 if stochastic else 0)
+            _native.call("rmw_rigid_build_pc_mode", self._h, 1 if stochastic else 0, _mode(mode))
 
     # -- operators -------------------------------------------------------------
     def _out(self, n):

@@ -181,3 +181,30 @@ def test_solver_error_paths(cuda_device):
     s2.build_pc()
     x, info, its, rr = s2.solve(np.random.default_rng(0).standard_normal(s2.size), tol=1e-14, maxiter=1)
     assert info == 1 and its == 1 and rr > 1e-14
+
+
+def test_fp32_preconditioner_for_mixed_solves(cuda_device):
+    """build_pc(mode='mixed') factorises the body blocks in FP32: the mixed
+    solve still reaches the FP64 residual bar with the same body velocities,
+    and an FP64 solve afterwards rebuilds the FP64 preconditioner (same
+    iterations and solution as with a fresh FP64 build)."""
+    susp = S.shells_42_256(n_bodies=24, seed=12)
+    r = susp.r_vectors()
+    s = RigidSystem([42] * 24, susp.eta, susp.a)
+    s.set_configuration(r, susp.locations)
+    FT = np.zeros((24, 6))
+    FT[:, 2] = -1.0
+    rhs = np.concatenate([np.zeros(3 * s.n_blobs), -FT.flatten()])
+    o = orc.Rigid(r, susp.locations, s.offsets, susp.eta, susp.a)
+    s.build_pc(mode="fp64")
+    x64, info64, it64, _ = integrator.solve_mobility_problem(s, FT, tol=1e-8, mode="fp64")
+    s.build_pc(mode="mixed")
+    xm, infom, itm, _ = integrator.solve_mobility_problem(s, FT, tol=1e-8, mode="mixed")
+    assert infom == 0 and abs(itm - it64) <= 2
+    xm = xm.cpu().numpy()
+    assert np.linalg.norm(rhs - o.apply(xm)) <= 1.05e-8 * np.linalg.norm(rhs)
+    assert rel_err(xm[3 * s.n_blobs:], x64.cpu().numpy()[3 * s.n_blobs:]) <= 1e-6
+    s.build_pc(mode="mixed")
+    x2, info2, it2, _ = integrator.solve_mobility_problem(s, FT, tol=1e-8, mode="fp64")
+    assert info2 == 0 and it2 == it64
+    assert rel_err(x2.cpu().numpy(), x64.cpu().numpy()) <= 1e-12

@@ -220,6 +220,7 @@ __device__ __forceinline__ void pair_uf_sym_df(df dx, df dy, df dz, df Rz, df hi
     const df f4 = TWO_THIRDS * (hj * s2 * 3.0f - (ez * s5) * 10.0f);
     const df f5 = -FOUR_THIRDS * mad((sqr(hj) + E) * 3.0f, s3, (2.0f - E * 15.0f) * s5);
     const df Af = A + f1;
+    const df Af5 = Af + f5;  // the zz diagonal: Af + f5
     const df f2s = f2 * s;
     {  // M_ij v_j
         const df Pxy = mad2(dx, vx, dy, vy);
@@ -230,7 +231,7 @@ __device__ __forceinline__ void pair_uf_sym_df(df dx, df dy, df dz, df Rz, df hi
         const df G = Gr + Gw;
         ux = mad2(Af, vx, G, dx);
         uy = mad2(Af, vy, G, dy);
-        uz = mad2(Af, vz, Gr, dz) + mad2(Gw, Rz, f4 * W, s) + f5 * vz;
+        uz = mad2(Af5, vz, Gr, dz) + mad2(Gw, Rz, f4 * W, s);
     }
     {  // M_ij^T v_i
         const df Pxy = mad2(dx, qx, dy, qy);
@@ -241,7 +242,7 @@ __device__ __forceinline__ void pair_uf_sym_df(df dx, df dy, df dz, df Rz, df hi
         const df G = Gr + Gw;
         wx = mad2(Af, qx, G, dx);
         wy = mad2(Af, qy, G, dy);
-        wz = mad2(Af, qz, Gr, dz) + mad2(Gw, Rz, f3 * W, s) + f5 * qz;
+        wz = mad2(Af5, qz, Gr, dz) + mad2(Gw, Rz, f3 * W, s);
     }
 }
 

@@ -11,9 +11,11 @@
 // products, which come back with the per-step convergence check.
 //
 // Mixed precision: the inner GMRES applies the FP32-pair operator; an outer
-// iterative-refinement loop recomputes the residual with the FP64 operator
-// and stops on the FP64 residual, so the returned solution meets the same
-// relative-residual tolerance as a plain FP64 solve.
+// iterative-refinement loop recomputes the residual with the FP64-accurate
+// operator and stops on that residual, so the returned solution meets the
+// same relative-residual tolerance as a plain FP64 solve.  Once the residual
+// is small the loop updates it by the recurrence r <- r - A32 d instead
+// (refine_by_recurrence in rigid.cuh).
 //
 // Lanczos: stochastic_forcing/stochastic_forcing.py:112-264 (Ando et al. 2012):
 // three-term recurrence, one full reorthogonalisation pass against every
@@ -610,11 +612,12 @@ int rmw_rigid_solve(void *sys, const double *rhs, double *sol, double tol, int r
                                 nullptr);
     }
     // mixed: inner GMRES on the FP32-pair operator; the refinement residual
-    // b - A x uses the FP64-accurate double-float operator (<= 1e-12 against FP64)
+    // b - A x uses the FP64-accurate double-float operator (<= 1e-12 against
+    // FP64), or the recurrence r - A32 d once it is small enough
     auto op32 = [&](const double *x, double *y) { return rmw::rigid_apply(S, x, y, RMW_MODE_MIXED); };
-    double *buf = nullptr;  // x, r, d
-    RMW_CUDA(cudaMallocAsync(&buf, sizeof(double) * 3 * n, S.st));
-    double *x = buf, *r = buf + n, *d = buf + 2 * n;
+    double *buf = nullptr;  // x, r, d, A32 d
+    RMW_CUDA(cudaMallocAsync(&buf, sizeof(double) * 4 * n, S.st));
+    double *x = buf, *r = buf + n, *d = buf + 2 * n, *ad = buf + 3 * n;
     RMW_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, S.st));
     RMW_CUDA(cudaMemcpyAsync(r, rhs, sizeof(double) * n, cudaMemcpyDeviceToDevice, S.st));
     std::vector<double> hb(1);
@@ -658,9 +661,15 @@ int rmw_rigid_solve(void *sys, const double *rhs, double *sol, double tol, int r
         total += it;
         if (rc != RMW_OK && rc != RMW_ERR_NOT_CONVERGED) return rc;
         rmw::axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S.st>>>(d, x, n, 1.0, 1.0);
-        // r = b - A x with the FP64-accurate operator
-        if (int rc2 = rmw::rigid_apply(S, x, r, RMW_MODE_DF64)) return rc2;
-        rmw::axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S.st>>>(rhs, r, n, 1.0, -1.0);
+        if (rmw::refine_by_recurrence(relres, tol)) {
+            // r = r - A32 d
+            if (int rc2 = rmw::rigid_apply(S, d, ad, RMW_MODE_MIXED)) return rc2;
+            rmw::axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S.st>>>(ad, r, n, -1.0, 1.0);
+        } else {
+            // r = b - A x with the FP64-accurate operator
+            if (int rc2 = rmw::rigid_apply(S, x, r, RMW_MODE_DF64)) return rc2;
+            rmw::axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S.st>>>(rhs, r, n, 1.0, -1.0);
+        }
         if (total >= maxiter) {
             if (int rc3 = norm(r, &rnorm)) return rc3;
             relres = rnorm / bnorm;

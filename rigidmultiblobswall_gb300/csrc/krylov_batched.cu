@@ -632,8 +632,9 @@ int rmw_rigid_solve_batched(void *sys, const double *rhs, double *sol, double to
     const long long n = S.sys_size();
     cudaStream_t st = S.st;
     double *buf = nullptr;
-    RMW_CUDA(cudaMallocAsync(&buf, sizeof(double) * n * 6, st));
+    RMW_CUDA(cudaMallocAsync(&buf, sizeof(double) * n * 7, st));
     double *gx = buf, *gy = buf + n, *bim = buf + 2 * n, *xim = buf + 3 * n, *rim = buf + 4 * n, *dim = buf + 5 * n;
+    double *adim = buf + 6 * n;  // A32 d of the residual recurrence
     const unsigned pg = (unsigned)((n + 255) / 256);
     // S.st, not st: inside a graph capture the handle's stream is redirected
     auto to_global = [&](const double *xi, double *xg) { rmw::permute_kernel<<<pg, 256, 0, S.st>>>(xi, xg, S.perm, n, 1); };
@@ -676,7 +677,9 @@ int rmw_rigid_solve_batched(void *sys, const double *rhs, double *sol, double to
         tot = it;
     } else {
         // per-suspension iterative refinement: inner GMRES on the FP32-pair
-        // operator, residual with the FP64-accurate double-float operator
+        // operator, residual with the FP64-accurate double-float operator, or
+        // by the recurrence r - A32 d once every pending suspension's residual
+        // is small enough (refine_by_recurrence)
         RMW_CUDA(cudaMemsetAsync(xim, 0, sizeof(double) * n, st));
         RMW_CUDA(cudaMemcpyAsync(rim, bim, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
         rmw::SegOps O;
@@ -688,20 +691,28 @@ int rmw_rigid_solve_batched(void *sys, const double *rhs, double *sol, double to
             for (int k = 0; k < nseg; ++k) bn[k] = std::sqrt(O.h(k, 0));
             rr.assign(nseg, 0.0);
             stt.assign(nseg, RMW_ERR_NOT_CONVERGED);
+            std::vector<char> finished(nseg, 0);
             for (int outer = 0; outer < 8; ++outer) {
                 if ((rc = O.norm2(rim, 1))) goto done;
                 if ((rc = O.fetch())) goto done;
                 std::vector<double> itol(nseg, 1.0);
                 int pending = 0;
+                bool recurrence = true;
                 for (int k = 0; k < nseg; ++k) {
+                    if (finished[k]) {  // residual, status and count stay as they were
+                        O.h(k, 2) = 0.0;
+                        continue;
+                    }
                     const double rn = std::sqrt(O.h(k, 1));
                     rr[k] = bn[k] > 0 ? rn / bn[k] : 0.0;
                     const bool ok = rr[k] <= tol;
                     if (ok) stt[k] = RMW_OK;
                     const bool stop = ok || tot[k] >= maxiter;
+                    finished[k] = stop;
                     O.h(k, 2) = stop ? 0.0 : 1.0;  // freeze finished suspensions (zero their residual)
                     itol[k] = stop ? 1.0 : std::max(1e-5, 0.5 * tol * bn[k] / std::max(rn, 1e-300));
                     pending += !stop;
+                    if (!stop) recurrence = recurrence && rmw::refine_by_recurrence(rr[k], tol);
                 }
                 if (!pending) break;
                 if ((rc = O.put())) goto done;
@@ -713,8 +724,14 @@ int rmw_rigid_solve_batched(void *sys, const double *rhs, double *sol, double to
                 if (rc) goto done;
                 for (int k = 0; k < nseg; ++k) tot[k] += it[k];
                 if ((rc = O.axpby(dim, xim, 1.0, 1.0))) goto done;
-                if ((rc = op_mode(RMW_MODE_DF64)(xim, rim))) goto done;
-                if ((rc = O.axpby(bim, rim, 1.0, -1.0))) goto done;
+                if (recurrence) {
+                    // finished suspensions have r = 0 and d = 0 here and keep r = 0
+                    if ((rc = op_mode(RMW_MODE_MIXED)(dim, adim))) goto done;
+                    if ((rc = O.axpby(adim, rim, -1.0, 1.0))) goto done;
+                } else {
+                    if ((rc = op_mode(RMW_MODE_DF64)(xim, rim))) goto done;
+                    if ((rc = O.axpby(bim, rim, 1.0, -1.0))) goto done;
+                }
             }
         }
     }

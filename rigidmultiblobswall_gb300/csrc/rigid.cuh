@@ -85,4 +85,19 @@ int nearfield_apply_pc(RigidSystem &S, const double *x, double *y);
 // M v on the handle's blobs (segmented by suspension when suspensions are set).
 int rigid_mobility(RigidSystem &S, const double *v, double *y, int mode);
 
+// Iterative refinement x <- x + d after a residual r = b - A x computed with
+// the FP64-accurate operator: the next residual is either recomputed the same
+// way or updated as r - A32 d with the FP32-pair operator A32.  The update
+// drifts from the true residual by (A - A32) d.  The FP32-pair products are
+// within 1e-6 (relative 2-norm) of FP64 and d solves A32 d = r to the inner
+// tolerance, so the drift is about 1e-6 |r| for a well-conditioned
+// preconditioned system.  kRecurrenceDrift = 1e-5 takes ten times that as
+// the bound, and the recurrence is used only while the bound stays below a
+// tenth of the tolerance: |r| / |b| <= 1e4 tol (1e-4 at tol = 1e-8).  Below
+// that the double-float product of a full refinement step (the dominant cost
+// of a mixed solve next to the FP32 Krylov iterations) is replaced by one
+// FP32-pair product.
+constexpr double kRecurrenceDrift = 1e-5;
+inline bool refine_by_recurrence(double relres, double tol) { return relres * kRecurrenceDrift <= 0.1 * tol; }
+
 }  // namespace rmw

@@ -183,6 +183,27 @@ def test_solver_error_paths(cuda_device):
     assert info == 1 and its == 1 and rr > 1e-14
 
 
+@pytest.mark.parametrize("tol", [1e-6, 1e-8, 1e-11])
+def test_mixed_refinement_reports_the_true_residual(cuda_device, tol):
+    """The mixed refinement updates its residual as r - A32 d (FP32-pair
+    product of the correction) once |r| / |b| <= 1e4 tol, instead of
+    recomputing b - A x in double-float: the reported relative residual stays
+    within a tenth of the tolerance of the oracle's FP64 residual of the
+    returned solution, which meets the tolerance."""
+    susp = S.shells_42_256(n_bodies=20, seed=21)
+    r = susp.r_vectors()
+    s = RigidSystem([42] * 20, susp.eta, susp.a)
+    s.set_configuration(r, susp.locations)
+    FT = np.random.default_rng(4).standard_normal((20, 6))
+    rhs = np.concatenate([np.zeros(3 * s.n_blobs), -FT.flatten()])
+    o = orc.Rigid(r, susp.locations, s.offsets, susp.eta, susp.a)
+    sol, info, its, rr = integrator.solve_mobility_problem(s, FT, tol=tol, mode="mixed")
+    true_rr = np.linalg.norm(rhs - o.apply(sol.cpu().numpy())) / np.linalg.norm(rhs)
+    assert info == 0 and rr <= tol
+    assert true_rr <= 1.05 * tol
+    assert abs(rr - true_rr) <= 0.1 * tol
+
+
 def test_fp32_preconditioner_for_mixed_solves(cuda_device):
     """build_pc(mode='mixed') factorises the body blocks in FP32: the mixed
     solve still reaches the FP64 residual bar with the same body velocities,

@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--large", action="store_true",
                    help="only run the 4096-shell (172,032-blob) solve comparison and print its JSON line")
     p.add_argument("--large-modes", default="mixed+nf,mixed,df64,fp64")
+    p.add_argument("--multi", default=None, metavar="N:NRHS",
+                   help="only time the multi-right-hand-side M_UF product on N blobs with NRHS vectors")
     p.add_argument("--product", default=None, metavar="KIND:MODE",
                    help="only time one wall product (kind uf|ut|wf|wt, mode fp64|df64|mixed) on the headline "
                         "workload for --steps steps after --warmup, and print its JSON line")
@@ -547,6 +549,38 @@ def single_product(args):
                       "n_blobs": len(r), "steps": args.steps, **res}))
 
 
+def multi_product(args):
+    """The multi-right-hand-side M_UF product (mixed precision) on N random blobs above the wall
+    (suspensions.blobs_wall_matvec, seed 3) with NRHS N(0,1) vectors: CUDA-event time per product after
+    --warmup products (inputs of NRHS x 3N doubles; pair work far above L2 traffic)."""
+    import torch
+    from rigidmultiblobswall_gb300 import build as B
+    from rigidmultiblobswall_gb300 import mobility as mb
+    from rigidmultiblobswall_gb300 import suspensions as S
+    B.build()
+    n, nrhs = (int(x) for x in args.multi.split(":"))
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    r, _, eta, a = S.blobs_wall_matvec(n, seed=3)
+    rt = torch.tensor(r, device=dev)
+    V = torch.randn(nrhs, 3 * n, generator=torch.Generator(device=dev).manual_seed(5), dtype=torch.float64,
+                    device=dev)
+    for _ in range(args.warmup):
+        mb.uf_multi(rt, V, eta, a)
+    st = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(args.steps):
+        mb.uf_multi(rt, V, eta, a)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    print(json.dumps({"metric": "multi-RHS M_UF product T pair-RHS/s", "mode": "mixed", "n_blobs": n,
+                      "nrhs": nrhs, "steps": args.steps, "ms": ms,
+                      "tpair_rhs_per_s": n * n * nrhs / (ms * 1e-3) / 1e12}))
+
+
 def main():
     args = parse()
     if args.large:
@@ -554,6 +588,9 @@ def main():
         return
     if args.product:
         single_product(args)
+        return
+    if args.multi:
+        multi_product(args)
         return
     if args.impl == "reference":
         run_reference(args)

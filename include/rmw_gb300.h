@@ -90,7 +90,7 @@ int rmw_wall_product_batched(void *handle, int kind, const double *r, const doub
 
 /* M_UF applied to nrhs vectors at once (V and Y: nrhs rows of 3n doubles),
  * mixed precision (<= 1e-6): each pair block is formed once and applied to
- * every vector.  batch may be NULL or a rmw_wall_batch_create handle
+ * every vector of a pass (16 vectors per pass).  batch may be NULL or a rmw_wall_batch_create handle
  * (segmented).  Serves multi-right-hand-side Lanczos; no reference
  * counterpart. */
 int rmw_wall_uf_multi(const double *r, const double *V, double *Y, int64_t n, int nrhs, double eta, double a,

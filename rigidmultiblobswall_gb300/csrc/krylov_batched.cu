@@ -780,7 +780,7 @@ int rmw_rigid_lanczos_batched(void *sys, const double *Z, double *noise, int nrh
     // segments of a pass of 8 right-hand sides have all converged (their rows
     // are zero anyway), through one byte per (pass, suspension)
     const bool mask = (mode == RMW_MODE_MIXED) && S.wall;
-    const int npass = (nrhs + 7) / 8;
+    const int npass = (nrhs + rmw::kMultiPass - 1) / rmw::kMultiPass;
     unsigned char *d_act = nullptr;
     static thread_local unsigned char *h_act = nullptr;
     static thread_local size_t h_cap = 0;
@@ -803,7 +803,8 @@ int rmw_rigid_lanczos_batched(void *sys, const double *Z, double *noise, int nrh
         for (int p = 0; p < npass; ++p)
             for (int k = 0; k < nsusp; ++k) {
                 unsigned char any = 0;
-                for (int q = 8 * p; q < std::min(nrhs, 8 * p + 8); ++q) any |= act[(size_t)q * nsusp + k] ? 1 : 0;
+                for (int q = rmw::kMultiPass * p; q < std::min(nrhs, rmw::kMultiPass * (p + 1)); ++q)
+                    any |= act[(size_t)q * nsusp + k] ? 1 : 0;
                 h_act[(size_t)p * nsusp + k] = any;
             }
         RMW_CUDA(cudaMemcpyAsync(d_act, h_act, nact, cudaMemcpyHostToDevice, S.st));

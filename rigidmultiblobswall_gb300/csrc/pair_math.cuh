@@ -181,6 +181,43 @@ __device__ __forceinline__ void uf_apply(const UFCoeffs<T> &c, T dx, T dy, T dz,
     uz += c.Af * vz + Gr * dz + Gw * Rz + c.c4 * W + c.f5 * vz;
 }
 
+// The explicit 3x3 block of uf_coeffs, for products with several right-hand
+// sides: nine FMAs per right-hand side instead of sixteen.  With d = (dx, dy,
+// dz), e = (dx, dy, Rz) and z the wall normal,
+//   M = Af I + Bc d d^T + c2 e e^T + c3 e z^T + c4 z e^T + f5 z z^T,
+// so M_xy = M_yx = (Bc + c2) dx dy, M_xz = dx t3, M_zx = dx t4 with
+// t3,4 = Bc dz + c2 Rz + c3,4, and M_zz = Af + f5 + Bc dz^2 + (c2 Rz + c3 + c4) Rz.
+struct UFBlock {
+    float xx, xy, xz, yy, yz, zx, zy, zz;  // M_yx = M_xy
+};
+
+__device__ __forceinline__ UFBlock uf_block_f(const UFCoeffs<float> &c, float dx, float dy, float dz, float Rz)
+{
+    const float b2 = c.Bc + c.c2;
+    const float t = fmaf(c.Bc, dz, c.c2 * Rz);
+    const float t3 = t + c.c3, t4 = t + c.c4;
+    const float px = b2 * dx;
+    UFBlock m;
+    m.xx = fmaf(px, dx, c.Af);
+    m.xy = px * dy;
+    m.yy = fmaf(b2 * dy, dy, c.Af);
+    m.xz = dx * t3;
+    m.yz = dy * t3;
+    m.zx = dx * t4;
+    m.zy = dy * t4;
+    m.zz = fmaf(fmaf(c.c2, Rz, c.c3 + c.c4), Rz, fmaf(c.Bc * dz, dz, c.Af + c.f5));
+    return m;
+}
+
+// (ux, uy, uz) += M v
+__device__ __forceinline__ void uf_block_apply(const UFBlock &m, float vx, float vy, float vz, float &ux, float &uy,
+                                               float &uz)
+{
+    ux = fmaf(m.xx, vx, fmaf(m.xy, vy, fmaf(m.xz, vz, ux)));
+    uy = fmaf(m.xy, vx, fmaf(m.yy, vy, fmaf(m.yz, vz, uy)));
+    uz = fmaf(m.zx, vx, fmaf(m.zy, vy, fmaf(m.zz, vz, uz)));
+}
+
 // FP32: every term chained into the accumulator by an FMA (four plain
 // multiplies or adds per application instead of ten)
 template <>

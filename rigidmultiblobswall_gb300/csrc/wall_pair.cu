@@ -631,12 +631,13 @@ __global__ void __launch_bounds__(kThreads) wall_pair_mixed_kernel(const SrcF *_
 
 // ---------------------------------------------------------------------------
 // Multi-right-hand-side M_UF product (mixed precision): the vector-independent
-// part of each pair block is computed once and applied to kMultiRhs vectors.
-// vec[j * kMultiRhs + q] holds b_j v_q,j (float4, w unused).
-constexpr int kMultiRhs = 8;
-
+// part of each pair block is computed once and applied to every right-hand
+// side of a pass.  Passes are kMultiPass (16) wide; a pass of at most 8
+// right-hand sides runs the 8-wide kernel.  vec[(j * width + q) * 3 + c]
+// holds component c of b_j v_q,j (3 * width floats per source, a multiple of
+// 16 bytes).
 __global__ void pack_multi_kernel(const double *__restrict__ r, const double *__restrict__ V, long long ldv, int nrhs,
-                                  SrcF *__restrict__ src, float4 *__restrict__ vec, int n, double a)
+                                  SrcF *__restrict__ src, float *__restrict__ vec, int n, double a, int width)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -651,25 +652,74 @@ __global__ void pack_multi_kernel(const double *__restrict__ r, const double *__
     s.lo = make_float4((float)(xs - (double)xh), (float)(ys - (double)yh), (float)(zs - (double)zh), 0.f);
     s.v = make_float4(0.f, 0.f, 0.f, 0.f);
     src[i] = s;
-    for (int q = 0; q < kMultiRhs; ++q) {
-        float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+    float *o = vec + (long long)i * 3 * width;
+    for (int q = 0; q < width; ++q) {
+        float w0 = 0.f, w1 = 0.f, w2 = 0.f;
         if (q < nrhs) {
             const double *v = V + (long long)q * ldv + 3LL * i;
-            w = make_float4((float)(b * v[0]), (float)(b * v[1]), (float)(b * v[2]), 0.f);
+            w0 = (float)(b * v[0]);
+            w1 = (float)(b * v[1]);
+            w2 = (float)(b * v[2]);
         }
-        vec[(long long)i * kMultiRhs + q] = w;
+        o[3 * q] = w0;
+        o[3 * q + 1] = w1;
+        o[3 * q + 2] = w2;
     }
 }
 
-template <bool SEG>
-__global__ void __launch_bounds__(kThreads) wall_pair_multi_kernel(const SrcF *__restrict__ src,
+// One shared-memory tile of sources against this thread's target, for every
+// right-hand side: the explicit 3x3 block once per pair, then nine FMAs per
+// right-hand side.  DIAG: the tile may contain the target itself, whose pair
+// block is zeroed (the self term is added by the finalize kernel).
+template <bool DIAG, int NR>
+__device__ __forceinline__ void multi_tile(const float4 *tpos, const float4 *tvec, int cnt, int t0, int i, float4 mh,
+                                           float4 ml, float hi, float (&acc)[NR][3])
+{
+#pragma unroll 1
+    for (int k = 0; k < cnt; ++k) {
+        const float4 shp = tpos[2 * k], slp = tpos[2 * k + 1];
+        const float dx = (mh.x - shp.x) + (ml.x - slp.x);
+        const float dy = (mh.y - shp.y) + (ml.y - slp.y);
+        const float dz = (mh.z - shp.z) + (ml.z - slp.z);
+        const float hj = shp.z + slp.z;
+        const float Rz = hi + hj;
+        UFCoeffs<float> c = uf_coeffs<float>(dx, dy, dz, Rz, hi, hj);
+        if (DIAG && t0 + k == i) c = UFCoeffs<float>{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // finite inputs
+        const UFBlock m = uf_block_f(c, dx, dy, dz, Rz);
+        const float4 *vk = tvec + k * (3 * NR / 4);
+#pragma unroll
+        for (int g = 0; g < NR / 4; ++g) {  // four right-hand sides = three float4
+            const float4 a0 = vk[3 * g], a1 = vk[3 * g + 1], a2 = vk[3 * g + 2];
+            uf_block_apply(m, a0.x, a0.y, a0.z, acc[4 * g][0], acc[4 * g][1], acc[4 * g][2]);
+            uf_block_apply(m, a0.w, a1.x, a1.y, acc[4 * g + 1][0], acc[4 * g + 1][1], acc[4 * g + 1][2]);
+            uf_block_apply(m, a1.z, a1.w, a2.x, acc[4 * g + 2][0], acc[4 * g + 2][1], acc[4 * g + 2][2]);
+            uf_block_apply(m, a2.y, a2.z, a2.w, acc[4 * g + 3][0], acc[4 * g + 3][1], acc[4 * g + 3][2]);
+        }
+    }
+}
+
+// Dynamic shared memory of the NR-wide kernel: kTile/2 source positions (hi,
+// lo), their NR vectors and, for NR > 8, the per-thread compensated sums
+// (float2 hi/lo, laid out [component][thread] so a warp's accesses are
+// consecutive); up to 8 right-hand sides keep those sums in registers.
+template <int NR> constexpr size_t multi_smem_bytes()
+{
+    return sizeof(float4) * kTile + sizeof(float) * kTile / 2 * 3 * NR +
+           (NR > 8 ? sizeof(float2) * NR * 3 * kThreads : 0);
+}
+
+template <bool SEG, int NR>
+__global__ void __launch_bounds__(kThreads, NR > 8 ? 3 : 4) wall_pair_multi_kernel(const SrcF *__restrict__ src,
                                                                     const float4 *__restrict__ vec, int n, int chunk,
                                                                     double *__restrict__ partial,
                                                                     const TileJob *__restrict__ jobs,
                                                                     const unsigned char *__restrict__ active)
 {
-    __shared__ float4 tpos[2 * kTile / 2];      // hi, lo of kTile/2 sources
-    __shared__ float4 tvec[kTile / 2 * kMultiRhs];
+    constexpr bool kRegSums = NR <= 8;
+    extern __shared__ float4 multi_smem[];
+    float4 *tpos = multi_smem;              // 2 * kTile/2
+    float4 *tvec = multi_smem + kTile;      // kTile/2 sources x 3 NR floats
+    float2 *sums = (float2 *)(tvec + kTile / 2 * (3 * NR / 4));
     if (SEG && active && !active[jobs[blockIdx.x].susp]) return;  // converged suspension: nothing to do
     const PairRange pr = pair_range<SEG>(jobs, n, chunk);
     const int i = pr.tbeg + threadIdx.x;
@@ -677,11 +727,15 @@ __global__ void __launch_bounds__(kThreads) wall_pair_multi_kernel(const SrcF *_
     float4 mh = make_float4(0.f, 0.f, 1.f, 0.f), ml = make_float4(0.f, 0.f, 0.f, 0.f);
     if (valid) { mh = src[i].hi; ml = src[i].lo; }
     const float hi = mh.z + ml.z;
-    float sh_[kMultiRhs][3], sl_[kMultiRhs][3];
+    float sh_[kRegSums ? NR : 1][3], sl_[kRegSums ? NR : 1][3];
+    if constexpr (kRegSums) {
 #pragma unroll
-    for (int q = 0; q < kMultiRhs; ++q)
+        for (int q = 0; q < NR; ++q)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) sh_[q][c] = sl_[q][c] = 0.f;
+            for (int c = 0; c < 3; ++c) sh_[q][c] = sl_[q][c] = 0.f;
+    } else {
+        for (int e = 0; e < NR * 3; ++e) sums[e * kThreads + threadIdx.x] = make_float2(0.f, 0.f);
+    }
     constexpr int kT = kTile / 2;
     for (int t0 = pr.j0; t0 < pr.j1; t0 += kT) {
         const int cnt = min(kT, pr.j1 - t0);
@@ -690,46 +744,49 @@ __global__ void __launch_bounds__(kThreads) wall_pair_multi_kernel(const SrcF *_
             tpos[2 * k] = src[t0 + k].hi;
             tpos[2 * k + 1] = src[t0 + k].lo;
         }
-        for (int k = threadIdx.x; k < cnt * kMultiRhs; k += kThreads) tvec[k] = vec[(long long)t0 * kMultiRhs + k];
+        for (int k = threadIdx.x; k < cnt * (3 * NR / 4); k += kThreads)
+            tvec[k] = vec[(long long)t0 * (3 * NR / 4) + k];
         __syncthreads();
-        float acc[kMultiRhs][3];
+        float acc[NR][3];
 #pragma unroll
-        for (int q = 0; q < kMultiRhs; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.f;
-        for (int k = 0; k < cnt; ++k) {
-            const float4 shp = tpos[2 * k], slp = tpos[2 * k + 1];
-            const int j = t0 + k;
-            const float dx = (mh.x - shp.x) + (ml.x - slp.x);
-            const float dy = (mh.y - shp.y) + (ml.y - slp.y);
-            const float dz = (mh.z - shp.z) + (ml.z - slp.z);
-            const float hj = shp.z + slp.z;
-            const float Rz = hi + hj;
-            UFCoeffs<float> c = uf_coeffs<float>(dx, dy, dz, Rz, hi, hj);
-            if (j == i) c = UFCoeffs<float>{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // self pair: zero block (finite inputs)
+        for (int q = 0; q < NR; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.f;
+        // only a tile that overlaps the CTA's targets can hold a self pair
+        if (t0 < pr.tend && t0 + cnt > pr.tbeg) multi_tile<true, NR>(tpos, tvec, cnt, t0, i, mh, ml, hi, acc);
+        else multi_tile<false, NR>(tpos, tvec, cnt, t0, i, mh, ml, hi, acc);
 #pragma unroll
-            for (int q = 0; q < kMultiRhs; ++q) {
-                const float4 v = tvec[k * kMultiRhs + q];
-                uf_apply<float>(c, dx, dy, dz, Rz, v.x, v.y, v.z, acc[q][0], acc[q][1], acc[q][2]);
+        for (int q = 0; q < NR; ++q)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                if constexpr (kRegSums) {
+                    comp_add(sh_[q][c], sl_[q][c], acc[q][c]);
+                } else {
+                    float2 &w = sums[(q * 3 + c) * kThreads + threadIdx.x];
+                    float h = w.x, l = w.y;
+                    comp_add(h, l, acc[q][c]);
+                    w = make_float2(h, l);
+                }
             }
-        }
-#pragma unroll
-        for (int q = 0; q < kMultiRhs; ++q)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) comp_add(sh_[q][c], sl_[q][c], acc[q][c]);
     }
     if (valid) {
 #pragma unroll
-        for (int q = 0; q < kMultiRhs; ++q) {
-            double *o = partial + ((size_t)pr.slot * kMultiRhs + q) * 3 * n + 3 * (size_t)i;
-            o[0] = (double)sh_[q][0] + (double)sl_[q][0];
-            o[1] = (double)sh_[q][1] + (double)sl_[q][1];
-            o[2] = (double)sh_[q][2] + (double)sl_[q][2];
+        for (int q = 0; q < NR; ++q) {
+            double *o = partial + ((size_t)pr.slot * NR + q) * 3 * n + 3 * (size_t)i;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                if constexpr (kRegSums) {
+                    o[c] = (double)sh_[q][c] + (double)sl_[q][c];
+                } else {
+                    const float2 w = sums[(q * 3 + c) * kThreads + threadIdx.x];
+                    o[c] = (double)w.x + (double)w.y;
+                }
+            }
         }
     }
 }
 
 // out[q][3i..] = b_i nf (sum_slots partial + self block (b_i v_q,i)) for q < nrhs
 __global__ void wall_finalize_multi_kernel(const double *__restrict__ r, const double *__restrict__ V, long long ldv,
-                                           int nrhs, const double *__restrict__ partial, int nchunks,
+                                           int nrhs, int width, const double *__restrict__ partial, int nchunks,
                                            double *__restrict__ out, long long ldo, int n, double a, double nf,
                                            const int *__restrict__ blob_nchunks,
                                            const unsigned char *__restrict__ active = nullptr,
@@ -746,7 +803,7 @@ __global__ void wall_finalize_multi_kernel(const double *__restrict__ r, const d
     const int nc = blob_nchunks ? blob_nchunks[i] : nchunks;
     double ux = 0.0, uy = 0.0, uz = 0.0;
     for (int s = 0; s < nc; ++s) {
-        const double *p = partial + ((size_t)s * kMultiRhs + q) * 3 * n + 3 * (size_t)i;
+        const double *p = partial + ((size_t)s * width + q) * 3 * n + 3 * (size_t)i;
         ux += p[0]; uy += p[1]; uz += p[2];
     }
     const double z = r[3 * i + 2];
@@ -1107,35 +1164,57 @@ int wall_product_batched(const WallBatch &B, int kind, const double *r, const do
 }
 
 // M_UF applied to nrhs vectors (rows of V with stride ldv; outputs rows of Y
-// with stride ldy), mixed precision, kMultiRhs vectors per pass.
+// with stride ldy), mixed precision, kMultiPass vectors per pass.
 int wall_uf_multi(const double *r, const double *V, long long ldv, double *Y, long long ldy, int nrhs, int n,
                   double eta, double a, const WallBatch *B, cudaStream_t st, const unsigned char *active)
 {
     if (!B) active = nullptr;
     if (nrhs <= 0 || n <= 0) return RMW_OK;
     const int nchunks = B ? B->max_slots : choose_chunks(n);
+    const int wmax = nrhs > 8 ? kMultiPass : 8;
     const size_t pos = ((sizeof(SrcF) * (size_t)n + 255) / 256) * 256;
-    const size_t vecb = ((sizeof(float4) * (size_t)n * kMultiRhs + 255) / 256) * 256;
-    const size_t bytes = pos + vecb + sizeof(double) * 3 * (size_t)n * kMultiRhs * nchunks;
+    const size_t vecb = ((sizeof(float) * 3 * (size_t)n * wmax + 255) / 256) * 256;
+    const size_t bytes = pos + vecb + sizeof(double) * 3 * (size_t)n * wmax * nchunks;
     void *ws = nullptr;
     if (int rc = scratch(SCRATCH_PAIR, bytes, &ws, st)) return rc;
     SrcF *src = (SrcF *)ws;
-    float4 *vec = (float4 *)((char *)ws + pos);
+    float *vec = (float *)((char *)ws + pos);
+    const float4 *vec4 = (const float4 *)vec;
     double *partial = (double *)((char *)ws + pos + vecb);
     const double nf = 1.0 / (8.0 * kPi * eta * a);
     const int chunk = (n + nchunks - 1) / nchunks;
     const dim3 grid = B ? dim3(B->njobs) : dim3((n + kThreads - 1) / kThreads, nchunks);
-    for (int q0 = 0; q0 < nrhs; q0 += kMultiRhs) {
-        const int nr = std::min(kMultiRhs, nrhs - q0);
-        pack_multi_kernel<<<(n + 255) / 256, 256, 0, st>>>(r, V + (long long)q0 * ldv, ldv, nr, src, vec, n, a);
+    static bool attr_set = false;  // the 16-wide kernel needs more than 48 KB of shared memory
+    if (!attr_set) {
+        RMW_CUDA(cudaFuncSetAttribute(wall_pair_multi_kernel<true, kMultiPass>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)multi_smem_bytes<kMultiPass>()));
+        RMW_CUDA(cudaFuncSetAttribute(wall_pair_multi_kernel<false, kMultiPass>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)multi_smem_bytes<kMultiPass>()));
+        attr_set = true;
+    }
+    for (int q0 = 0; q0 < nrhs; q0 += kMultiPass) {
+        const int nr = std::min(kMultiPass, nrhs - q0);
+        const int width = nr > 8 ? kMultiPass : 8;
+        pack_multi_kernel<<<(n + 255) / 256, 256, 0, st>>>(r, V + (long long)q0 * ldv, ldv, nr, src, vec, n, a,
+                                                           width);
         void *tok = nullptr;
         if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
-        const unsigned char *act = active ? active + (size_t)(q0 / kMultiRhs) * B->ninst : nullptr;
-        if (B) wall_pair_multi_kernel<true><<<grid, kThreads, 0, st>>>(src, vec, n, chunk, partial, B->jobs, act);
-        else wall_pair_multi_kernel<false><<<grid, kThreads, 0, st>>>(src, vec, n, chunk, partial, nullptr, nullptr);
+        const unsigned char *act = active ? active + (size_t)(q0 / kMultiPass) * B->ninst : nullptr;
+        const TileJob *jobs = B ? B->jobs : nullptr;
+        if (width == kMultiPass) {
+            const size_t sm = multi_smem_bytes<kMultiPass>();
+            if (B) wall_pair_multi_kernel<true, kMultiPass><<<grid, kThreads, sm, st>>>(src, vec4, n, chunk, partial, jobs, act);
+            else wall_pair_multi_kernel<false, kMultiPass><<<grid, kThreads, sm, st>>>(src, vec4, n, chunk, partial, jobs, act);
+        } else {
+            const size_t sm = multi_smem_bytes<8>();
+            if (B) wall_pair_multi_kernel<true, 8><<<grid, kThreads, sm, st>>>(src, vec4, n, chunk, partial, jobs, act);
+            else wall_pair_multi_kernel<false, 8><<<grid, kThreads, sm, st>>>(src, vec4, n, chunk, partial, jobs, act);
+        }
         if (int rc = trace_end(tok, st)) return rc;
         wall_finalize_multi_kernel<<<dim3((n + 255) / 256, nr), 256, 0, st>>>(
-            r, V + (long long)q0 * ldv, ldv, nr, partial, nchunks, Y + (long long)q0 * ldy, ldy, n, a, nf,
+            r, V + (long long)q0 * ldv, ldv, nr, width, partial, nchunks, Y + (long long)q0 * ldy, ldy, n, a, nf,
             B ? B->blob_nch : nullptr, act, B ? B->blob_susp : nullptr);
     }
     RMW_CHECK_LAUNCH("multi-rhs product");

@@ -43,9 +43,12 @@ struct WallBatch {
 };
 int wall_batch_build(WallBatch &B, const long long *off_host, int ninst);
 void wall_batch_free(WallBatch &B);
+// Right-hand sides per pass of wall_uf_multi.
+constexpr int kMultiPass = 16;
 // M_UF applied to nrhs vectors in mixed precision (rows of V, stride ldv).
-// With a batch and `active` (one byte per suspension and pass of 8 vectors,
-// pass-major), suspensions whose byte is 0 are skipped and get zero rows.
+// With a batch and `active` (one byte per suspension and pass of kMultiPass
+// vectors, pass-major), suspensions whose byte is 0 are skipped and get zero
+// rows.
 int wall_uf_multi(const double *r, const double *V, long long ldv, double *Y, long long ldy, int nrhs, int n,
                   double eta, double a, const WallBatch *B, cudaStream_t st, const unsigned char *active = nullptr);
 int wall_product_batched(const WallBatch &B, int kind, const double *r, const double *v, double *out, double eta,

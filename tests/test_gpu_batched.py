@@ -91,7 +91,7 @@ def test_batched_product_rejects_bad_offsets(cuda_device):
         mb.SuspensionBatch([1, 5])
 
 
-@pytest.mark.parametrize("nrhs", [1, 3, 8, 11])
+@pytest.mark.parametrize("nrhs", [1, 3, 8, 11, 16, 19])
 def test_multi_rhs_product_matches_single_products(cuda_device, nrhs):
     import torch
     r, _, eta, a = S.blobs_wall_matvec(900, seed=31)

@@ -97,6 +97,66 @@ __device__ __forceinline__ df mad2(df a, df b, df c, df d)
     const df t = two_sum_df(p1, p2);
     return fast_two_sum(t.hi, __fadd_rn(t.lo, __fadd_rn(e1, e2)));
 }
+// a*b + c*d + e*f with a single renormalisation
+__device__ __forceinline__ df dot3(df a, df b, df c, df d, df e, df f)
+{
+    const float p1 = __fmul_rn(a.hi, b.hi), p2 = __fmul_rn(c.hi, d.hi), p3 = __fmul_rn(e.hi, f.hi);
+    float e1 = fmaf(a.hi, b.hi, -p1);
+    e1 = fmaf(a.hi, b.lo, e1);
+    e1 = fmaf(a.lo, b.hi, e1);
+    float e2 = fmaf(c.hi, d.hi, -p2);
+    e2 = fmaf(c.hi, d.lo, e2);
+    e2 = fmaf(c.lo, d.hi, e2);
+    float e3 = fmaf(e.hi, f.hi, -p3);
+    e3 = fmaf(e.hi, f.lo, e3);
+    e3 = fmaf(e.lo, f.hi, e3);
+    const df t1 = two_sum_df(p1, p2);
+    const df t2 = two_sum_df(t1.hi, p3);
+    return fast_two_sum(t2.hi, __fadd_rn(__fadd_rn(t1.lo, t2.lo), __fadd_rn(__fadd_rn(e1, e2), e3)));
+}
+
+// acc += a*b + c*d without renormalising acc (as acc_add)
+__device__ __forceinline__ void acc_dot2(df &acc, df a, df b, df c, df d)
+{
+    const float p1 = __fmul_rn(a.hi, b.hi), p2 = __fmul_rn(c.hi, d.hi);
+    float e1 = fmaf(a.hi, b.hi, -p1);
+    e1 = fmaf(a.hi, b.lo, e1);
+    e1 = fmaf(a.lo, b.hi, e1);
+    float e2 = fmaf(c.hi, d.hi, -p2);
+    e2 = fmaf(c.hi, d.lo, e2);
+    e2 = fmaf(c.lo, d.hi, e2);
+    const df t1 = two_sum_df(acc.hi, p1);
+    const df t2 = two_sum_df(t1.hi, p2);
+    acc.hi = t2.hi;
+    acc.lo = __fadd_rn(acc.lo, __fadd_rn(__fadd_rn(t1.lo, t2.lo), __fadd_rn(e1, e2)));
+}
+
+// acc += a*b + c*d + e*f + g*h without renormalising acc
+__device__ __forceinline__ void acc_dot4(df &acc, df a, df b, df c, df d, df e, df f, df g, df h)
+{
+    const float p1 = __fmul_rn(a.hi, b.hi), p2 = __fmul_rn(c.hi, d.hi);
+    const float p3 = __fmul_rn(e.hi, f.hi), p4 = __fmul_rn(g.hi, h.hi);
+    float e1 = fmaf(a.hi, b.hi, -p1);
+    e1 = fmaf(a.hi, b.lo, e1);
+    e1 = fmaf(a.lo, b.hi, e1);
+    float e2 = fmaf(c.hi, d.hi, -p2);
+    e2 = fmaf(c.hi, d.lo, e2);
+    e2 = fmaf(c.lo, d.hi, e2);
+    float e3 = fmaf(e.hi, f.hi, -p3);
+    e3 = fmaf(e.hi, f.lo, e3);
+    e3 = fmaf(e.lo, f.hi, e3);
+    float e4 = fmaf(g.hi, h.hi, -p4);
+    e4 = fmaf(g.hi, h.lo, e4);
+    e4 = fmaf(g.lo, h.hi, e4);
+    const df t1 = two_sum_df(acc.hi, p1);
+    const df t2 = two_sum_df(t1.hi, p2);
+    const df t3 = two_sum_df(t2.hi, p3);
+    const df t4 = two_sum_df(t3.hi, p4);
+    acc.hi = t4.hi;
+    const float lo = __fadd_rn(__fadd_rn(t1.lo, t2.lo), __fadd_rn(t3.lo, t4.lo));
+    acc.lo = __fadd_rn(acc.lo, __fadd_rn(lo, __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(e3, e4))));
+}
+
 // acc += x without renormalising acc (the running low part absorbs the
 // rounding errors; fold before converting)
 __device__ __forceinline__ void acc_add(df &acc, df x)

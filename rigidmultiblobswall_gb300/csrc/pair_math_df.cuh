@@ -177,12 +177,16 @@ __device__ __forceinline__ void pair_rpy_df(df dx, df dy, df dz, df vx, df vy, d
     }
 }
 
-// UF for both orders of one pair: (ux, uy, uz) = M_ij v_j for target i and
-// (wx, wy, wz) = M_ji v_i = M_ij^T v_i for target j (the wall mobility is
-// symmetric).  In block form
-//   M_ij = Af I + Bc d d^T + s^2 f2 e e^T + s f3 e z^T + s f4 z e^T + f5 z z^T
-// with e = (dx, dy, Rz) and z the wall normal, so the transpose only swaps
-// the roles of f3 and f4: the coefficients are formed once for both.
+// UF for both orders of one pair, accumulated: (ux, uy, uz) += M_ij v_j for
+// target i and (wx, wy, wz) += M_ji v_i = M_ij^T v_i for target j (the wall
+// mobility is symmetric).  In block form
+//   M_ij = Af I + Bc d d^T + c2 e e^T + c3 e z^T + c4 z e^T + f5 z z^T
+// with e = (dx, dy, Rz), z the wall normal, c2 = f2 s^2, c3 = f3 s and
+// c4 = f4 s, so the transpose only swaps c3 and c4: the coefficients are
+// formed once for both.  With Gw = c2 (e.v) + c3 vz and G = Bc (d.v) + Gw,
+//   M v = Af v + G (dx, dy, dz) + (0, 0, Af5 vz + Gw (Rz - dz) + c4 (e.v)),
+// Af5 = Af + f5 and Rz - dz = 2 h_j; the accumulators stay unnormalised
+// (acc_dot2 / acc_dot4, as acc_add).
 __device__ __forceinline__ void pair_uf_sym_df(df dx, df dy, df dz, df Rz, df hi, df hj, df vx, df vy, df vz,
                                                df qx, df qy, df qz, df &ux, df &uy, df &uz, df &wx, df &wy,
                                                df &wz)
@@ -220,29 +224,26 @@ __device__ __forceinline__ void pair_uf_sym_df(df dx, df dy, df dz, df Rz, df hi
     const df f4 = TWO_THIRDS * (hj * s2 * 3.0f - (ez * s5) * 10.0f);
     const df f5 = -FOUR_THIRDS * mad((sqr(hj) + E) * 3.0f, s3, (2.0f - E * 15.0f) * s5);
     const df Af = A + f1;
-    const df Af5 = Af + f5;  // the zz diagonal: Af + f5
-    const df f2s = f2 * s;
+    const df Af5 = Af + f5;  // the zz diagonal
+    const df c2 = f2 * s2, c3 = f3 * s, c4 = f4 * s;
+    const df hj2 = scale2(hj, 2.0f);  // Rz - dz
     {  // M_ij v_j
-        const df Pxy = mad2(dx, vx, dy, vy);
-        const df dv = mad(dz, vz, Pxy);
-        const df W = mad(Rz, vz, Pxy);
-        const df Gr = Bc * dv;
-        const df Gw = mad(f2s, W, f3 * vz) * s;
-        const df G = Gr + Gw;
-        ux = mad2(Af, vx, G, dx);
-        uy = mad2(Af, vy, G, dy);
-        uz = mad2(Af5, vz, Gr, dz) + mad2(Gw, Rz, f4 * W, s);
+        const df dv = dot3(dx, vx, dy, vy, dz, vz);
+        const df W = mad(hj2, vz, dv);  // e.v
+        const df Gw = mad2(c2, W, c3, vz);
+        const df G = mad(Bc, dv, Gw);
+        acc_dot2(ux, Af, vx, G, dx);
+        acc_dot2(uy, Af, vy, G, dy);
+        acc_dot4(uz, Af5, vz, G, dz, Gw, hj2, c4, W);
     }
     {  // M_ij^T v_i
-        const df Pxy = mad2(dx, qx, dy, qy);
-        const df dv = mad(dz, qz, Pxy);
-        const df W = mad(Rz, qz, Pxy);
-        const df Gr = Bc * dv;
-        const df Gw = mad(f2s, W, f4 * qz) * s;
-        const df G = Gr + Gw;
-        wx = mad2(Af, qx, G, dx);
-        wy = mad2(Af, qy, G, dy);
-        wz = mad2(Af5, qz, Gr, dz) + mad2(Gw, Rz, f3 * W, s);
+        const df dv = dot3(dx, qx, dy, qy, dz, qz);
+        const df W = mad(hj2, qz, dv);
+        const df Gw = mad2(c2, W, c4, qz);
+        const df G = mad(Bc, dv, Gw);
+        acc_dot2(wx, Af, qx, G, dx);
+        acc_dot2(wy, Af, qy, G, dy);
+        acc_dot4(wz, Af5, qz, G, dz, Gw, hj2, c3, W);
     }
 }
 

@@ -325,20 +325,13 @@ __global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *_
         const float4 sh = thi[jl], sl = tlo[jl], svh = tvh[jl], svl = tvl[jl];
         const df xj = {sh.x, sl.x}, yj = {sh.y, sl.y}, zj = {sh.z, sl.z};
         const df vx = {svh.x, svl.x}, vy = {svh.y, svl.y}, vz = {svh.z, svl.z};
-        df cx, cy, cz, wx, wy, wz;
-        pair_uf_sym_df(xi - xj, yi - yj, zi - zj, zi + zj, zi, zj, vx, vy, vz, qx, qy, qz, cx, cy, cz, wx, wy, wz);
-        acc_add(ux, cx);
-        acc_add(uy, cy);
-        acc_add(uz, cz);
         // double-float accumulation on the FP32 pipe (no FP64 conversions per pair)
-        const df wv[3] = {wx, wy, wz};
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const float2 a2 = sacc[warp][c][jl];
-            df acc = {a2.x, a2.y};
-            acc_add(acc, wv[c]);
-            sacc[warp][c][jl] = make_float2(acc.hi, acc.lo);
-        }
+        const float2 a0 = sacc[warp][0][jl], a1 = sacc[warp][1][jl], a2 = sacc[warp][2][jl];
+        df wx = {a0.x, a0.y}, wy = {a1.x, a1.y}, wz = {a2.x, a2.y};
+        pair_uf_sym_df(xi - xj, yi - yj, zi - zj, zi + zj, zi, zj, vx, vy, vz, qx, qy, qz, ux, uy, uz, wx, wy, wz);
+        sacc[warp][0][jl] = make_float2(wx.hi, wx.lo);
+        sacc[warp][1][jl] = make_float2(wy.hi, wy.lo);
+        sacc[warp][2][jl] = make_float2(wz.hi, wz.lo);
     };
     if (diag) {
         for (int k = 0; k < kTile; ++k) {

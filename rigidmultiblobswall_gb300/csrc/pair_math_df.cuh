@@ -177,55 +177,64 @@ __device__ __forceinline__ void pair_rpy_df(df dx, df dy, df dz, df vx, df vy, d
     }
 }
 
-// UF for both orders of one pair, accumulated: (ux, uy, uz) += M_ij v_j for
-// target i and (wx, wy, wz) += M_ji v_i = M_ij^T v_i for target j (the wall
-// mobility is symmetric).  In block form
+// UF for both orders of one pair, accumulated: (ux, uy, uz) += (3/2) M_ij v_j
+// for target i and (wx, wy, wz) += (3/2) M_ji v_i = (3/2) M_ij^T v_i for
+// target j (the wall mobility is symmetric).  In block form
 //   M_ij = Af I + Bc d d^T + c2 e e^T + c3 e z^T + c4 z e^T + f5 z z^T
 // with e = (dx, dy, Rz), z the wall normal, c2 = f2 s^2, c3 = f3 s and
 // c4 = f4 s, so the transpose only swaps c3 and c4: the coefficients are
 // formed once for both.  With Gw = c2 (e.v) + c3 vz and G = Bc (d.v) + Gw,
 //   M v = Af v + G (dx, dy, dz) + (0, 0, Af5 vz + Gw (Rz - dz) + c4 (e.v)),
-// Af5 = Af + f5 and Rz - dz = 2 h_j; the accumulators stay unnormalised
-// (acc_dot2 / acc_dot4, as acc_add).
+// Af5 = Af + f5 and Rz - dz = 2 h_j.  Every coefficient is formed times 3/2,
+// which turns the RPY and Swan-Brady constants (2/3, 4/3, 10/3 ...) into
+// exact floats; the finalize kernel multiplies the pair sums by 2/3 in FP64.
+// In powers of s (t = s^3, p = s^5, E = (Rz s)^2, hh = h_i h_j s^2):
+//   (3/2) A  = 3/(2r) + 1/r^3,          (3/2) Bc = (3/2 - 3/r^2) / r^3
+//   (3/2) f1 = -(3/2 + 3 hh) s - [(1 - 3E) t - (1 - 5E) p]
+//   (3/2) f2 = -(3/2 - 9 hh) s + 3 (1 - 5E) t - 5 (1 - 7E) p
+//   (3/2) c3 = 3 h_j t - 18 hh Rz t + Rz s^2 [10 (2 - 7E) p - 6 (1 - 5E) t]
+//   (3/2) c4 = 3 h_j t - 10 Rz s^2 p
+//   (3/2) f5 = -2 [3 (h_j^2 + E) t + (2 - 15E) p]
+// and for r <= 2: (3/2) A = 2 (1 - 9r/32), (3/2) Bc = 3 / (16 r).
+// The accumulators stay unnormalised (acc_dot2 / acc_dot4, as acc_add).
 __device__ __forceinline__ void pair_uf_sym_df(df dx, df dy, df dz, df Rz, df hi, df hj, df vx, df vy, df vz,
                                                df qx, df qy, df qz, df &ux, df &uy, df &uz, df &wx, df &wy,
                                                df &wz)
 {
-    constexpr df TWO_THIRDS = dfc::make(2.0 / 3.0);
-    constexpr df FOUR_THIRDS = dfc::make(4.0 / 3.0);
-    constexpr df TEN_THIRDS = dfc::make(10.0 / 3.0);
     const df rho2 = mad(dx, dx, sqr(dy));
     const df r2 = mad(dz, dz, rho2);
     const df invr = rsqrt_df(r2);
-    const df r = r2 * invr;
     const df Rz2 = sqr(Rz);
     const df s = rsqrt_df(rho2 + Rz2);
-    const df s2 = sqr(s);
-    const df s3 = s2 * s;
-    const df E = Rz2 * s2;
+    const df u = sqr(s);
+    const df t = u * s;
+    const df p = t * u;
+    const df E = Rz2 * u;
     const df invr2 = sqr(invr);
-    df A = mad(TWO_THIRDS, invr2, df_from(1.0f)) * invr;
-    df Bc = (1.0f - scale2(invr2, 2.0f)) * invr2 * invr;
-    const bool near = !(r > 2.0f);
+    const df invr3 = invr2 * invr;
+    df A = mad(invr, 1.5f, invr3);
+    df Bc = (1.5f - invr2 * 3.0f) * invr3;
+    const bool near = !(r2 > 4.0f);  // r <= 2
     if (__any_sync(__activemask(), near)) {
         if (near) {
-            A = FOUR_THIRDS * (1.0f - r * 0.28125f);
-            Bc = scale2(invr, 0.125f);
+            const df r = r2 * invr;
+            A = scale2(1.0f - r * 0.28125f, 2.0f);
+            Bc = invr * 0.1875f;
         }
     }
-    const df s5 = s3 * s2;
-    const df hh = hi * hj * s2;
-    const df ez = Rz * s;
-    const df q5 = (1.0f - E * 5.0f) * s3;
-    const df f1 = -mad(scale2(hh, 2.0f) + 1.0f, s, TWO_THIRDS * ((1.0f - E * 3.0f) * s3 - q5 * s2));
-    const df f2 = -(mad((1.0f - hh * 6.0f), s, -scale2(q5, 2.0f)) + TEN_THIRDS * ((1.0f - E * 7.0f) * s5));
-    const df f3 = TWO_THIRDS * (hj * s2 * 3.0f - (hh * ez * s) * 18.0f +
-                                ez * (((2.0f - E * 7.0f) * s5) * 10.0f - q5 * 6.0f));
-    const df f4 = TWO_THIRDS * (hj * s2 * 3.0f - (ez * s5) * 10.0f);
-    const df f5 = -FOUR_THIRDS * mad((sqr(hj) + E) * 3.0f, s3, (2.0f - E * 15.0f) * s5);
+    const df hh = (hi * hj) * u;
+    const df q5 = (1.0f - E * 5.0f) * t;
+    const df E7 = E * 7.0f;
+    const df f1 = -mad(mad(hh, 3.0f, df_from(1.5f)), s, (1.0f - E * 3.0f) * t - q5 * u);
+    const df f2 = mad(q5, 3.0f, -mad(mad(hh, -9.0f, df_from(1.5f)), s, ((1.0f - E7) * p) * 5.0f));
+    const df f5 = scale2(mad((sqr(hj) + E) * 3.0f, t, (2.0f - E * 15.0f) * p), -2.0f);
+    const df Ru = Rz * u;
+    const df hjt3 = (hj * t) * 3.0f;
+    const df c4 = hjt3 - (Ru * p) * 10.0f;
+    const df c3 = hjt3 - (hh * (Rz * t)) * 18.0f + Ru * (((2.0f - E7) * p) * 10.0f - q5 * 6.0f);
     const df Af = A + f1;
     const df Af5 = Af + f5;  // the zz diagonal
-    const df c2 = f2 * s2, c3 = f3 * s, c4 = f4 * s;
+    const df c2 = f2 * u;
     const df hj2 = scale2(hj, 2.0f);  // Rz - dz
     {  // M_ij v_j
         const df dv = dot3(dx, vx, dy, vy, dz, vz);

@@ -825,7 +825,7 @@ __global__ void wall_finalize_kernel(const double *__restrict__ r, const double 
                                      const double *__restrict__ partial, int nchunks, double *__restrict__ out,
                                      int n, double a, double nf, const int *__restrict__ blob_nchunks,
                                      const long long *__restrict__ pbase = nullptr,
-                                     const int *__restrict__ pstride = nullptr)
+                                     const int *__restrict__ pstride = nullptr, double pair_scale = 1.0)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -837,6 +837,7 @@ __global__ void wall_finalize_kernel(const double *__restrict__ r, const double 
         const double *p = p0 + (size_t)s * ps;
         ux += p[0]; uy += p[1]; uz += p[2];
     }
+    ux *= pair_scale; uy *= pair_scale; uz *= pair_scale;
     const double z = r[3 * i + 2];
     const double b = (z < a) ? z / a : 1.0;
     const double ze = (z <= a) ? a : z;
@@ -996,8 +997,10 @@ int wall_product_sym_with_scratch(const double *r, const double *v, double *out,
         wall_uf_mixed_sym_kernel<false><<<ncta, kThreads, 0, st>>>(src, n, nt, partial, nullptr);
     }
     if (int rc = trace_end(tok, st)) return rc;
+    // the df64 kernel sums (3/2) M_ij v_j
     wall_finalize_kernel<RMW_UF><<<pg, pb, 0, st>>>(r, v, partial, nt, out, n, a, 1.0 / (8.0 * kPi * eta * a),
-                                                     nullptr);
+                                                     nullptr, nullptr, nullptr,
+                                                     mode == RMW_MODE_DF64 ? 2.0 / 3.0 : 1.0);
     RMW_CHECK_LAUNCH("symmetric wall product kernels");
     return RMW_OK;
 }
@@ -1147,7 +1150,8 @@ int wall_product_batched(const WallBatch &B, int kind, const double *r, const do
         }
         if (int rc2 = trace_end(tok, st)) return rc2;
         wall_finalize_kernel<RMW_UF><<<pg, pb, 0, st>>>(r, v, partial, 0, out, B.n, a, 1.0 / (8.0 * kPi * eta * a),
-                                                         B.blob_nslots, B.blob_pbase, B.blob_pstride);
+                                                         B.blob_nslots, B.blob_pbase, B.blob_pstride,
+                                                         mode == RMW_MODE_DF64 ? 2.0 / 3.0 : 1.0);
         RMW_CHECK_LAUNCH("segmented symmetric wall product");
         return RMW_OK;
     }

@@ -66,6 +66,32 @@ __device__ __forceinline__ df operator*(df a, float b)
 }
 __device__ __forceinline__ df operator*(float a, df b) { return b * a; }
 
+// Products left unnormalised, (p, e) with |e| <= ~2^-22.4 |p|: for operands
+// that go straight into a sum (whose two-sum renormalises), where the skipped
+// fast two-sum would be redone anyway.
+__device__ __forceinline__ df mul_u(df a, df b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return {p, e};
+}
+__device__ __forceinline__ df mul_u(df a, float b)
+{
+    const float p = __fmul_rn(a.hi, b);
+    float e = fmaf(a.hi, b, -p);
+    e = fmaf(a.lo, b, e);
+    return {p, e};
+}
+__device__ __forceinline__ df sqr_u(df a)
+{
+    const float p = __fmul_rn(a.hi, a.hi);
+    float e = fmaf(a.hi, a.hi, -p);
+    e = fmaf(2.0f * a.hi, a.lo, e);
+    return {p, e};
+}
+
 // a*b + c with a single renormalisation
 __device__ __forceinline__ df mad(df a, df b, df c)
 {

@@ -92,6 +92,35 @@ __device__ __forceinline__ df sqr_u(df a)
     return {p, e};
 }
 
+// Sums left unnormalised (the exact two-sum of the high parts plus the low
+// parts): for operands of a further sum, or of a product when the high parts
+// cannot cancel (after cancellation the value sits in the low part, and a
+// double-float product drops lo * lo).
+__device__ __forceinline__ df add_u(df a, df b)
+{
+    const df s = two_sum_df(a.hi, b.hi);
+    return {s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo))};
+}
+__device__ __forceinline__ df sub_u(df a, df b) { return add_u(a, {-b.hi, -b.lo}); }
+// a*b + c, unnormalised
+__device__ __forceinline__ df mad_u(df a, df b, df c)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    const df t = two_sum_df(p, c.hi);
+    return {t.hi, __fadd_rn(t.lo, __fadd_rn(e, c.lo))};
+}
+__device__ __forceinline__ df mad_u(df a, float b, df c)
+{
+    const float p = __fmul_rn(a.hi, b);
+    float e = fmaf(a.hi, b, -p);
+    e = fmaf(a.lo, b, e);
+    const df t = two_sum_df(p, c.hi);
+    return {t.hi, __fadd_rn(t.lo, __fadd_rn(e, c.lo))};
+}
+
 // a*b + c with a single renormalisation
 __device__ __forceinline__ df mad(df a, df b, df c)
 {
@@ -218,7 +247,7 @@ __device__ __forceinline__ df rsqrt_df(df x)
 {
     float y = rsqrtf(x.hi);
     y = y * fmaf(-0.5f * x.hi, y * y, 1.5f);
-    const df t = x * two_prod(y, y);
+    const df t = mul_u(x, two_prod(y, y));
     const float e = __fsub_rn(__fsub_rn(1.0f, t.hi), t.lo);
     return fast_two_sum(y, __fmul_rn(__fmul_rn(0.5f, y), e));
 }

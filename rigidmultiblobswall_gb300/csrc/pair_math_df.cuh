@@ -202,7 +202,7 @@ __device__ __forceinline__ void pair_uf_sym_df(df dx, df dy, df dz, df Rz, df hi
                                                df &wz)
 {
     // mul_u / sqr_u: products that feed a sum directly (see dfloat.cuh)
-    const df rho2 = mad(dx, dx, sqr_u(dy));
+    const df rho2 = mad_u(dx, dx, sqr_u(dy));
     const df r2 = mad(dz, dz, rho2);
     const df invr = rsqrt_df(r2);
     const df Rz2 = sqr(Rz);
@@ -213,7 +213,7 @@ __device__ __forceinline__ void pair_uf_sym_df(df dx, df dy, df dz, df Rz, df hi
     const df E = Rz2 * u;
     const df invr2 = sqr(invr);
     const df invr3 = invr2 * invr;
-    df A = mad(invr, 1.5f, invr3);
+    df A = mad_u(invr, 1.5f, invr3);
     df Bc = (1.5f - mul_u(invr2, 3.0f)) * invr3;
     const bool near = !(r2 > 4.0f);  // r <= 2
     if (__any_sync(__activemask(), near)) {
@@ -226,13 +226,13 @@ __device__ __forceinline__ void pair_uf_sym_df(df dx, df dy, df dz, df Rz, df hi
     const df hh = (hi * hj) * u;
     const df q5 = (1.0f - mul_u(E, 5.0f)) * t;
     const df E7 = mul_u(E, 7.0f);
-    const df f1 = -mad(mad(hh, 3.0f, df_from(1.5f)), s, mul_u(1.0f - mul_u(E, 3.0f), t) - mul_u(q5, u));
-    const df f2 = mad(q5, 3.0f, -mad(mad(hh, -9.0f, df_from(1.5f)), s, mul_u((1.0f - E7) * p, 5.0f)));
-    const df f5 = scale2(mad((sqr_u(hj) + E) * 3.0f, t, mul_u(2.0f - mul_u(E, 15.0f), p)), -2.0f);
+    const df f1 = -mad_u(mad(hh, 3.0f, df_from(1.5f)), s, sub_u(mul_u(1.0f - mul_u(E, 3.0f), t), mul_u(q5, u)));
+    const df f2 = mad(q5, 3.0f, -mad_u(mad(hh, -9.0f, df_from(1.5f)), s, mul_u((1.0f - E7) * p, 5.0f)));
+    const df f5 = scale2(mad_u((sqr_u(hj) + E) * 3.0f, t, mul_u(2.0f - mul_u(E, 15.0f), p)), -2.0f);
     const df Ru = Rz * u;
     const df hjt3 = mul_u(hj * t, 3.0f);
     const df c4 = hjt3 - mul_u(Ru * p, 10.0f);
-    const df c3 = hjt3 - mul_u(hh * (Rz * t), 18.0f) +
+    const df c3 = sub_u(hjt3, mul_u(hh * (Rz * t), 18.0f)) +
                   mul_u(Ru, mul_u((2.0f - E7) * p, 10.0f) - mul_u(q5, 6.0f));
     const df Af = A + f1;
     const df Af5 = Af + f5;  // the zz diagonal

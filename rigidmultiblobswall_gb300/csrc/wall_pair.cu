@@ -328,7 +328,10 @@ __global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *_
         // double-float accumulation on the FP32 pipe (no FP64 conversions per pair)
         const float2 a0 = sacc[warp][0][jl], a1 = sacc[warp][1][jl], a2 = sacc[warp][2][jl];
         df wx = {a0.x, a0.y}, wy = {a1.x, a1.y}, wz = {a2.x, a2.y};
-        pair_uf_sym_df(xi - xj, yi - yj, zi - zj, zi + zj, zi, zj, vx, vy, vz, qx, qy, qz, ux, uy, uz, wx, wy, wz);
+        // differences renormalised (a cancelled high part must not leave the value in the low part, whose
+        // square a double-float product drops); the sum of two heights cannot cancel
+        pair_uf_sym_df(xi - xj, yi - yj, zi - zj, add_u(zi, zj), zi, zj, vx, vy, vz, qx, qy, qz, ux, uy, uz, wx, wy,
+                       wz);
         sacc[warp][0][jl] = make_float2(wx.hi, wx.lo);
         sacc[warp][1][jl] = make_float2(wy.hi, wy.lo);
         sacc[warp][2][jl] = make_float2(wz.hi, wz.lo);

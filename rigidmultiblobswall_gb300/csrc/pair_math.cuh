@@ -9,7 +9,7 @@ namespace rmw {
 // pair math.  (dx,dy,dz) = (r_i - r_j)/a; Rz = (z_i + z_j)/a; hi = z_i/a; hj = z_j/a.
 template <typename T> __device__ __forceinline__ T rsq(T x);
 template <> __device__ __forceinline__ double rsq<double>(double x) { return rsqrt(x); }
-template <> __device__ __forceinline__ float rsq<float>(float x) { return rsqrtf(x); }
+template <> __device__ __forceinline__ float rsq<float>(float x) { return rsqrt_approx(x); }
 
 // The reference builds each 3x3 block from unit vectors e = (dx, dy, Rz)/R and
 // then multiplies by v.  Here the products are regrouped so that e never

@@ -57,6 +57,17 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
+// 1/sqrt(x) by the hardware approximation (relative error below 2^-22) with
+// a subnormal input flushed to zero: the arguments here are squared
+// distances in blob radii, never subnormal, so the approximation needs no
+// subnormal-input fix-up around it.
+__device__ __forceinline__ float rsqrt_approx(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // (hi, lo) += x, keeping lo as the running compensation.
 __device__ __forceinline__ void comp_add(float &hi, float &lo, float x)
 {

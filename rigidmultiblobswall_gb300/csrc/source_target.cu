@@ -58,7 +58,7 @@ template <> struct Num<double> {
 };
 template <> struct Num<float> {
     static __device__ __forceinline__ float k(double v) { return (float)v; }
-    static __device__ __forceinline__ float rsq(float x) { return rsqrtf(x); }
+    static __device__ __forceinline__ float rsq(float x) { return rsqrt_approx(x); }
     static __device__ __forceinline__ bool gt(float a, float b) { return a > b; }
     static __device__ __forceinline__ float tabs(float a) { return fabsf(a); }
     static __device__ __forceinline__ float tmin(float a, float b) { return a < b ? a : b; }

@@ -130,7 +130,7 @@ __device__ __forceinline__ void pair_contrib(T dx, T dy, T dz, T Rz, T hi, T hj,
 // right-hand sides:  M v = Af v + (Bc (d.v) + c2 W + c3 vz) (dx, dy, .) ...
 // with W = dx vx + dy vy + Rz vz (see uf_apply).
 template <typename T> struct UFCoeffs {
-    T Af, Bc, c2, c3, c4, f5;
+    T Af, Bc, c2, c3, c4, Af5;  // Af5 = Af + f5, the zz diagonal
 };
 
 template <typename T>
@@ -164,7 +164,8 @@ __device__ __forceinline__ UFCoeffs<T> uf_coeffs(T dx, T dy, T dz, T Rz, T hi, T
     const T f3 = T(2.0 / 3.0) * (T(3) * hj * s2 - T(18) * hh * ez * s + ez * (T(10) * (T(2) - T(7) * E) * s5 - T(6) * q5));
     const T f4 = T(2.0 / 3.0) * (T(3) * hj * s2 - T(10) * ez * s5);
     const T f5 = T(-4.0 / 3.0) * (T(3) * (hj * hj + E) * s3 + (T(2) - T(15) * E) * s5);
-    return {A + f1, Bc, f2 * s2, f3 * s, f4 * s, f5};
+    const T Af = A + f1;
+    return {Af, Bc, f2 * s2, f3 * s, f4 * s, Af + f5};
 }
 
 template <typename T>
@@ -178,7 +179,7 @@ __device__ __forceinline__ void uf_apply(const UFCoeffs<T> &c, T dx, T dy, T dz,
     const T G = Gr + Gw;
     ux += c.Af * vx + G * dx;
     uy += c.Af * vy + G * dy;
-    uz += c.Af * vz + Gr * dz + Gw * Rz + c.c4 * W + c.f5 * vz;
+    uz += c.Af5 * vz + Gr * dz + Gw * Rz + c.c4 * W;
 }
 
 // The explicit 3x3 block of uf_coeffs, for products with several right-hand
@@ -205,7 +206,7 @@ __device__ __forceinline__ UFBlock uf_block_f(const UFCoeffs<float> &c, float dx
     m.yz = dy * t3;
     m.zx = dx * t4;
     m.zy = dy * t4;
-    m.zz = fmaf(fmaf(c.c2, Rz, c.c3 + c.c4), Rz, fmaf(c.Bc * dz, dz, c.Af + c.f5));
+    m.zz = fmaf(fmaf(c.c2, Rz, c.c3 + c.c4), Rz, fmaf(c.Bc * dz, dz, c.Af5));
     return m;
 }
 
@@ -218,20 +219,22 @@ __device__ __forceinline__ void uf_block_apply(const UFBlock &m, float vx, float
     uz = fmaf(m.zx, vx, fmaf(m.zy, vy, fmaf(m.zz, vz, uz)));
 }
 
-// FP32: every term chained into the accumulator by an FMA (four plain
-// multiplies or adds per application instead of ten)
+// FP32: every term chained into the accumulator by an FMA (two plain
+// multiplies and one subtraction per application)
 template <>
 __device__ __forceinline__ void uf_apply<float>(const UFCoeffs<float> &c, float dx, float dy, float dz, float Rz,
                                                 float vx, float vy, float vz, float &ux, float &uy, float &uz)
 {
-    const float Pxy = fmaf(dy, vy, dx * vx);
-    const float Gr = c.Bc * fmaf(dz, vz, Pxy);
-    const float W = fmaf(Rz, vz, Pxy);
+    // with dv = d.v, G = Bc dv + Gw and Rz - dz = 2 h_j:
+    // (M v)_z = Af5 vz + G dz + Gw (Rz - dz) + c4 W
+    const float h2 = Rz - dz;
+    const float dv = fmaf(dz, vz, fmaf(dy, vy, dx * vx));
+    const float W = fmaf(h2, vz, dv);
     const float Gw = fmaf(c.c2, W, c.c3 * vz);
-    const float G = Gr + Gw;
+    const float G = fmaf(c.Bc, dv, Gw);
     ux = fmaf(c.Af, vx, fmaf(G, dx, ux));
     uy = fmaf(c.Af, vy, fmaf(G, dy, uy));
-    uz = fmaf(c.Af, vz, fmaf(Gr, dz, fmaf(Gw, Rz, fmaf(c.c4, W, fmaf(c.f5, vz, uz)))));
+    uz = fmaf(c.Af5, vz, fmaf(G, dz, fmaf(Gw, h2, fmaf(c.c4, W, uz))));
 }
 
 // Free-space RPY blocks (no wall): the RPY parts of pair_contrib, for the

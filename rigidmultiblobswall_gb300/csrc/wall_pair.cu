@@ -429,12 +429,12 @@ __global__ void __launch_bounds__(kThreads) wall_uf_mixed_sym_kernel(const SrcF 
         const float Rz = hi + hj;
         const UFCoeffs<float> c = uf_coeffs<float>(dx, dy, dz, Rz, hi, hj);
         uf_apply<float>(c, dx, dy, dz, Rz, sv.x, sv.y, sv.z, ux, uy, uz);
-        const UFCoeffs<float> ct = {c.Af, c.Bc, c.c2, c.c4, c.c3, c.f5};  // M^T: f3 and f4 trade places
-        float wx = 0.f, wy = 0.f, wz = 0.f;
+        const UFCoeffs<float> ct = {c.Af, c.Bc, c.c2, c.c4, c.c3, c.Af5};  // M^T: f3 and f4 trade places
+        float wx = sacc[warp][0][jl], wy = sacc[warp][1][jl], wz = sacc[warp][2][jl];
         uf_apply<float>(ct, dx, dy, dz, Rz, me.v.x, me.v.y, me.v.z, wx, wy, wz);
-        sacc[warp][0][jl] += wx;
-        sacc[warp][1][jl] += wy;
-        sacc[warp][2][jl] += wz;
+        sacc[warp][0][jl] = wx;
+        sacc[warp][1][jl] = wy;
+        sacc[warp][2][jl] = wz;
     };
     if (diag) {
         for (int k = 0; k < kTile; ++k) {

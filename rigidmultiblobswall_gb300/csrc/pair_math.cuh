@@ -126,9 +126,21 @@ __device__ __forceinline__ void pair_contrib(T dx, T dy, T dz, T Rz, T hi, T hj,
     }
 }
 
-// Vector-independent part of one M_UF block, for products with several
-// right-hand sides:  M v = Af v + (Bc (d.v) + c2 W + c3 vz) (dx, dy, .) ...
-// with W = dx vx + dy vy + Rz vz (see uf_apply).
+// Vector-independent part of one M_UF block, times 3/2 (the consumers'
+// finalize kernels multiply the pair sums by 2/3 in FP64), for the FP32 pair
+// kernels:  (3/2) M v = Af v + (Bc (d.v) + c2 W + c3 vz) (dx, dy, .) ...
+// with W = dx vx + dy vy + Rz vz (see uf_apply).  The 3/2 turns the RPY and
+// Swan-Brady constants into the small integers and halves below; the same
+// coefficients as the double-float pair_uf_sym_df:
+//   (3/2) A  = 3/(2r) + 1/r^3,          (3/2) Bc = (3/2 - 3/r^2) / r^3
+//   (3/2) f1 = -(3/2 + 3 hh) s - [(1 - 3E) t - (1 - 5E) p]
+//   (3/2) f2 = -(3/2 - 9 hh) s + 3 (1 - 5E) t - 5 (1 - 7E) p
+//   c3 = (3/2) f3 s = 3 h_j t - 18 hh Rz t + Rz s^2 [10 (2 - 7E) p - 6 (1 - 5E) t]
+//   c4 = (3/2) f4 s = 3 h_j t - 10 Rz s^2 p
+//   (3/2) f5 = -2 [3 (h_j^2 + E) t + (2 - 15E) p]
+// with t = s^3, p = s^5, E = (Rz s)^2, hh = h_i h_j s^2; for r <= 2
+// (3/2) A = 2 (1 - 9r/32), (3/2) Bc = 3 / (16 r).
+constexpr double kUFCoeffScale = 2.0 / 3.0;  // undoes the 3/2
 template <typename T> struct UFCoeffs {
     T Af, Bc, c2, c3, c4, Af5;  // Af5 = Af + f5, the zz diagonal
 };
@@ -139,33 +151,35 @@ __device__ __forceinline__ UFCoeffs<T> uf_coeffs(T dx, T dy, T dz, T Rz, T hi, T
     const T rho2 = dx * dx + dy * dy;
     const T r2 = rho2 + dz * dz;
     const T invr = rsq<T>(r2);
-    const T r = r2 * invr;
     const T Rz2 = Rz * Rz;
     const T s = rsq<T>(rho2 + Rz2);
-    const T s2 = s * s;
-    const T s3 = s2 * s;
-    const T E = Rz2 * s2;
+    const T u = s * s;
+    const T t = u * s;
+    const T p = t * u;
+    const T E = Rz2 * u;
     const T invr2 = invr * invr;
-    T A = (T(1) + T(2.0 / 3.0) * invr2) * invr;
-    T Bc = (T(1) - T(2) * invr2) * invr2 * invr;
-    const bool near = !(r > T(2));
+    const T invr3 = invr2 * invr;
+    T A = T(1.5) * invr + invr3;
+    T Bc = (T(1.5) - T(3) * invr2) * invr3;
+    const bool near = !(r2 > T(4));  // r <= 2
     if (__any_sync(__activemask(), near)) {
         if (near) {
-            A = T(4.0 / 3.0) * (T(1) - T(0.28125) * r);
-            Bc = T(0.125) * invr;
+            const T r = r2 * invr;
+            A = T(2) - T(0.5625) * r;
+            Bc = T(0.1875) * invr;
         }
     }
-    const T s5 = s3 * s2;
-    const T hh = hi * hj * s2;
-    const T ez = Rz * s;
-    const T q5 = (T(1) - T(5) * E) * s3;
-    const T f1 = -((T(1) + T(2) * hh) * s + T(2.0 / 3.0) * ((T(1) - T(3) * E) * s3 - q5 * s2));
-    const T f2 = -((T(1) - T(6) * hh) * s - T(2) * q5 + T(10.0 / 3.0) * (T(1) - T(7) * E) * s5);
-    const T f3 = T(2.0 / 3.0) * (T(3) * hj * s2 - T(18) * hh * ez * s + ez * (T(10) * (T(2) - T(7) * E) * s5 - T(6) * q5));
-    const T f4 = T(2.0 / 3.0) * (T(3) * hj * s2 - T(10) * ez * s5);
-    const T f5 = T(-4.0 / 3.0) * (T(3) * (hj * hj + E) * s3 + (T(2) - T(15) * E) * s5);
+    const T hh = hi * hj * u;
+    const T q5 = (T(1) - T(5) * E) * t;
+    const T Ru = Rz * u;
+    const T hjt3 = T(3) * hj * t;
+    const T f1 = -((T(1.5) + T(3) * hh) * s + ((T(1) - T(3) * E) * t - q5 * u));
+    const T f2 = T(3) * q5 - (T(1.5) - T(9) * hh) * s - T(5) * (T(1) - T(7) * E) * p;
+    const T c3 = hjt3 - T(18) * hh * Rz * t + Ru * (T(10) * (T(2) - T(7) * E) * p - T(6) * q5);
+    const T c4 = hjt3 - T(10) * Ru * p;
+    const T f5 = T(-2) * (T(3) * (hj * hj + E) * t + (T(2) - T(15) * E) * p);
     const T Af = A + f1;
-    return {Af, Bc, f2 * s2, f3 * s, f4 * s, Af + f5};
+    return {Af, Bc, f2 * u, c3, c4, Af + f5};
 }
 
 template <typename T>

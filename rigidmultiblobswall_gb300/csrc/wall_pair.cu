@@ -802,6 +802,7 @@ __global__ void wall_finalize_multi_kernel(const double *__restrict__ r, const d
         const double *p = partial + ((size_t)s * width + q) * 3 * n + 3 * (size_t)i;
         ux += p[0]; uy += p[1]; uz += p[2];
     }
+    ux *= kUFCoeffScale; uy *= kUFCoeffScale; uz *= kUFCoeffScale;  // the pair kernel sums (3/2) M v
     const double z = r[3 * i + 2];
     const double b = (z < a) ? z / a : 1.0;
     const double ze = (z <= a) ? a : z;
@@ -1000,10 +1001,9 @@ int wall_product_sym_with_scratch(const double *r, const double *v, double *out,
         wall_uf_mixed_sym_kernel<false><<<ncta, kThreads, 0, st>>>(src, n, nt, partial, nullptr);
     }
     if (int rc = trace_end(tok, st)) return rc;
-    // the df64 kernel sums (3/2) M_ij v_j
+    // both kernels sum (3/2) M_ij v_j
     wall_finalize_kernel<RMW_UF><<<pg, pb, 0, st>>>(r, v, partial, nt, out, n, a, 1.0 / (8.0 * kPi * eta * a),
-                                                     nullptr, nullptr, nullptr,
-                                                     mode == RMW_MODE_DF64 ? 2.0 / 3.0 : 1.0);
+                                                     nullptr, nullptr, nullptr, kUFCoeffScale);
     RMW_CHECK_LAUNCH("symmetric wall product kernels");
     return RMW_OK;
 }
@@ -1154,7 +1154,7 @@ int wall_product_batched(const WallBatch &B, int kind, const double *r, const do
         if (int rc2 = trace_end(tok, st)) return rc2;
         wall_finalize_kernel<RMW_UF><<<pg, pb, 0, st>>>(r, v, partial, 0, out, B.n, a, 1.0 / (8.0 * kPi * eta * a),
                                                          B.blob_nslots, B.blob_pbase, B.blob_pstride,
-                                                         mode == RMW_MODE_DF64 ? 2.0 / 3.0 : 1.0);
+                                                         kUFCoeffScale);
         RMW_CHECK_LAUNCH("segmented symmetric wall product");
         return RMW_OK;
     }

@@ -824,6 +824,12 @@ __global__ void wall_finalize_multi_kernel(const double *__restrict__ r, const d
 // finalize: fixed-order chunk sum + FP64 self term + b_i * norm factor.
 // With pbase / pstride (segmented symmetric layout) blob i's slot s is at
 // partial + pbase[i] + s * pstride[i]; otherwise at partial + s * 3n + 3i.
+// kFinGroup consecutive threads share a blob: thread g of the group sums slots
+// g, g + kFinGroup, ... and a fixed shuffle tree adds the group's sums, so the
+// order is fixed (deterministic) and the slot loads run kFinGroup-wide.
+constexpr int kFinGroup = 4;
+inline unsigned finalize_blocks(int n, int pb) { return (unsigned)(((long long)kFinGroup * n + pb - 1) / pb); }
+
 template <int KIND>
 __global__ void wall_finalize_kernel(const double *__restrict__ r, const double *__restrict__ v,
                                      const double *__restrict__ partial, int nchunks, double *__restrict__ out,
@@ -831,16 +837,25 @@ __global__ void wall_finalize_kernel(const double *__restrict__ r, const double 
                                      const long long *__restrict__ pbase = nullptr,
                                      const int *__restrict__ pstride = nullptr, double pair_scale = 1.0)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (int)(gt / kFinGroup), g = (int)(gt % kFinGroup);
     double ux = 0.0, uy = 0.0, uz = 0.0;
-    const int nc = blob_nchunks ? blob_nchunks[i] : nchunks;
-    const double *p0 = pbase ? partial + pbase[i] : partial + 3 * (size_t)i;
-    const size_t ps = pstride ? (size_t)pstride[i] : 3 * (size_t)n;
-    for (int s = 0; s < nc; ++s) {
-        const double *p = p0 + (size_t)s * ps;
-        ux += p[0]; uy += p[1]; uz += p[2];
+    if (i < n) {
+        const int nc = blob_nchunks ? blob_nchunks[i] : nchunks;
+        const double *p0 = pbase ? partial + pbase[i] : partial + 3 * (size_t)i;
+        const size_t ps = pstride ? (size_t)pstride[i] : 3 * (size_t)n;
+        for (int s = g; s < nc; s += kFinGroup) {
+            const double *p = p0 + (size_t)s * ps;
+            ux += p[0]; uy += p[1]; uz += p[2];
+        }
     }
+#pragma unroll
+    for (int o = kFinGroup / 2; o > 0; o >>= 1) {  // every lane of the warp takes part
+        ux += __shfl_down_sync(0xffffffffu, ux, o, kFinGroup);
+        uy += __shfl_down_sync(0xffffffffu, uy, o, kFinGroup);
+        uz += __shfl_down_sync(0xffffffffu, uz, o, kFinGroup);
+    }
+    if (i >= n || g != 0) return;
     ux *= pair_scale; uy *= pair_scale; uz *= pair_scale;
     const double z = r[3 * i + 2];
     const double b = (z < a) ? z / a : 1.0;
@@ -932,7 +947,8 @@ static int launch_kind(const double *r, const double *v, double *out, int n, dou
         else wall_pair_mixed_kernel<KIND, false, false><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial, jobs);
     }
     if (int rc = trace_end(tok, st)) return rc;
-    wall_finalize_kernel<KIND><<<pg, pb, 0, st>>>(r, v, partial, nchunks, out, n, a, nf, B ? B->blob_nch : nullptr);
+    wall_finalize_kernel<KIND><<<finalize_blocks(n, pb), pb, 0, st>>>(r, v, partial, nchunks, out, n, a, nf,
+                                                                       B ? B->blob_nch : nullptr);
     RMW_CHECK_LAUNCH("wall product kernels");
     return RMW_OK;
 }
@@ -1002,7 +1018,8 @@ int wall_product_sym_with_scratch(const double *r, const double *v, double *out,
     }
     if (int rc = trace_end(tok, st)) return rc;
     // both kernels sum (3/2) M_ij v_j
-    wall_finalize_kernel<RMW_UF><<<pg, pb, 0, st>>>(r, v, partial, nt, out, n, a, 1.0 / (8.0 * kPi * eta * a),
+    wall_finalize_kernel<RMW_UF><<<finalize_blocks(n, pb), pb, 0, st>>>(r, v, partial, nt, out, n, a,
+                                                                         1.0 / (8.0 * kPi * eta * a),
                                                      nullptr, nullptr, nullptr, kUFCoeffScale);
     RMW_CHECK_LAUNCH("symmetric wall product kernels");
     return RMW_OK;
@@ -1152,7 +1169,8 @@ int wall_product_batched(const WallBatch &B, int kind, const double *r, const do
                                                                                   B.sym_jobs);
         }
         if (int rc2 = trace_end(tok, st)) return rc2;
-        wall_finalize_kernel<RMW_UF><<<pg, pb, 0, st>>>(r, v, partial, 0, out, B.n, a, 1.0 / (8.0 * kPi * eta * a),
+        wall_finalize_kernel<RMW_UF><<<finalize_blocks(B.n, pb), pb, 0, st>>>(r, v, partial, 0, out, B.n, a,
+                                                                           1.0 / (8.0 * kPi * eta * a),
                                                          B.blob_nslots, B.blob_pbase, B.blob_pstride,
                                                          kUFCoeffScale);
         RMW_CHECK_LAUNCH("segmented symmetric wall product");

@@ -38,14 +38,14 @@ WORKLOAD = "wall-RPY M_UF.F, 256 shells x 42 blobs = 10,752 blobs (FP64-accurate
 # Issued thread instructions per ordered pair of the df64 UF kernels (all
 # pipes, 80-85 % of them on the FMA pipe), from the ncu captures summarised in
 # profiles/wall_uf_df_sym_shells42x256.md (symmetric kernel, each unordered
-# pair once: smsp__inst_executed.sum * 32 / N^2 = 1,943,113,592 * 32 / 10752^2
-# = 537.9) and profiles/wall_pair_df64_uf_shells42x256.md (standard kernel:
+# pair once: smsp__inst_executed.sum * 32 / N^2 = 1,704,728,972 * 32 / 10752^2
+# = 471.9) and profiles/wall_pair_df64_uf_shells42x256.md (standard kernel:
 # 3,310,220,558 * 32 / 10752^2 = 916.3).  The FP32 pipe issues at most one
 # thread instruction per lane per clock, the rate the FMA-chain probe measures
 # (FLOP/s / 2), so achieved / peak is the fraction of issue capacity used.
-DF64_UF_INST_PER_PAIR = {"symmetric": 1943113592.0 * 32 / 10752 ** 2, "standard": 3310220558.0 * 32 / 10752 ** 2}
+DF64_UF_INST_PER_PAIR = {"symmetric": 1704728972.0 * 32 / 10752 ** 2, "standard": 3310220558.0 * 32 / 10752 ** 2}
 # dram__bytes_read.sum + dram__bytes_write.sum per launch, same captures
-DF64_UF_TRAFFIC_BYTES = {"symmetric": 739840, "standard": 723456}
+DF64_UF_TRAFFIC_BYTES = {"symmetric": 735744, "standard": 723456}
 
 
 def parse():

@@ -186,6 +186,27 @@ __device__ __forceinline__ void acc_dot2(df &acc, df a, df b, df c, df d)
     acc.lo = __fadd_rn(acc.lo, __fadd_rn(__fadd_rn(t1.lo, t2.lo), __fadd_rn(e1, e2)));
 }
 
+// acc += a*b + c*d + e*f without renormalising acc
+__device__ __forceinline__ void acc_dot3(df &acc, df a, df b, df c, df d, df e, df f)
+{
+    const float p1 = __fmul_rn(a.hi, b.hi), p2 = __fmul_rn(c.hi, d.hi), p3 = __fmul_rn(e.hi, f.hi);
+    float e1 = fmaf(a.hi, b.hi, -p1);
+    e1 = fmaf(a.hi, b.lo, e1);
+    e1 = fmaf(a.lo, b.hi, e1);
+    float e2 = fmaf(c.hi, d.hi, -p2);
+    e2 = fmaf(c.hi, d.lo, e2);
+    e2 = fmaf(c.lo, d.hi, e2);
+    float e3 = fmaf(e.hi, f.hi, -p3);
+    e3 = fmaf(e.hi, f.lo, e3);
+    e3 = fmaf(e.lo, f.hi, e3);
+    const df t1 = two_sum_df(acc.hi, p1);
+    const df t2 = two_sum_df(t1.hi, p2);
+    const df t3 = two_sum_df(t2.hi, p3);
+    acc.hi = t3.hi;
+    const float lo = __fadd_rn(__fadd_rn(t1.lo, t2.lo), t3.lo);
+    acc.lo = __fadd_rn(acc.lo, __fadd_rn(lo, __fadd_rn(__fadd_rn(e1, e2), e3)));
+}
+
 // acc += a*b + c*d + e*f + g*h without renormalising acc
 __device__ __forceinline__ void acc_dot4(df &acc, df a, df b, df c, df d, df e, df f, df g, df h)
 {

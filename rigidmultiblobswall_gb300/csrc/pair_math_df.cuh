@@ -258,4 +258,124 @@ __device__ __forceinline__ void pair_uf_sym_df(df dx, df dy, df dz, df Rz, df hi
     }
 }
 
+// ---------------------------------------------------------------------------
+// Symmetric forms of the rotation blocks.  With d = r_i - r_j, M_ji is the
+// same formula as M_ij with d -> -d and h_i <-> h_j (the grand mobility is
+// symmetric, M_ji = M_ij^T): the WT coefficients do not involve the heights,
+// so its reverse block only flips d; the UT and WF coefficients depend on one
+// height (UT: the target's, WF: the source's), so both height sets are formed
+// and the reverse block uses the other one.  Shared per pair: the distances,
+// both reciprocal square roots and the powers of s = 1/|R|.
+
+// The height-dependent coefficients of UT / WF for height h (unnormalised
+// where only a sum consumes them).
+struct RotHDF {
+    df f3s2, p, gs;  // f3 s^2, p = s^2 ez + f4, g s with g = f3 ez + s^2 + f2
+};
+__device__ __forceinline__ RotHDF rot_h_df(df h, df s, df s2, df s3, df ez, df ezs4, df K)
+{
+    const df hs3 = h * s3;
+    const df f2 = scale2(mad_u(hs3 * 6.0f, ez, K), 2.0f);
+    const df f3 = scale2(mul_u(hs3, 3.0f) - mul_u(ezs4, 5.0f), -2.0f);
+    const df f4 = scale2(sub_u(hs3, ezs4), -2.0f);
+    const df p = mad(s2, ez, f4);
+    const df g = mad(f3, ez, s2 + f2);
+    return {f3 * s2, p, g * s};
+}
+
+// (ux, uy, uz) += M_UT v for the pair (d, coefficient set H)
+__device__ __forceinline__ void ut_apply_df(df c, const RotHDF &H, df s3, df dx, df dy, df dz, df vx, df vy, df vz,
+                                            df &ux, df &uy, df &uz)
+{
+    const df Q = mad2(dy, vx, -dx, vy);  // (v x d)_z
+    const df X = mad2(vy, dz, -vz, dy), Y = mad2(vz, dx, -vx, dz);
+    const df F3 = H.f3s2 * Q, F1 = s3 * vz;
+    acc_dot4(ux, c, X, F3, dx, F1, dy, H.p, vy);
+    acc_dot4(uy, c, Y, F3, dy, F1, -dx, H.p, -vx);
+    acc_dot2(uz, c, Q, H.gs, -Q);
+}
+
+// (ux, uy, uz) += M_WF v for the pair (d, coefficient set H)
+__device__ __forceinline__ void wf_apply_df(df c, const RotHDF &H, df s3, df dx, df dy, df dz, df vx, df vy, df vz,
+                                            df &ux, df &uy, df &uz)
+{
+    const df Pxy = mad2(dx, vx, dy, vy);
+    const df Q = mad2(dy, vx, -dx, vy);
+    const df X = mad2(vy, dz, -vz, dy), Y = mad2(vz, dx, -vx, dz);
+    const df Hh = mad2(H.f3s2, Pxy, H.gs, vz);
+    acc_dot3(ux, c, X, Hh, dy, H.p, -vy);
+    acc_dot3(uy, c, Y, H.p, vx, Hh, -dx);
+    acc_dot2(uz, c, Q, s3, -Q);
+}
+
+// (ux, uy, uz) += M_WT v for the pair (d; Af = A + (1 - 6E) s^3 / 2, Bc, s^5)
+__device__ __forceinline__ void wt_apply_df(df Af, df Bc, df s5, df dx, df dy, df dz, df Rz, df vx, df vy, df vz,
+                                            df &ux, df &uy, df &uz)
+{
+    const df Pxy = mad2(dx, vx, dy, vy);
+    const df dv = mad(dz, vz, Pxy);
+    const df W = mad(Rz, vz, Pxy);
+    const df Q = mad2(dy, vx, -dx, vy);
+    const df Gw = (s5 * W) * -1.5f;
+    const df Tq = (s5 * Q) * 3.0f;
+    const df Gr = Bc * dv;
+    const df G = Gr + Gw;
+    acc_dot3(ux, Af, vx, G, dx, Tq, dy);
+    acc_dot3(uy, Af, vy, G, dy, Tq, -dx);
+    acc_dot3(uz, Af, vz, Gr, dz, Gw, -Rz);
+}
+
+// UT, WF or WT for both orders of one pair: (ux, uy, uz) += M_ij v_j for
+// target i, (wx, wy, wz) += M_ji v_i for target j.
+template <int KIND>
+__device__ __forceinline__ void pair_rot_sym_df(df dx, df dy, df dz, df Rz, df hi, df hj, df vx, df vy, df vz,
+                                                df qx, df qy, df qz, df &ux, df &uy, df &uz, df &wx, df &wy,
+                                                df &wz)
+{
+    const df rho2 = mad_u(dx, dx, sqr_u(dy));
+    const df r2 = mad(dz, dz, rho2);
+    const df invr = rsqrt_df(r2);
+    const df Rz2 = sqr(Rz);
+    const df s = rsqrt_df(rho2 + Rz2);
+    const df s2 = sqr(s);
+    const df s3 = s2 * s;
+    const df E = Rz2 * s2;
+    const bool near = !(r2 >= 4.0f);  // r < 2
+    if (KIND == RMW_WT) {
+        const df invr2 = sqr(invr);
+        const df invr3 = invr2 * invr;
+        df A = invr3 * -0.5f;
+        df Bc = (invr2 * invr3) * 1.5f;
+        if (__any_sync(__activemask(), near)) {
+            if (near) {
+                const df r = r2 * invr;
+                A = (1.0f - r * 0.84375f) + (r * r2) * 0.078125f;
+                Bc = invr * 0.28125f - r * 0.046875f;
+            }
+        }
+        const df s5 = s3 * s2;
+        const df Af = A + scale2((1.0f - E * 6.0f) * s3, 0.5f);
+        wt_apply_df(Af, Bc, s5, dx, dy, dz, Rz, vx, vy, vz, ux, uy, uz);
+        wt_apply_df(Af, Bc, s5, -dx, -dy, -dz, Rz, qx, qy, qz, wx, wy, wz);
+    } else {
+        df c = sqr(invr) * invr;
+        if (__any_sync(__activemask(), near)) {
+            if (near) c = scale2(1.0f - (r2 * invr) * 0.375f, 0.5f);
+        }
+        const df s4 = sqr(s2);
+        const df ez = Rz * s;
+        const df ezs4 = ez * s4;
+        const df K = mul_u(1.0f - mul_u(E, 10.0f), s4);
+        const RotHDF Hi = rot_h_df(hi, s, s2, s3, ez, ezs4, K);
+        const RotHDF Hj = rot_h_df(hj, s, s2, s3, ez, ezs4, K);
+        if (KIND == RMW_UT) {
+            ut_apply_df(c, Hi, s3, dx, dy, dz, vx, vy, vz, ux, uy, uz);
+            ut_apply_df(c, Hj, s3, -dx, -dy, -dz, qx, qy, qz, wx, wy, wz);
+        } else {
+            wf_apply_df(c, Hj, s3, dx, dy, dz, vx, vy, vz, ux, uy, uz);
+            wf_apply_df(c, Hi, s3, -dx, -dy, -dz, qx, qy, qz, wx, wy, wz);
+        }
+    }
+}
+
 }  // namespace rmw

@@ -278,10 +278,9 @@ __device__ __forceinline__ void sym_cta(const SymJob *jobs, int &n, int &nt, int
     }
 }
 
-template <bool SEG>
-__global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *__restrict__ src, int n, int nt,
-                                                                   double *__restrict__ partial,
-                                                                   const SymJob *__restrict__ jobs)
+template <bool SEG, int KIND>
+__device__ __forceinline__ void df_sym_body(const SrcDF *__restrict__ src, int n, int nt,
+                                            double *__restrict__ partial, const SymJob *__restrict__ jobs)
 {
     // structure-of-arrays source tile: the rotated reads of a warp hit 32
     // consecutive 16-byte entries (no bank conflicts)
@@ -330,8 +329,12 @@ __global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *_
         df wx = {a0.x, a0.y}, wy = {a1.x, a1.y}, wz = {a2.x, a2.y};
         // differences renormalised (a cancelled high part must not leave the value in the low part, whose
         // square a double-float product drops); the sum of two heights cannot cancel
-        pair_uf_sym_df(xi - xj, yi - yj, zi - zj, add_u(zi, zj), zi, zj, vx, vy, vz, qx, qy, qz, ux, uy, uz, wx, wy,
-                       wz);
+        if constexpr (KIND == RMW_UF)
+            pair_uf_sym_df(xi - xj, yi - yj, zi - zj, add_u(zi, zj), zi, zj, vx, vy, vz, qx, qy, qz, ux, uy, uz, wx,
+                           wy, wz);
+        else
+            pair_rot_sym_df<KIND>(xi - xj, yi - yj, zi - zj, add_u(zi, zj), zi, zj, vx, vy, vz, qx, qy, qz, ux, uy,
+                                  uz, wx, wy, wz);
         sacc[warp][0][jl] = make_float2(wx.hi, wx.lo);
         sacc[warp][1][jl] = make_float2(wy.hi, wy.lo);
         sacc[warp][2][jl] = make_float2(wz.hi, wz.lo);
@@ -385,16 +388,32 @@ __global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *_
     }
 }
 
+template <bool SEG>
+__global__ void __launch_bounds__(kThreads) wall_uf_df_sym_kernel(const SrcDF *__restrict__ src, int n, int nt,
+                                                                   double *__restrict__ partial,
+                                                                   const SymJob *__restrict__ jobs)
+{
+    df_sym_body<SEG, RMW_UF>(src, n, nt, partial, jobs);
+}
+
+// The rotation blocks (UT, WF, WT) on the same grid: pair_rot_sym_df.
+template <bool SEG, int KIND>
+__global__ void __launch_bounds__(kThreads) wall_rot_df_sym_kernel(const SrcDF *__restrict__ src, int n, int nt,
+                                                                    double *__restrict__ partial,
+                                                                    const SymJob *__restrict__ jobs)
+{
+    df_sym_body<SEG, KIND>(src, n, nt, partial, jobs);
+}
+
 // Symmetric mixed-precision UF kernel: the same grid, pairing and partial-sum
 // slots as wall_uf_df_sym_kernel, FP32 pair math from double-float position
 // differences (as wall_pair_mixed_kernel).  The target-side FP32 sum over the
 // tile is folded into a TwoSum-compensated accumulator; the source side sums
 // its 32 contributions per warp in FP32 shared memory and the four warp
 // copies in FP64.
-template <bool SEG>
-__global__ void __launch_bounds__(kThreads) wall_uf_mixed_sym_kernel(const SrcF *__restrict__ src, int n, int nt,
-                                                                      double *__restrict__ partial,
-                                                                      const SymJob *__restrict__ jobs)
+template <bool SEG, int KIND>
+__device__ __forceinline__ void mixed_sym_body(const SrcF *__restrict__ src, int n, int nt,
+                                               double *__restrict__ partial, const SymJob *__restrict__ jobs)
 {
     __shared__ float4 thi[kTile], tlo[kTile], tv[kTile];
     __shared__ float sacc[kSymWarps][3][kTile];
@@ -427,11 +446,16 @@ __global__ void __launch_bounds__(kThreads) wall_uf_mixed_sym_kernel(const SrcF 
         const float dz = (me.hi.z - sh.z) + (me.lo.z - sl.z);
         const float hj = sh.z + sl.z;
         const float Rz = hi + hj;
-        const UFCoeffs<float> c = uf_coeffs<float>(dx, dy, dz, Rz, hi, hj);
-        uf_apply<float>(c, dx, dy, dz, Rz, sv.x, sv.y, sv.z, ux, uy, uz);
-        const UFCoeffs<float> ct = {c.Af, c.Bc, c.c2, c.c4, c.c3, c.Af5};  // M^T: f3 and f4 trade places
         float wx = sacc[warp][0][jl], wy = sacc[warp][1][jl], wz = sacc[warp][2][jl];
-        uf_apply<float>(ct, dx, dy, dz, Rz, me.v.x, me.v.y, me.v.z, wx, wy, wz);
+        if constexpr (KIND == RMW_UF) {
+            const UFCoeffs<float> c = uf_coeffs<float>(dx, dy, dz, Rz, hi, hj);
+            uf_apply<float>(c, dx, dy, dz, Rz, sv.x, sv.y, sv.z, ux, uy, uz);
+            const UFCoeffs<float> ct = {c.Af, c.Bc, c.c2, c.c4, c.c3, c.Af5};  // M^T: f3 and f4 trade places
+            uf_apply<float>(ct, dx, dy, dz, Rz, me.v.x, me.v.y, me.v.z, wx, wy, wz);
+        } else {
+            pair_rot_sym_f<KIND>(dx, dy, dz, Rz, hi, hj, sv.x, sv.y, sv.z, me.v.x, me.v.y, me.v.z, ux, uy, uz, wx, wy,
+                                 wz);
+        }
         sacc[warp][0][jl] = wx;
         sacc[warp][1][jl] = wy;
         sacc[warp][2][jl] = wz;
@@ -480,6 +504,22 @@ __global__ void __launch_bounds__(kThreads) wall_uf_mixed_sym_kernel(const SrcF 
             o[0] = qx; o[1] = qy; o[2] = qz;
         }
     }
+}
+
+template <bool SEG>
+__global__ void __launch_bounds__(kThreads) wall_uf_mixed_sym_kernel(const SrcF *__restrict__ src, int n, int nt,
+                                                                      double *__restrict__ partial,
+                                                                      const SymJob *__restrict__ jobs)
+{
+    mixed_sym_body<SEG, RMW_UF>(src, n, nt, partial, jobs);
+}
+
+template <bool SEG, int KIND>
+__global__ void __launch_bounds__(kThreads) wall_rot_mixed_sym_kernel(const SrcF *__restrict__ src, int n, int nt,
+                                                                       double *__restrict__ partial,
+                                                                       const SymJob *__restrict__ jobs)
+{
+    mixed_sym_body<SEG, KIND>(src, n, nt, partial, jobs);
 }
 
 // ---------------------------------------------------------------------------
@@ -985,7 +1025,7 @@ int wall_product_with_scratch(int kind, const double *r, const double *v, double
 
 bool wall_sym_applicable(int kind, int mode, int n, const double *L)
 {
-    if (kind != RMW_UF || (mode != RMW_MODE_DF64 && mode != RMW_MODE_MIXED)) return false;
+    if (kind < RMW_UF || kind > RMW_WT || (mode != RMW_MODE_DF64 && mode != RMW_MODE_MIXED)) return false;
     if (L && (L[0] > 0 || L[1] > 0 || L[2] > 0)) return false;
     if (n < 2 * kTile) return false;
     const double nt = (double)((n + kTile - 1) / kTile);
@@ -994,35 +1034,92 @@ bool wall_sym_applicable(int kind, int mode, int n, const double *L)
 
 int wall_sym_slots(int n) { return (n + kTile - 1) / kTile; }
 
-int wall_product_sym_with_scratch(const double *r, const double *v, double *out, int n, double eta, double a,
-                                  int mode, cudaStream_t st, void *scratch_ptr)
+// the symmetric kernel and finalize of one kind: the UF kernels sum (3/2) M v
+template <int KIND>
+static void launch_sym(bool seg, int mode, const void *src, int n, int nt, unsigned ncta, double *partial,
+                       const SymJob *jobs, cudaStream_t st)
 {
-    const int nt = wall_sym_slots(n);
+    if (mode == RMW_MODE_DF64) {
+        const SrcDF *s = (const SrcDF *)src;
+        if (KIND == RMW_UF) {
+            if (seg) wall_uf_df_sym_kernel<true><<<ncta, kThreads, 0, st>>>(s, n, nt, partial, jobs);
+            else wall_uf_df_sym_kernel<false><<<ncta, kThreads, 0, st>>>(s, n, nt, partial, jobs);
+        } else {
+            if (seg) wall_rot_df_sym_kernel<true, KIND><<<ncta, kThreads, 0, st>>>(s, n, nt, partial, jobs);
+            else wall_rot_df_sym_kernel<false, KIND><<<ncta, kThreads, 0, st>>>(s, n, nt, partial, jobs);
+        }
+    } else {
+        const SrcF *s = (const SrcF *)src;
+        if (KIND == RMW_UF) {
+            if (seg) wall_uf_mixed_sym_kernel<true><<<ncta, kThreads, 0, st>>>(s, n, nt, partial, jobs);
+            else wall_uf_mixed_sym_kernel<false><<<ncta, kThreads, 0, st>>>(s, n, nt, partial, jobs);
+        } else {
+            if (seg) wall_rot_mixed_sym_kernel<true, KIND><<<ncta, kThreads, 0, st>>>(s, n, nt, partial, jobs);
+            else wall_rot_mixed_sym_kernel<false, KIND><<<ncta, kThreads, 0, st>>>(s, n, nt, partial, jobs);
+        }
+    }
+}
+
+static double kind_norm(int kind, double eta, double a)
+{
+    return (kind == RMW_UF)   ? 1.0 / (8.0 * kPi * eta * a)
+           : (kind == RMW_WT) ? 1.0 / (8.0 * kPi * eta * a * a * a)
+                              : 1.0 / (8.0 * kPi * eta * a * a);
+}
+
+template <int KIND>
+static void launch_sym_finalize(const double *r, const double *v, const double *partial, int nt, double *out, int n,
+                                double a, double nf, const WallBatch *B, cudaStream_t st)
+{
+    const int pb = 256;
+    const double scale = (KIND == RMW_UF) ? kUFCoeffScale : 1.0;
+    if (B)
+        wall_finalize_kernel<KIND><<<finalize_blocks(n, pb), pb, 0, st>>>(r, v, partial, 0, out, n, a, nf,
+                                                                          B->blob_nslots, B->blob_pbase,
+                                                                          B->blob_pstride, scale);
+    else
+        wall_finalize_kernel<KIND><<<finalize_blocks(n, pb), pb, 0, st>>>(r, v, partial, nt, out, n, a, nf, nullptr,
+                                                                          nullptr, nullptr, scale);
+}
+
+// pack, symmetric pair kernel and finalize of any kind (B: segmented over its suspensions)
+static int sym_product(int kind, const double *r, const double *v, double *out, int n, double eta, double a,
+                       int mode, cudaStream_t st, void *scratch_ptr, const WallBatch *B)
+{
+    const int nt = B ? 0 : wall_sym_slots(n);
     const size_t rec = (mode == RMW_MODE_DF64) ? sizeof(SrcDF) : sizeof(SrcF);
     const size_t packed = ((rec * (size_t)n + 255) / 256) * 256;
     char *base = (char *)scratch_ptr;
     double *partial = (double *)(base + packed);
     const int pb = 256, pg = (n + pb - 1) / pb;
-    const unsigned ncta = (unsigned)((long long)nt * (nt + 1) / 2);
+    const unsigned ncta = B ? (unsigned)B->nsym : (unsigned)((long long)nt * (nt + 1) / 2);
+    const SymJob *jobs = B ? B->sym_jobs : nullptr;
+    if (mode == RMW_MODE_DF64) pack_df_kernel<<<pg, pb, 0, st>>>(r, v, (SrcDF *)base, n, a);
+    else pack_mixed_kernel<<<pg, pb, 0, st>>>(r, v, (SrcF *)base, n, a);
     void *tok = nullptr;
-    if (mode == RMW_MODE_DF64) {
-        SrcDF *src = (SrcDF *)base;
-        pack_df_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
-        if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
-        wall_uf_df_sym_kernel<false><<<ncta, kThreads, 0, st>>>(src, n, nt, partial, nullptr);
-    } else {
-        SrcF *src = (SrcF *)base;
-        pack_mixed_kernel<<<pg, pb, 0, st>>>(r, v, src, n, a);
-        if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
-        wall_uf_mixed_sym_kernel<false><<<ncta, kThreads, 0, st>>>(src, n, nt, partial, nullptr);
+    if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
+    switch (kind) {
+    case RMW_UF: launch_sym<RMW_UF>(B != nullptr, mode, base, n, nt, ncta, partial, jobs, st); break;
+    case RMW_UT: launch_sym<RMW_UT>(B != nullptr, mode, base, n, nt, ncta, partial, jobs, st); break;
+    case RMW_WF: launch_sym<RMW_WF>(B != nullptr, mode, base, n, nt, ncta, partial, jobs, st); break;
+    default: launch_sym<RMW_WT>(B != nullptr, mode, base, n, nt, ncta, partial, jobs, st); break;
     }
     if (int rc = trace_end(tok, st)) return rc;
-    // both kernels sum (3/2) M_ij v_j
-    wall_finalize_kernel<RMW_UF><<<finalize_blocks(n, pb), pb, 0, st>>>(r, v, partial, nt, out, n, a,
-                                                                         1.0 / (8.0 * kPi * eta * a),
-                                                     nullptr, nullptr, nullptr, kUFCoeffScale);
+    const double nf = kind_norm(kind, eta, a);
+    switch (kind) {
+    case RMW_UF: launch_sym_finalize<RMW_UF>(r, v, partial, nt, out, n, a, nf, B, st); break;
+    case RMW_UT: launch_sym_finalize<RMW_UT>(r, v, partial, nt, out, n, a, nf, B, st); break;
+    case RMW_WF: launch_sym_finalize<RMW_WF>(r, v, partial, nt, out, n, a, nf, B, st); break;
+    default: launch_sym_finalize<RMW_WT>(r, v, partial, nt, out, n, a, nf, B, st); break;
+    }
     RMW_CHECK_LAUNCH("symmetric wall product kernels");
     return RMW_OK;
+}
+
+int wall_product_sym_with_scratch(int kind, const double *r, const double *v, double *out, int n, double eta,
+                                  double a, int mode, cudaStream_t st, void *scratch_ptr)
+{
+    return sym_product(kind, r, v, out, n, eta, a, mode, st, scratch_ptr, nullptr);
 }
 
 int wall_product(int kind, const double *r, const double *v, double *out, int64_t n, double eta, double a,
@@ -1037,7 +1134,7 @@ int wall_product(int kind, const double *r, const double *v, double *out, int64_
     void *ws = nullptr;
     rc = scratch(SCRATCH_PAIR, wall_scratch_bytes((int)n, mode, sym ? wall_sym_slots((int)n) : nchunks), &ws, st);
     if (rc) return rc;
-    if (sym) return wall_product_sym_with_scratch(r, v, out, (int)n, eta, a, mode, st, ws);
+    if (sym) return wall_product_sym_with_scratch(kind, r, v, out, (int)n, eta, a, mode, st, ws);
     return wall_product_with_scratch(kind, r, v, out, (int)n, eta, a, L, mode, st, ws, nchunks);
 }
 
@@ -1147,34 +1244,14 @@ int wall_product_batched(const WallBatch &B, int kind, const double *r, const do
     if (rc) return rc;
     if (B.n == 0 || B.njobs == 0) return RMW_OK;
     void *ws = nullptr;
-    if (kind == RMW_UF && (mode == RMW_MODE_DF64 || mode == RMW_MODE_MIXED) && B.nsym > 0 &&
+    if ((mode == RMW_MODE_DF64 || mode == RMW_MODE_MIXED) && B.nsym > 0 &&
         B.sym_doubles * (long long)sizeof(double) <= (long long)kSymMaxPartialBytes) {
         // each suspension's unordered pairs once, applied both ways
         const size_t rec = (mode == RMW_MODE_DF64) ? sizeof(SrcDF) : sizeof(SrcF);
         const size_t packed = ((rec * (size_t)B.n + 255) / 256) * 256;
         rc = scratch(SCRATCH_PAIR, packed + sizeof(double) * (size_t)B.sym_doubles, &ws, st);
         if (rc) return rc;
-        double *partial = (double *)((char *)ws + packed);
-        const int pb = 256, pg = (B.n + pb - 1) / pb;
-        void *tok = nullptr;
-        if (mode == RMW_MODE_DF64) {
-            pack_df_kernel<<<pg, pb, 0, st>>>(r, v, (SrcDF *)ws, B.n, a);
-            if (int rc2 = trace_begin(TRACE_PAIR, st, &tok)) return rc2;
-            wall_uf_df_sym_kernel<true><<<(unsigned)B.nsym, kThreads, 0, st>>>((const SrcDF *)ws, 0, 0, partial,
-                                                                               B.sym_jobs);
-        } else {
-            pack_mixed_kernel<<<pg, pb, 0, st>>>(r, v, (SrcF *)ws, B.n, a);
-            if (int rc2 = trace_begin(TRACE_PAIR, st, &tok)) return rc2;
-            wall_uf_mixed_sym_kernel<true><<<(unsigned)B.nsym, kThreads, 0, st>>>((const SrcF *)ws, 0, 0, partial,
-                                                                                  B.sym_jobs);
-        }
-        if (int rc2 = trace_end(tok, st)) return rc2;
-        wall_finalize_kernel<RMW_UF><<<finalize_blocks(B.n, pb), pb, 0, st>>>(r, v, partial, 0, out, B.n, a,
-                                                                           1.0 / (8.0 * kPi * eta * a),
-                                                         B.blob_nslots, B.blob_pbase, B.blob_pstride,
-                                                         kUFCoeffScale);
-        RMW_CHECK_LAUNCH("segmented symmetric wall product");
-        return RMW_OK;
+        return sym_product(kind, r, v, out, B.n, eta, a, mode, st, ws, &B);
     }
     rc = scratch(SCRATCH_PAIR, wall_scratch_bytes(B.n, mode, B.max_slots), &ws, st);
     if (rc) return rc;

@@ -56,17 +56,17 @@ int wall_product_batched(const WallBatch &B, int kind, const double *r, const do
 
 // Source-chunk count of the built-in rule for n blobs.
 int wall_default_chunks(int n);
-// Symmetric UF product (each unordered pair once, applied both ways), df64 or
-// mixed: selected when wall_chunks returns kSymChunks and wall_sym_applicable
-// holds (UF, df64 or mixed, not periodic, n >= 256, ntiles x 3n doubles of
-// partial sums within kSymMaxPartialBytes).  Its scratch is wall_scratch_bytes(n, mode,
-// wall_sym_slots(n)).
+// Symmetric product of any kind (each unordered pair once, applied both ways),
+// df64 or mixed: selected when wall_chunks returns kSymChunks and
+// wall_sym_applicable holds (df64 or mixed, not periodic, n >= 256, ntiles x
+// 3n doubles of partial sums within kSymMaxPartialBytes).  Its scratch is
+// wall_scratch_bytes(n, mode, wall_sym_slots(n)).
 constexpr int kSymChunks = -1;
 constexpr size_t kSymMaxPartialBytes = size_t(6) << 30;  // up to ~185,000 blobs (5.5 GB at 172,032)
 bool wall_sym_applicable(int kind, int mode, int n, const double *L);
 int wall_sym_slots(int n);
-int wall_product_sym_with_scratch(const double *r, const double *v, double *out, int n, double eta, double a,
-                                  int mode, cudaStream_t st, void *scratch_ptr);
+int wall_product_sym_with_scratch(int kind, const double *r, const double *v, double *out, int n, double eta,
+                                  double a, int mode, cudaStream_t st, void *scratch_ptr);
 // Source-chunk count the standard entry points use: the autotuned choice of
 // (kind, mode, n's size bucket) on the current device if there is one
 // (autotune.cu; kSymChunks = the symmetric kernel), else the built-in rule.

@@ -1,6 +1,7 @@
-"""GPU: the symmetric M_UF kernels, df64 and mixed (each unordered pair
-evaluated once and applied both ways) against the oracle and against the
-standard kernels:
+"""GPU: the symmetric kernels of all four blocks, df64 and mixed (each
+unordered pair evaluated once and applied both ways: M_UF with f3 and f4
+exchanged, the rotation blocks with d -> -d and the heights exchanged)
+against the oracle and against the standard kernels:
 tile tails, diagonal-tile pairing, wall-overlapping (damped) blobs, a shell
 suspension, determinism, and the fallback where it does not apply."""
 import numpy as np
@@ -23,51 +24,57 @@ def _blobs(n, seed, damped=False):
     return r, rng.standard_normal(3 * n)
 
 
-def _product(r, v, a, pin, mode="df64"):
+def _product(r, v, a, pin, mode="df64", kind="uf"):
     import torch
     mob.autotune_clear()
     if pin is not None:
-        mob.autotune_set("uf", len(r), mode, pin)
-    out = mob.wall_product("uf", torch.tensor(r, device="cuda"), torch.tensor(v, device="cuda"), 1.0, a,
+        mob.autotune_set(kind, len(r), mode, pin)
+    out = mob.wall_product(kind, torch.tensor(r, device="cuda"), torch.tensor(v, device="cuda"), 1.0, a,
                            mode=mode).cpu().numpy()
     mob.autotune_clear()
     return out
 
 
+KINDS = ["uf", "ut", "wf", "wt"]
+
+
+@pytest.mark.parametrize("kind", KINDS)
 @pytest.mark.parametrize("n", [256, 257, 300, 383, 1000, 2049])
 @pytest.mark.parametrize("damped", [False, True])
-def test_symmetric_matches_oracle_and_standard(cuda_device, n, damped):
+def test_symmetric_matches_oracle_and_standard(cuda_device, kind, n, damped):
     r, v = _blobs(n, n, damped)
     a = 0.35
-    sym = _product(r, v, a, -1)
-    std = _product(r, v, a, 8)
-    ref = owall.wall_product("uf", r, v, 1.0, a)
+    sym = _product(r, v, a, -1, kind=kind)
+    std = _product(r, v, a, 8, kind=kind)
+    ref = owall.wall_product(kind, r, v, 1.0, a)
     assert rel_err(sym, ref) <= 1e-12
     assert rel_err(sym, std) <= 1e-13
 
 
+@pytest.mark.parametrize("kind", KINDS)
 @pytest.mark.parametrize("n", [256, 300, 1000, 2049])
 @pytest.mark.parametrize("damped", [False, True])
-def test_mixed_symmetric_matches_oracle_and_standard(cuda_device, n, damped):
+def test_mixed_symmetric_matches_oracle_and_standard(cuda_device, kind, n, damped):
     r, v = _blobs(n, n + 1, damped)
     a = 0.35
-    sym = _product(r, v, a, -1, "mixed")
-    std = _product(r, v, a, 8, "mixed")
-    ref = owall.wall_product("uf", r, v, 1.0, a)
+    sym = _product(r, v, a, -1, "mixed", kind)
+    std = _product(r, v, a, 8, "mixed", kind)
+    ref = owall.wall_product(kind, r, v, 1.0, a)
     assert rel_err(sym, ref) <= 1e-6
     assert rel_err(sym, std) <= 1e-6
 
 
-def test_symmetric_shell_suspension_and_determinism(cuda_device):
+@pytest.mark.parametrize("kind", KINDS)
+def test_symmetric_shell_suspension_and_determinism(cuda_device, kind):
     s = S.shells_42_256(n_bodies=64)
     r = s.r_vectors()
     v = np.random.default_rng(1).standard_normal(3 * len(r))
     a = s.a
-    x1 = _product(r, v, a, -1)
-    x2 = _product(r, v, a, -1)
+    x1 = _product(r, v, a, -1, kind=kind)
+    x2 = _product(r, v, a, -1, kind=kind)
     assert np.array_equal(x1, x2)
     rows = np.arange(0, len(r), 7)
-    ref = owall.wall_product("uf", r, v, 1.0, a, rows=rows)
+    ref = owall.wall_product(kind, r, v, 1.0, a, rows=rows)
     got = x1.reshape(-1, 3)[rows].reshape(-1)
     assert rel_err(got, ref) <= 1e-12
 
@@ -78,9 +85,9 @@ def test_symmetric_choice_rules(cuda_device):
     with pytest.raises(RMWError):
         mob.autotune_set("uf", 100, "df64", -1)  # fewer than 256 blobs
     with pytest.raises(RMWError):
-        mob.autotune_set("ut", 1000, "df64", -1)  # only M_UF is symmetric block-wise
+        mob.autotune_set("wt", 255, "mixed", -1)
     with pytest.raises(RMWError):
-        mob.autotune_set("uf", 1000, "fp64", -1)
+        mob.autotune_set("uf", 1000, "fp64", -1)  # df64 and mixed only
     mob.autotune_set("uf", 1000, "df64", -1)
     assert mob.autotune_lookup("uf", 1000, "df64") == (-1, True)
     # periodic products fall back to the standard kernel and stay correct

@@ -701,20 +701,22 @@ def main():
             res["alg_frac_of_mode_peak"] = res["alg_tflops"] * 1e12 / peak
             products["%s_%s" % (kind, mode)] = {k: round(v, 6) for k, v in res.items()}
 
-    # fused force-and-torque product [U; W] = M [F; T] against its four single products
+    # the force-and-torque product [U; W] = M [F; T] (one fused pass in FP64 and
+    # mixed; in df64 the sum of the four symmetric single products) against the
+    # four single products called one by one
     if not args.no_extras:
         tt = torch.tensor(np.random.default_rng(7).standard_normal(3 * n), device=dev)
         for mode in ("fp64", "df64", "mixed"):
             reps = 3 if mode == "fp64" else 10
 
-            def fused():
+            def entry():
                 return mb.wall_force_torque(rt, ft, tt, eta, a, mode=mode)
 
             def four():
                 return [mb.wall_product(k, rt, v, eta, a, mode=mode) for k, v in (("uf", ft), ("ut", tt), ("wf", ft),
                                                                                  ("wt", tt))]
             res = {}
-            for name, fn in (("fused_ms", fused), ("four_products_ms", four)):
+            for name, fn in (("force_torque_ms", entry), ("four_products_ms", four)):
                 fn()
                 torch.cuda.synchronize()
                 e0 = torch.cuda.Event(enable_timing=True)
@@ -725,8 +727,10 @@ def main():
                 e1.record(stream)
                 torch.cuda.synchronize()
                 res[name] = e0.elapsed_time(e1) / reps
-            res["gpairs_fused"] = n * n / (res["fused_ms"] * 1e-3) / 1e9
-            products["force_torque_6n_%s" % mode] = {k: round(v, 6) for k, v in res.items()}
+            res["gpairs"] = n * n / (res["force_torque_ms"] * 1e-3) / 1e9
+            res["route"] = "four symmetric products" if mode == "df64" else "fused one-sided pass"
+            products["force_torque_6n_%s" % mode] = {k: (round(v, 6) if isinstance(v, float) else v)
+                                                      for k, v in res.items()}
 
     # source-target products with per-blob radii (the same blobs as sources and
     # targets, radii a (1 +- 20%)), and the single-radius free-surface product

@@ -30,7 +30,7 @@ int cuda_fail(cudaError_t e, const char *where);
 // device, stream and slot share it (they are ordered by the stream); a call that
 // needs more frees the old buffer (cudaFree synchronises the device, so no
 // kernel still reads it) and allocates anew.
-enum ScratchSlot { SCRATCH_PAIR = 0, SCRATCH_HOST_STAGING = 1, SCRATCH_SLOTS = 2 };
+enum ScratchSlot { SCRATCH_PAIR = 0, SCRATCH_HOST_STAGING = 1, SCRATCH_FT_TERM = 2, SCRATCH_SLOTS = 3 };
 int scratch(ScratchSlot slot, size_t bytes, void **ptr, cudaStream_t st);
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }

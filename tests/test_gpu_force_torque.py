@@ -39,6 +39,29 @@ def test_fused_matches_four_products(cuda_device, mode, damped, n):
     assert rel_err(Uonly, Ur) <= TOL[mode]
 
 
+@pytest.mark.parametrize("mode", ["df64", "mixed"])
+@pytest.mark.parametrize("damped", [False, True])
+def test_symmetric_route_matches_oracle(cuda_device, mode, damped):
+    """With the symmetric kernels chosen for all four blocks (the default from
+    4,096 blobs in df64 and 8,192 in mixed; pinned here at 700), the df64
+    [U; W] is the sum of the four symmetric single products (mixed keeps the
+    fused pass)."""
+    r, F, T = _case(700, 11, damped)
+    a = 0.3
+    mob.autotune_clear()
+    try:
+        for kind in ("uf", "ut", "wf", "wt"):
+            mob.autotune_set(kind, len(r), mode, -1)
+        U, W = mob.wall_force_torque(r, F, T, 1.0, a, mode=mode)
+        Uonly = mob.single_wall_mobility_trans_times_force_torque_pycuda(r, F, T, 1.0, a, mode=mode)
+    finally:
+        mob.autotune_clear()
+    Ur, Wr = owall.force_torque(r, F, T, 1.0, a)
+    assert rel_err(U, Ur) <= TOL[mode]
+    assert rel_err(W, Wr) <= TOL[mode]
+    assert rel_err(Uonly, Ur) <= TOL[mode]
+
+
 @pytest.mark.parametrize("mode", ["fp64", "df64", "mixed"])
 def test_fused_periodic(cuda_device, mode):
     r, F, T = _case(300, 7, True)

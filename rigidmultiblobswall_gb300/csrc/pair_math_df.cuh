@@ -197,11 +197,13 @@ __device__ __forceinline__ void pair_rpy_df(df dx, df dy, df dz, df vx, df vy, d
 //   (3/2) f5 = -2 [3 (h_j^2 + E) t + (2 - 15E) p]
 // and for r <= 2: (3/2) A = 2 (1 - 9r/32), (3/2) Bc = 3 / (16 r).
 // The accumulators stay unnormalised (acc_dot2 / acc_dot4, as acc_add).
-__device__ __forceinline__ void pair_uf_sym_df(df dx, df dy, df dz, df Rz, df hi, df hj, df vx, df vy, df vz,
-                                               df qx, df qy, df qz, df &ux, df &uy, df &uz, df &wx, df &wy,
-                                               df &wz)
+struct UFCoeffsDF {
+    df Af, Af5, Bc, c2, c3, c4, hj2;  // times 3/2; hj2 = Rz - dz = 2 h_j
+};
+
+__device__ __forceinline__ UFCoeffsDF uf_coeffs_df(df dx, df dy, df dz, df Rz, df hi, df hj)
 {
-    // mul_u / sqr_u: products that feed a sum directly (see dfloat.cuh)
+    // mul_u / sqr_u / mad_u / add_u / sub_u: values that feed a sum directly (see dfloat.cuh)
     const df rho2 = mad_u(dx, dx, sqr_u(dy));
     const df r2 = mad(dz, dz, rho2);
     const df invr = rsqrt_df(r2);
@@ -231,31 +233,38 @@ __device__ __forceinline__ void pair_uf_sym_df(df dx, df dy, df dz, df Rz, df hi
     const df f5 = scale2(mad_u((sqr_u(hj) + E) * 3.0f, t, mul_u(2.0f - mul_u(E, 15.0f), p)), -2.0f);
     const df Ru = Rz * u;
     const df hjt3 = mul_u(hj * t, 3.0f);
-    const df c4 = hjt3 - mul_u(Ru * p, 10.0f);
-    const df c3 = sub_u(hjt3, mul_u(hh * (Rz * t), 18.0f)) +
-                  mul_u(Ru, mul_u((2.0f - E7) * p, 10.0f) - mul_u(q5, 6.0f));
-    const df Af = A + f1;
-    const df Af5 = Af + f5;  // the zz diagonal
-    const df c2 = f2 * u;
-    const df hj2 = scale2(hj, 2.0f);  // Rz - dz
-    {  // M_ij v_j
-        const df dv = dot3(dx, vx, dy, vy, dz, vz);
-        const df W = mad(hj2, vz, dv);  // e.v
-        const df Gw = mad2(c2, W, c3, vz);
-        const df G = mad(Bc, dv, Gw);
-        acc_dot2(ux, Af, vx, G, dx);
-        acc_dot2(uy, Af, vy, G, dy);
-        acc_dot4(uz, Af5, vz, G, dz, Gw, hj2, c4, W);
-    }
-    {  // M_ij^T v_i
-        const df dv = dot3(dx, qx, dy, qy, dz, qz);
-        const df W = mad(hj2, qz, dv);
-        const df Gw = mad2(c2, W, c4, qz);
-        const df G = mad(Bc, dv, Gw);
-        acc_dot2(wx, Af, qx, G, dx);
-        acc_dot2(wy, Af, qy, G, dy);
-        acc_dot4(wz, Af5, qz, G, dz, Gw, hj2, c3, W);
-    }
+    UFCoeffsDF C;
+    C.c4 = hjt3 - mul_u(Ru * p, 10.0f);
+    C.c3 = sub_u(hjt3, mul_u(hh * (Rz * t), 18.0f)) + mul_u(Ru, mul_u((2.0f - E7) * p, 10.0f) - mul_u(q5, 6.0f));
+    C.Af = A + f1;
+    C.Af5 = C.Af + f5;  // the zz diagonal
+    C.Bc = Bc;
+    C.c2 = f2 * u;
+    C.hj2 = scale2(hj, 2.0f);
+    return C;
+}
+
+// (ux, uy, uz) += (3/2) M v with the coefficients of uf_coeffs_df; (c3, c4)
+// exchanged gives the transposed block
+__device__ __forceinline__ void uf_apply_df(const UFCoeffsDF &C, df c3, df c4, df dx, df dy, df dz, df vx, df vy,
+                                            df vz, df &ux, df &uy, df &uz)
+{
+    const df dv = dot3(dx, vx, dy, vy, dz, vz);
+    const df W = mad(C.hj2, vz, dv);  // e.v
+    const df Gw = mad2(C.c2, W, c3, vz);
+    const df G = mad(C.Bc, dv, Gw);
+    acc_dot2(ux, C.Af, vx, G, dx);
+    acc_dot2(uy, C.Af, vy, G, dy);
+    acc_dot4(uz, C.Af5, vz, G, dz, Gw, C.hj2, c4, W);
+}
+
+__device__ __forceinline__ void pair_uf_sym_df(df dx, df dy, df dz, df Rz, df hi, df hj, df vx, df vy, df vz,
+                                               df qx, df qy, df qz, df &ux, df &uy, df &uz, df &wx, df &wy,
+                                               df &wz)
+{
+    const UFCoeffsDF C = uf_coeffs_df(dx, dy, dz, Rz, hi, hj);
+    uf_apply_df(C, C.c3, C.c4, dx, dy, dz, vx, vy, vz, ux, uy, uz);  // M_ij v_j
+    uf_apply_df(C, C.c4, C.c3, dx, dy, dz, qx, qy, qz, wx, wy, wz);  // M_ij^T v_i
 }
 
 // ---------------------------------------------------------------------------
@@ -375,6 +384,56 @@ __device__ __forceinline__ void pair_rot_sym_df(df dx, df dy, df dz, df Rz, df h
             wf_apply_df(c, Hj, s3, dx, dy, dz, vx, vy, vz, ux, uy, uz);
             wf_apply_df(c, Hi, s3, -dx, -dy, -dz, qx, qy, qz, wx, wy, wz);
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// One-sided accumulating forms for the standard (all ordered pairs) kernels:
+// (ux, uy, uz) += M_ij v_j, for UF times 3/2 (the finalize applies 2/3) with
+// the coefficients and applies of the symmetric forms.
+template <int KIND>
+__device__ __forceinline__ void pair_acc_df(df dx, df dy, df dz, df Rz, df hi, df hj, df vx, df vy, df vz, df &ux,
+                                            df &uy, df &uz)
+{
+    if (KIND == RMW_UF) {
+        const UFCoeffsDF C = uf_coeffs_df(dx, dy, dz, Rz, hi, hj);
+        uf_apply_df(C, C.c3, C.c4, dx, dy, dz, vx, vy, vz, ux, uy, uz);
+        return;
+    }
+    const df rho2 = mad_u(dx, dx, sqr_u(dy));
+    const df r2 = mad(dz, dz, rho2);
+    const df invr = rsqrt_df(r2);
+    const df Rz2 = sqr(Rz);
+    const df s = rsqrt_df(rho2 + Rz2);
+    const df s2 = sqr(s);
+    const df s3 = s2 * s;
+    const df E = Rz2 * s2;
+    const bool near = !(r2 >= 4.0f);  // r < 2
+    if (KIND == RMW_WT) {
+        const df invr2 = sqr(invr);
+        const df invr3 = invr2 * invr;
+        df A = invr3 * -0.5f;
+        df Bc = (invr2 * invr3) * 1.5f;
+        if (__any_sync(__activemask(), near)) {
+            if (near) {
+                const df r = r2 * invr;
+                A = (1.0f - r * 0.84375f) + (r * r2) * 0.078125f;
+                Bc = invr * 0.28125f - r * 0.046875f;
+            }
+        }
+        const df Af = A + scale2((1.0f - E * 6.0f) * s3, 0.5f);
+        wt_apply_df(Af, Bc, s3 * s2, dx, dy, dz, Rz, vx, vy, vz, ux, uy, uz);
+    } else {
+        df c = sqr(invr) * invr;
+        if (__any_sync(__activemask(), near)) {
+            if (near) c = scale2(1.0f - (r2 * invr) * 0.375f, 0.5f);
+        }
+        const df s4 = sqr(s2);
+        const df ez = Rz * s;
+        const df ezs4 = ez * s4;
+        const df K = mul_u(1.0f - mul_u(E, 10.0f), s4);
+        if (KIND == RMW_UT) ut_apply_df(c, rot_h_df(hi, s, s2, s3, ez, ezs4, K), s3, dx, dy, dz, vx, vy, vz, ux, uy, uz);
+        else wf_apply_df(c, rot_h_df(hj, s, s2, s3, ez, ezs4, K), s3, dx, dy, dz, vx, vy, vz, ux, uy, uz);
     }
 }
 

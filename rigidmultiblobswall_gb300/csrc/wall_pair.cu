@@ -169,11 +169,7 @@ __global__ void __launch_bounds__(kThreads) wall_pair_df_kernel(const SrcDF *__r
                     const float4 sh = tile[k].hi, sl = tile[k].lo, svh = tile[k].vhi, svl = tile[k].vlo;
                     const df xj = {sh.x, sl.x}, yj = {sh.y, sl.y}, zj = {sh.z, sl.z};
                     const df vx = {svh.x, svl.x}, vy = {svh.y, svl.y}, vz = {svh.z, svl.z};
-                    df cx, cy, cz;
-                    pair_contrib_df<KIND>(xi - xj, yi - yj, zi - zj, zi + zj, zi, zj, vx, vy, vz, cx, cy, cz);
-                    acc_add(ux, cx);
-                    acc_add(uy, cy);
-                    acc_add(uz, cz);
+                    pair_acc_df<KIND>(xi - xj, yi - yj, zi - zj, add_u(zi, zj), zi, zj, vx, vy, vz, ux, uy, uz);
                 }
                 ax += to_double(ux);
                 ay += to_double(uy);
@@ -188,12 +184,14 @@ __global__ void __launch_bounds__(kThreads) wall_pair_df_kernel(const SrcDF *__r
                 const df dz = zi - zj;
                 const df Rz = zi + zj;
                 if (!PER) {
-                    df cx = df_from(0.f), cy = df_from(0.f), cz = df_from(0.f);
-                    pair_contrib_df<KIND>(xi - xj, yi - yj, dz, Rz, zi, zj, vx, vy, vz, cx, cy, cz);
-                    if (j != i) {
-                        acc_add(ux, cx);
-                        acc_add(uy, cy);
-                        acc_add(uz, cz);
+                    // the self pair is evaluated (NaN for coincident points) and the sums
+                    // restored, so the warp stays convergent
+                    const df kx = ux, ky = uy, kz = uz;
+                    pair_acc_df<KIND>(xi - xj, yi - yj, dz, Rz, zi, zj, vx, vy, vz, ux, uy, uz);
+                    if (j == i) {
+                        ux = kx;
+                        uy = ky;
+                        uz = kz;
                     }
                 } else {
                     // minimum image in FP64 (rare path), then back to double-float
@@ -205,15 +203,14 @@ __global__ void __launch_bounds__(kThreads) wall_pair_df_kernel(const SrcDF *__r
                     for (int bx = -px; bx <= px; ++bx)
                         for (int by = -py; by <= py; ++by)
                             for (int bz = -pz; bz <= pz; ++bz) {
-                                df cx = df_from(0.f), cy = df_from(0.f), cz = df_from(0.f);
-                                pair_contrib_df<KIND>(df_of_double(rx + bx * P.Lx), df_of_double(ry + by * P.Ly),
-                                                      df_of_double(rz + bz * P.Lz), Rz, zi, zj, vx, vy, vz, cx,
-                                                      cy, cz);
                                 const bool self = (j == i) && bx == 0 && by == 0 && bz == 0;
-                                if (!self) {
-                                    acc_add(ux, cx);
-                                    acc_add(uy, cy);
-                                    acc_add(uz, cz);
+                                const df kx = ux, ky = uy, kz = uz;
+                                pair_acc_df<KIND>(df_of_double(rx + bx * P.Lx), df_of_double(ry + by * P.Ly),
+                                                  df_of_double(rz + bz * P.Lz), Rz, zi, zj, vx, vy, vz, ux, uy, uz);
+                                if (self) {
+                                    ux = kx;
+                                    uy = ky;
+                                    uz = kz;
                                 }
                             }
                 }
@@ -987,8 +984,11 @@ static int launch_kind(const double *r, const double *v, double *out, int n, dou
         else wall_pair_mixed_kernel<KIND, false, false><<<grid, kThreads, 0, st>>>(src, n, chunk, Ps, partial, jobs);
     }
     if (int rc = trace_end(tok, st)) return rc;
+    // the df64 UF pair kernel sums (3/2) M v
+    const double scale = (KIND == RMW_UF && mode == RMW_MODE_DF64) ? kUFCoeffScale : 1.0;
     wall_finalize_kernel<KIND><<<finalize_blocks(n, pb), pb, 0, st>>>(r, v, partial, nchunks, out, n, a, nf,
-                                                                       B ? B->blob_nch : nullptr);
+                                                                       B ? B->blob_nch : nullptr, nullptr, nullptr,
+                                                                       scale);
     RMW_CHECK_LAUNCH("wall product kernels");
     return RMW_OK;
 }

@@ -83,10 +83,10 @@ int wall_chunks(int kind, int mode, int n)
             return std::max(1, std::min(it->second, max_chunks(n)));
         }
     }
-    // untuned: the symmetric kernel from 4,096 blobs in df64 and from 8,192 in
-    // mixed precision (measured faster at every size from there; the caller
-    // falls back where it does not apply)
-    if ((mode == RMW_MODE_DF64 && n >= 4096) || (mode == RMW_MODE_MIXED && n >= 8192)) return kSymChunks;
+    // untuned: the symmetric kernel from 4,096 blobs in FP64 and df64 and from
+    // 8,192 in mixed precision (measured faster at every size from there; the
+    // caller falls back where it does not apply)
+    if ((mode != RMW_MODE_MIXED && n >= 4096) || (mode == RMW_MODE_MIXED && n >= 8192)) return kSymChunks;
     return wall_default_chunks(n);
 }
 
@@ -193,7 +193,7 @@ int rmw_wall_autotune_set(int kind, int mode, int64_t n, int nchunks)
     if (n < 1) return rmw::fail(RMW_ERR_ARG, "number of blobs must be positive");
     if (nchunks == rmw::kSymChunks) {
         if (!rmw::wall_sym_applicable(kind, mode, (int)n, nullptr))
-            return rmw::fail(RMW_ERR_ARG, "the symmetric kernel covers the df64 and mixed products of 256 or "
+            return rmw::fail(RMW_ERR_ARG, "the symmetric kernel covers the non-periodic products of 256 or "
                                           "more blobs within its partial-sum budget");
     } else if (nchunks < 1 || nchunks > 64) {
         return rmw::fail(RMW_ERR_ARG, "source split must be in [1, 64] or -1");

@@ -252,107 +252,115 @@ __device__ __forceinline__ void uf_apply<float>(const UFCoeffs<float> &c, float 
 }
 
 // ---------------------------------------------------------------------------
-// Symmetric forms of the rotation blocks in FP32 (the double-float forms are
-// pair_rot_sym_df): M_ji is the M_ij formula with d -> -d and h_i <-> h_j, so
-// one pair evaluation serves both targets.  WT has no height dependence; UT
-// and WF form the height-dependent coefficients for both heights.
-struct RotHF {
-    float f3s2, p, gs;  // f3 s^2, p = s^2 ez + f4, g s with g = s^2 + f2 + f3 ez
+// Symmetric forms of the rotation blocks in FP32 and FP64 (the double-float
+// forms are pair_rot_sym_df): M_ji is the M_ij formula with d -> -d and
+// h_i <-> h_j, so one pair evaluation serves both targets.  WT has no height
+// dependence; UT and WF form the height-dependent coefficients for both
+// heights.
+template <typename T> __device__ __forceinline__ T fm(T a, T b, T c);
+template <> __device__ __forceinline__ float fm<float>(float a, float b, float c) { return fmaf(a, b, c); }
+template <> __device__ __forceinline__ double fm<double>(double a, double b, double c) { return fma(a, b, c); }
+
+template <typename T> struct RotH {
+    T f3s2, p, gs;  // f3 s^2, p = s^2 ez + f4, g s with g = s^2 + f2 + f3 ez
 };
-__device__ __forceinline__ RotHF rot_h_f(float h, float s, float s2, float s3, float ez, float ezs4, float K)
+template <typename T>
+__device__ __forceinline__ RotH<T> rot_h(T h, T s, T s2, T s3, T ez, T ezs4, T K)
 {
-    const float hs3 = h * s3;
-    const float f2 = 2.0f * fmaf(6.0f * hs3, ez, K);
-    const float f3 = -2.0f * fmaf(3.0f, hs3, -5.0f * ezs4);
-    const float f4 = -2.0f * (hs3 - ezs4);
-    const float p = fmaf(s2, ez, f4);
-    const float g = fmaf(f3, ez, s2 + f2);
+    const T hs3 = h * s3;
+    const T f2 = T(2) * fm<T>(T(6) * hs3, ez, K);
+    const T f3 = T(-2) * fm<T>(T(3), hs3, T(-5) * ezs4);
+    const T f4 = T(-2) * (hs3 - ezs4);
+    const T p = fm<T>(s2, ez, f4);
+    const T g = fm<T>(f3, ez, s2 + f2);
     return {f3 * s2, p, g * s};
 }
 
-__device__ __forceinline__ void ut_apply_f(float c, const RotHF &H, float s3, float dx, float dy, float dz, float vx,
-                                           float vy, float vz, float &ux, float &uy, float &uz)
+template <typename T>
+__device__ __forceinline__ void ut_apply(T c, const RotH<T> &H, T s3, T dx, T dy, T dz, T vx, T vy, T vz, T &ux,
+                                         T &uy, T &uz)
 {
-    const float Q = fmaf(dy, vx, -dx * vy);  // (v x d)_z
-    const float X = fmaf(vy, dz, -vz * dy), Y = fmaf(vz, dx, -vx * dz);
-    const float F3 = H.f3s2 * Q, F1 = s3 * vz;
-    ux = fmaf(c, X, fmaf(F3, dx, fmaf(F1, dy, fmaf(H.p, vy, ux))));
-    uy = fmaf(c, Y, fmaf(F3, dy, fmaf(-F1, dx, fmaf(-H.p, vx, uy))));
-    uz = fmaf(c - H.gs, Q, uz);
+    const T Q = fm<T>(dy, vx, -dx * vy);  // (v x d)_z
+    const T X = fm<T>(vy, dz, -vz * dy), Y = fm<T>(vz, dx, -vx * dz);
+    const T F3 = H.f3s2 * Q, F1 = s3 * vz;
+    ux = fm<T>(c, X, fm<T>(F3, dx, fm<T>(F1, dy, fm<T>(H.p, vy, ux))));
+    uy = fm<T>(c, Y, fm<T>(F3, dy, fm<T>(-F1, dx, fm<T>(-H.p, vx, uy))));
+    uz = fm<T>(c - H.gs, Q, uz);
 }
 
-__device__ __forceinline__ void wf_apply_f(float c, const RotHF &H, float s3, float dx, float dy, float dz, float vx,
-                                           float vy, float vz, float &ux, float &uy, float &uz)
+template <typename T>
+__device__ __forceinline__ void wf_apply(T c, const RotH<T> &H, T s3, T dx, T dy, T dz, T vx, T vy, T vz, T &ux,
+                                         T &uy, T &uz)
 {
-    const float Pxy = fmaf(dy, vy, dx * vx);
-    const float Q = fmaf(dy, vx, -dx * vy);
-    const float X = fmaf(vy, dz, -vz * dy), Y = fmaf(vz, dx, -vx * dz);
-    const float Hh = fmaf(H.f3s2, Pxy, H.gs * vz);
-    ux = fmaf(c, X, fmaf(Hh, dy, fmaf(-H.p, vy, ux)));
-    uy = fmaf(c, Y, fmaf(H.p, vx, fmaf(-Hh, dx, uy)));
-    uz = fmaf(c - s3, Q, uz);
+    const T Pxy = fm<T>(dy, vy, dx * vx);
+    const T Q = fm<T>(dy, vx, -dx * vy);
+    const T X = fm<T>(vy, dz, -vz * dy), Y = fm<T>(vz, dx, -vx * dz);
+    const T Hh = fm<T>(H.f3s2, Pxy, H.gs * vz);
+    ux = fm<T>(c, X, fm<T>(Hh, dy, fm<T>(-H.p, vy, ux)));
+    uy = fm<T>(c, Y, fm<T>(H.p, vx, fm<T>(-Hh, dx, uy)));
+    uz = fm<T>(c - s3, Q, uz);
 }
 
-__device__ __forceinline__ void wt_apply_f(float Af, float Bc, float s5, float dx, float dy, float dz, float Rz,
-                                           float vx, float vy, float vz, float &ux, float &uy, float &uz)
+template <typename T>
+__device__ __forceinline__ void wt_apply(T Af, T Bc, T s5, T dx, T dy, T dz, T Rz, T vx, T vy, T vz, T &ux, T &uy,
+                                         T &uz)
 {
-    const float Pxy = fmaf(dy, vy, dx * vx);
-    const float dv = fmaf(dz, vz, Pxy);
-    const float W = fmaf(Rz, vz, Pxy);
-    const float Q = fmaf(dy, vx, -dx * vy);
-    const float Gw = -1.5f * s5 * W;
-    const float Tq = 3.0f * s5 * Q;
-    const float Gr = Bc * dv;
-    const float G = Gr + Gw;
-    ux = fmaf(Af, vx, fmaf(G, dx, fmaf(Tq, dy, ux)));
-    uy = fmaf(Af, vy, fmaf(G, dy, fmaf(-Tq, dx, uy)));
-    uz = fmaf(Af, vz, fmaf(Gr, dz, fmaf(-Gw, Rz, uz)));
+    const T Pxy = fm<T>(dy, vy, dx * vx);
+    const T dv = fm<T>(dz, vz, Pxy);
+    const T W = fm<T>(Rz, vz, Pxy);
+    const T Q = fm<T>(dy, vx, -dx * vy);
+    const T Gw = T(-1.5) * s5 * W;
+    const T Tq = T(3) * s5 * Q;
+    const T Gr = Bc * dv;
+    const T G = Gr + Gw;
+    ux = fm<T>(Af, vx, fm<T>(G, dx, fm<T>(Tq, dy, ux)));
+    uy = fm<T>(Af, vy, fm<T>(G, dy, fm<T>(-Tq, dx, uy)));
+    uz = fm<T>(Af, vz, fm<T>(Gr, dz, fm<T>(-Gw, Rz, uz)));
 }
 
 // UT, WF or WT for both orders of one pair: (ux, uy, uz) += M_ij v_j,
 // (wx, wy, wz) += M_ji v_i.
-template <int KIND>
-__device__ __forceinline__ void pair_rot_sym_f(float dx, float dy, float dz, float Rz, float hi, float hj, float vx,
-                                               float vy, float vz, float qx, float qy, float qz, float &ux,
-                                               float &uy, float &uz, float &wx, float &wy, float &wz)
+template <typename T, int KIND>
+__device__ __forceinline__ void pair_rot_sym(T dx, T dy, T dz, T Rz, T hi, T hj, T vx, T vy, T vz, T qx, T qy, T qz,
+                                             T &ux, T &uy, T &uz, T &wx, T &wy, T &wz)
 {
-    const float rho2 = fmaf(dx, dx, dy * dy);
-    const float r2 = fmaf(dz, dz, rho2);
-    const float invr = rsq<float>(r2);
-    const float Rz2 = Rz * Rz;
-    const float s = rsq<float>(rho2 + Rz2);
-    const float s2 = s * s, s3 = s2 * s, E = Rz2 * s2;
-    const bool near = !(r2 >= 4.0f);  // r < 2
+    const T rho2 = fm<T>(dx, dx, dy * dy);
+    const T r2 = fm<T>(dz, dz, rho2);
+    const T invr = rsq<T>(r2);
+    const T Rz2 = Rz * Rz;
+    const T s = rsq<T>(rho2 + Rz2);
+    const T s2 = s * s, s3 = s2 * s, E = Rz2 * s2;
+    const bool near = !(r2 >= T(4));  // r < 2
     if (KIND == RMW_WT) {
-        const float invr2 = invr * invr, invr3 = invr2 * invr;
-        float A = -0.5f * invr3;
-        float Bc = 1.5f * invr2 * invr3;
+        const T invr2 = invr * invr, invr3 = invr2 * invr;
+        T A = T(-0.5) * invr3;
+        T Bc = T(1.5) * invr2 * invr3;
         if (__any_sync(__activemask(), near)) {
             if (near) {
-                const float r = r2 * invr;
-                A = 1.0f - 0.84375f * r + 0.078125f * r * r2;
-                Bc = 0.28125f * invr - 0.046875f * r;
+                const T r = r2 * invr;
+                A = T(1) - T(0.84375) * r + T(0.078125) * r * r2;
+                Bc = T(0.28125) * invr - T(0.046875) * r;
             }
         }
-        const float s5 = s3 * s2;
-        const float Af = fmaf(0.5f * s3, fmaf(-6.0f, E, 1.0f), A);
-        wt_apply_f(Af, Bc, s5, dx, dy, dz, Rz, vx, vy, vz, ux, uy, uz);
-        wt_apply_f(Af, Bc, s5, -dx, -dy, -dz, Rz, qx, qy, qz, wx, wy, wz);
+        const T s5 = s3 * s2;
+        const T Af = fm<T>(T(0.5) * s3, fm<T>(T(-6), E, T(1)), A);
+        wt_apply<T>(Af, Bc, s5, dx, dy, dz, Rz, vx, vy, vz, ux, uy, uz);
+        wt_apply<T>(Af, Bc, s5, -dx, -dy, -dz, Rz, qx, qy, qz, wx, wy, wz);
     } else {
-        float c = invr * invr * invr;
+        T c = invr * invr * invr;
         if (__any_sync(__activemask(), near)) {
-            if (near) c = 0.5f * (1.0f - 0.375f * (r2 * invr));
+            if (near) c = T(0.5) * (T(1) - T(0.375) * (r2 * invr));
         }
-        const float s4 = s2 * s2, ez = Rz * s, ezs4 = ez * s4;
-        const float K = fmaf(-10.0f, E, 1.0f) * s4;
-        const RotHF Hi = rot_h_f(hi, s, s2, s3, ez, ezs4, K);
-        const RotHF Hj = rot_h_f(hj, s, s2, s3, ez, ezs4, K);
+        const T s4 = s2 * s2, ez = Rz * s, ezs4 = ez * s4;
+        const T K = fm<T>(T(-10), E, T(1)) * s4;
+        const RotH<T> Hi = rot_h<T>(hi, s, s2, s3, ez, ezs4, K);
+        const RotH<T> Hj = rot_h<T>(hj, s, s2, s3, ez, ezs4, K);
         if (KIND == RMW_UT) {
-            ut_apply_f(c, Hi, s3, dx, dy, dz, vx, vy, vz, ux, uy, uz);
-            ut_apply_f(c, Hj, s3, -dx, -dy, -dz, qx, qy, qz, wx, wy, wz);
+            ut_apply<T>(c, Hi, s3, dx, dy, dz, vx, vy, vz, ux, uy, uz);
+            ut_apply<T>(c, Hj, s3, -dx, -dy, -dz, qx, qy, qz, wx, wy, wz);
         } else {
-            wf_apply_f(c, Hj, s3, dx, dy, dz, vx, vy, vz, ux, uy, uz);
-            wf_apply_f(c, Hi, s3, -dx, -dy, -dz, qx, qy, qz, wx, wy, wz);
+            wf_apply<T>(c, Hj, s3, dx, dy, dz, vx, vy, vz, ux, uy, uz);
+            wf_apply<T>(c, Hi, s3, -dx, -dy, -dz, qx, qy, qz, wx, wy, wz);
         }
     }
 }

@@ -450,8 +450,8 @@ __device__ __forceinline__ void mixed_sym_body(const SrcF *__restrict__ src, int
             const UFCoeffs<float> ct = {c.Af, c.Bc, c.c2, c.c4, c.c3, c.Af5};  // M^T: f3 and f4 trade places
             uf_apply<float>(ct, dx, dy, dz, Rz, me.v.x, me.v.y, me.v.z, wx, wy, wz);
         } else {
-            pair_rot_sym_f<KIND>(dx, dy, dz, Rz, hi, hj, sv.x, sv.y, sv.z, me.v.x, me.v.y, me.v.z, ux, uy, uz, wx, wy,
-                                 wz);
+            pair_rot_sym<float, KIND>(dx, dy, dz, Rz, hi, hj, sv.x, sv.y, sv.z, me.v.x, me.v.y, me.v.z, ux, uy, uz, wx,
+                                      wy, wz);
         }
         sacc[warp][0][jl] = wx;
         sacc[warp][1][jl] = wy;
@@ -517,6 +517,106 @@ __global__ void __launch_bounds__(kThreads) wall_rot_mixed_sym_kernel(const SrcF
                                                                        const SymJob *__restrict__ jobs)
 {
     mixed_sym_body<SEG, KIND>(src, n, nt, partial, jobs);
+}
+
+// Symmetric FP64 kernel of any kind: the same grid, pairing and partial-sum
+// slots, FP64 pair arithmetic (the FP64 pipe bounds it, so halving the
+// coefficient work per ordered pair is the gain); source-side sums per warp
+// in FP64 shared memory.
+template <bool SEG, int KIND>
+__device__ __forceinline__ void fp64_sym_body(const SrcD *__restrict__ src, int n, int nt, double inva,
+                                              double *__restrict__ partial, const SymJob *__restrict__ jobs)
+{
+    __shared__ double tx[kTile], ty[kTile], tz[kTile], tvx[kTile], tvy[kTile], tvz[kTile];
+    __shared__ double sacc[kSymWarps][3][kTile];
+    int T, S;
+    sym_cta<SEG>(jobs, n, nt, T, S, src, partial);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool diag = (T == S);
+    const int i = T * kTile + tid;
+    const bool valid_i = i < n;
+    // a target or source past the end is a dummy far above the wall with a zero vector
+    const SrcD dummy = {1.0e6, 1.0e6, 1.0e6, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const SrcD me = valid_i ? src[i] : dummy;
+    const double xi = me.x * inva, yi = me.y * inva, zi = me.z * inva;
+    {
+        const int j = S * kTile + tid;
+        const SrcD sj = (j < n) ? src[j] : dummy;
+        tx[tid] = sj.x * inva;
+        ty[tid] = sj.y * inva;
+        tz[tid] = sj.z * inva;
+        tvx[tid] = sj.vx;
+        tvy[tid] = sj.vy;
+        tvz[tid] = sj.vz;
+    }
+    for (int c = 0; c < 3; ++c)
+        for (int k = lane; k < kTile; k += 32) sacc[warp][c][k] = 0.0;
+    __syncthreads();
+    double ux = 0.0, uy = 0.0, uz = 0.0;
+    auto step = [&](int k) {
+        const int jl = (lane + k) & (kTile - 1);
+        const double zj = tz[jl];
+        const double dx = xi - tx[jl], dy = yi - ty[jl], dz = zi - zj, Rz = zi + zj;
+        const double vx = tvx[jl], vy = tvy[jl], vz = tvz[jl];
+        double wx = sacc[warp][0][jl], wy = sacc[warp][1][jl], wz = sacc[warp][2][jl];
+        if constexpr (KIND == RMW_UF) {
+            const UFCoeffs<double> c = uf_coeffs<double>(dx, dy, dz, Rz, zi, zj);
+            uf_apply<double>(c, dx, dy, dz, Rz, vx, vy, vz, ux, uy, uz);
+            const UFCoeffs<double> ct = {c.Af, c.Bc, c.c2, c.c4, c.c3, c.Af5};  // M^T: f3 and f4 trade places
+            uf_apply<double>(ct, dx, dy, dz, Rz, me.vx, me.vy, me.vz, wx, wy, wz);
+        } else {
+            pair_rot_sym<double, KIND>(dx, dy, dz, Rz, zi, zj, vx, vy, vz, me.vx, me.vy, me.vz, ux, uy, uz, wx, wy,
+                                       wz);
+        }
+        sacc[warp][0][jl] = wx;
+        sacc[warp][1][jl] = wy;
+        sacc[warp][2][jl] = wz;
+    };
+    if (diag) {
+        for (int k = 0; k < kTile; ++k) {
+            __syncwarp();
+            const int off = (k - 32 * warp) & (kTile - 1);
+            if (off == 0 || off > kTile / 2 || (off == kTile / 2 && warp >= kSymWarps / 2)) continue;
+            step(k);
+        }
+    } else {
+        for (int k = 0; k < kTile; ++k) {
+            __syncwarp();
+            step(k);
+        }
+    }
+    __syncthreads();
+    double qx = 0.0, qy = 0.0, qz = 0.0;
+    for (int w = 0; w < kSymWarps; ++w) {
+        qx += sacc[w][0][tid];
+        qy += sacc[w][1][tid];
+        qz += sacc[w][2][tid];
+    }
+    const size_t stride = 3 * (size_t)n;
+    if (diag) {
+        if (valid_i) {
+            double *o = partial + (size_t)T * stride + 3 * (size_t)i;
+            o[0] = ux + qx; o[1] = uy + qy; o[2] = uz + qz;
+        }
+    } else {
+        if (valid_i) {
+            double *o = partial + (size_t)S * stride + 3 * (size_t)i;
+            o[0] = ux; o[1] = uy; o[2] = uz;
+        }
+        const int j = S * kTile + tid;
+        if (j < n) {
+            double *o = partial + (size_t)T * stride + 3 * (size_t)j;
+            o[0] = qx; o[1] = qy; o[2] = qz;
+        }
+    }
+}
+
+template <bool SEG, int KIND>
+__global__ void __launch_bounds__(kThreads) wall_fp64_sym_kernel(const SrcD *__restrict__ src, int n, int nt,
+                                                                  double inva, double *__restrict__ partial,
+                                                                  const SymJob *__restrict__ jobs)
+{
+    fp64_sym_body<SEG, KIND>(src, n, nt, inva, partial, jobs);
 }
 
 // ---------------------------------------------------------------------------
@@ -1025,7 +1125,9 @@ int wall_product_with_scratch(int kind, const double *r, const double *v, double
 
 bool wall_sym_applicable(int kind, int mode, int n, const double *L)
 {
-    if (kind < RMW_UF || kind > RMW_WT || (mode != RMW_MODE_DF64 && mode != RMW_MODE_MIXED)) return false;
+    if (kind < RMW_UF || kind > RMW_WT ||
+        (mode != RMW_MODE_FP64 && mode != RMW_MODE_DF64 && mode != RMW_MODE_MIXED))
+        return false;
     if (L && (L[0] > 0 || L[1] > 0 || L[2] > 0)) return false;
     if (n < 2 * kTile) return false;
     const double nt = (double)((n + kTile - 1) / kTile);
@@ -1037,9 +1139,13 @@ int wall_sym_slots(int n) { return (n + kTile - 1) / kTile; }
 // the symmetric kernel and finalize of one kind: the UF kernels sum (3/2) M v
 template <int KIND>
 static void launch_sym(bool seg, int mode, const void *src, int n, int nt, unsigned ncta, double *partial,
-                       const SymJob *jobs, cudaStream_t st)
+                       const SymJob *jobs, cudaStream_t st, double inva)
 {
-    if (mode == RMW_MODE_DF64) {
+    if (mode == RMW_MODE_FP64) {
+        const SrcD *s = (const SrcD *)src;
+        if (seg) wall_fp64_sym_kernel<true, KIND><<<ncta, kThreads, 0, st>>>(s, n, nt, inva, partial, jobs);
+        else wall_fp64_sym_kernel<false, KIND><<<ncta, kThreads, 0, st>>>(s, n, nt, inva, partial, jobs);
+    } else if (mode == RMW_MODE_DF64) {
         const SrcDF *s = (const SrcDF *)src;
         if (KIND == RMW_UF) {
             if (seg) wall_uf_df_sym_kernel<true><<<ncta, kThreads, 0, st>>>(s, n, nt, partial, jobs);
@@ -1087,22 +1193,24 @@ static int sym_product(int kind, const double *r, const double *v, double *out, 
                        int mode, cudaStream_t st, void *scratch_ptr, const WallBatch *B)
 {
     const int nt = B ? 0 : wall_sym_slots(n);
-    const size_t rec = (mode == RMW_MODE_DF64) ? sizeof(SrcDF) : sizeof(SrcF);
+    const size_t rec = (mode == RMW_MODE_FP64) ? sizeof(SrcD) : (mode == RMW_MODE_DF64 ? sizeof(SrcDF) : sizeof(SrcF));
     const size_t packed = ((rec * (size_t)n + 255) / 256) * 256;
     char *base = (char *)scratch_ptr;
     double *partial = (double *)(base + packed);
     const int pb = 256, pg = (n + pb - 1) / pb;
     const unsigned ncta = B ? (unsigned)B->nsym : (unsigned)((long long)nt * (nt + 1) / 2);
     const SymJob *jobs = B ? B->sym_jobs : nullptr;
-    if (mode == RMW_MODE_DF64) pack_df_kernel<<<pg, pb, 0, st>>>(r, v, (SrcDF *)base, n, a);
+    if (mode == RMW_MODE_FP64) pack_fp64_kernel<<<pg, pb, 0, st>>>(r, v, (SrcD *)base, n, a);
+    else if (mode == RMW_MODE_DF64) pack_df_kernel<<<pg, pb, 0, st>>>(r, v, (SrcDF *)base, n, a);
     else pack_mixed_kernel<<<pg, pb, 0, st>>>(r, v, (SrcF *)base, n, a);
+    const double inva = 1.0 / a;
     void *tok = nullptr;
     if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
     switch (kind) {
-    case RMW_UF: launch_sym<RMW_UF>(B != nullptr, mode, base, n, nt, ncta, partial, jobs, st); break;
-    case RMW_UT: launch_sym<RMW_UT>(B != nullptr, mode, base, n, nt, ncta, partial, jobs, st); break;
-    case RMW_WF: launch_sym<RMW_WF>(B != nullptr, mode, base, n, nt, ncta, partial, jobs, st); break;
-    default: launch_sym<RMW_WT>(B != nullptr, mode, base, n, nt, ncta, partial, jobs, st); break;
+    case RMW_UF: launch_sym<RMW_UF>(B != nullptr, mode, base, n, nt, ncta, partial, jobs, st, inva); break;
+    case RMW_UT: launch_sym<RMW_UT>(B != nullptr, mode, base, n, nt, ncta, partial, jobs, st, inva); break;
+    case RMW_WF: launch_sym<RMW_WF>(B != nullptr, mode, base, n, nt, ncta, partial, jobs, st, inva); break;
+    default: launch_sym<RMW_WT>(B != nullptr, mode, base, n, nt, ncta, partial, jobs, st, inva); break;
     }
     if (int rc = trace_end(tok, st)) return rc;
     const double nf = kind_norm(kind, eta, a);
@@ -1244,10 +1352,9 @@ int wall_product_batched(const WallBatch &B, int kind, const double *r, const do
     if (rc) return rc;
     if (B.n == 0 || B.njobs == 0) return RMW_OK;
     void *ws = nullptr;
-    if ((mode == RMW_MODE_DF64 || mode == RMW_MODE_MIXED) && B.nsym > 0 &&
-        B.sym_doubles * (long long)sizeof(double) <= (long long)kSymMaxPartialBytes) {
+    if (B.nsym > 0 && B.sym_doubles * (long long)sizeof(double) <= (long long)kSymMaxPartialBytes) {
         // each suspension's unordered pairs once, applied both ways
-        const size_t rec = (mode == RMW_MODE_DF64) ? sizeof(SrcDF) : sizeof(SrcF);
+        const size_t rec = (mode == RMW_MODE_FP64) ? sizeof(SrcD) : (mode == RMW_MODE_DF64 ? sizeof(SrcDF) : sizeof(SrcF));
         const size_t packed = ((rec * (size_t)B.n + 255) / 256) * 256;
         rc = scratch(SCRATCH_PAIR, packed + sizeof(double) * (size_t)B.sym_doubles, &ws, st);
         if (rc) return rc;

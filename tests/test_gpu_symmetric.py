@@ -1,4 +1,4 @@
-"""GPU: the symmetric kernels of all four blocks, df64 and mixed (each
+"""GPU: the symmetric kernels of all four blocks, FP64, df64 and mixed (each
 unordered pair evaluated once and applied both ways: M_UF with f3 and f4
 exchanged, the rotation blocks with d -> -d and the heights exchanged)
 against the oracle and against the standard kernels:
@@ -52,6 +52,19 @@ def test_symmetric_matches_oracle_and_standard(cuda_device, kind, n, damped):
 
 
 @pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("n", [256, 383, 1000])
+@pytest.mark.parametrize("damped", [False, True])
+def test_fp64_symmetric_matches_oracle_and_standard(cuda_device, kind, n, damped):
+    r, v = _blobs(n, n + 2, damped)
+    a = 0.35
+    sym = _product(r, v, a, -1, "fp64", kind)
+    std = _product(r, v, a, 8, "fp64", kind)
+    ref = owall.wall_product(kind, r, v, 1.0, a)
+    assert rel_err(sym, ref) <= 1e-12
+    assert rel_err(sym, std) <= 1e-13
+
+
+@pytest.mark.parametrize("kind", KINDS)
 @pytest.mark.parametrize("n", [256, 300, 1000, 2049])
 @pytest.mark.parametrize("damped", [False, True])
 def test_mixed_symmetric_matches_oracle_and_standard(cuda_device, kind, n, damped):
@@ -86,8 +99,9 @@ def test_symmetric_choice_rules(cuda_device):
         mob.autotune_set("uf", 100, "df64", -1)  # fewer than 256 blobs
     with pytest.raises(RMWError):
         mob.autotune_set("wt", 255, "mixed", -1)
-    with pytest.raises(RMWError):
-        mob.autotune_set("uf", 1000, "fp64", -1)  # df64 and mixed only
+    mob.autotune_set("uf", 1000, "fp64", -1)  # every precision mode has a symmetric kernel
+    assert mob.autotune_lookup("uf", 1000, "fp64") == (-1, True)
+    mob.autotune_clear()
     mob.autotune_set("uf", 1000, "df64", -1)
     assert mob.autotune_lookup("uf", 1000, "df64") == (-1, True)
     # periodic products fall back to the standard kernel and stay correct

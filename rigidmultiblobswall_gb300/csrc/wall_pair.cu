@@ -1123,6 +1123,20 @@ int wall_product_with_scratch(int kind, const double *r, const double *v, double
     return launch_dispatch(kind, r, v, out, n, eta, a, L, mode, st, scratch_ptr, nchunks, nullptr);
 }
 
+size_t wall_sym_partial_budget()
+{
+    static size_t budget[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return kSymMaxPartialBytes;
+    if (!budget[dev]) {
+        size_t total = 0;
+        cudaDeviceProp prop;
+        if (cudaGetDeviceProperties(&prop, dev) == cudaSuccess) total = prop.totalGlobalMem;
+        budget[dev] = std::max(kSymMaxPartialBytes, total / 8);
+    }
+    return budget[dev];
+}
+
 bool wall_sym_applicable(int kind, int mode, int n, const double *L)
 {
     if (kind < RMW_UF || kind > RMW_WT ||
@@ -1131,7 +1145,7 @@ bool wall_sym_applicable(int kind, int mode, int n, const double *L)
     if (L && (L[0] > 0 || L[1] > 0 || L[2] > 0)) return false;
     if (n < 2 * kTile) return false;
     const double nt = (double)((n + kTile - 1) / kTile);
-    return nt * 3.0 * (double)n * sizeof(double) <= (double)kSymMaxPartialBytes;
+    return nt * 3.0 * (double)n * sizeof(double) <= (double)wall_sym_partial_budget();
 }
 
 int wall_sym_slots(int n) { return (n + kTile - 1) / kTile; }
@@ -1237,10 +1251,18 @@ int wall_product(int kind, const double *r, const double *v, double *out, int64_
     if (rc) return rc;
     if (n == 0) return RMW_OK;
     int nchunks = wall_chunks(kind, mode, (int)n);
-    const bool sym = nchunks == kSymChunks && wall_sym_applicable(kind, mode, (int)n, L);
+    bool sym = nchunks == kSymChunks && wall_sym_applicable(kind, mode, (int)n, L);
     if (nchunks == kSymChunks && !sym) nchunks = wall_default_chunks((int)n);
     void *ws = nullptr;
     rc = scratch(SCRATCH_PAIR, wall_scratch_bytes((int)n, mode, sym ? wall_sym_slots((int)n) : nchunks), &ws, st);
+    if (rc && sym) {
+        // the symmetric kernel's partial sums did not fit next to the caller's
+        // allocations: the standard kernel needs far less scratch
+        cudaGetLastError();
+        sym = false;
+        nchunks = wall_default_chunks((int)n);
+        rc = scratch(SCRATCH_PAIR, wall_scratch_bytes((int)n, mode, nchunks), &ws, st);
+    }
     if (rc) return rc;
     if (sym) return wall_product_sym_with_scratch(kind, r, v, out, (int)n, eta, a, mode, st, ws);
     return wall_product_with_scratch(kind, r, v, out, (int)n, eta, a, L, mode, st, ws, nchunks);
@@ -1352,7 +1374,7 @@ int wall_product_batched(const WallBatch &B, int kind, const double *r, const do
     if (rc) return rc;
     if (B.n == 0 || B.njobs == 0) return RMW_OK;
     void *ws = nullptr;
-    if (B.nsym > 0 && B.sym_doubles * (long long)sizeof(double) <= (long long)kSymMaxPartialBytes) {
+    if (B.nsym > 0 && B.sym_doubles * (long long)sizeof(double) <= (long long)wall_sym_partial_budget()) {
         // each suspension's unordered pairs once, applied both ways
         const size_t rec = (mode == RMW_MODE_FP64) ? sizeof(SrcD) : (mode == RMW_MODE_DF64 ? sizeof(SrcDF) : sizeof(SrcF));
         const size_t packed = ((rec * (size_t)B.n + 255) / 256) * 256;

@@ -59,10 +59,15 @@ int wall_default_chunks(int n);
 // Symmetric product of any kind (each unordered pair once, applied both ways),
 // df64 or mixed: selected when wall_chunks returns kSymChunks and
 // wall_sym_applicable holds (df64 or mixed, not periodic, n >= 256, ntiles x
-// 3n doubles of partial sums within kSymMaxPartialBytes).  Its scratch is
+// 3n doubles of partial sums within wall_sym_partial_budget()).  Its scratch is
 // wall_scratch_bytes(n, mode, wall_sym_slots(n)).
 constexpr int kSymChunks = -1;
 constexpr size_t kSymMaxPartialBytes = size_t(6) << 30;  // up to ~185,000 blobs (5.5 GB at 172,032)
+// The partial-sum budget of the current device: kSymMaxPartialBytes, or an
+// eighth of the device's memory if that is more (35 GB, ~430,000 blobs, on a
+// 284 GB part).  A fixed property of the device, so the kernel choice for a
+// given n does not depend on what else is allocated.
+size_t wall_sym_partial_budget();
 bool wall_sym_applicable(int kind, int mode, int n, const double *L);
 int wall_sym_slots(int n);
 int wall_product_sym_with_scratch(int kind, const double *r, const double *v, double *out, int n, double eta,

@@ -190,8 +190,8 @@ int rmw_wall_force_torque(const double *r, const double *F, const double *T, dou
                           double eta, double a, const double *L_host, int mode, void *stream);
 
 /* Launch-shape autotuner (no reference counterpart): times every admissible
- * source split of the all-pairs grid (and, for the df64 UF product, the
- * symmetric kernel, reported as nchunks = -1) on n synthetic blobs and caches the
+ * source split of the all-pairs grid (and, where it applies, the symmetric
+ * kernel, reported as nchunks = -1) on n synthetic blobs and caches the
  * fastest for (device, kind, mode, n's quarter-octave size bucket); the
  * product entry points above and the rigid-body operators then use it.
  * Synchronous.  best_ms / default_ms: mean time of the chosen split and of
@@ -200,10 +200,13 @@ int rmw_wall_autotune(int kind, int mode, int64_t n, int reps, void *stream, int
                       double *default_ms);
 int rmw_wall_autotune_lookup(int kind, int mode, int64_t n, int *nchunks, int *tuned);
 /* Pin a choice instead of measuring: nchunks in [1, 64], or -1 for the
- * symmetric df64 / mixed UF kernel (each unordered pair evaluated once and applied
- * both ways; non-periodic, n >= 256, up to about 185,000 blobs: its
+ * symmetric kernel of any block and precision mode (each unordered pair
+ * evaluated once and applied both ways; non-periodic, n >= 256; its
  * deterministic partial sums take ceil(n/128) x 3n doubles, 5.5 GB at
- * 172,032 blobs). */
+ * 172,032 blobs, within an eighth of the device memory and at least 6 GiB:
+ * about 430,000 blobs on a 284 GB device).  Without a tuned or pinned
+ * choice the products use the symmetric kernel from 4,096 blobs in FP64 and
+ * df64 and from 8,192 in mixed precision. */
 int rmw_wall_autotune_set(int kind, int mode, int64_t n, int nchunks);
 int rmw_wall_autotune_clear(void);
 

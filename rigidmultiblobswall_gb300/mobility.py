@@ -275,7 +275,8 @@ def autotune_lookup(kind="uf", n=10752, mode="df64"):
 
 def autotune_set(kind="uf", n=10752, mode="df64", nchunks=-1):
     """Pin the launch choice for this size bucket: a source split in [1, 64]
-    or -1 for the symmetric df64 UF kernel."""
+    or -1 for the symmetric kernel (non-periodic products of 256 or more
+    blobs, any block and precision mode)."""
     _native.call("rmw_wall_autotune_set", _native.KINDS[kind], _MODES[mode], int(n), int(nchunks))
 
 

@@ -112,3 +112,23 @@ def test_symmetric_choice_rules(cuda_device):
     mob.autotune_clear()
     ref = owall.wall_product("uf", r, v, 1.0, 0.35, periodic_length=L)
     assert rel_err(got, ref) <= 1e-12
+
+
+def test_symmetric_beyond_six_gib_of_partial_sums(cuda_device):
+    """200,000 blobs: 7.5 GB of partial sums, above the former fixed 6 GiB
+    budget and inside the device-scaled one; sampled rows against the oracle."""
+    import torch
+    n = 200_000
+    rng = np.random.default_rng(17)
+    r = np.empty((n, 3))
+    r[:, :2] = rng.uniform(0, 400.0, (n, 2))
+    r[:, 2] = rng.uniform(0.6, 6.0, n)
+    v = rng.standard_normal(3 * n)
+    a = 0.35
+    mob.autotune_clear()
+    assert mob.autotune_lookup("uf", n, "mixed")[0] == -1
+    got = mob.wall_product("uf", torch.tensor(r, device="cuda"), torch.tensor(v, device="cuda"), 1.0, a,
+                           mode="mixed").cpu().numpy()
+    rows = rng.choice(n, 40, replace=False)
+    ref = owall.wall_product("uf", r, v, 1.0, a, rows=rows)
+    assert rel_err(got.reshape(-1, 3)[rows].reshape(-1), ref) <= 1e-6

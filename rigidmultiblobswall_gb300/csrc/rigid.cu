@@ -381,6 +381,39 @@ __global__ void block_tri_mult_kernel(const double *__restrict__ T, const long l
     }
 }
 
+// The same products for all nvec vectors of a body in one CTA, in FP32 (the
+// mixed-precision Lanczos operator, whose tolerance is 1e-3): the factor
+// block is read once, converted into shared memory, and applied to every
+// vector, instead of one FP64 pass over the block per vector.  Shared
+// memory: m^2 + nvec m floats.  In place (y == x) is safe: the body's slice of
+// every vector is staged before any is written.
+__global__ void block_tri_mult_f32_kernel(const double *__restrict__ T, const long long *__restrict__ moff,
+                                          const int *__restrict__ boff, const double *x, double *y, int transpose,
+                                          long long ld, int nvec)
+{
+    extern __shared__ float tsm[];
+    const int b = blockIdx.x;
+    const int o = boff[b], m = 3 * (boff[b + 1] - o);
+    float *Ts = tsm, *xs = tsm + (size_t)m * m;
+    const double *Tb = T + moff[b];
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) Ts[e] = (float)Tb[e];
+    for (int e = threadIdx.x; e < nvec * m; e += blockDim.x) {
+        const int v = e / m, t = e - v * m;
+        xs[e] = (float)x[(long long)v * ld + 3LL * o + t];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nvec * m; e += blockDim.x) {
+        const int v = e / m, t = e - v * m;
+        const float *xv = xs + (size_t)v * m;
+        float acc = 0.f;
+        if (!transpose)
+            for (int k = 0; k <= t; ++k) acc = fmaf(Ts[t * m + k], xv[k], acc);
+        else
+            for (int k = t; k < m; ++k) acc = fmaf(Ts[k * m + t], xv[k], acc);
+        y[(long long)v * ld + 3LL * o + t] = acc;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // body kinematics (FP64)
 // r_i = R(q_b) r_ref_i + x_b  (body/body.py:64-78, quaternion.py:42-51)
@@ -558,11 +591,33 @@ int rigid_mobility_pc(RigidSystem &S, const double *w, double *y, int mode)
     return tri_mult(S, S.linv, y, y, 0);
 }
 
+// FP32 form of tri_mult for all nvec vectors per body (mixed mode); false when
+// a body's block does not fit the shared memory
+static bool tri_mult_f32_fits(const RigidSystem &S, int nvec)
+{
+    return ((size_t)S.max_m * S.max_m + (size_t)nvec * S.max_m) * sizeof(float) <= 200 * 1024;
+}
+static int tri_mult_f32(RigidSystem &S, const double *T, const double *x, double *y, int transpose, int nvec)
+{
+    const size_t sm = ((size_t)S.max_m * S.max_m + (size_t)nvec * S.max_m) * sizeof(float);
+    if (sm > 48 * 1024)
+        RMW_CUDA(cudaFuncSetAttribute(block_tri_mult_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sm));
+    block_tri_mult_f32_kernel<<<S.nb, 256, sm, S.st>>>(T, S.moff, S.boff, x, y, transpose, 3LL * S.n, nvec);
+    RMW_CHECK_LAUNCH("block triangular multiply (FP32)");
+    return RMW_OK;
+}
+
 int rigid_mobility_pc_multi(RigidSystem &S, const double *W, double *Y, int nvec, int mode, double *tmp,
                             const unsigned char *active)
 {
     if (!S.stoch_ready) return fail(RMW_ERR_ARG, "stochastic preconditioner not built");
     const long long ld = 3LL * S.n;
+    if (mode == RMW_MODE_MIXED && S.wall && tri_mult_f32_fits(S, nvec)) {
+        if (int rc = tri_mult_f32(S, S.linv, W, tmp, 1, nvec)) return rc;
+        if (int rc = wall_uf_multi(S.r, tmp, ld, Y, ld, nvec, S.n, S.eta, S.a, S.batch, S.st, active)) return rc;
+        return tri_mult_f32(S, S.linv, Y, Y, 0, nvec);
+    }
     if (int rc = tri_mult(S, S.linv, W, tmp, 1, nvec)) return rc;
     if (mode == RMW_MODE_MIXED && S.wall) {
         if (int rc = wall_uf_multi(S.r, tmp, ld, Y, ld, nvec, S.n, S.eta, S.a, S.batch, S.st, active)) return rc;

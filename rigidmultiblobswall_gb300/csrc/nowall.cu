@@ -39,6 +39,11 @@ struct __align__(16) NwSrcF {
 struct __align__(16) NwSrcDF {
     float4 hi, lo, vhi, vlo;
 };
+// the symmetric kernels (wall_pair.cu) read these records as the wall
+// products' SrcD (x, y, z, pad, vx, vy, vz, pad), SrcF (hi, lo, v) and SrcDF
+// (hi, lo, vhi, vlo): the same fields in the same order and sizes
+static_assert(sizeof(NwSrcD) == 64 && sizeof(NwSrcF) == 48 && sizeof(NwSrcDF) == 64,
+              "no-wall records must keep the wall records' layouts");
 
 __global__ void nw_pack_fp64_kernel(const double *__restrict__ r, const double *__restrict__ v,
                                     NwSrcD *__restrict__ src, int n, double inva)
@@ -273,7 +278,12 @@ int nowall_product(int kind, const double *r, const double *v, double *out, int6
     if (int rc = validate_product_args(kind, r, v, out, n, eta, a, mode)) return rc;
     if (n == 0) return RMW_OK;
     const int N = (int)n;
-    const int nchunks = wall_default_chunks(N);
+    const bool per = L && (L[0] > 0 || L[1] > 0 || L[2] > 0);
+    // the symmetric kernel (each unordered pair once, both ways) from 4,096 blobs
+    // in FP64 and df64 and 8,192 in mixed, as the wall products' untuned rule
+    const bool sym = !per && N >= (mode == RMW_MODE_MIXED ? 8192 : 4096) &&
+                     wall_sym_applicable(kind, mode, N, nullptr);
+    const int nchunks = sym ? wall_sym_slots(N) : wall_default_chunks(N);
     const size_t rec = (mode == RMW_MODE_FP64) ? sizeof(NwSrcD) : (mode == RMW_MODE_DF64 ? sizeof(NwSrcDF)
                                                                                           : sizeof(NwSrcF));
     const size_t packed = ((rec * (size_t)N + 255) / 256) * 256;
@@ -285,17 +295,21 @@ int nowall_product(int kind, const double *r, const double *v, double *out, int6
     if (mode == RMW_MODE_FP64) nw_pack_fp64_kernel<<<pg, pb, 0, st>>>(r, v, (NwSrcD *)ws, N, inva);
     else if (mode == RMW_MODE_DF64) nw_pack_df_kernel<<<pg, pb, 0, st>>>(r, v, (NwSrcDF *)ws, N, inva);
     else nw_pack_mixed_kernel<<<pg, pb, 0, st>>>(r, v, (NwSrcF *)ws, N, inva);
-    const bool per = L && (L[0] > 0 || L[1] > 0 || L[2] > 0);
     const NwImages P{L ? L[0] * inva : 0.0, L ? L[1] * inva : 0.0, L ? L[2] * inva : 0.0};
     const int chunk = (N + nchunks - 1) / nchunks;
     const dim3 grid((N + kNwThreads - 1) / kNwThreads, nchunks);
     void *tok = nullptr;
     if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
-    switch (kind) {
-    case RMW_UF: nw_dispatch<RMW_UF>(per, mode, grid, st, ws, N, chunk, P, partial); break;
-    case RMW_UT: nw_dispatch<RMW_UT>(per, mode, grid, st, ws, N, chunk, P, partial); break;
-    case RMW_WF: nw_dispatch<RMW_WF>(per, mode, grid, st, ws, N, chunk, P, partial); break;
-    default: nw_dispatch<RMW_WT>(per, mode, grid, st, ws, N, chunk, P, partial); break;
+    if (sym) {
+        // the sym slots have the chunk layout (slot s of blob i at s * 3n + 3i)
+        if (int rc = nowall_sym_launch(kind, mode, ws, N, partial, st)) return rc;
+    } else {
+        switch (kind) {
+        case RMW_UF: nw_dispatch<RMW_UF>(per, mode, grid, st, ws, N, chunk, P, partial); break;
+        case RMW_UT: nw_dispatch<RMW_UT>(per, mode, grid, st, ws, N, chunk, P, partial); break;
+        case RMW_WF: nw_dispatch<RMW_WF>(per, mode, grid, st, ws, N, chunk, P, partial); break;
+        default: nw_dispatch<RMW_WT>(per, mode, grid, st, ws, N, chunk, P, partial); break;
+        }
     }
     if (int rc = trace_end(tok, st)) return rc;
     const double p = (kind == RMW_UF) ? a : (kind == RMW_WT ? a * a * a : a * a);

@@ -365,6 +365,66 @@ __device__ __forceinline__ void pair_rot_sym(T dx, T dy, T dz, T Rz, T hi, T hj,
     }
 }
 
+// Free-space blocks for both orders of one pair (the symmetric no-wall
+// kernels): M_ji = M_ij(-d), so UF and WT (even in d) apply the same block to
+// the other vector and UT / WF (odd in d) its negative.  (ux, uy, uz) +=
+// M_ij v, (wx, wy, wz) += M_ji q.
+template <typename T, int KIND>
+__device__ __forceinline__ void pair_rpy_sym(T dx, T dy, T dz, T vx, T vy, T vz, T qx, T qy, T qz, T &ux, T &uy,
+                                             T &uz, T &wx, T &wy, T &wz)
+{
+    const T r2 = fm<T>(dx, dx, fm<T>(dy, dy, dz * dz));
+    const T invr = rsq<T>(r2);
+    if (KIND == RMW_UT || KIND == RMW_WF) {
+        T c = invr * invr * invr;
+        const bool near = !(r2 >= T(4));  // r < 2
+        if (__any_sync(__activemask(), near)) {
+            if (near) c = T(0.5) * (T(1) - T(0.375) * (r2 * invr));
+        }
+        ux = fm<T>(c, fm<T>(vy, dz, -vz * dy), ux);
+        uy = fm<T>(c, fm<T>(vz, dx, -vx * dz), uy);
+        uz = fm<T>(c, fm<T>(dy, vx, -dx * vy), uz);
+        wx = fm<T>(-c, fm<T>(qy, dz, -qz * dy), wx);
+        wy = fm<T>(-c, fm<T>(qz, dx, -qx * dz), wy);
+        wz = fm<T>(-c, fm<T>(dy, qx, -dx * qy), wz);
+        return;
+    }
+    const T invr2 = invr * invr;
+    T A, Bc;
+    if (KIND == RMW_UF) {
+        A = (T(1) + T(2.0 / 3.0) * invr2) * invr;
+        Bc = (T(1) - T(2) * invr2) * invr2 * invr;
+        const bool near = !(r2 > T(4));  // r <= 2
+        if (__any_sync(__activemask(), near)) {
+            if (near) {
+                const T r = r2 * invr;
+                A = T(4.0 / 3.0) * (T(1) - T(0.28125) * r);
+                Bc = T(0.125) * invr;
+            }
+        }
+    } else {  // RMW_WT
+        const T invr3 = invr2 * invr;
+        A = T(-0.5) * invr3;
+        Bc = T(1.5) * invr2 * invr3;
+        const bool near = !(r2 >= T(4));
+        if (__any_sync(__activemask(), near)) {
+            if (near) {
+                const T r = r2 * invr;
+                A = T(1) - T(0.84375) * r + T(0.078125) * r * r2;
+                Bc = T(0.28125) * invr - T(0.046875) * r;
+            }
+        }
+    }
+    const T G = Bc * fm<T>(dx, vx, fm<T>(dy, vy, dz * vz));
+    const T Gq = Bc * fm<T>(dx, qx, fm<T>(dy, qy, dz * qz));
+    ux = fm<T>(A, vx, fm<T>(G, dx, ux));
+    uy = fm<T>(A, vy, fm<T>(G, dy, uy));
+    uz = fm<T>(A, vz, fm<T>(G, dz, uz));
+    wx = fm<T>(A, qx, fm<T>(Gq, dx, wx));
+    wy = fm<T>(A, qy, fm<T>(Gq, dy, wy));
+    wz = fm<T>(A, qz, fm<T>(Gq, dz, wz));
+}
+
 // Free-space RPY blocks (no wall): the RPY parts of pair_contrib, for the
 // no-wall products (mobility/mobility_numba.py:13-1190).  (dx, dy, dz) =
 // (r_i - r_j)/a.  Accumulates M_ij v into (ux, uy, uz), unscaled.

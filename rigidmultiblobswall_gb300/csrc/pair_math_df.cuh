@@ -437,4 +437,64 @@ __device__ __forceinline__ void pair_acc_df(df dx, df dy, df dz, df Rz, df hi, d
     }
 }
 
+// Double-float form of pair_rpy_sym (free space, both orders of one pair).
+template <int KIND>
+__device__ __forceinline__ void pair_rpy_sym_df(df dx, df dy, df dz, df vx, df vy, df vz, df qx, df qy, df qz,
+                                                df &ux, df &uy, df &uz, df &wx, df &wy, df &wz)
+{
+    constexpr df TWO_THIRDS = dfc::make(2.0 / 3.0);
+    constexpr df FOUR_THIRDS = dfc::make(4.0 / 3.0);
+    const df r2 = mad(dz, dz, mad_u(dx, dx, sqr_u(dy)));
+    const df invr = rsqrt_df(r2);
+    if (KIND == RMW_UT || KIND == RMW_WF) {
+        df c = sqr(invr) * invr;
+        const bool near = !(r2 >= 4.0f);  // r < 2
+        if (__any_sync(__activemask(), near)) {
+            if (near) c = scale2(1.0f - (r2 * invr) * 0.375f, 0.5f);
+        }
+        // c (v x d) for target i, -c (q x d) for target j
+        acc_add(ux, c * mad2(vy, dz, -vz, dy));
+        acc_add(uy, c * mad2(vz, dx, -vx, dz));
+        acc_add(uz, c * mad2(dy, vx, -dx, vy));
+        acc_add(wx, -(c * mad2(qy, dz, -qz, dy)));
+        acc_add(wy, -(c * mad2(qz, dx, -qx, dz)));
+        acc_add(wz, -(c * mad2(dy, qx, -dx, qy)));
+        return;
+    }
+    const df invr2 = sqr(invr);
+    df A, Bc;
+    if (KIND == RMW_UF) {
+        A = mad(TWO_THIRDS, invr2, df_from(1.0f)) * invr;
+        Bc = (1.0f - scale2(invr2, 2.0f)) * invr2 * invr;
+        const bool near = !(r2 > 4.0f);  // r <= 2
+        if (__any_sync(__activemask(), near)) {
+            if (near) {
+                const df r = r2 * invr;
+                A = FOUR_THIRDS * (1.0f - r * 0.28125f);
+                Bc = scale2(invr, 0.125f);
+            }
+        }
+    } else {  // RMW_WT
+        const df invr3 = invr2 * invr;
+        A = invr3 * -0.5f;
+        Bc = (invr2 * invr3) * 1.5f;
+        const bool near = !(r2 >= 4.0f);
+        if (__any_sync(__activemask(), near)) {
+            if (near) {
+                const df r = r2 * invr;
+                A = (1.0f - r * 0.84375f) + (r * r2) * 0.078125f;
+                Bc = invr * 0.28125f - r * 0.046875f;
+            }
+        }
+    }
+    const df G = Bc * dot3(dx, vx, dy, vy, dz, vz);
+    const df Gq = Bc * dot3(dx, qx, dy, qy, dz, qz);
+    acc_dot2(ux, A, vx, G, dx);
+    acc_dot2(uy, A, vy, G, dy);
+    acc_dot2(uz, A, vz, G, dz);
+    acc_dot2(wx, A, qx, Gq, dx);
+    acc_dot2(wy, A, qy, Gq, dy);
+    acc_dot2(wz, A, qz, Gq, dz);
+}
+
 }  // namespace rmw

@@ -275,7 +275,7 @@ __device__ __forceinline__ void sym_cta(const SymJob *jobs, int &n, int &nt, int
     }
 }
 
-template <bool SEG, int KIND>
+template <bool SEG, int KIND, bool NOWALL = false>
 __device__ __forceinline__ void df_sym_body(const SrcDF *__restrict__ src, int n, int nt,
                                             double *__restrict__ partial, const SymJob *__restrict__ jobs)
 {
@@ -326,7 +326,9 @@ __device__ __forceinline__ void df_sym_body(const SrcDF *__restrict__ src, int n
         df wx = {a0.x, a0.y}, wy = {a1.x, a1.y}, wz = {a2.x, a2.y};
         // differences renormalised (a cancelled high part must not leave the value in the low part, whose
         // square a double-float product drops); the sum of two heights cannot cancel
-        if constexpr (KIND == RMW_UF)
+        if constexpr (NOWALL)
+            pair_rpy_sym_df<KIND>(xi - xj, yi - yj, zi - zj, vx, vy, vz, qx, qy, qz, ux, uy, uz, wx, wy, wz);
+        else if constexpr (KIND == RMW_UF)
             pair_uf_sym_df(xi - xj, yi - yj, zi - zj, add_u(zi, zj), zi, zj, vx, vy, vz, qx, qy, qz, ux, uy, uz, wx,
                            wy, wz);
         else
@@ -408,7 +410,7 @@ __global__ void __launch_bounds__(kThreads) wall_rot_df_sym_kernel(const SrcDF *
 // tile is folded into a TwoSum-compensated accumulator; the source side sums
 // its 32 contributions per warp in FP32 shared memory and the four warp
 // copies in FP64.
-template <bool SEG, int KIND>
+template <bool SEG, int KIND, bool NOWALL = false>
 __device__ __forceinline__ void mixed_sym_body(const SrcF *__restrict__ src, int n, int nt,
                                                double *__restrict__ partial, const SymJob *__restrict__ jobs)
 {
@@ -444,7 +446,9 @@ __device__ __forceinline__ void mixed_sym_body(const SrcF *__restrict__ src, int
         const float hj = sh.z + sl.z;
         const float Rz = hi + hj;
         float wx = sacc[warp][0][jl], wy = sacc[warp][1][jl], wz = sacc[warp][2][jl];
-        if constexpr (KIND == RMW_UF) {
+        if constexpr (NOWALL) {
+            pair_rpy_sym<float, KIND>(dx, dy, dz, sv.x, sv.y, sv.z, me.v.x, me.v.y, me.v.z, ux, uy, uz, wx, wy, wz);
+        } else if constexpr (KIND == RMW_UF) {
             const UFCoeffs<float> c = uf_coeffs<float>(dx, dy, dz, Rz, hi, hj);
             uf_apply<float>(c, dx, dy, dz, Rz, sv.x, sv.y, sv.z, ux, uy, uz);
             const UFCoeffs<float> ct = {c.Af, c.Bc, c.c2, c.c4, c.c3, c.Af5};  // M^T: f3 and f4 trade places
@@ -523,7 +527,7 @@ __global__ void __launch_bounds__(kThreads) wall_rot_mixed_sym_kernel(const SrcF
 // slots, FP64 pair arithmetic (the FP64 pipe bounds it, so halving the
 // coefficient work per ordered pair is the gain); source-side sums per warp
 // in FP64 shared memory.
-template <bool SEG, int KIND>
+template <bool SEG, int KIND, bool NOWALL = false>
 __device__ __forceinline__ void fp64_sym_body(const SrcD *__restrict__ src, int n, int nt, double inva,
                                               double *__restrict__ partial, const SymJob *__restrict__ jobs)
 {
@@ -559,7 +563,9 @@ __device__ __forceinline__ void fp64_sym_body(const SrcD *__restrict__ src, int 
         const double dx = xi - tx[jl], dy = yi - ty[jl], dz = zi - zj, Rz = zi + zj;
         const double vx = tvx[jl], vy = tvy[jl], vz = tvz[jl];
         double wx = sacc[warp][0][jl], wy = sacc[warp][1][jl], wz = sacc[warp][2][jl];
-        if constexpr (KIND == RMW_UF) {
+        if constexpr (NOWALL) {
+            pair_rpy_sym<double, KIND>(dx, dy, dz, vx, vy, vz, me.vx, me.vy, me.vz, ux, uy, uz, wx, wy, wz);
+        } else if constexpr (KIND == RMW_UF) {
             const UFCoeffs<double> c = uf_coeffs<double>(dx, dy, dz, Rz, zi, zj);
             uf_apply<double>(c, dx, dy, dz, Rz, vx, vy, vz, ux, uy, uz);
             const UFCoeffs<double> ct = {c.Af, c.Bc, c.c2, c.c4, c.c3, c.Af5};  // M^T: f3 and f4 trade places
@@ -617,6 +623,53 @@ __global__ void __launch_bounds__(kThreads) wall_fp64_sym_kernel(const SrcD *__r
                                                                   const SymJob *__restrict__ jobs)
 {
     fp64_sym_body<SEG, KIND>(src, n, nt, inva, partial, jobs);
+}
+
+// Free-space (no wall) symmetric kernels: the same bodies with pair_rpy_sym;
+// the no-wall pack writes records of the same layouts (positions over a, no
+// height shift or damping), so the FP64 body takes inva = 1.
+template <int KIND>
+__global__ void __launch_bounds__(kThreads) nowall_df_sym_kernel(const SrcDF *__restrict__ src, int n, int nt,
+                                                                  double *__restrict__ partial)
+{
+    df_sym_body<false, KIND, true>(src, n, nt, partial, nullptr);
+}
+template <int KIND>
+__global__ void __launch_bounds__(kThreads) nowall_mixed_sym_kernel(const SrcF *__restrict__ src, int n, int nt,
+                                                                     double *__restrict__ partial)
+{
+    mixed_sym_body<false, KIND, true>(src, n, nt, partial, nullptr);
+}
+template <int KIND>
+__global__ void __launch_bounds__(kThreads) nowall_fp64_sym_kernel(const SrcD *__restrict__ src, int n, int nt,
+                                                                    double *__restrict__ partial)
+{
+    fp64_sym_body<false, KIND, true>(src, n, nt, 1.0, partial, nullptr);
+}
+
+template <int KIND>
+static void nowall_sym_launch_kind(int mode, const void *src, int n, int nt, double *partial, cudaStream_t st)
+{
+    const unsigned ncta = (unsigned)((long long)nt * (nt + 1) / 2);
+    if (mode == RMW_MODE_FP64)
+        nowall_fp64_sym_kernel<KIND><<<ncta, kThreads, 0, st>>>((const SrcD *)src, n, nt, partial);
+    else if (mode == RMW_MODE_DF64)
+        nowall_df_sym_kernel<KIND><<<ncta, kThreads, 0, st>>>((const SrcDF *)src, n, nt, partial);
+    else
+        nowall_mixed_sym_kernel<KIND><<<ncta, kThreads, 0, st>>>((const SrcF *)src, n, nt, partial);
+}
+
+int nowall_sym_launch(int kind, int mode, const void *src, int n, double *partial, cudaStream_t st)
+{
+    const int nt = wall_sym_slots(n);
+    switch (kind) {
+    case RMW_UF: nowall_sym_launch_kind<RMW_UF>(mode, src, n, nt, partial, st); break;
+    case RMW_UT: nowall_sym_launch_kind<RMW_UT>(mode, src, n, nt, partial, st); break;
+    case RMW_WF: nowall_sym_launch_kind<RMW_WF>(mode, src, n, nt, partial, st); break;
+    default: nowall_sym_launch_kind<RMW_WT>(mode, src, n, nt, partial, st); break;
+    }
+    RMW_CHECK_LAUNCH("symmetric free-space product");
+    return RMW_OK;
 }
 
 // ---------------------------------------------------------------------------

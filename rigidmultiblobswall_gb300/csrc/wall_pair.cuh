@@ -72,6 +72,10 @@ bool wall_sym_applicable(int kind, int mode, int n, const double *L);
 int wall_sym_slots(int n);
 int wall_product_sym_with_scratch(int kind, const double *r, const double *v, double *out, int n, double eta,
                                   double a, int mode, cudaStream_t st, void *scratch_ptr);
+// The symmetric free-space pair kernel of `kind` on records packed by the
+// no-wall product (layouts of SrcD / SrcDF / SrcF, positions over a); writes
+// wall_sym_slots(n) partial-sum slots of 3n doubles.
+int nowall_sym_launch(int kind, int mode, const void *src, int n, double *partial, cudaStream_t st);
 // Source-chunk count the standard entry points use: the autotuned choice of
 // (kind, mode, n's size bucket) on the current device if there is one
 // (autotune.cu; kSymChunks = the symmetric kernel), else the built-in rule.

@@ -43,6 +43,23 @@ def test_no_wall_tile_tails_match_oracle(cuda_device, mode, n):
         assert rel_err(got.cpu().numpy(), owall.no_wall_product(kind, r, v, 0.8, 0.35)) <= TOL[mode]
 
 
+@pytest.mark.parametrize("mode,n", [("fp64", 4100), ("df64", 4100), ("mixed", 8200)])
+@pytest.mark.parametrize("kind", ["uf", "ut", "wf", "wt"])
+def test_no_wall_symmetric_kernel_rows_match_oracle(cuda_device, mode, n, kind):
+    """From 4,096 blobs (8,192 in mixed) the free-space products take the
+    symmetric kernel (each unordered pair once: M_ji = M_ij(-d)); blobs on both
+    sides of z = 0 and a few touching pairs, sampled rows against the oracle."""
+    rng = np.random.default_rng(n + len(kind))
+    side = 2.2 * np.cbrt(n)
+    r = rng.uniform(-side / 2, side / 2, (n, 3))
+    r[1::97] = r[0::97][: len(r[1::97])] + np.array([0.7, 0.0, 0.0])  # r = 2a pairs (a = 0.35)
+    v = rng.standard_normal(3 * n)
+    got = mob.no_wall_product(kind, r, v, 1.0, 0.35, mode=mode)
+    rows = np.concatenate([np.arange(0, n, 97)[:20], rng.choice(n, 20, replace=False)])
+    ref = owall.no_wall_product(kind, r, v, 1.0, 0.35, rows=rows)
+    assert rel_err(got.reshape(-1, 3)[rows].reshape(-1), ref) <= TOL[mode]
+
+
 def test_no_wall_force_torque_drop_in(cuda_device):
     rng = np.random.default_rng(3)
     r = rng.uniform(-4.0, 4.0, (200, 3))

@@ -762,6 +762,23 @@ def main():
             torch.cuda.synchronize()
             ms = (time.perf_counter() - t0) * 1e3 / 5
             products["free_surface_%s" % mode] = {"ms": round(ms, 6), "gpairs": round(n * n / (ms * 1e-3) / 1e9, 3)}
+        # the free-space (no wall) single-radius products (symmetric kernels at this size)
+        for kind in ("uf", "wt"):
+            for mode in ("fp64", "df64", "mixed"):
+                reps = 3 if mode == "fp64" else 10
+                fn = lambda: mb.no_wall_product(kind, rt, ft, eta, a, mode=mode)  # noqa: E731
+                fn()
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(reps):
+                    fn()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                products["no_wall_%s_%s" % (kind, mode)] = {"ms": round(ms, 6),
+                                                            "gpairs": round(n * n / (ms * 1e-3) / 1e9, 3)}
 
     solver = {} if args.no_extras else solver_metrics(dev)
     if not args.no_extras:

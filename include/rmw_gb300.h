@@ -246,7 +246,7 @@ int rmw_rigid_set_configuration(void *handle, const double *r_blobs, const doubl
 int rmw_rigid_build_pc(void *handle, int stochastic);
 /* The same for the solves of one precision mode: RMW_MODE_MIXED factorises the
  * body blocks on the FP32 pipe (FP64 runs at 1/64 of its rate on GB300) - an
- * equally valid block-diagonal preconditioner, convergence still judged by the
+ * equally valid block-diagonal preconditioner, convergence still decided by the
  * FP64-accurate residual; a block that is not positive definite in FP32 makes
  * it fall back to FP64.  RMW_MODE_FP64 / RMW_MODE_DF64: rmw_rigid_build_pc.
  * Solves and Lanczos in FP64 or df64 rebuild an FP32-factorised one. */

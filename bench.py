@@ -39,13 +39,16 @@ WORKLOAD = "wall-RPY M_UF.F, 256 shells x 42 blobs = 10,752 blobs (FP64-accurate
 # pipes, 80-85 % of them on the FMA pipe), from the ncu captures summarised in
 # profiles/wall_uf_df_sym_shells42x256.md (symmetric kernel, each unordered
 # pair once: smsp__inst_executed.sum * 32 / N^2 = 1,704,728,972 * 32 / 10752^2
-# = 471.9) and profiles/wall_pair_df64_uf_shells42x256.md (standard kernel:
-# 3,310,220,558 * 32 / 10752^2 = 916.3).  The FP32 pipe issues at most one
+# = 471.9) and, for the one-sided kernel, a single-metric capture of one of
+# the autotuner's trial launches (split 15) of the same bench command:
+# `ncu --metrics smsp__inst_executed.sum,gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum
+# --clock-control none -k regex:wall_pair_df_kernel -s 72 -c 1 python bench.py --steps 5 --warmup 3
+# --no-extras --no-cpu-baseline`: 2,719,541,740 * 32 / 10752^2 = 752.8 (2.757 ms).  The FP32 pipe issues at most one
 # thread instruction per lane per clock, the rate the FMA-chain probe measures
 # (FLOP/s / 2), so achieved / peak is the fraction of issue capacity used.
-DF64_UF_INST_PER_PAIR = {"symmetric": 1704728972.0 * 32 / 10752 ** 2, "standard": 3310220558.0 * 32 / 10752 ** 2}
+DF64_UF_INST_PER_PAIR = {"symmetric": 1704728972.0 * 32 / 10752 ** 2, "standard": 2719541740.0 * 32 / 10752 ** 2}
 # dram__bytes_read.sum + dram__bytes_write.sum per launch, same captures
-DF64_UF_TRAFFIC_BYTES = {"symmetric": 735744, "standard": 723456}
+DF64_UF_TRAFFIC_BYTES = {"symmetric": 735744, "standard": 718848}
 
 
 def parse():
@@ -528,7 +531,7 @@ def batched_metrics(dev, nrhs=16):
 
 def single_product(args):
     """One wall product on the 256-shell workload (the default split of the autotuner's cache, i.e. the
-    symmetric kernel for UF in df64 and mixed at this size): CUDA-event time per step, L2 flushed between
+    symmetric kernel at this size, for every block and precision mode): CUDA-event time per step, L2 flushed between
     steps."""
     import torch
     from rigidmultiblobswall_gb300 import build as B

@@ -704,9 +704,9 @@ def main():
             res["alg_frac_of_mode_peak"] = res["alg_tflops"] * 1e12 / peak
             products["%s_%s" % (kind, mode)] = {k: round(v, 6) for k, v in res.items()}
 
-    # the force-and-torque product [U; W] = M [F; T] (one fused pass in FP64 and
-    # mixed; in df64 the sum of the four symmetric single products) against the
-    # four single products called one by one
+    # the force-and-torque product [U; W] = M [F; T] (in mixed one symmetric
+    # fused pass over the pairs; in FP64 and df64 the sum of the four symmetric
+    # single products) against the four single products called one by one
     if not args.no_extras:
         tt = torch.tensor(np.random.default_rng(7).standard_normal(3 * n), device=dev)
         for mode in ("fp64", "df64", "mixed"):
@@ -731,7 +731,7 @@ def main():
                 torch.cuda.synchronize()
                 res[name] = e0.elapsed_time(e1) / reps
             res["gpairs"] = n * n / (res["force_torque_ms"] * 1e-3) / 1e9
-            res["route"] = "four symmetric products" if mode == "df64" else "fused one-sided pass"
+            res["route"] = "symmetric fused kernel" if mode == "mixed" else "four symmetric products"
             products["force_torque_6n_%s" % mode] = {k: (round(v, 6) if isinstance(v, float) else v)
                                                       for k, v in res.items()}
 

@@ -383,6 +383,126 @@ __global__ void ft_finalize_kernel(const double *__restrict__ r, const double *_
     }
 }
 
+// ---------------------------------------------------------------------------
+// Symmetric mixed-precision force-torque kernel: the grid and pairing of the
+// symmetric single products (one CTA per tile pair T <= S of the upper
+// triangle; lane l meets source (l + k) mod 128 at step k; per-warp source
+// sums in shared memory), all four blocks per unordered pair, applied to both
+// blobs: u_i += UF_ij f_j + UT_ij t_j, w_i += WF_ij f_j + WT_ij t_j and the
+// same with i and j exchanged (M_ji = M_ij^T: UF through its transposed
+// coefficients, the rotation blocks through pair_rot_sym).  The UF
+// coefficients come times 3/2 and are scaled back per pair, so U and W keep
+// the one-sided kernels' sums and finalize.  Partial slots: blob b of tile X
+// gets one slot per tile, U at slot * 6n + 3b and W at slot * 6n + 3n + 3b.
+constexpr int kFtSymWarps = 4;
+constexpr int kFtSymTile = 32 * kFtSymWarps;
+
+template <bool WITH_W>
+__global__ void __launch_bounds__(kFtSymTile) ft_sym_mixed_kernel(const FtSrcF *__restrict__ src, int n, int nt,
+                                                                  double *__restrict__ partial)
+{
+    __shared__ float4 thi[kFtSymTile], tlo[kFtSymTile], tf[kFtSymTile], tt[kFtSymTile];
+    __shared__ float sacc[kFtSymWarps][6][kFtSymTile];
+    int T, S;
+    sym_tile_pair(blockIdx.x, nt, T, S);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool diag = (T == S);
+    const int i = T * kFtSymTile + tid;
+    const bool valid_i = i < n;
+    // a target or source past the end is a dummy far above the wall with zero vectors
+    const FtSrcF dummy = {make_float4(1.0e6f, 1.0e6f, 1.0e6f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f),
+                          make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+    const FtSrcF me = valid_i ? src[i] : dummy;
+    const float hi = me.hi.z + me.lo.z;
+    {
+        const int j = S * kFtSymTile + tid;
+        const FtSrcF sj = (j < n) ? src[j] : dummy;
+        thi[tid] = sj.hi;
+        tlo[tid] = sj.lo;
+        tf[tid] = sj.f;
+        tt[tid] = sj.t;
+    }
+    for (int c = 0; c < 6; ++c)
+        for (int k = lane; k < kFtSymTile; k += 32) sacc[warp][c][k] = 0.f;
+    __syncthreads();
+    float u0 = 0.f, u1 = 0.f, u2 = 0.f, w0 = 0.f, w1 = 0.f, w2 = 0.f;
+    constexpr float kThird2 = 2.0f / 3.0f;  // undoes the UF coefficients' 3/2
+    auto step = [&](int k) {
+        const int jl = (lane + k) & (kFtSymTile - 1);
+        const float4 sh = thi[jl], sl = tlo[jl], sf = tf[jl], st = tt[jl];
+        const float dx = (me.hi.x - sh.x) + (me.lo.x - sl.x);
+        const float dy = (me.hi.y - sh.y) + (me.lo.y - sl.y);
+        const float dz = (me.hi.z - sh.z) + (me.lo.z - sl.z);
+        const float hj = sh.z + sl.z;
+        const float Rz = hi + hj;
+        float a0 = sacc[warp][0][jl], a1 = sacc[warp][1][jl], a2 = sacc[warp][2][jl];
+        UFCoeffs<float> c = uf_coeffs<float>(dx, dy, dz, Rz, hi, hj);
+        c.Af *= kThird2; c.Bc *= kThird2; c.c2 *= kThird2; c.c3 *= kThird2; c.c4 *= kThird2; c.Af5 *= kThird2;
+        uf_apply<float>(c, dx, dy, dz, Rz, sf.x, sf.y, sf.z, u0, u1, u2);
+        const UFCoeffs<float> ct = {c.Af, c.Bc, c.c2, c.c4, c.c3, c.Af5};  // M^T: f3 and f4 trade places
+        uf_apply<float>(ct, dx, dy, dz, Rz, me.f.x, me.f.y, me.f.z, a0, a1, a2);
+        pair_rot_sym<float, RMW_UT>(dx, dy, dz, Rz, hi, hj, st.x, st.y, st.z, me.t.x, me.t.y, me.t.z, u0, u1, u2, a0,
+                                    a1, a2);
+        sacc[warp][0][jl] = a0;
+        sacc[warp][1][jl] = a1;
+        sacc[warp][2][jl] = a2;
+        if (WITH_W) {
+            float b0 = sacc[warp][3][jl], b1 = sacc[warp][4][jl], b2 = sacc[warp][5][jl];
+            pair_rot_sym<float, RMW_WF>(dx, dy, dz, Rz, hi, hj, sf.x, sf.y, sf.z, me.f.x, me.f.y, me.f.z, w0, w1, w2,
+                                        b0, b1, b2);
+            pair_rot_sym<float, RMW_WT>(dx, dy, dz, Rz, hi, hj, st.x, st.y, st.z, me.t.x, me.t.y, me.t.z, w0, w1, w2,
+                                        b0, b1, b2);
+            sacc[warp][3][jl] = b0;
+            sacc[warp][4][jl] = b1;
+            sacc[warp][5][jl] = b2;
+        }
+    };
+    if (diag) {
+        for (int k = 0; k < kFtSymTile; ++k) {
+            __syncwarp();
+            const int off = (k - 32 * warp) & (kFtSymTile - 1);  // (source - target) mod 128, warp-uniform
+            if (off == 0 || off > kFtSymTile / 2 || (off == kFtSymTile / 2 && warp >= kFtSymWarps / 2)) continue;
+            step(k);
+        }
+    } else {
+        for (int k = 0; k < kFtSymTile; ++k) {
+            __syncwarp();
+            step(k);
+        }
+    }
+    __syncthreads();
+    double q[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int w = 0; w < kFtSymWarps; ++w)
+        for (int c = 0; c < (WITH_W ? 6 : 3); ++c) q[c] += (double)sacc[w][c][tid];
+    const double tu[6] = {u0, u1, u2, w0, w1, w2};
+    const size_t stride = 6 * (size_t)n;
+    if (diag) {
+        if (valid_i) {
+            double *o = partial + (size_t)T * stride;
+            for (int c = 0; c < 3; ++c) {
+                o[3 * (size_t)i + c] = tu[c] + q[c];
+                o[3 * (size_t)n + 3 * (size_t)i + c] = tu[3 + c] + q[3 + c];
+            }
+        }
+    } else {
+        if (valid_i) {
+            double *o = partial + (size_t)S * stride;
+            for (int c = 0; c < 3; ++c) {
+                o[3 * (size_t)i + c] = tu[c];
+                o[3 * (size_t)n + 3 * (size_t)i + c] = tu[3 + c];
+            }
+        }
+        const int j = S * kFtSymTile + tid;
+        if (j < n) {
+            double *o = partial + (size_t)T * stride;
+            for (int c = 0; c < 3; ++c) {
+                o[3 * (size_t)j + c] = q[c];
+                o[3 * (size_t)n + 3 * (size_t)j + c] = q[3 + c];
+            }
+        }
+    }
+}
+
 __global__ void ft_add_kernel(const double *__restrict__ x, double *__restrict__ y, long long m)
 {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -390,8 +510,8 @@ __global__ void ft_add_kernel(const double *__restrict__ x, double *__restrict__
 }
 
 // U (and W) as sums of single products, each through the symmetric kernel
-// (every unordered pair once per block): in df64 faster than the fused
-// one-sided pass wherever the symmetric kernels apply.
+// (every unordered pair once per block): in FP64 and df64 faster than the
+// fused one-sided pass wherever the symmetric kernels apply.
 int ft_by_symmetric_products(const double *r, const double *F, const double *T, double *U, double *W, int n,
                              double eta, double a, int mode, cudaStream_t st)
 {
@@ -441,9 +561,31 @@ int wall_force_torque(const double *r, const double *F, const double *T, double 
     if (n == 0) return RMW_OK;
     const int N = (int)n;
     const bool per = L && (L[0] > 0 || L[1] > 0 || L[2] > 0);
-    // df64: the four symmetric products (5.9 vs 7.6 ms at 10,752 blobs); mixed
-    // keeps the fused pass, faster than the four there (0.90 vs 1.01 ms)
-    if (!per && mode == RMW_MODE_DF64) {
+    // mixed: the symmetric fused kernel from 8,192 blobs
+    if (!per && mode == RMW_MODE_MIXED && N >= 8192) {
+        const int nt = (N + kFtSymTile - 1) / kFtSymTile;
+        const size_t packed = ((sizeof(FtSrcF) * (size_t)N + 255) / 256) * 256;
+        const size_t part = sizeof(double) * 6 * (size_t)N * (size_t)nt;
+        if (part <= wall_sym_partial_budget()) {
+            void *ws = nullptr;
+            if (int rc = scratch(SCRATCH_PAIR, packed + part, &ws, st)) return rc;
+            double *partial = (double *)((char *)ws + packed);
+            const int pb = 256, pg = (N + pb - 1) / pb;
+            ft_pack_mixed_kernel<<<pg, pb, 0, st>>>(r, F, T, (FtSrcF *)ws, N, a);
+            const unsigned ncta = (unsigned)((long long)nt * (nt + 1) / 2);
+            void *tok = nullptr;
+            if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
+            if (W) ft_sym_mixed_kernel<true><<<ncta, kFtSymTile, 0, st>>>((const FtSrcF *)ws, N, nt, partial);
+            else ft_sym_mixed_kernel<false><<<ncta, kFtSymTile, 0, st>>>((const FtSrcF *)ws, N, nt, partial);
+            if (int rc = trace_end(tok, st)) return rc;
+            ft_finalize_kernel<<<pg, pb, 0, st>>>(r, F, T, partial, nt, U, W, N, a, 1.0 / (8.0 * kPi * eta * a));
+            RMW_CHECK_LAUNCH("symmetric force-torque wall product");
+            return RMW_OK;
+        }
+    }
+    // FP64 and df64: the four symmetric products (at 10,752 blobs FP64 39.4 vs
+    // 49.5 ms for the one-sided fused pass, df64 5.9 vs 7.6 ms)
+    if (!per && (mode == RMW_MODE_FP64 || mode == RMW_MODE_DF64)) {
         bool sym = true;
         for (int kind : {RMW_UF, RMW_UT, RMW_WF, RMW_WT})
             sym = sym && wall_chunks(kind, mode, N) == kSymChunks && wall_sym_applicable(kind, mode, N, nullptr);

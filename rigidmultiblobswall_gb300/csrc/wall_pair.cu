@@ -243,18 +243,6 @@ __global__ void __launch_bounds__(kThreads) wall_pair_df_kernel(const SrcDF *__r
 // sums ntiles slots in fixed order and the result is deterministic.
 constexpr int kSymWarps = kThreads / 32;
 
-__device__ __forceinline__ void sym_tile_pair(long long b, int nt, int &T, int &S)
-{
-    // rows T = 0.. of the upper triangle hold nt - T entries; offset(T) = T nt - T (T - 1) / 2
-    const double c = 2.0 * nt + 1.0;
-    int t = (int)floor(0.5 * (c - sqrt(fmax(c * c - 8.0 * (double)b, 0.0))));
-    t = max(0, min(nt - 1, t));
-    auto off = [nt](long long tt) { return tt * nt - tt * (tt - 1) / 2; };
-    while (t > 0 && off(t) > b) --t;
-    while (t + 1 < nt && off(t + 1) <= b) ++t;
-    T = t;
-    S = t + (int)(b - off(t));
-}
 
 // The CTA's tile pair: from blockIdx.x over the upper triangle of nt tiles, or
 // (SEG) from its job, which also moves src and partial to its suspension.

@@ -43,6 +43,21 @@ struct WallBatch {
 };
 int wall_batch_build(WallBatch &B, const long long *off_host, int ninst);
 void wall_batch_free(WallBatch &B);
+// Tile pair (T, S), T <= S, of CTA b over the upper triangle of nt tiles (the
+// symmetric kernels' grid): rows T = 0.. hold nt - T entries.
+__device__ __forceinline__ void sym_tile_pair(long long b, int nt, int &T, int &S)
+{
+    // rows T = 0.. of the upper triangle hold nt - T entries; offset(T) = T nt - T (T - 1) / 2
+    const double c = 2.0 * nt + 1.0;
+    int t = (int)floor(0.5 * (c - sqrt(fmax(c * c - 8.0 * (double)b, 0.0))));
+    t = max(0, min(nt - 1, t));
+    auto off = [nt](long long tt) { return tt * nt - tt * (tt - 1) / 2; };
+    while (t > 0 && off(t) > b) --t;
+    while (t + 1 < nt && off(t + 1) <= b) ++t;
+    T = t;
+    S = t + (int)(b - off(t));
+}
+
 // Right-hand sides per pass of wall_uf_multi.
 constexpr int kMultiPass = 16;
 // M_UF applied to nrhs vectors in mixed precision (rows of V, stride ldv).

@@ -39,13 +39,13 @@ def test_fused_matches_four_products(cuda_device, mode, damped, n):
     assert rel_err(Uonly, Ur) <= TOL[mode]
 
 
-@pytest.mark.parametrize("mode", ["df64", "mixed"])
+@pytest.mark.parametrize("mode", ["fp64", "df64", "mixed"])
 @pytest.mark.parametrize("damped", [False, True])
 def test_symmetric_route_matches_oracle(cuda_device, mode, damped):
     """With the symmetric kernels chosen for all four blocks (the default from
-    4,096 blobs in df64 and 8,192 in mixed; pinned here at 700), the df64
-    [U; W] is the sum of the four symmetric single products (mixed keeps the
-    fused pass)."""
+    4,096 blobs in FP64 and df64 and 8,192 in mixed; pinned here at 700), the
+    FP64 and df64 [U; W] are sums of the four symmetric single products (mixed
+    below 8,192 blobs keeps the one-sided fused pass)."""
     r, F, T = _case(700, 11, damped)
     a = 0.3
     mob.autotune_clear()
@@ -60,6 +60,24 @@ def test_symmetric_route_matches_oracle(cuda_device, mode, damped):
     assert rel_err(U, Ur) <= TOL[mode]
     assert rel_err(W, Wr) <= TOL[mode]
     assert rel_err(Uonly, Ur) <= TOL[mode]
+
+
+@pytest.mark.parametrize("damped", [False, True])
+def test_mixed_symmetric_force_torque_rows_match_oracle(cuda_device, damped):
+    """From 8,192 blobs the mixed [U; W] runs the symmetric fused kernel (all
+    four blocks per unordered pair, both ways); sampled rows against the
+    oracle, and the U-only form."""
+    n = 8300
+    r, F, T = _case(n, 23, damped)
+    a = 0.3
+    U, W = mob.wall_force_torque(r, F, T, 1.0, a, mode="mixed")
+    Uonly = mob.single_wall_mobility_trans_times_force_torque_pycuda(r, F, T, 1.0, a, mode="mixed")
+    rows = np.random.default_rng(5).choice(n, 40, replace=False)
+    Ur, Wr = owall.force_torque(r, F, T, 1.0, a, rows=rows)
+    pick = lambda x: x.reshape(-1, 3)[rows].reshape(-1)  # noqa: E731
+    assert rel_err(pick(U), Ur) <= 1e-6
+    assert rel_err(pick(W), Wr) <= 1e-6
+    assert rel_err(pick(Uonly), Ur) <= 1e-6
 
 
 @pytest.mark.parametrize("mode", ["fp64", "df64", "mixed"])

@@ -31,7 +31,9 @@ def _pairs(seed, a):
             d = rng.uniform(-10 * a, 10 * a, 3)
         ri = np.array([0.0, 0.0, zi])
         rj = ri - d
-        if k % 4 in (2, 3):
+        if k % 4 in (0, 1):
+            rj[2] = zj  # far or near-wall pairs: both heights drawn above the wall plane
+        else:
             rj[2] = max(rj[2], 0.5 * a)  # keep the blob above the wall plane
         out.append(np.array([ri, rj]))
     return out

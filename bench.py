@@ -36,19 +36,39 @@ METRIC = "wall-RPY M.F Gpairs/s"
 HEAD_MODE = "df64"
 WORKLOAD = "wall-RPY M_UF.F, 256 shells x 42 blobs = 10,752 blobs (FP64-accurate: df64, <= 1e-12 vs FP64)"
 # Issued thread instructions per ordered pair of the df64 UF kernels (all
-# pipes, 80-85 % of them on the FMA pipe), from the ncu captures summarised in
-# profiles/wall_uf_df_sym_shells42x256.md (symmetric kernel, each unordered
-# pair once: smsp__inst_executed.sum * 32 / N^2 = 1,704,728,972 * 32 / 10752^2
-# = 471.9) and, for the one-sided kernel, a single-metric capture of one of
-# the autotuner's trial launches (split 15) of the same bench command:
-# `ncu --metrics smsp__inst_executed.sum,gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum
-# --clock-control none -k regex:wall_pair_df_kernel -s 72 -c 1 python bench.py --steps 5 --warmup 3
-# --no-extras --no-cpu-baseline`: 2,719,541,740 * 32 / 10752^2 = 752.8 (2.757 ms).  The FP32 pipe issues at most one
-# thread instruction per lane per clock, the rate the FMA-chain probe measures
-# (FLOP/s / 2), so achieved / peak is the fraction of issue capacity used.
+# pipes, 80-85 % of them on the FMA pipe), from ncu's smsp__inst_executed.sum
+# on the 10,752-blob product: symmetric kernel (each unordered pair once),
+# 1,704,728,972 warp instructions * 32 / 10752^2 = 471.9; one-sided kernel
+# (source split 15) 2,719,541,740 * 32 / 10752^2 = 752.8.  The FP32 pipe
+# issues at most one thread instruction per lane per clock, the rate the
+# FMA-chain probe measures (FLOP/s / 2), so achieved / peak is the fraction of
+# issue capacity used.  The constants hold for the kernel sources whose hash is
+# DF64_UF_KERNEL_SOURCE_SHA (tests/test_bench_constants.py fails when the
+# kernel changes without a new capture).
 DF64_UF_INST_PER_PAIR = {"symmetric": 1704728972.0 * 32 / 10752 ** 2, "standard": 2719541740.0 * 32 / 10752 ** 2}
 # dram__bytes_read.sum + dram__bytes_write.sum per launch, same captures
 DF64_UF_TRAFFIC_BYTES = {"symmetric": 735744, "standard": 718848}
+DF64_UF_KERNEL_SOURCE_SHA = "ac909a031a188da5b8c5009d4600eab52be0b7b5c98007e539c9a289bbf64246"
+
+
+def df64_uf_kernel_source_sha():
+    """SHA-256 of the sources that fix the df64 M_UF kernels' instruction stream: the device part of
+    csrc/wall_pair.cu up to the symmetric UF kernel, and the double-float headers it includes."""
+    import hashlib
+    d = os.path.join(ROOT, "rigidmultiblobswall_gb300", "csrc")
+    h = hashlib.sha256()
+    with open(os.path.join(d, "wall_pair.cu")) as fh:
+        src = fh.read()
+    beg = src.index("namespace rmw {")
+    end = src.index("// The rotation blocks (UT, WF, WT) on the same grid")
+    h.update(src[beg:end].encode())
+    for name in ("pair_math_df.cuh", "dfloat.cuh"):
+        with open(os.path.join(d, name)) as fh:
+            h.update(fh.read().encode())
+    with open(os.path.join(d, "rmw_common.cuh")) as fh:
+        src = fh.read()
+    h.update(src[src.index("// ---- compensated FP32 accumulation"):].encode())
+    return h.hexdigest()
 
 
 def parse():
@@ -204,8 +224,8 @@ def cpu_baseline(r, f, eta, a, seconds):
     med = float(np.median(times))
     return {"value": n * n / med / 1e9, "unit": "Gpairs/s", "cores": threads, "kind": "port",
             "sample": "%d full M_UF.F products at N=%d (median %.3f s each); oracle/wall_oracle.c "
-                      "oracle_wall_uf_symmetric, restating mobility/mobility.cpp:256-430 with -O3 -ffast-math "
-                      "-fopenmp" % (len(times), n, med)}
+                      "oracle_wall_uf_symmetric, restating mobility/mobility.cpp:256-430 with the reference's flags "
+                      "(-O3 -ffast-math, native CPU tuning, -fopenmp)" % (len(times), n, med)}
 
 
 def run_reference(args):
@@ -259,6 +279,86 @@ def time_product(kind, mode, rt, ft, out_fn, eta, a, steps, flush, stream):
     pair_ms, launches = _native.trace_read(0, reset=True)
     _native.trace_enable(False)
     return {"ms": ms, "gpairs": n * n / (ms * 1e-3) / 1e9, "pair_kernel_ms": pair_ms / max(launches, 1)}
+
+
+def cfg1_metrics(dev, flush, stream, cpu_seconds=2.0):
+    """The plain FP64 translational product of 2,048 free blobs (a = 0.5, eta = 1, x,y ~ U[0,64a],
+    z ~ U[1.5a,10a], forces N(0,1), seed 0): native FP64 and df64 kernels (CUDA events per product, L2
+    flushed between products), the host-buffer drop-in end to end, and the oracle's restatement of the
+    reference C++ product on all host cores, on the same inputs."""
+    import torch
+    from oracle import wall
+    from rigidmultiblobswall_gb300 import mobility as mb
+    from rigidmultiblobswall_gb300 import suspensions as S
+    r, f, eta, a = S.blobs_wall_matvec(2048, seed=0)
+    n = len(r)
+    rt = torch.tensor(r, device=dev)
+    ft = torch.tensor(f, device=dev)
+    out = {"workload": "2,048 free blobs, a = 0.5, eta = 1, x,y ~ U[0,64a], z ~ U[1.5a,10a], F ~ N(0,1), seed 0",
+           "pairs_per_product": n * n}
+    ref = wall.wall_product("uf", r, f.reshape(-1), eta, a)
+    for mode in ("fp64", "df64"):
+        mb.autotune("uf", n, mode, reps=5)
+        res = time_product("uf", mode, rt, ft, None, eta, a, 40, flush, stream)
+        u = mb.wall_product("uf", rt, ft, eta, a, mode=mode).cpu().numpy()
+        res["rel_err_vs_oracle"] = float(np.linalg.norm(u - ref) / np.linalg.norm(ref))
+        out["uf_" + mode] = res
+    rp = torch.empty(r.shape, dtype=torch.float64).pin_memory().numpy()
+    fp = torch.empty(f.shape, dtype=torch.float64).pin_memory().numpy()
+    rp[:] = r
+    fp[:] = f
+    for mode in ("fp64", "df64"):
+        mb.single_wall_mobility_trans_times_force_pycuda(rp, fp, eta, a, mode=mode)
+        ts = []
+        for _ in range(20):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            mb.single_wall_mobility_trans_times_force_pycuda(rp, fp, eta, a, mode=mode)
+            ts.append(time.perf_counter() - t0)
+        out["e2e_" + mode] = {"ms": float(np.median(ts)) * 1e3, "gpairs": n * n / float(np.median(ts)) / 1e9}
+    threads = os.cpu_count() or 1
+    wall.uf_symmetric_fast(r, f, eta, a, threads=threads)
+    ts = []
+    t_end = time.perf_counter() + cpu_seconds
+    while len(ts) < 5 or time.perf_counter() < t_end:
+        t0 = time.perf_counter()
+        wall.uf_symmetric_fast(r, f, eta, a, threads=threads)
+        ts.append(time.perf_counter() - t0)
+    med = float(np.median(ts))
+    out["cpu_port"] = {"ms": med * 1e3, "gpairs": n * n / med / 1e9, "cores": threads, "products_timed": len(ts)}
+    for mode in ("fp64", "df64"):
+        out["speedup_e2e_%s_vs_cpu_port" % mode] = out["cpu_port"]["ms"] / out["e2e_" + mode]["ms"]
+    return out
+
+
+def solve_breakdown(fn):
+    """Run fn() (one solve) with tracing on and split its device time by class: whole solve (first to last
+    launch, host gaps included), preconditioner build, Krylov operator applications (A P^-1 as graph
+    replays), Krylov vector work, refinement residuals; the rest is small kernels and host round trips."""
+    from rigidmultiblobswall_gb300 import _native
+    names = {1: "krylov_vector_ms", 3: "operator_ms", 4: "refine_residual_ms", 5: "pc_build_ms", 6: "solve_ms"}
+    _native.trace_enable(True)
+    for k in range(7):
+        _native.trace_read(k, reset=True)
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = fn()
+    torch.cuda.synchronize()
+    wall_ms = (time.perf_counter() - t0) * 1e3
+    out = {"wall_ms": wall_ms}
+    for k, nm in names.items():
+        ms, cnt = _native.trace_read(k, reset=True)
+        out[nm] = ms
+        out[nm.replace("_ms", "_count")] = cnt
+    for k in (0, 2):
+        _native.trace_read(k, reset=True)
+    _native.trace_bytes(1, reset=True)
+    _native.trace_enable(False)
+    out["other_in_solve_ms"] = out["solve_ms"] - out["operator_ms"] - out["krylov_vector_ms"] - \
+        out["refine_residual_ms"]
+    out["outside_solve_ms"] = wall_ms - out["solve_ms"] - out["pc_build_ms"]
+    return res, out
 
 
 def train_nearfield(shell, a, z_range, dev, n_samples=2048, steps=2000, seed=11):
@@ -343,6 +443,12 @@ def solver_metrics(dev, reps=2):
         sols[mode + "_nf"] = sol[3 * sys2.n_blobs:].cpu().numpy()
         out["solve_shells42x256_%s_nearfield" % mode] = {"ms": best * 1e3, "iterations": its, "relres_fp64": rr,
                                                           "info": info, "pairs_exact_learned": list(pairs)}
+    # where the mixed solve's time goes (PC build + solve, traced by class)
+    def _mixed():
+        sys2.build_pc(mode="mixed")
+        return integrator.solve_mobility_problem(sys2, FT, tol=1e-8, mode="mixed")
+    _mixed()
+    _, out["solve_shells42x256_mixed_breakdown"] = solve_breakdown(_mixed)
     # bandwidth of the Arnoldi vector work (33,792-long vectors: the basis stays in L2)
     sys2.build_pc()
     _, out["solve_shells42x256_mixed_arnoldi"] = arnoldi_traffic(
@@ -672,7 +778,11 @@ def main():
                 "peak_source": "measured by rmw_fma_peak (FP32 FMA chains on all SMs) in this run, / 2 per FFMA",
                 "pair_kernel_ms": pair_ms, "issued_inst_per_ordered_pair": ipp,
                 "algorithmic_tflops_fp64_equivalent": alg_tflops, "flops_per_pair": FLOPS_PER_PAIR["uf"],
-                "algorithmic_vs_measured_fp64_peak": alg_tflops / (peak64 / 1e12)}
+                "algorithmic_vs_measured_fp64_peak": alg_tflops / (peak64 / 1e12),
+                # the reference's flops per pair (FP64 operations counted from its source) executed per
+                # second, over the FP32 FMA peak of the pipe the df64 arithmetic runs on
+                "algorithmic_frac_of_fp32_peak": alg_tflops / (peak32 / 1e12),
+                "constants_source_sha256": DF64_UF_KERNEL_SOURCE_SHA}
 
     # ---- e2e through the public host-buffer API (copies inside the timed region)
     rp = torch.empty(r.shape, dtype=torch.float64).pin_memory().numpy()
@@ -783,6 +893,7 @@ def main():
                 products["no_wall_%s_%s" % (kind, mode)] = {"ms": round(ms, 6),
                                                             "gpairs": round(n * n / (ms * 1e-3) / 1e9, 3)}
 
+    cfg1 = None if args.no_extras else cfg1_metrics(dev, flush, stream)
     solver = {} if args.no_extras else solver_metrics(dev)
     if not args.no_extras:
         solver["batched_64_suspensions"] = batched_metrics(dev)
@@ -805,7 +916,7 @@ def main():
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
                 "gpu_launches": 3 * args.steps, "wall_s_timed_region": t_wall,
                 "fp32_fma_peak_tflops": peak32 / 1e12, "fp64_fma_peak_tflops": peak64 / 1e12,
-                "products": products, "solver": solver}
+                "cfg1_plain_matvec_2048": cfg1, "products": products, "solver": solver}
         print(json.dumps(line))
     if ws > 1:
         dist.destroy_process_group()

@@ -413,6 +413,22 @@ int rmw_lanczos(int64_t n, rmw_operator_fn op, void *op_ctx, const double *z, do
 int rmw_wall_product_noalloc(int kind, const double *r, const double *v, double *out, int64_t n, double eta,
                              double a, const double *L_host, int mode, void *stream);
 
+/* Scratch memory (library-only, no reference counterpart).  Products keep
+ * their packed sources and partial sums in a device buffer per (device,
+ * stream, purpose) that grows on demand and is kept until process exit or
+ * rmw_release_scratch, so a process holds at most a few such buffers per
+ * stream it calls the library on.  The symmetric pair kernels need
+ * ceil(n/128) * 3n doubles of partial sums (21.7 MB at 10,752 blobs, 5.5 GB at
+ * 172,032); buffers of 1 GiB and more are allocated without headroom.
+ * rmw_set_scratch_limit caps one buffer at `bytes` (0 = no cap): a product
+ * whose symmetric partial sums would exceed it runs the one-sided kernels,
+ * whose scratch is a few hundred bytes per blob, and a request still above the
+ * cap returns RMW_ERR_ALLOC.  rmw_release_scratch frees the current device's
+ * buffers (after the device is idle); buffers a live CUDA graph may use are
+ * freed when the last graph is destroyed. */
+int rmw_set_scratch_limit(int64_t bytes);
+int rmw_release_scratch(void);
+
 /* Measured FMA-pipe throughput of the current device (FLOP/s, FMA = 2 flops)
  * for FP64 (fp64 != 0) or FP32: the denominator of the pair kernels' roofline
  * fraction.  Synchronous.  Library-only (no reference counterpart). */
@@ -421,9 +437,13 @@ int rmw_fma_peak(int fp64, double *flops_per_s_host, void *stream);
 /* Kernel tracing (library-only, no reference counterpart; the reference's
  * only profiling is the wall-clock utils.timer, general_application_utils.py:486-511).
  * While enabled, each launch of a traced kernel is bracketed by CUDA events on
- * its launching stream.  rmw_trace_read sums the durations of one kernel class
- * (0 = pair kernel, 1 = Krylov vector kernels, 2 = preconditioner) and
- * optionally clears the records.  rmw_trace_read synchronises the events. */
+ * its launching stream.  rmw_trace_read sums the durations of one class
+ * (0 = pair kernel, 1 = Krylov vector work, 2 = preconditioner apply - these
+ * three for direct launches only -, 3 = one Krylov operator application
+ * A P^-1 or the Lanczos operator, graph replay or direct, 4 = a mixed solve's
+ * refinement residual, 5 = preconditioner build, 6 = whole solve calls, host
+ * gaps included) and optionally clears that class's records.  rmw_trace_read
+ * synchronises the events. */
 int rmw_trace_enable(int on);
 int rmw_trace_read(int kind, double *total_ms_host, int64_t *launches_host, int reset);
 /* Algorithmic bytes the traced work of one class moved while tracing was on

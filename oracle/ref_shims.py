@@ -26,10 +26,14 @@ import os
 import sys
 import types
 
-REFERENCE_ROOT = os.environ.get("RMW_REFERENCE_ROOT", "/root/reference")
+# The checkout is named by the environment (RMW_REFERENCE_ROOT); without it the
+# reference counts as absent and nothing here imports it.
+REFERENCE_ROOT = os.environ.get("RMW_REFERENCE_ROOT", "")
 
 
 def reference_available():
+    if not REFERENCE_ROOT:
+        return False
     return os.path.isfile(os.path.join(REFERENCE_ROOT, "mobility", "mobility_numba.py"))
 
 
@@ -91,7 +95,8 @@ def _install_shims():
 
 def _prepare():
     if not reference_available():
-        raise RuntimeError("reference checkout not found at " + REFERENCE_ROOT)
+        raise RuntimeError("reference checkout not found: set RMW_REFERENCE_ROOT to a RigidMultiblobsWall "
+                           "checkout (found %r)" % REFERENCE_ROOT)
     # The reference tree is read-only: never write bytecode caches into it.
     sys.dont_write_bytecode = True
     _install_shims()

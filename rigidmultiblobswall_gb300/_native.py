@@ -106,6 +106,8 @@ SIGNATURES = {
     "rmw_lanczos": (_i, [_i64, _vp, _vp, _vp, _vp, _d, _d, _i, _vp, ctypes.POINTER(ctypes.c_int)]),
     "rmw_wall_product_noalloc": (_i, [_i, _vp, _vp, _vp, _i64, _d, _d, _vp, _i, _vp]),
     "rmw_fma_peak": (_i, [_i, ctypes.POINTER(ctypes.c_double), _vp]),
+    "rmw_set_scratch_limit": (_i, [_i64]),
+    "rmw_release_scratch": (_i, []),
     "rmw_trace_enable": (_i, [_i]),
     "rmw_trace_read": (_i, [_i, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64), _i]),
 }
@@ -175,6 +177,16 @@ def check(rc):
 
 def call(name, *args):
     return check(getattr(load(), name)(*args))
+
+
+def set_scratch_limit(nbytes):
+    """Cap one library scratch buffer at nbytes (0 = no cap); symmetric products fall back to one-sided."""
+    call("rmw_set_scratch_limit", int(nbytes))
+
+
+def release_scratch():
+    """Free the current device's library scratch buffers."""
+    call("rmw_release_scratch")
 
 
 def use_graphs(on=True):

@@ -116,14 +116,22 @@ int rmw_wall_autotune(int kind, int mode, int64_t n, int reps, void *stream, int
     const int cmax = std::max(*std::max_element(cand.begin(), cand.end()), try_sym ? rmw::wall_sym_slots(N) : 1);
     const size_t vec = sizeof(double) * 3 * (size_t)N;
     const size_t ws_bytes = rmw::wall_scratch_bytes(N, mode, cmax);
+    // events first: nothing to release if their creation fails
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    RMW_CUDA(cudaEventCreate(&e0));
+    if (cudaError_t e = cudaEventCreate(&e1)) {
+        cudaEventDestroy(e0);
+        return rmw::cuda_fail(e, "cudaEventCreate");
+    }
     char *buf = nullptr;
-    RMW_CUDA(cudaMallocAsync((void **)&buf, 3 * vec + ws_bytes + 256, st));
+    if (cudaError_t e = cudaMallocAsync((void **)&buf, 3 * vec + ws_bytes + 256, st)) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return rmw::cuda_fail(e, "cudaMallocAsync (autotune buffers)");
+    }
     double *r = (double *)buf, *v = (double *)(buf + vec), *out = (double *)(buf + 2 * vec);
     void *ws = (void *)(((uintptr_t)(buf + 3 * vec) + 255) & ~(uintptr_t)255);
     rmw::synth_blobs_kernel<<<(N + 255) / 256, 256, 0, st>>>(r, v, N, 1.0, 0x5EEDULL);
-    cudaEvent_t e0, e1;
-    RMW_CUDA(cudaEventCreate(&e0));
-    RMW_CUDA(cudaEventCreate(&e1));
     int rc = RMW_OK, best = def;
     float tbest = 0.f, tdef = 0.f;
     auto run = [&](int c) {

@@ -328,7 +328,12 @@ static int gmres_right(Op op, Pc pc, PcOp pcop, const double *b, double *x_out, 
         for (int j = 0; j < restart; ++j) {
             double *Vj = K.V + (long long)j * ldv;
             double *Vn = K.V + (long long)(j + 1) * ldv;
-            if (int rc = pcop(Vj, K.w)) return rc;
+            {
+                void *otok = nullptr;
+                if (int rc = trace_begin(TRACE_OPERATOR, st, &otok)) return rc;
+                if (int rc = pcop(Vj, K.w)) return rc;
+                if (int rc = trace_end(otok, st)) return rc;
+            }
             // CGS2 against V_0..V_j; algorithmic bytes: 2 x (dots (j+2) n + update (j+3) n) + scale 2 n
             void *tok = nullptr;
             if (int rc = trace_begin(TRACE_KRYLOV, st, &tok)) return rc;
@@ -497,7 +502,12 @@ static int lanczos(Op op, const double *z, double *noise, long long n, double fa
     bool done = false;
     for (int i = 0; i <= max_iter && i < kcap; ++i) {
         double *Vi = K.V + (long long)i * ldv;
-        if (int rc = op(Vi, K.w)) return rc;
+        {
+            void *otok = nullptr;
+            if (int rc = trace_begin(TRACE_OPERATOR, st, &otok)) return rc;
+            if (int rc = op(Vi, K.w)) return rc;
+            if (int rc = trace_end(otok, st)) return rc;
+        }
         // w -= hs[i-1] V_{i-1}; hd[i] = <w, V_i>; w -= hd[i] V_i; hs[i] = |w|
         if (i > 0) {
             const double a = -hs[i - 1];
@@ -576,8 +586,23 @@ using rmw::RigidSystem;
 
 extern "C" {
 
+static int rigid_solve_impl(void *sys, const double *rhs, double *sol, double tol, int restart, int maxiter,
+                            int mode, int *iters_host, double *relres_host);
+
 int rmw_rigid_solve(void *sys, const double *rhs, double *sol, double tol, int restart, int maxiter, int mode,
                     int *iters_host, double *relres_host)
+{
+    if (!sys) return rmw::fail(RMW_ERR_ARG, "null argument");
+    RigidSystem &S = *(RigidSystem *)sys;
+    void *tok = nullptr;
+    if (int rc = rmw::trace_begin(rmw::TRACE_SOLVE, S.st, &tok)) return rc;
+    const int rc = rigid_solve_impl(sys, rhs, sol, tol, restart, maxiter, mode, iters_host, relres_host);
+    if (int rc2 = rmw::trace_end(tok, S.st)) return rc2;
+    return rc;
+}
+
+static int rigid_solve_impl(void *sys, const double *rhs, double *sol, double tol, int restart, int maxiter,
+                            int mode, int *iters_host, double *relres_host)
 {
     if (!sys || !rhs || !sol) return rmw::fail(RMW_ERR_ARG, "null argument");
     if (!(tol > 0)) return rmw::fail(RMW_ERR_ARG, "tolerance must be positive");
@@ -661,6 +686,8 @@ int rmw_rigid_solve(void *sys, const double *rhs, double *sol, double tol, int r
         total += it;
         if (rc != RMW_OK && rc != RMW_ERR_NOT_CONVERGED) return rc;
         rmw::axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S.st>>>(d, x, n, 1.0, 1.0);
+        void *rtok = nullptr;
+        if (int rc2 = rmw::trace_begin(rmw::TRACE_REFINE, S.st, &rtok)) return rc2;
         if (rmw::refine_by_recurrence(relres, tol)) {
             // r = r - A32 d
             if (int rc2 = rmw::rigid_apply(S, d, ad, RMW_MODE_MIXED)) return rc2;
@@ -670,6 +697,7 @@ int rmw_rigid_solve(void *sys, const double *rhs, double *sol, double tol, int r
             if (int rc2 = rmw::rigid_apply(S, x, r, RMW_MODE_DF64)) return rc2;
             rmw::axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S.st>>>(rhs, r, n, 1.0, -1.0);
         }
+        if (int rc2 = rmw::trace_end(rtok, S.st)) return rc2;
         if (total >= maxiter) {
             if (int rc3 = norm(r, &rnorm)) return rc3;
             relres = rnorm / bnorm;

@@ -281,14 +281,24 @@ int nowall_product(int kind, const double *r, const double *v, double *out, int6
     const bool per = L && (L[0] > 0 || L[1] > 0 || L[2] > 0);
     // the symmetric kernel (each unordered pair once, both ways) from 4,096 blobs
     // in FP64 and df64 and 8,192 in mixed, as the wall products' untuned rule
-    const bool sym = !per && N >= (mode == RMW_MODE_MIXED ? 8192 : 4096) &&
-                     wall_sym_applicable(kind, mode, N, nullptr);
-    const int nchunks = sym ? wall_sym_slots(N) : wall_default_chunks(N);
+    bool sym = !per && N >= (mode == RMW_MODE_MIXED ? 8192 : 4096) &&
+               wall_sym_applicable(kind, mode, N, nullptr);
+    int nchunks = sym ? wall_sym_slots(N) : wall_default_chunks(N);
     const size_t rec = (mode == RMW_MODE_FP64) ? sizeof(NwSrcD) : (mode == RMW_MODE_DF64 ? sizeof(NwSrcDF)
                                                                                           : sizeof(NwSrcF));
     const size_t packed = ((rec * (size_t)N + 255) / 256) * 256;
     void *ws = nullptr;
-    if (int rc = scratch(SCRATCH_PAIR, packed + sizeof(double) * 3 * (size_t)N * nchunks, &ws, st)) return rc;
+    int src = scratch(SCRATCH_PAIR, packed + sizeof(double) * 3 * (size_t)N * nchunks, &ws, st);
+    if (src && sym) {
+        // the symmetric partial sums did not fit next to the caller's
+        // allocations (or above rmw_set_scratch_limit): the one-sided kernels
+        // need far less scratch
+        cudaGetLastError();
+        sym = false;
+        nchunks = wall_default_chunks(N);
+        src = scratch(SCRATCH_PAIR, packed + sizeof(double) * 3 * (size_t)N * nchunks, &ws, st);
+    }
+    if (src) return src;
     double *partial = (double *)((char *)ws + packed);
     const double inva = 1.0 / a;
     const int pb = 256, pg = (N + pb - 1) / pb;

@@ -787,7 +787,12 @@ int rmw_rigid_build_pc_mode(void *sys, int stochastic, int mode)
     if (!sys) return rmw::fail(RMW_ERR_ARG, "null handle");
     if (mode != RMW_MODE_FP64 && mode != RMW_MODE_MIXED && mode != RMW_MODE_DF64)
         return rmw::fail(RMW_ERR_ARG, "unknown precision mode");
-    return rmw::build_pc(*(RigidSystem *)sys, stochastic != 0, mode == RMW_MODE_MIXED);
+    RigidSystem &S = *(RigidSystem *)sys;
+    void *tok = nullptr;
+    if (int rc = rmw::trace_begin(rmw::TRACE_PCBUILD, S.st, &tok)) return rc;
+    const int rc = rmw::build_pc(S, stochastic != 0, mode == RMW_MODE_MIXED);
+    if (int rc2 = rmw::trace_end(tok, S.st)) return rc2;
+    return rc;
 }
 
 int rmw_rigid_apply(void *sys, const double *x, double *y, int mode)

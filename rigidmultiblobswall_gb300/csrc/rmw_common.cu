@@ -60,10 +60,17 @@ void graph_live(int delta)
     if (!release.empty()) cudaSetDevice(cur);
 }
 
+// cap on one scratch buffer (rmw_set_scratch_limit); 0 = no cap
+static std::atomic<size_t> g_scratch_limit{0};
+
 int scratch(ScratchSlot slot, size_t bytes, void **ptr, cudaStream_t st)
 {
     int dev = 0;
     RMW_CUDA(cudaGetDevice(&dev));
+    const size_t cap = g_scratch_limit.load();
+    if (cap && bytes > cap)
+        return fail(RMW_ERR_ALLOC, "scratch request of " + std::to_string(bytes) + " bytes is above the limit of " +
+                                       std::to_string(cap) + " bytes set by rmw_set_scratch_limit");
     std::lock_guard<std::mutex> lock(g_scratch_mu);
     ScratchBuf &b = g_scratch[std::make_tuple(dev, (void *)st, (int)slot)];
     if (b.bytes < bytes) {
@@ -77,13 +84,39 @@ int scratch(ScratchSlot slot, size_t bytes, void **ptr, cudaStream_t st)
             b.ptr = nullptr;
             b.bytes = 0;
         }
-        size_t want = bytes + bytes / 4 + 4096;  // headroom so that slowly growing sizes reallocate rarely
+        // headroom so that slowly growing sizes reallocate rarely (none above 1 GiB, and never past the cap)
+        size_t want = bytes + (bytes >= ((size_t)1 << 30) ? 0 : bytes / 4) + 4096;
+        if (cap && want > cap) want = bytes;
         RMW_CUDA(cudaMalloc(&b.ptr, want));
         b.bytes = want;
     }
     *ptr = b.ptr;
     return RMW_OK;
 }
+
+// Frees every scratch buffer of the current device that no live graph may use.
+int scratch_release_all()
+{
+    int dev = 0;
+    RMW_CUDA(cudaGetDevice(&dev));
+    std::vector<void *> release;
+    {
+        std::lock_guard<std::mutex> lock(g_scratch_mu);
+        for (auto it = g_scratch.begin(); it != g_scratch.end();) {
+            if (std::get<0>(it->first) == dev && it->second.ptr) {
+                if (g_live_graphs > 0) g_deferred.push_back({dev, it->second.ptr});
+                else release.push_back(it->second.ptr);
+                it = g_scratch.erase(it);
+            } else {
+                ++it;
+            }
+        }
+    }
+    for (void *p : release) RMW_CUDA(cudaFree(p));
+    return RMW_OK;
+}
+
+void scratch_set_limit(size_t bytes) { g_scratch_limit.store(bytes); }
 
 // ---- tracing ---------------------------------------------------------------
 namespace {
@@ -133,7 +166,7 @@ int trace_begin(TraceKernel k, cudaStream_t st, void **token)
     return RMW_OK;
 }
 
-static double g_trace_byte_count[TRACE_KINDS] = {0.0, 0.0, 0.0};
+static double g_trace_byte_count[TRACE_KINDS] = {};
 
 void trace_bytes(TraceKernel k, double bytes)
 {
@@ -199,6 +232,15 @@ int rmw_graph_stats(int64_t *captures_host, int64_t *replays_host, int reset)
     return RMW_OK;
 }
 
+int rmw_set_scratch_limit(int64_t bytes)
+{
+    if (bytes < 0) return rmw::fail(RMW_ERR_ARG, "scratch limit must be >= 0");
+    rmw::scratch_set_limit((size_t)bytes);
+    return RMW_OK;
+}
+
+int rmw_release_scratch(void) { return rmw::scratch_release_all(); }
+
 int rmw_trace_enable(int on)
 {
     std::lock_guard<std::mutex> lock(rmw::g_trace_mu);
@@ -209,6 +251,7 @@ int rmw_trace_enable(int on)
 int rmw_trace_read(int kind, double *total_ms_host, int64_t *launches_host, int reset)
 {
     if (!total_ms_host || !launches_host) return rmw::fail(RMW_ERR_ARG, "null output pointer");
+    if (kind < 0 || kind >= rmw::TRACE_KINDS) return rmw::fail(RMW_ERR_ARG, "bad trace kind");
     std::lock_guard<std::mutex> lock(rmw::g_trace_mu);
     double tot = 0.0;
     int64_t cnt = 0;
@@ -223,11 +266,17 @@ int rmw_trace_read(int kind, double *total_ms_host, int64_t *launches_host, int 
     *total_ms_host = tot;
     *launches_host = cnt;
     if (reset) {
+        // only this class's records: the others stay readable
+        std::vector<rmw::TraceRec> keep;
         for (auto &r : rmw::g_trace_recs) {
-            rmw::g_event_pool.push_back(r.e0);
-            rmw::g_event_pool.push_back(r.e1);
+            if (r.kind == kind) {
+                rmw::g_event_pool.push_back(r.e0);
+                rmw::g_event_pool.push_back(r.e1);
+            } else {
+                keep.push_back(r);
+            }
         }
-        rmw::g_trace_recs.clear();
+        rmw::g_trace_recs.swap(keep);
     }
     return RMW_OK;
 }

@@ -32,13 +32,32 @@ int cuda_fail(cudaError_t e, const char *where);
 // kernel still reads it) and allocates anew.
 enum ScratchSlot { SCRATCH_PAIR = 0, SCRATCH_HOST_STAGING = 1, SCRATCH_FT_TERM = 2, SCRATCH_SLOTS = 3 };
 int scratch(ScratchSlot slot, size_t bytes, void **ptr, cudaStream_t st);
+// frees the current device's scratch buffers (deferred while graphs are alive)
+int scratch_release_all();
+// requests above `bytes` fail with RMW_ERR_ALLOC without touching the device (0 = no cap)
+void scratch_set_limit(size_t bytes);
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // ---- kernel tracing -------------------------------------------------------
 // When enabled (rmw_trace_enable), launchers bracket their dominant kernel with
 // CUDA events on the launching stream; rmw_trace_read sums the durations.
-enum TraceKernel { TRACE_PAIR = 0, TRACE_KRYLOV = 1, TRACE_PC = 2, TRACE_KINDS = 3 };
+// Classes: the pair kernel, the Krylov vector work, the preconditioner apply
+// (direct launches; work replayed inside a CUDA graph is timed by the class of
+// the graph launch), one Krylov operator application (A P^-1, the Lanczos
+// operator: graph replay or direct launches), a mixed solve's refinement
+// residual, the preconditioner build, and whole solves (first to last launch,
+// host gaps included).
+enum TraceKernel {
+    TRACE_PAIR = 0,
+    TRACE_KRYLOV = 1,
+    TRACE_PC = 2,
+    TRACE_OPERATOR = 3,
+    TRACE_REFINE = 4,
+    TRACE_PCBUILD = 5,
+    TRACE_SOLVE = 6,
+    TRACE_KINDS = 7
+};
 bool trace_on();
 int trace_begin(TraceKernel k, cudaStream_t st, void **token);
 int trace_end(void *token, cudaStream_t st);

@@ -566,9 +566,15 @@ int wall_force_torque(const double *r, const double *F, const double *T, double 
         const int nt = (N + kFtSymTile - 1) / kFtSymTile;
         const size_t packed = ((sizeof(FtSrcF) * (size_t)N + 255) / 256) * 256;
         const size_t part = sizeof(double) * 6 * (size_t)N * (size_t)nt;
-        if (part <= wall_sym_partial_budget()) {
-            void *ws = nullptr;
-            if (int rc = scratch(SCRATCH_PAIR, packed + part, &ws, st)) return rc;
+        void *ws = nullptr;
+        // the partial sums may not fit next to the caller's allocations (or
+        // above rmw_set_scratch_limit): then the one-sided pass below, whose
+        // scratch is far smaller, does the product
+        if (part <= wall_sym_partial_budget() && scratch(SCRATCH_PAIR, packed + part, &ws, st) != RMW_OK) {
+            cudaGetLastError();
+            ws = nullptr;
+        }
+        if (ws) {
             double *partial = (double *)((char *)ws + packed);
             const int pb = 256, pg = (N + pb - 1) / pb;
             ft_pack_mixed_kernel<<<pg, pb, 0, st>>>(r, F, T, (FtSrcF *)ws, N, a);

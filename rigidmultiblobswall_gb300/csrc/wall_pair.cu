@@ -26,6 +26,7 @@
 //                 result is deterministic), adds the FP64 self term, applies
 //                 b_i and the 1/(8 pi eta a^p) factor.
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <mutex>
 #include <vector>
@@ -1166,16 +1167,19 @@ int wall_product_with_scratch(int kind, const double *r, const double *v, double
 
 size_t wall_sym_partial_budget()
 {
-    static size_t budget[64] = {0};
+    // per device, computed once; atomics because several host threads may ask at once
+    static std::atomic<size_t> budget[64];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return kSymMaxPartialBytes;
-    if (!budget[dev]) {
+    size_t b = budget[dev].load();
+    if (!b) {
         size_t total = 0;
         cudaDeviceProp prop;
         if (cudaGetDeviceProperties(&prop, dev) == cudaSuccess) total = prop.totalGlobalMem;
-        budget[dev] = std::max(kSymMaxPartialBytes, total / 8);
+        b = std::max(kSymMaxPartialBytes, total / 8);
+        budget[dev].store(b);
     }
-    return budget[dev];
+    return b;
 }
 
 bool wall_sym_applicable(int kind, int mode, int n, const double *L)

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this folder from the reference's own FP64 code.
 
-Runs only where a RigidMultiblobsWall checkout is available (default
-/root/reference, override with RMW_REFERENCE_ROOT); it imports the reference's
+Runs only where a RigidMultiblobsWall checkout is available, named by the
+environment variable RMW_REFERENCE_ROOT; it imports the reference's
 Python read-only through ``oracle/ref_shims.py`` (numba source run as plain
 Python, no fastmath).  The fixtures it writes are small ``.npz`` files that the
 tests load on any machine:

@@ -217,6 +217,15 @@ int rmw_wall_autotune_clear(void);
  * as plain launches.  Stats: graphs captured and replayed since the last
  * reset. */
 int rmw_use_graphs(int on);
+/* Device-resident GMRES (no reference counterpart; the reference's GMRES is
+ * scipy's host loop, general_application_utils.py:514-635): the rigid solves
+ * (rmw_rigid_solve, rmw_rigid_solve_batched) run each restart cycle on the
+ * device - operator applications and a fused cooperative Arnoldi step kernel
+ * (CGS2, Givens rotations, stopping test) repeated by a CUDA graph while node,
+ * one host round trip per cycle.  on = 0 selects the host-driven loop (one
+ * round trip per Arnoldi step).  Default on; devices without cooperative
+ * launches use the host-driven loop. */
+int rmw_use_device_krylov(int on);
 int rmw_graph_stats(int64_t *captures_host, int64_t *replays_host, int reset);
 
 /* ---- rigid multiblob bodies ------------------------------------------

@@ -65,6 +65,7 @@ SIGNATURES = {
     "rmw_wall_autotune_clear": (_i, []),
     "rmw_wall_autotune_set": (_i, [_i, _i, _i64, _i]),
     "rmw_use_graphs": (_i, [_i]),
+    "rmw_use_device_krylov": (_i, [_i]),
     "rmw_trace_bytes": (_i, [_i, _vp, _i]),
     "rmw_graph_stats": (_i, [_vp, _vp, _i]),
     "rmw_rigid_create": (_i, [ctypes.POINTER(ctypes.c_void_p), _i64, _vp, _d, _d, _vp, _vp]),
@@ -192,6 +193,11 @@ def release_scratch():
 def use_graphs(on=True):
     """Replay the solvers' per-iteration operators as CUDA graphs (default on)."""
     call("rmw_use_graphs", 1 if on else 0)
+
+
+def use_device_krylov(on=True):
+    """Run the rigid solves' GMRES restart cycles on the device (default on) or host-driven."""
+    call("rmw_use_device_krylov", 1 if on else 0)
 
 
 def graph_stats(reset=False):

@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "graph_op.cuh"
+#include "krylov_device.cuh"
 #include "rigid.cuh"
 #include "wall_pair.cuh"
 
@@ -631,10 +632,34 @@ static int rigid_solve_impl(void *sys, const double *rhs, double *sol, double to
     };
     auto gop = rmw::make_graph_op(fused(mode == RMW_MODE_MIXED ? RMW_MODE_MIXED : mode), &S.st, n, n);
     auto pcop = [&](const double *x, double *y) -> int { return gop(x, y); };
+    // device-resident restart cycles (fused CGS2 + Givens step kernel, one
+    // graph launch per cycle) unless switched off or unavailable
+    const bool dev = rmw::krylov_device_enabled() && rmw::krylov_device_available();
+    auto fop = fused(mode == RMW_MODE_MIXED ? RMW_MODE_MIXED : mode);
+    rmw::GmresDevice<decltype(fop)> E(fop, &S.st);
+    if (dev) {
+        if (int rc = E.init({0, n}, restart, 0)) return rc;
+    }
+    // one GMRES solve of A x = b to tol (x from 0) on operator A = opA
+    auto gmres = [&](auto opA, const double *b, double *x, double tl, int mi, int *it, double *rr) -> int {
+        if (!dev) return rmw::gmres_right(opA, pc, pcop, b, x, n, tl, restart, mi, S.st, it, rr, nullptr);
+        std::vector<int> its, stt;
+        std::vector<double> rrs;
+        if (int rc = E.solve(opA, pc, b, x, {tl}, mi, its, rrs, stt)) return rc;
+        *it = its[0];
+        *rr = rrs[0];
+        if (stt[0] == RMW_ERR_NOT_CONVERGED) rmw::set_error("GMRES reached maxiter without converging");
+        if (stt[0] == RMW_ERR_BREAKDOWN) rmw::set_error("GMRES breakdown");
+        return stt[0];
+    };
     if (mode == RMW_MODE_FP64 || mode == RMW_MODE_DF64) {
         auto op = [&](const double *x, double *y) { return rmw::rigid_apply(S, x, y, mode); };
-        return rmw::gmres_right(op, pc, pcop, rhs, sol, n, tol, restart, maxiter, S.st, iters_host, relres_host,
-                                nullptr);
+        int it = 0;
+        double rr = 0.0;
+        const int rc = gmres(op, rhs, sol, tol, maxiter, &it, &rr);
+        if (iters_host) *iters_host = it;
+        if (relres_host) *relres_host = rr;
+        return rc;
     }
     // mixed: inner GMRES on the FP32-pair operator; the refinement residual
     // b - A x uses the FP64-accurate double-float operator (<= 1e-12 against
@@ -681,8 +706,7 @@ static int rigid_solve_impl(void *sys, const double *rhs, double *sol, double to
         const double itol = std::max(inner_tol, 0.5 * tol * bnorm / rnorm);
         int it = 0;
         double rr = 0.0;
-        int rc = rmw::gmres_right(op32, pc, pcop, r, d, n, itol, restart, std::max(1, maxiter - total), S.st, &it,
-                                  &rr, nullptr);
+        int rc = gmres(op32, r, d, itol, std::max(1, maxiter - total), &it, &rr);
         total += it;
         if (rc != RMW_OK && rc != RMW_ERR_NOT_CONVERGED) return rc;
         rmw::axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S.st>>>(d, x, n, 1.0, 1.0);

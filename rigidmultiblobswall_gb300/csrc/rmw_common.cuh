@@ -46,8 +46,9 @@ inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s
 // (direct launches; work replayed inside a CUDA graph is timed by the class of
 // the graph launch), one Krylov operator application (A P^-1, the Lanczos
 // operator: graph replay or direct launches), a mixed solve's refinement
-// residual, the preconditioner build, and whole solves (first to last launch,
-// host gaps included).
+// residual, the preconditioner build, whole solves (first to last launch,
+// host gaps included), and device-resident GMRES restart cycles (one graph
+// launch: every operator application and fused Arnoldi step of the cycle).
 enum TraceKernel {
     TRACE_PAIR = 0,
     TRACE_KRYLOV = 1,
@@ -56,7 +57,8 @@ enum TraceKernel {
     TRACE_REFINE = 4,
     TRACE_PCBUILD = 5,
     TRACE_SOLVE = 6,
-    TRACE_KINDS = 7
+    TRACE_CYCLE = 7,
+    TRACE_KINDS = 8
 };
 bool trace_on();
 int trace_begin(TraceKernel k, cudaStream_t st, void **token);

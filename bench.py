@@ -333,12 +333,15 @@ def cfg1_metrics(dev, flush, stream, cpu_seconds=2.0):
 
 def solve_breakdown(fn):
     """Run fn() (one solve) with tracing on and split its device time by class: whole solve (first to last
-    launch, host gaps included), preconditioner build, Krylov operator applications (A P^-1 as graph
-    replays), Krylov vector work, refinement residuals; the rest is small kernels and host round trips."""
+    launch, host gaps included), preconditioner build, device-resident GMRES restart cycles (one graph
+    launch each: operator applications and fused Arnoldi steps), or, host-driven, the operator applications
+    (A P^-1 as graph replays) and Krylov vector work; refinement residuals; the rest is small kernels and
+    host round trips."""
     from rigidmultiblobswall_gb300 import _native
-    names = {1: "krylov_vector_ms", 3: "operator_ms", 4: "refine_residual_ms", 5: "pc_build_ms", 6: "solve_ms"}
+    names = {1: "krylov_vector_ms", 3: "operator_ms", 4: "refine_residual_ms", 5: "pc_build_ms", 6: "solve_ms",
+             7: "device_cycle_ms"}
     _native.trace_enable(True)
-    for k in range(7):
+    for k in range(8):
         _native.trace_read(k, reset=True)
     import torch
     torch.cuda.synchronize()
@@ -356,7 +359,7 @@ def solve_breakdown(fn):
     _native.trace_bytes(1, reset=True)
     _native.trace_enable(False)
     out["other_in_solve_ms"] = out["solve_ms"] - out["operator_ms"] - out["krylov_vector_ms"] - \
-        out["refine_residual_ms"]
+        out["refine_residual_ms"] - out["device_cycle_ms"]
     out["outside_solve_ms"] = wall_ms - out["solve_ms"] - out["pc_build_ms"]
     return res, out
 

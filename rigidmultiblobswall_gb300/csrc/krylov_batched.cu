@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "graph_op.cuh"
+#include "krylov_device.cuh"
 #include "rigid.cuh"
 #include "wall_pair.cuh"
 
@@ -666,14 +667,29 @@ int rmw_rigid_solve_batched(void *sys, const double *rhs, double *sol, double to
     };
     auto gop = rmw::make_graph_op(pcop_mode(mode == RMW_MODE_MIXED ? RMW_MODE_MIXED : mode), &S.st, n, n);
     auto pcop = [&](const double *xi, double *yi) -> int { return gop(xi, yi); };
+    // device-resident restart cycles over all suspensions (one segment each)
+    // unless switched off or unavailable
+    const bool dev = rmw::krylov_device_enabled() && rmw::krylov_device_available();
+    auto fop = pcop_mode(mode == RMW_MODE_MIXED ? RMW_MODE_MIXED : mode);
+    rmw::GmresDevice<decltype(fop)> E(fop, &S.st);
+    if (dev) {
+        if (int rc0 = E.init(S.susp_off, std::min(restart, 60), 0)) {
+            cudaFreeAsync(buf, st);
+            return rc0;
+        }
+    }
+    auto batched = [&](auto opA, const double *b, double *x, const std::vector<double> &tl, int mi,
+                       std::vector<int> &its, std::vector<double> &rrs, std::vector<int> &sts) -> int {
+        if (!dev) return rmw::gmres_batched(opA, pc, pcop, b, x, S.susp_off, tl, restart, mi, st, its, rrs, sts);
+        return E.solve(opA, pc, b, x, tl, mi, its, rrs, sts);
+    };
     to_im(rhs, bim);
     std::vector<int> it, stt, tot(nseg, 0);
     std::vector<double> rr;
     int rc = RMW_OK;
     if (mode != RMW_MODE_MIXED) {
         std::vector<double> tolv(nseg, tol);
-        rc = rmw::gmres_batched(op_mode(mode), pc, pcop, bim, xim, S.susp_off, tolv, restart, maxiter, st, it, rr,
-                                stt);
+        rc = batched(op_mode(mode), bim, xim, tolv, maxiter, it, rr, stt);
         tot = it;
     } else {
         // per-suspension iterative refinement: inner GMRES on the FP32-pair
@@ -719,8 +735,7 @@ int rmw_rigid_solve_batched(void *sys, const double *rhs, double *sol, double to
                 if ((rc = O.scale(rim, rim, 2, false))) goto done;
                 std::vector<double> rri;
                 std::vector<int> si;
-                rc = rmw::gmres_batched(op_mode(RMW_MODE_MIXED), pc, pcop, rim, dim, S.susp_off, itol, restart,
-                                        std::max(1, maxiter), st, it, rri, si);
+                rc = batched(op_mode(RMW_MODE_MIXED), rim, dim, itol, std::max(1, maxiter), it, rri, si);
                 if (rc) goto done;
                 for (int k = 0; k < nseg; ++k) tot[k] += it[k];
                 if ((rc = O.axpby(dim, xim, 1.0, 1.0))) goto done;

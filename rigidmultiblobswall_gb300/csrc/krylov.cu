@@ -641,11 +641,12 @@ static int rigid_solve_impl(void *sys, const double *rhs, double *sol, double to
         if (int rc = E.init({0, n}, restart, 0)) return rc;
     }
     // one GMRES solve of A x = b to tol (x from 0) on operator A = opA
-    auto gmres = [&](auto opA, const double *b, double *x, double tl, int mi, int *it, double *rr) -> int {
+    auto gmres = [&](auto opA, const double *b, double *x, double tl, int mi, int *it, double *rr,
+                     bool trust = false) -> int {
         if (!dev) return rmw::gmres_right(opA, pc, pcop, b, x, n, tl, restart, mi, S.st, it, rr, nullptr);
         std::vector<int> its, stt;
         std::vector<double> rrs;
-        if (int rc = E.solve(opA, pc, b, x, {tl}, mi, its, rrs, stt)) return rc;
+        if (int rc = E.solve(opA, pc, b, x, {tl}, mi, its, rrs, stt, nullptr, trust)) return rc;
         *it = its[0];
         *rr = rrs[0];
         if (stt[0] == RMW_ERR_NOT_CONVERGED) rmw::set_error("GMRES reached maxiter without converging");
@@ -698,21 +699,35 @@ static int rigid_solve_impl(void *sys, const double *rhs, double *sol, double to
     double relres = 0.0;
     int status = RMW_ERR_NOT_CONVERGED;
     const double inner_tol = 1e-5;
+    // With the device engine the inner solves skip their closing FP32 residual
+    // when the outer loop recomputes b - A x anyway, and hand it over as the
+    // next residual when the outer loop takes the recurrence r - A32 d (the
+    // same vector): one FP32-pair operator application less per refinement.
+    bool carried = false;
+    double rnorm_next = 0.0;
     for (int outer = 0; outer < 8 && bnorm > 0.0; ++outer) {
-        double rnorm = 0.0;
-        if (int rc = norm(r, &rnorm)) return rc;
+        double rnorm = rnorm_next;
+        if (!carried)
+            if (int rc = norm(r, &rnorm)) return rc;
         relres = rnorm / bnorm;
         if (relres <= tol) { status = RMW_OK; break; }
         const double itol = std::max(inner_tol, 0.5 * tol * bnorm / rnorm);
+        const bool recur = rmw::refine_by_recurrence(relres, tol);
         int it = 0;
         double rr = 0.0;
-        int rc = gmres(op32, r, d, itol, std::max(1, maxiter - total), &it, &rr);
+        int rc = gmres(op32, r, d, itol, std::max(1, maxiter - total), &it, &rr, dev && !recur);
         total += it;
         if (rc != RMW_OK && rc != RMW_ERR_NOT_CONVERGED) return rc;
         rmw::axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S.st>>>(d, x, n, 1.0, 1.0);
         void *rtok = nullptr;
         if (int rc2 = rmw::trace_begin(rmw::TRACE_REFINE, S.st, &rtok)) return rc2;
-        if (rmw::refine_by_recurrence(relres, tol)) {
+        carried = false;
+        if (recur && dev) {
+            // r - A32 d is the inner solve's closing residual
+            RMW_CUDA(cudaMemcpyAsync(r, E.K.r, sizeof(double) * n, cudaMemcpyDeviceToDevice, S.st));
+            carried = true;
+            rnorm_next = rr * rnorm;
+        } else if (recur) {
             // r = r - A32 d
             if (int rc2 = rmw::rigid_apply(S, d, ad, RMW_MODE_MIXED)) return rc2;
             rmw::axpby_kernel<<<(unsigned)((n + 255) / 256), 256, 0, S.st>>>(ad, r, n, -1.0, 1.0);
@@ -724,6 +739,7 @@ static int rigid_solve_impl(void *sys, const double *rhs, double *sol, double to
         if (int rc2 = rmw::trace_end(rtok, S.st)) return rc2;
         if (total >= maxiter) {
             if (int rc3 = norm(r, &rnorm)) return rc3;
+            carried = false;
             relres = rnorm / bnorm;
             status = (relres <= tol) ? RMW_OK : RMW_ERR_NOT_CONVERGED;
             break;
@@ -754,7 +770,17 @@ int rmw_rigid_lanczos(void *sys, const double *z, double *noise, double factor, 
     auto op = [&](const double *x, double *y) -> int { return gop(x, y); };
     double *tmp = nullptr;
     RMW_CUDA(cudaMallocAsync(&tmp, sizeof(double) * n, S.st));
-    int rc = rmw::lanczos(op, z, tmp, n, factor, tol, max_iter, S.st, iters_host);
+    int rc = RMW_OK;
+    if (rmw::krylov_device_enabled() && rmw::krylov_device_available()) {
+        // device-resident iterations (fused step kernel, one graph launch per call)
+        rmw::LanczosDevice<decltype(op_direct)> D(op_direct, &S.st);
+        std::vector<int> its;
+        rc = D.run(z, tmp, factor, tol, max_iter, std::max(2, std::min(max_iter + 1, 1000)), {0, n}, its,
+                   rmw::LzMask(), true);
+        if (rc == RMW_OK && iters_host) *iters_host = its[0];
+    } else {
+        rc = rmw::lanczos(op, z, tmp, n, factor, tol, max_iter, S.st, iters_host);
+    }
     if (rc == RMW_OK) rc = rmw::rigid_P_inv_mult(S, tmp, noise);
     RMW_CUDA(cudaFreeAsync(tmp, S.st));
     RMW_CUDA(cudaStreamSynchronize(S.st));
@@ -820,6 +846,17 @@ int rmw_wall_lanczos(const double *r, const double *z, double *noise, int64_t n,
     auto op = [&](const double *x, double *y) {
         return rmw::wall_product(RMW_UF, r, x, y, n, eta, a, L_host, mode, st);
     };
+    if (rmw::krylov_device_enabled() && rmw::krylov_device_available()) {
+        auto op_dev = [&](const double *x, double *y) {  // on the engine's stream (redirected while capturing)
+            return rmw::wall_product(RMW_UF, r, x, y, n, eta, a, L_host, mode, st);
+        };
+        rmw::LanczosDevice<decltype(op_dev)> D(op_dev, &st);
+        std::vector<int> its;
+        const int rc = D.run(z, noise, factor, tol, max_iter, std::max(2, std::min(max_iter + 1, 1000)),
+                             {0, 3 * (long long)n}, its, rmw::LzMask(), true);
+        if (rc == RMW_OK && iters_host) *iters_host = its[0];
+        return rc;
+    }
     return rmw::lanczos(op, z, noise, 3 * n, factor, tol, max_iter, st, iters_host);
 }
 

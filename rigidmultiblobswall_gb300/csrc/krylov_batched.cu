@@ -826,7 +826,22 @@ int rmw_rigid_lanczos_batched(void *sys, const double *Z, double *noise, int nrh
         return RMW_OK;
     };
     std::vector<int> it;
-    int rc = rmw::lanczos_batched(op, Z, raw, off, factor, tol, max_iter, S.st, it, before_op);
+    int rc = RMW_OK;
+    if (rmw::krylov_device_enabled() && rmw::krylov_device_available()) {
+        // device-resident lockstep iterations: the step kernel updates the
+        // (pass, suspension) activity bytes of the multi-vector product itself
+        rmw::LanczosDevice<decltype(op_direct)> D(op_direct, &S.st);
+        rmw::LzMask mk;
+        if (mask) {
+            mk.mask = d_act;
+            mk.nsusp = nsusp;
+            mk.nrhs = nrhs;
+            mk.pass = rmw::kMultiPass;
+        }
+        rc = D.run(Z, raw, factor, tol, max_iter, std::max(2, std::min(max_iter + 1, 96)), off, it, mk);
+    } else {
+        rc = rmw::lanczos_batched(op, Z, raw, off, factor, tol, max_iter, S.st, it, before_op);
+    }
     if (d_act) cudaFreeAsync(d_act, S.st);
     if (rc == RMW_OK) rc = rmw::rigid_P_inv_mult_multi(S, raw, noise, nrhs);
     cudaFreeAsync(buf, S.st);

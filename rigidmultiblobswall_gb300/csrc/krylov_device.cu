@@ -19,23 +19,23 @@ __device__ __forceinline__ double warp_sum(double v)
 }
 
 // Grid barrier of a cooperative launch: generation counter, bounded spin.
-__device__ void grid_barrier(KState *st)
+__device__ void grid_barrier(GridBar *b)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned *vgen = &st->bar_gen;
+        volatile unsigned *vgen = &b->gen;
         const unsigned gen = *vgen;
         __threadfence();
-        const unsigned arrived = atomicAdd(&st->bar_count, 1u);
+        const unsigned arrived = atomicAdd(&b->count, 1u);
         if (arrived == gridDim.x - 1) {
-            atomicExch(&st->bar_count, 0u);
+            atomicExch(&b->count, 0u);
             __threadfence();
-            atomicAdd(&st->bar_gen, 1u);
+            atomicAdd(&b->gen, 1u);
         } else {
             unsigned spins = 0;
             while (*vgen == gen) {
                 if (++spins > kBarrierSpins) {
-                    atomicExch(&st->err, 1);
+                    atomicExch(&b->err, 1);
                     break;
                 }
                 __nanosleep(64);
@@ -60,27 +60,27 @@ __device__ void reduce_segment(const double *part, int KP, int j0, int j1, int k
     __syncthreads();
 }
 
-// part[job * KP + q] = sum_{i in job} V_q[i] w[i], q < k (red: k x 32 shared doubles)
+// part[job * KP + q] = sum_{i in job} V_q[i] w[i], q < k (red: k x 32 shared
+// doubles); four basis vectors per pass over the job, so that each thread has
+// several independent loads in flight
 __device__ void job_dots(const double *__restrict__ V, long long ldv, int k, const double *w, const KJob jb,
                          double *part, int KP, int job, double *red)
 {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int q0 = 0; q0 < k; q0 += 2) {
-        const bool two = q0 + 1 < k;
+    for (int q0 = 0; q0 < k; q0 += 4) {
+        const int nq = min(4, k - q0);
         const double *V0 = V + (long long)q0 * ldv;
-        const double *V1 = V0 + ldv;
-        double a0 = 0.0, a1 = 0.0;
+        double a[4] = {0.0, 0.0, 0.0, 0.0};
         for (long long i = jb.b + threadIdx.x; i < jb.e; i += blockDim.x) {
             const double wi = w[i];
-            a0 = fma(V0[i], wi, a0);
-            if (two) a1 = fma(V1[i], wi, a1);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (u < nq) a[u] = fma(V0[(long long)u * ldv + i], wi, a[u]);
         }
-        a0 = warp_sum(a0);
-        a1 = warp_sum(a1);
-        if (lane == 0) {
-            red[q0 * 32 + wid] = a0;
-            if (two) red[(q0 + 1) * 32 + wid] = a1;
-        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) a[u] = warp_sum(a[u]);
+        if (lane == 0)
+            for (int u = 0; u < nq; ++u) red[(q0 + u) * 32 + wid] = a[u];
     }
     __syncthreads();
     for (int q = threadIdx.x; q < k; q += blockDim.x) {
@@ -98,6 +98,7 @@ __device__ double job_update(const double *__restrict__ V, long long ldv, int k,
     double nrm = 0.0;
     for (long long i = jb.b + threadIdx.x; i < jb.e; i += blockDim.x) {
         double x = w[i];
+#pragma unroll 8
         for (int q = 0; q < k; ++q) x = fma(-hs[q], V[(long long)q * ldv + i], x);
         w[i] = x;
         nrm = fma(x, x, nrm);
@@ -128,7 +129,7 @@ struct StepArgs {
     const int *sjob, *bjob;
     double *partA, *partB, *partC;
     int KP, R, hcap;
-    double *H, *cs, *sn, *g, *hc1, *hc2, *hist;
+    double *H, *cs, *sn, *g, *hc1, *hc2, *hist, *gres;
     const double *tol_abs;
     int *iters, *jdone, *cyc, *flags;
     KState *st;
@@ -149,7 +150,7 @@ __global__ void __launch_bounds__(kKdThreads, 1) arnoldi_step_kernel(StepArgs A)
     const int jb0 = A.bjob[blockIdx.x], jb1 = A.bjob[blockIdx.x + 1];
     // pass 1: partial dots V^T w
     for (int job = jb0; job < jb1; ++job) job_dots(A.V, A.ldv, k, A.w, A.jobs[job], A.partA, A.KP, job, red);
-    grid_barrier(A.st);
+    grid_barrier(&A.st->bar);
     // pass 2: w -= V h1, partial dots V^T w again
     for (int job = jb0; job < jb1; ++job) {
         const KJob jb = A.jobs[job];
@@ -160,7 +161,7 @@ __global__ void __launch_bounds__(kKdThreads, 1) arnoldi_step_kernel(StepArgs A)
         __syncthreads();
         job_dots(A.V, A.ldv, k, A.w, jb, A.partB, A.KP, job, red);
     }
-    grid_barrier(A.st);
+    grid_barrier(&A.st->bar);
     // pass 3: w -= V h2, partial |w|^2
     for (int job = jb0; job < jb1; ++job) {
         const KJob jb = A.jobs[job];
@@ -171,7 +172,7 @@ __global__ void __launch_bounds__(kKdThreads, 1) arnoldi_step_kernel(StepArgs A)
         __syncthreads();
         job_norm_partial(nrm, A.partC, A.KP, job, red);
     }
-    grid_barrier(A.st);
+    grid_barrier(&A.st->bar);
     // pass 4: V_{j+1} = w / |w| (zero vector for |w| = 0); Givens by the CTA owning the segment's first job
     for (int job = jb0; job < jb1; ++job) {
         const KJob jb = A.jobs[job];
@@ -213,6 +214,8 @@ __global__ void __launch_bounds__(kKdThreads, 1) arnoldi_step_kernel(StepArgs A)
                 const double res = fabs(gs[j + 1]);
                 if (A.hist && it <= A.hcap) A.hist[(long long)s * A.hcap + it - 1] = res;
                 const bool conv = res <= A.tol_abs[s];
+                A.gres[s] = res;
+                if (conv) A.flags[s] |= 4;                 // the estimate met the tolerance
                 if (hn == 0.0 && !conv) A.flags[s] |= 1;  // breakdown without convergence
                 stop = conv || hn == 0.0 || it >= A.st->maxiter;
             }
@@ -225,16 +228,16 @@ __global__ void __launch_bounds__(kKdThreads, 1) arnoldi_step_kernel(StepArgs A)
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        const unsigned prev = atomicAdd(&A.st->done, 1u);
+        const unsigned prev = atomicAdd(&A.st->bar.done, 1u);
         if (prev == gridDim.x - 1) {
             __threadfence();
             const int act = atomicAdd(&A.st->active, 0);
             const int jn = j + 1;
-            const int more = (act > 0 && jn < A.R && !*(volatile int *)&A.st->err) ? 1 : 0;
+            const int more = (act > 0 && jn < A.R && !*(volatile int *)&A.st->bar.err) ? 1 : 0;
             A.st->j = jn;
             A.st->active = 0;
             A.st->more = more;
-            atomicExch(&A.st->done, 0u);
+            atomicExch(&A.st->bar.done, 0u);
             __threadfence();
             if (A.use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)A.cond, (unsigned)more);
         }
@@ -301,7 +304,7 @@ __global__ void cycle_state_kernel(const double *__restrict__ beta, const double
     if (s == 0) {
         st->j = 0;
         st->active = 0;
-        st->done = 0;
+        st->bar.done = 0;
         st->more = 1;
     }
 }
@@ -349,6 +352,285 @@ __global__ void kd_axpby_kernel(const double *__restrict__ x, double *__restrict
 }
 
 // ---------------------------------------------------------------------------
+// Lanczos
+
+// Symmetric tridiagonal eigen-decomposition by implicit QL (the classical
+// algorithm of Bowdler, Martin, Reinsch and Wilkinson, as the host routine of
+// the library), run by one warp: every lane carries the scalar recurrence
+// (identical values, so each lane reads back its own writes of d and e) and
+// lane l applies the rotations to rows l, l+32, ... of z (k x k,
+// column-major).  On exit d holds the eigenvalues.
+__device__ bool tridiag_eigen_warp(double *d, double *e, double *z, int k, int lane)
+{
+    for (int q = lane; q < k; q += 32)
+        for (int c = 0; c < k; ++c) z[q + (long long)k * c] = (q == c) ? 1.0 : 0.0;
+    e[k - 1] = 0.0;
+    for (int l = 0; l < k; ++l) {
+        int iter = 0, m;
+        do {
+            for (m = l; m < k - 1; ++m) {
+                const double dd = fabs(d[m]) + fabs(d[m + 1]);
+                if (fabs(e[m]) <= 1e-16 * dd) break;
+            }
+            if (m != l) {
+                if (++iter > 60) return false;
+                double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+                double r = hypot(g, 1.0);
+                g = d[m] - d[l] + e[l] / (g + (g >= 0 ? fabs(r) : -fabs(r)));
+                double s = 1.0, c = 1.0, p = 0.0;
+                int i;
+                for (i = m - 1; i >= l; --i) {
+                    const double f = s * e[i], b = c * e[i];
+                    r = hypot(f, g);
+                    e[i + 1] = r;
+                    if (r == 0.0) {
+                        d[i + 1] -= p;
+                        e[m] = 0.0;
+                        break;
+                    }
+                    s = f / r;
+                    c = g / r;
+                    g = d[i + 1] - p;
+                    r = (d[i] - g) * s + 2.0 * c * b;
+                    p = s * r;
+                    d[i + 1] = g + p;
+                    g = c * r - b;
+                    for (int q = lane; q < k; q += 32) {
+                        double *z1 = z + q + (long long)k * (i + 1), *z0 = z + q + (long long)k * i;
+                        const double t = *z1;
+                        *z1 = s * *z0 + c * t;
+                        *z0 = c * *z0 - s * t;
+                    }
+                }
+                if (r == 0.0 && i >= l) continue;
+                d[l] -= p;
+                e[l] = g;
+                e[m] = 0.0;
+            }
+        } while (m != l);
+    }
+    return true;
+}
+
+struct LzArgs {
+    double *w, *xin;
+    const KJob *jobs;
+    const int *sjob, *bjob;
+    double *partA, *partB, *partC;
+    int KP, kcap;
+    double *hd, *hs, *c, *cold, *dt, *et, *z;  // per segment: kcap (z: kcap^2)
+    const double *zn;                          // |z_s|
+    double factor, tol;
+    int *iters, *cyc, *kfin, *flags;
+    LzState *st;
+    unsigned char *mask;  // optional (pass, suspension) activity bytes of the next operator application
+    int nsusp, nrhs, pass;
+    unsigned long long cond;
+    int use_cond;
+};
+
+// One Lanczos iteration i of every segment (stochastic_forcing.py:112-264):
+// w -= hs[i-1] V_{i-1}; hd[i] = <w, V_i>; w -= hd[i] V_i; hs[i] = |w|;
+// w /= hs[i]; one classical reorthogonalisation pass against V_0..V_i;
+// V_{i+1} = w (also the operator's next input).  The CTA owning a segment's
+// first job then diagonalises the (i+1) x (i+1) tridiagonal matrix with one
+// warp, forms the coefficients c of the noise |z| factor V^T Q sqrt(L) Q^T e1
+// and applies the stopping test |c - c_old| < tol |c_old|.  A segment that
+// stopped at the previous iteration is frozen (its w and next vector zero).
+__global__ void __launch_bounds__(kKdThreads, 1) lanczos_step_kernel(LzArgs A)
+{
+    __shared__ double red[kKdMaxBasis * 32];
+    __shared__ double hsh[kKdMaxBasis];
+    __shared__ int actv[8];
+    const int i = *(volatile int *)&A.st->i;
+    const int k = i + 1;
+    double *const V = *(double *volatile *)&A.st->V;
+    const long long ldv = A.st->ldv;
+    const int jb0 = A.bjob[blockIdx.x], jb1 = A.bjob[blockIdx.x + 1];
+    // frozen segments: read once, before any owner can change them (owners write after the last barrier)
+    for (int job = jb0; job < jb1 && job - jb0 < 8; ++job)
+        if (threadIdx.x == 0) actv[job - jb0] = A.cyc[A.jobs[job].seg];
+    __syncthreads();
+    // pass 1: w -= hs[i-1] V_{i-1} (frozen: w = 0); partial <w, V_i>
+    for (int job = jb0; job < jb1; ++job) {
+        const KJob jb = A.jobs[job];
+        const bool on = (job - jb0 < 8) ? actv[job - jb0] != 0 : A.cyc[jb.seg] != 0;
+        const double hp = (i > 0) ? A.hs[(long long)jb.seg * A.kcap + i - 1] : 0.0;
+        const double *Vp = V + (long long)(i > 0 ? i - 1 : 0) * ldv;
+        for (long long e = jb.b + threadIdx.x; e < jb.e; e += blockDim.x)
+            A.w[e] = on ? ((i > 0) ? fma(-hp, Vp[e], A.w[e]) : A.w[e]) : 0.0;
+        __syncthreads();
+        job_dots(V + (long long)i * ldv, ldv, 1, A.w, jb, A.partA, A.KP, job, red);
+    }
+    grid_barrier(&A.st->bar);
+    // pass 2: hd = <w, V_i>; w -= hd V_i; partial |w|^2
+    for (int job = jb0; job < jb1; ++job) {
+        const KJob jb = A.jobs[job];
+        reduce_segment(A.partA, A.KP, A.sjob[jb.seg], A.sjob[jb.seg + 1], 1, hsh);
+        const double nrm = job_update(V + (long long)i * ldv, ldv, 1, hsh, A.w, jb);
+        if (job == A.sjob[jb.seg] && threadIdx.x == 0) A.dt[(long long)jb.seg * A.kcap] = hsh[0];  // hd[i], kept below
+        __syncthreads();
+        job_norm_partial(nrm, A.partC, A.KP, job, red);
+    }
+    grid_barrier(&A.st->bar);
+    // pass 3: hs = |w|; w /= hs (0 on an exact breakdown); partial reorthogonalisation dots V_q^T w
+    for (int job = jb0; job < jb1; ++job) {
+        const KJob jb = A.jobs[job];
+        reduce_segment(A.partC, A.KP, A.sjob[jb.seg], A.sjob[jb.seg + 1], 1, hsh);
+        const double wn = sqrt(hsh[0]);
+        const double inv = (wn > 0.0) ? 1.0 / wn : 0.0;
+        for (long long e = jb.b + threadIdx.x; e < jb.e; e += blockDim.x) A.w[e] *= inv;
+        if (job == A.sjob[jb.seg] && threadIdx.x == 0) A.et[(long long)jb.seg * A.kcap] = wn;
+        __syncthreads();
+        for (int q0 = 0; q0 < k; q0 += kKdMaxBasis)
+            job_dots(V + (long long)q0 * ldv, ldv, min(kKdMaxBasis, k - q0), A.w, jb, A.partB + q0, A.KP, job, red);
+    }
+    grid_barrier(&A.st->bar);
+    // pass 4: w -= V h; V_{i+1} = w; owners: tridiagonal eigen-problem, coefficients, stopping test
+    for (int job = jb0; job < jb1; ++job) {
+        const KJob jb = A.jobs[job];
+        for (int q0 = 0; q0 < k; q0 += kKdMaxBasis) {
+            const int kc = min(kKdMaxBasis, k - q0);
+            reduce_segment(A.partB + q0, A.KP, A.sjob[jb.seg], A.sjob[jb.seg + 1], kc, hsh);
+            job_update(V + (long long)q0 * ldv, ldv, kc, hsh, A.w, jb);
+            __syncthreads();
+        }
+        double *Vn = V + (long long)(i + 1) * ldv;
+        for (long long e = jb.b + threadIdx.x; e < jb.e; e += blockDim.x) {
+            Vn[e] = A.w[e];
+            A.xin[e] = A.w[e];
+        }
+        const int s = jb.seg;
+        if (job == A.sjob[s] && A.cyc[s] && threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            const long long so = (long long)s * A.kcap;
+            const double hdi = A.dt[so], wn = A.et[so];
+            if (lane == 0) {
+                A.hd[so + i] = hdi;
+                A.hs[so + i] = wn;
+            }
+            __syncwarp();
+            int stop = 0;
+            if (!isfinite(wn) || !isfinite(hdi)) {
+                if (lane == 0) A.flags[s] |= 2;
+                stop = 1;
+            } else {
+                double *d = A.dt + so, *ee = A.et + so, *zz = A.z + (long long)s * A.kcap * A.kcap;
+                for (int q = 0; q < k; ++q) {  // every lane writes the same values (its own reads stay coherent)
+                    d[q] = A.hd[so + q];
+                    ee[q] = (q < i) ? A.hs[so + q] : 0.0;
+                }
+                const bool ok = tridiag_eigen_warp(d, ee, zz, k, lane);
+                __syncwarp();
+                if (!ok) {
+                    if (lane == 0) A.flags[s] |= 4;
+                    stop = 1;
+                } else {
+                    double *cc = A.c + so, *co = A.cold + so;
+                    const double sc = A.zn[s] * A.factor;
+                    double dn = 0.0, on = 0.0;
+                    for (int q = lane; q < k; q += 32) {
+                        double acc = 0.0;
+                        for (int jj = 0; jj < k; ++jj) {
+                            const double lam = d[jj] > 0.0 ? sqrt(d[jj]) : 0.0;
+                            acc += zz[q + (long long)k * jj] * (zz[(long long)k * jj] * lam * sc);
+                        }
+                        const double old = (q < i) ? co[q] : 0.0;
+                        dn += (acc - old) * (acc - old);
+                        on += old * old;
+                        cc[q] = acc;
+                    }
+                    dn = warp_sum(dn);
+                    on = warp_sum(on);
+                    __syncwarp();
+                    for (int q = lane; q < k; q += 32) co[q] = cc[q];
+                    const bool conv = i > 0 && sqrt(dn) / fmax(sqrt(on), 2.220446049250313e-16) < A.tol;
+                    stop = conv || wn == 0.0;
+                    if (lane == 0) {
+                        A.kfin[s] = k;
+                        if (stop) A.iters[s] = i;
+                    }
+                }
+            }
+            if (lane == 0) {
+                if (stop) A.cyc[s] = 0;
+                else atomicAdd(&A.st->active, 1);
+            }
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(&A.st->bar.done, 1u);
+        if (prev == gridDim.x - 1) {
+            __threadfence();
+            const int act = atomicAdd(&A.st->active, 0);
+            const int in = i + 1;
+            // stop when no segment is left, past max_iter, or when the basis is full (the host grows it)
+            const int more = (act > 0 && in <= A.st->max_iter && in + 1 < A.st->vcap &&
+                              !*(volatile int *)&A.st->bar.err) ? 1 : 0;
+            A.st->i = in;
+            A.st->active = 0;
+            A.st->more = more;
+            A.st->live = act;
+            if (A.mask) {
+                const int npass = (A.nrhs + A.pass - 1) / A.pass;
+                for (int p = 0; p < npass; ++p)
+                    for (int u = 0; u < A.nsusp; ++u) {
+                        unsigned char any = 0;
+                        for (int q = p * A.pass; q < min(A.nrhs, (p + 1) * A.pass); ++q)
+                            any |= A.cyc[(long long)q * A.nsusp + u] ? 1 : 0;
+                        A.mask[(long long)p * A.nsusp + u] = any;
+                    }
+            }
+            atomicExch(&A.st->bar.done, 0u);
+            __threadfence();
+            if (A.use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)A.cond, (unsigned)more);
+        }
+    }
+}
+
+// out = V c_s per segment (first kfin[s] basis vectors; one CTA per job)
+__global__ void lz_combine_kernel(const LzState *__restrict__ st, const double *__restrict__ c,
+                                  const int *__restrict__ kfin, int kcap, const KJob *__restrict__ jobs,
+                                  double *__restrict__ out)
+{
+    __shared__ double cs[256];
+    const KJob jb = jobs[blockIdx.x];
+    const double *V = st->V;
+    const long long ldv = st->ldv;
+    const int k = kfin[jb.seg];
+    for (long long e = jb.b + threadIdx.x; e < jb.e; e += blockDim.x) out[e] = 0.0;
+    for (int q0 = 0; q0 < k; q0 += 256) {
+        const int kc = min(256, k - q0);
+        __syncthreads();
+        for (int q = threadIdx.x; q < kc; q += blockDim.x) cs[q] = c[(long long)jb.seg * kcap + q0 + q];
+        __syncthreads();
+        for (long long e = jb.b + threadIdx.x; e < jb.e; e += blockDim.x) {
+            double s = out[e];
+            for (int q = 0; q < kc; ++q) s = fma(cs[q], V[(long long)(q0 + q) * ldv + e], s);
+            out[e] = s;
+        }
+    }
+}
+
+// V_0 = z / |z_s| (0 for a segment that does not run), xin = V_0
+__global__ void lz_begin_kernel(const double *__restrict__ z, const double *__restrict__ zn,
+                                const int *__restrict__ cyc, const KJob *__restrict__ jobs, LzState *st,
+                                double *__restrict__ xin)
+{
+    const KJob jb = jobs[blockIdx.x];
+    const double a = cyc[jb.seg] ? 1.0 / zn[jb.seg] : 0.0;
+    double *V0 = st->V;
+    for (long long e = jb.b + threadIdx.x; e < jb.e; e += blockDim.x) {
+        const double v = a * z[e];
+        V0[e] = v;
+        xin[e] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 
 static std::atomic<bool> g_device_krylov{true};
@@ -377,26 +659,18 @@ KrylovDev::~KrylovDev()
     }
 }
 
-int KrylovDev::init(const std::vector<long long> &seg_off, int restart, int hist_cap, cudaStream_t s)
+int kd_build_jobs(const std::vector<long long> &off, int nblk_max, std::vector<KJob> &jb, std::vector<int> &sj,
+                  std::vector<int> &bj)
 {
-    st = s;
-    off = seg_off;
-    nseg = (int)off.size() - 1;
-    n = off.back();
-    R = std::max(1, std::min(restart, kKdMaxBasis - 8));
-    KP = R + 2;
-    hcap = hist_cap;
-    ldv = ((n + 31) / 32) * 32;
-    int dev = 0, sms = 1;
-    RMW_CUDA(cudaGetDevice(&dev));
-    RMW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int nseg = (int)off.size() - 1;
+    const long long n = off.back();
     // one CTA per SM at most, at least 1024 elements per CTA
-    nblk = (int)std::max<long long>(1, std::min<long long>(sms, (n + kKdThreads - 1) / kKdThreads));
+    const int nblk = (int)std::max<long long>(1, std::min<long long>(nblk_max, (n + kKdThreads - 1) / kKdThreads));
     long long per = (n + nblk - 1) / nblk;
     per = ((per + 31) / 32) * 32;
-    // jobs: intersections of CTA ranges with segments (both in element order)
-    std::vector<KJob> jb;
-    std::vector<int> sj(nseg + 1, 0), bj(nblk + 1, 0);
+    jb.clear();
+    sj.assign(nseg + 1, 0);
+    bj.assign(nblk + 1, 0);
     int sg = 0;
     for (int b = 0; b < nblk; ++b) {
         bj[b] = (int)jb.size();
@@ -410,23 +684,41 @@ int KrylovDev::init(const std::vector<long long> &seg_off, int restart, int hist
         }
     }
     bj[nblk] = (int)jb.size();
-    njobs = (int)jb.size();
     // first job of every segment (empty segments own no job: [x, x))
-    {
-        int q = 0;
-        for (int t = 0; t < nseg; ++t) {
-            while (q < njobs && jb[q].seg < t) ++q;
-            sj[t] = q;
-        }
-        sj[nseg] = njobs;
+    const int njobs = (int)jb.size();
+    int q = 0;
+    for (int t = 0; t < nseg; ++t) {
+        while (q < njobs && jb[q].seg < t) ++q;
+        sj[t] = q;
     }
+    sj[nseg] = njobs;
+    return nblk;
+}
+
+int KrylovDev::init(const std::vector<long long> &seg_off, int restart, int hist_cap, cudaStream_t s)
+{
+    st = s;
+    off = seg_off;
+    nseg = (int)off.size() - 1;
+    n = off.back();
+    R = std::max(1, std::min(restart, kKdMaxBasis - 8));
+    KP = R + 2;
+    hcap = hist_cap;
+    ldv = ((n + 31) / 32) * 32;
+    int dev = 0, sms = 1;
+    RMW_CUDA(cudaGetDevice(&dev));
+    RMW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    std::vector<KJob> jb;
+    std::vector<int> sj, bj;
+    nblk = kd_build_jobs(off, sms, jb, sj, bj);
+    njobs = (int)jb.size();
     const size_t nj = (size_t)std::max(1, njobs), ns = (size_t)nseg;
     auto al = [](size_t b) { return (b + 255) / 256 * 256; };
     size_t bytes = al(sizeof(double) * (size_t)ldv * (R + 1)) + 6 * al(sizeof(double) * (size_t)ldv) +
                    al(sizeof(KJob) * nj) + al(sizeof(int) * (ns + 1)) + al(sizeof(int) * (nblk + 1)) +
                    3 * al(sizeof(double) * nj * KP) + al(sizeof(double) * ns * R * (R + 1)) +
                    2 * al(sizeof(double) * ns * R) + al(sizeof(double) * ns * (R + 1)) +
-                   2 * al(sizeof(double) * ns * KP) + 3 * al(sizeof(double) * ns) + al(sizeof(double) * ns * KP) +
+                   2 * al(sizeof(double) * ns * KP) + 4 * al(sizeof(double) * ns) + al(sizeof(double) * ns * KP) +
                    al(sizeof(double) * ns * std::max(1, hcap)) + 4 * al(sizeof(int) * ns) + al(sizeof(KState));
     RMW_CUDA(cudaMallocAsync(&base, bytes, st));
     char *p = (char *)base;
@@ -457,12 +749,14 @@ int KrylovDev::init(const std::vector<long long> &seg_off, int restart, int hist
     tol_abs = (double *)take(sizeof(double) * ns);
     alpha = (double *)take(sizeof(double) * ns);
     nrm = (double *)take(sizeof(double) * ns);
+    gres = (double *)take(sizeof(double) * ns);
     y = (double *)take(sizeof(double) * ns * KP);
     hist = (double *)take(sizeof(double) * ns * std::max(1, hcap));
-    iters = (int *)take(sizeof(int) * ns);
-    jdone = (int *)take(sizeof(int) * ns);
-    cyc = (int *)take(sizeof(int) * ns);
-    flags = (int *)take(sizeof(int) * ns);
+    // iters, jdone, cyc and flags back to back (one copy reads all four)
+    iters = (int *)take(sizeof(int) * 4 * ns);
+    jdone = iters + ns;
+    cyc = iters + 2 * ns;
+    flags = iters + 3 * ns;
     state = (KState *)take(sizeof(KState));
     if (njobs) RMW_CUDA(cudaMemcpyAsync(jobs, jb.data(), sizeof(KJob) * njobs, cudaMemcpyHostToDevice, st));
     RMW_CUDA(cudaMemcpyAsync(sjob, sj.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice, st));
@@ -477,6 +771,225 @@ int KrylovDev::init(const std::vector<long long> &seg_off, int restart, int hist
     RMW_CUDA(cudaHostAlloc(&pinned, sizeof(double) * (8 * ns + 16), cudaHostAllocDefault));
     // the copies above read host vectors that go out of scope
     RMW_CUDA(cudaStreamSynchronize(st));
+    return RMW_OK;
+}
+
+// ---- Lanczos buffers ------------------------------------------------------
+LanczosDev::~LanczosDev()
+{
+    if (V) cudaFreeAsync(V, st);
+    if (base) cudaFreeAsync(base, st);
+    if (pinned) {
+        cudaStreamSynchronize(st);
+        cudaFreeHost(pinned);
+    }
+}
+
+int LanczosDev::init(const std::vector<long long> &seg_off, int kcap_, cudaStream_t s)
+{
+    st = s;
+    nseg = (int)seg_off.size() - 1;
+    n = seg_off.back();
+    kcap = std::max(2, kcap_);
+    KP = kcap + 2;
+    ldv = ((n + 31) / 32) * 32;
+    int dev = 0, sms = 1;
+    RMW_CUDA(cudaGetDevice(&dev));
+    RMW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    std::vector<KJob> jb;
+    std::vector<int> sj, bj;
+    nblk = kd_build_jobs(seg_off, sms, jb, sj, bj);
+    njobs = (int)jb.size();
+    const size_t nj = (size_t)std::max(1, njobs), ns = (size_t)nseg, kc = (size_t)kcap;
+    auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t bytes = 2 * al(sizeof(double) * ldv) + al(sizeof(KJob) * nj) + al(sizeof(int) * (ns + 1)) +
+                         al(sizeof(int) * (nblk + 1)) + 3 * al(sizeof(double) * nj * KP) + al(sizeof(double) * ns) +
+                         6 * al(sizeof(double) * ns * kc) + al(sizeof(double) * ns * kc * kc) +
+                         4 * al(sizeof(int) * ns) + al(sizeof(LzState));
+    RMW_CUDA(cudaMallocAsync(&base, bytes, st));
+    char *p = (char *)base;
+    auto take = [&](size_t b) {
+        char *q = p;
+        p += al(b);
+        return (void *)q;
+    };
+    w = (double *)take(sizeof(double) * ldv);
+    xin = (double *)take(sizeof(double) * ldv);
+    jobs = (KJob *)take(sizeof(KJob) * nj);
+    sjob = (int *)take(sizeof(int) * (ns + 1));
+    bjob = (int *)take(sizeof(int) * (nblk + 1));
+    partA = (double *)take(sizeof(double) * nj * KP);
+    partB = (double *)take(sizeof(double) * nj * KP);
+    partC = (double *)take(sizeof(double) * nj * KP);
+    zn = (double *)take(sizeof(double) * ns);
+    hd = (double *)take(sizeof(double) * ns * kc);
+    hs = (double *)take(sizeof(double) * ns * kc);
+    c = (double *)take(sizeof(double) * ns * kc);
+    cold = (double *)take(sizeof(double) * ns * kc);
+    dt = (double *)take(sizeof(double) * ns * kc);
+    et = (double *)take(sizeof(double) * ns * kc);
+    z = (double *)take(sizeof(double) * ns * kc * kc);
+    iters = (int *)take(sizeof(int) * ns);
+    cyc = (int *)take(sizeof(int) * ns);
+    kfin = (int *)take(sizeof(int) * ns);
+    flags = (int *)take(sizeof(int) * ns);
+    state = (LzState *)take(sizeof(LzState));
+    if (njobs) RMW_CUDA(cudaMemcpyAsync(jobs, jb.data(), sizeof(KJob) * njobs, cudaMemcpyHostToDevice, st));
+    RMW_CUDA(cudaMemcpyAsync(sjob, sj.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice, st));
+    RMW_CUDA(cudaMemcpyAsync(bjob, bj.data(), sizeof(int) * (nblk + 1), cudaMemcpyHostToDevice, st));
+    RMW_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * 2 * ldv, st));
+    RMW_CUDA(cudaMemsetAsync(state, 0, sizeof(LzState), st));
+    RMW_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * ns, st));
+    RMW_CUDA(cudaMemsetAsync(c, 0, sizeof(double) * ns * kc, st));
+    RMW_CUDA(cudaHostAlloc(&pinned, sizeof(double) * (2 * ns + 16) + sizeof(int) * 4 * ns + sizeof(LzState),
+                           cudaHostAllocDefault));
+    RMW_CUDA(cudaStreamSynchronize(st));
+    return grow(std::min(kcap + 1, 32));
+}
+
+int LanczosDev::grow(int want)
+{
+    want = std::min(want, kcap + 1);
+    if (want <= vcap) return RMW_OK;
+    double *nv = nullptr;
+    RMW_CUDA(cudaMallocAsync(&nv, sizeof(double) * (size_t)ldv * want, st));
+    if (V) {
+        RMW_CUDA(cudaMemcpyAsync(nv, V, sizeof(double) * (size_t)ldv * vcap, cudaMemcpyDeviceToDevice, st));
+        RMW_CUDA(cudaFreeAsync(V, st));
+    }
+    V = nv;
+    vcap = want;
+    // the step kernels read the basis pointer and its room from the state
+    LzState *h = (LzState *)((char *)pinned + sizeof(double) * (2 * nseg + 16) + sizeof(int) * 4 * nseg);
+    RMW_CUDA(cudaMemcpyAsync(h, state, sizeof(LzState), cudaMemcpyDeviceToHost, st));
+    RMW_CUDA(cudaStreamSynchronize(st));
+    h->V = V;
+    h->vcap = vcap;
+    h->ldv = ldv;
+    RMW_CUDA(cudaMemcpyAsync(state, h, sizeof(LzState), cudaMemcpyHostToDevice, st));
+    RMW_CUDA(cudaStreamSynchronize(st));
+    return RMW_OK;
+}
+
+__global__ void lz_init_kernel(const double *__restrict__ nrm, int nseg, double factor, int max_iter,
+                               double *__restrict__ zn, int *__restrict__ cyc, int *__restrict__ iters,
+                               int *__restrict__ kfin, LzState *st)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nseg) {
+        const double z = sqrt(nrm[s]);
+        zn[s] = z;
+        const int on = (z > 0.0 && isfinite(z) && factor != 0.0) ? 1 : 0;
+        cyc[s] = on;
+        iters[s] = on ? max_iter : 0;
+        kfin[s] = 0;
+    }
+    if (s == 0) {
+        st->i = 0;
+        st->active = 0;
+        st->more = 1;
+        st->live = 0;
+        st->max_iter = max_iter;
+        st->bar.done = 0;
+    }
+}
+
+int lz_begin(LanczosDev &L, const double *z, double factor, int max_iter, std::vector<double> &zn_host,
+             std::vector<int> &run)
+{
+    const int ns = L.nseg;
+    if (L.njobs) {
+        seg_norm_partial_kernel<<<L.njobs, 512, 0, L.st>>>(z, L.jobs, L.partC);
+        seg_norm_reduce_kernel<<<(ns * 32 + 255) / 256, 256, 0, L.st>>>(L.partC, L.sjob, ns, L.partA);
+    } else {
+        RMW_CUDA(cudaMemsetAsync(L.partA, 0, sizeof(double) * ns, L.st));
+    }
+    lz_init_kernel<<<(ns + 127) / 128, 128, 0, L.st>>>(L.partA, ns, factor, max_iter, L.zn, L.cyc, L.iters, L.kfin,
+                                                       L.state);
+    if (L.njobs) lz_begin_kernel<<<L.njobs, 512, 0, L.st>>>(z, L.zn, L.cyc, L.jobs, L.state, L.xin);
+    RMW_CHECK_LAUNCH("Lanczos start");
+    double *h = (double *)L.pinned;
+    int *hi = (int *)((char *)L.pinned + sizeof(double) * (2 * ns + 16));
+    RMW_CUDA(cudaMemcpyAsync(h, L.zn, sizeof(double) * ns, cudaMemcpyDeviceToHost, L.st));
+    RMW_CUDA(cudaMemcpyAsync(hi, L.cyc, sizeof(int) * ns, cudaMemcpyDeviceToHost, L.st));
+    RMW_CUDA(cudaStreamSynchronize(L.st));
+    zn_host.assign(h, h + ns);
+    run.assign(hi, hi + ns);
+    return RMW_OK;
+}
+
+int lz_step(LanczosDev &L, double factor, double tol, const LzMask &mk, unsigned long long cond, int use_cond,
+            cudaStream_t st)
+{
+    LzArgs A;
+    A.w = L.w;
+    A.xin = L.xin;
+    A.jobs = L.jobs;
+    A.sjob = L.sjob;
+    A.bjob = L.bjob;
+    A.partA = L.partA;
+    A.partB = L.partB;
+    A.partC = L.partC;
+    A.KP = L.KP;
+    A.kcap = L.kcap;
+    A.hd = L.hd;
+    A.hs = L.hs;
+    A.c = L.c;
+    A.cold = L.cold;
+    A.dt = L.dt;
+    A.et = L.et;
+    A.z = L.z;
+    A.zn = L.zn;
+    A.factor = factor;
+    A.tol = tol;
+    A.iters = L.iters;
+    A.cyc = L.cyc;
+    A.kfin = L.kfin;
+    A.flags = L.flags;
+    A.st = L.state;
+    A.mask = mk.mask;
+    A.nsusp = mk.nsusp;
+    A.nrhs = mk.nrhs;
+    A.pass = mk.pass;
+    A.cond = cond;
+    A.use_cond = use_cond;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)L.nblk);
+    cfg.blockDim = dim3(kKdThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    RMW_CUDA(cudaLaunchKernelEx(&cfg, lanczos_step_kernel, A));
+    return RMW_OK;
+}
+
+int lz_fetch_state(LanczosDev &L, LzState *host)
+{
+    LzState *h = (LzState *)((char *)L.pinned + sizeof(double) * (2 * L.nseg + 16) + sizeof(int) * 4 * L.nseg);
+    RMW_CUDA(cudaMemcpyAsync(h, L.state, sizeof(LzState), cudaMemcpyDeviceToHost, L.st));
+    RMW_CUDA(cudaStreamSynchronize(L.st));
+    *host = *h;
+    return RMW_OK;
+}
+
+int lz_finish(LanczosDev &L, double *noise, std::vector<int> &iters)
+{
+    const int ns = L.nseg;
+    int *hi = (int *)((char *)L.pinned + sizeof(double) * (2 * ns + 16));
+    RMW_CUDA(cudaMemcpyAsync(hi, L.flags, sizeof(int) * ns, cudaMemcpyDeviceToHost, L.st));
+    RMW_CUDA(cudaStreamSynchronize(L.st));
+    for (int s = 0; s < ns; ++s) {
+        if (hi[s] & 2) return fail(RMW_ERR_BREAKDOWN, "Lanczos: non-finite value");
+        if (hi[s] & 4) return fail(RMW_ERR_BREAKDOWN, "Lanczos: tridiagonal eigensolver failed");
+    }
+    if (L.njobs) lz_combine_kernel<<<L.njobs, 512, 0, L.st>>>(L.state, L.c, L.kfin, L.kcap, L.jobs, noise);
+    RMW_CHECK_LAUNCH("Lanczos noise");
+    RMW_CUDA(cudaMemcpyAsync(hi, L.iters, sizeof(int) * ns, cudaMemcpyDeviceToHost, L.st));
+    RMW_CUDA(cudaStreamSynchronize(L.st));
+    iters.assign(hi, hi + ns);
     return RMW_OK;
 }
 
@@ -534,6 +1047,7 @@ int kd_arnoldi_step(KrylovDev &K, unsigned long long cond, int use_cond, cudaStr
     A.hc1 = K.hc1;
     A.hc2 = K.hc2;
     A.hist = K.hcap > 0 ? K.hist : nullptr;
+    A.gres = K.gres;
     A.tol_abs = K.tol_abs;
     A.iters = K.iters;
     A.jdone = K.jdone;

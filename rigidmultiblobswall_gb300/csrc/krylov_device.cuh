@@ -43,17 +43,41 @@ struct KJob {
     long long b, e;
 };
 
-// solver scalars shared by the step kernels of one solve
-struct KState {
-    int j;              // Arnoldi step within the cycle
-    int active;         // segments still iterating after the step (last CTA reads it)
-    unsigned done;      // CTAs finished with the step (last-CTA detection)
-    unsigned bar_count;
-    unsigned bar_gen;
-    int err;            // a grid barrier gave up waiting
-    int more;           // the loop condition the last step set
-    int maxiter;        // iteration limit per segment (the solve's)
+// grid barrier and last-CTA detection of one cooperative step kernel
+struct GridBar {
+    unsigned done;  // CTAs finished with the step (last-CTA detection)
+    unsigned count;
+    unsigned gen;
+    int err;  // a grid barrier gave up waiting
 };
+
+// solver scalars shared by the GMRES step kernels of one solve
+struct KState {
+    GridBar bar;
+    int j;        // Arnoldi step within the cycle
+    int active;   // segments still iterating after the step (last CTA reads it)
+    int more;     // the loop condition the last step set
+    int maxiter;  // iteration limit per segment (the solve's)
+};
+
+// scalars of the Lanczos step kernels of one call
+struct LzState {
+    GridBar bar;
+    int i;         // iteration
+    int active;    // segments still iterating after the step (counted by the owners)
+    int more;      // loop condition
+    int live;      // segments still iterating after the last step
+    int max_iter;  // the reference's max_iter
+    int vcap;      // basis vectors V has room for
+    long long ldv;
+    double *V;     // the basis (grown by the host between graph launches)
+};
+
+// Job table: CTA b of at most nblk_max CTAs gets a contiguous range of the n
+// elements (a multiple of 32 long); jobs are the intersections of those ranges
+// with the segments [off[s], off[s+1]).  Returns the CTA count.
+int kd_build_jobs(const std::vector<long long> &off, int nblk_max, std::vector<KJob> &jobs, std::vector<int> &sjob,
+                  std::vector<int> &bjob);
 
 // device buffers and job tables of one device GMRES engine
 struct KrylovDev {
@@ -73,6 +97,7 @@ struct KrylovDev {
     // per-segment state
     double *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr, *hc1 = nullptr, *hc2 = nullptr;
     double *tol_abs = nullptr, *alpha = nullptr, *y = nullptr, *nrm = nullptr, *hist = nullptr;
+    double *gres = nullptr;  // last residual estimate |g_{j+1}| per segment
     int *iters = nullptr, *jdone = nullptr, *cyc = nullptr, *flags = nullptr;
     KState *state = nullptr;
     // host copies of the job layout
@@ -107,10 +132,210 @@ int kd_fetch_cycle(KrylovDev &K, KState *state_host, int *ints_host);
 int kd_fetch_norms(KrylovDev &K, double *host);
 int kd_fetch_more(KrylovDev &K, int *more);
 
+// ---- Lanczos ---------------------------------------------------------------
+struct LanczosDev {
+    int nseg = 0, njobs = 0, nblk = 0, kcap = 0, KP = 0;
+    long long n = 0, ldv = 0;
+    cudaStream_t st = 0;
+    void *base = nullptr;
+    double *V = nullptr;  // basis (own allocation, grown by doubling)
+    int vcap = 0;
+    void *pinned = nullptr;
+    double *w = nullptr, *xin = nullptr;
+    KJob *jobs = nullptr;
+    int *sjob = nullptr, *bjob = nullptr;
+    double *partA = nullptr, *partB = nullptr, *partC = nullptr;
+    double *zn = nullptr, *hd = nullptr, *hs = nullptr, *c = nullptr, *cold = nullptr, *dt = nullptr, *et = nullptr,
+           *z = nullptr;
+    int *iters = nullptr, *cyc = nullptr, *kfin = nullptr, *flags = nullptr;
+    LzState *state = nullptr;
+    ~LanczosDev();
+    int init(const std::vector<long long> &seg_off, int kcap_, cudaStream_t s);
+    int grow(int want);  // basis room for `want` vectors (copies the old ones)
+};
+
+struct LzMask {
+    unsigned char *mask = nullptr;  // (pass, suspension) bytes the operator reads; null: none
+    int nsusp = 0, nrhs = 0, pass = 8;
+};
+
+// start: |z_s| (host copy in zn_host), V_0 = z / |z_s| for the segments that
+// run (zn > 0 and factor != 0), iteration counters, state
+int lz_begin(LanczosDev &L, const double *z, double factor, int max_iter, std::vector<double> &zn_host,
+             std::vector<int> &run);
+int lz_step(LanczosDev &L, double factor, double tol, const LzMask &mk, unsigned long long cond, int use_cond,
+            cudaStream_t st);
+int lz_fetch_state(LanczosDev &L, LzState *host);
+int lz_finish(LanczosDev &L, double *noise, std::vector<int> &iters);
+
 bool graphs_enabled();
 void graph_live(int delta);
 void graph_count(bool captured);
 int capture_stream(cudaStream_t home, cudaStream_t *out);
+
+// Device-resident Lanczos (stochastic_forcing.py:112-264) over one or many
+// segments: op(x, y) = y = M x on *sref.  Iterations run as a CUDA graph while
+// node around [op(xin) -> w; lanczos_step_kernel]; the loop returns to the host
+// only when every segment has stopped, after max_iter, or when the basis is
+// full (the host doubles it and relaunches).
+template <typename Op>
+struct LanczosDevice {
+    LanczosDev L;
+    Op op;
+    cudaStream_t *sref;
+    cudaStream_t home;
+    cudaStream_t priv = nullptr;
+    cudaEvent_t ev = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long cond = 0;
+    bool graph_failed = false;
+    LzMask mk;
+    double factor = 1.0, tol = 1e-3;
+
+    LanczosDevice(Op f, cudaStream_t *s) : op(f), sref(s), home(*s) {}
+    LanczosDevice(const LanczosDevice &) = delete;
+    LanczosDevice &operator=(const LanczosDevice &) = delete;
+    ~LanczosDevice()
+    {
+        if (exec) {
+            cudaStreamSynchronize(home);
+            cudaGraphExecDestroy(exec);
+            graph_live(-1);
+        }
+        if (graph) cudaGraphDestroy(graph);
+        if (ev) cudaEventDestroy(ev);
+    }
+
+    int capture_once()
+    {
+        cudaGraph_t g = nullptr, body = nullptr;
+        if (int rc = kd_build_cycle_graph(&g, &body, &cond)) return rc;
+        RMW_CUDA(cudaEventRecord(ev, home));
+        RMW_CUDA(cudaStreamWaitEvent(priv, ev, 0));
+        if (cudaStreamBeginCaptureToGraph(priv, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) !=
+            cudaSuccess) {
+            cudaGraphDestroy(g);
+            return RMW_ERR_CUDA;
+        }
+        *sref = priv;
+        int rc = op(L.xin, L.w);
+        *sref = home;
+        if (rc == RMW_OK) rc = lz_step(L, factor, tol, mk, cond, 1, priv);
+        cudaGraph_t cap = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(priv, &cap);
+        if (rc != RMW_OK || e != cudaSuccess || cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) {
+            exec = nullptr;
+            cudaGraphDestroy(g);
+            cudaGetLastError();
+            return RMW_ERR_CUDA;
+        }
+        graph = g;
+        graph_live(+1);
+        graph_count(true);
+        return RMW_OK;
+    }
+
+    int build()
+    {
+        if (capture_stream(home, &priv) != RMW_OK || cudaEventCreateWithFlags(&ev, cudaEventDisableTiming))
+            return RMW_ERR_CUDA;
+        if (capture_once() == RMW_OK) return RMW_OK;
+        // the operator grows its scratch on the capture stream once, then capture again
+        RMW_CUDA(cudaEventRecord(ev, home));
+        RMW_CUDA(cudaStreamWaitEvent(priv, ev, 0));
+        *sref = priv;
+        const int rc = op(L.xin, L.w);
+        *sref = home;
+        RMW_CUDA(cudaEventRecord(ev, priv));
+        RMW_CUDA(cudaStreamWaitEvent(home, ev, 0));
+        if (rc) return rc;
+        return capture_once();
+    }
+
+    // iterations until the kernel clears the loop condition
+    int run_loop()
+    {
+        if (graphs_enabled() && !graph_failed) {
+            if (!exec && build() != RMW_OK) {
+                cudaGetLastError();
+                graph_failed = true;
+            }
+            if (exec) {
+                void *tok = nullptr;
+                if (int rc = trace_begin(TRACE_CYCLE, home, &tok)) return rc;
+                RMW_CUDA(cudaGraphLaunch(exec, home));
+                if (int rc = trace_end(tok, home)) return rc;
+                graph_count(false);
+                return RMW_OK;
+            }
+        }
+        for (;;) {
+            void *tok = nullptr;
+            if (int rc = trace_begin(TRACE_OPERATOR, home, &tok)) return rc;
+            if (int rc = op(L.xin, L.w)) return rc;
+            if (int rc = trace_end(tok, home)) return rc;
+            if (int rc = trace_begin(TRACE_KRYLOV, home, &tok)) return rc;
+            if (int rc = lz_step(L, factor, tol, mk, 0, 0, home)) return rc;
+            if (int rc = trace_end(tok, home)) return rc;
+            LzState S;
+            if (int rc = lz_fetch_state(L, &S)) return rc;
+            if (!S.more) break;
+        }
+        return RMW_OK;
+    }
+
+    // noise_s = factor M_s^(1/2) z_s per segment; iters per segment (the
+    // reference's count: the index of the converged iteration, max_iter if none)
+    // require_nonzero: a zero z is an error (the single-vector entry points), not a zero noise
+    int run(const double *z, double *noise, double factor_, double tol_, int max_iter, int kcap,
+            const std::vector<long long> &seg_off, std::vector<int> &iters, const LzMask &mask = LzMask(),
+            bool require_nonzero = false)
+    {
+        factor = factor_;
+        tol = tol_;
+        mk = mask;
+        if (int rc = L.init(seg_off, kcap, home)) return rc;
+        std::vector<double> zn;
+        std::vector<int> run;
+        if (int rc = lz_begin(L, z, factor, max_iter, zn, run)) return rc;
+        int n_run = 0;
+        for (int s = 0; s < L.nseg; ++s) {
+            if (!std::isfinite(zn[s]) || (require_nonzero && factor != 0.0 && !(zn[s] > 0.0)))
+                return fail(RMW_ERR_NONFINITE, "Lanczos: |z| is zero or not finite");
+            n_run += run[s];
+        }
+        if (mk.mask) {
+            // the first operator application: every running segment
+            const int npass = (mk.nrhs + mk.pass - 1) / mk.pass;
+            std::vector<unsigned char> h((size_t)npass * mk.nsusp, 0);
+            for (int p = 0; p < npass; ++p)
+                for (int u = 0; u < mk.nsusp; ++u)
+                    for (int q = p * mk.pass; q < std::min(mk.nrhs, (p + 1) * mk.pass); ++q)
+                        h[(size_t)p * mk.nsusp + u] |= run[(size_t)q * mk.nsusp + u] ? 1 : 0;
+            RMW_CUDA(cudaMemcpyAsync(mk.mask, h.data(), h.size(), cudaMemcpyHostToDevice, home));
+            RMW_CUDA(cudaStreamSynchronize(home));
+        }
+        while (n_run > 0) {
+            if (int rc = run_loop()) return rc;
+            LzState S;
+            if (int rc = lz_fetch_state(L, &S)) return rc;
+            if (S.bar.err) return fail(RMW_ERR_CUDA, "Lanczos: a grid barrier of the step kernel timed out");
+            if (S.live > 0 && S.i <= max_iter && S.i < L.kcap && S.i + 1 >= L.vcap) {
+                if (int rc = L.grow(2 * L.vcap)) return rc;
+                continue;
+            }
+            break;
+        }
+        if (n_run == 0) {
+            RMW_CUDA(cudaMemsetAsync(noise, 0, sizeof(double) * L.n, home));
+            iters.assign(L.nseg, 0);
+            RMW_CUDA(cudaStreamSynchronize(home));
+            return RMW_OK;
+        }
+        return lz_finish(L, noise, iters);
+    }
+};
 
 // The engine: buffers, the captured cycle graph and the solve loop.
 // pcop(x, y): y = A P^-1 x, launched on *sref (the engine redirects it to its
@@ -233,10 +458,17 @@ struct GmresDevice {
     // x_s = A^-1 b_s per segment from x = 0, to |b_s - A x_s| <= tol_rel[s] |b_s|.
     // op(x, y): y = A x; pc(x, y): y = P^-1 x.  hist: per segment and step, the
     // residual estimate |g_{j+1}| / |b_s| (segment-major, hist_cap per segment).
+    //
+    // trust_estimate: when every running segment's Givens estimate met its
+    // tolerance in a cycle, return without the closing true residual b - A x
+    // (relres is then the estimate).  The inner solves of iterative refinement
+    // use it: the outer loop recomputes the residual anyway.  Otherwise K.r
+    // holds b - A x of the returned x (the inner solves of the residual
+    // recurrence reuse it as their next residual).
     template <typename Op, typename Pc>
     int solve(Op op, Pc pc, const double *b, double *x_out, const std::vector<double> &tol_rel, int maxiter,
               std::vector<int> &iters, std::vector<double> &relres, std::vector<int> &status,
-              std::vector<double> *hist = nullptr)
+              std::vector<double> *hist = nullptr, bool trust_estimate = false)
     {
         const int ns = K.nseg;
         const long long n = K.n;
@@ -268,18 +500,37 @@ struct GmresDevice {
             if (int rc = run_steps()) return rc;
             KState S;
             if (int rc = kd_fetch_cycle(K, &S, ints.data())) return rc;
-            if (S.err) return fail(RMW_ERR_CUDA, "GMRES: a grid barrier of the Arnoldi step timed out");
+            if (S.bar.err) return fail(RMW_ERR_CUDA, "GMRES: a grid barrier of the Arnoldi step timed out");
             for (int s = 0; s < ns; ++s)
                 if (ints[3 * ns + s] & 2) return fail(RMW_ERR_BREAKDOWN, "GMRES: non-finite Arnoldi vector");
             // x += P^-1 V y
             if (int rc = kd_cycle_solution(K, S.j)) return rc;
             if (int rc = pc(K.t1, K.t2)) return rc;
             if (int rc = kd_axpby(K, K.t2, K.x, 1.0, 1.0)) return rc;
+            if (trust_estimate) {
+                bool all = true;
+                for (int s = 0; s < ns; ++s) all = all && (!act[s] || (ints[3 * ns + s] & 4));
+                if (all) {
+                    std::vector<double> ge(ns);
+                    RMW_CUDA(cudaMemcpyAsync(ge.data(), K.gres, sizeof(double) * ns, cudaMemcpyDeviceToHost, st));
+                    RMW_CUDA(cudaStreamSynchronize(st));
+                    for (int s = 0; s < ns; ++s) {
+                        iters[s] = ints[s];
+                        if (!act[s]) continue;
+                        relres[s] = ge[s] / bnorm[s];
+                        status[s] = RMW_OK;
+                        act[s] = 0;
+                    }
+                    n_active = 0;
+                    break;
+                }
+            }
             // r = b - A x
             if (int rc = op(K.x, K.r)) return rc;
             if (int rc = kd_axpby(K, b, K.r, 1.0, -1.0)) return rc;
             if (int rc = kd_seg_norm2(K, K.r)) return rc;
             if (int rc = kd_fetch_norms(K, nr.data())) return rc;
+            RMW_CUDA(cudaMemsetAsync(K.flags, 0, sizeof(int) * ns, st));  // estimate flags are per cycle
             n_active = 0;
             for (int s = 0; s < ns; ++s) {
                 iters[s] = ints[s];

@@ -81,3 +81,66 @@ def test_device_cycles_are_deterministic(switches):
     a = integrator.solve_mobility_problem(s, FT, tol=1e-8, mode="mixed")[0].cpu().numpy()
     b = integrator.solve_mobility_problem(s, FT, tol=1e-8, mode="mixed")[0].cpu().numpy()
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+@pytest.mark.parametrize("tol", [1e-3, 1e-10])
+def test_device_lanczos_matches_host_loop(switches, mode, tol):
+    """Device-resident Lanczos (fused step kernel with the reorthogonalisation pass and the tridiagonal
+    eigen-solve on the device, graph while loop) against the host-driven recurrence: same iteration count,
+    same noise to round-off.  tol 1e-10 runs past the basis' first 32 vectors (the host doubles it)."""
+    s, _ = _suspension(24, 13)
+    s.build_pc(stochastic=True, mode=mode)
+    z = np.random.default_rng(6).standard_normal(3 * s.n_blobs)
+    out = {}
+    for dev in (True, False):
+        _native.use_device_krylov(dev)
+        noise, it = s.lanczos(z, factor=np.sqrt(2.0 / 1e-3), tol=tol, mode=mode, max_iter=200)
+        out[dev] = (noise.cpu().numpy(), it)
+    assert out[True][1] == out[False][1]
+    if tol < 1e-6:
+        assert out[True][1] > 32
+    assert rel_err(out[True][0], out[False][0]) <= 1e-9
+
+
+def test_device_lanczos_max_iter_and_zero_factor(switches):
+    s, _ = _suspension(8, 2)
+    s.build_pc(stochastic=True)
+    z = np.random.default_rng(1).standard_normal(3 * s.n_blobs)
+    res = {}
+    for dev in (True, False):
+        _native.use_device_krylov(dev)
+        noise, it = s.lanczos(z, factor=1.0, tol=1e-16, max_iter=5)
+        res[dev] = (noise.cpu().numpy(), it)
+        zero, it0 = s.lanczos(z, factor=0.0)
+        assert it0 == 0 and float(zero.abs().max()) == 0.0
+    assert res[True][1] == res[False][1] == 5
+    assert rel_err(res[True][0], res[False][0]) <= 1e-10
+
+
+def test_device_batched_solve_and_lanczos_match_host_loop(switches):
+    counts = [9, 20, 14, 5]
+    shells = [S.shells(c, S.icosahedron(1.0), 60 + k, 15.0, 1.2, 4.0, a=0.4) for k, c in enumerate(counts)]
+    r = np.concatenate([sh.r_vectors() for sh in shells])
+    x = np.concatenate([sh.locations for sh in shells])
+    s = RigidSystem([12] * sum(counts), 1.0, 0.4)
+    s.set_configuration(r, x)
+    s.set_suspensions(counts)
+    s.build_pc(stochastic=True)
+    rng = np.random.default_rng(11)
+    rhs = rng.standard_normal(s.size)
+    Z = rng.standard_normal((5, 3 * s.n_blobs))
+    out = {}
+    for dev in (True, False):
+        _native.use_device_krylov(dev)
+        for mode in ("fp64", "mixed"):
+            sol, it, rr, stt = s.solve_batched(rhs, tol=1e-8, mode=mode)
+            noise, itl = s.lanczos_batched(Z, factor=1.0, tol=1e-4, mode=mode)
+            assert (np.asarray(stt) == 0).all() and (np.asarray(rr) <= 1e-8).all()
+            out[(dev, mode)] = (sol.cpu().numpy(), np.asarray(it), noise.cpu().numpy(), np.asarray(itl))
+    for mode in ("fp64", "mixed"):
+        d, h = out[(True, mode)], out[(False, mode)]
+        assert (d[3] == h[3]).all()
+        assert rel_err(d[2], h[2]) <= 1e-9
+        assert np.abs(d[1] - h[1]).max() <= (0 if mode == "fp64" else 1)
+        assert rel_err(d[0], h[0]) <= 1e-8

@@ -65,7 +65,8 @@ def test_graph_replayed_solve_matches_direct(cuda_device, mode):
         caps, reps = _native.graph_stats(reset=True)
     finally:
         _native.use_graphs(True)
-    assert caps >= 1 and reps >= it1 - 2
+    # device-resident GMRES: one graph launch per restart cycle (every Arnoldi step of the cycle inside it)
+    assert caps >= 1 and reps >= 1
     assert info0 == info1 == 0 and it0 == it1
     assert rel_err(x1.cpu().numpy(), x0.cpu().numpy()) <= 1e-13
 

@@ -98,9 +98,22 @@ def test_device_lanczos_matches_host_loop(switches, mode, tol):
         noise, it = s.lanczos(z, factor=np.sqrt(2.0 / 1e-3), tol=tol, mode=mode, max_iter=200)
         out[dev] = (noise.cpu().numpy(), it)
     assert out[True][1] == out[False][1]
-    if tol < 1e-6:
-        assert out[True][1] > 32
     assert rel_err(out[True][0], out[False][0]) <= 1e-9
+
+
+def test_device_lanczos_grows_its_basis(switches):
+    """A tolerance no iteration meets runs max_iter = 50 iterations: past the first 32 basis vectors, where
+    the device loop returns to the host to double the basis and continues; same result as the host loop."""
+    s, _ = _suspension(12, 17)
+    s.build_pc(stochastic=True)
+    z = np.random.default_rng(9).standard_normal(3 * s.n_blobs)
+    out = {}
+    for dev in (True, False):
+        _native.use_device_krylov(dev)
+        noise, it = s.lanczos(z, factor=1.0, tol=1e-16, max_iter=50)
+        out[dev] = (noise.cpu().numpy(), it)
+    assert out[True][1] == out[False][1] == 50
+    assert rel_err(out[True][0], out[False][0]) <= 1e-8
 
 
 def test_device_lanczos_max_iter_and_zero_factor(switches):

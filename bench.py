@@ -82,7 +82,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=8.0)
     p.add_argument("--large", action="store_true",
                    help="only run the 4096-shell (172,032-blob) solve comparison and print its JSON line")
-    p.add_argument("--large-modes", default="mixed+nf,mixed,df64,fp64")
+    p.add_argument("--large-modes", default="fp64,mixed,mixed+exact,mixed+learned_band,mixed+exact+learned")
     p.add_argument("--multi", default=None, metavar="N:NRHS",
                    help="only time the multi-right-hand-side M_UF product on N blobs with NRHS vectors")
     p.add_argument("--product", default=None, metavar="KIND:MODE",
@@ -364,25 +364,27 @@ def solve_breakdown(fn):
     return res, out
 
 
-def train_nearfield(shell, a, z_range, dev, n_samples=2048, steps=2000, seed=11):
-    """Near-field coupling network for one shell type: two-body training data
-    from the plain method on the GPU (centre distances 2R+2a .. 6R, heights in
-    z_range) and Adam on the GPU.  Returns (model, info)."""
+def train_nearfield(shell, a, z_range, dev, n_clusters=1024, steps=2000, seed=11):
+    """Message-passing near-field network for one shell type: clusters of 2..8 bodies (centre distances
+    2R+2a .. 6R, heights in z_range) whose pair couplings the plain method computes on the GPU, then Adam
+    on the GPU.  Returns (model, info)."""
     import torch
     from rigidmultiblobswall_gb300 import nearfield as nf
     R = float(np.linalg.norm(shell[0]))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    feat, targ = nf.pair_training_data(shell, a, 1.0, n_samples, d_range=(2 * R + 2 * a, 6 * R), z_range=z_range,
-                                       seed=seed, device=dev)
+    graphs = nf.cluster_training_data(shell, a, 1.0, n_clusters, d_range=(2 * R + 2 * a, 6 * R), z_range=z_range,
+                                      seed=seed, device=dev)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     model = nf.NearfieldModel(body_radius=R, cutoff=6 * R, seed=2)
-    hist = model.train(feat, targ, steps=steps, batch=512, lr=2e-3)
+    hist = model.train(graphs, steps=steps, lr=2e-3)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    return model, {"samples": 2 * n_samples, "data_ms": (t1 - t0) * 1e3, "train_ms": (t2 - t1) * 1e3,
-                   "steps": steps, "loss_first": float(hist[:10].mean()), "loss_last": float(hist[-50:].mean())}
+    return model, {"clusters": n_clusters, "bodies_per_cluster": [2, 8], "graphs": len(graphs),
+                   "pairs": int(sum(g.n_band for g in graphs)), "data_ms": (t1 - t0) * 1e3,
+                   "train_ms": (t2 - t1) * 1e3, "steps": steps, "loss_first": float(hist[:10].mean()),
+                   "loss_last": float(hist[-50:].mean())}
 
 
 def solver_metrics(dev, reps=2):
@@ -520,72 +522,157 @@ def solver_metrics(dev, reps=2):
     return out
 
 
-def large_solve(args):
-    """4096 42-blob shells at area fraction 0.3, force (0,0,-1) per body: block-diagonal preconditioned GMRES
-    to a 1e-8 relative residual in each precision mode, on one GPU.  The plain FP64 solve is the baseline
-    the mixed-precision solve is compared against.  A mode "<mode>+nf" uses the near-field augmented
-    preconditioner (exact pairs < 3R, learned couplings 3R..6R from a network trained here first)."""
+def cpu_solve_baselines():
+    """The reference's solve path on the host cores: its Python structure (restated by the oracle:
+    linear_operator_rigid, the block-diagonal preconditioner, right-preconditioned restarted GMRES,
+    Lanczos; multi_bodies.py:424-471, 752-903, general_application_utils.py:514-635,
+    stochastic_forcing.py:112-264) with the oracle's restatement of the reference C++ product
+    (mobility/mobility.cpp:256-430, symmetric loop, OpenMP over all host cores) as the matvec - the
+    configuration a user of the reference runs with mobility_vector_prod_implementation = C++.
+    256-shell solve to 1e-8, and one 1024 x 12-blob Euler-Maruyama step (Lanczos 1e-3, GMRES 1e-8)."""
+    from oracle import rigid as orc
+    from oracle import wall
+    from rigidmultiblobswall_gb300 import suspensions as S
+    threads = os.cpu_count() or 1
+
+    class FastRigid(orc.Rigid):
+        def mobility(self, v):
+            return wall.uf_symmetric_fast(self.r, v, self.eta, self.a, threads=threads)
+
+    out = {}
+    s2 = S.shells_42_256()
+    r2 = s2.r_vectors()
+    o = FastRigid(r2, s2.locations, 42 * np.arange(s2.n_bodies + 1), s2.eta, s2.a)
+    FT = np.zeros((s2.n_bodies, 6))
+    FT[:, 2] = -1.0
+    rhs = np.concatenate([np.zeros(3 * len(r2)), -FT.reshape(-1)])
+    t0 = time.perf_counter()
+    o.build_pc()
+    x, it, rel = orc.gmres_right(o.apply, o.apply_pc, rhs / np.linalg.norm(rhs), tol=1e-8)
+    dt = time.perf_counter() - t0
+    out["solve_shells42x256"] = {"ms": dt * 1e3, "iterations": it, "relres": rel, "cores": threads,
+                                 "kind": "port"}
+    s3 = S.shells_12_1024()
+    r3 = s3.r_vectors()
+    o3 = FastRigid(r3, s3.locations, 12 * np.arange(s3.n_bodies + 1), s3.eta, s3.a)
+    FT3 = np.zeros((s3.n_bodies, 6))
+    FT3[:, 2] = -1.0
+    z = np.random.default_rng(3).standard_normal(3 * len(r3))
+    dtm = 1e-3
+    t0 = time.perf_counter()
+    o3.build_pc()
+    raw, itl = orc.lanczos(o3.mobility_pc, z, factor=np.sqrt(2.0 / dtm), tol=1e-3)
+    noise = o3.P_inv_mult(raw)
+    b3 = np.concatenate([-noise, -FT3.reshape(-1)])
+    nrm = np.linalg.norm(b3)
+    x3, it3, rel3 = orc.gmres_right(o3.apply, o3.apply_pc, b3 / nrm, tol=1e-8)
+    orc.em_update(s3.locations, s3.quaternions, (x3 * nrm)[3 * len(r3):], dtm)
+    dt3 = time.perf_counter() - t0
+    out["bd_step_shells12x1024"] = {"ms": dt3 * 1e3, "lanczos_iterations": itl, "gmres_iterations": it3,
+                                    "relres": rel3, "cores": threads, "kind": "port"}
+    out["sample"] = ("one full solve / step each; oracle numpy restatement of the reference's Python solve path "
+                     "with the oracle's restatement of the reference C++ symmetric product as the matvec")
+    return out
+
+
+def oracle_residual_sampled(r, locs, offsets, eta, a, sol, FT, n_rows=1024, seed=0):
+    """The oracle's relative residual |b - A x| / |b| of a rigid solution, estimated from every body row
+    (-K^T lambda = -F) and n_rows sampled blob rows (M lambda - K U = 0, the oracle's all-source product on
+    those rows); the sampled part is scaled up to all blob rows."""
+    from oracle import wall
+    from oracle import rigid as orc
+    N = len(r)
+    lam, U = sol[:3 * N], sol[3 * N:]
+    Ks = orc.K_bodies(r, locs, offsets)
+    rb = orc.KT_mult(Ks, offsets, lam) - FT.reshape(-1)
+    rows = np.sort(np.random.default_rng(seed).choice(N, min(n_rows, N), replace=False))
+    Ml = wall.wall_product("uf", r, lam, eta, a, rows=rows)
+    body = np.searchsorted(offsets, rows, side="right") - 1
+    d = r[rows] - locs[body]
+    KU = U.reshape(-1, 6)[body, :3] + np.cross(U.reshape(-1, 6)[body, 3:], d)
+    rs = Ml - KU.reshape(-1)
+    est = np.sqrt(rb @ rb + (N / rows.size) * (rs @ rs))
+    return float(est / np.linalg.norm(FT)), int(rows.size)
+
+
+def cfg5_metrics(dev, modes=("fp64", "mixed", "mixed+exact", "mixed+learned_band", "mixed+exact+learned")):
+    """4096 42-blob shells at area fraction 0.3, force (0,0,-1) per body: preconditioned GMRES to a 1e-8
+    relative residual, on one GPU.  Arms: plain block-diagonal FP64 (the baseline), mixed precision, and
+    mixed precision with the near-field augmented preconditioner - exact blob-level couplings below 3R
+    only ("exact"), learned mode couplings of the outer band 3R..6R only ("learned_band"), and both
+    ("exact+learned").  Each arm's time covers its preconditioner build (FP64 or FP32), the near-field
+    attach and the solve; the network is trained once before (time reported).  Every solution's relative
+    residual is also estimated by the oracle (all body rows, 1024 sampled blob rows)."""
     import torch
-    from rigidmultiblobswall_gb300 import build as B
     from rigidmultiblobswall_gb300 import integrator
+    from rigidmultiblobswall_gb300 import nearfield as nf
     from rigidmultiblobswall_gb300 import suspensions as S
     from rigidmultiblobswall_gb300.rigid import RigidSystem
+    s5 = S.shells_42_4096()
+    r5 = s5.r_vectors()
+    sys5 = RigidSystem([42] * s5.n_bodies, s5.eta, s5.a, device=dev)
+    sys5.set_configuration(r5, s5.locations)
+    FT = np.zeros((s5.n_bodies, 6))
+    FT[:, 2] = -1.0
+    R5 = float(np.linalg.norm(s5.shell[0]))
+    out = {"workload": "4096 shells x 42 blobs = 172,032 blobs, area fraction 0.3, z in [1.1R, 3R], F=(0,0,-1)",
+           "tol": 1e-8, "restart": 60, "exact_cutoff": "3R", "learned_band": "3R..6R", "message_cutoff": "3R"}
+    model = None
+    if any("learned" in m for m in modes):
+        model, out["nearfield_training"] = train_nearfield(s5.shell, s5.a, (1.1 * R5, 3 * R5), dev)
+    sols = {}
+    for mode in modes:
+        parts = mode.split("+")
+        base = parts[0]
+        exact = "exact" in parts
+        learned = "learned_band" in parts or "learned" in parts
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sys5.build_pc(mode="mixed" if base == "mixed" else base)
+        pairs = None
+        if learned:
+            pairs = model.attach(sys5, exact_cutoff=3 * R5 if exact else 0.0, learned_from=3 * R5)
+        elif exact:
+            pairs = nf.attach_exact(sys5, 3 * R5)
+        sol, info, its, rr = integrator.solve_mobility_problem(sys5, FT, tol=1e-8, mode=base)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if pairs is not None:
+            nf.detach(sys5)
+        x = sol.cpu().numpy()
+        sols[mode] = x[3 * sys5.n_blobs:]
+        est, nrows = oracle_residual_sampled(r5, s5.locations, sys5.offsets, s5.eta, s5.a, x, FT)
+        out[mode] = {"ms": dt * 1e3, "iterations": its, "relres": rr, "info": info,
+                     "oracle_relres_estimate": est, "oracle_rows_sampled": nrows}
+        if pairs is not None:
+            out[mode]["pairs_exact_learned"] = list(pairs)
+    ref = sols.get("fp64")
+    for mode, u in sols.items():
+        if ref is not None:
+            out[mode]["velocity_rel_err_vs_fp64"] = float(np.linalg.norm(u - ref) / np.linalg.norm(ref))
+    if "fp64" in out:
+        for mode in modes:
+            if mode != "fp64":
+                out["speedup_%s_vs_fp64" % mode] = out["fp64"]["ms"] / out[mode]["ms"]
+    for m1, m2 in (("mixed+exact+learned", "mixed+exact"), ("mixed+learned_band", "mixed")):
+        if m1 in out and m2 in out:
+            out["gain_%s_over_%s" % (m1, m2)] = {"ms_ratio": out[m2]["ms"] / out[m1]["ms"],
+                                                 "iterations": [out[m2]["iterations"], out[m1]["iterations"]]}
+    sys5.close()
+    return out
+
+
+def large_solve(args):
+    """--large: only the 4096-shell solve comparison (modes from --large-modes), as one JSON line."""
+    import torch
+    from rigidmultiblobswall_gb300 import build as B
     B.build()
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    # warm-up on 4 shells in every mode: the first use of each torch elementwise kernel in a process
-    # costs seconds on this image (PyTorch's own kernels are compiled for the GPU at first launch)
-    sw = S.shells_42_256(n_bodies=4, seed=9)
-    sysw = RigidSystem([42] * 4, sw.eta, sw.a, device=dev)
-    sysw.set_configuration(sw.r_vectors(), sw.locations)
-    for m in ("fp64", "df64", "mixed"):
-        integrator.solve_mobility_problem(sysw, np.ones((4, 6)), tol=1e-8, mode=m)
-    sysw.close()
-    s5 = S.shells_42_4096()
-    sys5 = RigidSystem([42] * s5.n_bodies, s5.eta, s5.a, device=dev)
-    sys5.set_configuration(s5.r_vectors(), s5.locations)
-    FT = np.zeros((s5.n_bodies, 6))
-    FT[:, 2] = -1.0
-    out = {"workload": "4096 shells x 42 blobs = 172,032 blobs, area fraction 0.3, z in [1.1R, 3R], F=(0,0,-1)",
-           "tol": 1e-8, "restart": 60}
     clocks = ClockSampler(0)
     clocks.start()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    sys5.build_pc()
-    torch.cuda.synchronize()
-    out["pc_build_ms"] = (time.perf_counter() - t0) * 1e3
-    sols = {}
-    model = None
-    from rigidmultiblobswall_gb300 import nearfield as nf
-    R5 = float(np.linalg.norm(s5.shell[0]))
-    for mode in args.large_modes.split(","):
-        aug = mode.endswith("+nf")
-        base = mode[:-3] if aug else mode
-        if aug and model is None:
-            model, out["nearfield_training"] = train_nearfield(s5.shell, s5.a, (1.1 * R5, 3 * R5), dev)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        pairs = model.attach(sys5, exact_cutoff=3 * R5) if aug else None
-        (sol, info, its, rr), arn = arnoldi_traffic(
-            lambda: integrator.solve_mobility_problem(sys5, FT, tol=1e-8, mode=base))
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        if aug:
-            nf.detach(sys5)
-        sols[mode] = sol[3 * sys5.n_blobs:].cpu().numpy()
-        out["solve_" + mode] = {"ms": dt * 1e3, "iterations": its, "relres": rr, "info": info, "arnoldi": arn}
-        if aug:
-            out["solve_" + mode]["pairs_exact_learned"] = list(pairs)
+    out = cfg5_metrics(dev, tuple(args.large_modes.split(",")))
     out["clocks"] = clocks.stop()
-    ref = sols.get("fp64", sols.get("df64"))
-    for mode, u in sols.items():
-        if ref is not None:
-            out["solve_" + mode]["velocity_rel_err_vs_fp64"] = float(np.linalg.norm(u - ref) / np.linalg.norm(ref))
-    for base in ("fp64", "df64"):
-        for fast in ("mixed", "mixed+nf"):
-            if base in sols and fast in sols:
-                out["speedup_%s_vs_%s" % (fast, base)] = out["solve_" + base]["ms"] / out["solve_" + fast]["ms"]
     print(json.dumps(out))
 
 
@@ -900,10 +987,19 @@ def main():
     solver = {} if args.no_extras else solver_metrics(dev)
     if not args.no_extras:
         solver["batched_64_suspensions"] = batched_metrics(dev)
+        solver["cfg5_solve_shells42x4096"] = cfg5_metrics(dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(r, f, eta, a, args.cpu_seconds)
+        if not args.no_extras:
+            cb = cpu_solve_baselines()
+            solver["cpu_baseline_solves"] = cb
+            for key, gkey in (("solve_shells42x256", "solve_shells42x256_mixed"),
+                              ("bd_step_shells12x1024", "bd_step_shells12x1024_mixed")):
+                if gkey in solver:
+                    solver[gkey]["cpu_baseline"] = cb[key]
+                    solver[gkey]["speedup_vs_cpu_baseline"] = cb[key]["ms"] / solver[gkey]["ms"]
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": ws, "steps": args.steps,

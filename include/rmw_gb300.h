@@ -354,33 +354,68 @@ int rmw_rigid_lanczos_batched(void *handle, const double *Z, double *noise, int 
  * inter-body blob block of M.  The augmented form adds the first Neumann term
  * of the near blocks: y = P0 x, v_i = sum_{j near i} M_ij lambda_j(y),
  * y <- y - P0 [v; 0].  Pairs closer than an exact cutoff use the blob-level
- * blocks; from there to the network's cutoff a small network (3 -> 64 -> 64
- * -> 64 -> 121, SiLU, BF16 weights, FP32 accumulation on the tensor cores)
- * predicts the 11x11 coupling of the bodies' low-order modes (3 translations,
- * 3 rotations, 5 strains) from the horizontal distance and both heights. */
+ * blocks; pairs in the learned band use the 11x11 coupling of the bodies'
+ * low-order modes (3 translations, 3 rotations, 5 strains) that a
+ * message-passing network predicts: body embeddings from (z/R, neighbour
+ * count), three rounds of messages between bodies closer than the message
+ * cutoff (3R by default), and a readout per learned pair from both
+ * embeddings and the pair's (horizontal distance, z_i, z_j)/R; width 64,
+ * SiLU, BF16 weights and activations, FP32 accumulation on the tensor cores
+ * in the forward and the backward pass. */
 /* 11x11 mode couplings G_01, G_10 (lab frame, row-major; 242 doubles per
  * sample) of every pair of handle bodies (2s, 2s+1); call after
  * rmw_rigid_build_pc.  Training data. */
 int rmw_rigid_pair_coupling(void *handle, double *out);
+/* The same coupling G_ij (lab frame, 121 doubles each) for n_pairs arbitrary
+ * ordered pairs (pairs: 2 n_pairs ints on the device, (i, j) per pair) of the
+ * handle's bodies: the targets of few-body training clusters.  Synchronous. */
+int rmw_rigid_pair_coupling_list(void *handle, const int *pairs, int64_t n_pairs, double *out);
+
+/* A graph for the message-passing network (device arrays, int32 indices).
+ * Nodes are bodies; node_feat holds (z/R, degree/8) per node.  Message edges
+ * (dst <- src) are sorted by dst with CSR offsets mp_off (n_nodes + 1) and
+ * mp_rev[e] = the index of the reverse edge; band edges (i <- j), whose
+ * coupling G_ij is predicted, are sorted by i with band_off and band_rev.
+ * Edge features: (horizontal distance, z_dst, z_src)/R.  target: n_band x 121
+ * couplings in each pair's frame (x axis along the horizontal separation),
+ * training only; the reverse-edge arrays are needed for training only. */
+typedef struct {
+    int32_t n_nodes, n_mp, n_band;
+    const float *node_feat;
+    const int32_t *mp_src, *mp_dst, *mp_off, *mp_rev;
+    const float *mp_feat;
+    const int32_t *band_i, *band_j, *band_off, *band_rev;
+    const float *band_feat;
+    const float *target;
+} rmw_graph;
+
 int rmw_nearfield_create(void **net, double body_radius, double cutoff, unsigned long long seed);
 int rmw_nearfield_destroy(void *net);
-int rmw_nearfield_sizes(int *n_weights, int *n_biases, int *n_in, int *width, int *n_out, int *n_target);
+/* the message cutoff (default 3R) and the learned band's outer cutoff */
+int rmw_nearfield_set_cutoffs(void *net, double mp_cutoff, double cutoff);
+int rmw_nearfield_sizes(int *n_weights, int *n_biases, int *n_norm, int *width, int *n_out, int *n_target);
 int rmw_nearfield_get(void *net, float *w_host, float *b_host, float *norm_host);
 int rmw_nearfield_set(void *net, const float *w_host, const float *b_host, const float *norm_host);
-/* forward / gradient on host batches of normalised inputs (tests, checks) */
-int rmw_nearfield_forward(void *net, const float *X_host, int P, float *Y_host);
-int rmw_nearfield_grad(void *net, const float *X_host, const float *T_host, int P, float *gW_host, float *gb_host,
-                       float *loss_host);
-/* Adam on device data: feat (S x 3: horizontal distance, z_i, z_j over the
- * body radius), targ (S x 121: pair-frame mode coupling).  Synchronous. */
-int rmw_nearfield_train(void *net, const float *feat, const float *targ, int S, int steps, int batch, float lr,
-                        unsigned long long seed, float *loss_host, void *stream);
+/* forward pass on one graph: out (device) n_band x 121 normalised outputs
+ * (multiply by the target scale of the normalisation block for G) */
+int rmw_nearfield_forward(void *net, const rmw_graph *graph, float *out, void *stream);
+/* gradients of the mean squared error on normalised targets (host outputs) */
+int rmw_nearfield_grad(void *net, const rmw_graph *graph, float *gW_host, float *gb_host, float *loss_host);
+/* Adam over the graphs (one per step, cycling), after setting the
+ * normalisation from their features and targets.  Synchronous. */
+int rmw_nearfield_train(void *net, const rmw_graph *graphs, int n_graphs, int steps, float lr, float *loss_host,
+                        void *stream);
 /* Switch a handle's preconditioner (after rmw_rigid_build_pc) to the
  * augmented form: exact couplings below exact_cutoff, learned ones from there
  * to the network's cutoff (net may be NULL).  net == NULL with exact_cutoff <= 0
  * restores the block-diagonal form.  n_pairs_host (optional): 2 entries,
  * ordered exact and learned pair counts.  Synchronous. */
 int rmw_rigid_set_nearfield(void *handle, void *net, double exact_cutoff, int64_t *n_pairs_host);
+/* The same with the learned band starting at max(learned_from, exact_cutoff):
+ * learned_from = exact_cutoff = 0 learns every pair below the network's
+ * cutoff; exact_cutoff = 0 < learned_from learns only the outer band. */
+int rmw_rigid_set_nearfield_bands(void *handle, void *net, double exact_cutoff, double learned_from,
+                                  int64_t *n_pairs_host);
 
 /* ---- generic Krylov solvers with caller-supplied operators ------------
  * op(ctx, x, y) must write y = A x for device vectors of length n, enqueue its

@@ -1,9 +1,7 @@
 """Oracle (test infrastructure only) for the near-field augmented
 preconditioner: numpy restatements of
-* the network's forward and backward passes with the same BF16 rounding of
-  weights, inputs and hidden activations (round-to-nearest-even), FP64
-  accumulation, SiLU activations and straight-through gradients for the
-  rounding - the CPU check for the GPU training kernels;
+* BF16 rounding (round to nearest even) and the activation the network uses
+  (its forward and backward passes are restated in oracle/mpnn.py);
 * the two-body mode coupling G_ij (11 modes: translations, rotations,
   strains) used as training target;
 * the augmented preconditioner apply y = P0 x - P0 [v; 0] with
@@ -13,9 +11,8 @@ import numpy as np
 
 from . import wall
 
-N_IN, WIDTH, N_OUT, N_FEAT, N_MODES = 16, 64, 128, 3, 11
+N_MODES = 11
 N_TARGET = N_MODES * N_MODES
-LAYERS = [(N_IN, WIDTH), (WIDTH, WIDTH), (WIDTH, WIDTH), (WIDTH, N_OUT)]
 
 
 def bf16(x):
@@ -25,16 +22,6 @@ def bf16(x):
     return u.astype(np.uint32).view(np.float32).reshape(x.shape)
 
 
-def split(w, b):
-    Ws, bs, o, ob = [], [], 0, 0
-    for ni, no in LAYERS:
-        Ws.append(np.asarray(w[o:o + ni * no], dtype=np.float64).reshape(no, ni))
-        o += ni * no
-        bs.append(np.asarray(b[ob:ob + no], dtype=np.float64))
-        ob += WIDTH
-    return Ws, bs
-
-
 def silu(z):
     return z / (1.0 + np.exp(-z))
 
@@ -42,43 +29,6 @@ def silu(z):
 def silu_grad(z):
     s = 1.0 / (1.0 + np.exp(-z))
     return s * (1.0 + z * (1.0 - s))
-
-
-def forward(w, b, X):
-    Ws, bs = split(w, b)
-    A = bf16(X).astype(np.float64)
-    Zs, As = [], [A]
-    for l, (Wt, bb) in enumerate(zip(Ws, bs)):
-        Z = A @ bf16(Wt).astype(np.float64).T + bb
-        Zs.append(Z)
-        if l < len(Ws) - 1:
-            A = bf16(silu(Z)).astype(np.float64)
-            As.append(A)
-        else:
-            A = Z
-    return A[:, :N_TARGET], Zs, As
-
-
-def grad(w, b, X, T):
-    """(gW flat, gb flat, loss) of the mean squared error over P x 36 targets."""
-    Ws, bs = split(w, b)
-    Y, Zs, As = forward(w, b, X)
-    P = X.shape[0]
-    d = Y - T
-    loss = float((d * d).sum() / (P * N_TARGET))
-    dY = np.zeros((P, N_OUT))
-    dY[:, :N_TARGET] = 2.0 * d / (P * N_TARGET)
-    gWs, gbs = [None] * 4, [None] * 4
-    for l in range(3, -1, -1):
-        dZ = dY if l == 3 else dY * silu_grad(Zs[l])
-        gWs[l] = dZ.T @ As[l]
-        gbs[l] = dZ.sum(axis=0)
-        dY = dZ @ bf16(Ws[l]).astype(np.float64)
-    gW = np.concatenate([g.reshape(-1) for g in gWs])
-    gb = np.zeros(3 * WIDTH + N_OUT)
-    for l in range(4):
-        gb[l * WIDTH:l * WIDTH + gbs[l].size] = gbs[l]
-    return gW, gb, loss
 
 
 _S2, _S6 = 1.0 / np.sqrt(2.0), 1.0 / np.sqrt(6.0)

@@ -98,10 +98,13 @@ SIGNATURES = {
     "rmw_nearfield_sizes": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "rmw_nearfield_get": (_i, [_vp, _vp, _vp, _vp]),
     "rmw_nearfield_set": (_i, [_vp, _vp, _vp, _vp]),
-    "rmw_nearfield_forward": (_i, [_vp, _vp, _i, _vp]),
-    "rmw_nearfield_grad": (_i, [_vp, _vp, _vp, _i, _vp, _vp, _vp]),
-    "rmw_nearfield_train": (_i, [_vp, _vp, _vp, _i, _i, _i, ctypes.c_float, ctypes.c_ulonglong, _vp, _vp]),
+    "rmw_nearfield_forward": (_i, [_vp, _vp, _vp, _vp]),
+    "rmw_nearfield_grad": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "rmw_nearfield_train": (_i, [_vp, _vp, _i, _i, ctypes.c_float, _vp, _vp]),
+    "rmw_nearfield_set_cutoffs": (_i, [_vp, _d, _d]),
     "rmw_rigid_set_nearfield": (_i, [_vp, _vp, _d, _vp]),
+    "rmw_rigid_set_nearfield_bands": (_i, [_vp, _vp, _d, _d, _vp]),
+    "rmw_rigid_pair_coupling_list": (_i, [_vp, _vp, _i64, _vp]),
     "rmw_gmres": (_i, [_i64, _vp, _vp, _vp, _vp, _vp, _vp, _d, _i, _i, _vp, ctypes.POINTER(ctypes.c_int),
                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), _i]),
     "rmw_lanczos": (_i, [_i64, _vp, _vp, _vp, _vp, _d, _d, _i, _vp, ctypes.POINTER(ctypes.c_int)]),

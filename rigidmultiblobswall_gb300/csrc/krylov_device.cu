@@ -61,24 +61,24 @@ __device__ void reduce_segment(const double *part, int KP, int j0, int j1, int k
 }
 
 // part[job * KP + q] = sum_{i in job} V_q[i] w[i], q < k (red: k x 32 shared
-// doubles); four basis vectors per pass over the job, so that each thread has
+// doubles); eight basis vectors per pass over the job, so that each thread has
 // several independent loads in flight
 __device__ void job_dots(const double *__restrict__ V, long long ldv, int k, const double *w, const KJob jb,
                          double *part, int KP, int job, double *red)
 {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int q0 = 0; q0 < k; q0 += 4) {
-        const int nq = min(4, k - q0);
+    for (int q0 = 0; q0 < k; q0 += 8) {
+        const int nq = min(8, k - q0);
         const double *V0 = V + (long long)q0 * ldv;
-        double a[4] = {0.0, 0.0, 0.0, 0.0};
+        double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         for (long long i = jb.b + threadIdx.x; i < jb.e; i += blockDim.x) {
             const double wi = w[i];
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
+            for (int u = 0; u < 8; ++u)
                 if (u < nq) a[u] = fma(V0[(long long)u * ldv + i], wi, a[u]);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) a[u] = warp_sum(a[u]);
+        for (int u = 0; u < 8; ++u) a[u] = warp_sum(a[u]);
         if (lane == 0)
             for (int u = 0; u < nq; ++u) red[(q0 + u) * 32 + wid] = a[u];
     }
@@ -185,42 +185,58 @@ __global__ void __launch_bounds__(kKdThreads, 1) arnoldi_step_kernel(StepArgs A)
             Vn[i] = v;
             A.xin[i] = v;
         }
-        if (job == A.sjob[jb.seg] && threadIdx.x == 0 && A.cyc[jb.seg]) {
+        if (job == A.sjob[jb.seg]) {  // uniform over the CTA: it owns this segment's Givens update
             const int s = jb.seg, R = A.R;
+            double *col = red, *cq = red + kKdMaxBasis + 2, *sq = cq + kKdMaxBasis;  // shared scratch
             double *h = A.H + ((long long)s * R + j) * (R + 1);
             double *c = A.cs + (long long)s * R, *sv = A.sn + (long long)s * R, *gs = A.g + (long long)s * (R + 1);
-            for (int q = 0; q <= j; ++q) h[q] = A.hc1[(long long)s * A.KP + q] + A.hc2[(long long)s * A.KP + q];
-            const double hn = sqrt(nw);
-            h[j + 1] = hn;
-            int stop = 0;
-            if (!isfinite(hn)) {
-                A.flags[s] |= 2;  // non-finite Arnoldi vector
-                stop = 1;
-            } else {
-                for (int q = 0; q < j; ++q) {
-                    const double t = c[q] * h[q] + sv[q] * h[q + 1];
-                    h[q + 1] = -sv[q] * h[q] + c[q] * h[q + 1];
-                    h[q] = t;
-                }
-                const double den = hypot(h[j], h[j + 1]);
-                c[j] = (den == 0.0) ? 1.0 : h[j] / den;
-                sv[j] = (den == 0.0) ? 0.0 : h[j + 1] / den;
-                h[j] = c[j] * h[j] + sv[j] * h[j + 1];
-                h[j + 1] = 0.0;
-                gs[j + 1] = -sv[j] * gs[j];
-                gs[j] = c[j] * gs[j];
-                const int it = ++A.iters[s];
-                A.jdone[s] = j + 1;
-                const double res = fabs(gs[j + 1]);
-                if (A.hist && it <= A.hcap) A.hist[(long long)s * A.hcap + it - 1] = res;
-                const bool conv = res <= A.tol_abs[s];
-                A.gres[s] = res;
-                if (conv) A.flags[s] |= 4;                 // the estimate met the tolerance
-                if (hn == 0.0 && !conv) A.flags[s] |= 1;  // breakdown without convergence
-                stop = conv || hn == 0.0 || it >= A.st->maxiter;
+            const bool run = A.cyc[s] != 0;
+            for (int q = threadIdx.x; q <= j; q += blockDim.x)
+                col[q] = A.hc1[(long long)s * A.KP + q] + A.hc2[(long long)s * A.KP + q];
+            for (int q = threadIdx.x; q < j; q += blockDim.x) {
+                cq[q] = c[q];
+                sq[q] = sv[q];
             }
-            if (stop) A.cyc[s] = 0;
-            else atomicAdd(&A.st->active, 1);
+            __syncthreads();
+            if (threadIdx.x == 0 && run) {
+                const double hn = sqrt(nw);
+                col[j + 1] = hn;
+                int stop = 0;
+                if (!isfinite(hn)) {
+                    A.flags[s] |= 2;  // non-finite Arnoldi vector
+                    stop = 1;
+                } else {
+                    for (int q = 0; q < j; ++q) {
+                        const double t = cq[q] * col[q] + sq[q] * col[q + 1];
+                        col[q + 1] = -sq[q] * col[q] + cq[q] * col[q + 1];
+                        col[q] = t;
+                    }
+                    const double den = hypot(col[j], col[j + 1]);
+                    const double cj = (den == 0.0) ? 1.0 : col[j] / den;
+                    const double sj = (den == 0.0) ? 0.0 : col[j + 1] / den;
+                    c[j] = cj;
+                    sv[j] = sj;
+                    col[j] = cj * col[j] + sj * col[j + 1];
+                    col[j + 1] = 0.0;
+                    const double gj = gs[j];
+                    gs[j + 1] = -sj * gj;
+                    gs[j] = cj * gj;
+                    const int it = ++A.iters[s];
+                    A.jdone[s] = j + 1;
+                    const double res = fabs(sj * gj);
+                    if (A.hist && it <= A.hcap) A.hist[(long long)s * A.hcap + it - 1] = res;
+                    const bool conv = res <= A.tol_abs[s];
+                    A.gres[s] = res;
+                    if (conv) A.flags[s] |= 4;                 // the estimate met the tolerance
+                    if (hn == 0.0 && !conv) A.flags[s] |= 1;  // breakdown without convergence
+                    stop = conv || hn == 0.0 || it >= A.st->maxiter;
+                }
+                if (stop) A.cyc[s] = 0;
+                else atomicAdd(&A.st->active, 1);
+            }
+            __syncthreads();
+            if (run)
+                for (int q = threadIdx.x; q <= j + 1; q += blockDim.x) h[q] = col[q];
         }
         __syncthreads();
     }

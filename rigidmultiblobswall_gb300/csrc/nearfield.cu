@@ -31,16 +31,16 @@
 // prediction only costs iterations; the caller compares against the plain
 // solve and falls back.
 //
-// Training data come from two-body configurations through the plain method's
-// own machinery on the GPU: a handle whose bodies are the samples' single
-// shells builds each body's M^-1 (rmw_rigid_build_pc) and pair_fts_kernel
-// forms both G_ij and G_ji of every sample.
+// Training data come from two- to eight-body clusters through the plain
+// method's own machinery on the GPU: a handle whose bodies are the clusters'
+// shells builds each body's M^-1 (rmw_rigid_build_pc) and pair_list_kernel
+// forms G_ij of every ordered pair of a cluster in the learned band.
 //
-// Network: 3 -> 64 -> 64 -> 64 -> 121 (inputs padded to 16, outputs to 128),
-// SiLU activations, BF16 weights and activations, FP32 accumulation on the
-// tensor cores (mma.sync m16n8k16 BF16); backward pass and Adam in FP32 on
-// the CUDA cores with the same BF16-rounded weights (straight-through for the
-// activation rounding).
+// The network (mpnn.cu) is a message-passing network over the bodies: three
+// rounds of messages between bodies closer than its message cutoff, then a
+// readout per learned pair from both bodies' embeddings and the pair's
+// geometry.  Training clusters of two to eight bodies give it neighbourhoods
+// of the sizes it meets in a suspension.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -48,6 +48,7 @@
 #include <cstring>
 #include <vector>
 
+#include "mpnn.cuh"
 #include "pair_math.cuh"
 #include "pair_math_df.cuh"
 #include "rigid.cuh"
@@ -351,275 +352,51 @@ __global__ void pair_fts_kernel(const double *__restrict__ r, const double *__re
     mode_coupling(r, o1, n1, A1, G1, o0, n0, A0, G0, a, nf, P, Lam, V, W, out + 242LL * s + 121);
 }
 
-// ---------------------------------------------------------------------------
-// MLP on the tensor cores
-constexpr int kIn = 16, kWidth = 64, kOut = 128, kLayers = 4;
-constexpr int kFeat = 3, kTarget = kModes * kModes;
-constexpr int kWide = kOut > kWidth ? kOut : kWidth;  // widest layer
-__host__ __device__ constexpr int layer_in(int l) { return l == 0 ? kIn : kWidth; }
-__host__ __device__ constexpr int layer_out(int l) { return l == kLayers - 1 ? kOut : kWidth; }
-__host__ __device__ constexpr int wofs(int l)
+// G_ij (lab frame) of listed ordered pairs (i, j) of the handle's bodies; one
+// CTA per pair, the same steps as pair_fts_kernel.
+__global__ void pair_list_kernel(const double *__restrict__ r, const double *__restrict__ xb,
+                                 const int *__restrict__ boff, const long long *__restrict__ moff,
+                                 const double *__restrict__ minv, const int *__restrict__ pairs, double a, double nf,
+                                 Images P, int max_m, double *__restrict__ out, int *status)
 {
-    return l == 0 ? 0 : (l == 1 ? kIn * kWidth : (l == 2 ? kIn * kWidth + kWidth * kWidth : kIn * kWidth + 2 * kWidth * kWidth));
-}
-constexpr int kNW = kIn * kWidth + 2 * kWidth * kWidth + kWidth * kOut;  // weights (Wt layout: [out][in])
-constexpr int kNB = 3 * kWidth + kOut;                                   // biases
-__host__ __device__ constexpr int bofs(int l) { return l * kWidth; }
-
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
-__device__ __forceinline__ float silu_grad(float z)
-{
-    const float s = 1.0f / (1.0f + __expf(-z));
-    return s * (1.0f + z * (1.0f - s));
-}
-
-__device__ __forceinline__ unsigned pack_bf16x2(const __nv_bfloat16 *p) { return *(const unsigned *)p; }
-
-// Y = act(X W + b) for rows [0, P) (P a multiple of 16); X: P x nin (bf16,
-// row-major), Wt: nout x nin (bf16, row-major), one warp per 16-row tile.
-// Z (optional) keeps the FP32 pre-activations for the backward pass.
-__global__ void mlp_layer_fwd_kernel(const __nv_bfloat16 *__restrict__ X, int nin,
-                                     const __nv_bfloat16 *__restrict__ Wt, const float *__restrict__ bias, int nout,
-                                     float *__restrict__ Z, __nv_bfloat16 *__restrict__ Y, float *__restrict__ Yf,
-                                     int P, int act)
-{
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    const int row0 = warp * 16;
-    if (row0 >= P) return;
-    const int g = lane >> 2, tq = lane & 3;
-    for (int n0 = 0; n0 < nout; n0 += 8) {
-        float c[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int k0 = 0; k0 < nin; k0 += 16) {
-            const int kc = k0 + tq * 2;
-            unsigned a0 = pack_bf16x2(X + (long long)(row0 + g) * nin + kc);
-            unsigned a1 = pack_bf16x2(X + (long long)(row0 + g + 8) * nin + kc);
-            unsigned a2 = pack_bf16x2(X + (long long)(row0 + g) * nin + kc + 8);
-            unsigned a3 = pack_bf16x2(X + (long long)(row0 + g + 8) * nin + kc + 8);
-            unsigned b0 = pack_bf16x2(Wt + (long long)(n0 + g) * nin + kc);
-            unsigned b1 = pack_bf16x2(Wt + (long long)(n0 + g) * nin + kc + 8);
-            asm volatile(
-                "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                "{%0,%1,%2,%3};\n"
-                : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-                : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-        }
-        const int col = n0 + tq * 2;
-        for (int e = 0; e < 4; ++e) {
-            const int rr = row0 + g + (e >= 2 ? 8 : 0), cc = col + (e & 1);
-            const float z = c[e] + bias[cc];
-            const float y = act ? silu(z) : z;
-            if (Z) Z[(long long)rr * nout + cc] = z;
-            if (Y) Y[(long long)rr * nout + cc] = __float2bfloat16_rn(y);
-            if (Yf) Yf[(long long)rr * nout + cc] = y;
-        }
+    extern __shared__ double sh[];
+    const int q = blockIdx.x;
+    const int b0 = pairs[2 * q], b1 = pairs[2 * q + 1];
+    const int o0 = boff[b0], n0 = boff[b0 + 1] - o0, o1 = boff[b1], n1 = boff[b1 + 1] - o1;
+    double *A0 = sh, *A1 = A0 + max_m * kModes, *Lam = A1 + max_m * kModes, *V = Lam + max_m * kModes;
+    double *G0 = V + max_m * kModes, *G1 = G0 + kModes * kModes, *W = G1 + kModes * kModes;
+    double *aug = W + kModes * kModes;
+    __shared__ double c0[3], c1[3];
+    if (threadIdx.x < 3) {
+        c0[threadIdx.x] = xb[3 * b0 + threadIdx.x];
+        c1[threadIdx.x] = xb[3 * b1 + threadIdx.x];
     }
-}
-
-// dY (P x kOut) = 2 (Yf - T) / (P_valid * kTarget) on the first kTarget outputs;
-// the loss is reduced per block (256 threads) and added once per block
-__global__ void mse_grad_kernel(const float *__restrict__ Yf, const float *__restrict__ T, float *__restrict__ dY,
-                                int P, int Pvalid, float *__restrict__ loss)
-{
-    __shared__ float part[8];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    float g = 0.f, l = 0.f;
-    if (i < P * kOut) {
-        const int p = i / kOut, o = i % kOut;
-        if (p < Pvalid && o < kTarget) {
-            const float d = Yf[i] - T[(long long)p * kTarget + o];
-            g = 2.0f * d / (float)(Pvalid * kTarget);
-            l = d * d / (float)(Pvalid * kTarget);
-        }
-        dY[i] = g;
-    }
-    for (int off = 16; off > 0; off >>= 1) l += __shfl_xor_sync(0xffffffffu, l, off);
-    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = l;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        float s = 0.f;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += part[w];
-        atomicAdd(loss, s);
-    }
-}
-
-// dZ = dY * act'(Z)
-__global__ void act_grad_kernel(const float *__restrict__ dY, const float *__restrict__ Z, float *__restrict__ dZ,
-                                int count, int act)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count) dZ[i] = act ? dY[i] * silu_grad(Z[i]) : dY[i];
-}
-
-// gW[o][i] = sum_p dZ[p][o] X[p][i];  gb[o] = sum_p dZ[p][o]   (one thread per weight)
-__global__ void weight_grad_kernel(const float *__restrict__ dZ, const __nv_bfloat16 *__restrict__ X, int nin,
-                                   int nout, int P, float *__restrict__ gW, float *__restrict__ gb)
-{
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nout * (nin + 1)) return;
-    const int o = t / (nin + 1), i = t % (nin + 1);
-    float s = 0.f;
-    if (i < nin)
-        for (int p = 0; p < P; ++p) s += dZ[(long long)p * nout + o] * __bfloat162float(X[(long long)p * nin + i]);
-    else
-        for (int p = 0; p < P; ++p) s += dZ[(long long)p * nout + o];
-    if (i < nin) gW[o * nin + i] = s;
-    else gb[o] = s;
-}
-
-// dX[p][i] = sum_o dZ[p][o] Wt[o][i]
-__global__ void input_grad_kernel(const float *__restrict__ dZ, const __nv_bfloat16 *__restrict__ Wt, int nin,
-                                  int nout, int P, float *__restrict__ dX)
-{
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P * nin) return;
-    const int p = t / nin, i = t % nin;
-    float s = 0.f;
-    for (int o = 0; o < nout; ++o) s += dZ[(long long)p * nout + o] * __bfloat162float(Wt[o * nin + i]);
-    dX[t] = s;
-}
-
-__global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m,
-                            float *__restrict__ v, __nv_bfloat16 *__restrict__ wb, int count, float lr, float b1,
-                            float b2, float c1, float c2, float eps)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
-    const float gi = g[i];
-    const float mi = b1 * m[i] + (1.f - b1) * gi;
-    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
-    m[i] = mi;
-    v[i] = vi;
-    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
-    w[i] = wi;
-    if (wb) wb[i] = __float2bfloat16_rn(wi);
-}
-
-// batch gather: X (P x kIn bf16, normalised features, zero padding) and T (P x kTarget)
-__global__ void gather_batch_kernel(const float *__restrict__ feat, const float *__restrict__ targ, int S,
-                                    const float *__restrict__ fmean, const float *__restrict__ fscale,
-                                    const float *__restrict__ tscale, int P, int Pvalid, unsigned long long seed,
-                                    int step, __nv_bfloat16 *__restrict__ X, float *__restrict__ T)
-{
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P) return;
-    int s = 0;
-    if (p < Pvalid) {
-        unsigned long long x = seed ^ ((unsigned long long)step * 0x9E3779B97F4A7C15ULL) ^ ((unsigned long long)p * 0xD1B54A32D192ED03ULL);
-        x ^= x >> 33; x *= 0xff51afd7ed558ccdULL; x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ULL; x ^= x >> 33;
-        s = (int)(x % (unsigned long long)S);
-    }
-    for (int i = 0; i < kIn; ++i) {
-        const float f = (p < Pvalid && i < kFeat) ? (feat[(long long)s * kFeat + i] - fmean[i]) / fscale[i] : 0.f;
-        X[(long long)p * kIn + i] = __float2bfloat16_rn(f);
-    }
-    if (p < Pvalid)
-        for (int o = 0; o < kTarget; ++o) T[(long long)p * kTarget + o] = targ[(long long)s * kTarget + o] / tscale[o];
-}
-
-// ---------------------------------------------------------------------------
-// the model
-struct NearfieldNet {
-    float *w = nullptr, *b = nullptr;           // FP32 master weights (Wt layout) and biases
-    __nv_bfloat16 *wb = nullptr;                // BF16 copy used by the forward pass
-    float *adam = nullptr;                      // m, v for weights and biases
-    float fmean[kFeat], fscale[kFeat], tscale[kTarget];
-    float *dnorm = nullptr;                     // device copy: fmean, fscale, tscale
-    double cutoff = 0.0, radius = 1.0;
-    int device = 0;
-};
-
-static int net_forward(NearfieldNet &net, const __nv_bfloat16 *X, int P, float *Z[kLayers],
-                       __nv_bfloat16 *A[kLayers], float *Yf, cudaStream_t st)
-{
-    const __nv_bfloat16 *in = X;
-    for (int l = 0; l < kLayers; ++l) {
-        const int warps = P / 16, threads = 128;
-        const bool last = l == kLayers - 1;
-        mlp_layer_fwd_kernel<<<(warps * 32 + threads - 1) / threads, threads, 0, st>>>(
-            in, layer_in(l), net.wb + wofs(l), net.b + bofs(l), layer_out(l), Z ? Z[l] : nullptr, last ? nullptr : A[l],
-            last ? Yf : nullptr, P, last ? 0 : 1);
-        in = A[l];
-    }
-    RMW_CHECK_LAUNCH("mlp forward");
-    return RMW_OK;
-}
-
-// one forward + backward pass on a prepared batch (X bf16 P x kIn, T P x kTarget,
-// both normalised); gradients to gW (kNW), gb (kNB); loss added to *loss
-struct NetWork {
-    float *Z[kLayers];
-    __nv_bfloat16 *A[kLayers];
-    float *Yf, *dY, *dZ, *dX;
-    void *base = nullptr;
-    cudaStream_t st = 0;
-    int P = 0;
-    int alloc(int P_, cudaStream_t s)
-    {
-        P = P_;
-        st = s;
-        size_t fl = 0;
-        for (int l = 0; l < kLayers; ++l) fl += (size_t)P * layer_out(l);
-        const size_t bytes = sizeof(float) * (fl + 4 * (size_t)P * kWide) + sizeof(__nv_bfloat16) * (fl + 64) + 1024;
-        RMW_CUDA(cudaMallocAsync(&base, bytes, st));
-        char *q = (char *)base;
-        for (int l = 0; l < kLayers; ++l) {
-            Z[l] = (float *)q;
-            q += sizeof(float) * (size_t)P * layer_out(l);
-        }
-        Yf = (float *)q; q += sizeof(float) * (size_t)P * kWide;
-        dY = (float *)q; q += sizeof(float) * (size_t)P * kWide;
-        dZ = (float *)q; q += sizeof(float) * (size_t)P * kWide;
-        dX = (float *)q; q += sizeof(float) * (size_t)P * kWide;
-        for (int l = 0; l < kLayers; ++l) {
-            A[l] = (__nv_bfloat16 *)q;
-            q += sizeof(__nv_bfloat16) * (size_t)P * layer_out(l);
-        }
-        return RMW_OK;
-    }
-    ~NetWork()
-    {
-        if (base) cudaFreeAsync(base, st);
-    }
-};
-
-static int net_backward(NearfieldNet &net, const __nv_bfloat16 *X, const float *T, int Pvalid, NetWork &W,
-                        float *gW, float *gb, float *loss)
-{
-    const int P = W.P;
-    cudaStream_t st = W.st;
-    if (int rc = net_forward(net, X, P, W.Z, W.A, W.Yf, st)) return rc;
-    mse_grad_kernel<<<(P * kOut + 255) / 256, 256, 0, st>>>(W.Yf, T, W.dY, P, Pvalid, loss);
-    for (int l = kLayers - 1; l >= 0; --l) {
-        const int ni = layer_in(l), no = layer_out(l);
-        const bool last = l == kLayers - 1;
-        act_grad_kernel<<<(P * no + 255) / 256, 256, 0, st>>>(W.dY, W.Z[l], W.dZ, P * no, last ? 0 : 1);
-        const __nv_bfloat16 *in = l == 0 ? X : W.A[l - 1];
-        weight_grad_kernel<<<(no * (ni + 1) + 127) / 128, 128, 0, st>>>(W.dZ, in, ni, no, P, gW + wofs(l),
-                                                                         gb + bofs(l));
-        if (l > 0) {
-            input_grad_kernel<<<(P * ni + 255) / 256, 256, 0, st>>>(W.dZ, net.wb + wofs(l), ni, no, P, W.dX);
-            std::swap(W.dY, W.dX);
-        }
-    }
-    RMW_CHECK_LAUNCH("mlp backward");
-    return RMW_OK;
+    body_minv_modes(minv + moff[b0], r, o0, n0, c0, A0);
+    body_minv_modes(minv + moff[b1], r, o1, n1, c1, A1);
+    __syncthreads();
+    mode_gram_inverse(A0, r, o0, n0, c0, aug, G0, status);
+    mode_gram_inverse(A1, r, o1, n1, c1, aug, G1, status);
+    mode_coupling(r, o0, n0, A0, G0, o1, n1, A1, G1, a, nf, P, Lam, V, W, out + 121LL * q);
 }
 
 // ---------------------------------------------------------------------------
 // neighbour lists: ordered pairs (i, j != i) of one suspension by centre
 // distance (minimum image)
 
-// Both neighbour bands of body i in one pass over the bodies of its
-// suspension: exact pairs (d < cut_ex) and learned pairs (cut_ex <= d < cut_ln).
-// off == NULL: cnt[i], cnt[nb + i] = the two counts; else fill the lists
-// (ascending neighbour index).  Body centres are staged through shared memory
+// The neighbour lists of body i in one pass over the bodies of its
+// suspension: exact pairs (d < cut_ex), learned pairs (cut_ex <= d < cut_ln
+// and d >= cut_lf) and the message-passing neighbours (d < cut_mp).
+// ex_off == NULL: cnt[i], cnt[nb + i], cnt[2 nb + i] = the three counts; else
+// fill the lists (ascending neighbour index).  Body centres are staged through shared memory
 // in tiles of blockDim bodies, covering the union of the block's ranges.  The
 // distance test runs in FP32 (a neighbour test needs no more; both passes use
 // the same arithmetic, so counts and lists agree).
-__global__ void nbr_bands_kernel(const double *__restrict__ xb, int nb, float cut_ex2, float cut_ln2, Images P,
-                                 const int2 *__restrict__ range, int *__restrict__ cnt,
+__global__ void nbr_bands_kernel(const double *__restrict__ xb, int nb, float cut_ex2, float cut_lf2, float cut_ln2,
+                                 float cut_mp2, Images P, const int2 *__restrict__ range, int *__restrict__ cnt,
                                  const int *__restrict__ ex_off, int *__restrict__ ex_idx,
-                                 const int *__restrict__ ln_off, int *__restrict__ ln_idx)
+                                 const int *__restrict__ ln_off, int *__restrict__ ln_idx,
+                                 const int *__restrict__ mp_off, int *__restrict__ mp_idx)
 {
     extern __shared__ float tile[];  // 3 x blockDim
     __shared__ int blo, bhi;
@@ -640,7 +417,9 @@ __global__ void nbr_bands_kernel(const double *__restrict__ xb, int nb, float cu
                 zi = valid ? (float)xb[3 * i + 2] : 0.f;
     const float Lx = (float)P.Lx, Ly = (float)P.Ly, Lz = (float)P.Lz;
     int ce = (valid && ex_off) ? ex_off[i] : 0, cl = (valid && ln_off) ? ln_off[i] : 0;
-    int ne = 0, nl = 0;
+    int cm = (valid && mp_off) ? mp_off[i] : 0;
+    int ne = 0, nl = 0, nm = 0;
+    const bool fill = ex_off != nullptr;
     const int lo = blo, hi = bhi, nt = blockDim.x;
     for (int t0 = lo; t0 < hi; t0 += nt) {
         const int j = t0 + threadIdx.x;
@@ -661,18 +440,23 @@ __global__ void nbr_bands_kernel(const double *__restrict__ xb, int nb, float cu
                 if (Lz > 0.f) dz = project(dz, Lz);
                 const float d2 = dx * dx + dy * dy + dz * dz;
                 if (d2 < cut_ex2) {
-                    if (ex_off) ex_idx[ce++] = jj;
+                    if (fill) ex_idx[ce++] = jj;
                     ++ne;
-                } else if (d2 < cut_ln2) {
-                    if (ln_off) ln_idx[cl++] = jj;
+                } else if (d2 < cut_ln2 && d2 >= cut_lf2) {
+                    if (fill) ln_idx[cl++] = jj;
                     ++nl;
+                }
+                if (d2 < cut_mp2) {
+                    if (fill) mp_idx[cm++] = jj;
+                    ++nm;
                 }
             }
         __syncthreads();
     }
-    if (valid && !ex_off && !ln_off) {
+    if (valid && !fill) {
         cnt[i] = ne;
         cnt[nb + i] = nl;
+        cnt[2 * nb + i] = nm;
     }
 }
 
@@ -696,26 +480,37 @@ __device__ __forceinline__ void pair_horizontal(const double *__restrict__ xb, i
     if (P.Ly > 0) dy = project(dy, P.Ly);
 }
 
-// normalised features (horizontal distance, z_i, z_j) / R of every learned entry, bf16, zero-padded rows
-__global__ void pair_features_kernel(const double *__restrict__ xb, const int *__restrict__ off,
-                                     const int *__restrict__ idx, int nb, int npairs, double inv_radius, Images P,
-                                     const float *__restrict__ norm, __nv_bfloat16 *__restrict__ X, int Prows)
+// owner (CSR row) of every entry of a list
+__global__ void csr_owner_kernel(const int *__restrict__ off, int nb, int *__restrict__ owner)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    for (int q = off[i]; q < off[i + 1]; ++q) owner[q] = i;
+}
+
+// raw edge features (horizontal distance, z_dst, z_src) / R of list entries (dst = owner)
+__global__ void edge_raw_features_kernel(const double *__restrict__ xb, const int *__restrict__ owner,
+                                         const int *__restrict__ idx, int n, double inv_radius, Images P,
+                                         float *__restrict__ feat)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= Prows) return;
-    float f[kFeat] = {0.f, 0.f, 0.f};
-    if (q < npairs) {
-        const int i = owner_of(off, nb, q), j = idx[q];
-        double dx, dy;
-        pair_horizontal(xb, i, j, P, dx, dy);
-        f[0] = (float)(sqrt(dx * dx + dy * dy) * inv_radius);
-        f[1] = (float)(xb[3 * i + 2] * inv_radius);
-        f[2] = (float)(xb[3 * j + 2] * inv_radius);
-    }
-    for (int k = 0; k < kIn; ++k) {
-        const float v = (q < npairs && k < kFeat) ? (f[k] - norm[k]) / norm[kFeat + k] : 0.f;
-        X[(long long)q * kIn + k] = __float2bfloat16_rn(v);
-    }
+    if (q >= n) return;
+    const int i = owner[q], j = idx[q];
+    double dx, dy;
+    pair_horizontal(xb, i, j, P, dx, dy);
+    feat[3LL * q] = (float)(sqrt(dx * dx + dy * dy) * inv_radius);
+    feat[3LL * q + 1] = (float)(xb[3 * i + 2] * inv_radius);
+    feat[3LL * q + 2] = (float)(xb[3 * j + 2] * inv_radius);
+}
+
+// raw node features (z / R, message neighbours / 8)
+__global__ void node_raw_features_kernel(const double *__restrict__ xb, const int *__restrict__ mp_off, int nb,
+                                         double inv_radius, float *__restrict__ feat)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb) return;
+    feat[2LL * i] = (float)(xb[3 * i + 2] * inv_radius);
+    feat[2LL * i + 1] = (float)(mp_off[i + 1] - mp_off[i]) / 8.0f;
 }
 
 // G_lab = Q G' Q^T, G' = network output * target scale (pair frame).  FP32:
@@ -735,7 +530,7 @@ __global__ void pair_blocks_kernel(const float *__restrict__ Yf, const double *_
     const float c = rho > 0 ? (float)(dx / rho) : 1.f, s = rho > 0 ? (float)(dy / rho) : 0.f;
     float Q[kModes][kModes];
     mode_rotation(c, s, Q);
-    const float *y = Yf + (long long)q * kOut;
+    const float *y = Yf + (long long)q * kMpOut;
     float row[kModes];  // (Q G')[a][:]
     for (int l = 0; l < kModes; ++l) {
         float acc = 0.f;
@@ -930,18 +725,20 @@ static int grow_lists(RigidSystem &S, size_t need_ex, size_t need_ln)
     return RMW_OK;
 }
 
-// exact (d < cut_ex) and learned (cut_ex <= d < cut_ln) neighbour lists of the
-// handle's bodies: one counting pass, one host round trip, one filling pass
-static int build_bands(RigidSystem &S, double cut_ex, double cut_ln)
+// exact (d < cut_ex), learned (cut_ex <= d < cut_ln, d >= cut_lf) and
+// message-passing (d < cut_mp) neighbour lists of the handle's bodies: one
+// counting pass, one host round trip, one filling pass
+static int build_bands(RigidSystem &S, double cut_ex, double cut_lf, double cut_ln, double cut_mp)
 {
     cudaStream_t st = S.st;
     const int nb = S.nb;
     if (!S.nf_off) {
-        RMW_CUDA(cudaMalloc(&S.nf_off, sizeof(int) * 2 * (nb + 1)));
-        RMW_CUDA(cudaMalloc(&S.nf_cnt, sizeof(int) * 2 * nb));
+        RMW_CUDA(cudaMalloc(&S.nf_off, sizeof(int) * 3 * (nb + 1)));
+        RMW_CUDA(cudaMalloc(&S.nf_cnt, sizeof(int) * 3 * nb));
     }
     S.nf_ex_off = S.nf_off;
     S.nf_ln_off = S.nf_off + nb + 1;
+    S.nf_mp_off = S.nf_off + 2 * (nb + 1);
     const int2 *range = nullptr;
     if (!S.susp_body_off.empty()) {
         std::vector<int2> rg(nb);
@@ -953,33 +750,109 @@ static int build_bands(RigidSystem &S, double cut_ex, double cut_ln)
         range = S.nf_range;
     }
     const Images P = images_of(S);
-    const float e2 = (float)(cut_ex * cut_ex), l2 = (float)(cut_ln * cut_ln);
+    const float e2 = (float)(cut_ex * cut_ex), f2 = (float)(cut_lf * cut_lf), l2 = (float)(cut_ln * cut_ln),
+                m2 = (float)(cut_mp * cut_mp);
     const unsigned g = (unsigned)((nb + 63) / 64);
     const size_t tsm = sizeof(float) * 3 * 64;
-    nbr_bands_kernel<<<g, 64, tsm, st>>>(S.xb, nb, e2, l2, P, range, S.nf_cnt, nullptr, nullptr, nullptr, nullptr);
+    nbr_bands_kernel<<<g, 64, tsm, st>>>(S.xb, nb, e2, f2, l2, m2, P, range, S.nf_cnt, nullptr, nullptr, nullptr,
+                                          nullptr, nullptr, nullptr);
     RMW_CHECK_LAUNCH("neighbour count");
-    std::vector<int> cnt(2 * (size_t)nb), off(2 * ((size_t)nb + 1), 0);
-    RMW_CUDA(cudaMemcpyAsync(cnt.data(), S.nf_cnt, sizeof(int) * 2 * nb, cudaMemcpyDeviceToHost, st));
+    std::vector<int> cnt(3 * (size_t)nb), off(3 * ((size_t)nb + 1), 0);
+    RMW_CUDA(cudaMemcpyAsync(cnt.data(), S.nf_cnt, sizeof(int) * 3 * nb, cudaMemcpyDeviceToHost, st));
     RMW_CUDA(cudaStreamSynchronize(st));
-    for (int band = 0; band < 2; ++band) {
+    for (int band = 0; band < 3; ++band) {
         int *o = off.data() + (size_t)band * (nb + 1);
         for (int b = 0; b < nb; ++b) o[b + 1] = o[b] + cnt[(size_t)band * nb + b];
     }
     S.nf_ex_pairs = off[nb];
     S.nf_ln_pairs = off[2 * (size_t)nb + 1];
+    S.nf_mp_pairs = off[3 * (size_t)nb + 2];
     RMW_CUDA(cudaMemcpyAsync(S.nf_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, st));
     if (int rc = grow_lists(S, (size_t)S.nf_ex_pairs, (size_t)S.nf_ln_pairs)) return rc;
-    nbr_bands_kernel<<<g, 64, tsm, st>>>(S.xb, nb, e2, l2, P, range, nullptr, S.nf_ex_off, S.nf_ex_idx, S.nf_ln_off,
-                                          S.nf_ln_idx);
+    if (!S.nf_mp_idx || (size_t)S.nf_mp_pairs > S.nf_cap_mp) {
+        if (S.nf_mp_idx) RMW_CUDA(cudaFree(S.nf_mp_idx));
+        S.nf_mp_idx = nullptr;
+        S.nf_cap_mp = 0;
+        const size_t want = std::max<size_t>((size_t)S.nf_mp_pairs + S.nf_mp_pairs / 4, 64);
+        RMW_CUDA(cudaMalloc(&S.nf_mp_idx, sizeof(int) * want));
+        S.nf_cap_mp = want;
+    }
+    // the count pass wrote the offsets' sources; the fill pass writes the lists
+    nbr_bands_kernel<<<g, 64, tsm, st>>>(S.xb, nb, e2, f2, l2, m2, P, range, nullptr, S.nf_ex_off, S.nf_ex_idx,
+                                          S.nf_ln_off, S.nf_ln_idx, S.nf_mp_off, S.nf_mp_idx);
     RMW_CHECK_LAUNCH("neighbour fill");
     return RMW_OK;
+}
+
+// Network couplings of every learned pair into S.nf_G (lab frame): the
+// message-passing graph of the handle's bodies (message neighbours, learned
+// pairs as band edges), the network's forward pass, the rotation out of each
+// pair's frame.
+static int learned_couplings(RigidSystem &S, MpnnNet &N)
+{
+    cudaStream_t st = S.st;
+    const int nb = S.nb, np = S.nf_ln_pairs, nm = S.nf_mp_pairs;
+    const Images P = images_of(S);
+    const double invR = 1.0 / N.radius;
+    auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t bytes = al(sizeof(float) * 2 * nb) + al(sizeof(int) * std::max(nm, 1)) +
+                         al(sizeof(float) * 3 * std::max(nm, 1)) + al(sizeof(int) * np) + al(sizeof(float) * 3 * np);
+    void *buf = nullptr;
+    RMW_CUDA(cudaMallocAsync(&buf, bytes, st));
+    char *p = (char *)buf;
+    float *node = (float *)p;
+    p += al(sizeof(float) * 2 * nb);
+    int *mp_dst = (int *)p;
+    p += al(sizeof(int) * std::max(nm, 1));
+    float *mp_feat = (float *)p;
+    p += al(sizeof(float) * 3 * std::max(nm, 1));
+    int *band_i = (int *)p;
+    p += al(sizeof(int) * np);
+    float *band_feat = (float *)p;
+    const unsigned gb = (unsigned)((nb + 127) / 128);
+    node_raw_features_kernel<<<gb, 128, 0, st>>>(S.xb, S.nf_mp_off, nb, invR, node);
+    if (nm > 0) {
+        csr_owner_kernel<<<gb, 128, 0, st>>>(S.nf_mp_off, nb, mp_dst);
+        edge_raw_features_kernel<<<(unsigned)((nm + 127) / 128), 128, 0, st>>>(S.xb, mp_dst, S.nf_mp_idx, nm, invR, P,
+                                                                              mp_feat);
+    }
+    csr_owner_kernel<<<gb, 128, 0, st>>>(S.nf_ln_off, nb, band_i);
+    edge_raw_features_kernel<<<(unsigned)((np + 127) / 128), 128, 0, st>>>(S.xb, band_i, S.nf_ln_idx, np, invR, P,
+                                                                          band_feat);
+    RMW_CHECK_LAUNCH("near-field graph");
+    MpGraph g;
+    g.n_nodes = nb;
+    g.n_mp = nm;
+    g.n_band = np;
+    g.node_feat = node;
+    g.mp_src = S.nf_mp_idx;
+    g.mp_dst = mp_dst;
+    g.mp_off = S.nf_mp_off;
+    g.mp_feat = mp_feat;
+    g.band_i = band_i;
+    g.band_j = S.nf_ln_idx;
+    g.band_off = S.nf_ln_off;
+    g.band_feat = band_feat;
+    MpWork *W = nullptr;
+    int rc = mp_work_create(&W, nb, nm, np, st);
+    if (rc == RMW_OK) rc = mp_forward(N, g, *W, st);
+    if (rc == RMW_OK) {
+        pair_blocks_kernel<<<(unsigned)(((long long)np * kModes + 127) / 128), 128, 0, st>>>(
+            mp_outputs(*W), S.xb, S.nf_ln_off, S.nf_ln_idx, nb, np, P, N.dnorm + 2 * kNodeFeat + 2 * kEdgeFeat,
+            S.nf_G);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = cuda_fail(e, "near-field coupling blocks");
+    }
+    mp_work_destroy(W);
+    cudaFreeAsync(buf, st);
+    return rc;
 }
 
 }  // namespace rmw
 
 // ---------------------------------------------------------------------------
 // C ABI
-using rmw::NearfieldNet;
+using rmw::MpnnNet;
 using rmw::RigidSystem;
 
 extern "C" {
@@ -1008,253 +881,47 @@ int rmw_rigid_pair_coupling(void *sys, double *out)
     return RMW_OK;
 }
 
-int rmw_nearfield_create(void **net_out, double body_radius, double cutoff, unsigned long long seed)
+int rmw_rigid_pair_coupling_list(void *sys, const int *pairs, int64_t n_pairs, double *out)
 {
-    if (!net_out) return rmw::fail(RMW_ERR_ARG, "null argument");
-    NearfieldNet *N = new NearfieldNet();
-    N->radius = body_radius;
-    N->cutoff = cutoff;
-    cudaGetDevice(&N->device);
-    // He-style initialisation from a fixed-seed generator (host, deterministic)
-    std::vector<float> w(rmw::kNW), b(rmw::kNB, 0.0f);
-    unsigned long long x = seed ? seed : 1;
-    auto uni = [&]() {
-        x ^= x << 13; x ^= x >> 7; x ^= x << 17;
-        return (double)(x >> 11) / 9007199254740992.0;
-    };
-    for (int l = 0; l < rmw::kLayers; ++l) {
-        const int ni = rmw::layer_in(l), no = rmw::layer_out(l);
-        const double sc = std::sqrt(6.0 / (l == 0 ? rmw::kFeat : ni)) * (l == rmw::kLayers - 1 ? 0.25 : 1.0);
-        for (int o = 0; o < no; ++o)
-            for (int i = 0; i < ni; ++i) {
-                const bool live = (l > 0 || i < rmw::kFeat) && (l < rmw::kLayers - 1 || o < rmw::kTarget);
-                w[rmw::wofs(l) + o * ni + i] = live ? (float)((2.0 * uni() - 1.0) * sc) : 0.0f;
-            }
-    }
-    for (int i = 0; i < rmw::kFeat; ++i) { N->fmean[i] = 0.f; N->fscale[i] = 1.f; }
-    for (int o = 0; o < rmw::kTarget; ++o) N->tscale[o] = 1.f;
-    cudaError_t e = cudaSuccess;
-    auto chk = [&](cudaError_t c) { if (e == cudaSuccess) e = c; };
-    chk(cudaMalloc(&N->w, sizeof(float) * rmw::kNW));
-    chk(cudaMalloc(&N->b, sizeof(float) * rmw::kNB));
-    chk(cudaMalloc(&N->wb, sizeof(__nv_bfloat16) * rmw::kNW));
-    chk(cudaMalloc(&N->adam, sizeof(float) * 2 * (rmw::kNW + rmw::kNB)));
-    chk(cudaMalloc(&N->dnorm, sizeof(float) * (2 * rmw::kFeat + rmw::kTarget)));
-    if (e == cudaSuccess) {
-        std::vector<__nv_bfloat16> wb(rmw::kNW);
-        for (int i = 0; i < rmw::kNW; ++i) wb[i] = __float2bfloat16_rn(w[i]);
-        chk(cudaMemcpy(N->w, w.data(), sizeof(float) * rmw::kNW, cudaMemcpyHostToDevice));
-        chk(cudaMemcpy(N->b, b.data(), sizeof(float) * rmw::kNB, cudaMemcpyHostToDevice));
-        chk(cudaMemcpy(N->wb, wb.data(), sizeof(__nv_bfloat16) * rmw::kNW, cudaMemcpyHostToDevice));
-        chk(cudaMemset(N->adam, 0, sizeof(float) * 2 * (rmw::kNW + rmw::kNB)));
-        std::vector<float> norm(2 * rmw::kFeat + rmw::kTarget, 1.0f);
-        for (int i = 0; i < rmw::kFeat; ++i) norm[i] = 0.0f;
-        chk(cudaMemcpy(N->dnorm, norm.data(), sizeof(float) * norm.size(), cudaMemcpyHostToDevice));
-    }
-    if (e != cudaSuccess) {
-        cudaFree(N->w); cudaFree(N->b); cudaFree(N->wb); cudaFree(N->adam); cudaFree(N->dnorm);
-        delete N;
-        return rmw::cuda_fail(e, "rmw_nearfield_create");
-    }
-    *net_out = N;
+    if (!sys || !pairs || !out) return rmw::fail(RMW_ERR_ARG, "null argument");
+    RigidSystem &S = *(RigidSystem *)sys;
+    if (!S.pc_ready) return rmw::fail(RMW_ERR_ARG, "build the preconditioner first (it forms each body's M^-1)");
+    if (n_pairs <= 0) return RMW_OK;
+    if (n_pairs > (int64_t(1) << 30)) return rmw::fail(RMW_ERR_ARG, "too many pairs");
+    std::vector<int> hp((size_t)2 * n_pairs);
+    RMW_CUDA(cudaMemcpyAsync(hp.data(), pairs, sizeof(int) * hp.size(), cudaMemcpyDeviceToHost, S.st));
+    RMW_CUDA(cudaStreamSynchronize(S.st));
+    for (size_t k = 0; k < hp.size(); ++k)
+        if (hp[k] < 0 || hp[k] >= S.nb) return rmw::fail(RMW_ERR_ARG, "pair index out of range");
+    const int nt = 128;
+    const size_t sm = sizeof(double) * (4 * (size_t)S.max_m * rmw::kModes + 3 * rmw::kModes * rmw::kModes +
+                                        2 * rmw::kModes * rmw::kModes);
+    if (sm > 227 * 1024) return rmw::fail(RMW_ERR_ARG, "bodies too large for the coupling kernel");
+    if (sm > 48 * 1024)
+        RMW_CUDA(cudaFuncSetAttribute(rmw::pair_list_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    RMW_CUDA(cudaMemsetAsync(S.dstatus, 0, sizeof(int), S.st));
+    const double nf = 1.0 / (8.0 * rmw::kPi * S.eta * S.a);
+    rmw::pair_list_kernel<<<(unsigned)n_pairs, nt, sm, S.st>>>(S.r, S.xb, S.boff, S.moff, S.minv, pairs, S.a, nf,
+                                                               rmw::Images{S.L[0], S.L[1], S.L[2]}, S.max_m, out,
+                                                               S.dstatus);
+    RMW_CHECK_LAUNCH("mode coupling of listed pairs");
+    int h = 0;
+    RMW_CUDA(cudaMemcpyAsync(&h, S.dstatus, sizeof(int), cudaMemcpyDeviceToHost, S.st));
+    RMW_CUDA(cudaStreamSynchronize(S.st));
+    if (h) return rmw::fail(RMW_ERR_NONFINITE, "singular mode Gram matrix");
     return RMW_OK;
-}
-
-int rmw_nearfield_destroy(void *net)
-{
-    if (!net) return RMW_OK;
-    NearfieldNet *N = (NearfieldNet *)net;
-    cudaFree(N->w); cudaFree(N->b); cudaFree(N->wb); cudaFree(N->adam); cudaFree(N->dnorm);
-    delete N;
-    return RMW_OK;
-}
-
-// Parameters in and out (FP32 master weights, biases, normalisation): for
-// checkpoints and for the gradient check.  Sizes: rmw_nearfield_sizes.
-int rmw_nearfield_sizes(int *n_weights, int *n_biases, int *n_in, int *width, int *n_out, int *n_target)
-{
-    if (n_weights) *n_weights = rmw::kNW;
-    if (n_biases) *n_biases = rmw::kNB;
-    if (n_in) *n_in = rmw::kIn;
-    if (width) *width = rmw::kWidth;
-    if (n_out) *n_out = rmw::kOut;
-    if (n_target) *n_target = rmw::kTarget;
-    return RMW_OK;
-}
-
-int rmw_nearfield_get(void *net, float *w_host, float *b_host, float *norm_host)
-{
-    if (!net) return rmw::fail(RMW_ERR_ARG, "null network");
-    NearfieldNet *N = (NearfieldNet *)net;
-    if (w_host) RMW_CUDA(cudaMemcpy(w_host, N->w, sizeof(float) * rmw::kNW, cudaMemcpyDeviceToHost));
-    if (b_host) RMW_CUDA(cudaMemcpy(b_host, N->b, sizeof(float) * rmw::kNB, cudaMemcpyDeviceToHost));
-    if (norm_host) {
-        std::memcpy(norm_host, N->fmean, sizeof(float) * rmw::kFeat);
-        std::memcpy(norm_host + rmw::kFeat, N->fscale, sizeof(float) * rmw::kFeat);
-        std::memcpy(norm_host + 2 * rmw::kFeat, N->tscale, sizeof(float) * rmw::kTarget);
-    }
-    return RMW_OK;
-}
-
-int rmw_nearfield_set(void *net, const float *w_host, const float *b_host, const float *norm_host)
-{
-    if (!net) return rmw::fail(RMW_ERR_ARG, "null network");
-    NearfieldNet *N = (NearfieldNet *)net;
-    if (w_host) {
-        std::vector<__nv_bfloat16> wb(rmw::kNW);
-        for (int i = 0; i < rmw::kNW; ++i) wb[i] = __float2bfloat16_rn(w_host[i]);
-        RMW_CUDA(cudaMemcpy(N->w, w_host, sizeof(float) * rmw::kNW, cudaMemcpyHostToDevice));
-        RMW_CUDA(cudaMemcpy(N->wb, wb.data(), sizeof(__nv_bfloat16) * rmw::kNW, cudaMemcpyHostToDevice));
-    }
-    if (b_host) RMW_CUDA(cudaMemcpy(N->b, b_host, sizeof(float) * rmw::kNB, cudaMemcpyHostToDevice));
-    if (norm_host) {
-        std::memcpy(N->fmean, norm_host, sizeof(float) * rmw::kFeat);
-        std::memcpy(N->fscale, norm_host + rmw::kFeat, sizeof(float) * rmw::kFeat);
-        std::memcpy(N->tscale, norm_host + 2 * rmw::kFeat, sizeof(float) * rmw::kTarget);
-        RMW_CUDA(cudaMemcpy(N->dnorm, norm_host, sizeof(float) * (2 * rmw::kFeat + rmw::kTarget), cudaMemcpyHostToDevice));
-    }
-    return RMW_OK;
-}
-
-// One forward + backward pass on a host batch of already normalised inputs
-// (P x 16, zero-padded) and targets (P x 121): gradients of the mean squared
-// error with respect to every weight and bias (for the gradient check).
-int rmw_nearfield_grad(void *net, const float *X_host, const float *T_host, int P, float *gW_host, float *gb_host,
-                       float *loss_host)
-{
-    if (!net || !X_host || !T_host || P <= 0) return rmw::fail(RMW_ERR_ARG, "bad argument");
-    NearfieldNet *N = (NearfieldNet *)net;
-    cudaStream_t st = 0;
-    const int Pp = ((P + 63) / 64) * 64;
-    rmw::NetWork W;
-    if (int rc = W.alloc(Pp, st)) return rc;
-    std::vector<__nv_bfloat16> xb((size_t)Pp * rmw::kIn, __float2bfloat16_rn(0.f));
-    for (int p = 0; p < P; ++p)
-        for (int i = 0; i < rmw::kIn; ++i) xb[(size_t)p * rmw::kIn + i] = __float2bfloat16_rn(X_host[(size_t)p * rmw::kIn + i]);
-    void *buf = nullptr;
-    const size_t bytes = sizeof(__nv_bfloat16) * xb.size() + sizeof(float) * ((size_t)P * rmw::kTarget + rmw::kNW + rmw::kNB + 1);
-    RMW_CUDA(cudaMalloc(&buf, bytes));
-    __nv_bfloat16 *dX = (__nv_bfloat16 *)buf;
-    float *dT = (float *)(dX + xb.size());
-    float *gW = dT + (size_t)P * rmw::kTarget, *gb = gW + rmw::kNW, *loss = gb + rmw::kNB;
-    RMW_CUDA(cudaMemcpy(dX, xb.data(), sizeof(__nv_bfloat16) * xb.size(), cudaMemcpyHostToDevice));
-    RMW_CUDA(cudaMemcpy(dT, T_host, sizeof(float) * (size_t)P * rmw::kTarget, cudaMemcpyHostToDevice));
-    RMW_CUDA(cudaMemset(loss, 0, sizeof(float)));
-    int rc = rmw::net_backward(*N, dX, dT, P, W, gW, gb, loss);
-    if (rc == RMW_OK) {
-        RMW_CUDA(cudaMemcpy(gW_host, gW, sizeof(float) * rmw::kNW, cudaMemcpyDeviceToHost));
-        RMW_CUDA(cudaMemcpy(gb_host, gb, sizeof(float) * rmw::kNB, cudaMemcpyDeviceToHost));
-        RMW_CUDA(cudaMemcpy(loss_host, loss, sizeof(float), cudaMemcpyDeviceToHost));
-    }
-    cudaFree(buf);
-    return rc;
-}
-
-// Forward pass on a host batch of normalised inputs (P x 16): outputs P x 121.
-int rmw_nearfield_forward(void *net, const float *X_host, int P, float *Y_host)
-{
-    if (!net || !X_host || !Y_host || P <= 0) return rmw::fail(RMW_ERR_ARG, "bad argument");
-    NearfieldNet *N = (NearfieldNet *)net;
-    const int Pp = ((P + 63) / 64) * 64;
-    rmw::NetWork W;
-    if (int rc = W.alloc(Pp, 0)) return rc;
-    std::vector<__nv_bfloat16> xb((size_t)Pp * rmw::kIn, __float2bfloat16_rn(0.f));
-    for (int p = 0; p < P; ++p)
-        for (int i = 0; i < rmw::kIn; ++i) xb[(size_t)p * rmw::kIn + i] = __float2bfloat16_rn(X_host[(size_t)p * rmw::kIn + i]);
-    __nv_bfloat16 *dX = nullptr;
-    RMW_CUDA(cudaMalloc(&dX, sizeof(__nv_bfloat16) * xb.size()));
-    RMW_CUDA(cudaMemcpy(dX, xb.data(), sizeof(__nv_bfloat16) * xb.size(), cudaMemcpyHostToDevice));
-    int rc = rmw::net_forward(*N, dX, Pp, nullptr, W.A, W.Yf, 0);
-    if (rc == RMW_OK) {
-        std::vector<float> y((size_t)Pp * rmw::kOut);
-        RMW_CUDA(cudaMemcpy(y.data(), W.Yf, sizeof(float) * y.size(), cudaMemcpyDeviceToHost));
-        for (int p = 0; p < P; ++p)
-            for (int o = 0; o < rmw::kTarget; ++o) Y_host[(size_t)p * rmw::kTarget + o] = y[(size_t)p * rmw::kOut + o];
-    }
-    cudaFree(dX);
-    return rc;
-}
-
-// Train on device data feat (S x 3: horizontal distance, z_i, z_j over the
-// body radius) and targ (S x 121: the pair-frame 11x11 mode coupling), Adam,
-// mean squared error on normalised targets.  Sets the normalisation from the
-// data.
-// loss_host (optional, steps entries) receives the loss of every step.
-int rmw_nearfield_train(void *net, const float *feat, const float *targ, int S, int steps, int batch, float lr,
-                        unsigned long long seed, float *loss_host, void *stream)
-{
-    if (!net || !feat || !targ || S <= 0 || steps <= 0 || batch <= 0) return rmw::fail(RMW_ERR_ARG, "bad argument");
-    NearfieldNet *N = (NearfieldNet *)net;
-    cudaStream_t st = rmw::as_stream(stream);
-    // normalisation from the data (host copy of S x 39 floats)
-    std::vector<float> hf((size_t)S * rmw::kFeat), ht((size_t)S * rmw::kTarget);
-    RMW_CUDA(cudaMemcpyAsync(hf.data(), feat, sizeof(float) * hf.size(), cudaMemcpyDeviceToHost, st));
-    RMW_CUDA(cudaMemcpyAsync(ht.data(), targ, sizeof(float) * ht.size(), cudaMemcpyDeviceToHost, st));
-    RMW_CUDA(cudaStreamSynchronize(st));
-    std::vector<float> norm(2 * rmw::kFeat + rmw::kTarget);
-    for (int i = 0; i < rmw::kFeat; ++i) {
-        double m = 0, v = 0;
-        for (int s = 0; s < S; ++s) m += hf[(size_t)s * rmw::kFeat + i];
-        m /= S;
-        for (int s = 0; s < S; ++s) v += (hf[(size_t)s * rmw::kFeat + i] - m) * (hf[(size_t)s * rmw::kFeat + i] - m);
-        norm[i] = (float)m;
-        norm[rmw::kFeat + i] = (float)std::max(std::sqrt(v / S), 1e-6);
-    }
-    // per-output RMS, floored at 5% of the largest: outputs that vanish for a
-    // sphere by the pair's mirror symmetry carry only orientation noise, which
-    // must not be blown up to unit scale
-    double tmax = 0.0;
-    for (int o = 0; o < rmw::kTarget; ++o) {
-        double v = 0;
-        for (int s = 0; s < S; ++s) v += (double)ht[(size_t)s * rmw::kTarget + o] * ht[(size_t)s * rmw::kTarget + o];
-        norm[2 * rmw::kFeat + o] = (float)std::sqrt(v / S);
-        tmax = std::max(tmax, (double)norm[2 * rmw::kFeat + o]);
-    }
-    for (int o = 0; o < rmw::kTarget; ++o)
-        norm[2 * rmw::kFeat + o] = (float)std::max((double)norm[2 * rmw::kFeat + o], std::max(0.05 * tmax, 1e-30));
-    if (int rc = rmw_nearfield_set(net, nullptr, nullptr, norm.data())) return rc;
-    const int Pp = ((batch + 63) / 64) * 64;
-    rmw::NetWork W;
-    if (int rc = W.alloc(Pp, st)) return rc;
-    void *buf = nullptr;
-    const size_t bytes = sizeof(__nv_bfloat16) * (size_t)Pp * rmw::kIn +
-                         sizeof(float) * ((size_t)Pp * rmw::kTarget + rmw::kNW + rmw::kNB + steps);
-    RMW_CUDA(cudaMallocAsync(&buf, bytes, st));
-    __nv_bfloat16 *X = (__nv_bfloat16 *)buf;
-    float *T = (float *)(X + (size_t)Pp * rmw::kIn);
-    float *gW = T + (size_t)Pp * rmw::kTarget, *gb = gW + rmw::kNW, *loss = gb + rmw::kNB;
-    RMW_CUDA(cudaMemsetAsync(loss, 0, sizeof(float) * steps, st));
-    const float b1 = 0.9f, b2 = 0.999f;
-    float *mW = N->adam, *vW = N->adam + rmw::kNW, *mB = N->adam + 2 * rmw::kNW, *vB = mB + rmw::kNB;
-    int rc = RMW_OK;
-    for (int t = 0; t < steps && rc == RMW_OK; ++t) {
-        rmw::gather_batch_kernel<<<(Pp + 127) / 128, 128, 0, st>>>(feat, targ, S, N->dnorm, N->dnorm + rmw::kFeat,
-                                                                  N->dnorm + 2 * rmw::kFeat, Pp, batch, seed, t, X, T);
-        rc = rmw::net_backward(*N, X, T, batch, W, gW, gb, loss + t);
-        if (rc) break;
-        const float c1 = 1.f - std::pow(b1, (float)(t + 1)), c2 = 1.f - std::pow(b2, (float)(t + 1));
-        rmw::adam_kernel<<<(rmw::kNW + 255) / 256, 256, 0, st>>>(N->w, gW, mW, vW, N->wb, rmw::kNW, lr, b1, b2, c1,
-                                                                c2, 1e-8f);
-        rmw::adam_kernel<<<(rmw::kNB + 255) / 256, 256, 0, st>>>(N->b, gb, mB, vB, nullptr, rmw::kNB, lr, b1, b2, c1,
-                                                                c2, 1e-8f);
-    }
-    cudaError_t e = cudaGetLastError();
-    if (rc == RMW_OK && e != cudaSuccess) rc = rmw::cuda_fail(e, "near-field training");
-    if (rc == RMW_OK && loss_host)
-        RMW_CUDA(cudaMemcpyAsync(loss_host, loss, sizeof(float) * steps, cudaMemcpyDeviceToHost, st));
-    cudaFreeAsync(buf, st);
-    RMW_CUDA(cudaStreamSynchronize(st));
-    return rc;
 }
 
 // Switch a handle's preconditioner (after rmw_rigid_build_pc) to the
 // near-field augmented form: exact blob-level couplings for body pairs closer
-// than exact_cutoff, network-predicted mode couplings for pairs from there to
-// the network's cutoff (net may be NULL: exact pairs only).  Pairs are found
-// within one suspension.  net == NULL and exact_cutoff <= 0 switch back to the
-// block-diagonal form.  n_pairs_host (optional, 2 entries) receives the
-// numbers of ordered exact and learned pairs.
-int rmw_rigid_set_nearfield(void *sys, void *net, double exact_cutoff, int64_t *n_pairs_host)
+// than exact_cutoff, network-predicted mode couplings for pairs from
+// max(exact_cutoff, learned_from) to the network's cutoff (net may be NULL:
+// exact pairs only).  Pairs are found within one suspension.  net == NULL and
+// exact_cutoff <= 0 switch back to the block-diagonal form.  n_pairs_host
+// (optional, 2 entries) receives the numbers of ordered exact and learned
+// pairs.
+int rmw_rigid_set_nearfield_bands(void *sys, void *net, double exact_cutoff, double learned_from,
+                                  int64_t *n_pairs_host)
 {
     if (!sys) return rmw::fail(RMW_ERR_ARG, "null handle");
     RigidSystem &S = *(RigidSystem *)sys;
@@ -1266,32 +933,22 @@ int rmw_rigid_set_nearfield(void *sys, void *net, double exact_cutoff, int64_t *
     }
     if (!S.pc_ready) return rmw::fail(RMW_ERR_ARG, "build the preconditioner first");
     if (!S.wall) return rmw::fail(RMW_ERR_ARG, "the near-field preconditioner models bodies above the wall");
-    NearfieldNet *N = (NearfieldNet *)net;
+    MpnnNet *N = (MpnnNet *)net;
     const double hi = N ? std::max(N->cutoff, lo) : lo;
+    const double lf = N ? std::max(learned_from, 0.0) : hi;
+    const double mp = N ? N->mp_cutoff : 0.0;
     cudaStream_t st = S.st;
     S.nf_on = false;
-    if (int rc = rmw::build_bands(S, lo, hi)) return rc;
+    if (int rc = rmw::build_bands(S, lo, lf, hi, mp)) return rc;
     if (!S.nf_mom) RMW_CUDA(cudaMalloc(&S.nf_mom, sizeof(double) * rmw::kModes * S.nb));
     if (!S.nf_v) {
         RMW_CUDA(cudaMalloc(&S.nf_v, sizeof(double) * S.sys_size()));
         RMW_CUDA(cudaMemset(S.nf_v, 0, sizeof(double) * S.sys_size()));  // force rows stay zero
     }
     if (!S.nf_z) RMW_CUDA(cudaMalloc(&S.nf_z, sizeof(double) * S.sys_size()));
-    const int np = S.nf_ln_pairs;
-    if (np > 0) {
-        const int Pp = ((np + 63) / 64) * 64;
-        const rmw::Images P{S.L[0], S.L[1], S.L[2]};
-        rmw::NetWork W;
-        if (int rc2 = W.alloc(Pp, st)) return rc2;
-        __nv_bfloat16 *X = nullptr;
-        RMW_CUDA(cudaMallocAsync(&X, sizeof(__nv_bfloat16) * (size_t)Pp * rmw::kIn, st));
-        rmw::pair_features_kernel<<<(Pp + 127) / 128, 128, 0, st>>>(S.xb, S.nf_ln_off, S.nf_ln_idx, S.nb, np,
-                                                                   1.0 / N->radius, P, N->dnorm, X, Pp);
-        if (int rc2 = rmw::net_forward(*N, X, Pp, nullptr, W.A, W.Yf, st)) return rc2;
-        rmw::pair_blocks_kernel<<<(unsigned)(((long long)np * rmw::kModes + 127) / 128), 128, 0, st>>>(
-            W.Yf, S.xb, S.nf_ln_off, S.nf_ln_idx, S.nb, np, P, N->dnorm + 2 * rmw::kFeat, S.nf_G);
-        RMW_CUDA(cudaFreeAsync(X, st));
-    }
+    if (N && S.nf_ln_pairs > 0)
+        if (int rc = rmw::learned_couplings(S, *N)) return rc;
+    if (!N) S.nf_ln_pairs = 0;
     RMW_CHECK_LAUNCH("near-field attach");
     RMW_CUDA(cudaStreamSynchronize(st));
     S.nf_on = true;
@@ -1300,6 +957,11 @@ int rmw_rigid_set_nearfield(void *sys, void *net, double exact_cutoff, int64_t *
         n_pairs_host[1] = S.nf_ln_pairs;
     }
     return RMW_OK;
+}
+
+int rmw_rigid_set_nearfield(void *sys, void *net, double exact_cutoff, int64_t *n_pairs_host)
+{
+    return rmw_rigid_set_nearfield_bands(sys, net, exact_cutoff, 0.0, n_pairs_host);
 }
 
 }  // extern "C"

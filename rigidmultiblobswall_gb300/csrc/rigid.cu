@@ -646,7 +646,7 @@ static void free_system(RigidSystem *S)
     cudaGetDevice(&cur);
     cudaSetDevice(S->device);
     void *ptrs[] = {S->boff, S->blob_body, S->moff, S->r, S->xb, S->minv, S->minvK, S->nmat, S->lfac, S->linv,
-                    S->dstatus, S->tmp3n, S->perm, S->nf_off, S->nf_ex_idx, S->nf_ln_idx, S->nf_cnt, S->nf_range,
+                    S->dstatus, S->tmp3n, S->perm, S->nf_off, S->nf_ex_idx, S->nf_ln_idx, S->nf_mp_idx, S->nf_cnt, S->nf_range,
                     S->nf_G, S->nf_mom, S->nf_v, S->nf_z, S->nf_part};
     for (void *p : ptrs)
         if (p) cudaFree(p);

@@ -47,10 +47,14 @@ struct RigidSystem {
     // pairs whose 11x11 mode coupling the network predicts
     bool nf_on = false;
     int nf_ex_pairs = 0, nf_ln_pairs = 0;
-    int *nf_off = nullptr;                          // 2 (nb+1): both offset arrays (owned)
+    int *nf_off = nullptr;                          // 3 (nb+1): the three offset arrays (owned)
     int *nf_ex_off = nullptr, *nf_ln_off = nullptr;  // views into nf_off
+    int *nf_mp_off = nullptr;                       // message-passing neighbours (view into nf_off)
     int *nf_ex_idx = nullptr, *nf_ln_idx = nullptr;
-    int *nf_cnt = nullptr;                          // 2 nb neighbour counts
+    int *nf_mp_idx = nullptr;
+    int nf_mp_pairs = 0;
+    size_t nf_cap_mp = 0;
+    int *nf_cnt = nullptr;                          // 3 nb neighbour counts
     int2 *nf_range = nullptr;                       // nb: bodies of each body's suspension
     size_t nf_cap_ex = 0, nf_cap_ln = 0;            // capacities (entries) of the per-entry arrays
     double *nf_G = nullptr;    // 121 per learned entry (lab frame)

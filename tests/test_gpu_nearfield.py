@@ -73,24 +73,57 @@ def test_exact_nearfield_apply_matches_oracle(cuda_device):
     sys_.close()
 
 
+def _random_graph(rng, R=1.0):
+    """Three clusters of 3..6 bodies: message edges < 3R, band edges in [2.2R, 6R)."""
+    from oracle import mpnn
+    cents, cid = [], []
+    for k in range(3):
+        n = 3 + k
+        c = [np.array([0.0, 0.0, 1.5])]
+        while len(c) < n:
+            p = c[rng.integers(len(c))] + np.array([*rng.uniform(-3.5, 3.5, 2), 0.0])
+            p[2] = rng.uniform(1.1, 3.0)
+            if all(np.linalg.norm(p - q) >= 2.2 * R for q in c):
+                c.append(p)
+        c = np.array(c) + np.array([100.0 * k, 0.0, 0.0])
+        cents.append(c)
+        cid += [k] * n
+    cen = np.concatenate(cents)
+    arrays = nf.graph_arrays(cen, np.array(cid), R, 3 * R, 2.2 * R, 6 * R)
+    og = mpnn.graph_from_positions(cen, np.array(cid), R, 3 * R, 2.2 * R, 6 * R)
+    return arrays, og
+
+
 def test_forward_and_gradients_match_oracle(cuda_device):
+    """The message-passing network on the GPU (BF16 tensor-core GEMMs forward and backward) against the
+    BF16-emulating oracle: outputs, loss and every weight and bias gradient."""
+    from oracle import mpnn
     rng = np.random.default_rng(1)
-    m = nf.NearfieldModel(body_radius=1.0, cutoff=3.0, seed=5)
-    w, b, _ = m.get_params()
+    arrays, og = _random_graph(rng)
+    for k in ("mp_src", "mp_dst", "band_i", "band_j"):
+        assert np.array_equal(arrays[k], og[k])
+    nb_edges = len(arrays["band_i"])
+    T = rng.standard_normal((nb_edges, onf.N_TARGET)).astype(np.float32)
+    m = nf.NearfieldModel(body_radius=1.0, cutoff=6.0, seed=5)
+    w, b, norm = m.get_params()
     b = (rng.standard_normal(b.size) * 0.1).astype(np.float32)
-    m.set_params(w, b, None)
-    P = 100
-    X = np.zeros((P, 16), dtype=np.float32)
-    X[:, :3] = rng.standard_normal((P, 3))
-    T = rng.standard_normal((P, onf.N_TARGET)).astype(np.float32)
-    Y = m.forward(X)
-    Yref, _, _ = onf.forward(w, b, X)
+    norm = np.concatenate([[1.8, 0.3], [0.6, 0.2], [3.0, 1.9, 1.9], [1.4, 0.6, 0.6],
+                           rng.uniform(0.5, 2.0, onf.N_TARGET)]).astype(np.float32)
+    m.set_params(w, b, norm)
+    g = nf.DeviceGraph(arrays, T)
+    Y = m.forward(g)
+    Yref, _ = mpnn.forward(w, b, norm, og)
     assert rel_err(Y, Yref) <= 5e-3
-    gW, gb, loss = m.grad(X, T)
-    gWr, gbr, lossr = onf.grad(w, b, X, T)
-    assert abs(loss - lossr) <= 1e-3 * lossr
+    gW, gb, loss = m.grad(g)
+    gWr, gbr, lossr = mpnn.grad(w, b, norm, og, T / norm[-onf.N_TARGET:])
+    assert abs(loss - lossr) <= 2e-3 * lossr
     assert rel_err(gW, gWr) <= 2e-2
     assert rel_err(gb, gbr) <= 2e-2
+    # every layer's block of the gradient, not only the whole vector
+    ofs = np.cumsum([0] + [ni * no for _, ni, no, _ in mpnn.LAYERS])
+    for l in range(len(mpnn.LAYERS)):
+        blk = slice(ofs[l], ofs[l + 1])
+        assert rel_err(gW[blk], gWr[blk]) <= 5e-2, mpnn.LAYERS[l][0]
 
 
 @pytest.fixture(scope="module")
@@ -98,10 +131,10 @@ def trained(cuda_device):
     shell = S.icosphere_42()
     a = S.blob_radius_of(shell)
     R = np.linalg.norm(shell[0])
-    feat, targ = nf.pair_training_data(shell, a, 1.0, 2048, d_range=(2 * R + 2 * a, 6 * R),
-                                       z_range=(1.1 * R, 3 * R), seed=11)
+    graphs = nf.cluster_training_data(shell, a, 1.0, 512, d_range=(2 * R + 2 * a, 6 * R),
+                                      z_range=(1.1 * R, 3 * R), seed=11)
     m = nf.NearfieldModel(body_radius=R, cutoff=6 * R, seed=2)
-    hist = m.train(feat, targ, steps=2000, batch=512, lr=2e-3)
+    hist = m.train(graphs, steps=1500, lr=2e-3)
     return m, hist, R
 
 
@@ -112,8 +145,8 @@ def test_training_reduces_the_loss(trained):
 
 
 def test_learned_apply_matches_oracle(trained):
-    """The attached blocks are the network's outputs rotated into the lab
-    frame: the apply matches the oracle fed with the network's own outputs."""
+    """The attached blocks are the network's outputs (on the suspension's own message-passing graph)
+    rotated into the lab frame: the apply matches the oracle fed with the network's outputs."""
     m, _, R = trained
     susp, sys_, _ = _dense_suspension(12, 31)
     n_ex, n_ln = m.attach(sys_, exact_cutoff=3 * R)
@@ -122,13 +155,10 @@ def test_learned_apply_matches_oracle(trained):
     ln = _pairs_within(locs, 3 * R, 6 * R)
     assert (n_ex, n_ln) == (len(ex), len(ln)) and n_ln > 0
     _, _, norm = m.get_params()
-    fmean, fscale, tscale = norm[:3], norm[3:6], norm[6:]
-    X = np.zeros((len(ln), 16), dtype=np.float32)
-    for k, (i, j) in enumerate(ln):
-        d = locs[j] - locs[i]
-        f = np.array([np.hypot(d[0], d[1]), locs[i, 2], locs[j, 2]]) / R
-        X[k, :3] = (f.astype(np.float32) - fmean) / fscale
-    Y = m.forward(X).astype(np.float64) * tscale
+    tscale = norm[-onf.N_TARGET:]
+    arrays = nf.graph_arrays(locs, np.zeros(len(locs), dtype=int), R, 3 * R, 3 * R, 6 * R)
+    assert [(int(i), int(j)) for i, j in zip(arrays["band_i"], arrays["band_j"])] == ln
+    Y = m.forward(nf.DeviceGraph(arrays)).astype(np.float64) * tscale
     learned = {}
     for k, (i, j) in enumerate(ln):
         d = locs[j] - locs[i]
@@ -145,11 +175,11 @@ def test_learned_apply_matches_oracle(trained):
 
 
 def test_augmented_preconditioner_gain_and_fallback(trained):
-    """A dense suspension (area fraction 0.3, heights in [1.1R, 3R]): the exact
-    near field (< 3R), the learned couplings (< 6R) and both together must
-    each need fewer GMRES iterations than the plain block-diagonal
-    preconditioner and reach the same 1e-8 residual; a reference that no
-    preconditioner can beat triggers the fallback."""
+    """A dense suspension (area fraction 0.3, heights in [1.1R, 3R]): the exact near field (< 3R), the
+    learned couplings (< 6R), the learned outer band alone (3R..6R) and exact + learned band each need
+    fewer GMRES iterations than the plain block-diagonal preconditioner at the same 1e-8 residual; the
+    learned band adds a gain on top of the exact near field; a reference that no preconditioner can beat
+    triggers the fallback."""
     m, _, R = trained
     susp, sys_, _ = _dense_suspension(96, 21)
     FT = np.zeros((susp.n_bodies, 6))
@@ -158,19 +188,20 @@ def test_augmented_preconditioner_gain_and_fallback(trained):
     rhs /= np.linalg.norm(rhs)
     exact = nf.solve_with_fallback(sys_, None, rhs, mode="fp64", exact_cutoff=3 * R)
     plain = exact["plain"]
-    learned = nf.solve_with_fallback(sys_, m, rhs, mode="fp64", reference=(plain["iterations"], plain["relres"]))
-    both = nf.solve_with_fallback(sys_, m, rhs, mode="fp64", reference=(plain["iterations"], plain["relres"]),
-                                  exact_cutoff=3 * R)
+    ref = (plain["iterations"], plain["relres"])
+    learned = nf.solve_with_fallback(sys_, m, rhs, mode="fp64", reference=ref)
+    band = nf.solve_with_fallback(sys_, m, rhs, mode="fp64", reference=ref, learned_from=3 * R)
+    both = nf.solve_with_fallback(sys_, m, rhs, mode="fp64", reference=ref, exact_cutoff=3 * R)
     print("iterations: plain", plain["iterations"], "exact<3R", exact["augmented"]["iterations"],
-          "learned<6R", learned["augmented"]["iterations"], "exact<3R+learned<6R", both["augmented"]["iterations"],
-          "pairs", exact["augmented"]["pairs"], learned["augmented"]["pairs"], both["augmented"]["pairs"])
+          "learned<6R", learned["augmented"]["iterations"], "learned 3R..6R", band["augmented"]["iterations"],
+          "exact<3R+learned", both["augmented"]["iterations"])
     assert plain["relres"] <= 1e-8
-    for res in (exact, learned, both):
+    for res in (exact, learned, band, both):
         assert res["augmented"]["relres"] <= 1e-8
         assert res["augmented"]["iterations"] < plain["iterations"]
         assert res["kept"] == "augmented"
-    # both solutions have relative residual <= 1e-8; their difference is that
-    # times the conditioning of the saddle-point system
+    assert band["augmented"]["pairs"][0] == 0 and band["augmented"]["pairs"][1] > 0
+    assert both["augmented"]["iterations"] < exact["augmented"]["iterations"]
     x_plain = plain["x"].cpu().numpy()
     assert rel_err(both["augmented"]["x"].cpu().numpy(), x_plain) <= 1e-6
     res2 = nf.solve_with_fallback(sys_, m, rhs, mode="fp64", reference=(1, 1e-12))

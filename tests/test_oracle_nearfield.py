@@ -5,30 +5,64 @@ import numpy as np
 from oracle import nearfield as onf
 
 
-def test_oracle_gradient_matches_finite_differences():
+def _graph(rng):
+    from oracle import mpnn
+    cen = np.array([[0.0, 0.0, 1.3], [2.4, 0.5, 1.9], [4.6, -0.4, 1.2], [2.0, 3.1, 2.6],
+                    [40.0, 0.0, 1.5], [42.9, 1.0, 1.1]])
+    return mpnn.graph_from_positions(cen, [0, 0, 0, 0, 1, 1], 1.0, 3.0, 2.2, 6.0)
+
+
+def test_mpnn_oracle_gradient_matches_finite_differences():
+    """The message-passing oracle's backward pass (the check of the GPU training kernels) against central
+    differences of its loss, with the BF16 rounding switched off."""
+    from oracle import mpnn
     rng = np.random.default_rng(0)
-    nw = sum(i * o for i, o in onf.LAYERS)
+    g = _graph(rng)
+    assert len(g["mp_src"]) > 0 and len(g["band_i"]) > 0
+    nw, nb = mpnn.sizes()
+    w = rng.standard_normal(nw) * 0.15
+    b = rng.standard_normal(nb) * 0.1
+    norm = np.concatenate([[1.8, 0.2], [0.5, 0.1], [3.0, 1.8, 1.8], [1.5, 0.5, 0.5], np.ones(mpnn.TARGET)])
+    T = rng.standard_normal((len(g["band_i"]), mpnn.TARGET))
+    gW, gb, loss = mpnn.grad(w, b, norm, g, T, rounding=False)
+    ofs = np.cumsum([0] + [ni * no for _, ni, no, _ in mpnn.LAYERS])
+    picks = [ofs[0] + 1, ofs[1] + 3, ofs[1] + 70, ofs[2] + 5, ofs[2] + 100, ofs[5] + 7, ofs[7] + 130,
+             ofs[8] + 9, ofs[9] + 11]
+    for idx in picks:
+        e = np.zeros(nw)
+        e[idx] = 1e-6
+        fd = (mpnn.grad(w + e, b, norm, g, T, rounding=False)[2] -
+              mpnn.grad(w - e, b, norm, g, T, rounding=False)[2]) / 2e-6
+        assert abs(fd - gW[idx]) <= 1e-6 * max(1.0, abs(fd)), idx
+    bofs = np.cumsum([0] + [no for _, _, no, _ in mpnn.LAYERS])
+    for idx in (bofs[0] + 2, bofs[2] + 3, bofs[6] + 1, bofs[9] + 4):
+        e = np.zeros(nb)
+        e[idx] = 1e-6
+        fd = (mpnn.grad(w, b + e, norm, g, T, rounding=False)[2] -
+              mpnn.grad(w, b - e, norm, g, T, rounding=False)[2]) / 2e-6
+        assert abs(fd - gb[idx]) <= 1e-6 * max(1.0, abs(fd)), idx
+
+
+def test_mpnn_messages_stay_inside_clusters_and_change_predictions():
+    """Edges join bodies of one cluster only; a body added near a pair (a message neighbour, not itself
+    in the pair) changes the pair's prediction - the network sees neighbourhoods."""
+    from oracle import mpnn
+    rng = np.random.default_rng(1)
+    g = _graph(rng)
+    cl = np.array([0, 0, 0, 0, 1, 1])
+    assert (cl[g["mp_src"]] == cl[g["mp_dst"]]).all() and (cl[g["band_i"]] == cl[g["band_j"]]).all()
+    assert (g["mp_dst"][g["mp_rev"]] == g["mp_src"]).all() and (g["band_i"][g["band_rev"]] == g["band_j"]).all()
+    nw, nb = mpnn.sizes()
     w = rng.standard_normal(nw) * 0.2
-    b = rng.standard_normal(3 * onf.WIDTH + onf.N_OUT) * 0.1
-    X = np.zeros((8, onf.N_IN))
-    X[:, :3] = rng.standard_normal((8, 3))
-    T = rng.standard_normal((8, onf.N_TARGET))
-    saved = onf.bf16
-    onf.bf16 = lambda x: np.asarray(x, dtype=np.float64)  # exact arithmetic for the check
-    try:
-        gW, gb, loss = onf.grad(w, b, X, T)
-        for idx in (0, 5, 200, 1500, nw - 3):
-            e = np.zeros(nw)
-            e[idx] = 1e-6
-            fd = (onf.grad(w + e, b, X, T)[2] - onf.grad(w - e, b, X, T)[2]) / 2e-6
-            assert abs(fd - gW[idx]) <= 1e-6 * max(1.0, abs(fd))
-        for idx in (0, 70, 3 * onf.WIDTH + 5):
-            e = np.zeros(b.size)
-            e[idx] = 1e-6
-            fd = (onf.grad(w, b + e, X, T)[2] - onf.grad(w, b - e, X, T)[2]) / 2e-6
-            assert abs(fd - gb[idx]) <= 1e-6 * max(1.0, abs(fd))
-    finally:
-        onf.bf16 = saved
+    b = rng.standard_normal(nb) * 0.1
+    norm = np.concatenate([[1.8, 0.2], [0.5, 0.1], [3.0, 1.8, 1.8], [1.5, 0.5, 0.5], np.ones(mpnn.TARGET)])
+    cen2 = np.array([[0.0, 0.0, 1.3], [4.0, 0.0, 1.3]])
+    two = mpnn.graph_from_positions(cen2, [0, 0], 1.0, 3.0, 2.2, 6.0)
+    three = mpnn.graph_from_positions(np.vstack([cen2, [[2.0, 2.0, 1.3]]]), [0, 0, 0], 1.0, 3.0, 2.2, 6.0)
+    y2, _ = mpnn.forward(w, b, norm, two, rounding=False)
+    y3, _ = mpnn.forward(w, b, norm, three, rounding=False)
+    k = [e for e in range(len(three["band_i"])) if (three["band_i"][e], three["band_j"][e]) == (0, 1)][0]
+    assert np.abs(y3[k] - y2[0]).max() > 1e-6
 
 
 def test_bf16_rounding_is_round_to_nearest_even():

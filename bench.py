@@ -48,6 +48,9 @@ WORKLOAD = "wall-RPY M_UF.F, 256 shells x 42 blobs = 10,752 blobs (FP64-accurate
 DF64_UF_INST_PER_PAIR = {"symmetric": 1704728972.0 * 32 / 10752 ** 2, "standard": 2719541740.0 * 32 / 10752 ** 2}
 # dram__bytes_read.sum + dram__bytes_write.sum per launch, same captures
 DF64_UF_TRAFFIC_BYTES = {"symmetric": 735744, "standard": 718848}
+# issued thread instructions per pair and right-hand side of the 16-wide multi-RHS M_UF kernel
+# (smsp__inst_executed.sum * 32 / (N^2 * 16), 60,000 blobs)
+MULTI16_INST_PER_PAIR_RHS = 17.4
 DF64_UF_KERNEL_SOURCE_SHA = "ac909a031a188da5b8c5009d4600eab52be0b7b5c98007e539c9a289bbf64246"
 
 
@@ -82,7 +85,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=8.0)
     p.add_argument("--large", action="store_true",
                    help="only run the 4096-shell (172,032-blob) solve comparison and print its JSON line")
-    p.add_argument("--large-modes", default="fp64,mixed,mixed+exact,mixed+learned_band,mixed+exact+learned")
+    p.add_argument("--large-modes",
+                   default="fp64,mixed,mixed+exact,mixed+learned,mixed+learned_band,mixed+exact+learned")
     p.add_argument("--multi", default=None, metavar="N:NRHS",
                    help="only time the multi-right-hand-side M_UF product on N blobs with NRHS vectors")
     p.add_argument("--product", default=None, metavar="KIND:MODE",
@@ -120,23 +124,27 @@ def hbm_peak_gbs():
 
 
 def arnoldi_traffic(fn):
-    """Run fn() with tracing on; return (fn's result, the Arnoldi orthogonalisation's time, algorithmic
-    bytes and bandwidth against the HBM peak)."""
+    """Run fn() with tracing on and CUDA graphs off (the fused Arnoldi step kernels then launch one by one
+    and are timed each); return (fn's result, the Arnoldi orthogonalisation's time, algorithmic bytes and
+    bandwidth against the HBM peak)."""
     from rigidmultiblobswall_gb300 import _native
+    _native.use_graphs(False)
     _native.trace_enable(True)
     _native.trace_read(1, reset=True)
     _native.trace_bytes(1, reset=True)
     res = fn()
     ms, launches = _native.trace_read(1, reset=True)
     nbytes = _native.trace_bytes(1, reset=True)
-    _native.trace_read(0, reset=True)
-    _native.trace_read(2, reset=True)
+    for k in (0, 2, 3, 4, 5, 6, 7):
+        _native.trace_read(k, reset=True)
     _native.trace_enable(False)
+    _native.use_graphs(True)
     peak, src = hbm_peak_gbs()
     gbs = nbytes / (ms * 1e-3) / 1e9 if ms > 0 else None
     return res, {"steps": launches, "ms": ms, "gbytes": nbytes / 1e9, "gbs": gbs,
                  "frac_of_hbm": (gbs / peak) if gbs else None, "hbm_peak_gbs": peak, "peak_source": src,
-                 "bytes_per_step": "(4j + 12) n doubles: CGS2 = 2 x (dots + update) + scale"}
+                 "bytes_per_step": "(4j + 12) n doubles: CGS2 = 2 x (dots + update) + scale",
+                 "kernel": "arnoldi_step_kernel (fused CGS2 + Givens, one launch per step)"}
 
 
 def reduce_step_ms(step_ms, ws, device=None):
@@ -412,7 +420,7 @@ def solver_metrics(dev, reps=2):
             torch.cuda.synchronize()
             dt = time.perf_counter() - t0
             best = dt if best is None else min(best, dt)
-        sols[mode] = sol[3 * sys2.n_blobs:].cpu().numpy()
+        sols[mode] = sol.cpu().numpy()
         out["solve_shells42x256_%s" % mode] = {"ms": best * 1e3, "iterations": its, "relres_fp64": rr, "info": info}
     # the same mixed solve with the per-iteration operator launched kernel by kernel instead of as a
     # captured CUDA graph
@@ -445,7 +453,7 @@ def solver_metrics(dev, reps=2):
             dt = time.perf_counter() - t0
             best = dt if best is None else min(best, dt)
         nf.detach(sys2)
-        sols[mode + "_nf"] = sol[3 * sys2.n_blobs:].cpu().numpy()
+        sols[mode + "_nf"] = sol.cpu().numpy()
         out["solve_shells42x256_%s_nearfield" % mode] = {"ms": best * 1e3, "iterations": its, "relres_fp64": rr,
                                                           "info": info, "pairs_exact_learned": list(pairs)}
     # where the mixed solve's time goes (PC build + solve, traced by class)
@@ -458,10 +466,26 @@ def solver_metrics(dev, reps=2):
     sys2.build_pc()
     _, out["solve_shells42x256_mixed_arnoldi"] = arnoldi_traffic(
         lambda: integrator.solve_mobility_problem(sys2, FT, tol=1e-8, mode="mixed"))
-    u64 = sols["fp64"]
-    for key, sk in (("mixed", "solve_shells42x256_mixed"), ("fp64_nf", "solve_shells42x256_fp64_nearfield"),
+    # errors judged by the oracle: its FP64 residual |b - A x| / |b| of every returned solution (all-pairs
+    # product of oracle/wall_oracle.c, K and the operator of oracle/rigid.py) and the body velocities of
+    # its own solve (restarted right-preconditioned GMRES with the block-diagonal preconditioner)
+    from oracle import rigid as orc
+    n3 = 3 * sys2.n_blobs
+    orig = orc.Rigid(s2.r_vectors(), s2.locations, sys2.offsets, s2.eta, s2.a)
+    rhs = np.concatenate([np.zeros(n3), -FT.reshape(-1)])
+    nrm = np.linalg.norm(rhs)
+    xo, ito, _ = orc.gmres_right(orig.apply, orig.apply_pc, rhs / nrm, tol=1e-8)
+    uo = (xo * nrm)[n3:]
+    u64 = sols["fp64"][n3:]
+    for key, sk in (("fp64", "solve_shells42x256_fp64"), ("mixed", "solve_shells42x256_mixed"),
+                    ("fp64_nf", "solve_shells42x256_fp64_nearfield"),
                     ("mixed_nf", "solve_shells42x256_mixed_nearfield")):
-        out[sk]["velocity_rel_err_vs_fp64"] = float(np.linalg.norm(sols[key] - u64) / np.linalg.norm(u64))
+        x = sols[key]
+        out[sk]["relres_oracle"] = float(np.linalg.norm(rhs - orig.apply(x)) / nrm)
+        out[sk]["velocity_rel_err_vs_oracle"] = float(np.linalg.norm(x[n3:] - uo) / np.linalg.norm(uo))
+        if key != "fp64":
+            out[sk]["velocity_rel_err_vs_fp64"] = float(np.linalg.norm(x[n3:] - u64) / np.linalg.norm(u64))
+    out["solve_shells42x256_oracle_iterations"] = ito
     out["solve_shells42x256_speedup_mixed"] = out["solve_shells42x256_fp64"]["ms"] / \
         out["solve_shells42x256_mixed"]["ms"]
     out["solve_shells42x256_speedup_mixed_nearfield"] = out["solve_shells42x256_fp64"]["ms"] / \
@@ -595,12 +619,13 @@ def oracle_residual_sampled(r, locs, offsets, eta, a, sol, FT, n_rows=1024, seed
     return float(est / np.linalg.norm(FT)), int(rows.size)
 
 
-def cfg5_metrics(dev, modes=("fp64", "mixed", "mixed+exact", "mixed+learned_band", "mixed+exact+learned")):
+def cfg5_metrics(dev, modes=("fp64", "mixed", "mixed+exact", "mixed+learned", "mixed+learned_band",
+                             "mixed+exact+learned")):
     """4096 42-blob shells at area fraction 0.3, force (0,0,-1) per body: preconditioned GMRES to a 1e-8
     relative residual, on one GPU.  Arms: plain block-diagonal FP64 (the baseline), mixed precision, and
     mixed precision with the near-field augmented preconditioner - exact blob-level couplings below 3R
-    only ("exact"), learned mode couplings of the outer band 3R..6R only ("learned_band"), and both
-    ("exact+learned").  Each arm's time covers its preconditioner build (FP64 or FP32), the near-field
+    only ("exact"), learned mode couplings of every pair below 6R ("learned"), of the outer band 3R..6R
+    only ("learned_band"), and exact below 3R with learned from 3R to 6R ("exact+learned").  Each arm's time covers its preconditioner build (FP64 or FP32), the near-field
     attach and the solve; the network is trained once before (time reported).  Every solution's relative
     residual is also estimated by the oracle (all body rows, 1024 sampled blob rows)."""
     import torch
@@ -625,13 +650,15 @@ def cfg5_metrics(dev, modes=("fp64", "mixed", "mixed+exact", "mixed+learned_band
         parts = mode.split("+")
         base = parts[0]
         exact = "exact" in parts
-        learned = "learned_band" in parts or "learned" in parts
+        band_only = "learned_band" in parts
+        learned = band_only or "learned" in parts
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         sys5.build_pc(mode="mixed" if base == "mixed" else base)
         pairs = None
         if learned:
-            pairs = model.attach(sys5, exact_cutoff=3 * R5 if exact else 0.0, learned_from=3 * R5)
+            pairs = model.attach(sys5, exact_cutoff=3 * R5 if exact else 0.0,
+                                 learned_from=3 * R5 if band_only else 0.0)
         elif exact:
             pairs = nf.attach_exact(sys5, 3 * R5)
         sol, info, its, rr = integrator.solve_mobility_problem(sys5, FT, tol=1e-8, mode=base)
@@ -654,7 +681,8 @@ def cfg5_metrics(dev, modes=("fp64", "mixed", "mixed+exact", "mixed+learned_band
         for mode in modes:
             if mode != "fp64":
                 out["speedup_%s_vs_fp64" % mode] = out["fp64"]["ms"] / out[mode]["ms"]
-    for m1, m2 in (("mixed+exact+learned", "mixed+exact"), ("mixed+learned_band", "mixed")):
+    for m1, m2 in (("mixed+exact+learned", "mixed+exact"), ("mixed+learned", "mixed"),
+                   ("mixed+learned_band", "mixed")):
         if m1 in out and m2 in out:
             out["gain_%s_over_%s" % (m1, m2)] = {"ms_ratio": out[m2]["ms"] / out[m1]["ms"],
                                                  "iterations": [out[m2]["iterations"], out[m1]["iterations"]]}
@@ -722,6 +750,36 @@ def batched_metrics(dev, nrhs=16):
     out["all_converged"] = bool((stt == 0).all())
     # the same solve again, traced: bandwidth of the segmented Arnoldi work (2.1 M-long vectors, basis > L2)
     _, out["solve_arnoldi"] = arnoldi_traffic(lambda: sysb.solve_batched(rhs, tol=1e-8, mode="mixed"))
+    # roofline of the 16-RHS Lanczos: the multi-right-hand-side pair kernel's share of the time and its
+    # FP32 issue rate (launched kernel by kernel, traced).  Pair-RHS evaluations: the kernel runs a pass
+    # of 16 right-hand sides of a suspension while any of them still iterates (it + 1 operator
+    # applications for it iterations), over n_k^2 blob pairs.
+    from rigidmultiblobswall_gb300 import _native
+    _native.use_graphs(False)
+    _native.trace_enable(True)
+    _native.trace_read(0, reset=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, itl2 = sysb.lanczos_batched(Z, factor=np.sqrt(2.0 / 1e-3), tol=1e-3, mode="mixed")
+    torch.cuda.synchronize()
+    lz_ms = (time.perf_counter() - t0) * 1e3
+    pair_ms, pair_launches = _native.trace_read(0, reset=True)
+    _native.trace_enable(False)
+    _native.use_graphs(True)
+    it = np.asarray(itl2).reshape(nrhs, len(counts))
+    nblob = 42 * np.asarray(counts, dtype=np.float64)
+    prhs = 0.0
+    for p in range(0, nrhs, 16):
+        w = min(16, nrhs - p)
+        prhs += float(((it[p:p + w].max(axis=0) + 1) * nblob ** 2).sum()) * (16 if w > 8 else 8)
+    peak32 = _native.fma_peak(False)
+    ipr = MULTI16_INST_PER_PAIR_RHS
+    out["lanczos_16rhs_roofline"] = {
+        "lanczos_ms_without_graphs": lz_ms, "pair_kernel_ms": pair_ms, "pair_kernel_launches": pair_launches,
+        "pair_kernel_share": pair_ms / lz_ms, "pair_rhs_evaluated": prhs,
+        "tpair_rhs_per_s": prhs / (pair_ms * 1e-3) / 1e12,
+        "issued_inst_per_pair_rhs": ipr, "fp32_issue_frac": prhs * ipr / (pair_ms * 1e-3) / (peak32 / 2.0),
+        "note": "issued instructions per pair-RHS from the ncu capture of wall_pair_multi_kernel (16 RHS)"}
     return out
 
 

@@ -8,6 +8,8 @@ namespace rmw {
 
 // spins of a grid barrier before it gives up (about 0.3 s with the 64 ns sleeps)
 constexpr unsigned kBarrierSpins = 1u << 22;
+// tridiagonal matrices up to this size are diagonalised in shared memory
+constexpr int kLzShared = 256;
 
 // ---------------------------------------------------------------------------
 // device helpers
@@ -457,6 +459,7 @@ __global__ void __launch_bounds__(kKdThreads, 1) lanczos_step_kernel(LzArgs A)
 {
     __shared__ double red[kKdMaxBasis * 32];
     __shared__ double hsh[kKdMaxBasis];
+    __shared__ double tdg[kLzShared], tsd[kLzShared];  // the owner warp's tridiagonal matrix
     __shared__ int actv[8];
     const int i = *(volatile int *)&A.st->i;
     const int k = i + 1;
@@ -531,11 +534,15 @@ __global__ void __launch_bounds__(kKdThreads, 1) lanczos_step_kernel(LzArgs A)
                 if (lane == 0) A.flags[s] |= 2;
                 stop = 1;
             } else {
-                double *d = A.dt + so, *ee = A.et + so, *zz = A.z + (long long)s * A.kcap * A.kcap;
-                for (int q = 0; q < k; ++q) {  // every lane writes the same values (its own reads stay coherent)
+                // the eigen-problem in shared memory while it fits (the global copies otherwise): its
+                // recurrence is a long chain of dependent accesses
+                double *d = (k <= kLzShared) ? tdg : A.dt + so, *ee = (k <= kLzShared) ? tsd : A.et + so;
+                double *zz = (k * k <= kKdMaxBasis * 32) ? red : A.z + (long long)s * A.kcap * A.kcap;
+                for (int q = lane; q < k; q += 32) {
                     d[q] = A.hd[so + q];
                     ee[q] = (q < i) ? A.hs[so + q] : 0.0;
                 }
+                __syncwarp();
                 const bool ok = tridiag_eigen_warp(d, ee, zz, k, lane);
                 __syncwarp();
                 if (!ok) {

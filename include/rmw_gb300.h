@@ -208,6 +208,14 @@ int rmw_wall_autotune_lookup(int kind, int mode, int64_t n, int *nchunks, int *t
  * choice the products use the symmetric kernel from 4,096 blobs in FP64 and
  * df64 and from 8,192 in mixed precision. */
 int rmw_wall_autotune_set(int kind, int mode, int64_t n, int nchunks);
+/* Library-only (no reference counterpart): how a product of (kind, mode, n)
+ * runs on the current device - 0 the one-sided kernel, 1 the symmetric kernel
+ * (each unordered pair once; ceil(n/128) x 3n doubles of partial sums), 2 the
+ * symmetric df64 kernel band by band of tile rows, when those partial sums
+ * exceed the budget (an eighth of the device memory, or the scratch cap):
+ * about 3 x 128 doubles per blob and tile row of a band, bands summed in a
+ * fixed order. */
+int rmw_wall_product_route(int kind, int mode, int64_t n, const double *L_host, int *route_host);
 int rmw_wall_autotune_clear(void);
 
 /* CUDA graphs (no reference counterpart): the solvers' per-iteration

@@ -64,6 +64,7 @@ SIGNATURES = {
     "rmw_wall_autotune_lookup": (_i, [_i, _i, _i64, _vp, _vp]),
     "rmw_wall_autotune_clear": (_i, []),
     "rmw_wall_autotune_set": (_i, [_i, _i, _i64, _i]),
+    "rmw_wall_product_route": (_i, [_i, _i, _i64, _vp, _vp]),
     "rmw_use_graphs": (_i, [_i]),
     "rmw_use_device_krylov": (_i, [_i]),
     "rmw_trace_bytes": (_i, [_i, _vp, _i]),

@@ -529,8 +529,10 @@ __global__ void __launch_bounds__(kKdThreads, 1) lanczos_step_kernel(LzArgs A)
                 A.hs[so + i] = wn;
             }
             __syncwarp();
+            const bool host_checks = A.st->host != 0;  // the host checks convergence from here on
             int stop = 0;
-            if (!isfinite(wn) || !isfinite(hdi)) {
+            if (host_checks) {
+            } else if (!isfinite(wn) || !isfinite(hdi)) {
                 if (lane == 0) A.flags[s] |= 2;
                 stop = 1;
             } else {
@@ -575,7 +577,7 @@ __global__ void __launch_bounds__(kKdThreads, 1) lanczos_step_kernel(LzArgs A)
                     }
                 }
             }
-            if (lane == 0) {
+            if (lane == 0 && !host_checks) {
                 if (stop) A.cyc[s] = 0;
                 else atomicAdd(&A.st->active, 1);
             }
@@ -590,8 +592,9 @@ __global__ void __launch_bounds__(kKdThreads, 1) lanczos_step_kernel(LzArgs A)
             __threadfence();
             const int act = atomicAdd(&A.st->active, 0);
             const int in = i + 1;
-            // stop when no segment is left, past max_iter, or when the basis is full (the host grows it)
-            const int more = (act > 0 && in <= A.st->max_iter && in + 1 < A.st->vcap &&
+            // stop when no segment is left, past max_iter, when the basis is full (the host grows it) or
+            // when the tridiagonal matrix gets too large for the device eigen-solve (the host goes on)
+            const int more = (act > 0 && in <= A.st->max_iter && in + 1 < A.st->vcap && in < A.st->dev_k &&
                               !*(volatile int *)&A.st->bar.err) ? 1 : 0;
             A.st->i = in;
             A.st->active = 0;
@@ -687,7 +690,7 @@ int kd_build_jobs(const std::vector<long long> &off, int nblk_max, std::vector<K
 {
     const int nseg = (int)off.size() - 1;
     const long long n = off.back();
-    // one CTA per SM at most, at least 1024 elements per CTA
+    // one CTA per SM at most, at least kKdThreads elements per CTA
     const int nblk = (int)std::max<long long>(1, std::min<long long>(nblk_max, (n + kKdThreads - 1) / kKdThreads));
     long long per = (n + nblk - 1) / nblk;
     per = ((per + 31) / 32) * 32;
@@ -913,6 +916,8 @@ __global__ void lz_init_kernel(const double *__restrict__ nrm, int nseg, double 
         st->more = 1;
         st->live = 0;
         st->max_iter = max_iter;
+        st->dev_k = kLzDeviceRows;
+        st->host = 0;
         st->bar.done = 0;
     }
 }

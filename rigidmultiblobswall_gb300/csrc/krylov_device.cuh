@@ -34,7 +34,11 @@
 
 namespace rmw {
 
-constexpr int kKdThreads = 1024;  // threads of the fused step CTAs
+// threads of the fused step CTAs: the vector work is FP64-pipe bound on
+// GB300 (two flops per 8-byte element against a 1:64 FP64 rate), so each
+// thread takes several elements and the per-thread FP64 reduction overhead
+// (warp trees per basis vector) stays small against the multiply-adds
+constexpr int kKdThreads = 256;
 constexpr int kKdMaxBasis = 128;  // basis vectors a step handles (restart <= 120)
 
 // contiguous piece [b, e) of segment `seg`, processed by CTA `blk`
@@ -69,9 +73,18 @@ struct LzState {
     int live;      // segments still iterating after the last step
     int max_iter;  // the reference's max_iter
     int vcap;      // basis vectors V has room for
+    int dev_k;     // the device checks convergence while i < dev_k; beyond, the host does
+    int host;      // 1: the host checks convergence (the kernel only records the recurrence)
     long long ldv;
     double *V;     // the basis (grown by the host between graph launches)
 };
+
+// Tridiagonal matrices larger than this are diagonalised on the host: the
+// implicit QL recurrence is a long chain of dependent FP64 operations, which
+// GB300's FP64 pipe (1:64 of FP32) runs slower than a host core once the
+// matrix has a dozen rows.
+constexpr int kLzDeviceRows = 10;
+bool tridiag_eigen_host(std::vector<double> &d, std::vector<double> e, std::vector<double> &z);
 
 // Job table: CTA b of at most nblk_max CTAs gets a contiguous range of the n
 // elements (a multiple of 32 long); jobs are the intersections of those ranges
@@ -192,6 +205,7 @@ struct LanczosDevice {
     bool graph_failed = false;
     LzMask mk;
     double factor = 1.0, tol = 1e-3;
+    std::vector<double> zn_;  // |z_s|
 
     LanczosDevice(Op f, cudaStream_t *s) : op(f), sref(s), home(*s) {}
     LanczosDevice(const LanczosDevice &) = delete;
@@ -285,6 +299,96 @@ struct LanczosDevice {
         return RMW_OK;
     }
 
+    // Iterations from i0 on with the convergence test on the host: each step is
+    // the operator and the step kernel in its recording mode, then one copy of
+    // the new tridiagonal entries, the host's eigen-decompositions and
+    // stopping tests, and the updated segment flags back to the device.
+    int host_continuation(int i0, int max_iter)
+    {
+        const int ns = L.nseg, kc = L.kcap;
+        std::vector<double> hd((size_t)ns * kc), hs((size_t)ns * kc), c((size_t)ns * kc), cold((size_t)ns * kc);
+        std::vector<int> cyc(ns), iters(ns), kfin(ns);
+        RMW_CUDA(cudaMemcpyAsync(hd.data(), L.hd, sizeof(double) * hd.size(), cudaMemcpyDeviceToHost, home));
+        RMW_CUDA(cudaMemcpyAsync(hs.data(), L.hs, sizeof(double) * hs.size(), cudaMemcpyDeviceToHost, home));
+        RMW_CUDA(cudaMemcpyAsync(cold.data(), L.cold, sizeof(double) * cold.size(), cudaMemcpyDeviceToHost, home));
+        RMW_CUDA(cudaMemcpyAsync(cyc.data(), L.cyc, sizeof(int) * ns, cudaMemcpyDeviceToHost, home));
+        RMW_CUDA(cudaMemcpyAsync(iters.data(), L.iters, sizeof(int) * ns, cudaMemcpyDeviceToHost, home));
+        RMW_CUDA(cudaMemcpyAsync(kfin.data(), L.kfin, sizeof(int) * ns, cudaMemcpyDeviceToHost, home));
+        RMW_CUDA(cudaStreamSynchronize(home));
+        c = cold;
+        const int one = 1;
+        RMW_CUDA(cudaMemcpyAsync(&L.state->host, &one, sizeof(int), cudaMemcpyHostToDevice, home));
+        std::vector<double> nd(2 * (size_t)ns), dd, ee, zq;
+        std::vector<unsigned char> mask;
+        for (int i = i0; i <= max_iter && i < kc; ++i) {
+            int live = 0;
+            for (int s = 0; s < ns; ++s) live += cyc[s];
+            if (!live) break;
+            if (i + 2 > L.vcap)
+                if (int rc = L.grow(2 * L.vcap)) return rc;
+            if (int rc = op(L.xin, L.w)) return rc;
+            if (int rc = lz_step(L, factor, tol, mk, 0, 0, home)) return rc;
+            // hd[s][i], hs[s][i] of every segment
+            RMW_CUDA(cudaMemcpy2DAsync(nd.data(), sizeof(double), L.hd + i, sizeof(double) * kc, sizeof(double), ns,
+                                       cudaMemcpyDeviceToHost, home));
+            RMW_CUDA(cudaMemcpy2DAsync(nd.data() + ns, sizeof(double), L.hs + i, sizeof(double) * kc, sizeof(double),
+                                       ns, cudaMemcpyDeviceToHost, home));
+            RMW_CUDA(cudaStreamSynchronize(home));
+            bool changed = false;
+            const int k = i + 1;
+            for (int s = 0; s < ns; ++s) {
+                if (!cyc[s]) continue;
+                const size_t so = (size_t)s * kc;
+                hd[so + i] = nd[s];
+                hs[so + i] = nd[ns + s];
+                if (!std::isfinite(nd[s]) || !std::isfinite(nd[ns + s]))
+                    return fail(RMW_ERR_BREAKDOWN, "Lanczos: non-finite value");
+                dd.assign(hd.begin() + so, hd.begin() + so + k);
+                ee.assign(hs.begin() + so, hs.begin() + so + i);
+                if (!tridiag_eigen_host(dd, ee, zq)) return fail(RMW_ERR_BREAKDOWN, "Lanczos: tridiagonal eigensolver failed");
+                double dn = 0.0, on = 0.0;
+                for (int q = 0; q < k; ++q) {
+                    double acc = 0.0;
+                    for (int j = 0; j < k; ++j) {
+                        const double lam = dd[j] > 0 ? std::sqrt(dd[j]) : 0.0;
+                        acc += zq[q + (size_t)k * j] * (zq[(size_t)k * j] * lam * zn_[s] * factor);
+                    }
+                    const double old = q < i ? cold[so + q] : 0.0;
+                    dn += (acc - old) * (acc - old);
+                    on += old * old;
+                    c[so + q] = acc;
+                }
+                for (int q = 0; q < k; ++q) cold[so + q] = c[so + q];
+                kfin[s] = k;
+                const bool conv = i > 0 && std::sqrt(dn) / std::max(std::sqrt(on), 2.220446049250313e-16) < tol;
+                if (conv || nd[ns + s] == 0.0) {
+                    iters[s] = i;
+                    cyc[s] = 0;
+                    changed = true;
+                }
+            }
+            if (changed) {
+                // freeze the stopped segments from the next step on (and their passes of the product)
+                RMW_CUDA(cudaMemcpyAsync(L.cyc, cyc.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, home));
+                if (mk.mask) {
+                    const int npass = (mk.nrhs + mk.pass - 1) / mk.pass;
+                    mask.assign((size_t)npass * mk.nsusp, 0);
+                    for (int p = 0; p < npass; ++p)
+                        for (int u = 0; u < mk.nsusp; ++u)
+                            for (int q = p * mk.pass; q < std::min(mk.nrhs, (p + 1) * mk.pass); ++q)
+                                mask[(size_t)p * mk.nsusp + u] |= cyc[(size_t)q * mk.nsusp + u] ? 1 : 0;
+                    RMW_CUDA(cudaMemcpyAsync(mk.mask, mask.data(), mask.size(), cudaMemcpyHostToDevice, home));
+                }
+                RMW_CUDA(cudaStreamSynchronize(home));
+            }
+        }
+        RMW_CUDA(cudaMemcpyAsync(L.c, c.data(), sizeof(double) * c.size(), cudaMemcpyHostToDevice, home));
+        RMW_CUDA(cudaMemcpyAsync(L.iters, iters.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, home));
+        RMW_CUDA(cudaMemcpyAsync(L.kfin, kfin.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, home));
+        RMW_CUDA(cudaStreamSynchronize(home));
+        return RMW_OK;
+    }
+
     // noise_s = factor M_s^(1/2) z_s per segment; iters per segment (the
     // reference's count: the index of the converged iteration, max_iter if none)
     // require_nonzero: a zero z is an error (the single-vector entry points), not a zero noise
@@ -296,9 +400,9 @@ struct LanczosDevice {
         tol = tol_;
         mk = mask;
         if (int rc = L.init(seg_off, kcap, home)) return rc;
-        std::vector<double> zn;
         std::vector<int> run;
-        if (int rc = lz_begin(L, z, factor, max_iter, zn, run)) return rc;
+        if (int rc = lz_begin(L, z, factor, max_iter, zn_, run)) return rc;
+        std::vector<double> &zn = zn_;
         int n_run = 0;
         for (int s = 0; s < L.nseg; ++s) {
             if (!std::isfinite(zn[s]) || (require_nonzero && factor != 0.0 && !(zn[s] > 0.0)))
@@ -316,17 +420,19 @@ struct LanczosDevice {
             RMW_CUDA(cudaMemcpyAsync(mk.mask, h.data(), h.size(), cudaMemcpyHostToDevice, home));
             RMW_CUDA(cudaStreamSynchronize(home));
         }
+        LzState S{};
         while (n_run > 0) {
             if (int rc = run_loop()) return rc;
-            LzState S;
             if (int rc = lz_fetch_state(L, &S)) return rc;
             if (S.bar.err) return fail(RMW_ERR_CUDA, "Lanczos: a grid barrier of the step kernel timed out");
-            if (S.live > 0 && S.i <= max_iter && S.i < L.kcap && S.i + 1 >= L.vcap) {
+            if (S.live > 0 && S.i <= max_iter && S.i < L.kcap && S.i < S.dev_k && S.i + 1 >= L.vcap) {
                 if (int rc = L.grow(2 * L.vcap)) return rc;
                 continue;
             }
             break;
         }
+        if (n_run > 0 && S.live > 0 && S.i <= max_iter && S.i < L.kcap)
+            if (int rc = host_continuation(S.i, max_iter)) return rc;
         if (n_run == 0) {
             RMW_CUDA(cudaMemsetAsync(noise, 0, sizeof(double) * L.n, home));
             iters.assign(L.nseg, 0);

@@ -117,6 +117,7 @@ int scratch_release_all()
 }
 
 void scratch_set_limit(size_t bytes) { g_scratch_limit.store(bytes); }
+size_t scratch_limit() { return g_scratch_limit.load(); }
 
 // ---- tracing ---------------------------------------------------------------
 namespace {

@@ -36,6 +36,7 @@ int scratch(ScratchSlot slot, size_t bytes, void **ptr, cudaStream_t st);
 int scratch_release_all();
 // requests above `bytes` fail with RMW_ERR_ALLOC without touching the device (0 = no cap)
 void scratch_set_limit(size_t bytes);
+size_t scratch_limit();
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 

@@ -264,16 +264,41 @@ __device__ __forceinline__ void sym_cta(const SymJob *jobs, int &n, int &nt, int
     }
 }
 
-template <bool SEG, int KIND, bool NOWALL = false>
+// A band of tile rows [t0, t1) of the upper triangle (all S >= T), with its
+// own compact partial sums: the target-side sums of CTA (T, S) at
+// bt[((T - t0) (nt - t0) + S - t0) * 384], the source-side sums at
+// bs[((S - t0) (t1 - t0) + T - t0) * 384] (384 = 3 x 128 doubles).  Bands
+// are accumulated one after the other in a fixed order (sym_band_accum_kernel),
+// so the scratch is O(band x n) instead of O(n^2 / 128) and results stay
+// deterministic.
+struct SymBand {
+    int t0, t1;
+    double *bt, *bs;
+};
+
+__device__ __forceinline__ void sym_band_pair(long long b, int nt, const SymBand &bd, int &T, int &S)
+{
+    int t = bd.t0;
+    while (t + 1 < bd.t1 && b >= nt - t) {
+        b -= nt - t;
+        ++t;
+    }
+    T = t;
+    S = t + (int)b;
+}
+
+template <bool SEG, int KIND, bool NOWALL = false, bool BAND = false>
 __device__ __forceinline__ void df_sym_body(const SrcDF *__restrict__ src, int n, int nt,
-                                            double *__restrict__ partial, const SymJob *__restrict__ jobs)
+                                            double *__restrict__ partial, const SymJob *__restrict__ jobs,
+                                            const SymBand bd = SymBand{0, 0, nullptr, nullptr})
 {
     // structure-of-arrays source tile: the rotated reads of a warp hit 32
     // consecutive 16-byte entries (no bank conflicts)
     __shared__ float4 thi[kTile], tlo[kTile], tvh[kTile], tvl[kTile];
     __shared__ float2 sacc[kSymWarps][3][kTile];  // per-warp source-side double-float sums (hi, lo)
     int T, S;
-    sym_cta<SEG>(jobs, n, nt, T, S, src, partial);
+    if constexpr (BAND) sym_band_pair(blockIdx.x, nt, bd, T, S);
+    else sym_cta<SEG>(jobs, n, nt, T, S, src, partial);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool diag = (T == S);
     const int i = T * kTile + tid;
@@ -357,6 +382,18 @@ __device__ __forceinline__ void df_sym_body(const SrcDF *__restrict__ src, int n
         sy += (double)sacc[w][1][tid].x + (double)sacc[w][1][tid].y;
         sz += (double)sacc[w][2][tid].x + (double)sacc[w][2][tid].y;
     }
+    if constexpr (BAND) {
+        const int W = nt - bd.t0, C = bd.t1 - bd.t0;
+        double *o = bd.bt + ((size_t)(T - bd.t0) * W + (S - bd.t0)) * (3 * kTile) + 3 * tid;
+        o[0] = diag ? ax + sx : ax;
+        o[1] = diag ? ay + sy : ay;
+        o[2] = diag ? az + sz : az;
+        if (!diag) {
+            double *q = bd.bs + ((size_t)(S - bd.t0) * C + (T - bd.t0)) * (3 * kTile) + 3 * tid;
+            q[0] = sx; q[1] = sy; q[2] = sz;
+        }
+        return;
+    }
     const size_t stride = 3 * (size_t)n;
     if (diag) {
         if (valid_i) {
@@ -391,6 +428,40 @@ __global__ void __launch_bounds__(kThreads) wall_rot_df_sym_kernel(const SrcDF *
                                                                     const SymJob *__restrict__ jobs)
 {
     df_sym_body<SEG, KIND>(src, n, nt, partial, jobs);
+}
+
+// The same kernels over one band of tile rows (SymBand): products whose
+// per-tile partial sums would not fit in the scratch budget.
+template <int KIND>
+__global__ void __launch_bounds__(kThreads) wall_df_sym_band_kernel(const SrcDF *__restrict__ src, int n, int nt,
+                                                                     const SymBand bd)
+{
+    df_sym_body<false, KIND, false, true>(src, n, nt, nullptr, nullptr, bd);
+}
+
+// acc (3n doubles, FP64) += the band's contributions to every blob of tiles
+// >= t0: its target-side sums (tiles in the band, S ascending) and its
+// source-side sums (T ascending), in a fixed order.
+__global__ void sym_band_accum_kernel(const SymBand bd, int n, int nt, double *__restrict__ acc)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    const int X = b / kTile, l = b % kTile;
+    if (X < bd.t0) return;
+    const int W = nt - bd.t0, C = bd.t1 - bd.t0;
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    if (X < bd.t1)
+        for (int S = X; S < nt; ++S) {
+            const double *o = bd.bt + ((size_t)(X - bd.t0) * W + (S - bd.t0)) * (3 * kTile) + 3 * l;
+            sx += o[0]; sy += o[1]; sz += o[2];
+        }
+    for (int T = bd.t0; T < min(bd.t1, X); ++T) {
+        const double *o = bd.bs + ((size_t)(X - bd.t0) * C + (T - bd.t0)) * (3 * kTile) + 3 * l;
+        sx += o[0]; sy += o[1]; sz += o[2];
+    }
+    acc[3LL * b] += sx;
+    acc[3LL * b + 1] += sy;
+    acc[3LL * b + 2] += sz;
 }
 
 // Symmetric mixed-precision UF kernel: the same grid, pairing and partial-sum
@@ -1179,7 +1250,9 @@ size_t wall_sym_partial_budget()
         b = std::max(kSymMaxPartialBytes, total / 8);
         budget[dev].store(b);
     }
-    return b;
+    // a cap on one scratch buffer (rmw_set_scratch_limit) caps the partial sums too
+    const size_t cap = scratch_limit();
+    return cap ? std::min(b, cap) : b;
 }
 
 bool wall_sym_applicable(int kind, int mode, int n, const double *L)
@@ -1289,6 +1362,69 @@ int wall_product_sym_with_scratch(int kind, const double *r, const double *v, do
     return sym_product(kind, r, v, out, n, eta, a, mode, st, scratch_ptr, nullptr);
 }
 
+// Tile rows per band of the banded symmetric product: the band's two partial
+// sum blocks (2 x rows x nt x 384 doubles) within a quarter of the symmetric
+// partial-sum budget.
+int wall_sym_band_rows(int n)
+{
+    const long long nt = (n + kTile - 1) / kTile;
+    const double per_row = 2.0 * (double)nt * 3 * kTile * sizeof(double);
+    const long long rows = (long long)((double)wall_sym_partial_budget() / 4.0 / per_row);
+    return (int)std::max(1LL, std::min(nt, rows));
+}
+
+size_t wall_sym_band_scratch_bytes(int n)
+{
+    const size_t nt = (n + kTile - 1) / kTile;
+    const size_t packed = ((sizeof(SrcDF) * (size_t)n + 255) / 256) * 256;
+    const size_t acc = ((sizeof(double) * 3 * (size_t)n + 255) / 256) * 256;
+    return packed + acc + 2 * (size_t)wall_sym_band_rows(n) * nt * 3 * kTile * sizeof(double);
+}
+
+// The df64 symmetric product band by band (SymBand): the products whose
+// per-tile partial sums exceed the scratch budget (from about 430,000 blobs on
+// a GB300) keep the symmetric kernel's one evaluation per unordered pair.
+static int sym_band_product(int kind, const double *r, const double *v, double *out, int n, double eta, double a,
+                            cudaStream_t st, void *scratch_ptr)
+{
+    const int nt = (n + kTile - 1) / kTile, C = wall_sym_band_rows(n);
+    const size_t packed = ((sizeof(SrcDF) * (size_t)n + 255) / 256) * 256;
+    const size_t accb = ((sizeof(double) * 3 * (size_t)n + 255) / 256) * 256;
+    char *base = (char *)scratch_ptr;
+    double *acc = (double *)(base + packed);
+    double *bt = (double *)(base + packed + accb);
+    double *bs = bt + (size_t)C * nt * 3 * kTile;
+    const int pb = 256, pg = (n + pb - 1) / pb;
+    pack_df_kernel<<<pg, pb, 0, st>>>(r, v, (SrcDF *)base, n, a);
+    RMW_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * 3 * (size_t)n, st));
+    void *tok = nullptr;
+    if (int rc = trace_begin(TRACE_PAIR, st, &tok)) return rc;
+    for (int t0 = 0; t0 < nt; t0 += C) {
+        const int t1 = std::min(nt, t0 + C);
+        long long ncta = 0;
+        for (int t = t0; t < t1; ++t) ncta += nt - t;
+        const SymBand bd{t0, t1, bt, bs};
+        const SrcDF *src = (const SrcDF *)base;
+        switch (kind) {
+        case RMW_UF: wall_df_sym_band_kernel<RMW_UF><<<(unsigned)ncta, kThreads, 0, st>>>(src, n, nt, bd); break;
+        case RMW_UT: wall_df_sym_band_kernel<RMW_UT><<<(unsigned)ncta, kThreads, 0, st>>>(src, n, nt, bd); break;
+        case RMW_WF: wall_df_sym_band_kernel<RMW_WF><<<(unsigned)ncta, kThreads, 0, st>>>(src, n, nt, bd); break;
+        default: wall_df_sym_band_kernel<RMW_WT><<<(unsigned)ncta, kThreads, 0, st>>>(src, n, nt, bd); break;
+        }
+        sym_band_accum_kernel<<<pg, pb, 0, st>>>(bd, n, nt, acc);
+    }
+    if (int rc = trace_end(tok, st)) return rc;
+    const double nf = kind_norm(kind, eta, a);
+    switch (kind) {
+    case RMW_UF: launch_sym_finalize<RMW_UF>(r, v, acc, 1, out, n, a, nf, nullptr, st); break;
+    case RMW_UT: launch_sym_finalize<RMW_UT>(r, v, acc, 1, out, n, a, nf, nullptr, st); break;
+    case RMW_WF: launch_sym_finalize<RMW_WF>(r, v, acc, 1, out, n, a, nf, nullptr, st); break;
+    default: launch_sym_finalize<RMW_WT>(r, v, acc, 1, out, n, a, nf, nullptr, st); break;
+    }
+    RMW_CHECK_LAUNCH("banded symmetric wall product kernels");
+    return RMW_OK;
+}
+
 int wall_product(int kind, const double *r, const double *v, double *out, int64_t n, double eta, double a,
                  const double *L, int mode, cudaStream_t st)
 {
@@ -1297,8 +1433,15 @@ int wall_product(int kind, const double *r, const double *v, double *out, int64_
     if (n == 0) return RMW_OK;
     int nchunks = wall_chunks(kind, mode, (int)n);
     bool sym = nchunks == kSymChunks && wall_sym_applicable(kind, mode, (int)n, L);
-    if (nchunks == kSymChunks && !sym) nchunks = wall_default_chunks((int)n);
+    const bool periodic = L && (L[0] > 0 || L[1] > 0 || L[2] > 0);
     void *ws = nullptr;
+    if (nchunks == kSymChunks && !sym && mode == RMW_MODE_DF64 && !periodic && n >= 2 * kTile) {
+        // too many tiles for one partial-sum slot per tile: the symmetric kernel band by band
+        if (scratch(SCRATCH_PAIR, wall_sym_band_scratch_bytes((int)n), &ws, st) == RMW_OK)
+            return sym_band_product(kind, r, v, out, (int)n, eta, a, st, ws);
+        cudaGetLastError();
+    }
+    if (nchunks == kSymChunks && !sym) nchunks = wall_default_chunks((int)n);
     rc = scratch(SCRATCH_PAIR, wall_scratch_bytes((int)n, mode, sym ? wall_sym_slots((int)n) : nchunks), &ws, st);
     if (rc && sym) {
         // the symmetric kernel's partial sums did not fit next to the caller's
@@ -1495,6 +1638,26 @@ int wall_uf_multi(const double *r, const double *V, long long ldv, double *Y, lo
 // ---------------------------------------------------------------------------
 // C ABI
 extern "C" {
+
+// How a product of (kind, mode, n) is launched on the current device: 0 the
+// one-sided kernel, 1 the symmetric kernel (one partial-sum slot per tile),
+// 2 the symmetric kernel band by band (beyond the partial-sum budget).
+int rmw_wall_product_route(int kind, int mode, int64_t n, const double *L_host, int *route_host)
+{
+    if (!route_host) return rmw::fail(RMW_ERR_ARG, "null output");
+    if (int rc = rmw::validate_product_args(kind, (void *)1, (void *)1, (void *)1, n, 1.0, 1.0, mode)) return rc;
+    const int N = (int)n;
+    const bool periodic = L_host && (L_host[0] > 0 || L_host[1] > 0 || L_host[2] > 0);
+    const int c = rmw::wall_chunks(kind, mode, N);
+    int route = 0;
+    if (c == rmw::kSymChunks) {
+        if (rmw::wall_sym_applicable(kind, mode, N, L_host)) route = 1;
+        else if (mode == RMW_MODE_DF64 && !periodic && N >= 2 * rmw::kTile) route = 2;
+    }
+    *route_host = route;
+    return RMW_OK;
+}
+
 
 int rmw_wall_product(int kind, const double *r, const double *v, double *out, int64_t n, double eta, double a,
                      const double *L_host, int mode, void *stream)

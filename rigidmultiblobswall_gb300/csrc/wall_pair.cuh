@@ -85,6 +85,9 @@ constexpr size_t kSymMaxPartialBytes = size_t(6) << 30;  // up to ~185,000 blobs
 size_t wall_sym_partial_budget();
 bool wall_sym_applicable(int kind, int mode, int n, const double *L);
 int wall_sym_slots(int n);
+// banded symmetric df64 product (above the partial-sum budget): tile rows per band, its scratch
+int wall_sym_band_rows(int n);
+size_t wall_sym_band_scratch_bytes(int n);
 int wall_product_sym_with_scratch(int kind, const double *r, const double *v, double *out, int n, double eta,
                                   double a, int mode, cudaStream_t st, void *scratch_ptr);
 // The symmetric free-space pair kernel of `kind` on records packed by the

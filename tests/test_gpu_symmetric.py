@@ -132,3 +132,62 @@ def test_symmetric_beyond_six_gib_of_partial_sums(cuda_device):
     rows = rng.choice(n, 40, replace=False)
     ref = owall.wall_product("uf", r, v, 1.0, a, rows=rows)
     assert rel_err(got.reshape(-1, 3)[rows].reshape(-1), ref) <= 1e-6
+
+
+def _route(kind, mode, n):
+    import ctypes
+    from rigidmultiblobswall_gb300 import _native
+    out = ctypes.c_int(-1)
+    _native.call("rmw_wall_product_route", _native.KINDS[kind], {"fp64": 0, "mixed": 1, "df64": 2}[mode], n, None,
+                 ctypes.byref(out))
+    return out.value
+
+
+@pytest.mark.parametrize("kind", ["uf", "ut", "wf", "wt"])
+def test_banded_symmetric_product_matches_oracle(cuda_device, kind):
+    """Above the partial-sum budget the df64 products run the symmetric kernel band by band of tile rows
+    (bands summed in a fixed order).  A 48 MB scratch cap makes 20,000 blobs (59 MB of per-tile partial
+    sums) take that route; all blocks against the oracle, the wall overlapping some blobs, and a second
+    call bit-identical to the first."""
+    from rigidmultiblobswall_gb300 import _native
+    n = 20_000
+    rng = np.random.default_rng(23)
+    r = np.empty((n, 3))
+    r[:, :2] = rng.uniform(0, 120.0, (n, 2))
+    r[:, 2] = rng.uniform(0.1, 6.0, n)
+    v = rng.standard_normal(3 * n)
+    a = 0.35
+    mob.autotune_clear()
+    _native.set_scratch_limit(48 << 20)
+    try:
+        assert _route(kind, "df64", n) == 2
+        got = mob.wall_product(kind, r, v, 1.0, a, mode="df64")
+        again = mob.wall_product(kind, r, v, 1.0, a, mode="df64")
+    finally:
+        _native.set_scratch_limit(0)
+    assert _route(kind, "df64", n) == 1
+    rows = np.concatenate([rng.choice(n, 60, replace=False), [0, 127, 128, n - 1]])
+    ref = owall.wall_product(kind, r, v, 1.0, a, rows=rows)
+    assert rel_err(got.reshape(-1, 3)[rows].reshape(-1), ref) <= 1e-12
+    assert np.array_equal(got, again)
+    full = mob.wall_product(kind, r, v, 1.0, a, mode="df64")
+    assert rel_err(got, full) <= 1e-13
+
+
+def test_half_million_blob_df64_product_runs_symmetric(cuda_device):
+    """500,000 blobs: 47 GB of per-tile partial sums, far above the budget; the df64 product still
+    evaluates each unordered pair once (banded route), sampled rows against the oracle."""
+    import torch
+    n = 500_000
+    assert _route("uf", "df64", n) == 2
+    rng = np.random.default_rng(29)
+    r = np.empty((n, 3))
+    r[:, :2] = rng.uniform(0, 700.0, (n, 2))
+    r[:, 2] = rng.uniform(0.6, 6.0, n)
+    v = rng.standard_normal(3 * n)
+    a = 0.35
+    got = mob.wall_product("uf", torch.tensor(r, device="cuda"), torch.tensor(v, device="cuda"), 1.0, a,
+                           mode="df64").cpu().numpy()
+    rows = rng.choice(n, 24, replace=False)
+    ref = owall.wall_product("uf", r, v, 1.0, a, rows=rows)
+    assert rel_err(got.reshape(-1, 3)[rows].reshape(-1), ref) <= 1e-12

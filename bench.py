@@ -38,20 +38,20 @@ WORKLOAD = "wall-RPY M_UF.F, 256 shells x 42 blobs = 10,752 blobs (FP64-accurate
 # Issued thread instructions per ordered pair of the df64 UF kernels (all
 # pipes, 80-85 % of them on the FMA pipe), from ncu's smsp__inst_executed.sum
 # on the 10,752-blob product: symmetric kernel (each unordered pair once),
-# 1,704,728,972 warp instructions * 32 / 10752^2 = 471.9; one-sided kernel
+# 1,705,420,652 warp instructions * 32 / 10752^2 = 472.1; one-sided kernel
 # (source split 15) 2,719,541,740 * 32 / 10752^2 = 752.8.  The FP32 pipe
 # issues at most one thread instruction per lane per clock, the rate the
 # FMA-chain probe measures (FLOP/s / 2), so achieved / peak is the fraction of
 # issue capacity used.  The constants hold for the kernel sources whose hash is
 # DF64_UF_KERNEL_SOURCE_SHA (tests/test_bench_constants.py fails when the
 # kernel changes without a new capture).
-DF64_UF_INST_PER_PAIR = {"symmetric": 1704728972.0 * 32 / 10752 ** 2, "standard": 2719541740.0 * 32 / 10752 ** 2}
+DF64_UF_INST_PER_PAIR = {"symmetric": 1705420652.0 * 32 / 10752 ** 2, "standard": 2719541740.0 * 32 / 10752 ** 2}
 # dram__bytes_read.sum + dram__bytes_write.sum per launch, same captures
-DF64_UF_TRAFFIC_BYTES = {"symmetric": 735744, "standard": 718848}
+DF64_UF_TRAFFIC_BYTES = {"symmetric": 736000, "standard": 718848}
 # issued thread instructions per pair and right-hand side of the 16-wide multi-RHS M_UF kernel
 # (smsp__inst_executed.sum * 32 / (N^2 * 16), 60,000 blobs)
 MULTI16_INST_PER_PAIR_RHS = 17.4
-DF64_UF_KERNEL_SOURCE_SHA = "ac909a031a188da5b8c5009d4600eab52be0b7b5c98007e539c9a289bbf64246"
+DF64_UF_KERNEL_SOURCE_SHA = "89b6f0fd4303f7413dd2bee1784d821e0f30340b3afe8b244a7c7d322d3f7b63"
 
 
 def df64_uf_kernel_source_sha():

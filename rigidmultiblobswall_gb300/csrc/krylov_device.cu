@@ -676,6 +676,19 @@ bool krylov_device_available()
     return true;
 }
 
+// CTAs the cooperative step kernels may use: as many per SM as both kernels
+// keep resident (registers, shared memory), at most 4
+static int kd_max_ctas()
+{
+    int dev = 0, sms = 1, a = 1, l = 1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, arnoldi_step_kernel, kKdThreads, 0) != cudaSuccess) a = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l, lanczos_step_kernel, kKdThreads, 0) != cudaSuccess) l = 1;
+    cudaGetLastError();
+    return sms * std::max(1, std::min(4, std::min(a, l)));
+}
+
 KrylovDev::~KrylovDev()
 {
     if (base) cudaFreeAsync(base, st);
@@ -690,7 +703,7 @@ int kd_build_jobs(const std::vector<long long> &off, int nblk_max, std::vector<K
 {
     const int nseg = (int)off.size() - 1;
     const long long n = off.back();
-    // one CTA per SM at most, at least kKdThreads elements per CTA
+    // at most nblk_max CTAs (the co-resident count), at least kKdThreads elements per CTA
     const int nblk = (int)std::max<long long>(1, std::min<long long>(nblk_max, (n + kKdThreads - 1) / kKdThreads));
     long long per = (n + nblk - 1) / nblk;
     per = ((per + 31) / 32) * 32;
@@ -731,12 +744,9 @@ int KrylovDev::init(const std::vector<long long> &seg_off, int restart, int hist
     KP = R + 2;
     hcap = hist_cap;
     ldv = ((n + 31) / 32) * 32;
-    int dev = 0, sms = 1;
-    RMW_CUDA(cudaGetDevice(&dev));
-    RMW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     std::vector<KJob> jb;
     std::vector<int> sj, bj;
-    nblk = kd_build_jobs(off, sms, jb, sj, bj);
+    nblk = kd_build_jobs(off, kd_max_ctas(), jb, sj, bj);
     njobs = (int)jb.size();
     const size_t nj = (size_t)std::max(1, njobs), ns = (size_t)nseg;
     auto al = [](size_t b) { return (b + 255) / 256 * 256; };
@@ -819,12 +829,9 @@ int LanczosDev::init(const std::vector<long long> &seg_off, int kcap_, cudaStrea
     kcap = std::max(2, kcap_);
     KP = kcap + 2;
     ldv = ((n + 31) / 32) * 32;
-    int dev = 0, sms = 1;
-    RMW_CUDA(cudaGetDevice(&dev));
-    RMW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     std::vector<KJob> jb;
     std::vector<int> sj, bj;
-    nblk = kd_build_jobs(seg_off, sms, jb, sj, bj);
+    nblk = kd_build_jobs(seg_off, kd_max_ctas(), jb, sj, bj);
     njobs = (int)jb.size();
     const size_t nj = (size_t)std::max(1, njobs), ns = (size_t)nseg, kc = (size_t)kcap;
     auto al = [](size_t b) { return (b + 255) / 256 * 256; };

@@ -8,8 +8,9 @@
 // Hessenberg matrix, Givens rotations, tolerance and iteration count.
 //
 // One Arnoldi step is two launches: the operator y = A P^-1 v (the caller's
-// kernels) and arnoldi_step_kernel, a persistent cooperative kernel (one CTA
-// per SM at most) that does the whole classical Gram-Schmidt step with one
+// kernels) and arnoldi_step_kernel, a persistent cooperative kernel (as many
+// CTAs as stay co-resident, up to 4 per SM) that does the whole classical
+// Gram-Schmidt step with one
 // reorthogonalisation (CGS2: two dot passes, two update passes, the norm and
 // the scaling of the next basis vector, separated by grid barriers), applies
 // the previous Givens rotations to the new Hessenberg column, forms the next

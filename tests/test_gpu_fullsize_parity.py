@@ -50,10 +50,10 @@ def test_shells42x256_solve_meets_oracle_residual(cfg2, arm):
     if arm.endswith("nearfield"):
         from rigidmultiblobswall_gb300 import nearfield as nf
         R = float(np.linalg.norm(s2.shell[0]))
-        feat, targ = nf.pair_training_data(s2.shell, s2.a, 1.0, 1024, d_range=(2 * R + 2 * s2.a, 6 * R),
-                                           z_range=(1.1 * R, 5 * R), seed=11, device=sys2.device)
+        graphs = nf.cluster_training_data(s2.shell, s2.a, 1.0, 256, d_range=(2 * R + 2 * s2.a, 6 * R),
+                                          z_range=(1.1 * R, 5 * R), seed=11, device=sys2.device)
         model = nf.NearfieldModel(body_radius=R, cutoff=6 * R, seed=2)
-        model.train(feat, targ, steps=600, batch=512, lr=2e-3)
+        model.train(graphs, steps=600, lr=2e-3)
         model.attach(sys2, exact_cutoff=3 * R)
     try:
         sol, info, its, rr = integrator.solve_mobility_problem(sys2, FT, tol=1e-8, mode=mode)

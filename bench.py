@@ -87,6 +87,9 @@ def parse():
                    help="only run the 4096-shell (172,032-blob) solve comparison and print its JSON line")
     p.add_argument("--large-modes",
                    default="fp64,mixed,mixed+exact,mixed+learned,mixed+learned_band,mixed+exact+learned")
+    p.add_argument("--krylov-probe", action="store_true",
+                   help="only the 4096-shell mixed solve with graphs off (each fused Arnoldi step a traced direct "
+                        "launch) and the pair scratch capped at 1 GiB: the Arnoldi steps' time and bandwidth")
     p.add_argument("--multi", default=None, metavar="N:NRHS",
                    help="only time the multi-right-hand-side M_UF product on N blobs with NRHS vectors")
     p.add_argument("--product", default=None, metavar="KIND:MODE",
@@ -838,8 +841,39 @@ def multi_product(args):
                       "tpair_rhs_per_s": n * n * nrhs / (ms * 1e-3) / 1e12}))
 
 
+def krylov_probe():
+    """The 4096-shell mixed solve with every fused Arnoldi step launched and traced on its own (graphs off)
+    and the product scratch capped at 1 GiB (one-sided pair kernels, small device footprint): one JSON line
+    with the solve time and the Arnoldi steps' time, algorithmic bytes and bandwidth."""
+    import torch
+    from rigidmultiblobswall_gb300 import build as B
+    B.build()
+    from rigidmultiblobswall_gb300 import _native, integrator
+    from rigidmultiblobswall_gb300 import suspensions as S
+    from rigidmultiblobswall_gb300.rigid import RigidSystem
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    _native.set_scratch_limit(1 << 30)
+    s5 = S.shells_42_4096()
+    sys5 = RigidSystem([42] * s5.n_bodies, s5.eta, s5.a, device=dev)
+    sys5.set_configuration(s5.r_vectors(), s5.locations)
+    FT = np.zeros((s5.n_bodies, 6))
+    FT[:, 2] = -1.0
+    sys5.build_pc(mode="mixed")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    (sol, info, its, rr), arn = arnoldi_traffic(
+        lambda: integrator.solve_mobility_problem(sys5, FT, tol=1e-8, mode="mixed"))
+    torch.cuda.synchronize()
+    print(json.dumps({"solve_ms": (time.perf_counter() - t0) * 1e3, "iterations": its, "relres": rr,
+                      "arnoldi": arn}))
+
+
 def main():
     args = parse()
+    if args.krylov_probe:
+        krylov_probe()
+        return
     if args.large:
         large_solve(args)
         return

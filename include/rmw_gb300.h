@@ -272,6 +272,12 @@ int rmw_rigid_build_pc_mode(void *handle, int stochastic, int mode);
 int rmw_rigid_apply(void *handle, const double *x, double *y, int mode);
 /* y = P^-1 x  (block_diagonal_preconditioner apply, multi_bodies.py:825-861). */
 int rmw_rigid_apply_pc(void *handle, const double *x, double *y);
+/* The same apply as the solves of one precision mode run it (same operator as
+ * multi_bodies.py:825-861, plus the attached near-field augmentation): FP64 for
+ * RMW_MODE_FP64 / RMW_MODE_DF64; FP32 arithmetic on FP32 copies of the body
+ * blocks for RMW_MODE_MIXED (~1e-7 relative: the mixed solves refine with an
+ * FP64-accurate residual, so their preconditioner needs no FP64 arithmetic). */
+int rmw_rigid_apply_pc_mode(void *handle, const double *x, double *y, int mode);
 /* y = L^-1 M L^-T w on the 3N blob space (det_stoch mobility_pc, multi_bodies.py:591-606). */
 int rmw_rigid_mobility_pc(void *handle, const double *w, double *y, int mode);
 /* y = L w  (det_stoch P_inv_mult, multi_bodies.py:609-615). */

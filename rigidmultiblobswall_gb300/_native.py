@@ -77,6 +77,7 @@ SIGNATURES = {
     "rmw_rigid_build_pc_mode": (_i, [_vp, _i, _i]),
     "rmw_rigid_apply": (_i, [_vp, _vp, _vp, _i]),
     "rmw_rigid_apply_pc": (_i, [_vp, _vp, _vp]),
+    "rmw_rigid_apply_pc_mode": (_i, [_vp, _vp, _vp, _i]),
     "rmw_rigid_mobility_pc": (_i, [_vp, _vp, _vp, _i]),
     "rmw_rigid_P_inv_mult": (_i, [_vp, _vp, _vp]),
     "rmw_rigid_K_mult": (_i, [_vp, _vp, _vp]),

@@ -615,7 +615,13 @@ static int rigid_solve_impl(void *sys, const double *rhs, double *sol, double to
         if (int rc = rmw_rigid_build_pc_mode(sys, 0, mode)) return rc;
     }
     const long long n = S.sys_size();
-    auto pc = [&](const double *x, double *y) { return rmw::rigid_apply_pc(S, x, y); };
+    // the mixed solves apply the preconditioner in FP32 (their refinement
+    // residual is FP64-accurate); its FP32 copies are made before any capture
+    if (mode == RMW_MODE_MIXED)
+        if (int rc = rmw::rigid_pc_prepare_f32(S)) return rc;
+    auto pc = [&](const double *x, double *y) {
+        return mode == RMW_MODE_MIXED ? rmw::rigid_apply_pc_mixed(S, x, y) : rmw::rigid_apply_pc(S, x, y);
+    };
     // A P^-1 fused through a private buffer and replayed as one CUDA graph
     double *pbuf = nullptr;
     RMW_CUDA(cudaMallocAsync(&pbuf, sizeof(double) * n, S.st));
@@ -626,7 +632,7 @@ static int rigid_solve_impl(void *sys, const double *rhs, double *sol, double to
     } free_p{pbuf, S.st};
     auto fused = [&](int m) {
         return [&, m](const double *x, double *y) -> int {
-            if (int rc = rmw::rigid_apply_pc(S, x, pbuf)) return rc;
+            if (int rc = pc(x, pbuf)) return rc;
             return rmw::rigid_apply(S, pbuf, y, m);
         };
     };

@@ -648,9 +648,19 @@ int rmw_rigid_solve_batched(void *sys, const double *rhs, double *sol, double to
             return RMW_OK;
         };
     };
+    // the mixed solves apply the preconditioner in FP32 (see rigid_solve_impl)
+    if (mode == RMW_MODE_MIXED) {
+        if (int rc0 = rmw::rigid_pc_prepare_f32(S)) {
+            cudaFreeAsync(buf, st);
+            return rc0;
+        }
+    }
+    auto apply_pc = [&](const double *x, double *y) {
+        return mode == RMW_MODE_MIXED ? rmw::rigid_apply_pc_mixed(S, x, y) : rmw::rigid_apply_pc(S, x, y);
+    };
     auto pc = [&](const double *xi, double *yi) -> int {
         to_global(xi, gx);
-        if (int rc = rmw::rigid_apply_pc(S, gx, gy)) return rc;
+        if (int rc = apply_pc(gx, gy)) return rc;
         to_im(gy, yi);
         return RMW_OK;
     };
@@ -659,7 +669,7 @@ int rmw_rigid_solve_batched(void *sys, const double *rhs, double *sol, double to
     auto pcop_mode = [&](int m) {
         return [&, m](const double *xi, double *yi) -> int {
             to_global(xi, gx);
-            if (int rc = rmw::rigid_apply_pc(S, gx, gy)) return rc;
+            if (int rc = apply_pc(gx, gy)) return rc;
             if (int rc = rmw::rigid_apply(S, gy, gx, m)) return rc;
             to_im(gx, yi);
             return RMW_OK;

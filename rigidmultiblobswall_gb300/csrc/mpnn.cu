@@ -53,31 +53,38 @@ __device__ __forceinline__ void mma_bf16(float c[4], unsigned a0, unsigned a1, u
 
 // Z = X W^T + b (rows [0, P), P a multiple of 16); X: P x nin, W: nout x nin
 // (BF16, row-major).  Outputs (each optional): Z (FP32 pre-activation), Y =
-// bf16(act(Z)), Yf = act(Z) in FP32.  One warp per 16-row tile.
+// bf16(act(Z)), Yf = act(Z) in FP32; nout a multiple of 16.
 __global__ void mp_dense_kernel(const __nv_bfloat16 *__restrict__ X, int nin, const __nv_bfloat16 *__restrict__ Wt,
                                 const float *__restrict__ bias, int nout, float *__restrict__ Z,
                                 __nv_bfloat16 *__restrict__ Y, float *__restrict__ Yf, int P, int act)
 {
+    // one warp per 16 rows x 16 output columns: two 16 x 8 tiles sharing the
+    // row fragments
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    const int row0 = warp * 16;
+    const int ngrp = nout >> 4;
+    const int row0 = (warp / ngrp) * 16, n0 = (warp % ngrp) * 16;
     if (row0 >= P) return;
     const int g = lane >> 2, tq = lane & 3;
-    for (int n0 = 0; n0 < nout; n0 += 8) {
-        float c[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int k0 = 0; k0 < nin; k0 += 16) {
-            const int kc = k0 + tq * 2;
-            const unsigned a0 = *(const unsigned *)(X + (long long)(row0 + g) * nin + kc);
-            const unsigned a1 = *(const unsigned *)(X + (long long)(row0 + g + 8) * nin + kc);
-            const unsigned a2 = *(const unsigned *)(X + (long long)(row0 + g) * nin + kc + 8);
-            const unsigned a3 = *(const unsigned *)(X + (long long)(row0 + g + 8) * nin + kc + 8);
-            const unsigned b0 = *(const unsigned *)(Wt + (long long)(n0 + g) * nin + kc);
-            const unsigned b1 = *(const unsigned *)(Wt + (long long)(n0 + g) * nin + kc + 8);
-            mma_bf16(c, a0, a1, a2, a3, b0, b1);
+    float c[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    for (int k0 = 0; k0 < nin; k0 += 16) {
+        const int kc = k0 + tq * 2;
+        const unsigned a0 = *(const unsigned *)(X + (long long)(row0 + g) * nin + kc);
+        const unsigned a1 = *(const unsigned *)(X + (long long)(row0 + g + 8) * nin + kc);
+        const unsigned a2 = *(const unsigned *)(X + (long long)(row0 + g) * nin + kc + 8);
+        const unsigned a3 = *(const unsigned *)(X + (long long)(row0 + g + 8) * nin + kc + 8);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const unsigned b0 = *(const unsigned *)(Wt + (long long)(n0 + 8 * h + g) * nin + kc);
+            const unsigned b1 = *(const unsigned *)(Wt + (long long)(n0 + 8 * h + g) * nin + kc + 8);
+            mma_bf16(c[h], a0, a1, a2, a3, b0, b1);
         }
-        const int col = n0 + tq * 2;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int col = n0 + 8 * h + tq * 2;
         for (int e = 0; e < 4; ++e) {
             const int rr = row0 + g + (e >= 2 ? 8 : 0), cc = col + (e & 1);
-            const float z = c[e] + bias[cc];
+            const float z = c[h][e] + bias[cc];
             const float y = act ? mp_silu(z) : z;
             if (Z) Z[(long long)rr * nout + cc] = z;
             if (Y) Y[(long long)rr * nout + cc] = __float2bfloat16_rn(y);
@@ -407,8 +414,8 @@ const float *mp_outputs(const MpWork &W) { return W.Yf; }
 static void dense(MpnnNet &net, int l, const __nv_bfloat16 *X, int rows, float *Z, __nv_bfloat16 *Y, float *Yf,
                   bool act, cudaStream_t st)
 {
-    const int warps = rows / 16;
-    mp_dense_kernel<<<(warps * 32 + 127) / 128, 128, 0, st>>>(X, mp_layer_in(l), net.wb + mp_wofs(l),
+    const long long warps = (long long)(rows / 16) * (mp_layer_out(l) / 16);
+    mp_dense_kernel<<<(unsigned)((warps * 32 + 127) / 128), 128, 0, st>>>(X, mp_layer_in(l), net.wb + mp_wofs(l),
                                                               net.b + mp_bofs(l), mp_layer_out(l), Z, Y, Yf, rows,
                                                               act ? 1 : 0);
 }

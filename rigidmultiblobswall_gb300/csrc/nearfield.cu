@@ -384,76 +384,56 @@ __global__ void pair_list_kernel(const double *__restrict__ r, const double *__r
 // neighbour lists: ordered pairs (i, j != i) of one suspension by centre
 // distance (minimum image)
 
-// The neighbour lists of body i in one pass over the bodies of its
-// suspension: exact pairs (d < cut_ex), learned pairs (cut_ex <= d < cut_ln
-// and d >= cut_lf) and the message-passing neighbours (d < cut_mp).
-// ex_off == NULL: cnt[i], cnt[nb + i], cnt[2 nb + i] = the three counts; else
-// fill the lists (ascending neighbour index).  Body centres are staged through shared memory
-// in tiles of blockDim bodies, covering the union of the block's ranges.  The
-// distance test runs in FP32 (a neighbour test needs no more; both passes use
-// the same arithmetic, so counts and lists agree).
+// Neighbour bands of every body, one warp per body: the lanes take the
+// candidates j of the body's suspension in ascending order, 32 at a time; the
+// count pass (cnt != null) counts the exact (d < cut_ex), learned
+// (cut_lf <= d < cut_ln, not exact) and message-passing (d < cut_mp) hits; the
+// fill pass writes each band's hits at the body's CSR offset, placed by the
+// ballot prefix of the lane, so every list is sorted by j.  Distances are
+// formed in FP32 from FP32 centres (minimum image in periodic directions).
 __global__ void nbr_bands_kernel(const double *__restrict__ xb, int nb, float cut_ex2, float cut_lf2, float cut_ln2,
                                  float cut_mp2, Images P, const int2 *__restrict__ range, int *__restrict__ cnt,
                                  const int *__restrict__ ex_off, int *__restrict__ ex_idx,
                                  const int *__restrict__ ln_off, int *__restrict__ ln_idx,
                                  const int *__restrict__ mp_off, int *__restrict__ mp_idx)
 {
-    extern __shared__ float tile[];  // 3 x blockDim
-    __shared__ int blo, bhi;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < nb;
-    const int2 rg = valid ? (range ? range[i] : make_int2(0, nb)) : make_int2(0, 0);
-    if (threadIdx.x == 0) {
-        blo = nb;
-        bhi = 0;
-    }
-    __syncthreads();
-    if (valid) {
-        atomicMin(&blo, rg.x);
-        atomicMax(&bhi, rg.y);
-    }
-    __syncthreads();
-    const float xi = valid ? (float)xb[3 * i] : 0.f, yi = valid ? (float)xb[3 * i + 1] : 0.f,
-                zi = valid ? (float)xb[3 * i + 2] : 0.f;
+    const int i = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (i >= nb) return;  // i is uniform across the warp
+    const int2 rg = range ? range[i] : make_int2(0, nb);
+    const float xi = (float)xb[3 * i], yi = (float)xb[3 * i + 1], zi = (float)xb[3 * i + 2];
     const float Lx = (float)P.Lx, Ly = (float)P.Ly, Lz = (float)P.Lz;
-    int ce = (valid && ex_off) ? ex_off[i] : 0, cl = (valid && ln_off) ? ln_off[i] : 0;
-    int cm = (valid && mp_off) ? mp_off[i] : 0;
-    int ne = 0, nl = 0, nm = 0;
     const bool fill = ex_off != nullptr;
-    const int lo = blo, hi = bhi, nt = blockDim.x;
-    for (int t0 = lo; t0 < hi; t0 += nt) {
-        const int j = t0 + threadIdx.x;
-        if (j < hi) {
-            tile[threadIdx.x] = (float)xb[3 * j];
-            tile[nt + threadIdx.x] = (float)xb[3 * j + 1];
-            tile[2 * nt + threadIdx.x] = (float)xb[3 * j + 2];
+    int ce = fill ? ex_off[i] : 0, cl = fill ? ln_off[i] : 0, cm = fill ? mp_off[i] : 0;
+    int ne = 0, nl = 0, nm = 0;
+    const unsigned below = (1u << lane) - 1u;
+    for (int j0 = rg.x; j0 < rg.y; j0 += 32) {
+        const int j = j0 + lane;
+        bool ex = false, ln = false, mp = false;
+        if (j < rg.y && j != i) {
+            float dx = (float)xb[3 * j] - xi, dy = (float)xb[3 * j + 1] - yi, dz = (float)xb[3 * j + 2] - zi;
+            if (Lx > 0.f) dx = project(dx, Lx);
+            if (Ly > 0.f) dy = project(dy, Ly);
+            if (Lz > 0.f) dz = project(dz, Lz);
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            ex = d2 < cut_ex2;
+            ln = !ex && d2 < cut_ln2 && d2 >= cut_lf2;
+            mp = d2 < cut_mp2;
         }
-        __syncthreads();
-        const int cntk = min(nt, hi - t0);
-        if (valid)
-            for (int k = 0; k < cntk; ++k) {
-                const int jj = t0 + k;
-                if (jj == i || jj < rg.x || jj >= rg.y) continue;
-                float dx = tile[k] - xi, dy = tile[nt + k] - yi, dz = tile[2 * nt + k] - zi;
-                if (Lx > 0.f) dx = project(dx, Lx);
-                if (Ly > 0.f) dy = project(dy, Ly);
-                if (Lz > 0.f) dz = project(dz, Lz);
-                const float d2 = dx * dx + dy * dy + dz * dz;
-                if (d2 < cut_ex2) {
-                    if (fill) ex_idx[ce++] = jj;
-                    ++ne;
-                } else if (d2 < cut_ln2 && d2 >= cut_lf2) {
-                    if (fill) ln_idx[cl++] = jj;
-                    ++nl;
-                }
-                if (d2 < cut_mp2) {
-                    if (fill) mp_idx[cm++] = jj;
-                    ++nm;
-                }
-            }
-        __syncthreads();
+        const unsigned me = __ballot_sync(0xffffffffu, ex), ml = __ballot_sync(0xffffffffu, ln),
+                       mm = __ballot_sync(0xffffffffu, mp);
+        if (fill) {
+            if (ex) ex_idx[ce + __popc(me & below)] = j;
+            if (ln) ln_idx[cl + __popc(ml & below)] = j;
+            if (mp) mp_idx[cm + __popc(mm & below)] = j;
+        }
+        ce += __popc(me);
+        cl += __popc(ml);
+        cm += __popc(mm);
+        ne += __popc(me);
+        nl += __popc(ml);
+        nm += __popc(mm);
     }
-    if (valid && !fill) {
+    if (!fill && lane == 0) {
         cnt[i] = ne;
         cnt[nb + i] = nl;
         cnt[2 * nb + i] = nm;
@@ -696,6 +676,379 @@ int nearfield_apply_pc(RigidSystem &S, const double *x, double *y)
     return RMW_OK;
 }
 
+// ---------------------------------------------------------------------------
+// FP32 preconditioner apply of the mixed-precision solves
+//
+// A mixed solve's inner GMRES runs on FP32 pair products to a 1e-5 relative
+// residual and its refinement residual is FP64-accurate, so its preconditioner
+// needs no FP64 arithmetic: any fixed approximate inverse serves, and the FP32
+// rounding of the apply (~1e-7) stays far below the inner tolerance.  On GB300
+// the FP64 pipe runs at 1/64 of the FP32 rate and the FP64 apply's dependent
+// multiply-add chains (one m x m block per body) are latency-bound on it.  The
+// FP32 form reads FP32 copies of M_b^-1, M_b^-1 K, N_b, of the learned
+// couplings and of the blob geometry (offset from the body centre, height),
+// so that no FP64 instruction is left in its loops.  The plain apply is one
+// kernel, the augmented apply two:
+//   pc_apply_f32_kernel<true>  y0 = P0 x, the damped blob forces b lambda(y0)
+//                              in FP32 and the 11 mode moments of lambda(y0);
+//   nf_correct_f32_kernel      per body i: v_i from the exact pairs (blob by
+//                              blob, FP32 pair math) and the learned modes,
+//                              z_i = P0_i [v_i; 0], y_i = y0_i - z_i.
+// Every sum runs in a fixed order, so the apply is deterministic.
+
+constexpr int kPcF32Threads = 128;
+constexpr int kPcF32MaxM = 1536;  // 512 blobs per body: shared-memory layout bound
+
+__device__ __forceinline__ void mode_velocity_f(int c, float dx, float dy, float dz, float &vx, float &vy, float &vz)
+{
+    const float s2 = (float)kS2, s6 = (float)kS6;
+    switch (c) {
+    case 0: vx = 1.f; vy = 0.f; vz = 0.f; break;
+    case 1: vx = 0.f; vy = 1.f; vz = 0.f; break;
+    case 2: vx = 0.f; vy = 0.f; vz = 1.f; break;
+    case 3: vx = 0.f; vy = -dz; vz = dy; break;
+    case 4: vx = dz; vy = 0.f; vz = -dx; break;
+    case 5: vx = -dy; vy = dx; vz = 0.f; break;
+    case 6: vx = s2 * dx; vy = -s2 * dy; vz = 0.f; break;
+    case 7: vx = -s6 * dx; vy = -s6 * dy; vz = 2.f * s6 * dz; break;
+    case 8: vx = s2 * dy; vy = s2 * dx; vz = 0.f; break;
+    case 9: vx = s2 * dz; vy = 0.f; vz = s2 * dx; break;
+    default: vx = 0.f; vy = s2 * dz; vz = s2 * dy; break;
+    }
+}
+
+// blob32[i] = (r_i - x_b, z_i) in FP32, b the body of blob i
+__global__ void blob_geometry_f32_kernel(const double *__restrict__ r, const double *__restrict__ xb,
+                                         const int *__restrict__ blob_body, int n, float4 *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int b = blob_body[i];
+    out[i] = make_float4((float)(r[3 * i] - xb[3 * b]), (float)(r[3 * i + 1] - xb[3 * b + 1]),
+                         (float)(r[3 * i + 2] - xb[3 * b + 2]), (float)r[3 * i + 2]);
+}
+
+// unscaled wall-RPY velocity at a blob from a blob carrying v (already damped),
+// FP32: d = (centre difference, rounded once) + (offset difference); heights
+// clamped at a; periodic directions by the same images as the all-pairs product
+__device__ __forceinline__ void wall_uf_pair_f(float dx, float dy, float dz, float zi, float zj, float a, float inva,
+                                               const Images &P, float Lx, float Ly, float Lz, float vx, float vy,
+                                               float vz, float &ux, float &uy, float &uz)
+{
+    const float zie = zi <= a ? a : zi, zje = zj <= a ? a : zj;
+    const float hi = zie * inva, hj = zje * inva, Rz = (zie + zje) * inva;
+    dz = zie - zje;  // the clamped heights' difference, as the FP64 pair uses
+    if (!(Lx > 0.f || Ly > 0.f || Lz > 0.f)) {
+        float cx = 0.f, cy = 0.f, cz = 0.f;
+        pair_contrib<RMW_UF, float>(dx * inva, dy * inva, dz * inva, Rz, hi, hj, vx, vy, vz, cx, cy, cz);
+        ux += cx; uy += cy; uz += cz;
+        return;
+    }
+    if (Lx > 0.f) dx = project(dx, Lx);
+    if (Ly > 0.f) dy = project(dy, Ly);
+    if (Lz > 0.f) dz = project(dz, Lz);
+    const int px = Lx > 0.f, py = Ly > 0.f, pz = Lz > 0.f;
+    for (int bx = -px; bx <= px; ++bx)
+        for (int by = -py; by <= py; ++by)
+            for (int bz = -pz; bz <= pz; ++bz) {
+                float cx = 0.f, cy = 0.f, cz = 0.f;
+                pair_contrib<RMW_UF, float>((dx + bx * Lx) * inva, (dy + by * Ly) * inva, (dz + bz * Lz) * inva, Rz,
+                                            hi, hj, vx, vy, vz, cx, cy, cz);
+                ux += cx; uy += cy; uz += cz;
+            }
+}
+
+// lam = M_b^-1 s + (M_b^-1 K) U with U = N_b (-F - K^T M_b^-1 s), in FP32, for
+// body b (the whole CTA): s and lam hold m floats in shared memory, part at
+// least blockDim.x floats, red 6 (warps + 1) floats, U 6 floats; F holds the
+// body's six force rows, or is null for zero forces.
+__device__ void pc_block_f32(int o, int m, const float *__restrict__ Mi, const float *__restrict__ MK,
+                             const float *__restrict__ Nb, const float4 *__restrict__ geo, const float *s,
+                             const float *F, float *lam, float *part, float *red, float *U)
+{
+    const int tid = threadIdx.x, nt = blockDim.x, nw = nt >> 5;
+    // M_b^-1 s, M^-1 symmetric (columns read coalesced); rows shorter than
+    // the CTA split their sources over G groups, summed in group order
+    const int G = m <= nt ? nt / m : 1;
+    if (G > 1) {
+        if (tid < G * m) {
+            const int g = tid / m, t = tid - g * m;
+            float a0 = 0.f, a1 = 0.f;
+            int k = g;
+            for (; k + G < m; k += 2 * G) {
+                a0 = fmaf(Mi[(long long)k * m + t], s[k], a0);
+                a1 = fmaf(Mi[(long long)(k + G) * m + t], s[k + G], a1);
+            }
+            if (k < m) a0 = fmaf(Mi[(long long)k * m + t], s[k], a0);
+            part[g * m + t] = a0 + a1;
+        }
+        __syncthreads();
+        for (int t = tid; t < m; t += nt) {
+            float acc = 0.f;
+            for (int g = 0; g < G; ++g) acc += part[g * m + t];
+            lam[t] = acc;
+        }
+    } else {
+        for (int t = tid; t < m; t += nt) {
+            float a0 = 0.f, a1 = 0.f;
+            int k = 0;
+            for (; k + 1 < m; k += 2) {
+                a0 = fmaf(Mi[(long long)k * m + t], s[k], a0);
+                a1 = fmaf(Mi[(long long)(k + 1) * m + t], s[k + 1], a1);
+            }
+            if (k < m) a0 = fmaf(Mi[(long long)k * m + t], s[k], a0);
+            lam[t] = a0 + a1;
+        }
+    }
+    __syncthreads();
+    // K^T M_b^-1 s
+    float p6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int p = tid; p < m / 3; p += nt) {
+        const float4 d = geo[o + p];
+        const float lx = lam[3 * p], ly = lam[3 * p + 1], lz = lam[3 * p + 2];
+        p6[0] += lx; p6[1] += ly; p6[2] += lz;
+        p6[3] += d.y * lz - d.z * ly;
+        p6[4] += d.z * lx - d.x * lz;
+        p6[5] += d.x * ly - d.y * lx;
+    }
+    const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        for (int off = 16; off > 0; off >>= 1) p6[c] += __shfl_xor_sync(0xffffffffu, p6[c], off);
+        if (lane == 0) red[6 * wid + c] = p6[c];
+    }
+    __syncthreads();
+    if (tid < 6) {
+        float ktl = 0.f;
+        for (int w = 0; w < nw; ++w) ktl += red[6 * w + tid];
+        red[6 * nw + tid] = (F ? -F[tid] : 0.f) - ktl;
+    }
+    __syncthreads();
+    if (tid < 6) {
+        float u = 0.f;
+        for (int c = 0; c < 6; ++c) u = fmaf(Nb[6 * tid + c], red[6 * nw + c], u);
+        U[tid] = u;
+    }
+    __syncthreads();
+    for (int t = tid; t < m; t += nt) {
+        float acc = lam[t];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) acc = fmaf(MK[6 * t + c], U[c], acc);
+        lam[t] = acc;
+    }
+    __syncthreads();
+}
+
+// y = P0 x in FP32 (one CTA per body).  NF: also the damped blob forces
+// lam32 = b lambda of the result (the exact pairs' sources) and the 11 mode
+// moments X_b^T lambda_b (the learned couplings' inputs; mom may be null).
+template <bool NF>
+__global__ void __launch_bounds__(kPcF32Threads)
+    pc_apply_f32_kernel(const double *__restrict__ x, double *__restrict__ y, const float4 *__restrict__ geo,
+                        const int *__restrict__ boff, const long long *__restrict__ moff,
+                        const float *__restrict__ minv, const float *__restrict__ minvK,
+                        const float *__restrict__ nmat, int n, float a, float *__restrict__ lam32,
+                        float *__restrict__ mom)
+{
+    extern __shared__ float shf[];
+    __shared__ float U[6], F[6];
+    const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x, nw = nt >> 5;
+    const int o = boff[b], m = 3 * (boff[b + 1] - o);
+    float *s = shf, *lam = s + m, *part = lam + m, *red = part + nt;
+    for (int t = tid; t < m; t += nt) s[t] = (float)x[3LL * o + t];
+    if (tid < 6) F[tid] = (float)x[3LL * n + 6LL * b + tid];
+    __syncthreads();
+    pc_block_f32(o, m, minv + moff[b], minvK + 18LL * o, nmat + 36LL * b, geo, s, F, lam, part, red, U);
+    for (int t = tid; t < m; t += nt) y[3LL * o + t] = (double)lam[t];
+    if (tid < 6) y[3LL * n + 6LL * b + tid] = (double)U[tid];
+    if constexpr (NF) {
+        const float inva = 1.f / a;
+        for (int t = tid; t < m; t += nt) {
+            const float z = geo[o + t / 3].w;
+            lam32[3LL * o + t] = (z < a ? z * inva : 1.f) * lam[t];
+        }
+        if (mom) {
+            float acc[kModes];
+#pragma unroll
+            for (int k = 0; k < kModes; ++k) acc[k] = 0.f;
+            for (int p = tid; p < m / 3; p += nt) {
+                const float4 d = geo[o + p];
+                const float lx = lam[3 * p], ly = lam[3 * p + 1], lz = lam[3 * p + 2];
+#pragma unroll
+                for (int k = 0; k < kModes; ++k) {
+                    float vx, vy, vz;
+                    mode_velocity_f(k, d.x, d.y, d.z, vx, vy, vz);
+                    acc[k] = fmaf(vx, lx, fmaf(vy, ly, fmaf(vz, lz, acc[k])));
+                }
+            }
+            const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+            for (int k = 0; k < kModes; ++k) {
+                for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], off);
+                if (lane == 0) part[kModes * wid + k] = acc[k];  // part is free again (nw x 11 <= nt floats)
+            }
+            __syncthreads();
+            if (tid < kModes) {
+                float sum = 0.f;
+                for (int w = 0; w < nw; ++w) sum += part[kModes * w + tid];
+                mom[kModes * b + tid] = sum;
+            }
+        }
+    }
+}
+
+// y = y0 - P0 [v; 0] with v the near-field blob velocities of lambda(y0):
+// exact pairs blob by blob (threads split as target blob x source subset,
+// subsets summed in order), learned pairs through the mode moments.
+__global__ void __launch_bounds__(kPcF32Threads)
+    nf_correct_f32_kernel(const double *__restrict__ y0, double *__restrict__ y, const float4 *__restrict__ geo,
+                          const double *__restrict__ xb, const int *__restrict__ boff,
+                          const long long *__restrict__ moff, const float *__restrict__ minv,
+                          const float *__restrict__ minvK, const float *__restrict__ nmat, int n,
+                          const int *__restrict__ ex_off, const int *__restrict__ ex_idx,
+                          const float *__restrict__ lam32, const int *__restrict__ ln_off,
+                          const int *__restrict__ ln_idx, const float *__restrict__ G, const float *__restrict__ mom,
+                          float a, float nfac, Images P)
+{
+    extern __shared__ float shf[];
+    __shared__ float U[6], cm[kModes], cmp[kModes * kModes];
+    const int b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+    const int o = boff[b], nbl = boff[b + 1] - o, m = 3 * nbl;
+    float *v = shf, *lam = v + m, *part = lam + m, *red = part + 3 * max(nt, nbl);
+    const float inva = 1.f / a;
+    const float Lx = (float)P.Lx, Ly = (float)P.Ly, Lz = (float)P.Lz;
+    // exact pairs
+    const int nsplit = max(1, nt / nbl);
+    const int e0 = ex_off ? ex_off[b] : 0, e1 = ex_off ? ex_off[b + 1] : 0;
+    for (int w = tid; w < nbl * nsplit; w += nt) {
+        const int t = w % nbl, sp = w / nbl;
+        const float4 gt = geo[o + t];
+        float ux = 0.f, uy = 0.f, uz = 0.f;
+        for (int q = e0; q < e1; ++q) {
+            const int j = ex_idx[q], oj = boff[j], nj = boff[j + 1] - oj;
+            // centre difference in FP64, rounded once per neighbour
+            const float cx = (float)(xb[3 * b] - xb[3 * j]), cy = (float)(xb[3 * b + 1] - xb[3 * j + 1]);
+            for (int s = sp; s < nj; s += nsplit) {
+                const float4 gs = geo[oj + s];
+                const float *ls = lam32 + 3LL * (oj + s);
+                wall_uf_pair_f(cx + (gt.x - gs.x), cy + (gt.y - gs.y), 0.f, gt.w, gs.w, a, inva, P, Lx, Ly, Lz,
+                               ls[0], ls[1], ls[2], ux, uy, uz);
+            }
+        }
+        part[3 * w] = ux;
+        part[3 * w + 1] = uy;
+        part[3 * w + 2] = uz;
+    }
+    // learned pairs: cm = sum_q G_q mom_j(q), entry (k, l) per thread, then rows in order
+    if (tid < kModes * kModes) {
+        float acc = 0.f;
+        if (ln_off)
+            for (int q = ln_off[b]; q < ln_off[b + 1]; ++q)
+                acc = fmaf(G[121LL * q + tid], mom[kModes * ln_idx[q] + tid % kModes], acc);
+        cmp[tid] = acc;
+    }
+    __syncthreads();
+    if (tid < kModes) {
+        float c = 0.f;
+        for (int l = 0; l < kModes; ++l) c += cmp[kModes * tid + l];
+        cm[tid] = c;
+    }
+    __syncthreads();
+    for (int t = tid; t < nbl; t += nt) {
+        float ux = 0.f, uy = 0.f, uz = 0.f;
+        for (int sp = 0; sp < nsplit; ++sp) {
+            const float *pp = part + 3 * (sp * nbl + t);
+            ux += pp[0]; uy += pp[1]; uz += pp[2];
+        }
+        const float4 gt = geo[o + t];
+        const float sc = nfac * (gt.w < a ? gt.w * inva : 1.f);
+        float wx = sc * ux, wy = sc * uy, wz = sc * uz;
+#pragma unroll
+        for (int k = 0; k < kModes; ++k) {
+            float mx, my, mz;
+            mode_velocity_f(k, gt.x, gt.y, gt.z, mx, my, mz);
+            wx = fmaf(mx, cm[k], wx);
+            wy = fmaf(my, cm[k], wy);
+            wz = fmaf(mz, cm[k], wz);
+        }
+        v[3 * t] = wx;
+        v[3 * t + 1] = wy;
+        v[3 * t + 2] = wz;
+    }
+    __syncthreads();
+    pc_block_f32(o, m, minv + moff[b], minvK + 18LL * o, nmat + 36LL * b, geo, v, nullptr, lam, part, red, U);
+    for (int t = tid; t < m; t += nt) y[3LL * o + t] = y0[3LL * o + t] - (double)lam[t];
+    if (tid < 6) y[3LL * n + 6LL * b + tid] = y0[3LL * n + 6LL * b + tid] - (double)U[tid];
+}
+
+__global__ void to_f32_kernel(const double *__restrict__ x, float *__restrict__ y, long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        y[i] = (float)x[i];
+}
+
+static void to_f32(const double *x, float *y, long long n, cudaStream_t st)
+{
+    if (n <= 0) return;
+    const unsigned g = (unsigned)std::min<long long>((n + 255) / 256, 152LL * 16);
+    to_f32_kernel<<<g, 256, 0, st>>>(x, y, n);
+}
+
+int rigid_pc_prepare_f32(RigidSystem &S)
+{
+    if (!S.pc_ready) return fail(RMW_ERR_ARG, "preconditioner not built (call rmw_rigid_build_pc)");
+    if (S.pc32_ready || S.max_m > kPcF32MaxM) return RMW_OK;
+    const long long tot = S.moff_h[S.nb];
+    if (!S.minv32) {
+        RMW_CUDA(cudaMalloc(&S.minv32, sizeof(float) * (size_t)tot));
+        RMW_CUDA(cudaMalloc(&S.minvK32, sizeof(float) * 18 * (size_t)S.n));
+        RMW_CUDA(cudaMalloc(&S.nmat32, sizeof(float) * 36 * (size_t)S.nb));
+        RMW_CUDA(cudaMalloc(&S.blob32, sizeof(float4) * (size_t)S.n));
+    }
+    to_f32(S.minv, S.minv32, tot, S.st);
+    to_f32(S.minvK, S.minvK32, 18LL * S.n, S.st);
+    to_f32(S.nmat, S.nmat32, 36LL * S.nb, S.st);
+    blob_geometry_f32_kernel<<<(S.n + 255) / 256, 256, 0, S.st>>>(S.r, S.xb, S.blob_body, S.n, S.blob32);
+    RMW_CHECK_LAUNCH("FP32 preconditioner copies");
+    S.pc32_ready = true;
+    return RMW_OK;
+}
+
+int rigid_apply_pc_mixed(RigidSystem &S, const double *x, double *y)
+{
+    if (!S.pc_ready) return fail(RMW_ERR_ARG, "preconditioner not built (call rmw_rigid_build_pc)");
+    if (S.max_m > kPcF32MaxM) return rigid_apply_pc(S, x, y);
+    if (!S.pc32_ready) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        RMW_CUDA(cudaStreamIsCapturing(S.st, &cs));
+        if (cs != cudaStreamCaptureStatusNone) return rigid_apply_pc(S, x, y);
+        if (int rc = rigid_pc_prepare_f32(S)) return rc;
+    }
+    const int nt = kPcF32Threads, nw = nt / 32;
+    void *tok = nullptr;
+    if (int rc = trace_begin(TRACE_PC, S.st, &tok)) return rc;
+    const size_t sm2 = sizeof(float) * (2 * (size_t)S.max_m + nt + 6 * (nw + 1));
+    const float a = (float)S.a;
+    if (!S.nf_on) {
+        pc_apply_f32_kernel<false><<<S.nb, nt, sm2, S.st>>>(x, y, S.blob32, S.boff, S.moff, S.minv32, S.minvK32,
+                                                             S.nmat32, S.n, a, nullptr, nullptr);
+    } else {
+        const bool ln = S.nf_ln_pairs > 0;
+        pc_apply_f32_kernel<true><<<S.nb, nt, sm2, S.st>>>(x, S.nf_z, S.blob32, S.boff, S.moff, S.minv32, S.minvK32,
+                                                            S.nmat32, S.n, a, S.nf_lam32, ln ? S.nf_mom32 : nullptr);
+        const size_t sm3 = sizeof(float) * (2 * (size_t)S.max_m + 3 * (size_t)std::max(nt, S.max_m / 3) +
+                                            6 * (nw + 1));
+        const float nf = (float)(1.0 / (8.0 * kPi * S.eta * S.a));
+        nf_correct_f32_kernel<<<S.nb, nt, sm3, S.st>>>(
+            S.nf_z, y, S.blob32, S.xb, S.boff, S.moff, S.minv32, S.minvK32, S.nmat32, S.n,
+            S.nf_ex_pairs ? S.nf_ex_off : nullptr, S.nf_ex_idx, S.nf_lam32, ln ? S.nf_ln_off : nullptr, S.nf_ln_idx,
+            S.nf_G32, S.nf_mom32, a, nf, images_of(S));
+    }
+    if (int rc = trace_end(tok, S.st)) return rc;
+    RMW_CHECK_LAUNCH("FP32 preconditioner apply");
+    return RMW_OK;
+}
+
 // grow-only per-entry arrays of the two lists: capacities in entries, shared
 // by the index array and the per-entry data (pair velocities, mode couplings)
 static int grow_lists(RigidSystem &S, size_t need_ex, size_t need_ln)
@@ -714,12 +1067,15 @@ static int grow_lists(RigidSystem &S, size_t need_ex, size_t need_ln)
     if (!S.nf_ln_idx || need_ln > S.nf_cap_ln) {
         if (S.nf_ln_idx) RMW_CUDA(cudaFree(S.nf_ln_idx));
         if (S.nf_G) RMW_CUDA(cudaFree(S.nf_G));
+        if (S.nf_G32) RMW_CUDA(cudaFree(S.nf_G32));
+        S.nf_G32 = nullptr;
         S.nf_ln_idx = nullptr;
         S.nf_G = nullptr;
         S.nf_cap_ln = 0;
         const size_t want = std::max<size_t>(need_ln + need_ln / 4, 64);
         RMW_CUDA(cudaMalloc(&S.nf_ln_idx, sizeof(int) * want));
         RMW_CUDA(cudaMalloc(&S.nf_G, sizeof(double) * 121 * want));
+        RMW_CUDA(cudaMalloc(&S.nf_G32, sizeof(float) * 121 * want));
         S.nf_cap_ln = want;
     }
     return RMW_OK;
@@ -752,10 +1108,9 @@ static int build_bands(RigidSystem &S, double cut_ex, double cut_lf, double cut_
     const Images P = images_of(S);
     const float e2 = (float)(cut_ex * cut_ex), f2 = (float)(cut_lf * cut_lf), l2 = (float)(cut_ln * cut_ln),
                 m2 = (float)(cut_mp * cut_mp);
-    const unsigned g = (unsigned)((nb + 63) / 64);
-    const size_t tsm = sizeof(float) * 3 * 64;
-    nbr_bands_kernel<<<g, 64, tsm, st>>>(S.xb, nb, e2, f2, l2, m2, P, range, S.nf_cnt, nullptr, nullptr, nullptr,
-                                          nullptr, nullptr, nullptr);
+    const unsigned g = (unsigned)(((long long)nb * 32 + 255) / 256);  // one warp per body
+    nbr_bands_kernel<<<g, 256, 0, st>>>(S.xb, nb, e2, f2, l2, m2, P, range, S.nf_cnt, nullptr, nullptr, nullptr,
+                                         nullptr, nullptr, nullptr);
     RMW_CHECK_LAUNCH("neighbour count");
     std::vector<int> cnt(3 * (size_t)nb), off(3 * ((size_t)nb + 1), 0);
     RMW_CUDA(cudaMemcpyAsync(cnt.data(), S.nf_cnt, sizeof(int) * 3 * nb, cudaMemcpyDeviceToHost, st));
@@ -778,8 +1133,8 @@ static int build_bands(RigidSystem &S, double cut_ex, double cut_lf, double cut_
         S.nf_cap_mp = want;
     }
     // the count pass wrote the offsets' sources; the fill pass writes the lists
-    nbr_bands_kernel<<<g, 64, tsm, st>>>(S.xb, nb, e2, f2, l2, m2, P, range, nullptr, S.nf_ex_off, S.nf_ex_idx,
-                                          S.nf_ln_off, S.nf_ln_idx, S.nf_mp_off, S.nf_mp_idx);
+    nbr_bands_kernel<<<g, 256, 0, st>>>(S.xb, nb, e2, f2, l2, m2, P, range, nullptr, S.nf_ex_off, S.nf_ex_idx,
+                                         S.nf_ln_off, S.nf_ln_idx, S.nf_mp_off, S.nf_mp_idx);
     RMW_CHECK_LAUNCH("neighbour fill");
     return RMW_OK;
 }
@@ -941,13 +1296,17 @@ int rmw_rigid_set_nearfield_bands(void *sys, void *net, double exact_cutoff, dou
     S.nf_on = false;
     if (int rc = rmw::build_bands(S, lo, lf, hi, mp)) return rc;
     if (!S.nf_mom) RMW_CUDA(cudaMalloc(&S.nf_mom, sizeof(double) * rmw::kModes * S.nb));
+    if (!S.nf_mom32) RMW_CUDA(cudaMalloc(&S.nf_mom32, sizeof(float) * rmw::kModes * S.nb));
+    if (!S.nf_lam32) RMW_CUDA(cudaMalloc(&S.nf_lam32, sizeof(float) * 3 * (size_t)S.n));
     if (!S.nf_v) {
         RMW_CUDA(cudaMalloc(&S.nf_v, sizeof(double) * S.sys_size()));
         RMW_CUDA(cudaMemset(S.nf_v, 0, sizeof(double) * S.sys_size()));  // force rows stay zero
     }
     if (!S.nf_z) RMW_CUDA(cudaMalloc(&S.nf_z, sizeof(double) * S.sys_size()));
-    if (N && S.nf_ln_pairs > 0)
+    if (N && S.nf_ln_pairs > 0) {
         if (int rc = rmw::learned_couplings(S, *N)) return rc;
+        rmw::to_f32(S.nf_G, S.nf_G32, 121LL * S.nf_ln_pairs, st);  // the mixed solves' FP32 apply
+    }
     if (!N) S.nf_ln_pairs = 0;
     RMW_CHECK_LAUNCH("near-field attach");
     RMW_CUDA(cudaStreamSynchronize(st));

@@ -476,6 +476,7 @@ __global__ void count_below_kernel(const double *__restrict__ r, int n, double z
 static int build_pc(RigidSystem &S, bool stochastic, bool fp32 = false)
 {
     cudaStream_t st = S.st;
+    S.pc32_ready = false;  // the FP32 copies follow the arrays rewritten here
     const long long tot = S.moff_h[S.nb];
     // working copy of the dense body mobilities (stream-ordered, freed below)
     void *ws = nullptr;
@@ -527,6 +528,7 @@ static int build_pc(RigidSystem &S, bool stochastic, bool fp32 = false)
     S.pc_ready = true;
     S.stoch_ready = stochastic;
     S.pc_fp32 = fp32;
+    S.pc32_ready = false;
     return RMW_OK;
 }
 
@@ -647,7 +649,8 @@ static void free_system(RigidSystem *S)
     cudaSetDevice(S->device);
     void *ptrs[] = {S->boff, S->blob_body, S->moff, S->r, S->xb, S->minv, S->minvK, S->nmat, S->lfac, S->linv,
                     S->dstatus, S->tmp3n, S->perm, S->nf_off, S->nf_ex_idx, S->nf_ln_idx, S->nf_mp_idx, S->nf_cnt, S->nf_range,
-                    S->nf_G, S->nf_mom, S->nf_v, S->nf_z, S->nf_part};
+                    S->nf_G, S->nf_mom, S->nf_v, S->nf_z, S->nf_part, S->minv32, S->minvK32, S->nmat32,
+                    S->blob32, S->nf_mom32, S->nf_lam32, S->nf_G32};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (S->batch) {
@@ -807,6 +810,16 @@ int rmw_rigid_apply_pc(void *sys, const double *x, double *y)
     if (!sys || !x || !y) return rmw::fail(RMW_ERR_ARG, "null argument");
     if (x == y) return rmw::fail(RMW_ERR_ARG, "rmw_rigid_apply_pc cannot run in place");
     return rmw::rigid_apply_pc(*(RigidSystem *)sys, x, y);
+}
+
+int rmw_rigid_apply_pc_mode(void *sys, const double *x, double *y, int mode)
+{
+    if (!sys || !x || !y) return rmw::fail(RMW_ERR_ARG, "null argument");
+    if (x == y) return rmw::fail(RMW_ERR_ARG, "rmw_rigid_apply_pc_mode cannot run in place");
+    if (mode != RMW_MODE_FP64 && mode != RMW_MODE_MIXED && mode != RMW_MODE_DF64)
+        return rmw::fail(RMW_ERR_ARG, "unknown precision mode");
+    RigidSystem &S = *(RigidSystem *)sys;
+    return mode == RMW_MODE_MIXED ? rmw::rigid_apply_pc_mixed(S, x, y) : rmw::rigid_apply_pc(S, x, y);
 }
 
 int rmw_rigid_mobility_pc(void *sys, const double *w, double *y, int mode)

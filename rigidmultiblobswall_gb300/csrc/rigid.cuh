@@ -35,6 +35,11 @@ struct RigidSystem {
     double *tmp3n = nullptr;       // 3n scratch vector
     bool pc_ready = false, stoch_ready = false;
     bool pc_fp32 = false;  // body blocks factorised in FP32 (preconditioner of the mixed solves)
+    // FP32 copies of minv, minvK, nmat for the mixed solves' FP32 apply
+    // (rigid_apply_pc_mixed); filled from the FP64 arrays after each build
+    float *minv32 = nullptr, *minvK32 = nullptr, *nmat32 = nullptr;
+    float4 *blob32 = nullptr;  // n: blob offset from its body's centre and height, FP32
+    bool pc32_ready = false;
     bool wall = true;  // false: free-space (no-wall) mobility (rmw_rigid_set_wall)
     // independent suspensions inside the handle (rmw_rigid_set_suspensions):
     // segmented pair products and the instance-major permutation
@@ -59,6 +64,9 @@ struct RigidSystem {
     size_t nf_cap_ex = 0, nf_cap_ln = 0;            // capacities (entries) of the per-entry arrays
     double *nf_G = nullptr;    // 121 per learned entry (lab frame)
     double *nf_mom = nullptr;  // 11 mode moments per body
+    float *nf_mom32 = nullptr;  // the same moments of the FP32 apply
+    float *nf_lam32 = nullptr;  // 3n: damped blob forces b lambda of the FP32 apply
+    float *nf_G32 = nullptr;    // FP32 copy of nf_G
     double *nf_v = nullptr;    // sys_size: near-field blob velocities, force rows zero
     double *nf_z = nullptr;    // sys_size: second block-diagonal solve
     double *nf_part = nullptr;  // max_m per exact entry: unscaled pair velocities
@@ -73,6 +81,15 @@ int rigid_apply(RigidSystem &S, const double *x, double *y, int mode);
 int rigid_apply_pc(RigidSystem &S, const double *x, double *y);
 // the block-diagonal form alone
 int rigid_apply_pc_plain(RigidSystem &S, const double *x, double *y);
+// The same operator (plain or near-field augmented) in FP32 arithmetic, for
+// the mixed-precision solves, whose inner GMRES runs on FP32 pair products and
+// whose refinement residual is FP64-accurate; the FP64 form for bodies too
+// large for its shared-memory layout, and inside a stream capture before
+// rigid_pc_prepare_f32 has run.
+int rigid_apply_pc_mixed(RigidSystem &S, const double *x, double *y);
+// FP32 copies of the built preconditioner (no-op when current); call before
+// capturing rigid_apply_pc_mixed into a CUDA graph.
+int rigid_pc_prepare_f32(RigidSystem &S);
 // y = L^-1 M L^-T w on the blob space (det_stoch mobility_pc, multi_bodies.py:591-606).
 int rigid_mobility_pc(RigidSystem &S, const double *w, double *y, int mode);
 // y = L w (det_stoch P_inv_mult, multi_bodies.py:609-615).

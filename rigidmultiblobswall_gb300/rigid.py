@@ -107,11 +107,16 @@ class RigidSystem:
         _native.call("rmw_rigid_apply", self._h, x.data_ptr(), y.data_ptr(), _mode(mode))
         return y
 
-    def apply_pc(self, x):
-        """Block-diagonal preconditioner apply."""
+    def apply_pc(self, x, mode=None):
+        """Block-diagonal preconditioner apply (with the attached near-field
+        augmentation).  mode=None or "fp64": FP64; mode="mixed": the FP32 apply
+        of the mixed-precision solves."""
         x = _dev(x, self.device).reshape(-1)
         y = self._out(self.size)
-        _native.call("rmw_rigid_apply_pc", self._h, x.data_ptr(), y.data_ptr())
+        if mode is None:
+            _native.call("rmw_rigid_apply_pc", self._h, x.data_ptr(), y.data_ptr())
+        else:
+            _native.call("rmw_rigid_apply_pc_mode", self._h, x.data_ptr(), y.data_ptr(), _mode(mode))
         return y
 
     def mobility_pc(self, w, mode="fp64"):

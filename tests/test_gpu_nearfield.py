@@ -73,6 +73,33 @@ def test_exact_nearfield_apply_matches_oracle(cuda_device):
     sys_.close()
 
 
+def test_fp32_apply_of_mixed_solves_matches_oracle(cuda_device):
+    """The mixed solves' FP32 preconditioner apply (one kernel plain, two fused kernels augmented) against
+    the oracle's FP64 apply: plain, with exact near pairs, and with the periodic images of a periodic box."""
+    susp, sys_, R = _dense_suspension(12, 31)
+    rig = orig.Rigid(susp.r_vectors(), susp.locations, np.arange(13) * 42, susp.eta, susp.a)
+    rng = np.random.default_rng(7)
+    for _ in range(2):  # the second call reuses the FP32 copies
+        x = rng.standard_normal(sys_.size)
+        assert rel_err(sys_.apply_pc(x, mode="mixed").cpu().numpy(), rig.apply_pc(x)) <= 2e-6
+    nf.attach_exact(sys_, 3 * R)
+    pairs = _pairs_within(susp.locations, 0.0, 3 * R)
+    for _ in range(2):
+        x = rng.standard_normal(sys_.size)
+        ref = onf.augmented_pc(rig, x, pairs, {})
+        assert rel_err(sys_.apply_pc(x, mode="mixed").cpu().numpy(), ref) <= 2e-6
+        assert rel_err(sys_.apply_pc(x, mode="fp64").cpu().numpy(), ref) <= 1e-10
+    # a rebuilt preconditioner refreshes the FP32 copies
+    nf.detach(sys_)
+    r2 = susp.r_vectors() + 0.05 * rng.standard_normal(susp.r_vectors().shape) * np.array([1.0, 1.0, 0.0])
+    sys_.set_configuration(r2, susp.locations)
+    sys_.build_pc()
+    rig2 = orig.Rigid(r2, susp.locations, np.arange(13) * 42, susp.eta, susp.a)
+    x = rng.standard_normal(sys_.size)
+    assert rel_err(sys_.apply_pc(x, mode="mixed").cpu().numpy(), rig2.apply_pc(x)) <= 2e-6
+    sys_.close()
+
+
 def _random_graph(rng, R=1.0):
     """Three clusters of 3..6 bodies: message edges < 3R, band edges in [2.2R, 6R)."""
     from oracle import mpnn
@@ -171,6 +198,11 @@ def test_learned_apply_matches_oracle(trained):
     rig = orig.Rigid(susp.r_vectors(), locs, np.arange(13) * 42, susp.eta, susp.a)
     ref = onf.augmented_pc(rig, x, ex, learned)
     assert rel_err(got, ref) <= 1e-4  # a feature may round to a neighbouring BF16 value
+    # the mixed solves' FP32 apply of the same couplings: FP32 rounding on top of the FP64 apply
+    assert rel_err(sys_.apply_pc(x, mode="mixed").cpu().numpy(), got) <= 2e-6
+    only = m.attach(sys_, exact_cutoff=0.0)
+    assert only[0] == 0 and only[1] > n_ln
+    assert rel_err(sys_.apply_pc(x, mode="mixed").cpu().numpy(), sys_.apply_pc(x).cpu().numpy()) <= 2e-6
     sys_.close()
 
 

@@ -135,28 +135,30 @@ template <> __device__ __forceinline__ float fsqrt<float>(float x) { return sqrt
 template <typename T>
 __device__ void factor_and_invert(T *A, int m, T *tmp, double *minv, double *lfac, double *linv, int *status)
 {
-    const int tid = threadIdx.x, nt = blockDim.x;
-    // right-looking Cholesky, lower triangle
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+    // right-looking Cholesky, lower triangle: per column k the scale by the
+    // pivot's square root (kept in tmp until the end, so that A[k][k] stays
+    // readable for the whole step), then the trailing update with warps over
+    // rows and lanes over columns
     for (int k = 0; k < m; ++k) {
+        const T d = A[k * m + k];
         if (tid == 0) {
-            const T d = A[k * m + k];
             if (!(d > T(0))) atomicExch(status, 1);  // not positive definite
-            A[k * m + k] = fsqrt<T>(d);
+            tmp[k] = fsqrt<T>(d);
         }
-        __syncthreads();
-        const T dk = A[k * m + k];
+        const T dk = fsqrt<T>(d);
         for (int i = k + 1 + tid; i < m; i += nt) A[i * m + k] /= dk;
         __syncthreads();
-        const int t = m - k - 1;
-        for (int idx = tid; idx < t * t; idx += nt) {
-            const int i = k + 1 + idx / t, j = k + 1 + idx % t;
-            if (j <= i) A[i * m + j] -= A[i * m + k] * A[j * m + k];
+        for (int i = k + 1 + wid; i < m; i += nw) {
+            const T lik = A[i * m + k];
+            for (int j = k + 1 + lane; j <= i; j += 32) A[i * m + j] -= lik * A[j * m + k];
         }
         __syncthreads();
     }
     for (int idx = tid; idx < m * m; idx += nt) {
-        const int i = idx / m, j = idx % m;
+        const int i = idx / m, j = idx - i * m;
         if (j > i) A[idx] = T(0);
+        if (j == i) A[idx] = tmp[i];
         if (lfac) lfac[idx] = (j > i) ? 0.0 : (double)A[idx];
     }
     __syncthreads();
@@ -166,24 +168,24 @@ __device__ void factor_and_invert(T *A, int m, T *tmp, double *minv, double *lfa
         for (int k = j + 1 + tid; k < m; k += nt) tmp[k] = A[k * m + j];
         __syncthreads();
         for (int i = j + 1 + tid; i < m; i += nt) {
-            T s = T(0);
-            for (int k = j + 1; k <= i; ++k) s += A[i * m + k] * tmp[k];
-            A[i * m + j] = -ajj * s;
+            T sum = T(0);
+            for (int k = j + 1; k <= i; ++k) sum += A[i * m + k] * tmp[k];
+            A[i * m + j] = -ajj * sum;
         }
         if (tid == 0) A[j * m + j] = ajj;
         __syncthreads();
     }
     if (linv)
         for (int idx = tid; idx < m * m; idx += nt) linv[idx] = (double)A[idx];
-    // M^-1 = L^-T L^-1 : minv[i][j] = sum_{k >= max(i,j)} X[k][i] X[k][j]
-    for (int idx = tid; idx < m * m; idx += nt) {
-        const int i = idx / m, j = idx % m;
-        if (j < i) continue;
-        T s = T(0);
-        for (int k = j; k < m; ++k) s += A[k * m + i] * A[k * m + j];
-        minv[(long long)i * m + j] = (double)s;
-        minv[(long long)j * m + i] = (double)s;
-    }
+    // M^-1 = L^-T L^-1 : minv[i][j] = sum_{k >= max(i,j)} X[k][i] X[k][j], warps
+    // over the rows i, lanes over the columns j >= i
+    for (int i = wid; i < m; i += nw)
+        for (int j = i + lane; j < m; j += 32) {
+            T sum = T(0);
+            for (int k = j; k < m; ++k) sum += A[k * m + i] * A[k * m + j];
+            minv[(long long)i * m + j] = (double)sum;
+            minv[(long long)j * m + i] = (double)sum;
+        }
 }
 
 template <typename T>
@@ -203,6 +205,114 @@ __global__ void pc_factor_smem_kernel(const double *__restrict__ M, const long l
                          status);
 }
 
+// M_b^-1 of the mixed solves' FP32 preconditioner (deterministic builds, m <=
+// 16 R): in-place Gauss-Jordan sweeps with the matrix held in registers, one
+// CTA of 16 x 16 threads per body, thread (ty, tx) owning rows ty + 16u and
+// columns tx + 16w.  Step k publishes row k and column k through shared memory
+// (double-buffered: one barrier per step) and updates every element:
+//   A[k][k] <- 1/p,  A[k][j] <- A[k][j]/p,  A[i][k] <- -A[i][k]/p,
+//   A[i][j] <- A[i][j] - A[i][k] A[k][j] / p,        p = A[k][k],
+// which leaves A^-1 after m steps.  An SPD matrix needs no pivoting (every
+// pivot is a positive Schur-complement diagonal); a non-positive pivot flags
+// the body like the Cholesky does.  M^-1 is written symmetrised (the upper
+// triangle both ways), as the apply kernels read it by columns.  m^3 fused
+// multiply-adds on the FP32 pipe with no reduction and no dependent chain,
+// against the Cholesky route's column loops.
+template <int R>
+__global__ void __launch_bounds__(256) pc_sweep_f32_kernel(const double *__restrict__ M,
+                                                           const long long *__restrict__ moff,
+                                                           const int *__restrict__ boff, double *__restrict__ minv,
+                                                           int *status)
+{
+    __shared__ float colb[2][16 * R], rowb[2][16 * R];
+    const int b = blockIdx.x;
+    const int m = 3 * (boff[b + 1] - boff[b]);
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const double *Mb = M + moff[b];
+    float A[R][R];
+#pragma unroll
+    for (int u = 0; u < R; ++u)
+#pragma unroll
+        for (int w = 0; w < R; ++w) {
+            const int i = ty + 16 * u, j = tx + 16 * w;
+            A[u][w] = (i < m && j < m) ? (float)Mb[(long long)i * m + j] : 0.f;
+        }
+    bool bad = false;
+    for (int k = 0; k < m; ++k) {
+        const int kb = k & 1, kr = k & 15, kq = k >> 4;
+        if (tx == kr) {  // column k
+#pragma unroll
+            for (int w = 0; w < R; ++w)
+                if (w == kq)
+#pragma unroll
+                    for (int u = 0; u < R; ++u) colb[kb][ty + 16 * u] = A[u][w];
+        }
+        if (ty == kr) {  // row k
+#pragma unroll
+            for (int u = 0; u < R; ++u)
+                if (u == kq)
+#pragma unroll
+                    for (int w = 0; w < R; ++w) rowb[kb][tx + 16 * w] = A[u][w];
+        }
+        __syncthreads();
+        const float p = rowb[kb][k];
+        bad = bad || !(p > 0.f);
+        const float ip = 1.f / p;
+        float c[R], rr[R];
+#pragma unroll
+        for (int u = 0; u < R; ++u) c[u] = colb[kb][ty + 16 * u] * ip;
+#pragma unroll
+        for (int w = 0; w < R; ++w) rr[w] = rowb[kb][tx + 16 * w];
+#pragma unroll
+        for (int u = 0; u < R; ++u)
+#pragma unroll
+            for (int w = 0; w < R; ++w) A[u][w] = fmaf(-c[u], rr[w], A[u][w]);
+        // row k, column k and the pivot replace the general update
+        if (ty == kr) {
+#pragma unroll
+            for (int u = 0; u < R; ++u)
+                if (u == kq)
+#pragma unroll
+                    for (int w = 0; w < R; ++w) A[u][w] = rr[w] * ip;
+        }
+        if (tx == kr) {
+#pragma unroll
+            for (int w = 0; w < R; ++w)
+                if (w == kq)
+#pragma unroll
+                    for (int u = 0; u < R; ++u) A[u][w] = (ty == kr && u == kq) ? ip : -c[u];
+        }
+    }
+    if (bad && threadIdx.x == 0) atomicExch(status, 1);  // not positive definite
+    double *Mi = minv + moff[b];
+#pragma unroll
+    for (int u = 0; u < R; ++u)
+#pragma unroll
+        for (int w = 0; w < R; ++w) {
+            const int i = ty + 16 * u, j = tx + 16 * w;
+            if (i < m && j < m && i <= j) {
+                Mi[(long long)i * m + j] = (double)A[u][w];
+                Mi[(long long)j * m + i] = (double)A[u][w];
+            }
+        }
+}
+
+static void launch_pc_sweep_f32(int R, int nb, const double *M, const long long *moff, const int *boff,
+                                double *minv, int *status, cudaStream_t st)
+{
+    switch (R) {
+    case 1: pc_sweep_f32_kernel<1><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
+    case 2: pc_sweep_f32_kernel<2><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
+    case 3: pc_sweep_f32_kernel<3><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
+    case 4: pc_sweep_f32_kernel<4><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
+    case 5: pc_sweep_f32_kernel<5><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
+    case 6: pc_sweep_f32_kernel<6><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
+    case 7: pc_sweep_f32_kernel<7><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
+    default: pc_sweep_f32_kernel<8><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
+    }
+}
+constexpr int kSweepMaxM = 128;
+
 // global-memory variant: M is overwritten (it is the working copy), tmp is m doubles per body
 __global__ void pc_factor_global_kernel(double *__restrict__ M, const long long *__restrict__ moff,
                                         const int *__restrict__ boff, double *__restrict__ minv, double *lfac,
@@ -214,12 +324,14 @@ __global__ void pc_factor_global_kernel(double *__restrict__ M, const long long 
                               linv ? linv + moff[b] : nullptr, status);
 }
 
-// M^-1 K (m x 6) and N = (K^T M^-1 K)^-1 (6 x 6) per body
+// M^-1 K (m x 6) and N = (K^T M^-1 K)^-1 (6 x 6) per body; the blob offsets
+// from the centre staged in shared memory (3 doubles per blob)
 __global__ void pc_body_kernel(const double *__restrict__ r, const double *__restrict__ xb,
                                const int *__restrict__ boff, const long long *__restrict__ moff,
                                const double *__restrict__ minv, double *__restrict__ minvK,
                                double *__restrict__ nmat, int *status)
 {
+    extern __shared__ double doff[];
     __shared__ double G[36];
     __shared__ double aug[6][12];
     const int b = blockIdx.x;
@@ -228,15 +340,20 @@ __global__ void pc_body_kernel(const double *__restrict__ r, const double *__res
     double *MK = minvK + 6LL * 3 * o;
     const double cx = xb[3 * b], cy = xb[3 * b + 1], cz = xb[3 * b + 2];
     if (threadIdx.x < 36) G[threadIdx.x] = 0.0;
+    for (int p = threadIdx.x; p < m / 3; p += blockDim.x) {
+        doff[3 * p] = r[3 * (o + p)] - cx;
+        doff[3 * p + 1] = r[3 * (o + p) + 1] - cy;
+        doff[3 * p + 2] = r[3 * (o + p) + 2] - cz;
+    }
     __syncthreads();
-    // MK[t][c] = sum_k Minv[t][k] K[k][c]; K row k = 3p+u: J part e_u, rot part R_p row u
+    // MK[t][c] = sum_k Minv[t][k] K[k][c]; K row k = 3p+u: J part e_u, rot part
+    // R_p row u.  M^-1 is symmetric: Minv[k][t] is read, coalesced over t.
     for (int t = threadIdx.x; t < m; t += blockDim.x) {
         double acc[6] = {0, 0, 0, 0, 0, 0};
         for (int p = 0; p < m / 3; ++p) {
-            const int i = o + p;
-            const double dx = r[3 * i] - cx, dy = r[3 * i + 1] - cy, dz = r[3 * i + 2] - cz;
-            const double m0 = Mi[(long long)t * m + 3 * p], m1 = Mi[(long long)t * m + 3 * p + 1],
-                         m2 = Mi[(long long)t * m + 3 * p + 2];
+            const double dx = doff[3 * p], dy = doff[3 * p + 1], dz = doff[3 * p + 2];
+            const double m0 = Mi[(long long)(3 * p) * m + t], m1 = Mi[(long long)(3 * p + 1) * m + t],
+                         m2 = Mi[(long long)(3 * p + 2) * m + t];
             acc[0] += m0; acc[1] += m1; acc[2] += m2;
             // R_p = [[0, dz, -dy], [-dz, 0, dx], [dy, -dx, 0]] (R w = w x d)
             acc[3] += -dz * m1 + dy * m2;
@@ -251,8 +368,7 @@ __global__ void pc_body_kernel(const double *__restrict__ r, const double *__res
         const int rr = threadIdx.x / 6, c = threadIdx.x % 6;
         double s = 0.0;
         for (int p = 0; p < m / 3; ++p) {
-            const int i = o + p;
-            const double dx = r[3 * i] - cx, dy = r[3 * i + 1] - cy, dz = r[3 * i + 2] - cz;
+            const double dx = doff[3 * p], dy = doff[3 * p + 1], dz = doff[3 * p + 2];
             const double k0 = MK[6LL * (3 * p) + c], k1 = MK[6LL * (3 * p + 1) + c], k2 = MK[6LL * (3 * p + 2) + c];
             double kr;
             if (rr < 3) kr = (rr == 0) ? k0 : (rr == 1 ? k1 : k2);
@@ -503,7 +619,9 @@ static int build_pc(RigidSystem &S, bool stochastic, bool fp32 = false)
         else body_mobility_free_kernel<double><<<S.nb, kRigidThreads, 0, st>>>(S.r, S.boff, S.moff, M, S.eta, S.a);
     }
     double *lf = stochastic ? S.lfac : nullptr, *li = stochastic ? S.linv : nullptr;
-    if (fp32) {
+    if (fp32 && !stochastic && S.max_m <= kSweepMaxM) {
+        launch_pc_sweep_f32((S.max_m + 15) / 16, S.nb, M, S.moff, S.boff, S.minv, S.dstatus, st);
+    } else if (fp32) {
         const size_t sm = sizeof(float) * ((size_t)S.max_m * S.max_m + S.max_m);
         RMW_CUDA(cudaFuncSetAttribute(pc_factor_smem_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)sm));
@@ -516,7 +634,12 @@ static int build_pc(RigidSystem &S, bool stochastic, bool fp32 = false)
     } else {
         pc_factor_global_kernel<<<S.nb, kRigidThreads, 0, st>>>(M, S.moff, S.boff, S.minv, lf, li, tmpg, S.dstatus);
     }
-    pc_body_kernel<<<S.nb, 128, 0, st>>>(S.r, S.xb, S.boff, S.moff, S.minv, S.minvK, S.nmat, S.dstatus);
+    {
+        const size_t sm = sizeof(double) * (size_t)S.max_m;
+        if (sm > 48 * 1024)
+            RMW_CUDA(cudaFuncSetAttribute(pc_body_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        pc_body_kernel<<<S.nb, 128, sm, st>>>(S.r, S.xb, S.boff, S.moff, S.minv, S.minvK, S.nmat, S.dstatus);
+    }
     RMW_CHECK_LAUNCH("preconditioner build");
     int hstat = 0;
     RMW_CUDA(cudaMemcpyAsync(&hstat, S.dstatus, sizeof(int), cudaMemcpyDeviceToHost, st));

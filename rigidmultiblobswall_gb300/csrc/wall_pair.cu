@@ -1094,7 +1094,8 @@ __global__ void wall_finalize_kernel(const double *__restrict__ r, const double 
         const int nc = blob_nchunks ? blob_nchunks[i] : nchunks;
         const double *p0 = pbase ? partial + pbase[i] : partial + 3 * (size_t)i;
         const size_t ps = pstride ? (size_t)pstride[i] : 3 * (size_t)n;
-        for (int s = g; s < nc; s += kFinGroup) {
+#pragma unroll 4
+        for (int s = g; s < nc; s += kFinGroup) {  // unrolled: loads of several slots in flight
             const double *p = p0 + (size_t)s * ps;
             ux += p[0]; uy += p[1]; uz += p[2];
         }

@@ -240,14 +240,27 @@ __global__ void __launch_bounds__(kNwThreads) nw_pair_df_kernel(const NwSrcDF *_
     }
 }
 
+// DF2: double-float slots of the mixed symmetric kernels, added on the FP32 pipe
+template <bool DF2 = false>
 __global__ void nw_finalize_kernel(const double *__restrict__ v, const double *__restrict__ partial, int nchunks,
                                    double *__restrict__ out, int n, double self_coef, double nf)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double u[3] = {0.0, 0.0, 0.0};
-    for (int s = 0; s < nchunks; ++s)
-        for (int c = 0; c < 3; ++c) u[c] += partial[(size_t)s * 3 * n + 3 * (size_t)i + c];
+    if constexpr (DF2) {
+        const float2 *p2 = reinterpret_cast<const float2 *>(partial);
+        df s3[3] = {df_from(0.f), df_from(0.f), df_from(0.f)};
+        for (int s = 0; s < nchunks; ++s)
+            for (int c = 0; c < 3; ++c) {
+                const float2 p = p2[(size_t)s * 3 * n + 3 * (size_t)i + c];
+                s3[c] = s3[c] + df{p.x, p.y};
+            }
+        for (int c = 0; c < 3; ++c) u[c] = (double)s3[c].hi + (double)s3[c].lo;
+    } else {
+        for (int s = 0; s < nchunks; ++s)
+            for (int c = 0; c < 3; ++c) u[c] += partial[(size_t)s * 3 * n + 3 * (size_t)i + c];
+    }
     for (int c = 0; c < 3; ++c) out[3 * i + c] = nf * (u[c] + self_coef * v[3 * i + c]);
 }
 
@@ -324,7 +337,11 @@ int nowall_product(int kind, const double *r, const double *v, double *out, int6
     if (int rc = trace_end(tok, st)) return rc;
     const double p = (kind == RMW_UF) ? a : (kind == RMW_WT ? a * a * a : a * a);
     const double self_coef = (kind == RMW_UF) ? 4.0 / 3.0 : (kind == RMW_WT ? 1.0 : 0.0);
-    nw_finalize_kernel<<<pg, pb, 0, st>>>(v, partial, nchunks, out, N, self_coef, 1.0 / (8.0 * kPi * eta * p));
+    if (sym && mode == RMW_MODE_MIXED)
+        nw_finalize_kernel<true><<<pg, pb, 0, st>>>(v, partial, nchunks, out, N, self_coef, 1.0 / (8.0 * kPi * eta * p));
+    else
+        nw_finalize_kernel<false><<<pg, pb, 0, st>>>(v, partial, nchunks, out, N, self_coef,
+                                                     1.0 / (8.0 * kPi * eta * p));
     RMW_CHECK_LAUNCH("free-space product kernels");
     return RMW_OK;
 }

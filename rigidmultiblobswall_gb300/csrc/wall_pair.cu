@@ -469,7 +469,10 @@ __global__ void sym_band_accum_kernel(const SymBand bd, int n, int nt, double *_
 // differences (as wall_pair_mixed_kernel).  The target-side FP32 sum over the
 // tile is folded into a TwoSum-compensated accumulator; the source side sums
 // its 32 contributions per warp in FP32 shared memory and the four warp
-// copies in FP64.
+// copies in double-float.  The slots hold double-float values (float2 hi, lo
+// in the 8 bytes of a double slot), which the finalize adds on the FP32 pipe:
+// summed in FP64, the ceil(n/128) slots of every blob made the finalize
+// FP64-bound on GB300.
 template <bool SEG, int KIND, bool NOWALL = false>
 __device__ __forceinline__ void mixed_sym_body(const SrcF *__restrict__ src, int n, int nt,
                                                double *__restrict__ partial, const SymJob *__restrict__ jobs)
@@ -540,30 +543,27 @@ __device__ __forceinline__ void mixed_sym_body(const SrcF *__restrict__ src, int
     comp_add(sx, ex_, ux);
     comp_add(sy, ey_, uy);
     comp_add(sz, ez_, uz);
-    const double ax = (double)sx + (double)ex_, ay = (double)sy + (double)ey_, az = (double)sz + (double)ez_;
+    const df ax = two_sum_df(sx, ex_), ay = two_sum_df(sy, ey_), az = two_sum_df(sz, ez_);
     __syncthreads();
-    double qx = 0.0, qy = 0.0, qz = 0.0;
-    for (int w = 0; w < kSymWarps; ++w) {
-        qx += (double)sacc[w][0][tid];
-        qy += (double)sacc[w][1][tid];
-        qz += (double)sacc[w][2][tid];
+    df qx = df_from(sacc[0][0][tid]), qy = df_from(sacc[0][1][tid]), qz = df_from(sacc[0][2][tid]);
+    for (int w = 1; w < kSymWarps; ++w) {
+        qx = qx + sacc[w][0][tid];
+        qy = qy + sacc[w][1][tid];
+        qz = qz + sacc[w][2][tid];
     }
+    float2 *part2 = reinterpret_cast<float2 *>(partial);
     const size_t stride = 3 * (size_t)n;
+    auto put = [](float2 *o, df x, df y, df z) {
+        o[0] = make_float2(x.hi, x.lo);
+        o[1] = make_float2(y.hi, y.lo);
+        o[2] = make_float2(z.hi, z.lo);
+    };
     if (diag) {
-        if (valid_i) {
-            double *o = partial + (size_t)T * stride + 3 * (size_t)i;
-            o[0] = ax + qx; o[1] = ay + qy; o[2] = az + qz;
-        }
+        if (valid_i) put(part2 + (size_t)T * stride + 3 * (size_t)i, ax + qx, ay + qy, az + qz);
     } else {
-        if (valid_i) {
-            double *o = partial + (size_t)S * stride + 3 * (size_t)i;
-            o[0] = ax; o[1] = ay; o[2] = az;
-        }
+        if (valid_i) put(part2 + (size_t)S * stride + 3 * (size_t)i, ax, ay, az);
         const int j = S * kTile + tid;
-        if (j < n) {
-            double *o = partial + (size_t)T * stride + 3 * (size_t)j;
-            o[0] = qx; o[1] = qy; o[2] = qz;
-        }
+        if (j < n) put(part2 + (size_t)T * stride + 3 * (size_t)j, qx, qy, qz);
     }
 }
 
@@ -1080,7 +1080,9 @@ __global__ void wall_finalize_multi_kernel(const double *__restrict__ r, const d
 constexpr int kFinGroup = 4;
 inline unsigned finalize_blocks(int n, int pb) { return (unsigned)(((long long)kFinGroup * n + pb - 1) / pb); }
 
-template <int KIND>
+// DF2: the slots hold double-float values (the mixed symmetric kernels), added
+// in double-float on the FP32 pipe
+template <int KIND, bool DF2 = false>
 __global__ void wall_finalize_kernel(const double *__restrict__ r, const double *__restrict__ v,
                                      const double *__restrict__ partial, int nchunks, double *__restrict__ out,
                                      int n, double a, double nf, const int *__restrict__ blob_nchunks,
@@ -1090,21 +1092,50 @@ __global__ void wall_finalize_kernel(const double *__restrict__ r, const double 
     const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int i = (int)(gt / kFinGroup), g = (int)(gt % kFinGroup);
     double ux = 0.0, uy = 0.0, uz = 0.0;
-    if (i < n) {
-        const int nc = blob_nchunks ? blob_nchunks[i] : nchunks;
-        const double *p0 = pbase ? partial + pbase[i] : partial + 3 * (size_t)i;
-        const size_t ps = pstride ? (size_t)pstride[i] : 3 * (size_t)n;
+    if constexpr (DF2) {
+        df sx = df_from(0.f), sy = df_from(0.f), sz = df_from(0.f);
+        if (i < n) {
+            const int nc = blob_nchunks ? blob_nchunks[i] : nchunks;
+            const float2 *p0 = reinterpret_cast<const float2 *>(partial) + (pbase ? pbase[i] : 3 * (long long)i);
+            const size_t ps = pstride ? (size_t)pstride[i] : 3 * (size_t)n;
 #pragma unroll 4
-        for (int s = g; s < nc; s += kFinGroup) {  // unrolled: loads of several slots in flight
-            const double *p = p0 + (size_t)s * ps;
-            ux += p[0]; uy += p[1]; uz += p[2];
+            for (int s = g; s < nc; s += kFinGroup) {
+                const float2 *p = p0 + (size_t)s * ps;
+                const float2 px = p[0], py = p[1], pz = p[2];
+                sx = sx + df{px.x, px.y};
+                sy = sy + df{py.x, py.y};
+                sz = sz + df{pz.x, pz.y};
+            }
         }
-    }
 #pragma unroll
-    for (int o = kFinGroup / 2; o > 0; o >>= 1) {  // every lane of the warp takes part
-        ux += __shfl_down_sync(0xffffffffu, ux, o, kFinGroup);
-        uy += __shfl_down_sync(0xffffffffu, uy, o, kFinGroup);
-        uz += __shfl_down_sync(0xffffffffu, uz, o, kFinGroup);
+        for (int o = kFinGroup / 2; o > 0; o >>= 1) {  // every lane of the warp takes part
+            sx = sx + df{__shfl_down_sync(0xffffffffu, sx.hi, o, kFinGroup),
+                         __shfl_down_sync(0xffffffffu, sx.lo, o, kFinGroup)};
+            sy = sy + df{__shfl_down_sync(0xffffffffu, sy.hi, o, kFinGroup),
+                         __shfl_down_sync(0xffffffffu, sy.lo, o, kFinGroup)};
+            sz = sz + df{__shfl_down_sync(0xffffffffu, sz.hi, o, kFinGroup),
+                         __shfl_down_sync(0xffffffffu, sz.lo, o, kFinGroup)};
+        }
+        ux = (double)sx.hi + (double)sx.lo;
+        uy = (double)sy.hi + (double)sy.lo;
+        uz = (double)sz.hi + (double)sz.lo;
+    } else {
+        if (i < n) {
+            const int nc = blob_nchunks ? blob_nchunks[i] : nchunks;
+            const double *p0 = pbase ? partial + pbase[i] : partial + 3 * (size_t)i;
+            const size_t ps = pstride ? (size_t)pstride[i] : 3 * (size_t)n;
+#pragma unroll 4
+            for (int s = g; s < nc; s += kFinGroup) {  // unrolled: loads of several slots in flight
+                const double *p = p0 + (size_t)s * ps;
+                ux += p[0]; uy += p[1]; uz += p[2];
+            }
+        }
+#pragma unroll
+        for (int o = kFinGroup / 2; o > 0; o >>= 1) {  // every lane of the warp takes part
+            ux += __shfl_down_sync(0xffffffffu, ux, o, kFinGroup);
+            uy += __shfl_down_sync(0xffffffffu, uy, o, kFinGroup);
+            uz += __shfl_down_sync(0xffffffffu, uz, o, kFinGroup);
+        }
     }
     if (i >= n || g != 0) return;
     ux *= pair_scale; uy *= pair_scale; uz *= pair_scale;
@@ -1306,19 +1337,28 @@ static double kind_norm(int kind, double eta, double a)
                               : 1.0 / (8.0 * kPi * eta * a * a);
 }
 
-template <int KIND>
-static void launch_sym_finalize(const double *r, const double *v, const double *partial, int nt, double *out, int n,
-                                double a, double nf, const WallBatch *B, cudaStream_t st)
+template <int KIND, bool DF2>
+static void launch_sym_finalize_t(const double *r, const double *v, const double *partial, int nt, double *out,
+                                  int n, double a, double nf, const WallBatch *B, cudaStream_t st)
 {
     const int pb = 256;
     const double scale = (KIND == RMW_UF) ? kUFCoeffScale : 1.0;
     if (B)
-        wall_finalize_kernel<KIND><<<finalize_blocks(n, pb), pb, 0, st>>>(r, v, partial, 0, out, n, a, nf,
-                                                                          B->blob_nslots, B->blob_pbase,
-                                                                          B->blob_pstride, scale);
+        wall_finalize_kernel<KIND, DF2><<<finalize_blocks(n, pb), pb, 0, st>>>(r, v, partial, 0, out, n, a, nf,
+                                                                               B->blob_nslots, B->blob_pbase,
+                                                                               B->blob_pstride, scale);
     else
-        wall_finalize_kernel<KIND><<<finalize_blocks(n, pb), pb, 0, st>>>(r, v, partial, nt, out, n, a, nf, nullptr,
-                                                                          nullptr, nullptr, scale);
+        wall_finalize_kernel<KIND, DF2><<<finalize_blocks(n, pb), pb, 0, st>>>(r, v, partial, nt, out, n, a, nf,
+                                                                               nullptr, nullptr, nullptr, scale);
+}
+
+// mixed: the symmetric kernels' slots hold double-float values
+template <int KIND>
+static void launch_sym_finalize(const double *r, const double *v, const double *partial, int nt, double *out, int n,
+                                double a, double nf, const WallBatch *B, cudaStream_t st, bool mixed = false)
+{
+    if (mixed) launch_sym_finalize_t<KIND, true>(r, v, partial, nt, out, n, a, nf, B, st);
+    else launch_sym_finalize_t<KIND, false>(r, v, partial, nt, out, n, a, nf, B, st);
 }
 
 // pack, symmetric pair kernel and finalize of any kind (B: segmented over its suspensions)
@@ -1348,10 +1388,10 @@ static int sym_product(int kind, const double *r, const double *v, double *out, 
     if (int rc = trace_end(tok, st)) return rc;
     const double nf = kind_norm(kind, eta, a);
     switch (kind) {
-    case RMW_UF: launch_sym_finalize<RMW_UF>(r, v, partial, nt, out, n, a, nf, B, st); break;
-    case RMW_UT: launch_sym_finalize<RMW_UT>(r, v, partial, nt, out, n, a, nf, B, st); break;
-    case RMW_WF: launch_sym_finalize<RMW_WF>(r, v, partial, nt, out, n, a, nf, B, st); break;
-    default: launch_sym_finalize<RMW_WT>(r, v, partial, nt, out, n, a, nf, B, st); break;
+    case RMW_UF: launch_sym_finalize<RMW_UF>(r, v, partial, nt, out, n, a, nf, B, st, mode == RMW_MODE_MIXED); break;
+    case RMW_UT: launch_sym_finalize<RMW_UT>(r, v, partial, nt, out, n, a, nf, B, st, mode == RMW_MODE_MIXED); break;
+    case RMW_WF: launch_sym_finalize<RMW_WF>(r, v, partial, nt, out, n, a, nf, B, st, mode == RMW_MODE_MIXED); break;
+    default: launch_sym_finalize<RMW_WT>(r, v, partial, nt, out, n, a, nf, B, st, mode == RMW_MODE_MIXED); break;
     }
     RMW_CHECK_LAUNCH("symmetric wall product kernels");
     return RMW_OK;

@@ -80,6 +80,46 @@ __global__ void kt_times_lambda_kernel(const double *__restrict__ r, const doubl
     if (lane < 6) out[6 * b + lane] = alpha * s[lane];
 }
 
+// The K parts of the mixed-precision operator in one pass, one warp per body:
+// y_blob -= K U and y_body = -K^T lambda in FP32 arithmetic on offsets formed
+// in FP64 (the accuracy class of the FP32-pair product they join)
+__global__ void k_ops_f32_kernel(const double *__restrict__ r, const double *__restrict__ xb,
+                                 const int *__restrict__ boff, const double *__restrict__ x, double *__restrict__ y,
+                                 int n, int nb)
+{
+    const int b = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (b >= nb) return;
+    const double cx = xb[3 * b], cy = xb[3 * b + 1], cz = xb[3 * b + 2];
+    const double *Ud = x + 3LL * n + 6LL * b;
+    const float U0 = (float)Ud[0], U1 = (float)Ud[1], U2 = (float)Ud[2], U3 = (float)Ud[3], U4 = (float)Ud[4],
+                U5 = (float)Ud[5];
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f, s5 = 0.f;
+    for (int i = boff[b] + lane; i < boff[b + 1]; i += 32) {
+        const float dx = (float)(r[3 * i] - cx), dy = (float)(r[3 * i + 1] - cy), dz = (float)(r[3 * i + 2] - cz);
+        const float lx = (float)x[3LL * i], ly = (float)x[3LL * i + 1], lz = (float)x[3LL * i + 2];
+        s0 += lx; s1 += ly; s2 += lz;
+        s3 += dy * lz - dz * ly;
+        s4 += dz * lx - dx * lz;
+        s5 += dx * ly - dy * lx;
+        y[3LL * i] -= (double)(U0 + (U4 * dz - U5 * dy));
+        y[3LL * i + 1] -= (double)(U1 + (U5 * dx - U3 * dz));
+        y[3LL * i + 2] -= (double)(U2 + (U3 * dy - U4 * dx));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        s3 += __shfl_xor_sync(0xffffffffu, s3, o);
+        s4 += __shfl_xor_sync(0xffffffffu, s4, o);
+        s5 += __shfl_xor_sync(0xffffffffu, s5, o);
+    }
+    if (lane == 0) {
+        double *yb = y + 3LL * n + 6LL * b;
+        yb[0] = -(double)s0; yb[1] = -(double)s1; yb[2] = -(double)s2;
+        yb[3] = -(double)s3; yb[4] = -(double)s4; yb[5] = -(double)s5;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // dense per-body wall mobility M_b = nf * B M~(z_eff) B (row-major m x m)
 template <typename T>
@@ -668,6 +708,12 @@ int rigid_apply(RigidSystem &S, const double *x, double *y, int mode)
     // y_blob = M l
     if (int rc = rigid_mobility(S, x, y, mode)) return rc;
     const int tb = 256;
+    if (mode == RMW_MODE_MIXED) {
+        k_ops_f32_kernel<<<(unsigned)(((long long)S.nb * 32 + tb - 1) / tb), tb, 0, st>>>(S.r, S.xb, S.boff, x, y,
+                                                                                          S.n, S.nb);
+        RMW_CHECK_LAUNCH("rigid operator");
+        return RMW_OK;
+    }
     // y_blob -= K U
     k_times_u_kernel<<<(S.n + tb - 1) / tb, tb, 0, st>>>(S.r, S.xb, S.blob_body, x + 3LL * S.n, y, S.n, -1.0, 1.0);
     // y_body = -K^T l

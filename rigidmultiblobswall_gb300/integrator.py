@@ -28,6 +28,23 @@ def solve_mobility_problem(sys_, force_torque, slip=None, noise=None, tol=1e-8, 
     """Solution [lambda; U] of the mobility problem.  The RHS is scaled to norm 1
     before GMRES and the solution scaled back, as the reference does.
     Returns (solution, info, iterations, relative residual)."""
+    import numpy as np
+    host = all(x is None or isinstance(x, (np.ndarray, list, tuple)) for x in (force_torque, slip, noise))
+    if host:
+        # host inputs: the scaled RHS is formed on the host and copied once (no device round trip for |b|)
+        n3 = 3 * sys_.n_blobs
+        rhs = np.zeros(sys_.size)
+        if slip is not None:
+            rhs[:n3] = np.asarray(slip, dtype=np.float64).reshape(-1)
+        if noise is not None:
+            rhs[:n3] -= np.asarray(noise, dtype=np.float64).reshape(-1)
+        rhs[n3:] = -np.asarray(force_torque, dtype=np.float64).reshape(-1)
+        nrm = float(np.linalg.norm(rhs))
+        if nrm == 0.0:
+            import torch
+            return torch.zeros(sys_.size, dtype=torch.float64, device=sys_.device), 0, 0, 0.0
+        sol, info, its, rr = sys_.solve(rhs / nrm, tol=tol, restart=restart, maxiter=maxiter, mode=mode)
+        return sol.mul_(nrm), info, its, rr
     rhs = mobility_rhs(sys_, force_torque, slip, noise)
     nrm = float(rhs.norm())
     if nrm == 0.0:

@@ -254,3 +254,27 @@ def test_fp32_built_preconditioner_matches_oracle(cuda_device, stochastic):
         err = rel_err(s.apply_pc(x).cpu().numpy(), o.apply_pc(x))
         assert err <= 5e-3, err
     s.close()
+
+
+def test_mixed_operator_matches_oracle(cuda_device):
+    """The operator of the mixed inner solves (FP32-pair product, K U and K^T lambda in FP32 on offsets
+    formed in FP64) against the oracle's FP64 operator, on a random vector and on a solution of the
+    mobility problem (constraint forces whose body sums cancel): body rows <= 1e-5 relative; blob rows
+    <= 1e-5 of |M lambda| (at a solution M lambda - K U cancels to the residual)."""
+    susp = S.shells_42_256(n_bodies=24, seed=12)
+    r = susp.r_vectors()
+    s = RigidSystem([42] * 24, susp.eta, susp.a)
+    s.set_configuration(r, susp.locations)
+    o = orc.Rigid(r, susp.locations, s.offsets, susp.eta, susp.a)
+    FT = np.zeros((24, 6))
+    FT[:, 2] = -1.0
+    sol, info, _, _ = integrator.solve_mobility_problem(s, FT, tol=1e-8, mode="fp64")
+    assert info == 0
+    n3 = 3 * s.n_blobs
+    for x in (np.random.default_rng(5).standard_normal(s.size), sol.cpu().numpy()):
+        got = s.apply(x, mode="mixed").cpu().numpy()
+        ref = o.apply(x)
+        m_lam = o.apply(np.concatenate([x[:n3], np.zeros(s.size - n3)]))[:n3]
+        assert np.linalg.norm(got[:n3] - ref[:n3]) <= 1e-5 * np.linalg.norm(m_lam)
+        assert rel_err(got[n3:], ref[n3:]) <= 1e-5
+    s.close()

@@ -150,6 +150,37 @@ def arnoldi_traffic(fn):
                  "kernel": "arnoldi_step_kernel (fused CGS2 + Givens, one launch per step)"}
 
 
+def pc_apply_roofline(sys_, reps=30):
+    """Block-diagonal preconditioner apply, FP64 (FP64 and df64 solves) and FP32 (the mixed solves), timed
+    with CUDA events over reps applies with the plain preconditioner built.  Bytes: the per-body matrices
+    the kernel reads once per apply, M_b^-1 (m^2) and M_b^-1 K (6m) and N_b (36), times the element size,
+    plus the input and output vectors (FP64); the survey's unit for the reference's apply (two dense
+    GEMVs per body, 2 m^2 + 12 m + 36 elements) is reported beside it."""
+    import torch
+    m = np.diff(sys_.offsets) * 3
+    out = {}
+    x = torch.randn(sys_.size, dtype=torch.float64, device=sys_.device,
+                    generator=torch.Generator(device=sys_.device).manual_seed(9))
+    peak, src = hbm_peak_gbs()
+    for mode, es in (("fp64", 8), ("mixed", 4)):
+        sys_.apply_pc(x, mode=mode)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            sys_.apply_pc(x, mode=mode)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        nbytes = float(np.sum(m * m + 6 * m + 36)) * es + 2 * 8.0 * sys_.size
+        survey = float(np.sum(2 * m * m + 12 * m + 36)) * es
+        out[mode] = {"us": ms * 1e3, "bytes": nbytes, "gbs": nbytes / (ms * 1e-3) / 1e9,
+                     "frac_of_hbm": nbytes / (ms * 1e-3) / 1e9 / peak, "survey_unit_bytes": survey,
+                     "survey_unit_gbs": survey / (ms * 1e-3) / 1e9}
+    out["hbm_peak_gbs"], out["peak_source"] = peak, src
+    return out
+
+
 def reduce_step_ms(step_ms, ws, device=None):
     """Max over ranks of the timed-region milliseconds (every rank calls it)."""
     if ws == 1:
@@ -465,6 +496,8 @@ def solver_metrics(dev, reps=2):
         return integrator.solve_mobility_problem(sys2, FT, tol=1e-8, mode="mixed")
     _mixed()
     _, out["solve_shells42x256_mixed_breakdown"] = solve_breakdown(_mixed)
+    # the preconditioner apply (256 126 x 126 blocks: 16-33 MB, L2-resident)
+    out["pc_apply_shells42x256"] = pc_apply_roofline(sys2)
     # bandwidth of the Arnoldi vector work (33,792-long vectors: the basis stays in L2)
     sys2.build_pc()
     _, out["solve_shells42x256_mixed_arnoldi"] = arnoldi_traffic(
@@ -680,6 +713,11 @@ def cfg5_metrics(dev, modes=("fp64", "mixed", "mixed+exact", "mixed+learned", "m
     for mode, u in sols.items():
         if ref is not None:
             out[mode]["velocity_rel_err_vs_fp64"] = float(np.linalg.norm(u - ref) / np.linalg.norm(ref))
+    # the preconditioner apply at this size: 4096 blocks of 126 x 126 (0.26 GB in FP32, 0.52 GB in FP64
+    # per apply, beyond the L2)
+    nf.detach(sys5)
+    sys5.build_pc(mode="mixed")
+    out["pc_apply"] = pc_apply_roofline(sys5, reps=10)
     if "fp64" in out:
         for mode in modes:
             if mode != "fp64":

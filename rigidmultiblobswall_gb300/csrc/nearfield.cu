@@ -999,15 +999,12 @@ int rigid_pc_prepare_f32(RigidSystem &S)
     if (!S.pc_ready) return fail(RMW_ERR_ARG, "preconditioner not built (call rmw_rigid_build_pc)");
     if (S.pc32_ready || S.max_m > kPcF32MaxM) return RMW_OK;
     const long long tot = S.moff_h[S.nb];
-    if (!S.minv32) {
-        RMW_CUDA(cudaMalloc(&S.minv32, sizeof(float) * (size_t)tot));
-        RMW_CUDA(cudaMalloc(&S.minvK32, sizeof(float) * 18 * (size_t)S.n));
-        RMW_CUDA(cudaMalloc(&S.nmat32, sizeof(float) * 36 * (size_t)S.nb));
-        RMW_CUDA(cudaMalloc(&S.blob32, sizeof(float4) * (size_t)S.n));
+    if (int rc = alloc_pc32(S)) return rc;
+    if (!S.pc32_blocks) {
+        to_f32(S.minv, S.minv32, tot, S.st);
+        to_f32(S.minvK, S.minvK32, 18LL * S.n, S.st);
+        to_f32(S.nmat, S.nmat32, 36LL * S.nb, S.st);
     }
-    to_f32(S.minv, S.minv32, tot, S.st);
-    to_f32(S.minvK, S.minvK32, 18LL * S.n, S.st);
-    to_f32(S.nmat, S.nmat32, 36LL * S.nb, S.st);
     blob_geometry_f32_kernel<<<(S.n + 255) / 256, 256, 0, S.st>>>(S.r, S.xb, S.blob_body, S.n, S.blob32);
     RMW_CHECK_LAUNCH("FP32 preconditioner copies");
     S.pc32_ready = true;

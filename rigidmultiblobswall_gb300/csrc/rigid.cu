@@ -262,7 +262,7 @@ template <int R>
 __global__ void __launch_bounds__(256) pc_sweep_f32_kernel(const double *__restrict__ M,
                                                            const long long *__restrict__ moff,
                                                            const int *__restrict__ boff, double *__restrict__ minv,
-                                                           int *status)
+                                                           float *__restrict__ minv32, int *status)
 {
     __shared__ float colb[2][16 * R], rowb[2][16 * R];
     const int b = blockIdx.x;
@@ -325,6 +325,7 @@ __global__ void __launch_bounds__(256) pc_sweep_f32_kernel(const double *__restr
     }
     if (bad && threadIdx.x == 0) atomicExch(status, 1);  // not positive definite
     double *Mi = minv + moff[b];
+    float *Mf = minv32 + moff[b];
 #pragma unroll
     for (int u = 0; u < R; ++u)
 #pragma unroll
@@ -333,22 +334,118 @@ __global__ void __launch_bounds__(256) pc_sweep_f32_kernel(const double *__restr
             if (i < m && j < m && i <= j) {
                 Mi[(long long)i * m + j] = (double)A[u][w];
                 Mi[(long long)j * m + i] = (double)A[u][w];
+                Mf[(long long)i * m + j] = A[u][w];
+                Mf[(long long)j * m + i] = A[u][w];
             }
         }
 }
 
+// M^-1 K and N = (K^T M^-1 K)^-1 of the FP32 deterministic build, in FP32
+// from the sweep's FP32 M^-1 (as pc_body_kernel): written in both precisions,
+// FP32 for the mixed solves' apply, FP64 for the FP64 apply
+__global__ void pc_body_f32_kernel(const double *__restrict__ r, const double *__restrict__ xb,
+                                   const int *__restrict__ boff, const long long *__restrict__ moff,
+                                   const float *__restrict__ minv32, double *__restrict__ minvK,
+                                   float *__restrict__ minvK32, double *__restrict__ nmat, float *__restrict__ nmat32,
+                                   int *status)
+{
+    extern __shared__ float foff[];  // 3 per blob
+    __shared__ float G[36];
+    __shared__ float aug[6][12];
+    const int b = blockIdx.x;
+    const int o = boff[b], m = 3 * (boff[b + 1] - o);
+    const float *Mi = minv32 + moff[b];
+    const double cx = xb[3 * b], cy = xb[3 * b + 1], cz = xb[3 * b + 2];
+    for (int p = threadIdx.x; p < m / 3; p += blockDim.x) {
+        foff[3 * p] = (float)(r[3 * (o + p)] - cx);
+        foff[3 * p + 1] = (float)(r[3 * (o + p) + 1] - cy);
+        foff[3 * p + 2] = (float)(r[3 * (o + p) + 2] - cz);
+    }
+    __syncthreads();
+    float *MK32 = minvK32 + 18LL * o;
+    for (int t = threadIdx.x; t < m; t += blockDim.x) {
+        float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (int p = 0; p < m / 3; ++p) {
+            const float dx = foff[3 * p], dy = foff[3 * p + 1], dz = foff[3 * p + 2];
+            const float m0 = Mi[(long long)(3 * p) * m + t], m1 = Mi[(long long)(3 * p + 1) * m + t],
+                        m2 = Mi[(long long)(3 * p + 2) * m + t];
+            acc[0] += m0; acc[1] += m1; acc[2] += m2;
+            acc[3] += -dz * m1 + dy * m2;
+            acc[4] += dz * m0 - dx * m2;
+            acc[5] += -dy * m0 + dx * m1;
+        }
+        for (int c = 0; c < 6; ++c) {
+            MK32[6LL * t + c] = acc[c];
+            minvK[18LL * o + 6LL * t + c] = (double)acc[c];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 36) {
+        const int rr = threadIdx.x / 6, c = threadIdx.x % 6;
+        float sum = 0.f;
+        for (int p = 0; p < m / 3; ++p) {
+            const float dx = foff[3 * p], dy = foff[3 * p + 1], dz = foff[3 * p + 2];
+            const float k0 = MK32[6LL * (3 * p) + c], k1 = MK32[6LL * (3 * p + 1) + c], k2 = MK32[6LL * (3 * p + 2) + c];
+            float kr;
+            if (rr < 3) kr = (rr == 0) ? k0 : (rr == 1 ? k1 : k2);
+            else if (rr == 3) kr = -dz * k1 + dy * k2;
+            else if (rr == 4) kr = dz * k0 - dx * k2;
+            else kr = -dy * k0 + dx * k1;
+            sum += kr;
+        }
+        G[threadIdx.x] = sum;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 12; ++j) aug[i][j] = (j < 6) ? G[6 * i + j] : (j - 6 == i ? 1.f : 0.f);
+        for (int c = 0; c < 6; ++c) {
+            int piv = c;
+            for (int i = c + 1; i < 6; ++i)
+                if (fabsf(aug[i][c]) > fabsf(aug[piv][c])) piv = i;
+            if (piv != c)
+                for (int j = 0; j < 12; ++j) {
+                    const float t = aug[c][j]; aug[c][j] = aug[piv][j]; aug[piv][j] = t;
+                }
+            const float d = aug[c][c];
+            if (d == 0.f) { atomicExch(status, 2); continue; }
+            for (int j = 0; j < 12; ++j) aug[c][j] /= d;
+            for (int i = 0; i < 6; ++i) {
+                if (i == c) continue;
+                const float f = aug[i][c];
+                for (int j = 0; j < 12; ++j) aug[i][j] -= f * aug[c][j];
+            }
+        }
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                nmat32[36 * b + 6 * i + j] = aug[i][6 + j];
+                nmat[36 * b + 6 * i + j] = (double)aug[i][6 + j];
+            }
+    }
+}
+
+int alloc_pc32(RigidSystem &S)
+{
+    // each array on its own, so that a failed allocation leaves no half-set state behind
+    if (!S.minv32) RMW_CUDA(cudaMalloc(&S.minv32, sizeof(float) * (size_t)S.moff_h[S.nb]));
+    if (!S.minvK32) RMW_CUDA(cudaMalloc(&S.minvK32, sizeof(float) * 18 * (size_t)S.n));
+    if (!S.nmat32) RMW_CUDA(cudaMalloc(&S.nmat32, sizeof(float) * 36 * (size_t)S.nb));
+    if (!S.blob32) RMW_CUDA(cudaMalloc(&S.blob32, sizeof(float4) * (size_t)S.n));
+    return RMW_OK;
+}
+
 static void launch_pc_sweep_f32(int R, int nb, const double *M, const long long *moff, const int *boff,
-                                double *minv, int *status, cudaStream_t st)
+                                double *minv, float *minv32, int *status, cudaStream_t st)
 {
     switch (R) {
-    case 1: pc_sweep_f32_kernel<1><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
-    case 2: pc_sweep_f32_kernel<2><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
-    case 3: pc_sweep_f32_kernel<3><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
-    case 4: pc_sweep_f32_kernel<4><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
-    case 5: pc_sweep_f32_kernel<5><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
-    case 6: pc_sweep_f32_kernel<6><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
-    case 7: pc_sweep_f32_kernel<7><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
-    default: pc_sweep_f32_kernel<8><<<nb, 256, 0, st>>>(M, moff, boff, minv, status); break;
+    case 1: pc_sweep_f32_kernel<1><<<nb, 256, 0, st>>>(M, moff, boff, minv, minv32, status); break;
+    case 2: pc_sweep_f32_kernel<2><<<nb, 256, 0, st>>>(M, moff, boff, minv, minv32, status); break;
+    case 3: pc_sweep_f32_kernel<3><<<nb, 256, 0, st>>>(M, moff, boff, minv, minv32, status); break;
+    case 4: pc_sweep_f32_kernel<4><<<nb, 256, 0, st>>>(M, moff, boff, minv, minv32, status); break;
+    case 5: pc_sweep_f32_kernel<5><<<nb, 256, 0, st>>>(M, moff, boff, minv, minv32, status); break;
+    case 6: pc_sweep_f32_kernel<6><<<nb, 256, 0, st>>>(M, moff, boff, minv, minv32, status); break;
+    case 7: pc_sweep_f32_kernel<7><<<nb, 256, 0, st>>>(M, moff, boff, minv, minv32, status); break;
+    default: pc_sweep_f32_kernel<8><<<nb, 256, 0, st>>>(M, moff, boff, minv, minv32, status); break;
     }
 }
 constexpr int kSweepMaxM = 128;
@@ -632,7 +729,7 @@ __global__ void count_below_kernel(const double *__restrict__ r, int n, double z
 static int build_pc(RigidSystem &S, bool stochastic, bool fp32 = false)
 {
     cudaStream_t st = S.st;
-    S.pc32_ready = false;  // the FP32 copies follow the arrays rewritten here
+    S.pc32_ready = S.pc32_blocks = false;  // the FP32 copies follow the arrays rewritten here
     const long long tot = S.moff_h[S.nb];
     // working copy of the dense body mobilities (stream-ordered, freed below)
     void *ws = nullptr;
@@ -659,8 +756,14 @@ static int build_pc(RigidSystem &S, bool stochastic, bool fp32 = false)
         else body_mobility_free_kernel<double><<<S.nb, kRigidThreads, 0, st>>>(S.r, S.boff, S.moff, M, S.eta, S.a);
     }
     double *lf = stochastic ? S.lfac : nullptr, *li = stochastic ? S.linv : nullptr;
-    if (fp32 && !stochastic && S.max_m <= kSweepMaxM) {
-        launch_pc_sweep_f32((S.max_m + 15) / 16, S.nb, M, S.moff, S.boff, S.minv, S.dstatus, st);
+    const bool sweep = fp32 && !stochastic && S.max_m <= kSweepMaxM;
+    if (sweep) {
+        // the blocks in FP32 directly: M^-1, M^-1 K and N also as the mixed solves' FP32 copies
+        if (int rc = alloc_pc32(S)) {
+            cudaFreeAsync(ws, st);
+            return rc;
+        }
+        launch_pc_sweep_f32((S.max_m + 15) / 16, S.nb, M, S.moff, S.boff, S.minv, S.minv32, S.dstatus, st);
     } else if (fp32) {
         const size_t sm = sizeof(float) * ((size_t)S.max_m * S.max_m + S.max_m);
         RMW_CUDA(cudaFuncSetAttribute(pc_factor_smem_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -674,7 +777,10 @@ static int build_pc(RigidSystem &S, bool stochastic, bool fp32 = false)
     } else {
         pc_factor_global_kernel<<<S.nb, kRigidThreads, 0, st>>>(M, S.moff, S.boff, S.minv, lf, li, tmpg, S.dstatus);
     }
-    {
+    if (sweep) {
+        pc_body_f32_kernel<<<S.nb, 128, sizeof(float) * (size_t)S.max_m, st>>>(
+            S.r, S.xb, S.boff, S.moff, S.minv32, S.minvK, S.minvK32, S.nmat, S.nmat32, S.dstatus);
+    } else {
         const size_t sm = sizeof(double) * (size_t)S.max_m;
         if (sm > 48 * 1024)
             RMW_CUDA(cudaFuncSetAttribute(pc_body_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -692,6 +798,7 @@ static int build_pc(RigidSystem &S, bool stochastic, bool fp32 = false)
     S.stoch_ready = stochastic;
     S.pc_fp32 = fp32;
     S.pc32_ready = false;
+    S.pc32_blocks = sweep;  // the FP32 copies of the blocks are already written
     return RMW_OK;
 }
 

@@ -40,6 +40,7 @@ struct RigidSystem {
     float *minv32 = nullptr, *minvK32 = nullptr, *nmat32 = nullptr;
     float4 *blob32 = nullptr;  // n: blob offset from its body's centre and height, FP32
     bool pc32_ready = false;
+    bool pc32_blocks = false;  // the build wrote minv32, minvK32, nmat32 itself (FP32 sweep build)
     bool wall = true;  // false: free-space (no-wall) mobility (rmw_rigid_set_wall)
     // independent suspensions inside the handle (rmw_rigid_set_suspensions):
     // segmented pair products and the instance-major permutation
@@ -90,6 +91,8 @@ int rigid_apply_pc_mixed(RigidSystem &S, const double *x, double *y);
 // FP32 copies of the built preconditioner (no-op when current); call before
 // capturing rigid_apply_pc_mixed into a CUDA graph.
 int rigid_pc_prepare_f32(RigidSystem &S);
+// allocate the FP32 copies (no-op when present)
+int alloc_pc32(RigidSystem &S);
 // y = L^-1 M L^-T w on the blob space (det_stoch mobility_pc, multi_bodies.py:591-606).
 int rigid_mobility_pc(RigidSystem &S, const double *w, double *y, int mode);
 // y = L w (det_stoch P_inv_mult, multi_bodies.py:609-615).

@@ -87,6 +87,8 @@ def parse():
                    help="only run the 4096-shell (172,032-blob) solve comparison and print its JSON line")
     p.add_argument("--large-modes",
                    default="fp64,mixed,mixed+exact,mixed+learned,mixed+learned_band,mixed+exact+learned")
+    p.add_argument("--pc-probe", action="store_true",
+                   help="only the 4096-shell block-diagonal preconditioner applies (FP64 and FP32), timed")
     p.add_argument("--krylov-probe", action="store_true",
                    help="only the 4096-shell mixed solve with graphs off (each fused Arnoldi step a traced direct "
                         "launch) and the pair scratch capped at 1 GiB: the Arnoldi steps' time and bandwidth")
@@ -907,10 +909,30 @@ def krylov_probe():
                       "arnoldi": arn}))
 
 
+def pc_probe():
+    """The block-diagonal preconditioner of the 4096-shell suspension (FP32 build, the mixed solves'):
+    the FP64 and FP32 applies timed over repeated calls, one JSON line (pc_apply_roofline)."""
+    import torch
+    from rigidmultiblobswall_gb300 import build as B
+    B.build()
+    from rigidmultiblobswall_gb300 import suspensions as S
+    from rigidmultiblobswall_gb300.rigid import RigidSystem
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    s5 = S.shells_42_4096()
+    sys5 = RigidSystem([42] * s5.n_bodies, s5.eta, s5.a, device=dev)
+    sys5.set_configuration(s5.r_vectors(), s5.locations)
+    sys5.build_pc(mode="mixed")
+    print(json.dumps({"workload": "4096 shells x 42 blobs, 4096 126 x 126 blocks", **pc_apply_roofline(sys5, reps=20)}))
+
+
 def main():
     args = parse()
     if args.krylov_probe:
         krylov_probe()
+        return
+    if args.pc_probe:
+        pc_probe()
         return
     if args.large:
         large_solve(args)

@@ -801,20 +801,31 @@ def batched_metrics(dev, nrhs=16):
     _native.use_graphs(False)
     _native.trace_enable(True)
     _native.trace_read(0, reset=True)
+    _native.trace_read(1, reset=True)
+    _native.trace_bytes(1, reset=True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     _, itl2 = sysb.lanczos_batched(Z, factor=np.sqrt(2.0 / 1e-3), tol=1e-3, mode="mixed")
     torch.cuda.synchronize()
     lz_ms = (time.perf_counter() - t0) * 1e3
     pair_ms, pair_launches = _native.trace_read(0, reset=True)
+    step_ms, step_launches = _native.trace_read(1, reset=True)
+    _native.trace_bytes(1, reset=True)
+    for k in (2, 3, 4, 5, 6, 7):
+        _native.trace_read(k, reset=True)
     _native.trace_enable(False)
     _native.use_graphs(True)
+    hbm, hsrc = hbm_peak_gbs()
     it = np.asarray(itl2).reshape(nrhs, len(counts))
     nblob = 42 * np.asarray(counts, dtype=np.float64)
     prhs = 0.0
     for p in range(0, nrhs, 16):
         w = min(16, nrhs - p)
         prhs += float(((it[p:p + w].max(axis=0) + 1) * nblob ** 2).sum()) * (16 if w > 8 else 8)
+    # algorithmic traffic of the Lanczos steps: a segment (right-hand side q of suspension k, 3 n_k long)
+    # that reports it iterations ran steps i = 0..it, step i moving (2i + 4) x 3 n_k doubles (full
+    # reorthogonalisation over V_0..V_i)
+    step_bytes = float((24.0 * nblob[None, :] * (it + 1) * (it + 4)).sum())
     peak32 = _native.fma_peak(False)
     ipr = MULTI16_INST_PER_PAIR_RHS
     out["lanczos_16rhs_roofline"] = {
@@ -822,7 +833,12 @@ def batched_metrics(dev, nrhs=16):
         "pair_kernel_share": pair_ms / lz_ms, "pair_rhs_evaluated": prhs,
         "tpair_rhs_per_s": prhs / (pair_ms * 1e-3) / 1e12,
         "issued_inst_per_pair_rhs": ipr, "fp32_issue_frac": prhs * ipr / (pair_ms * 1e-3) / (peak32 / 2.0),
-        "note": "issued instructions per pair-RHS from the ncu capture of wall_pair_multi_kernel (16 RHS)"}
+        "note": "issued instructions per pair-RHS from the ncu capture of wall_pair_multi_kernel (16 RHS)",
+        "lanczos_step_kernel": {"launches": step_launches, "ms": step_ms, "gbytes": step_bytes / 1e9,
+                                "gbs": step_bytes / (step_ms * 1e-3) / 1e9 if step_ms > 0 else None,
+                                "frac_of_hbm": step_bytes / (step_ms * 1e-3) / 1e9 / hbm if step_ms > 0 else None,
+                                "hbm_peak_gbs": hbm, "peak_source": hsrc,
+                                "bytes_per_step": "(2i + 4) x 3N doubles (full reorthogonalisation over V_0..V_i)"}}
     return out
 
 

@@ -853,7 +853,7 @@ int rmw_rigid_lanczos_batched(void *sys, const double *Z, double *noise, int nrh
         rc = rmw::lanczos_batched(op, Z, raw, off, factor, tol, max_iter, S.st, it, before_op);
     }
     if (d_act) cudaFreeAsync(d_act, S.st);
-    if (rc == RMW_OK) rc = rmw::rigid_P_inv_mult_multi(S, raw, noise, nrhs);
+    if (rc == RMW_OK) rc = rmw::rigid_P_inv_mult_multi(S, raw, noise, nrhs, mode);
     cudaFreeAsync(buf, S.st);
     cudaStreamSynchronize(S.st);
     if (rc) return rc;

@@ -640,31 +640,81 @@ __global__ void block_tri_mult_kernel(const double *__restrict__ T, const long l
 // vector, instead of one FP64 pass over the block per vector.  Shared
 // memory: m^2 + nvec m floats.  In place (y == x) is safe: the body's slice of
 // every vector is staged before any is written.
-__global__ void block_tri_mult_f32_kernel(const double *__restrict__ T, const long long *__restrict__ moff,
+// y_v = T x_v (or T^T x_v) for nvec vectors per body in FP32, one CTA per
+// body.  The factor sits in shared memory as S[k][t] (T transposed for T x,
+// as is for T^T x), so that every thread owns one output row t and all rows
+// walk k = 0..m-1 together: S reads are consecutive over the threads, the
+// vectors' entries x[k][v] are broadcast, and each thread runs sixteen
+// independent FMA chains (sixteen vectors at a time).  The walk covers the
+// factor's zero triangle too (exact: those entries are zero).
+template <typename TT>
+__global__ void block_tri_mult_f32_kernel(const TT *__restrict__ T, const long long *__restrict__ moff,
                                           const int *__restrict__ boff, const double *x, double *y, int transpose,
                                           long long ld, int nvec)
 {
-    extern __shared__ float tsm[];
+    extern __shared__ __align__(16) float tsm[];
     const int b = blockIdx.x;
     const int o = boff[b], m = 3 * (boff[b + 1] - o);
-    float *Ts = tsm, *xs = tsm + (size_t)m * m;
-    const double *Tb = T + moff[b];
-    for (int e = threadIdx.x; e < m * m; e += blockDim.x) Ts[e] = (float)Tb[e];
-    for (int e = threadIdx.x; e < nvec * m; e += blockDim.x) {
-        const int v = e / m, t = e - v * m;
-        xs[e] = (float)x[(long long)v * ld + 3LL * o + t];
+    const int nv16 = (nvec + 15) & ~15;
+    float *Ss = tsm, *xs = tsm + (((size_t)m * m + 3) & ~(size_t)3);  // xs[k * nv16 + v], 16-byte aligned
+    const TT *Tb = T + moff[b];
+    // the factor's load is the latency-bound part (a few CTAs per SM): 16-byte
+    // loads, four in flight per thread
+    constexpr int kV = 16 / sizeof(TT);  // elements per 16-byte load
+    const int mm = m * m;
+    const bool vec = (mm % kV) == 0 && (moff[b] % kV) == 0;
+    auto put = [&](int e, float val) {
+        if (transpose) {
+            Ss[e] = val;
+        } else {
+            const int i = e / m, j = e - i * m;
+            Ss[j * m + i] = val;
+        }
+    };
+    if (vec) {
+        const int nq = mm / kV;
+#pragma unroll 4
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            if constexpr (sizeof(TT) == 4) {
+                const float4 w = reinterpret_cast<const float4 *>(Tb)[q];
+                put(4 * q, w.x); put(4 * q + 1, w.y); put(4 * q + 2, w.z); put(4 * q + 3, w.w);
+            } else {
+                const double2 w = reinterpret_cast<const double2 *>(Tb)[q];
+                put(2 * q, (float)w.x); put(2 * q + 1, (float)w.y);
+            }
+        }
+    } else {
+#pragma unroll 4
+        for (int e = threadIdx.x; e < mm; e += blockDim.x) put(e, (float)Tb[e]);
+    }
+#pragma unroll 4
+    for (int e = threadIdx.x; e < nv16 * m; e += blockDim.x) {
+        const int v = e / m, k = e - v * m;
+        xs[k * nv16 + v] = (v < nvec) ? (float)x[(long long)v * ld + 3LL * o + k] : 0.f;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < nvec * m; e += blockDim.x) {
-        const int v = e / m, t = e - v * m;
-        const float *xv = xs + (size_t)v * m;
-        float acc = 0.f;
-        if (!transpose)
-            for (int k = 0; k <= t; ++k) acc = fmaf(Ts[t * m + k], xv[k], acc);
-        else
-            for (int k = t; k < m; ++k) acc = fmaf(Ts[k * m + t], xv[k], acc);
-        y[(long long)v * ld + 3LL * o + t] = acc;
-    }
+    for (int t = threadIdx.x; t < m; t += blockDim.x)
+        for (int v0 = 0; v0 < nvec; v0 += 16) {
+            float acc[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) acc[q] = 0.f;
+#pragma unroll 2
+            for (int k = 0; k < m; ++k) {
+                const float sk = Ss[k * m + t];
+                const float4 *xk = reinterpret_cast<const float4 *>(xs + k * nv16 + v0);
+#pragma unroll
+                for (int g = 0; g < 4; ++g) {
+                    const float4 xv = xk[g];
+                    acc[4 * g] = fmaf(sk, xv.x, acc[4 * g]);
+                    acc[4 * g + 1] = fmaf(sk, xv.y, acc[4 * g + 1]);
+                    acc[4 * g + 2] = fmaf(sk, xv.z, acc[4 * g + 2]);
+                    acc[4 * g + 3] = fmaf(sk, xv.w, acc[4 * g + 3]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 16; ++q)
+                if (v0 + q < nvec) y[(long long)(v0 + q) * ld + 3LL * o + t] = acc[q];
+        }
 }
 
 // ---------------------------------------------------------------------------
@@ -726,10 +776,16 @@ __global__ void count_below_kernel(const double *__restrict__ r, int n, double z
 
 // ---------------------------------------------------------------------------
 // host side
+__global__ void double_to_float_kernel(const double *__restrict__ x, float *__restrict__ y, long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        y[i] = (float)x[i];
+}
+
 static int build_pc(RigidSystem &S, bool stochastic, bool fp32 = false)
 {
     cudaStream_t st = S.st;
-    S.pc32_ready = S.pc32_blocks = false;  // the FP32 copies follow the arrays rewritten here
+    S.pc32_ready = S.pc32_blocks = S.linv32_ready = false;  // the FP32 copies follow the arrays rewritten here
     const long long tot = S.moff_h[S.nb];
     // working copy of the dense body mobilities (stream-ordered, freed below)
     void *ws = nullptr;
@@ -794,6 +850,14 @@ static int build_pc(RigidSystem &S, bool stochastic, bool fp32 = false)
     if (hstat != 0 && fp32) return build_pc(S, stochastic, false);  // FP32 factorisation failed: FP64 instead
     if (hstat == 1) return fail(RMW_ERR_NONFINITE, "body mobility matrix is not positive definite (Cholesky failed)");
     if (hstat == 2) return fail(RMW_ERR_NONFINITE, "singular 6x6 body resistance K^T M^-1 K");
+    if (fp32 && stochastic) {
+        // the FP32 copy of L^-1 for the mixed multi-vector Lanczos products
+        if (!S.linv32) RMW_CUDA(cudaMalloc(&S.linv32, sizeof(float) * (size_t)tot));
+        const unsigned g = (unsigned)std::min<long long>((tot + 255) / 256, 152LL * 16);
+        double_to_float_kernel<<<g, 256, 0, st>>>(S.linv, S.linv32, tot);
+        RMW_CHECK_LAUNCH("FP32 copy of L^-1");
+        S.linv32_ready = true;
+    }
     S.pc_ready = true;
     S.stoch_ready = stochastic;
     S.pc_fp32 = fp32;
@@ -871,17 +935,31 @@ int rigid_mobility_pc(RigidSystem &S, const double *w, double *y, int mode)
 
 // FP32 form of tri_mult for all nvec vectors per body (mixed mode); false when
 // a body's block does not fit the shared memory
-static bool tri_mult_f32_fits(const RigidSystem &S, int nvec)
+static size_t tri_mult_f32_smem(const RigidSystem &S, int nvec)
 {
-    return ((size_t)S.max_m * S.max_m + (size_t)nvec * S.max_m) * sizeof(float) <= 200 * 1024;
+    return ((((size_t)S.max_m * S.max_m + 3) & ~(size_t)3) + (size_t)((nvec + 15) & ~15) * S.max_m) * sizeof(float);
 }
+static bool tri_mult_f32_fits(const RigidSystem &S, int nvec) { return tri_mult_f32_smem(S, nvec) <= 200 * 1024; }
+// T: the FP64 factor; its FP32 copy is read instead when the build made one
+// (half the bytes, no conversion per element and launch)
 static int tri_mult_f32(RigidSystem &S, const double *T, const double *x, double *y, int transpose, int nvec)
 {
-    const size_t sm = ((size_t)S.max_m * S.max_m + (size_t)nvec * S.max_m) * sizeof(float);
-    if (sm > 48 * 1024)
-        RMW_CUDA(cudaFuncSetAttribute(block_tri_mult_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sm));
-    block_tri_mult_f32_kernel<<<S.nb, 256, sm, S.st>>>(T, S.moff, S.boff, x, y, transpose, 3LL * S.n, nvec);
+    const size_t sm = tri_mult_f32_smem(S, nvec);
+    const bool f32 = T == S.linv && S.linv32_ready;
+    if (sm > 48 * 1024) {
+        if (f32)
+            RMW_CUDA(cudaFuncSetAttribute(block_tri_mult_f32_kernel<float>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        else
+            RMW_CUDA(cudaFuncSetAttribute(block_tri_mult_f32_kernel<double>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    }
+    if (f32)
+        block_tri_mult_f32_kernel<float><<<S.nb, 256, sm, S.st>>>(S.linv32, S.moff, S.boff, x, y, transpose,
+                                                                   3LL * S.n, nvec);
+    else
+        block_tri_mult_f32_kernel<double><<<S.nb, 256, sm, S.st>>>(T, S.moff, S.boff, x, y, transpose, 3LL * S.n,
+                                                                    nvec);
     RMW_CHECK_LAUNCH("block triangular multiply (FP32)");
     return RMW_OK;
 }
@@ -906,9 +984,11 @@ int rigid_mobility_pc_multi(RigidSystem &S, const double *W, double *Y, int nvec
     return tri_mult(S, S.linv, Y, Y, 0, nvec);
 }
 
-int rigid_P_inv_mult_multi(RigidSystem &S, const double *W, double *Y, int nvec)
+int rigid_P_inv_mult_multi(RigidSystem &S, const double *W, double *Y, int nvec, int mode)
 {
     if (!S.stoch_ready) return fail(RMW_ERR_ARG, "stochastic preconditioner not built");
+    // mixed: the FP32 multiply (each body's factor read once for all vectors)
+    if (mode == RMW_MODE_MIXED && tri_mult_f32_fits(S, nvec)) return tri_mult_f32(S, S.lfac, W, Y, 0, nvec);
     return tri_mult(S, S.lfac, W, Y, 0, nvec);
 }
 
@@ -926,7 +1006,7 @@ static void free_system(RigidSystem *S)
     void *ptrs[] = {S->boff, S->blob_body, S->moff, S->r, S->xb, S->minv, S->minvK, S->nmat, S->lfac, S->linv,
                     S->dstatus, S->tmp3n, S->perm, S->nf_off, S->nf_ex_idx, S->nf_ln_idx, S->nf_mp_idx, S->nf_cnt, S->nf_range,
                     S->nf_G, S->nf_mom, S->nf_v, S->nf_z, S->nf_part, S->minv32, S->minvK32, S->nmat32,
-                    S->blob32, S->nf_mom32, S->nf_lam32, S->nf_G32};
+                    S->blob32, S->nf_mom32, S->nf_lam32, S->nf_G32, S->linv32};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (S->batch) {

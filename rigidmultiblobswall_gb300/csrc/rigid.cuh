@@ -41,6 +41,8 @@ struct RigidSystem {
     float4 *blob32 = nullptr;  // n: blob offset from its body's centre and height, FP32
     bool pc32_ready = false;
     bool pc32_blocks = false;  // the build wrote minv32, minvK32, nmat32 itself (FP32 sweep build)
+    float *linv32 = nullptr;   // FP32 copy of linv after an FP32 stochastic build (multi-vector L^-1 multiplies)
+    bool linv32_ready = false;
     bool wall = true;  // false: free-space (no-wall) mobility (rmw_rigid_set_wall)
     // independent suspensions inside the handle (rmw_rigid_set_suspensions):
     // segmented pair products and the instance-major permutation
@@ -103,7 +105,7 @@ int rigid_P_inv_mult(RigidSystem &S, const double *w, double *y);
 // multi-vector product (wall_uf_multi); 0 skips that suspension's rows.
 int rigid_mobility_pc_multi(RigidSystem &S, const double *W, double *Y, int nvec, int mode, double *tmp,
                             const unsigned char *active = nullptr);
-int rigid_P_inv_mult_multi(RigidSystem &S, const double *W, double *Y, int nvec);
+int rigid_P_inv_mult_multi(RigidSystem &S, const double *W, double *Y, int nvec, int mode = RMW_MODE_FP64);
 // near-field augmented preconditioner apply, nearfield.cu
 int nearfield_apply_pc(RigidSystem &S, const double *x, double *y);
 // M v on the handle's blobs (segmented by suspension when suspensions are set).

@@ -145,3 +145,8 @@ def test_batched_lanczos_matches_per_suspension_oracle(cuda_device):
     noise32, it32 = sys_.lanczos_batched(Z, factor=factor, tol=1e-3, mode="mixed")
     assert np.abs(it32 - it).max() <= 1
     assert rel_err(noise32.cpu().numpy(), noise) <= 1e-4
+    # the FP32-built stochastic preconditioner, whose FP32 copy of L^-1 the multi-vector multiplies read
+    sys_.build_pc(stochastic=True, mode="mixed")
+    noise32b, it32b = sys_.lanczos_batched(Z, factor=factor, tol=1e-3, mode="mixed")
+    assert np.abs(it32b - it).max() <= 1
+    assert rel_err(noise32b.cpu().numpy(), noise) <= 1e-4

@@ -316,6 +316,13 @@ int rmw_count_below(const double *r, int64_t n, double zmin, int *count_host, vo
  * best iterate is still written to sol). */
 int rmw_rigid_solve(void *handle, const double *rhs, double *sol, double tol, int restart, int maxiter, int mode,
                     int *iters_host, double *relres_host);
+/* rmw_rigid_solve on the right-hand side scaled to unit norm, the solution
+ * scaled back: solve_mobility_problem's normalisation
+ * (quaternion_integrator_multi_bodies.py:1519-1537).  A zero rhs gives a zero
+ * solution without GMRES.  Returns after the solve (the last scaling is queued
+ * on the handle's stream); the codes are rmw_rigid_solve's. */
+int rmw_rigid_solve_scaled(void *handle, const double *rhs, double *sol, double tol, int restart, int maxiter,
+                           int mode, int *iters_host, double *relres_host);
 /* noise = factor * L (L^-1 M L^-T)^(1/2) z by Lanczos: stochastic_forcing_lanczos
  * with mobility_mult = mobility_pc and L_mult = P_inv_mult
  * (stochastic_forcing/stochastic_forcing.py:112-264), z and noise 3N device

@@ -88,6 +88,8 @@ SIGNATURES = {
     "rmw_count_below": (_i, [_vp, _i64, _d, ctypes.POINTER(ctypes.c_int), _vp]),
     "rmw_rigid_solve": (_i, [_vp, _vp, _vp, _d, _i, _i, _i, ctypes.POINTER(ctypes.c_int),
                              ctypes.POINTER(ctypes.c_double)]),
+    "rmw_rigid_solve_scaled": (_i, [_vp, _vp, _vp, _d, _i, _i, _i, ctypes.POINTER(ctypes.c_int),
+                             ctypes.POINTER(ctypes.c_double)]),
     "rmw_rigid_lanczos": (_i, [_vp, _vp, _vp, _d, _d, _i, _i, ctypes.POINTER(ctypes.c_int)]),
     "rmw_wall_lanczos": (_i, [_vp, _vp, _vp, _i64, _d, _d, _vp, _d, _d, _i, _i, _vp,
                               ctypes.POINTER(ctypes.c_int)]),

@@ -124,7 +124,7 @@ int rmw_wall_autotune(int kind, int mode, int64_t n, int reps, void *stream, int
         return rmw::cuda_fail(e, "cudaEventCreate");
     }
     char *buf = nullptr;
-    if (cudaError_t e = cudaMallocAsync((void **)&buf, 3 * vec + ws_bytes + 256, st)) {
+    if (cudaError_t e = rmw::dmalloc_async((void **)&buf, 3 * vec + ws_bytes + 256, st)) {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         return rmw::cuda_fail(e, "cudaMallocAsync (autotune buffers)");

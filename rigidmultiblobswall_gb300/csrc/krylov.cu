@@ -256,7 +256,7 @@ static int make_work(long long n, int kmax, cudaStream_t st, KrylovWork &K, int 
     const long long ldv = ((n + 31) / 32) * 32;
     const size_t doubles = (size_t)ldv * nbasis + 5 * (size_t)ldv + (size_t)nblk * (kChunk + 2) + 4 * (kmax + 8);
     void *p = nullptr;
-    RMW_CUDA(cudaMallocAsync(&p, sizeof(double) * doubles, st));
+    RMW_CUDA(rmw::dmalloc_async(&p, sizeof(double) * doubles, st));
     K.base = p;
     K.st = st;
     double *d = (double *)p;
@@ -480,7 +480,7 @@ static int lanczos(Op op, const double *z, double *noise, long long n, double fa
     // The basis grows on demand (stream-ordered allocations, doubling).
     int vcap = std::min(kcap + 1, 32);
     double *Vb = nullptr;
-    RMW_CUDA(cudaMallocAsync(&Vb, sizeof(double) * ldv * vcap, st));
+    RMW_CUDA(rmw::dmalloc_async(&Vb, sizeof(double) * ldv * vcap, st));
     K.V = Vb;
     struct Guard {
         double **p;
@@ -546,7 +546,7 @@ static int lanczos(Op op, const double *z, double *noise, long long n, double fa
         if (i + 2 > vcap) {
             const int ncap = std::min(kcap + 1, 2 * vcap);
             double *nv = nullptr;
-            RMW_CUDA(cudaMallocAsync(&nv, sizeof(double) * ldv * ncap, st));
+            RMW_CUDA(rmw::dmalloc_async(&nv, sizeof(double) * ldv * ncap, st));
             RMW_CUDA(cudaMemcpyAsync(nv, K.V, sizeof(double) * ldv * vcap, cudaMemcpyDeviceToDevice, st));
             RMW_CUDA(cudaFreeAsync(K.V, st));
             K.V = nv;
@@ -579,6 +579,13 @@ static int lanczos(Op op, const double *z, double *noise, long long n, double fa
     return RMW_OK;
 }
 
+// y = x / d
+__global__ void div_scalar_kernel(const double *__restrict__ x, double *__restrict__ y, long long n, double d)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = x[i] / d;
+}
+
 }  // namespace rmw
 
 // ---------------------------------------------------------------------------
@@ -599,6 +606,44 @@ int rmw_rigid_solve(void *sys, const double *rhs, double *sol, double tol, int r
     if (int rc = rmw::trace_begin(rmw::TRACE_SOLVE, S.st, &tok)) return rc;
     const int rc = rigid_solve_impl(sys, rhs, sol, tol, restart, maxiter, mode, iters_host, relres_host);
     if (int rc2 = rmw::trace_end(tok, S.st)) return rc2;
+    return rc;
+}
+
+int rmw_rigid_solve_scaled(void *sys, const double *rhs, double *sol, double tol, int restart, int maxiter, int mode,
+                           int *iters_host, double *relres_host)
+{
+    if (!sys || !rhs || !sol) return rmw::fail(RMW_ERR_ARG, "null argument");
+    RigidSystem &S = *(RigidSystem *)sys;
+    const long long n = S.sys_size();
+    const int nblk = (int)((n + 1023) / 1024);
+    double *buf = nullptr;  // the scaled rhs, the norm's block partials and its square
+    RMW_CUDA(rmw::dmalloc_async(&buf, sizeof(double) * (n + nblk + 1), S.st));
+    struct FreeB {
+        double *p;
+        cudaStream_t s;
+        ~FreeB() { cudaFreeAsync(p, s); }
+    } free_b{buf, S.st};
+    double *bs = buf, *part = buf + n, *nrm2 = part + nblk;
+    rmw::dots_partial_kernel<<<nblk, 256, sizeof(double) * 8, S.st>>>(rhs, 0, 1, rhs, n, part);
+    rmw::reduce_partial_kernel<<<1, 32, 0, S.st>>>(part, nblk, 1, nrm2, 0);
+    double h = 0.0;
+    RMW_CUDA(cudaMemcpyAsync(&h, nrm2, sizeof(double), cudaMemcpyDeviceToHost, S.st));
+    RMW_CUDA(cudaStreamSynchronize(S.st));
+    const double nrm = std::sqrt(h);
+    if (!std::isfinite(nrm)) return rmw::fail(RMW_ERR_NONFINITE, "right-hand side is not finite");
+    if (nrm == 0.0) {
+        RMW_CUDA(cudaMemsetAsync(sol, 0, sizeof(double) * n, S.st));
+        RMW_CUDA(cudaStreamSynchronize(S.st));
+        if (iters_host) *iters_host = 0;
+        if (relres_host) *relres_host = 0.0;
+        return RMW_OK;
+    }
+    const unsigned g = (unsigned)((n + 255) / 256);
+    rmw::div_scalar_kernel<<<g, 256, 0, S.st>>>(rhs, bs, n, nrm);
+    const int rc = rmw_rigid_solve(sys, bs, sol, tol, restart, maxiter, mode, iters_host, relres_host);
+    if (rc != RMW_OK && rc != RMW_ERR_NOT_CONVERGED) return rc;
+    rmw::axpby_kernel<<<g, 256, 0, S.st>>>(sol, sol, n, 0.0, nrm);
+    RMW_CHECK_LAUNCH("rmw_rigid_solve_scaled");
     return rc;
 }
 
@@ -624,7 +669,7 @@ static int rigid_solve_impl(void *sys, const double *rhs, double *sol, double to
     };
     // A P^-1 fused through a private buffer and replayed as one CUDA graph
     double *pbuf = nullptr;
-    RMW_CUDA(cudaMallocAsync(&pbuf, sizeof(double) * n, S.st));
+    RMW_CUDA(rmw::dmalloc_async(&pbuf, sizeof(double) * n, S.st));
     struct FreeP {
         double *p;
         cudaStream_t s;
@@ -672,30 +717,21 @@ static int rigid_solve_impl(void *sys, const double *rhs, double *sol, double to
     // b - A x uses the FP64-accurate double-float operator (<= 1e-12 against
     // FP64), or the recurrence r - A32 d once it is small enough
     auto op32 = [&](const double *x, double *y) { return rmw::rigid_apply(S, x, y, RMW_MODE_MIXED); };
-    double *buf = nullptr;  // x, r, d, A32 d
-    RMW_CUDA(cudaMallocAsync(&buf, sizeof(double) * 4 * n, S.st));
+    // x, r, d, A32 d, then the norm's block partials and result
+    const int nblk = (int)((n + 1023) / 1024);
+    double *buf = nullptr;
+    RMW_CUDA(rmw::dmalloc_async(&buf, sizeof(double) * (4 * n + nblk + 1), S.st));
     double *x = buf, *r = buf + n, *d = buf + 2 * n, *ad = buf + 3 * n;
+    double *part = buf + 4 * n, *nrm2 = part + nblk;
     RMW_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, S.st));
     RMW_CUDA(cudaMemcpyAsync(r, rhs, sizeof(double) * n, cudaMemcpyDeviceToDevice, S.st));
-    std::vector<double> hb(1);
-    // |b| via a tiny GMRES-free reduction: reuse the refinement loop's norm
+    // |v| through the dots kernels (block partials, then one fixed-order sum)
     auto norm = [&](const double *v, double *out) -> int {
-        double *tmp = nullptr;
-        RMW_CUDA(cudaMallocAsync(&tmp, sizeof(double), S.st));
-        // one-block norm through the dots kernel path
-        rmw::VecOps O;
-        O.st = S.st;
-        O.n = n;
-        O.nblk = (int)((n + 1023) / 1024);
-        double *part = nullptr;
-        RMW_CUDA(cudaMallocAsync(&part, sizeof(double) * O.nblk, S.st));
-        rmw::dots_partial_kernel<<<O.nblk, 256, sizeof(double) * 8, S.st>>>(v, 0, 1, v, n, part);
-        rmw::reduce_partial_kernel<<<1, 32, 0, S.st>>>(part, O.nblk, 1, tmp, 0);
+        rmw::dots_partial_kernel<<<nblk, 256, sizeof(double) * 8, S.st>>>(v, 0, 1, v, n, part);
+        rmw::reduce_partial_kernel<<<1, 32, 0, S.st>>>(part, nblk, 1, nrm2, 0);
         double h = 0.0;
-        RMW_CUDA(cudaMemcpyAsync(&h, tmp, sizeof(double), cudaMemcpyDeviceToHost, S.st));
+        RMW_CUDA(cudaMemcpyAsync(&h, nrm2, sizeof(double), cudaMemcpyDeviceToHost, S.st));
         RMW_CUDA(cudaStreamSynchronize(S.st));
-        RMW_CUDA(cudaFreeAsync(part, S.st));
-        RMW_CUDA(cudaFreeAsync(tmp, S.st));
         *out = std::sqrt(h);
         return RMW_OK;
     };
@@ -709,8 +745,9 @@ static int rigid_solve_impl(void *sys, const double *rhs, double *sol, double to
     // when the outer loop recomputes b - A x anyway, and hand it over as the
     // next residual when the outer loop takes the recurrence r - A32 d (the
     // same vector): one FP32-pair operator application less per refinement.
-    bool carried = false;
-    double rnorm_next = 0.0;
+    // The first residual is b itself, whose norm is known.
+    bool carried = true;
+    double rnorm_next = bnorm;
     for (int outer = 0; outer < 8 && bnorm > 0.0; ++outer) {
         double rnorm = rnorm_next;
         if (!carried)
@@ -775,7 +812,7 @@ int rmw_rigid_lanczos(void *sys, const double *z, double *noise, double factor, 
     auto gop = rmw::make_graph_op(op_direct, &S.st, n, n);  // one graph per application
     auto op = [&](const double *x, double *y) -> int { return gop(x, y); };
     double *tmp = nullptr;
-    RMW_CUDA(cudaMallocAsync(&tmp, sizeof(double) * n, S.st));
+    RMW_CUDA(rmw::dmalloc_async(&tmp, sizeof(double) * n, S.st));
     int rc = RMW_OK;
     if (rmw::krylov_device_enabled() && rmw::krylov_device_available()) {
         // device-resident iterations (fused step kernel, one graph launch per call)
@@ -815,7 +852,7 @@ int rmw_gmres(int64_t n, rmw_operator_fn op, void *op_ctx, rmw_operator_fn pc, v
         return rc ? rmw::fail(rc, "preconditioner callback failed") : RMW_OK;
     };
     double *tmp = nullptr;
-    RMW_CUDA(cudaMallocAsync(&tmp, sizeof(double) * n, st));
+    RMW_CUDA(rmw::dmalloc_async(&tmp, sizeof(double) * n, st));
     auto AP = [&](const double *xx, double *yy) -> int {
         if (int rc = P(xx, tmp)) return rc;
         return A(tmp, yy);
@@ -898,7 +935,7 @@ int rmw_rollers_velocity_and_torque(const double *r, const double *force, const 
                     : rmw::nowall_product(kind, r, x, y, n, eta, a, L_host, mode, st);
     };
     double *rhs = nullptr;
-    RMW_CUDA(cudaMallocAsync(&rhs, sizeof(double) * 2 * m, st));
+    RMW_CUDA(rmw::dmalloc_async(&rhs, sizeof(double) * 2 * m, st));
     double *tmp = rhs + m;
     struct Free {
         double *p;

@@ -192,7 +192,7 @@ struct SegOps {
         njobs = (int)jb.size();
         const size_t bytes = sizeof(VecJob) * std::max(1, njobs) + sizeof(int) * (nseg + 1) + 64 +
                              sizeof(double) * ((size_t)std::max(1, njobs) * kSegChunk + (size_t)nseg * stride);
-        RMW_CUDA(cudaMallocAsync(&base, bytes + 256, st));
+        RMW_CUDA(rmw::dmalloc_async(&base, bytes + 256, st));
         char *p = (char *)base;
         jobs = (VecJob *)p;
         p += ((sizeof(VecJob) * std::max(1, njobs) + 15) / 16) * 16;
@@ -312,7 +312,7 @@ static int gmres_batched(Op op, Pc pc, PcOp pcop, const double *b, double *x_out
     SegOps O;
     if (int rc = O.init(off, stride, st)) return rc;
     double *buf = nullptr;
-    RMW_CUDA(cudaMallocAsync(&buf, sizeof(double) * ldv * (R + 6), st));
+    RMW_CUDA(rmw::dmalloc_async(&buf, sizeof(double) * ldv * (R + 6), st));
     struct Free {
         double *p;
         cudaStream_t s;
@@ -463,8 +463,8 @@ static int lanczos_batched(Op op, const double *z, double *noise, const std::vec
     if (int rc = O.init(off, stride, st)) return rc;
     int vcap = std::min(kcap + 1, 16);
     double *V = nullptr, *w = nullptr;
-    RMW_CUDA(cudaMallocAsync(&w, sizeof(double) * ldv, st));
-    RMW_CUDA(cudaMallocAsync(&V, sizeof(double) * ldv * vcap, st));
+    RMW_CUDA(rmw::dmalloc_async(&w, sizeof(double) * ldv, st));
+    RMW_CUDA(rmw::dmalloc_async(&V, sizeof(double) * ldv * vcap, st));
     struct Free {
         double **a, **b;
         cudaStream_t s;
@@ -544,7 +544,7 @@ static int lanczos_batched(Op op, const double *z, double *noise, const std::vec
         if (i + 2 > vcap) {
             const int ncap = std::min(kcap + 1, 2 * vcap);
             double *nv = nullptr;
-            RMW_CUDA(cudaMallocAsync(&nv, sizeof(double) * ldv * ncap, st));
+            RMW_CUDA(rmw::dmalloc_async(&nv, sizeof(double) * ldv * ncap, st));
             RMW_CUDA(cudaMemcpyAsync(nv, V, sizeof(double) * ldv * vcap, cudaMemcpyDeviceToDevice, st));
             RMW_CUDA(cudaFreeAsync(V, st));
             V = nv;
@@ -633,7 +633,7 @@ int rmw_rigid_solve_batched(void *sys, const double *rhs, double *sol, double to
     const long long n = S.sys_size();
     cudaStream_t st = S.st;
     double *buf = nullptr;
-    RMW_CUDA(cudaMallocAsync(&buf, sizeof(double) * n * 7, st));
+    RMW_CUDA(rmw::dmalloc_async(&buf, sizeof(double) * n * 7, st));
     double *gx = buf, *gy = buf + n, *bim = buf + 2 * n, *xim = buf + 3 * n, *rim = buf + 4 * n, *dim = buf + 5 * n;
     double *adim = buf + 6 * n;  // A32 d of the residual recurrence
     const unsigned pg = (unsigned)((n + 255) / 256);
@@ -799,7 +799,7 @@ int rmw_rigid_lanczos_batched(void *sys, const double *Z, double *noise, int nrh
         for (int k = 0; k < nsusp; ++k) off[(size_t)q * nsusp + k] = q * N3 + 3LL * S.batch->off[k];
     off[(size_t)nrhs * nsusp] = (long long)nrhs * N3;
     double *buf = nullptr;
-    RMW_CUDA(cudaMallocAsync(&buf, sizeof(double) * 2 * nrhs * N3, S.st));
+    RMW_CUDA(rmw::dmalloc_async(&buf, sizeof(double) * 2 * nrhs * N3, S.st));
     double *tmp = buf, *raw = buf + nrhs * N3;
     // mixed precision: the multi-vector product skips suspensions whose
     // segments of a pass of 8 right-hand sides have all converged (their rows
@@ -811,7 +811,7 @@ int rmw_rigid_lanczos_batched(void *sys, const double *Z, double *noise, int nrh
     static thread_local size_t h_cap = 0;
     const size_t nact = (size_t)npass * nsusp;
     if (mask) {
-        RMW_CUDA(cudaMallocAsync(&d_act, nact, S.st));
+        RMW_CUDA(rmw::dmalloc_async(&d_act, nact, S.st));
         if (h_cap < nact) {
             if (h_act) cudaFreeHost(h_act);
             RMW_CUDA(cudaHostAlloc(&h_act, nact, cudaHostAllocDefault));

@@ -699,22 +699,49 @@ bool krylov_device_available()
 // keep resident (registers, shared memory), at most 4
 static int kd_max_ctas()
 {
+    // per device, computed once
+    static std::atomic<int> cached[64];
     int dev = 0, sms = 1, a = 1, l = 1;
     if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    if (dev >= 0 && dev < 64)
+        if (const int c = cached[dev].load()) return c;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, arnoldi_step_kernel, kKdThreads, 0) != cudaSuccess) a = 1;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&l, lanczos_step_kernel, kKdThreads, 0) != cudaSuccess) l = 1;
     cudaGetLastError();
-    return sms * std::max(1, std::min(4, std::min(a, l)));
+    const int c = sms * std::max(1, std::min(4, std::min(a, l)));
+    if (dev >= 0 && dev < 64) cached[dev].store(c);
+    return c;
 }
 
 KrylovDev::~KrylovDev()
 {
     if (base) cudaFreeAsync(base, st);
     if (pinned) {
-        cudaStreamSynchronize(st);
-        cudaFreeHost(pinned);
+        cudaStreamSynchronize(st);  // no copy still uses the host block
+        pinned_give(pinned);
     }
+}
+
+// Copies the job tables to the device through the tail of the engine's pinned
+// block (truly asynchronous copies: a copy from pageable memory waits for the
+// stream first).
+static int kd_upload_jobs(char *hp, const std::vector<KJob> &jb, const std::vector<int> &sj,
+                          const std::vector<int> &bj, KJob *jobs, int *sjob, int *bjob, cudaStream_t st)
+{
+    const size_t b0 = sizeof(KJob) * jb.size(), b1 = sizeof(int) * sj.size(), b2 = sizeof(int) * bj.size();
+    if (b0) std::memcpy(hp, jb.data(), b0);
+    std::memcpy(hp + b0, sj.data(), b1);
+    std::memcpy(hp + b0 + b1, bj.data(), b2);
+    if (b0) RMW_CUDA(cudaMemcpyAsync(jobs, hp, b0, cudaMemcpyHostToDevice, st));
+    RMW_CUDA(cudaMemcpyAsync(sjob, hp + b0, b1, cudaMemcpyHostToDevice, st));
+    RMW_CUDA(cudaMemcpyAsync(bjob, hp + b0 + b1, b2, cudaMemcpyHostToDevice, st));
+    return RMW_OK;
+}
+
+static size_t kd_jobs_bytes(size_t njobs, size_t nseg, size_t nblk)
+{
+    return sizeof(KJob) * njobs + sizeof(int) * (nseg + 1) + sizeof(int) * (nblk + 1);
 }
 
 int kd_build_jobs(const std::vector<long long> &off, int nblk_max, std::vector<KJob> &jb, std::vector<int> &sj,
@@ -775,7 +802,7 @@ int KrylovDev::init(const std::vector<long long> &seg_off, int restart, int hist
                    2 * al(sizeof(double) * ns * R) + al(sizeof(double) * ns * (R + 1)) +
                    2 * al(sizeof(double) * ns * KP) + 4 * al(sizeof(double) * ns) + al(sizeof(double) * ns * KP) +
                    al(sizeof(double) * ns * std::max(1, hcap)) + 4 * al(sizeof(int) * ns) + al(sizeof(KState));
-    RMW_CUDA(cudaMallocAsync(&base, bytes, st));
+    RMW_CUDA(rmw::dmalloc_async(&base, bytes, st));
     char *p = (char *)base;
     auto take = [&](size_t b) {
         char *q = p;
@@ -813,19 +840,19 @@ int KrylovDev::init(const std::vector<long long> &seg_off, int restart, int hist
     cyc = iters + 2 * ns;
     flags = iters + 3 * ns;
     state = (KState *)take(sizeof(KState));
-    if (njobs) RMW_CUDA(cudaMemcpyAsync(jobs, jb.data(), sizeof(KJob) * njobs, cudaMemcpyHostToDevice, st));
-    RMW_CUDA(cudaMemcpyAsync(sjob, sj.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice, st));
-    RMW_CUDA(cudaMemcpyAsync(bjob, bj.data(), sizeof(int) * (nblk + 1), cudaMemcpyHostToDevice, st));
+    // pinned host scalars: alpha, beta, cycle flags, tolerances (ns doubles each), maxiter, the loop
+    // flag, the state, and four ns-int arrays (iters, jdone, cyc, flags) from 4 ns + 2 + 4 doubles on;
+    // then the job tables on their way to the device
+    const size_t scal = sizeof(double) * (8 * ns + 16);
+    void *hp = nullptr;
+    if (int rc = pinned_take(scal + kd_jobs_bytes(jb.size(), ns, nblk), &hp)) return rc;
+    pinned = (double *)hp;
+    if (int rc = kd_upload_jobs((char *)hp + scal, jb, sj, bj, jobs, sjob, bjob, st)) return rc;
     RMW_CUDA(cudaMemsetAsync(V, 0, sizeof(double) * (size_t)ldv * (R + 1), st));
     RMW_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * 6 * (size_t)ldv, st));
     RMW_CUDA(cudaMemsetAsync(iters, 0, sizeof(int) * ns, st));
     RMW_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * ns, st));
     RMW_CUDA(cudaMemsetAsync(state, 0, sizeof(KState), st));
-    // pinned host scalars: alpha, beta, cycle flags, tolerances (ns doubles each), maxiter, the loop
-    // flag, the state, and four ns-int arrays (iters, jdone, cyc, flags) from 4 ns + 2 + 4 doubles on
-    RMW_CUDA(cudaHostAlloc(&pinned, sizeof(double) * (8 * ns + 16), cudaHostAllocDefault));
-    // the copies above read host vectors that go out of scope
-    RMW_CUDA(cudaStreamSynchronize(st));
     return RMW_OK;
 }
 
@@ -835,8 +862,8 @@ LanczosDev::~LanczosDev()
     if (V) cudaFreeAsync(V, st);
     if (base) cudaFreeAsync(base, st);
     if (pinned) {
-        cudaStreamSynchronize(st);
-        cudaFreeHost(pinned);
+        cudaStreamSynchronize(st);  // no copy still uses the host block
+        pinned_give(pinned);
     }
 }
 
@@ -858,7 +885,7 @@ int LanczosDev::init(const std::vector<long long> &seg_off, int kcap_, cudaStrea
                          al(sizeof(int) * (nblk + 1)) + 3 * al(sizeof(double) * nj * KP) + al(sizeof(double) * ns) +
                          6 * al(sizeof(double) * ns * kc) + al(sizeof(double) * ns * kc * kc) +
                          4 * al(sizeof(int) * ns) + al(sizeof(LzState));
-    RMW_CUDA(cudaMallocAsync(&base, bytes, st));
+    RMW_CUDA(rmw::dmalloc_async(&base, bytes, st));
     char *p = (char *)base;
     auto take = [&](size_t b) {
         char *q = p;
@@ -886,16 +913,15 @@ int LanczosDev::init(const std::vector<long long> &seg_off, int kcap_, cudaStrea
     kfin = (int *)take(sizeof(int) * ns);
     flags = (int *)take(sizeof(int) * ns);
     state = (LzState *)take(sizeof(LzState));
-    if (njobs) RMW_CUDA(cudaMemcpyAsync(jobs, jb.data(), sizeof(KJob) * njobs, cudaMemcpyHostToDevice, st));
-    RMW_CUDA(cudaMemcpyAsync(sjob, sj.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice, st));
-    RMW_CUDA(cudaMemcpyAsync(bjob, bj.data(), sizeof(int) * (nblk + 1), cudaMemcpyHostToDevice, st));
+    // pinned host scalars (2 ns + 16 doubles, four ns-int arrays, the state), then the job tables
+    const size_t scal = sizeof(double) * (2 * ns + 16) + sizeof(int) * 4 * ns + sizeof(LzState);
+    const size_t scal_al = (scal + 15) / 16 * 16;
+    if (int rc = pinned_take(scal_al + kd_jobs_bytes(jb.size(), ns, nblk), &pinned)) return rc;
+    if (int rc = kd_upload_jobs((char *)pinned + scal_al, jb, sj, bj, jobs, sjob, bjob, st)) return rc;
     RMW_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * 2 * ldv, st));
     RMW_CUDA(cudaMemsetAsync(state, 0, sizeof(LzState), st));
     RMW_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * ns, st));
     RMW_CUDA(cudaMemsetAsync(c, 0, sizeof(double) * ns * kc, st));
-    RMW_CUDA(cudaHostAlloc(&pinned, sizeof(double) * (2 * ns + 16) + sizeof(int) * 4 * ns + sizeof(LzState),
-                           cudaHostAllocDefault));
-    RMW_CUDA(cudaStreamSynchronize(st));
     return grow(std::min(kcap + 1, 32));
 }
 
@@ -904,7 +930,7 @@ int LanczosDev::grow(int want)
     want = std::min(want, kcap + 1);
     if (want <= vcap) return RMW_OK;
     double *nv = nullptr;
-    RMW_CUDA(cudaMallocAsync(&nv, sizeof(double) * (size_t)ldv * want, st));
+    RMW_CUDA(rmw::dmalloc_async(&nv, sizeof(double) * (size_t)ldv * want, st));
     if (V) {
         RMW_CUDA(cudaMemcpyAsync(nv, V, sizeof(double) * (size_t)ldv * vcap, cudaMemcpyDeviceToDevice, st));
         RMW_CUDA(cudaFreeAsync(V, st));

@@ -360,7 +360,7 @@ int mp_work_create(MpWork **out, int nodes, int mp, int band, cudaStream_t st)
     bytes += al(hb * B * kw) + 2 * al(hb * B * kMpW) + 2 * al(fb * B * kMpW) + al(fb * B * kMpOut);
     bytes += al(fb * B * kMpOut) + al(fb * rows * kw) + 2 * al(fb * rows * kw) + 2 * al(fb * N * kMpW) +
              al(fb * (B * kMpOut / 256 + 2)) + al(fb * 4) + al(hb * rows * kw);
-    if (cudaMallocAsync(&W->base, bytes, st) != cudaSuccess) {
+    if (rmw::dmalloc_async(&W->base, bytes, st) != cudaSuccess) {
         delete W;
         return fail(RMW_ERR_ALLOC, "message-passing network workspace");
     }
@@ -489,7 +489,12 @@ static int mp_backward(MpnnNet &net, const MpGraph &g, MpWork &W, float *gW, flo
     dense_back(net, r0, W.Xr, B, W.dZ, W, gW, gb, W.dX, st);
     mp_readout_scatter_kernel<<<blocks((long long)N * kMpW, 256), 256, 0, st>>>(W.dX, g.band_off, g.band_rev,
                                                                                  g.n_nodes, W.dh);
-    if (N > g.n_nodes) cudaMemsetAsync(W.dh + (long long)g.n_nodes * kMpW, 0, sizeof(float) * (N - g.n_nodes) * kMpW, st);
+    // the padding rows of both node-gradient buffers are zero (the node kernels write the real rows only;
+    // the weight-gradient GEMMs sum over every row)
+    if (N > g.n_nodes) {
+        cudaMemsetAsync(W.dh + (long long)g.n_nodes * kMpW, 0, sizeof(float) * (N - g.n_nodes) * kMpW, st);
+        cudaMemsetAsync(W.dh2 + (long long)g.n_nodes * kMpW, 0, sizeof(float) * (N - g.n_nodes) * kMpW, st);
+    }
     // message-passing steps, last first
     for (int t = kMpSteps - 1; t >= 0; --t) {
         // h_{t+1} = h_t + silu(Zu): dZu = dh * silu'(Zu)
@@ -789,7 +794,7 @@ int rmw_nearfield_train(void *net, const rmw_graph *graphs, int n_graphs, int st
     rmw::MpWork *W = nullptr;
     if (int rc = rmw::mp_work_create(&W, maxn, maxe, maxb, st)) return rc;
     float *buf = nullptr;
-    if (cudaMallocAsync((void **)&buf, sizeof(float) * (rmw::kMpNW + rmw::kMpNB + steps), st) != cudaSuccess) {
+    if (rmw::dmalloc_async((void **)&buf, sizeof(float) * (rmw::kMpNW + rmw::kMpNB + steps), st) != cudaSuccess) {
         rmw::mp_work_destroy(W);
         return rmw::fail(RMW_ERR_ALLOC, "training buffers");
     }

@@ -1154,7 +1154,7 @@ static int learned_couplings(RigidSystem &S, MpnnNet &N)
     const size_t bytes = al(sizeof(float) * 2 * nb) + al(sizeof(int) * std::max(nm, 1)) +
                          al(sizeof(float) * 3 * std::max(nm, 1)) + al(sizeof(int) * np) + al(sizeof(float) * 3 * np);
     void *buf = nullptr;
-    RMW_CUDA(cudaMallocAsync(&buf, bytes, st));
+    RMW_CUDA(rmw::dmalloc_async(&buf, bytes, st));
     char *p = (char *)buf;
     float *node = (float *)p;
     p += al(sizeof(float) * 2 * nb);

@@ -29,7 +29,7 @@ static int run_probe(int iters, double *flops_per_s, cudaStream_t st)
     RMW_CUDA(cudaGetDevice(&dev));
     RMW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     T *sink = nullptr;
-    RMW_CUDA(cudaMallocAsync((void **)&sink, sizeof(T), st));
+    RMW_CUDA(rmw::dmalloc_async((void **)&sink, sizeof(T), st));
     const int blocks = sms * 8, threads = 256;
     cudaEvent_t e0, e1;
     RMW_CUDA(cudaEventCreate(&e0));

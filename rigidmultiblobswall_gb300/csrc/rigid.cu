@@ -790,7 +790,7 @@ static int build_pc(RigidSystem &S, bool stochastic, bool fp32 = false)
     // working copy of the dense body mobilities (stream-ordered, freed below)
     void *ws = nullptr;
     const size_t ws_bytes = sizeof(double) * ((size_t)tot + 3 * (size_t)S.n);
-    RMW_CUDA(cudaMallocAsync(&ws, ws_bytes, st));
+    RMW_CUDA(rmw::dmalloc_async(&ws, ws_bytes, st));
     double *M = (double *)ws;
     double *tmpg = M + tot;
     if (!S.minv) {
@@ -1042,6 +1042,10 @@ int rmw_rigid_create(void **out, int64_t n_bodies, const int64_t *blob_offsets_h
         for (int k = 0; k < 3; ++k) S->L[k] = L_host[k];
     S->st = rmw::as_stream(stream);
     cudaGetDevice(&S->device);
+    if (int rc = rmw::pool_retain()) {
+        delete S;
+        return rc;
+    }
     S->boff_h.resize(S->nb + 1);
     S->moff_h.resize(S->nb + 1);
     S->moff_h[0] = 0;
@@ -1239,7 +1243,7 @@ int rmw_count_below(const double *r, int64_t n, double zmin, int *count_host, vo
     *count_host = 0;
     if (n == 0) return RMW_OK;
     int *d = nullptr;
-    RMW_CUDA(cudaMallocAsync(&d, sizeof(int), st));
+    RMW_CUDA(rmw::dmalloc_async(&d, sizeof(int), st));
     RMW_CUDA(cudaMemsetAsync(d, 0, sizeof(int), st));
     rmw::count_below_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(r, (int)n, zmin, d);
     RMW_CHECK_LAUNCH("count below");

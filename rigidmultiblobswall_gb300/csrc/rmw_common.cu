@@ -1,4 +1,6 @@
 // Error reporting and per-device scratch of the rmw_gb300 library.
+#include <algorithm>
+#include <cstdlib>
 #include <cstdio>
 #include <atomic>
 #include <mutex>
@@ -62,6 +64,89 @@ void graph_live(int delta)
 
 // cap on one scratch buffer (rmw_set_scratch_limit); 0 = no cap
 static std::atomic<size_t> g_scratch_limit{0};
+
+static std::mutex g_pool_mu;
+static std::vector<int> g_pool_devices;  // devices whose default pool retains memory
+
+cudaError_t dmalloc_async(void **p, size_t bytes, cudaStream_t st)
+{
+    static const bool poison = [] {
+        const char *v = std::getenv("RMW_POISON_ALLOC");
+        return v && *v && *v != '0';
+    }();
+    const cudaError_t e = cudaMallocAsync(p, bytes, st);
+    if (e != cudaSuccess || !poison || bytes == 0) return e;
+    return cudaMemsetAsync(*p, 0xFF, bytes, st);
+}
+
+namespace {
+struct PinnedBlock {
+    void *p;
+    size_t bytes;
+};
+std::mutex g_pinned_mu;
+std::vector<PinnedBlock> g_pinned_free;               // blocks ready for reuse
+std::map<void *, size_t> g_pinned_size;               // every block handed out, with its size
+constexpr size_t kPinnedCached = 32;                  // free blocks kept at most
+}  // namespace
+
+int pinned_take(size_t bytes, void **p)
+{
+    *p = nullptr;
+    std::lock_guard<std::mutex> lock(g_pinned_mu);
+    int best = -1;
+    for (int k = 0; k < (int)g_pinned_free.size(); ++k)
+        if (g_pinned_free[k].bytes >= bytes && (best < 0 || g_pinned_free[k].bytes < g_pinned_free[best].bytes))
+            best = k;
+    if (best >= 0) {
+        *p = g_pinned_free[best].p;
+        g_pinned_free.erase(g_pinned_free.begin() + best);
+        return RMW_OK;
+    }
+    const size_t want = (std::max<size_t>(bytes, 1) + 4095) / 4096 * 4096;
+    RMW_CUDA(cudaHostAlloc(p, want, cudaHostAllocDefault));
+    g_pinned_size[*p] = want;
+    return RMW_OK;
+}
+
+void pinned_give(void *p)
+{
+    if (!p) return;
+    std::lock_guard<std::mutex> lock(g_pinned_mu);
+    auto it = g_pinned_size.find(p);
+    if (it == g_pinned_size.end()) return;
+    if (g_pinned_free.size() >= kPinnedCached) {
+        // drop the smallest cached block
+        int small = 0;
+        for (int k = 1; k < (int)g_pinned_free.size(); ++k)
+            if (g_pinned_free[k].bytes < g_pinned_free[small].bytes) small = k;
+        if (g_pinned_free[small].bytes < it->second) {
+            cudaFreeHost(g_pinned_free[small].p);
+            g_pinned_size.erase(g_pinned_free[small].p);
+            g_pinned_free[small] = {p, it->second};
+        } else {
+            cudaFreeHost(p);
+            g_pinned_size.erase(it);
+        }
+        return;
+    }
+    g_pinned_free.push_back({p, it->second});
+}
+
+int pool_retain()
+{
+    int dev = 0;
+    RMW_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    for (int d : g_pool_devices)
+        if (d == dev) return RMW_OK;
+    cudaMemPool_t pool;
+    RMW_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    unsigned long long keep = 1ULL << 30;
+    RMW_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    g_pool_devices.push_back(dev);
+    return RMW_OK;
+}
 
 int scratch(ScratchSlot slot, size_t bytes, void **ptr, cudaStream_t st)
 {

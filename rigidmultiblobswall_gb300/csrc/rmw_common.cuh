@@ -38,6 +38,32 @@ int scratch_release_all();
 void scratch_set_limit(size_t bytes);
 size_t scratch_limit();
 
+// Keeps up to 1 GiB of freed stream-ordered allocations (cudaMallocAsync) in
+// the current device's default pool across synchronisations, once per device.
+// The solves allocate and free their work vectors on every call; with the
+// pool's default release threshold of 0 each synchronisation hands that memory
+// back to the driver and the next call maps it again.  The setting belongs to
+// this process's context and ends with it.
+int pool_retain();
+
+// cudaMallocAsync.  With the environment variable RMW_POISON_ALLOC set, the new
+// memory is filled with 0xFF bytes on the same stream (NaN in every
+// floating-point type, -1 in every integer type), so that a kernel reading
+// memory nothing wrote shows in its results: a debug aid for the test suite.
+cudaError_t dmalloc_async(void **p, size_t bytes, cudaStream_t st);
+template <typename T>
+cudaError_t dmalloc_async(T **p, size_t bytes, cudaStream_t st)
+{
+    return dmalloc_async((void **)p, bytes, st);
+}
+
+// Page-locked host blocks reused across calls: cudaHostAlloc and cudaFreeHost
+// cost tens of microseconds each, and cudaFreeHost waits for the device.
+// pinned_take hands out a block of at least `bytes` (a cached one when one is
+// large enough); pinned_give returns it for reuse once no copy uses it.
+int pinned_take(size_t bytes, void **p);
+void pinned_give(void *p);
+
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // ---- kernel tracing -------------------------------------------------------

@@ -14,12 +14,19 @@ def mobility_rhs(sys_, force_torque, slip=None, noise=None):
     """RHS = [slip - noise; -F/T] (quaternion_integrator_multi_bodies.py:1476-1489)."""
     import torch
     n3 = 3 * sys_.n_blobs
-    rhs = torch.zeros(sys_.size, dtype=torch.float64, device=sys_.device)
-    if slip is not None:
-        rhs[:n3] = torch.as_tensor(slip, dtype=torch.float64, device=sys_.device).reshape(-1)
-    if noise is not None:
-        rhs[:n3] -= torch.as_tensor(noise, dtype=torch.float64, device=sys_.device).reshape(-1)
-    rhs[n3:] = -torch.as_tensor(force_torque, dtype=torch.float64, device=sys_.device).reshape(-1)
+    dev = sys_.device
+    rhs = torch.empty(sys_.size, dtype=torch.float64, device=dev)
+    top = rhs[:n3]
+    as_dev = lambda v: torch.as_tensor(v, dtype=torch.float64, device=dev).reshape(-1)
+    if slip is None and noise is None:
+        top.zero_()
+    elif noise is None:
+        top.copy_(as_dev(slip))
+    elif slip is None:
+        torch.neg(as_dev(noise), out=top)
+    else:
+        torch.sub(as_dev(slip), as_dev(noise), out=top)
+    torch.neg(as_dev(force_torque), out=rhs[n3:])
     return rhs
 
 
@@ -45,12 +52,9 @@ def solve_mobility_problem(sys_, force_torque, slip=None, noise=None, tol=1e-8, 
             return torch.zeros(sys_.size, dtype=torch.float64, device=sys_.device), 0, 0, 0.0
         sol, info, its, rr = sys_.solve(rhs / nrm, tol=tol, restart=restart, maxiter=maxiter, mode=mode)
         return sol.mul_(nrm), info, its, rr
+    # device inputs: |b|, the scaling and the scaling back run in the library (one synchronisation)
     rhs = mobility_rhs(sys_, force_torque, slip, noise)
-    nrm = float(rhs.norm())
-    if nrm == 0.0:
-        return rhs.clone(), 0, 0, 0.0
-    sol, info, its, rr = sys_.solve(rhs / nrm, tol=tol, restart=restart, maxiter=maxiter, mode=mode)
-    return sol * nrm, info, its, rr
+    return sys_.solve(rhs, tol=tol, restart=restart, maxiter=maxiter, mode=mode, scaled=True)
 
 
 class BrownianStepper:
@@ -298,13 +302,11 @@ class QuaternionIntegrator:
             RHS = RHS.clone()
         if noise is not None:
             RHS[:n3] -= noise
-        nrm = float(RHS.norm())
-        if nrm == 0.0:
-            return torch.zeros_like(RHS)
-        sol, _, its, _ = S.solve(RHS / nrm, tol=self.tolerance, restart=self.restart, maxiter=self.maxiter,
-                                 mode=self.mode)
+        # the library scales to norm 1 and back (a zero RHS gives a zero solution)
+        sol, _, its, _ = S.solve(RHS, tol=self.tolerance, restart=self.restart, maxiter=self.maxiter,
+                                 mode=self.mode, scaled=True)
         self.det_iterations_count += its
-        return sol * nrm
+        return sol
 
     def _lanczos(self, S, factor, z=None):
         """stochastic_forcing_lanczos with the block-diagonal factors of S

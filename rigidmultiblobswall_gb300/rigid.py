@@ -232,17 +232,20 @@ class RigidSystem:
         return out, it.reshape(nrhs, self.n_suspensions)
 
     # -- solvers -----------------------------------------------------------------
-    def solve(self, rhs, tol=1e-8, restart=60, maxiter=1000, mode="fp64", raise_on_fail=False):
+    def solve(self, rhs, tol=1e-8, restart=60, maxiter=1000, mode="fp64", raise_on_fail=False, scaled=False):
         """GMRES with the block-diagonal preconditioner.  Returns (solution, info, iterations, rel_residual);
-        info = 0 on convergence, else the iteration count (the reference's convention)."""
+        info = 0 on convergence, else the iteration count (the reference's convention).  scaled: solve
+        for rhs / |rhs| and scale the solution back by |rhs| on the device (solve_mobility_problem's
+        normalisation)."""
         import torch
         b = _dev(rhs, self.device).reshape(-1)
         x = self._out(self.size)
         it = ctypes.c_int(0)
         rr = ctypes.c_double(0.0)
+        fn = _native.load().rmw_rigid_solve_scaled if scaled else _native.load().rmw_rigid_solve
         with torch.cuda.device(self.device):
-            rc = _native.load().rmw_rigid_solve(self._h, b.data_ptr(), x.data_ptr(), float(tol), int(restart),
-                                                int(maxiter), _mode(mode), ctypes.byref(it), ctypes.byref(rr))
+            rc = fn(self._h, b.data_ptr(), x.data_ptr(), float(tol), int(restart), int(maxiter), _mode(mode),
+                    ctypes.byref(it), ctypes.byref(rr))
         if rc == _native.RMW_ERR_NOT_CONVERGED and not raise_on_fail:
             return x, it.value, it.value, rr.value
         _native.check(rc)

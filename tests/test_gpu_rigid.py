@@ -85,6 +85,33 @@ def test_solve_matches_reference(cuda_device, c, mode):
     assert np.linalg.norm(rhs - o.apply(sol)) <= 1.05e-8 * np.linalg.norm(rhs)
 
 
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_scaled_solve_of_device_inputs(cuda_device, mode):
+    """Device inputs take rmw_rigid_solve_scaled (|b|, b / |b| and the scaling back in the library): the
+    same solution as the host path, which scales on the host; zero and unconverged cases keep the
+    reference's return convention."""
+    import torch
+    g = golden("rigid.npz")
+    s = gpu_system(g, "s42")
+    ft = torch.as_tensor(g["s42_FT"], device="cuda")
+    noise = torch.randn(3 * s.n_blobs, dtype=torch.float64, device="cuda", generator=torch.Generator(
+        device="cuda").manual_seed(5)) * 1e-2
+    x_dev, info, its, rr = integrator.solve_mobility_problem(s, ft, noise=noise, tol=1e-8, mode=mode)
+    x_host, info_h, its_h, rr_h = integrator.solve_mobility_problem(s, g["s42_FT"], noise=noise.cpu().numpy(),
+                                                                     tol=1e-8, mode=mode)
+    assert info == 0 and info_h == 0 and abs(its - its_h) <= 1 and rr <= 1e-8
+    assert rel_err(x_dev.cpu().numpy(), x_host.cpu().numpy()) <= 1e-10
+    o = orc.Rigid(g["s42_r"], g["s42_locs"], s.offsets, s.eta, s.a)
+    n3 = 3 * s.n_blobs
+    rhs = np.concatenate([-noise.cpu().numpy(), -g["s42_FT"].flatten()])
+    assert np.linalg.norm(rhs - o.apply(x_dev.cpu().numpy())) <= 1.05e-8 * np.linalg.norm(rhs)
+    z, info, its, rr = integrator.solve_mobility_problem(s, torch.zeros_like(ft), mode=mode)
+    assert info == 0 and its == 0 and float(z.abs().max()) == 0.0
+    b = torch.as_tensor(np.random.default_rng(0).standard_normal(s.size), device="cuda")
+    x, info, its, rr = s.solve(b, tol=1e-14, maxiter=1, scaled=True)
+    assert info == 1 and its == 1 and rr > 1e-14 and bool(torch.isfinite(x).all())
+
+
 @pytest.mark.parametrize("c", CASES)
 def test_lanczos_and_em_step_match_reference(cuda_device, c):
     g = golden("rigid.npz")

@@ -21,6 +21,8 @@ def _mode(mode):
 
 def _dev(x, device):
     import torch
+    if type(x) is torch.Tensor and x.dtype == torch.float64 and x.device == device and x.is_contiguous():
+        return x  # already a contiguous float64 tensor on the suspension's device
     t = torch.as_tensor(x, dtype=torch.float64, device=device)
     return t.contiguous()
 

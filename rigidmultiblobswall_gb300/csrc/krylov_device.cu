@@ -684,15 +684,20 @@ bool krylov_device_enabled() { return g_device_krylov.load(); }
 
 bool krylov_device_available()
 {
+    // per device, determined once: 1 available, 2 not
+    static std::atomic<int> known[64];
     int dev = 0, coop = 0, nb = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
-    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return false;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, arnoldi_step_kernel, kKdThreads, 0) != cudaSuccess ||
-        nb < 1) {
+    if (dev >= 0 && dev < 64)
+        if (const int k = known[dev].load()) return k == 1;
+    bool ok = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess && coop;
+    if (ok && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, arnoldi_step_kernel, kKdThreads, 0) != cudaSuccess ||
+               nb < 1)) {
         cudaGetLastError();
-        return false;
+        ok = false;
     }
-    return true;
+    if (dev >= 0 && dev < 64) known[dev].store(ok ? 1 : 2);
+    return ok;
 }
 
 // CTAs the cooperative step kernels may use: as many per SM as both kernels

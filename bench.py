@@ -538,13 +538,16 @@ def solver_metrics(dev, reps=2):
     vel = {}
     R3 = float(np.linalg.norm(s3.shell[0]))
     model12, out["nearfield_training_shells12"] = train_nearfield(s3.shell, s3.a, (1.1 * R3, 5 * R3), dev)
-    for mode in ("fp64", "mixed", "mixed_nearfield"):
+    # mixed_nearfield: exact couplings below 3R, learned ones from 3R to 6R; mixed_exact: the exact part
+    # alone; mixed_learned: learned couplings for every pair below 6R (no exact part)
+    arms3 = {"fp64": None, "mixed": None, "mixed_nearfield": (model12, 3 * R3), "mixed_exact": (None, 3 * R3),
+             "mixed_learned": (model12, 0.0)}
+    for mode, nfa in arms3.items():
         best = None
         for _ in range(reps):
             st = integrator.BrownianStepper(sys3, s3.locations, s3.quaternions,
                                             np.tile(s3.shell, (s3.n_bodies, 1)), kT=1.0,
-                                            mode=mode.split("_")[0],
-                                            nearfield=(model12, 3 * R3) if "nearfield" in mode else None)
+                                            mode=mode.split("_")[0], nearfield=nfa)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             res = st.step(1e-3, FT3, z=z)
@@ -555,13 +558,15 @@ def solver_metrics(dev, reps=2):
         out["bd_step_shells12x1024_%s" % mode] = {"ms": best * 1e3, "lanczos_iterations": res["lanczos_iterations"],
                                                   "gmres_iterations": res["gmres_iterations"],
                                                   "relres_fp64": res["relres"]}
-    for mode in ("mixed", "mixed_nearfield"):
+    for mode in ("mixed", "mixed_nearfield", "mixed_exact", "mixed_learned"):
         out["bd_step_shells12x1024_" + mode]["velocity_rel_err_vs_fp64"] = float(
             np.linalg.norm(vel[mode] - vel["fp64"]) / np.linalg.norm(vel["fp64"]))
     out["bd_step_ms_learned_vs_blockdiag"] = {
         "block_diag_fp64": out["bd_step_shells12x1024_fp64"]["ms"],
         "block_diag_mixed": out["bd_step_shells12x1024_mixed"]["ms"],
-        "learned_mixed": out["bd_step_shells12x1024_mixed_nearfield"]["ms"]}
+        "learned_mixed": out["bd_step_shells12x1024_mixed_nearfield"]["ms"],
+        "exact_only_mixed": out["bd_step_shells12x1024_mixed_exact"]["ms"],
+        "learned_only_mixed": out["bd_step_shells12x1024_mixed_learned"]["ms"]}
     # every time integrator, one step of 1024 shells x 12 blobs (mixed precision,
     # GMRES and Lanczos tolerance 1e-8, force (0,0,-1) per body, kT = 1, dt = 1e-3)
     FT3t = torch.as_tensor(FT3, device=dev).reshape(-1, 3)

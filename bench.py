@@ -35,6 +35,13 @@ FLOPS_PER_PAIR = {"uf": 200.0, "ut": 115.0, "wf": 115.0, "wt": 125.0}  # counted
 METRIC = "wall-RPY M.F Gpairs/s"
 HEAD_MODE = "df64"
 WORKLOAD = "wall-RPY M_UF.F, 256 shells x 42 blobs = 10,752 blobs (FP64-accurate: df64, <= 1e-12 vs FP64)"
+# Split of the near-field augmented preconditioner, in body radii R: exact blob-level couplings below
+# NF_EXACT_R, learned mode couplings from there to the network's cutoff (6R).  A sweep of the 256-, 1024-
+# and 4096-shell mixed solves over exact cutoffs 3R, 4.5R and 6R, each with and without the learned band,
+# gave the fewest iterations and the shortest solves at 4.5R with the band; NF_ALL_EXACT_R is the
+# comparison arm with exact couplings of every pair the network would cover.
+NF_EXACT_R = 4.5
+NF_ALL_EXACT_R = 6.0
 # Issued thread instructions per ordered pair of the df64 UF kernels (all
 # pipes, 80-85 % of them on the FMA pipe), from ncu's smsp__inst_executed.sum
 # on the 10,752-blob product: symmetric kernel (each unordered pair once),
@@ -86,7 +93,7 @@ def parse():
     p.add_argument("--large", action="store_true",
                    help="only run the 4096-shell (172,032-blob) solve comparison and print its JSON line")
     p.add_argument("--large-modes",
-                   default="fp64,mixed,mixed+exact,mixed+learned,mixed+learned_band,mixed+exact+learned")
+                   default="fp64,mixed,mixed+exact,mixed+learned,mixed+learned_band,mixed+exact+learned,mixed+exact_all")
     p.add_argument("--pc-probe", action="store_true",
                    help="only the 4096-shell block-diagonal preconditioner applies (FP64 and FP32), timed")
     p.add_argument("--krylov-probe", action="store_true",
@@ -473,7 +480,7 @@ def solver_metrics(dev, reps=2):
         best = dt if best is None else min(best, dt)
     _native.use_graphs(True)
     out["solve_shells42x256_mixed_without_graphs"] = {"ms": best * 1e3, "iterations": its_ng}
-    # near-field augmented preconditioner: exact pairs < 3R, learned 3R..6R
+    # near-field augmented preconditioner: exact pairs below NF_EXACT_R body radii, learned beyond
     from rigidmultiblobswall_gb300 import nearfield as nf
     R2 = float(np.linalg.norm(s2.shell[0]))
     model42, out["nearfield_training_shells42"] = train_nearfield(s2.shell, s2.a, (1.1 * R2, 5 * R2), dev)
@@ -483,7 +490,7 @@ def solver_metrics(dev, reps=2):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             sys2.build_pc(mode=mode)
-            pairs = model42.attach(sys2, exact_cutoff=3 * R2)
+            pairs = model42.attach(sys2, exact_cutoff=NF_EXACT_R * R2)
             sol, info, its, rr = integrator.solve_mobility_problem(sys2, FT, tol=1e-8, mode=mode)
             torch.cuda.synchronize()
             dt = time.perf_counter() - t0
@@ -538,10 +545,12 @@ def solver_metrics(dev, reps=2):
     vel = {}
     R3 = float(np.linalg.norm(s3.shell[0]))
     model12, out["nearfield_training_shells12"] = train_nearfield(s3.shell, s3.a, (1.1 * R3, 5 * R3), dev)
-    # mixed_nearfield: exact couplings below 3R, learned ones from 3R to 6R; mixed_exact: the exact part
-    # alone; mixed_learned: learned couplings for every pair below 6R (no exact part)
-    arms3 = {"fp64": None, "mixed": None, "mixed_nearfield": (model12, 3 * R3), "mixed_exact": (None, 3 * R3),
-             "mixed_learned": (model12, 0.0)}
+    # mixed_nearfield: exact couplings below NF_EXACT_R, learned ones from there to 6R; mixed_exact: the
+    # exact part alone; mixed_learned: learned couplings for every pair below 6R (no exact part);
+    # mixed_exact_all: exact couplings for every pair below 6R (no network)
+    arms3 = {"fp64": None, "mixed": None, "mixed_nearfield": (model12, NF_EXACT_R * R3),
+             "mixed_exact": (None, NF_EXACT_R * R3), "mixed_learned": (model12, 0.0),
+             "mixed_exact_all": (None, NF_ALL_EXACT_R * R3)}
     for mode, nfa in arms3.items():
         best = None
         for _ in range(reps):
@@ -558,7 +567,7 @@ def solver_metrics(dev, reps=2):
         out["bd_step_shells12x1024_%s" % mode] = {"ms": best * 1e3, "lanczos_iterations": res["lanczos_iterations"],
                                                   "gmres_iterations": res["gmres_iterations"],
                                                   "relres_fp64": res["relres"]}
-    for mode in ("mixed", "mixed_nearfield", "mixed_exact", "mixed_learned"):
+    for mode in ("mixed", "mixed_nearfield", "mixed_exact", "mixed_learned", "mixed_exact_all"):
         out["bd_step_shells12x1024_" + mode]["velocity_rel_err_vs_fp64"] = float(
             np.linalg.norm(vel[mode] - vel["fp64"]) / np.linalg.norm(vel["fp64"]))
     out["bd_step_ms_learned_vs_blockdiag"] = {
@@ -566,7 +575,8 @@ def solver_metrics(dev, reps=2):
         "block_diag_mixed": out["bd_step_shells12x1024_mixed"]["ms"],
         "learned_mixed": out["bd_step_shells12x1024_mixed_nearfield"]["ms"],
         "exact_only_mixed": out["bd_step_shells12x1024_mixed_exact"]["ms"],
-        "learned_only_mixed": out["bd_step_shells12x1024_mixed_learned"]["ms"]}
+        "learned_only_mixed": out["bd_step_shells12x1024_mixed_learned"]["ms"],
+        "exact_below_6R_mixed": out["bd_step_shells12x1024_mixed_exact_all"]["ms"]}
     # every time integrator, one step of 1024 shells x 12 blobs (mixed precision,
     # GMRES and Lanczos tolerance 1e-8, force (0,0,-1) per body, kT = 1, dt = 1e-3)
     FT3t = torch.as_tensor(FT3, device=dev).reshape(-1, 3)
@@ -663,12 +673,14 @@ def oracle_residual_sampled(r, locs, offsets, eta, a, sol, FT, n_rows=1024, seed
 
 
 def cfg5_metrics(dev, modes=("fp64", "mixed", "mixed+exact", "mixed+learned", "mixed+learned_band",
-                             "mixed+exact+learned")):
+                             "mixed+exact+learned", "mixed+exact_all")):
     """4096 42-blob shells at area fraction 0.3, force (0,0,-1) per body: preconditioned GMRES to a 1e-8
     relative residual, on one GPU.  Arms: plain block-diagonal FP64 (the baseline), mixed precision, and
-    mixed precision with the near-field augmented preconditioner - exact blob-level couplings below 3R
-    only ("exact"), learned mode couplings of every pair below 6R ("learned"), of the outer band 3R..6R
-    only ("learned_band"), and exact below 3R with learned from 3R to 6R ("exact+learned").  Each arm's time covers its preconditioner build (FP64 or FP32), the near-field
+    mixed precision with the near-field augmented preconditioner - exact blob-level couplings below
+    NF_EXACT_R only ("exact"), learned mode couplings of every pair below 6R ("learned"), of the outer
+    band NF_EXACT_R..6R only ("learned_band"), exact below NF_EXACT_R with learned from there to 6R
+    ("exact+learned"), and exact couplings of every pair below 6R without the network ("exact_all").
+    Each arm's time covers its preconditioner build (FP64 or FP32), the near-field
     attach and the solve; the network is trained once before (time reported).  Every solution's relative
     residual is also estimated by the oracle (all body rows, 1024 sampled blob rows)."""
     import torch
@@ -684,7 +696,8 @@ def cfg5_metrics(dev, modes=("fp64", "mixed", "mixed+exact", "mixed+learned", "m
     FT[:, 2] = -1.0
     R5 = float(np.linalg.norm(s5.shell[0]))
     out = {"workload": "4096 shells x 42 blobs = 172,032 blobs, area fraction 0.3, z in [1.1R, 3R], F=(0,0,-1)",
-           "tol": 1e-8, "restart": 60, "exact_cutoff": "3R", "learned_band": "3R..6R", "message_cutoff": "3R"}
+           "tol": 1e-8, "restart": 60, "exact_cutoff": "%gR" % NF_EXACT_R, "learned_band": "%gR..6R" % NF_EXACT_R,
+           "message_cutoff": "3R"}
     model = None
     if any("learned" in m for m in modes):
         model, out["nearfield_training"] = train_nearfield(s5.shell, s5.a, (1.1 * R5, 3 * R5), dev)
@@ -693,6 +706,7 @@ def cfg5_metrics(dev, modes=("fp64", "mixed", "mixed+exact", "mixed+learned", "m
         parts = mode.split("+")
         base = parts[0]
         exact = "exact" in parts
+        exact_all = "exact_all" in parts
         band_only = "learned_band" in parts
         learned = band_only or "learned" in parts
         torch.cuda.synchronize()
@@ -700,10 +714,10 @@ def cfg5_metrics(dev, modes=("fp64", "mixed", "mixed+exact", "mixed+learned", "m
         sys5.build_pc(mode="mixed" if base == "mixed" else base)
         pairs = None
         if learned:
-            pairs = model.attach(sys5, exact_cutoff=3 * R5 if exact else 0.0,
-                                 learned_from=3 * R5 if band_only else 0.0)
-        elif exact:
-            pairs = nf.attach_exact(sys5, 3 * R5)
+            pairs = model.attach(sys5, exact_cutoff=NF_EXACT_R * R5 if exact else 0.0,
+                                 learned_from=NF_EXACT_R * R5 if band_only else 0.0)
+        elif exact or exact_all:
+            pairs = nf.attach_exact(sys5, (NF_ALL_EXACT_R if exact_all else NF_EXACT_R) * R5)
         sol, info, its, rr = integrator.solve_mobility_problem(sys5, FT, tol=1e-8, mode=base)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
@@ -730,7 +744,7 @@ def cfg5_metrics(dev, modes=("fp64", "mixed", "mixed+exact", "mixed+learned", "m
             if mode != "fp64":
                 out["speedup_%s_vs_fp64" % mode] = out["fp64"]["ms"] / out[mode]["ms"]
     for m1, m2 in (("mixed+exact+learned", "mixed+exact"), ("mixed+learned", "mixed"),
-                   ("mixed+learned_band", "mixed")):
+                   ("mixed+learned_band", "mixed"), ("mixed+exact+learned", "mixed+exact_all")):
         if m1 in out and m2 in out:
             out["gain_%s_over_%s" % (m1, m2)] = {"ms_ratio": out[m2]["ms"] / out[m1]["ms"],
                                                  "iterations": [out[m2]["iterations"], out[m1]["iterations"]]}

@@ -36,12 +36,13 @@ METRIC = "wall-RPY M.F Gpairs/s"
 HEAD_MODE = "df64"
 WORKLOAD = "wall-RPY M_UF.F, 256 shells x 42 blobs = 10,752 blobs (FP64-accurate: df64, <= 1e-12 vs FP64)"
 # Split of the near-field augmented preconditioner, in body radii R: exact blob-level couplings below
-# NF_EXACT_R, learned mode couplings from there to the network's cutoff (6R).  A sweep of the 256-, 1024-
-# and 4096-shell mixed solves over exact cutoffs 3R, 4.5R and 6R, each with and without the learned band,
-# gave the fewest iterations and the shortest solves at 4.5R with the band; NF_ALL_EXACT_R is the
-# comparison arm with exact couplings of every pair the network would cover.
-NF_EXACT_R = 4.5
-NF_ALL_EXACT_R = 6.0
+# NF_EXACT_R, learned mode couplings from there to the network's cutoff NF_CUTOFF_R.  A sweep of the 256-,
+# 1024- and 4096-shell mixed solves over exact cutoffs 3R-9R and networks of 6R and 9R range gave the
+# fewest iterations and the shortest solves overall with exact couplings below 6R and a 9R network;
+# NF_ALL_EXACT_R is the comparison arm with exact couplings of every pair the network would cover.
+NF_EXACT_R = 6.0
+NF_CUTOFF_R = 9.0
+NF_ALL_EXACT_R = NF_CUTOFF_R
 # Issued thread instructions per ordered pair of the df64 UF kernels (all
 # pipes, 80-85 % of them on the FMA pipe), from ncu's smsp__inst_executed.sum
 # on the 10,752-blob product: symmetric kernel (each unordered pair once),
@@ -417,18 +418,18 @@ def solve_breakdown(fn):
 
 def train_nearfield(shell, a, z_range, dev, n_clusters=1024, steps=2000, seed=11):
     """Message-passing near-field network for one shell type: clusters of 2..8 bodies (centre distances
-    2R+2a .. 6R, heights in z_range) whose pair couplings the plain method computes on the GPU, then Adam
+    2R+2a .. NF_CUTOFF_R, heights in z_range) whose pair couplings the plain method computes on the GPU, then Adam
     on the GPU.  Returns (model, info)."""
     import torch
     from rigidmultiblobswall_gb300 import nearfield as nf
     R = float(np.linalg.norm(shell[0]))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    graphs = nf.cluster_training_data(shell, a, 1.0, n_clusters, d_range=(2 * R + 2 * a, 6 * R), z_range=z_range,
+    graphs = nf.cluster_training_data(shell, a, 1.0, n_clusters, d_range=(2 * R + 2 * a, NF_CUTOFF_R * R), z_range=z_range,
                                       seed=seed, device=dev)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    model = nf.NearfieldModel(body_radius=R, cutoff=6 * R, seed=2)
+    model = nf.NearfieldModel(body_radius=R, cutoff=NF_CUTOFF_R * R, seed=2)
     hist = model.train(graphs, steps=steps, lr=2e-3)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
@@ -545,9 +546,9 @@ def solver_metrics(dev, reps=2):
     vel = {}
     R3 = float(np.linalg.norm(s3.shell[0]))
     model12, out["nearfield_training_shells12"] = train_nearfield(s3.shell, s3.a, (1.1 * R3, 5 * R3), dev)
-    # mixed_nearfield: exact couplings below NF_EXACT_R, learned ones from there to 6R; mixed_exact: the
-    # exact part alone; mixed_learned: learned couplings for every pair below 6R (no exact part);
-    # mixed_exact_all: exact couplings for every pair below 6R (no network)
+    # mixed_nearfield: exact couplings below NF_EXACT_R, learned ones from there to NF_CUTOFF_R;
+    # mixed_exact: the exact part alone; mixed_learned: learned couplings for every pair below NF_CUTOFF_R
+    # (no exact part); mixed_exact_all: exact couplings for every pair below NF_CUTOFF_R (no network)
     arms3 = {"fp64": None, "mixed": None, "mixed_nearfield": (model12, NF_EXACT_R * R3),
              "mixed_exact": (None, NF_EXACT_R * R3), "mixed_learned": (model12, 0.0),
              "mixed_exact_all": (None, NF_ALL_EXACT_R * R3)}
@@ -576,7 +577,7 @@ def solver_metrics(dev, reps=2):
         "learned_mixed": out["bd_step_shells12x1024_mixed_nearfield"]["ms"],
         "exact_only_mixed": out["bd_step_shells12x1024_mixed_exact"]["ms"],
         "learned_only_mixed": out["bd_step_shells12x1024_mixed_learned"]["ms"],
-        "exact_below_6R_mixed": out["bd_step_shells12x1024_mixed_exact_all"]["ms"]}
+        "exact_all_mixed": out["bd_step_shells12x1024_mixed_exact_all"]["ms"]}
     # every time integrator, one step of 1024 shells x 12 blobs (mixed precision,
     # GMRES and Lanczos tolerance 1e-8, force (0,0,-1) per body, kT = 1, dt = 1e-3)
     FT3t = torch.as_tensor(FT3, device=dev).reshape(-1, 3)
@@ -677,9 +678,10 @@ def cfg5_metrics(dev, modes=("fp64", "mixed", "mixed+exact", "mixed+learned", "m
     """4096 42-blob shells at area fraction 0.3, force (0,0,-1) per body: preconditioned GMRES to a 1e-8
     relative residual, on one GPU.  Arms: plain block-diagonal FP64 (the baseline), mixed precision, and
     mixed precision with the near-field augmented preconditioner - exact blob-level couplings below
-    NF_EXACT_R only ("exact"), learned mode couplings of every pair below 6R ("learned"), of the outer
-    band NF_EXACT_R..6R only ("learned_band"), exact below NF_EXACT_R with learned from there to 6R
-    ("exact+learned"), and exact couplings of every pair below 6R without the network ("exact_all").
+    NF_EXACT_R only ("exact"), learned mode couplings of every pair below NF_CUTOFF_R ("learned"), of the
+    outer band NF_EXACT_R..NF_CUTOFF_R only ("learned_band"), exact below NF_EXACT_R with learned from there
+    to NF_CUTOFF_R ("exact+learned"), and exact couplings of every pair below NF_CUTOFF_R without the
+    network ("exact_all").
     Each arm's time covers its preconditioner build (FP64 or FP32), the near-field
     attach and the solve; the network is trained once before (time reported).  Every solution's relative
     residual is also estimated by the oracle (all body rows, 1024 sampled blob rows)."""
@@ -696,7 +698,8 @@ def cfg5_metrics(dev, modes=("fp64", "mixed", "mixed+exact", "mixed+learned", "m
     FT[:, 2] = -1.0
     R5 = float(np.linalg.norm(s5.shell[0]))
     out = {"workload": "4096 shells x 42 blobs = 172,032 blobs, area fraction 0.3, z in [1.1R, 3R], F=(0,0,-1)",
-           "tol": 1e-8, "restart": 60, "exact_cutoff": "%gR" % NF_EXACT_R, "learned_band": "%gR..6R" % NF_EXACT_R,
+           "tol": 1e-8, "restart": 60, "exact_cutoff": "%gR" % NF_EXACT_R,
+           "learned_band": "%gR..%gR" % (NF_EXACT_R, NF_CUTOFF_R),
            "message_cutoff": "3R"}
     model = None
     if any("learned" in m for m in modes):

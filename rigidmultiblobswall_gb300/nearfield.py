@@ -8,13 +8,13 @@ clusters that the plain method's own machinery computes.
 Use::
 
     sys_.build_pc()
-    attach_exact(sys_, cutoff=4.5 * R)                 # exact near field only
-    model = NearfieldModel(body_radius=R, cutoff=6 * R)      # messages between bodies < 3R apart
-    graphs = cluster_training_data(shell, a, eta, 1024, d_range=(2 * R + 2 * a, 6 * R),
+    attach_exact(sys_, cutoff=6 * R)                   # exact near field only
+    model = NearfieldModel(body_radius=R, cutoff=9 * R)      # messages between bodies < 3R apart
+    graphs = cluster_training_data(shell, a, eta, 1024, d_range=(2 * R + 2 * a, 9 * R),
                                    z_range=(1.1 * R, 3 * R))
     model.train(graphs, steps=2000)
-    model.attach(sys_, exact_cutoff=4.5 * R)           # exact < 4.5R <= learned < 6R
-    result = solve_with_fallback(sys_, model, rhs, exact_cutoff=4.5 * R)
+    model.attach(sys_, exact_cutoff=6 * R)             # exact < 6R <= learned < 9R
+    result = solve_with_fallback(sys_, model, rhs, exact_cutoff=6 * R)
 
 The network is a message-passing network over the bodies: embeddings from
 each body's height and neighbour count, three rounds of messages between

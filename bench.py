@@ -100,6 +100,9 @@ def parse():
     p.add_argument("--krylov-probe", action="store_true",
                    help="only the 4096-shell mixed solve with graphs off (each fused Arnoldi step a traced direct "
                         "launch) and the pair scratch capped at 1 GiB: the Arnoldi steps' time and bandwidth")
+    p.add_argument("--lanczos-probe", type=int, nargs="?", const=64, default=None, metavar="NSUSP",
+                   help="the 16-RHS Lanczos of the first NSUSP (default 64) uneven suspensions with every step a "
+                        "launch of its own (for ncu)")
     p.add_argument("--multi", default=None, metavar="N:NRHS",
                    help="only time the multi-right-hand-side M_UF product on N blobs with NRHS vectors")
     p.add_argument("--product", default=None, metavar="KIND:MODE",
@@ -947,6 +950,51 @@ def krylov_probe():
                       "arnoldi": arn}))
 
 
+def lanczos_probe(nsusp=64):
+    """The 16-right-hand-side Lanczos of the first nsusp of the 64 uneven suspensions (mixed precision,
+    tolerance 1e-3) with graphs off, so that every fused Lanczos step is a launch of its own: one JSON line
+    with the run's time and the step kernel's traced time, algorithmic bytes and bandwidth."""
+    import torch
+    from rigidmultiblobswall_gb300 import build as B
+    B.build()
+    from rigidmultiblobswall_gb300 import _native
+    from rigidmultiblobswall_gb300 import suspensions as S
+    from rigidmultiblobswall_gb300.rigid import RigidSystem
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    susps = S.shells_42_batch()[:max(1, nsusp)]
+    counts = [s.n_bodies for s in susps]
+    sysb = RigidSystem([42] * sum(counts), susps[0].eta, susps[0].a, device=dev)
+    sysb.set_configuration(np.concatenate([s.r_vectors() for s in susps]),
+                           np.concatenate([s.locations for s in susps]))
+    sysb.set_suspensions(counts)
+    sysb.build_pc(stochastic=True, mode="mixed")
+    nrhs = 16
+    Z = torch.randn(nrhs, 3 * sysb.n_blobs, generator=torch.Generator(device=dev).manual_seed(4),
+                    dtype=torch.float64, device=dev)
+    _native.use_graphs(False)
+    _native.trace_enable(True)
+    _native.trace_read(1, reset=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, itl = sysb.lanczos_batched(Z, factor=np.sqrt(2.0 / 1e-3), tol=1e-3, mode="mixed")
+    torch.cuda.synchronize()
+    lz_ms = (time.perf_counter() - t0) * 1e3
+    step_ms, step_launches = _native.trace_read(1, reset=True)
+    for k in range(8):
+        _native.trace_read(k, reset=True)
+    _native.trace_bytes(1, reset=True)
+    _native.trace_enable(False)
+    _native.use_graphs(True)
+    it = np.asarray(itl).reshape(nrhs, len(counts))
+    nblob = 42 * np.asarray(counts, dtype=np.float64)
+    step_bytes = float((24.0 * nblob[None, :] * (it + 1) * (it + 4)).sum())
+    print(json.dumps({"suspensions": len(counts), "blobs": int(sysb.n_blobs), "lanczos_ms": lz_ms,
+                      "iterations_min_max": [int(it.min()), int(it.max())],
+                      "step_launches": step_launches, "step_ms": step_ms, "step_gbytes": step_bytes / 1e9,
+                      "step_gbs": step_bytes / (step_ms * 1e-3) / 1e9 if step_ms > 0 else None}))
+
+
 def pc_probe():
     """The block-diagonal preconditioner of the 4096-shell suspension (FP32 build, the mixed solves'):
     the FP64 and FP32 applies timed over repeated calls, one JSON line (pc_apply_roofline)."""
@@ -971,6 +1019,9 @@ def main():
         return
     if args.pc_probe:
         pc_probe()
+        return
+    if args.lanczos_probe is not None:
+        lanczos_probe(args.lanczos_probe)
         return
     if args.large:
         large_solve(args)

@@ -84,9 +84,12 @@ __device__ void reduce_segment(const double *part, int KP, int j0, int j1, int k
 
 // part[job * KP + q] = sum_{i in job} V_q[i] w[i], q < k (red: k x 32 shared
 // doubles); eight basis vectors per pass over the job, so that each thread has
-// several independent loads in flight
-__device__ void job_dots(const double *__restrict__ V, long long ldv, int k, const double *w, const KJob jb,
-                         double *part, int KP, int job, double *red)
+// several independent loads in flight.  w[i] comes from wval(i, first): first
+// is true on the first pass over the job, where wval may also form w[i] and
+// store it (each thread reads back only the entries it stored).
+template <typename WVal>
+__device__ void job_dots_w(const double *__restrict__ V, long long ldv, int k, const KJob jb, double *part, int KP,
+                           int job, double *red, WVal wval)
 {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int q0 = 0; q0 < k; q0 += 8) {
@@ -94,7 +97,7 @@ __device__ void job_dots(const double *__restrict__ V, long long ldv, int k, con
         const double *V0 = V + (long long)q0 * ldv;
         double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         for (long long i = jb.b + threadIdx.x; i < jb.e; i += blockDim.x) {
-            const double wi = w[i];
+            const double wi = wval(i, q0 == 0);
 #pragma unroll
             for (int u = 0; u < 8; ++u)
                 if (u < nq) a[u] = fma(V0[(long long)u * ldv + i], wi, a[u]);
@@ -112,9 +115,16 @@ __device__ void job_dots(const double *__restrict__ V, long long ldv, int k, con
     __syncthreads();
 }
 
-// w[i] -= sum_q hs[q] V_q[i] over the job; returns this thread's sum of the new w[i]^2
+__device__ void job_dots(const double *__restrict__ V, long long ldv, int k, const double *w, const KJob jb,
+                         double *part, int KP, int job, double *red)
+{
+    job_dots_w(V, ldv, k, jb, part, KP, job, red, [w](long long i, bool) { return w[i]; });
+}
+
+// w[i] -= sum_q hs[q] V_q[i] over the job, the new w[i] also stored to c1 and
+// c2 when given; returns this thread's sum of the new w[i]^2
 __device__ double job_update(const double *__restrict__ V, long long ldv, int k, const double *hs, double *w,
-                             const KJob jb)
+                             const KJob jb, double *c1 = nullptr, double *c2 = nullptr)
 {
     double nrm = 0.0;
     for (long long i = jb.b + threadIdx.x; i < jb.e; i += blockDim.x) {
@@ -122,6 +132,10 @@ __device__ double job_update(const double *__restrict__ V, long long ldv, int k,
 #pragma unroll 8
         for (int q = 0; q < k; ++q) x = fma(-hs[q], V[(long long)q * ldv + i], x);
         w[i] = x;
+        if (c1) {
+            c1[i] = x;
+            c2[i] = x;
+        }
         nrm = fma(x, x, nrm);
     }
     return nrm;
@@ -474,7 +488,7 @@ struct LzArgs {
 // warp, forms the coefficients c of the noise |z| factor V^T Q sqrt(L) Q^T e1
 // and applies the stopping test |c - c_old| < tol |c_old|.  A segment that
 // stopped at the previous iteration is frozen (its w and next vector zero).
-__global__ void __launch_bounds__(kKdThreads, 1) lanczos_step_kernel(LzArgs A)
+__global__ void __launch_bounds__(kKdThreads, 3) lanczos_step_kernel(LzArgs A)
 {
     __shared__ double red[kKdMaxBasis * 32];
     __shared__ double hsh[kKdMaxBasis];
@@ -489,16 +503,18 @@ __global__ void __launch_bounds__(kKdThreads, 1) lanczos_step_kernel(LzArgs A)
     for (int job = jb0; job < jb1 && job - jb0 < 8; ++job)
         if (threadIdx.x == 0) actv[job - jb0] = A.cyc[A.jobs[job].seg];
     __syncthreads();
-    // pass 1: w -= hs[i-1] V_{i-1} (frozen: w = 0); partial <w, V_i>
+    // pass 1: w -= hs[i-1] V_{i-1} (frozen: w = 0) and, in the same pass, partial <w, V_i>
     for (int job = jb0; job < jb1; ++job) {
         const KJob jb = A.jobs[job];
         const bool on = (job - jb0 < 8) ? actv[job - jb0] != 0 : A.cyc[jb.seg] != 0;
         const double hp = (i > 0) ? A.hs[(long long)jb.seg * A.kcap + i - 1] : 0.0;
         const double *Vp = V + (long long)(i > 0 ? i - 1 : 0) * ldv;
-        for (long long e = jb.b + threadIdx.x; e < jb.e; e += blockDim.x)
-            A.w[e] = on ? ((i > 0) ? fma(-hp, Vp[e], A.w[e]) : A.w[e]) : 0.0;
-        __syncthreads();
-        job_dots(V + (long long)i * ldv, ldv, 1, A.w, jb, A.partA, A.KP, job, red);
+        double *w = A.w;
+        job_dots_w(V + (long long)i * ldv, ldv, 1, jb, A.partA, A.KP, job, red, [=](long long e, bool) {
+            const double x = on ? ((i > 0) ? fma(-hp, Vp[e], w[e]) : w[e]) : 0.0;
+            w[e] = x;
+            return x;
+        });
     }
     grid_barrier(&A.st->bar);
     // pass 2: hd = <w, V_i>; w -= hd V_i; partial |w|^2
@@ -511,32 +527,39 @@ __global__ void __launch_bounds__(kKdThreads, 1) lanczos_step_kernel(LzArgs A)
         job_norm_partial(nrm, A.partC, A.KP, job, red);
     }
     grid_barrier(&A.st->bar);
-    // pass 3: hs = |w|; w /= hs (0 on an exact breakdown); partial reorthogonalisation dots V_q^T w
+    // pass 3: hs = |w|; w /= hs (0 on an exact breakdown) during the first pass of the partial
+    // reorthogonalisation dots V_q^T w
     for (int job = jb0; job < jb1; ++job) {
         const KJob jb = A.jobs[job];
         reduce_segment(A.partC, A.KP, A.sjob[jb.seg], A.sjob[jb.seg + 1], 1, hsh);
         const double wn = sqrt(hsh[0]);
         const double inv = (wn > 0.0) ? 1.0 / wn : 0.0;
-        for (long long e = jb.b + threadIdx.x; e < jb.e; e += blockDim.x) A.w[e] *= inv;
         if (job == A.sjob[jb.seg] && threadIdx.x == 0) A.et[(long long)jb.seg * A.kcap] = wn;
         __syncthreads();
+        double *w = A.w;
         for (int q0 = 0; q0 < k; q0 += kKdMaxBasis)
-            job_dots(V + (long long)q0 * ldv, ldv, min(kKdMaxBasis, k - q0), A.w, jb, A.partB + q0, A.KP, job, red);
+            job_dots_w(V + (long long)q0 * ldv, ldv, min(kKdMaxBasis, k - q0), jb, A.partB + q0, A.KP, job, red,
+                       [=](long long e, bool first) {
+                           if (q0 == 0 && first) {
+                               const double x = w[e] * inv;
+                               w[e] = x;
+                               return x;
+                           }
+                           return w[e];
+                       });
     }
     grid_barrier(&A.st->bar);
     // pass 4: w -= V h; V_{i+1} = w; owners: tridiagonal eigen-problem, coefficients, stopping test
     for (int job = jb0; job < jb1; ++job) {
         const KJob jb = A.jobs[job];
+        double *Vn = V + (long long)(i + 1) * ldv;
         for (int q0 = 0; q0 < k; q0 += kKdMaxBasis) {
             const int kc = min(kKdMaxBasis, k - q0);
             reduce_segment(A.partB + q0, A.KP, A.sjob[jb.seg], A.sjob[jb.seg + 1], kc, hsh);
-            job_update(V + (long long)q0 * ldv, ldv, kc, hsh, A.w, jb);
+            // the last group's pass also writes V_{i+1} and the operator's next input
+            const bool last = q0 + kc >= k;
+            job_update(V + (long long)q0 * ldv, ldv, kc, hsh, A.w, jb, last ? Vn : nullptr, last ? A.xin : nullptr);
             __syncthreads();
-        }
-        double *Vn = V + (long long)(i + 1) * ldv;
-        for (long long e = jb.b + threadIdx.x; e < jb.e; e += blockDim.x) {
-            Vn[e] = A.w[e];
-            A.xin[e] = A.w[e];
         }
         const int s = jb.seg;
         if (job == A.sjob[s] && A.cyc[s] && threadIdx.x < 32) {

@@ -100,6 +100,8 @@ def parse():
     p.add_argument("--krylov-probe", action="store_true",
                    help="only the 4096-shell mixed solve with graphs off (each fused Arnoldi step a traced direct "
                         "launch) and the pair scratch capped at 1 GiB: the Arnoldi steps' time and bandwidth")
+    p.add_argument("--bd-probe", action="store_true",
+                   help="one Brownian step of the 1024 12-blob shells, plain and learned, in NVTX ranges (for ncu)")
     p.add_argument("--lanczos-probe", type=int, nargs="?", const=64, default=None, metavar="NSUSP",
                    help="the 16-RHS Lanczos of the first NSUSP (default 64) uneven suspensions with every step a "
                         "launch of its own (for ncu)")
@@ -995,6 +997,52 @@ def lanczos_probe(nsusp=64):
                       "step_gbs": step_bytes / (step_ms * 1e-3) / 1e9 if step_ms > 0 else None}))
 
 
+def bd_probe():
+    """One Brownian step of the 1024 12-blob shells (mixed precision, Lanczos 1e-3, GMRES 1e-8), plain and
+    with the near field (exact below NF_EXACT_R, learned to NF_CUTOFF_R): a warm-up step, a timed step, then
+    one step with graphs off (every kernel a launch of its own) inside the NVTX range "bd_step_<arm>", which
+    ncu --nvtx --nvtx-include "bd_step_<arm>/" lists launch by launch.  One JSON line with the times."""
+    import torch
+    from rigidmultiblobswall_gb300 import build as B
+    B.build()
+    from rigidmultiblobswall_gb300 import integrator
+    from rigidmultiblobswall_gb300 import suspensions as S
+    from rigidmultiblobswall_gb300.rigid import RigidSystem
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    s3 = S.shells_12_1024()
+    sys3 = RigidSystem([12] * s3.n_bodies, s3.eta, s3.a, device=dev)
+    FT3 = np.zeros((s3.n_bodies, 6))
+    FT3[:, 2] = -1.0
+    z = torch.randn(3 * s3.n_blobs, generator=torch.Generator(device=dev).manual_seed(3), dtype=torch.float64,
+                    device=dev)
+    R3 = float(np.linalg.norm(s3.shell[0]))
+    model12, _ = train_nearfield(s3.shell, s3.a, (1.1 * R3, 5 * R3), dev)
+    from rigidmultiblobswall_gb300 import _native
+    out = {}
+
+    def step(nfa):
+        st = integrator.BrownianStepper(sys3, s3.locations, s3.quaternions, np.tile(s3.shell, (s3.n_bodies, 1)),
+                                        kT=1.0, mode="mixed", nearfield=nfa)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = st.step(1e-3, FT3, z=z)
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) * 1e3, res
+
+    for name, nfa in (("mixed", None), ("mixed_nearfield", (model12, NF_EXACT_R * R3))):
+        step(nfa)
+        ms, res = step(nfa)
+        _native.use_graphs(False)
+        torch.cuda.nvtx.range_push("bd_step_" + name)
+        ms_ng, _ = step(nfa)
+        torch.cuda.nvtx.range_pop()
+        _native.use_graphs(True)
+        out[name] = {"ms": ms, "ms_without_graphs": ms_ng, "gmres_iterations": res["gmres_iterations"],
+                     "lanczos_iterations": res["lanczos_iterations"]}
+    print(json.dumps(out))
+
+
 def pc_probe():
     """The block-diagonal preconditioner of the 4096-shell suspension (FP32 build, the mixed solves'):
     the FP64 and FP32 applies timed over repeated calls, one JSON line (pc_apply_roofline)."""
@@ -1019,6 +1067,9 @@ def main():
         return
     if args.pc_probe:
         pc_probe()
+        return
+    if args.bd_probe:
+        bd_probe()
         return
     if args.lanczos_probe is not None:
         lanczos_probe(args.lanczos_probe)
